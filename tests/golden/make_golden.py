@@ -1,0 +1,213 @@
+"""Freeze golden vectors by running the upstream SslabLU modules themselves.
+
+Run in a container that has the upstream tree (default /root/reference, or
+$SSLABLU_REF_ROOT):
+
+    python tests/golden/make_golden.py
+
+Every random input is drawn from numpy's legacy global RNG after
+``np.random.seed(seed)`` (a stream numpy keeps stable across versions) or from
+``default_rng(seed)``, so tests can regenerate inputs instead of storing them;
+the large outputs are stored.  Fixtures written (all small):
+
+  rb_dense.npz       upstream direct_solve/test_RB.py cases: RedBlackSolver and
+                     BlockTridiagonalSolver solutions
+  thomas_cyclic.npz  BlockTridiagonalSolver(cyclic=True) on a periodic system
+  hbs_*.npz          HBSnew.HBSMAT(...).construct(k, True) of exact random HBS
+                     matrices (test/rkprop/HBSnewTest.py generator): factors,
+                     matmat/rmatmat and solve (N and T) outputs
+  c1_poisson64.npz   multislab.oms + stencil 2D Poisson, 8 slabs, 64-point
+                     interfaces (the C1 layout at reduced size): S blocks, rhs
+                     and the Thomas / red-black / functional-Thomas solutions
+  rbhbs_kernel.npz   RedBlackSolverHBS / ThomasSolverHBS on a smooth-kernel
+                     block-tridiagonal system
+"""
+import contextlib
+import io
+import os
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+from oracle import refshim  # noqa: E402
+from oracle.hbs import gen_random_hbs  # noqa: E402
+
+QUIET = io.StringIO()
+
+
+def rb_dense(ref):
+    sys.path.insert(0, os.path.join(refshim.REF_ROOT, "direct_solve"))
+    with contextlib.redirect_stdout(QUIET):
+        import test_RB
+    out = {}
+    cases = [(8, 3), (2, 1), (2, 5), (4, 3), (8, 1), (8, 5), (8, 10), (16, 3), (32, 3)]
+    out["cases"] = np.array(cases)
+    for nS, m in cases:
+        S, T, mat, rhs = test_RB.make_block_tridiagonal(nS, m, 42)
+        with contextlib.redirect_stdout(QUIET):
+            rb = ref.omsdirectsolve.RedBlackSolver(m)
+            rb.factorize(S, T)
+            x_rb = rb.solve(rhs)
+        th = ref.omsdirectsolve.BlockTridiagonalSolver(m)
+        th.factorize(S, T)
+        x_th = th.solve(rhs)
+        key = "%d_%d" % (nS, m)
+        out["x_rb_" + key] = x_rb
+        out["x_th_" + key] = x_th
+        out["x_np_" + key] = np.linalg.solve(mat, rhs)
+    np.savez_compressed(os.path.join(HERE, "rb_dense.npz"), **out)
+
+
+def thomas_cyclic(ref):
+    nS, m = 6, 4
+    rng = np.random.default_rng(3)
+    S = [(0.1 * rng.standard_normal((m, m)), 0.1 * rng.standard_normal((m, m))) for _ in range(nS)]
+    T = [rng.standard_normal((m, m)) + 8 * np.eye(m) for _ in range(nS)]
+    rhs = rng.standard_normal((nS * m, 2))
+    th = ref.omsdirectsolve.BlockTridiagonalSolver(m, cyclic=True)
+    th.factorize(S, T)
+    np.savez_compressed(os.path.join(HERE, "thomas_cyclic.npz"),
+                        S=np.array(S), T=np.array(T), rhs=rhs, x=th.solve(rhs))
+
+
+def hbs_case(ref, name, k, nl, L, quad, seed, sigma=None, nrhs=3, store_factors=True):
+    """Exact random HBS -> upstream compression + ULV -> outputs."""
+    np.random.seed(seed)
+    S, Nbvec = gen_random_hbs(k, nl, L, quad, sigma=sigma)
+    fac = 4 if quad else 2
+    src = ref.HBSnew.HBSMAT()
+    src.set_mats(S.Umats, S.Dmats, S.Vmats, list(Nbvec), fac=fac)
+    with contextlib.redirect_stdout(QUIET):
+        H = ref.HBSnew.HBSMAT(src, tree=None, quad=quad)
+        H.set_Nbvec(list(Nbvec))
+        H.construct(k, True)
+    rng = np.random.default_rng(seed + 1)
+    x = rng.standard_normal((S.shape[0], nrhs))
+    out = dict(k=k, nl=nl, L=L, quad=int(quad), seed=seed, Nbvec=np.array(Nbvec),
+               NNvec=np.array(H.NNvec), nSamples=H.nSamples,
+               x=x, Ax_true=src.matmat(x), ATx_true=src.rmatmat(x),
+               mm=H.matmat(x), rmm=H.rmatmat(x),
+               sol=H.solve(x), solT=H.solve(x, mode="T"),
+               sol1=H.solve(x[:, 0]))
+    if sigma is not None:
+        out["sigma"] = np.asarray(sigma)
+    if store_factors:
+        for nm in ["Umats", "Vmats", "Dmats", "Qlist", "Rlist", "Uulist"]:
+            for i, M in enumerate(getattr(H, nm)):
+                out["%s_%d" % (nm, i)] = M
+        for i, M in enumerate(H.Wlist):
+            if M is not None:
+                out["Wlist_%d" % i] = M
+        # the standalone factorisation of the generator's own factors
+        Ql, Wl, Uul, Rl, NNv = ref.ULVsparse.compute_ULV(S.Umats, S.Dmats, S.Vmats, Nbvec)
+        out["ulv_NNvec"] = np.array(NNv)
+        out["ulv_sol"] = ref.ULVsparse.solve(S.Umats, S.Dmats, Ql, Wl, Uul, Rl, NNv, Nbvec, x.copy())
+        out["ulv_solT"] = ref.ULVsparse.solve(S.Umats, S.Dmats, Ql, Wl, Uul, Rl, NNv, Nbvec,
+                                               x.copy(), mode="T")
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+
+
+def c1_poisson(ref, P):
+    sq = P.square
+    nslabs, nx, ny = 8, 17, 66
+    slabs, conn, H = sq.dSlabs(nslabs)
+    gb = lambda p: sq.gb(p, jax_avail=False)
+    pdo = P.pdo.PDO2d(c11=P.pdo.const(1.0), c22=P.pdo.const(1.0))
+    opts = P.solver.solverOptions("stencil", [nx, ny])
+    O = P.oms.oms(slabs, pdo, gb, opts, conn)
+    bc = lambda p: np.sin(np.pi * p[:, 0]) * np.sinh(np.pi * p[:, 1])
+    import warnings
+    with contextlib.redirect_stdout(QUIET), warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        S, rhs_list, Ntot, nc = O.construct_Stot_helper(bc, P.matAssembler.denseMatAssembler())
+        Stot, rhs = O.construct_Stot_and_rhstot_linearOperator(S, rhs_list, Ntot, nc)
+    n = len(S)
+    Sl = np.zeros((n, nc, nc))
+    Sr = np.zeros((n, nc, nc))
+    for i, row in enumerate(S):
+        if i > 0:
+            Sl[i] = row[0]
+        if i < n - 1:
+            Sr[i] = row[-1]
+    T = [np.eye(nc) for _ in range(n)]
+    th = ref.omsdirectsolve.BlockTridiagonalSolver(nc)
+    th.factorize(S, T)
+    x_th = th.solve(rhs)
+    # red-black needs 2^p blocks: pad with one decoupled identity block
+    Sp = [[Sl[i], Sr[i]] for i in range(n)] + [[np.zeros((nc, nc)), np.zeros((nc, nc))]]
+    rhs_p = np.concatenate([rhs, np.zeros(nc)])
+    with contextlib.redirect_stdout(QUIET):
+        rb = ref.omsdirectsolve.RedBlackSolver(nc)
+        rb.factorize(Sp, [np.eye(nc)] * (n + 1))
+        x_rb = rb.solve(rhs_p)
+    # functional Thomas of multislab/omsdirectsolve.py
+    with contextlib.redirect_stdout(QUIET):
+        import multislab.omsdirectsolve as mods
+    Tf = mods.build_block_tridiagonal_solver(S)
+    x_f = mods.block_tridiagonal_solve(O, Tf, rhs)
+    np.savez_compressed(os.path.join(HERE, "c1_poisson64.npz"),
+                        Sl=Sl, Sr=Sr, rhs=rhs, x_th=x_th, x_rb=x_rb, x_f=x_f,
+                        Stot_x=Stot @ x_th, nc=nc)
+
+
+def kernel_system(m=64, nS=4):
+    x = np.linspace(0, 1, m)
+
+    def blk(shift):
+        return 0.3 * np.exp(-np.abs(x[:, None] - x[None, :] - shift) * 3)
+    S = []
+    for i in range(nS):
+        A = blk(0.2 + 0.01 * i) if i > 0 else np.zeros((m, m))
+        C = blk(-0.2 - 0.01 * i) if i < nS - 1 else np.zeros((m, m))
+        S.append((A, C))
+    return S
+
+
+def rbhbs(ref):
+    m, nS, leaf, nlev = 64, 4, 16, 3
+    tree = types.SimpleNamespace(perm_leaf=np.arange(m), nleaves=m // leaf, nlevels=nlev)
+    S = kernel_system(m, nS)
+
+    def lo(A):
+        o = ref.omsdirectsolveHBS.dense_to_linop(A)
+        o.tree, o.quad = tree, False
+        return o
+    Slo = [(lo(a), lo(c)) for a, c in S]
+    b = np.random.default_rng(7).standard_normal(nS * m)
+    out = dict(m=m, nS=nS, leaf=leaf, nlev=nlev, b=b)
+    for rk in (16, 24):
+        np.random.seed(11)
+        with contextlib.redirect_stdout(QUIET):
+            R = ref.omsdirectsolveHBS.RedBlackSolverHBS(m, rk, tree, False)
+            R.factorize(Slo)
+            out["x_rb_%d" % rk] = R.solve(b)
+        np.random.seed(12)
+        with contextlib.redirect_stdout(QUIET):
+            T = ref.omsdirectsolveHBS.ThomasSolverHBS(m, rk)
+            T.factorize(Slo)
+            out["x_th_%d" % rk] = T.solve(b)
+    np.savez_compressed(os.path.join(HERE, "rbhbs_kernel.npz"), **out)
+
+
+def main():
+    ref = refshim.import_hot_path()
+    P = refshim.import_pipeline()
+    rb_dense(ref)
+    thomas_cyclic(ref)
+    hbs_case(ref, "hbs_binary_k8", 8, 16, 4, False, 101)
+    hbs_case(ref, "hbs_quad_k8", 8, 8, 3, True, 102)
+    sig = 10.0 ** (-12.0 * np.arange(32) / 31.0)
+    hbs_case(ref, "hbs_c2_n512", 32, 64, 4, False, 103, sigma=sig, nrhs=4, store_factors=False)
+    c1_poisson(ref, P)
+    rbhbs(ref)
+    for f in sorted(os.listdir(HERE)):
+        if f.endswith(".npz"):
+            print(f, os.path.getsize(os.path.join(HERE, f)))
+
+
+if __name__ == "__main__":
+    main()

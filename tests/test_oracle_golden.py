@@ -1,0 +1,101 @@
+"""The CPU oracle reproduces the upstream golden vectors (no GPU)."""
+import numpy as np
+import pytest
+
+from oracle import direct as od
+from oracle import hbs as oh
+from tests._cases import hbs_from_fixture, kernel_system, relerr, test_rb_system
+
+
+def test_rb_dense_cases(golden):
+    g = golden("rb_dense")
+    for nS, m in g["cases"]:
+        S, T, mat, rhs = test_rb_system(int(nS), int(m))
+        key = "%d_%d" % (nS, m)
+        x = od.RedBlackDense(int(m)).factorize(S, T).solve(rhs)
+        assert relerr(x, g["x_rb_" + key]) < 1e-14
+        assert relerr(x, g["x_np_" + key]) < 1e-8      # upstream test_RB bar
+        xt = od.ThomasDense(int(m)).factorize(S, T).solve(rhs)
+        assert relerr(xt, g["x_th_" + key]) < 1e-14
+
+
+def test_thomas_cyclic(golden):
+    g = golden("thomas_cyclic")
+    S = [tuple(p) for p in g["S"]]
+    x = od.ThomasDense(4, cyclic=True).factorize(S, list(g["T"])).solve(g["rhs"])
+    assert relerr(x, g["x"]) < 1e-14
+
+
+@pytest.mark.parametrize("name", ["hbs_binary_k8", "hbs_quad_k8"])
+def test_hbs_construct_factors(golden, name):
+    g = golden(name)
+    S, Nbvec = hbs_from_fixture(g)
+    O = oh.OracleHBS(S, None, Nbvec[0], len(Nbvec), 4 if g["quad"] else 2)
+    O.construct(int(g["k"]))          # draws Om, Psi from the global RNG, as upstream
+    assert np.array_equal(O.NNvec, g["NNvec"])
+    for nm in ["Umats", "Vmats", "Dmats", "Qlist", "Rlist", "Uulist"]:
+        for i, M in enumerate(getattr(O, nm)):
+            ref = g["%s_%d" % (nm, i)]
+            assert M.shape == ref.shape
+            if ref.size == 0:
+                continue
+            assert np.abs(M - ref).max() <= 1e-12 * max(1.0, np.abs(ref).max())
+    x = g["x"]
+    assert relerr(O.matmat(x), g["mm"]) < 1e-13
+    assert relerr(O.rmatmat(x), g["rmm"]) < 1e-13
+    assert relerr(O.solve(x), g["sol"]) < 1e-13
+    assert relerr(O.solve(x, "T"), g["solT"]) < 1e-13
+    assert relerr(O.solve(x[:, 0]), g["sol1"]) < 1e-13
+    # exactness of the round trip (upstream HBSnewTest.py:93-110 bars)
+    assert relerr(O.matmat(x), g["Ax_true"]) < 1e-12
+    # standalone ULV of the generator factors
+    Ql, Wl, Uul, Rl, NNv = oh.compute_ULV(S.Umats, S.Dmats, S.Vmats, Nbvec)
+    assert np.array_equal(NNv, g["ulv_NNvec"])
+    y = oh.ulv_solve(S.Umats, S.Dmats, Ql, Wl, Uul, Rl, NNv, Nbvec, x.copy())
+    yt = oh.ulv_solve(S.Umats, S.Dmats, Ql, Wl, Uul, Rl, NNv, Nbvec, x.copy(), "T")
+    assert relerr(y, g["ulv_sol"]) < 1e-13
+    assert relerr(yt, g["ulv_solT"]) < 1e-13
+
+
+def test_hbs_c2_shape(golden):
+    g = golden("hbs_c2_n512")
+    S, Nbvec = hbs_from_fixture(g)
+    O = oh.OracleHBS(S, None, Nbvec[0], len(Nbvec), 2)
+    O.construct(int(g["k"]))
+    assert O.nSamples == int(g["nSamples"]) == 4 * 32 + 2 * 64 + 5
+    x = g["x"]
+    assert relerr(O.matmat(x), g["mm"]) < 1e-13
+    assert relerr(O.solve(x), g["sol"]) < 1e-12
+    assert relerr(O.solve(x, "T"), g["solT"]) < 1e-12
+    assert relerr(O.matmat(x), g["Ax_true"]) < 1e-12
+
+
+def test_c1_poisson(golden):
+    g = golden("c1_poisson64")
+    n = g["Sl"].shape[0]
+    nc = int(g["nc"])
+    S = [[g["Sr"][0]]] + [[g["Sl"][i], g["Sr"][i]] for i in range(1, n - 1)] + [[g["Sl"][n - 1]]]
+    T = [np.eye(nc)] * n
+    x = od.ThomasDense(nc).factorize(S, T).solve(g["rhs"])
+    assert relerr(x, g["x_th"]) < 1e-14
+    Sp = [[g["Sl"][i], g["Sr"][i]] for i in range(n)] + [[np.zeros((nc, nc))] * 2]
+    xr = od.RedBlackDense(nc).factorize(Sp, [np.eye(nc)] * (n + 1)).solve(
+        np.concatenate([g["rhs"], np.zeros(nc)]))
+    assert relerr(xr, g["x_rb"]) < 1e-13
+    A, B, C = od.build_block_tridiagonal_solver(S)
+    idx = [range(i * nc, (i + 1) * nc) for i in range(n)]
+    assert relerr(od.block_tridiagonal_solve(idx, (A, B, C), g["rhs"]), g["x_f"]) < 1e-14
+
+
+@pytest.mark.parametrize("rk", [16, 24])
+def test_rbhbs_kernel(golden, rk):
+    g = golden("rbhbs_kernel")
+    m, nS, leaf, nlev = int(g["m"]), int(g["nS"]), int(g["leaf"]), int(g["nlev"])
+    S = [(od.dense_op(a), od.dense_op(c)) for a, c in kernel_system(m, nS)]
+    td = (np.arange(m), m // leaf, nlev)
+    np.random.seed(11)
+    x = od.RedBlackHBS(m, rk, td, False).factorize(S).solve(g["b"])
+    assert relerr(x, g["x_rb_%d" % rk]) < 1e-12
+    np.random.seed(12)
+    y = od.ThomasHBS(m, rk, td, False).factorize(S).solve(g["b"])
+    assert relerr(y, g["x_th_%d" % rk]) < 1e-12
