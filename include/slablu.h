@@ -1,0 +1,159 @@
+/* slablu: GB300-native slab direct-solve path (HBS compression, HBS ULV,
+ * block-tridiagonal red-black / Thomas elimination) behind a C ABI.
+ *
+ * Conventions
+ *   - Every entry point returns an int status: 0 = SLU_OK, otherwise one of
+ *     the SLU_ERR_* codes below; slu_last_error() returns the message of the
+ *     most recent failure on the calling thread.  No C++ exception crosses
+ *     this boundary.
+ *   - All matrix arguments are DEVICE pointers to row-major float64 (or
+ *     float32 where the name says so) arrays with the stated leading
+ *     dimension.  HBS levels use the stacked block layout of the upstream
+ *     code: a level with Nb blocks of n rows is one (Nb*n) x c array.
+ *   - Work is enqueued on the handle's stream and is asynchronous; callers
+ *     synchronise with slu_sync() or their own stream events.
+ *   - A handle owns factor storage and a grow-only scratch arena; one handle
+ *     must not be used from two host threads at once.
+ *
+ * Each entry point names the upstream Python function it replaces (paths
+ * relative to the SslabLU repository).
+ */
+#ifndef SLABLU_H
+#define SLABLU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SLU_OK 0
+#define SLU_ERR_ARG 1
+#define SLU_ERR_ALLOC 2
+#define SLU_ERR_CUDA 3
+#define SLU_ERR_NUMERIC 4
+#define SLU_ERR_STATE 5
+#define SLU_ERR_NOT_CONVERGED 6
+#define SLU_ERR_TIMEOUT 7
+
+typedef struct slu_handle_s* slu_handle_t;
+typedef struct slu_hbs_s* slu_hbs_t;
+typedef struct slu_dense_rb_s* slu_rb_t;
+
+/* ---------------------------------------------------------------- runtime */
+int slu_version(void);
+/* Copies the last error message of this thread into buf (NUL terminated). */
+int slu_last_error(char* buf, size_t len);
+/* stream: a cudaStream_t (NULL = legacy default stream). */
+int slu_create(void* stream, slu_handle_t* out);
+int slu_destroy(slu_handle_t h);
+int slu_set_stream(slu_handle_t h, void* stream);
+/* Synchronises the handle's stream and reports device-side status words
+ * (e.g. a Jacobi SVD that did not converge) as SLU_ERR_NOT_CONVERGED. */
+int slu_sync(slu_handle_t h);
+
+/* ---------------------------------------------------------------- HBS operator
+ * Replaces matAssembly/HBS/HBSnew.py:82-118 (HBSMAT.__init__ with a tree):
+ * N points, L tree levels (leaves at level 0), fac = 2 (binary) or 4 (quad),
+ * perm_host = tree.perm_leaf (N host int64 entries, NULL = identity). */
+int slu_hbs_create(slu_handle_t h, int N, int L, int fac, const int64_t* perm_host,
+                   slu_hbs_t* out);
+int slu_hbs_destroy(slu_hbs_t op);
+
+/* Replaces HBSMAT.constructHBS_ULV (matAssembly/HBS/HBSnew.py:211-295) after
+ * the sampling step: Om, Psi are the N x s Gaussian sketches and Y = A Om',
+ * Z = A^T Psi' the samples, all in tree order (rows permuted by perm_leaf),
+ * leading dimension s.  nleaves = tree.nleaves, rk = target rank.  With
+ * compute_ulv = 1 the ULV factorisation is interleaved (construct(rk, True)). */
+int slu_hbs_compress(slu_handle_t h, slu_hbs_t op, int nleaves, int rk, int s, const double* Om,
+                     const double* Psi, const double* Y, const double* Z, int compute_ulv);
+
+/* Replaces HBSMAT.set_mats (matAssembly/HBS/HBSnew.py:125-133) one level at a
+ * time: level 0 = leaves.  U, V: (Nb*n) x k, D: (Nb*n) x n (device); on the
+ * root pass k = 0 and U = V = NULL.  Every level must be set before use. */
+int slu_hbs_set_level(slu_handle_t h, slu_hbs_t op, int level, int Nb, int n, int k,
+                      const double* U, const double* V, const double* D);
+
+/* Replaces ULVsparse.compute_ULV (matAssembly/HBS/ULVsparse.py:231-293) /
+ * HBSMAT.compute_ULV (HBSnew.py:390-391) for loaded factors. */
+int slu_ulv_factor(slu_handle_t h, slu_hbs_t op);
+
+/* Replaces HBSMAT.matmat / rmatmat (HBSnew.py:308-350): Y = A X (trans = 0)
+ * or A^T X, X and Y N x nrhs in the caller's (unpermuted) ordering. */
+int slu_hbs_apply(slu_handle_t h, slu_hbs_t op, int trans, const double* X, int ldx, double* Y,
+                  int ldy, int nrhs);
+
+/* Replaces HBSMAT.solve (HBSnew.py:393-416) -> ULVsparse.solve
+ * (ULVsparse.py:295-358), in place on B (N x nrhs, unpermuted ordering).
+ * trans = 1 reproduces upstream's mode 'T' handling of the permutation. */
+int slu_ulv_solve(slu_handle_t h, slu_hbs_t op, double* B, int ldb, int nrhs, int trans);
+
+/* Single-precision copy of the ULV factors and a float32 solve with the same
+ * sweep; used inside iterative refinement (no upstream counterpart: the
+ * mixed-precision path of this library). */
+int slu_hbs_prepare_f32(slu_handle_t h, slu_hbs_t op);
+int slu_ulv_solve_f32(slu_handle_t h, slu_hbs_t op, float* B, int ldb, int nrhs, int trans);
+
+/* Iterative refinement of A x = b with float32 ULV solves and a float64
+ * residual r = b - A x computed with the stored HBS factors (the operator the
+ * upstream solve inverts).  X holds the result (N x nrhs); iterations stop
+ * when every column reaches ||r||/||b|| <= tol or after maxit corrections.
+ * iters_out / relres_out (host pointers, may be NULL) receive the iteration
+ * count and the largest final relative residual. */
+int slu_refine(slu_handle_t h, slu_hbs_t op, const double* B, int ldb, double* X, int ldx,
+               int nrhs, double tol, int maxit, int* iters_out, double* relres_out);
+
+/* Geometry: L, N and per level (Nb, n, k, nu) into levels[4*L]; NNvec[L+1]
+ * (ULVsparse.compute_ULV's NNvec).  Host pointers, any may be NULL. */
+int slu_hbs_info(slu_hbs_t op, int* L, int* N, int* levels, long long* NNvec, int* nsamples);
+
+/* Copies one stored factor of one level into dst (device pointer, count
+ * doubles available).  what: 0 U, 1 V, 2 D, 3 Q, 4 W, 5 R (Rlist entry),
+ * 6 Uu.  *count_out receives the number of doubles of the factor. */
+int slu_hbs_export(slu_handle_t h, slu_hbs_t op, int what, int level, double* dst, size_t count,
+                   size_t* count_out);
+/* Bytes of stored factors: which = 0 HBS (U, V, D; HBSMAT.nbytes,
+ * HBSnew.py:296-302), 1 solve factors. */
+int slu_hbs_nbytes(slu_hbs_t op, int which, size_t* out);
+
+/* ---------------------------------------------------------------- dense kernels
+ * Batched LU with partial pivoting of nb matrices A_b (n x n, row-major, lda,
+ * batch stride sA), in place; piv (device int32, n per matrix, stride sP)
+ * receives LAPACK-style 0-based pivots.  info (device int32[nb], may be NULL)
+ * is set to j+1 for a zero pivot.  Replaces scipy.linalg.lu_factor at
+ * direct_solve/omsdirectsolve.py:84,96,211,333. */
+int slu_lu_factor(slu_handle_t h, int n, double* A, int lda, long long sA, int* piv,
+                  long long sP, int nb, int* info);
+/* X_b <- A_b^{-1} X_b (trans = 0) or A_b^{-T} X_b from slu_lu_factor output;
+ * X_b n x nrhs (ldx, stride sX).  Replaces scipy.linalg.lu_solve. */
+int slu_lu_solve(slu_handle_t h, int trans, int n, const double* LU, int lda, long long sA,
+                 const int* piv, long long sP, double* X, int ldx, long long sX, int nrhs, int nb);
+/* C_b = alpha op(A_b) op(B_b) + beta C_b, strided batch (row-major). */
+int slu_gemm_batched(slu_handle_t h, int transa, int transb, int M, int N, int K, double alpha,
+                     const double* A, int lda, long long sA, const double* B, int ldb,
+                     long long sB, double beta, double* C, int ldc, long long sC, int nb);
+
+/* ---------------------------------------------------------------- block tridiagonal
+ * Dense red-black cyclic reduction (direct_solve/omsdirectsolve.py:177-333,
+ * RedBlackSolver.factorize / solve) of nblk blocks of size m: SiM[i] couples
+ * block i to i-1, SiP[i] to i+1, T[i] is the diagonal (all nblk*m*m
+ * contiguous, device).  nblk must be a power of two (as upstream); the
+ * caller pads.  SiM[0] and SiP[nblk-1] are ignored (treated as zero). */
+int slu_rb_factor(slu_handle_t h, int nblk, int m, const double* SiM, const double* SiP,
+                  const double* T, slu_rb_t* out);
+/* B (nblk*m x nrhs, ldb) <- solution, in place. */
+int slu_rb_solve(slu_handle_t h, slu_rb_t rb, double* B, int ldb, int nrhs);
+int slu_rb_destroy(slu_rb_t rb);
+
+/* Dense block Thomas (direct_solve/omsdirectsolve.py:48-141,
+ * BlockTridiagonalSolver.factorize_helper / solve_helper) with the same block
+ * conventions as slu_rb_factor; nblk >= 1, any count. */
+int slu_thomas_factor(slu_handle_t h, int nblk, int m, const double* SiM, const double* SiP,
+                      const double* T, slu_rb_t* out);
+int slu_thomas_solve(slu_handle_t h, slu_rb_t th, double* B, int ldb, int nrhs);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SLABLU_H */

@@ -1,0 +1,471 @@
+// extern "C" boundary of libslablu (declared in include/slablu.h).
+// Every entry point catches slu::Error / std::exception and returns a status
+// code; the message is kept per thread for slu_last_error().
+#include <cstring>
+#include <memory>
+#include <string>
+
+#include "../../include/slablu.h"
+#include "tridiag.cuh"
+
+struct slu_handle_s {
+  slu::Handle h;
+};
+struct slu_hbs_s {
+  slu::Hbs H;
+};
+struct slu_dense_rb_s {
+  slu::RbSolver S;
+  bool thomas = false;
+};
+
+namespace {
+thread_local std::string g_err;
+
+template <class F>
+int guard(slu_handle_t h, F&& f) {
+  try {
+    f();
+    return SLU_OK;
+  } catch (const slu::Error& e) {
+    g_err = e.what();
+    if (h) h->h.last_error = g_err;
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    g_err = "host allocation failed";
+    return SLU_ERR_ALLOC;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return SLU_ERR_ARG;
+  } catch (...) {
+    g_err = "unknown error";
+    return SLU_ERR_ARG;
+  }
+}
+
+// per-column squared 2-norms of an rows x cols row-major array
+__global__ void colnorm2_kernel(int rows, int cols, const double* __restrict__ A, int lda,
+                                double* __restrict__ out) {
+  const int c = blockIdx.x;
+  double s = 0.0;
+  for (int i = threadIdx.x; i < rows; i += blockDim.x) {
+    double v = A[(long long)i * lda + c];
+    s += v * v;
+  }
+  __shared__ double red[32];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    out[c] = t;
+  }
+}
+
+// y = b - y  (rows x cols, leading dims)
+__global__ void residual_kernel(int rows, int cols, const double* __restrict__ b, int ldb,
+                                double* __restrict__ y, int ldy) {
+  long long n = (long long)rows * cols;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+       e += (long long)gridDim.x * blockDim.x) {
+    int i = (int)(e / cols), j = (int)(e % cols);
+    y[(long long)i * ldy + j] = b[(long long)i * ldb + j] - y[(long long)i * ldy + j];
+  }
+}
+// x += (double) d ; d float rows x cols dense (ld cols)
+__global__ void accum_kernel(int rows, int cols, const float* __restrict__ d, double* __restrict__ x,
+                             int ldx, int init) {
+  long long n = (long long)rows * cols;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+       e += (long long)gridDim.x * blockDim.x) {
+    int i = (int)(e / cols), j = (int)(e % cols);
+    double v = (double)d[e];
+    double* p = x + (long long)i * ldx + j;
+    *p = init ? v : *p + v;
+  }
+}
+// f = (float) r  (r ld ldr -> f dense)
+__global__ void tofloat_kernel(int rows, int cols, const double* __restrict__ r, int ldr,
+                               float* __restrict__ f) {
+  long long n = (long long)rows * cols;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+       e += (long long)gridDim.x * blockDim.x) {
+    int i = (int)(e / cols), j = (int)(e % cols);
+    f[e] = (float)r[(long long)i * ldr + j];
+  }
+}
+inline int gsz(long long n) {
+  long long g = (n + 255) / 256;
+  return (int)(g < 1 ? 1 : (g > 4096 ? 4096 : g));
+}
+}  // namespace
+
+extern "C" {
+
+int slu_version(void) { return 1; }
+
+int slu_last_error(char* buf, size_t len) {
+  if (!buf || len == 0) return SLU_ERR_ARG;
+  std::strncpy(buf, g_err.c_str(), len - 1);
+  buf[len - 1] = '\0';
+  return SLU_OK;
+}
+
+int slu_create(void* stream, slu_handle_t* out) {
+  return guard(nullptr, [&] {
+    SLU_REQUIRE(out, "null output pointer");
+    auto p = std::make_unique<slu_handle_s>();
+    p->h.stream = reinterpret_cast<cudaStream_t>(stream);
+    p->h.info.alloc(64 * sizeof(int), p->h.stream);
+    SLU_CHECK_CUDA(cudaMemsetAsync(p->h.info.p, 0, 64 * sizeof(int), p->h.stream));
+    *out = p.release();
+  });
+}
+
+int slu_destroy(slu_handle_t h) {
+  return guard(nullptr, [&] {
+    if (!h) return;
+    cudaStreamSynchronize(h->h.stream);
+    delete h;
+  });
+}
+
+int slu_set_stream(slu_handle_t h, void* stream) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h, "null handle");
+    SLU_CHECK_CUDA(cudaStreamSynchronize(h->h.stream));
+    h->h.stream = reinterpret_cast<cudaStream_t>(stream);
+  });
+}
+
+int slu_sync(slu_handle_t h) {
+  int st = guard(h, [&] {
+    SLU_REQUIRE(h, "null handle");
+    SLU_CHECK_CUDA(cudaStreamSynchronize(h->h.stream));
+  });
+  if (st != SLU_OK) return st;
+  int info[64];
+  st = guard(h, [&] {
+    SLU_CHECK_CUDA(cudaMemcpy(info, h->h.info.p, sizeof(info), cudaMemcpyDeviceToHost));
+  });
+  if (st != SLU_OK) return st;
+  if (info[0] != 0) {
+    cudaMemset(h->h.info.p, 0, sizeof(info));
+    g_err = "a device-side factorisation reported a failure (zero pivot or Jacobi sweep limit)";
+    h->h.last_error = g_err;
+    return SLU_ERR_NOT_CONVERGED;
+  }
+  return SLU_OK;
+}
+
+// ------------------------------------------------------------------ HBS
+int slu_hbs_create(slu_handle_t h, int N, int L, int fac, const int64_t* perm_host,
+                   slu_hbs_t* out) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h && out, "null argument");
+    SLU_REQUIRE(N > 0 && L >= 1 && (fac == 2 || fac == 4), "bad HBS geometry");
+    auto p = std::make_unique<slu_hbs_s>();
+    p->H.N = N;
+    p->H.L = L;
+    p->H.fac = fac;
+    std::vector<int64_t> perm(N);
+    bool ident = true;
+    if (perm_host) {
+      std::vector<char> seen(N, 0);
+      for (int i = 0; i < N; ++i) {
+        int64_t v = perm_host[i];
+        SLU_REQUIRE(v >= 0 && v < N && !seen[v], "perm is not a permutation of 0..N-1");
+        seen[v] = 1;
+        perm[i] = v;
+        ident = ident && (v == i);
+      }
+    } else {
+      for (int i = 0; i < N; ++i) perm[i] = i;
+    }
+    p->H.identity_perm = ident;
+    p->H.perm.alloc(sizeof(int64_t) * N, h->h.stream);
+    SLU_CHECK_CUDA(cudaMemcpyAsync(p->H.perm.p, perm.data(), sizeof(int64_t) * N,
+                                   cudaMemcpyHostToDevice, h->h.stream));
+    SLU_CHECK_CUDA(cudaStreamSynchronize(h->h.stream));
+    p->H.lv.resize(L);
+    *out = p.release();
+  });
+}
+
+int slu_hbs_destroy(slu_hbs_t op) {
+  return guard(nullptr, [&] { delete op; });
+}
+
+int slu_hbs_compress(slu_handle_t h, slu_hbs_t op, int nleaves, int rk, int s, const double* Om,
+                     const double* Psi, const double* Y, const double* Z, int compute_ulv) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h && op && Om && Psi && Y && Z, "null argument");
+    SLU_REQUIRE(s >= 1, "bad sample count");
+    slu::hbs_compress(h->h, op->H, nleaves, rk, s, Om, Psi, Y, Z, compute_ulv != 0);
+  });
+}
+
+int slu_hbs_set_level(slu_handle_t h, slu_hbs_t op, int level, int Nb, int n, int k,
+                      const double* U, const double* V, const double* D) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h && op && D, "null argument");
+    slu::Hbs& H = op->H;
+    SLU_REQUIRE(level >= 0 && level < H.L, "level out of range");
+    const bool root = (level == H.L - 1);
+    SLU_REQUIRE(Nb >= 1 && n >= 1 && k >= 0 && k <= n, "bad level geometry");
+    SLU_REQUIRE(root ? (k == 0 && Nb == 1) : (k >= 1 && U && V), "root takes k = 0, others U/V");
+    if (level == 0) SLU_REQUIRE((long long)Nb * n == H.N, "leaf level must cover N rows");
+    cudaStream_t st = h->h.stream;
+    slu::Level& l = H.lv[level];
+    l = slu::Level();
+    l.Nb = Nb;
+    l.n = n;
+    l.k = k;
+    const size_t rows = (size_t)Nb * n;
+    if (!root) {
+      l.U.alloc(8 * rows * k, st);
+      l.V.alloc(8 * rows * k, st);
+      SLU_CHECK_CUDA(cudaMemcpyAsync(l.U.p, U, 8 * rows * k, cudaMemcpyDeviceToDevice, st));
+      SLU_CHECK_CUDA(cudaMemcpyAsync(l.V.p, V, 8 * rows * k, cudaMemcpyDeviceToDevice, st));
+    }
+    l.D.alloc(8 * rows * n, st);
+    SLU_CHECK_CUDA(cudaMemcpyAsync(l.D.p, D, 8 * rows * n, cudaMemcpyDeviceToDevice, st));
+    // geometry is complete once every level is set
+    bool all = true;
+    for (const slu::Level& x : H.lv) all = all && x.D.p;
+    if (all) {
+      for (int t = 1; t < H.L; ++t) {
+        SLU_REQUIRE(H.lv[t].n == H.fac * H.lv[t - 1].k &&
+                        H.lv[t].Nb * H.fac == H.lv[t - 1].Nb,
+                    "inconsistent HBS level shapes");
+      }
+      H.NN.assign(H.L + 1, 0);
+      for (int t = 0; t < H.L; ++t) {
+        slu::Level& x = H.lv[t];
+        x.nu = (t == H.L - 1) ? x.n : x.n - x.k;
+        H.NN[t + 1] = H.NN[t] + (long long)x.nu * x.Nb;
+      }
+      H.has_mats = true;
+      H.has_ulv = false;
+      H.has_f32 = false;
+    }
+  });
+}
+
+int slu_ulv_factor(slu_handle_t h, slu_hbs_t op) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h && op, "null argument");
+    slu::hbs_factor(h->h, op->H);
+  });
+}
+
+int slu_hbs_apply(slu_handle_t h, slu_hbs_t op, int trans, const double* X, int ldx, double* Y,
+                  int ldy, int nrhs) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h && op && X && Y, "null argument");
+    SLU_REQUIRE(nrhs >= 1 && ldx >= nrhs && ldy >= nrhs, "bad right-hand side shape");
+    slu::hbs_apply(h->h, op->H, trans != 0, X, ldx, Y, ldy, nrhs);
+  });
+}
+
+int slu_ulv_solve(slu_handle_t h, slu_hbs_t op, double* B, int ldb, int nrhs, int trans) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h && op && B, "null argument");
+    SLU_REQUIRE(nrhs >= 1 && ldb >= nrhs, "bad right-hand side shape");
+    slu::hbs_solve<double>(h->h, op->H, trans != 0, B, ldb, nrhs);
+  });
+}
+
+int slu_hbs_prepare_f32(slu_handle_t h, slu_hbs_t op) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h && op, "null argument");
+    slu::hbs_make_f32(h->h, op->H);
+  });
+}
+
+int slu_ulv_solve_f32(slu_handle_t h, slu_hbs_t op, float* B, int ldb, int nrhs, int trans) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h && op && B, "null argument");
+    SLU_REQUIRE(nrhs >= 1 && ldb >= nrhs, "bad right-hand side shape");
+    slu::hbs_solve<float>(h->h, op->H, trans != 0, B, ldb, nrhs);
+  });
+}
+
+int slu_refine(slu_handle_t h, slu_hbs_t op, const double* B, int ldb, double* X, int ldx,
+               int nrhs, double tol, int maxit, int* iters_out, double* relres_out) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h && op && B && X, "null argument");
+    SLU_REQUIRE(nrhs >= 1 && ldb >= nrhs && ldx >= nrhs && maxit >= 1, "bad arguments");
+    slu::Hbs& H = op->H;
+    if (!H.has_f32) slu::hbs_make_f32(h->h, H);
+    cudaStream_t st = h->h.stream;
+    const int N = H.N, c = nrhs;
+    // own buffers: the apply/solve calls reuse the handle workspace
+    slu::DevBuf rbuf, fbuf, nbuf;
+    rbuf.alloc(8 * (size_t)N * c, st);
+    fbuf.alloc(4 * (size_t)N * c, st);
+    nbuf.alloc(8 * 2 * (size_t)c, st);
+    double* r = rbuf.as<double>();
+    float* f = fbuf.as<float>();
+    double* bn = nbuf.as<double>();
+    double* rn = bn + c;
+    colnorm2_kernel<<<c, 256, 0, st>>>(N, c, B, ldb, bn);
+    std::vector<double> hb(c), hr(c);
+    SLU_CHECK_CUDA(cudaMemcpyAsync(hb.data(), bn, 8 * c, cudaMemcpyDeviceToHost, st));
+    const long long nel = (long long)N * c;
+    tofloat_kernel<<<gsz(nel), 256, 0, st>>>(N, c, B, ldb, f);
+    int it = 0;
+    double worst = 0.0;
+    for (;;) {
+      slu::hbs_solve<float>(h->h, H, false, f, c, c);
+      accum_kernel<<<gsz(nel), 256, 0, st>>>(N, c, f, X, ldx, it == 0);
+      ++it;
+      slu::hbs_apply(h->h, H, false, X, ldx, r, c, c);
+      residual_kernel<<<gsz(nel), 256, 0, st>>>(N, c, B, ldb, r, c);
+      colnorm2_kernel<<<c, 256, 0, st>>>(N, c, r, c, rn);
+      SLU_CHECK_CUDA(cudaMemcpyAsync(hr.data(), rn, 8 * c, cudaMemcpyDeviceToHost, st));
+      SLU_CHECK_CUDA(cudaStreamSynchronize(st));
+      worst = 0.0;
+      for (int j = 0; j < c; ++j) {
+        double den = hb[j] > 0 ? std::sqrt(hb[j]) : 1.0;
+        worst = std::max(worst, std::sqrt(hr[j]) / den);
+      }
+      if (worst <= tol || it >= maxit) break;
+      tofloat_kernel<<<gsz(nel), 256, 0, st>>>(N, c, r, c, f);
+    }
+    slu::check_launch("refine kernels");
+    if (iters_out) *iters_out = it;
+    if (relres_out) *relres_out = worst;
+    if (worst > tol) throw slu::Error(SLU_ERR_NOT_CONVERGED, "refinement did not reach the tolerance");
+  });
+}
+
+int slu_hbs_info(slu_hbs_t op, int* L, int* N, int* levels, long long* NNvec, int* nsamples) {
+  return guard(nullptr, [&] {
+    SLU_REQUIRE(op, "null argument");
+    const slu::Hbs& H = op->H;
+    if (L) *L = H.L;
+    if (N) *N = H.N;
+    if (nsamples) *nsamples = H.nsamples;
+    if (levels)
+      for (int t = 0; t < H.L; ++t) {
+        levels[4 * t + 0] = H.lv[t].Nb;
+        levels[4 * t + 1] = H.lv[t].n;
+        levels[4 * t + 2] = H.lv[t].k;
+        levels[4 * t + 3] = H.lv[t].nu;
+      }
+    if (NNvec)
+      for (size_t t = 0; t < H.NN.size(); ++t) NNvec[t] = H.NN[t];
+  });
+}
+
+int slu_hbs_export(slu_handle_t h, slu_hbs_t op, int what, int level, double* dst, size_t count,
+                   size_t* count_out) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h && op, "null argument");
+    const slu::Hbs& H = op->H;
+    SLU_REQUIRE(level >= 0 && level < H.L, "level out of range");
+    const slu::Level& l = H.lv[level];
+    const slu::DevBuf* b = nullptr;
+    switch (what) {
+      case 0: b = &l.U; break;
+      case 1: b = &l.V; break;
+      case 2: b = &l.D; break;
+      case 3: b = &l.Q; break;
+      case 4: b = &l.W; break;
+      case 5: b = &l.R; break;
+      case 6: b = &l.Uu; break;
+      default: SLU_REQUIRE(false, "unknown factor id");
+    }
+    size_t n = b->bytes / 8;
+    if (count_out) *count_out = n;
+    if (dst && n) {
+      SLU_REQUIRE(count >= n, "destination too small");
+      SLU_CHECK_CUDA(cudaMemcpyAsync(dst, b->p, 8 * n, cudaMemcpyDeviceToDevice, h->h.stream));
+    }
+  });
+}
+
+int slu_hbs_nbytes(slu_hbs_t op, int which, size_t* out) {
+  return guard(nullptr, [&] {
+    SLU_REQUIRE(op && out, "null argument");
+    *out = slu::hbs_nbytes(op->H, which);
+  });
+}
+
+// ------------------------------------------------------------------ dense
+int slu_lu_factor(slu_handle_t h, int n, double* A, int lda, long long sA, int* piv,
+                  long long sP, int nb, int* info) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h && A && piv, "null argument");
+    SLU_REQUIRE(n >= 1 && lda >= n && nb >= 1, "bad shape");
+    slu::lu_factor(h->h.stream, n, A, lda, sA, piv, sP, nb, info);
+  });
+}
+
+int slu_lu_solve(slu_handle_t h, int trans, int n, const double* LU, int lda, long long sA,
+                 const int* piv, long long sP, double* X, int ldx, long long sX, int nrhs,
+                 int nb) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h && LU && piv && X, "null argument");
+    SLU_REQUIRE(n >= 1 && lda >= n && ldx >= nrhs && nb >= 1 && nrhs >= 1, "bad shape");
+    slu::lu_solve<double>(h->h.stream, trans != 0, n, LU, lda, sA, piv, sP, X, ldx, sX, nrhs, nb);
+  });
+}
+
+int slu_gemm_batched(slu_handle_t h, int transa, int transb, int M, int N, int K, double alpha,
+                     const double* A, int lda, long long sA, const double* B, int ldb,
+                     long long sB, double beta, double* C, int ldc, long long sC, int nb) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h && A && B && C, "null argument");
+    slu::gemm_batched<double>(h->h.stream, transa != 0, transb != 0, M, N, K, alpha, A, lda, sA,
+                              0, B, ldb, sB, 0, beta, C, ldc, sC, 0, nb, 1);
+  });
+}
+
+// ------------------------------------------------------------------ tridiagonal
+int slu_rb_factor(slu_handle_t h, int nblk, int m, const double* SiM, const double* SiP,
+                  const double* T, slu_rb_t* out) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h && SiM && SiP && T && out, "null argument");
+    auto p = std::make_unique<slu_dense_rb_s>();
+    slu::rb_factor(h->h, p->S, nblk, m, SiM, SiP, T);
+    *out = p.release();
+  });
+}
+
+int slu_rb_solve(slu_handle_t h, slu_rb_t rb, double* B, int ldb, int nrhs) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h && rb && B, "null argument");
+    SLU_REQUIRE(!rb->thomas, "handle was made by slu_thomas_factor");
+    SLU_REQUIRE(nrhs >= 1 && ldb >= nrhs, "bad right-hand side shape");
+    slu::rb_solve(h->h, rb->S, B, ldb, nrhs);
+  });
+}
+
+int slu_rb_destroy(slu_rb_t rb) {
+  return guard(nullptr, [&] { delete rb; });
+}
+
+int slu_thomas_factor(slu_handle_t h, int nblk, int m, const double* SiM, const double* SiP,
+                      const double* T, slu_rb_t* out) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h && SiM && SiP && T && out, "null argument");
+    auto p = std::make_unique<slu_dense_rb_s>();
+    p->thomas = true;
+    slu::thomas_factor(h->h, p->S, nblk, m, SiM, SiP, T);
+    *out = p.release();
+  });
+}
+
+int slu_thomas_solve(slu_handle_t h, slu_rb_t th, double* B, int ldb, int nrhs) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h && th && B, "null argument");
+    SLU_REQUIRE(th->thomas, "handle was made by slu_rb_factor");
+    SLU_REQUIRE(nrhs >= 1 && ldb >= nrhs, "bad right-hand side shape");
+    slu::thomas_solve(h->h, th->S, B, ldb, nrhs);
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,629 @@
+// HBS compression, ULV factorisation, apply and solve drivers.
+//
+// Follows the level recursions of
+//   matAssembly/HBS/HBSnew.py:211-295  (constructHBS_ULV: compression leaf ->
+//                                       root with the ULV interleaved)
+//   matAssembly/HBS/HBSnew.py:308-350  (matmat / rmatmat)
+//   matAssembly/HBS/HBSnew.py:393-416  (solve with the tree permutation)
+//   matAssembly/HBS/ULVsparse.py:64-100, 231-358 (compute_QRW_sparse,
+//                                       compute_ULV, solve N/T)
+// with every per-block loop replaced by one batched launch per level.
+//
+// Right pseudo-inverses X * pinv(Om_blk) (HBSnew.py:11-19, 48-62) are
+// evaluated as X * Q_1 * R^{-T} from the Householder QR Om_blk^T = Q_1 R that
+// compute_UV already needs, so each sketch block is factored once.  For the
+// full-row-rank Gaussian sketches this equals upstream's SVD pseudo-inverse
+// (rcond 1e-15 never truncates) to rounding.
+#include "hbs.cuh"
+
+#include <algorithm>
+#include <utility>
+
+namespace slu {
+namespace {
+
+inline double* dp(const DevBuf& b) { return b.as<double>(); }
+
+template <typename T>
+inline void gemm(cudaStream_t st, bool ta, bool tb, int M, int N, int K, T alpha, const T* A,
+                 int lda, long long sA0, long long sA1, const T* B, int ldb, long long sB0,
+                 long long sB1, T beta, T* C, int ldc, long long sC0, long long sC1, int b0,
+                 int b1 = 1) {
+  gemm_batched<T>(st, ta, tb, M, N, K, alpha, A, lda, sA0, sA1, B, ldb, sB0, sB1, beta, C, ldc,
+                  sC0, sC1, b0, b1);
+}
+
+inline void alloc_d(DevBuf& b, size_t count, cudaStream_t st) { b.alloc(count * sizeof(double), st); }
+
+void setup_geometry_common(Hbs& H) {
+  H.NN.assign(H.L + 1, 0);
+  for (int t = 0; t < H.L; ++t) {
+    Level& l = H.lv[t];
+    const bool root = (t == H.L - 1);
+    l.nu = root ? l.n : l.n - l.k;
+    H.NN[t + 1] = H.NN[t] + (long long)l.nu * l.Nb;
+  }
+}
+
+// ---------------------------------------------------------------- ULV level
+// One level of ULVsparse.compute_QRW_sparse (ULVsparse.py:64-100) plus the
+// Uhat recursion of compute_ULV / constructHBS_ULV (ULVsparse.py:273-287,
+// HBSnew.py:273-294).
+//   Rhat      : Nb*n x n (leaf: D; above: blkdiag(Ud_children) D + blkdiag(R22))
+//   Uhat      : Nb*n x kU
+//   kslice    : split of Q^T Uhat into Uu (first n-kslice rows) and Ud
+//   Ud_out    : Nb*kslice x kU, R22_out: Nb*k x k (non-root)
+struct UlvScratch {
+  double *WSV, *tauV, *Qk, *DWt, *tauQ, *Qc, *QtU;
+};
+
+void ulv_level(cudaStream_t st, Level& l, bool root, const double* Rhat, const double* Uhat,
+               int kU, int kslice, bool store_uu, double* Ud_out, double* R22_out,
+               const UlvScratch& s) {
+  const int Nb = l.Nb, n = l.n, k = root ? 0 : l.k, nu = l.nu;
+  const long long nn = (long long)n * n;
+  if (!root) {
+    // W1: trailing n-k columns of the complete QR of each V block (ULVsparse.py:18-25)
+    transpose_batched(st, n, k, dp(l.V), k, (long long)n * k, 0, s.WSV, n, (long long)n * k, 0, Nb);
+    panel_qr(st, n, k, k, s.WSV, n, (long long)n * k, s.tauV, k, Nb);
+    if (n > k) {
+      identity_cols(st, n, k, n - k, s.Qk, (long long)n * (n - k), Nb);
+      apply_q(st, false, n, k, s.WSV, n, (long long)n * k, s.tauV, k, s.Qk, n,
+              (long long)n * (n - k), n - k, Nb);
+      // W = [W1 | V]  (row-major n x n)
+      transpose_batched(st, n - k, n, s.Qk, n, (long long)n * (n - k), 0, dp(l.W), n, nn, 0, Nb);
+    }
+    copy_batched<double>(st, n, k, dp(l.V), k, (long long)n * k, 0, dp(l.W) + (n - k), n, nn, 0,
+                         Nb);
+    // (Rhat W)^T = W^T Rhat^T: row-major result == column-major Rhat W
+    gemm<double>(st, true, true, n, n, n, 1.0, dp(l.W), n, nn, 0, Rhat, n, nn, 0, 0.0, s.DWt, n,
+                 nn, 0, Nb);
+  } else {
+    transpose_batched(st, n, n, Rhat, n, nn, 0, s.DWt, n, nn, 0, Nb);
+  }
+  // square QR of Rhat W (ULVsparse.py:51-61)
+  panel_qr(st, n, n, n, s.DWt, n, nn, s.tauQ, n, Nb);
+  extract_upper(st, 0, nu, 0, n, s.DWt, n, nn, dp(l.R), n, (long long)nu * n, Nb);
+  if (!root && k > 0) extract_upper(st, nu, k, nu, k, s.DWt, n, nn, R22_out, k, (long long)k * k, Nb);
+  identity_cols(st, n, 0, n, s.Qc, nn, Nb);
+  apply_q(st, false, n, n, s.DWt, n, nn, s.tauQ, n, s.Qc, n, nn, n, Nb);
+  transpose_batched(st, n, n, s.Qc, n, nn, 0, dp(l.Q), n, nn, 0, Nb);
+  // Q^T Uhat -> Uu (leading rows) and Ud (trailing kslice rows)
+  if (kU > 0 && (store_uu || !root)) {
+    gemm<double>(st, true, false, n, kU, n, 1.0, dp(l.Q), n, nn, 0, Uhat, kU, (long long)n * kU,
+                 0, 0.0, s.QtU, kU, (long long)n * kU, 0, Nb);
+    if (store_uu && n > kslice)
+      copy_blocks(st, Nb, (long long)(n - kslice) * kU * 8, s.QtU, (long long)n * kU * 8,
+                  dp(l.Uu), (long long)(n - kslice) * kU * 8);
+    if (!root)
+      copy_blocks(st, Nb, (long long)kslice * kU * 8, s.QtU + (long long)(n - kslice) * kU,
+                  (long long)n * kU * 8, Ud_out, (long long)kslice * kU * 8);
+  }
+}
+
+size_t ulv_scratch_doubles(const Hbs& H) {
+  size_t m = 0;
+  for (const Level& l : H.lv) {
+    size_t nb = l.Nb, n = l.n, k = l.k;
+    size_t kU = std::max<size_t>(k, n);
+    m = std::max(m, nb * (n * k + k + n * n + n * n + n + n * n + n * kU));
+  }
+  return m;
+}
+
+UlvScratch carve_ulv(Workspace& ws, const Hbs& H) {
+  size_t a = 0, b = 0, c = 0, d = 0, e = 0;
+  for (const Level& l : H.lv) {
+    size_t nb = l.Nb, n = l.n, k = l.k;
+    a = std::max(a, nb * n * std::max<size_t>(k, 1));
+    b = std::max(b, nb * std::max<size_t>(k, 1));
+    c = std::max(c, nb * n * n);
+    d = std::max(d, nb * n);
+    e = std::max(e, nb * n * std::max<size_t>(std::max<size_t>(k, n), 1));
+  }
+  UlvScratch s;
+  s.WSV = ws.take<double>(a);
+  s.tauV = ws.take<double>(b);
+  s.Qk = ws.take<double>(c);
+  s.DWt = ws.take<double>(c);
+  s.tauQ = ws.take<double>(d);
+  s.Qc = ws.take<double>(c);
+  s.QtU = ws.take<double>(e);
+  return s;
+}
+
+size_t ulv_scratch_bytes(const Hbs& H) {
+  size_t a = 0, b = 0, c = 0, d = 0, e = 0;
+  for (const Level& l : H.lv) {
+    size_t nb = l.Nb, n = l.n, k = l.k;
+    a = std::max(a, nb * n * std::max<size_t>(k, 1));
+    b = std::max(b, nb * std::max<size_t>(k, 1));
+    c = std::max(c, nb * n * n);
+    d = std::max(d, nb * n);
+    e = std::max(e, nb * n * std::max<size_t>(std::max<size_t>(k, n), 1));
+  }
+  return 8 * (a + b + 3 * c + d + e) + 7 * 256;
+}
+
+// Rhat / Uhat of a non-leaf level from the children's Ud and R22.
+void merge_children(cudaStream_t st, const Hbs& H, int t, const double* Ud_c, const double* R22_c,
+                    double* Rhat, double* Uhat, bool root_uhat) {
+  const Level& l = H.lv[t];
+  const Level& c = H.lv[t - 1];
+  const int fac = H.fac, Nb = l.Nb, n = l.n, kc = c.k;
+  const long long kk = (long long)kc * kc, nn = (long long)n * n;
+  // Rhat = blkdiag(Ud_children) D + blkdiag(R22_children)  (ULVsparse.py:263-264)
+  gemm<double>(st, false, false, kc, n, kc, 1.0, Ud_c, kc, kk, fac * kk, dp(l.D), n,
+               (long long)kc * n, nn, 0.0, Rhat, n, (long long)kc * n, nn, fac, Nb);
+  add_batched<double>(st, kc, kc, 1.0, R22_c, kc, kk, fac * kk, Rhat, n, (long long)kc * n + kc,
+                      nn, fac, Nb);
+  const bool root = (t == H.L - 1);
+  if (!root) {
+    // Uhat = blkdiag(Ud_children) U  (ULVsparse.py:283)
+    const int k = l.k;
+    gemm<double>(st, false, false, kc, k, kc, 1.0, Ud_c, kc, kk, fac * kk, dp(l.U), k,
+                 (long long)kc * k, (long long)n * k, 0.0, Uhat, k, (long long)kc * k,
+                 (long long)n * k, fac, Nb);
+  } else if (root_uhat) {
+    // root: U = I, Uhat = blkdiag(Ud_children)  (HBSnew.py:271, 289)
+    SLU_CHECK_CUDA(cudaMemsetAsync(Uhat, 0, sizeof(double) * nn, st));
+    copy_batched<double>(st, kc, kc, Ud_c, kc, kk, 0, Uhat, n, (long long)kc * n + kc, 0, fac);
+  }
+}
+
+}  // namespace
+
+// ============================================================== compression
+void hbs_compress(Handle& h, Hbs& H, int Nb0, int rk, int s, const double* Om, const double* Psi,
+                  const double* Y, const double* Z, bool ulv) {
+  cudaStream_t st = h.stream;
+  const int N = H.N, L = H.L, fac = H.fac;
+  SLU_REQUIRE(L >= 1 && N > 0, "bad HBS geometry");
+  long long p = 1;
+  for (int t = 1; t < L; ++t) p *= fac;
+  SLU_REQUIRE(Nb0 == p, "leaf count must equal fac^(L-1)");
+  const int nl = N / Nb0;
+  SLU_REQUIRE((long long)nl * Nb0 == N, "N must be a multiple of the leaf count");
+  SLU_REQUIRE(rk >= 1, "rank must be positive");
+  SLU_REQUIRE(L == 1 || nl >= rk,
+              "leaf size smaller than the rank is not supported (upstream slices Q by rk)");
+  // ---- level geometry (HBSnew.py:234-256)
+  H.lv.clear();
+  H.lv.resize(L);
+  {
+    int Nb = Nb0, n = nl;
+    long long nomin = nl;
+    for (int t = 0; t < L; ++t) {
+      Level& l = H.lv[t];
+      l.Nb = Nb;
+      l.n = n;
+      int rkm = (int)std::min<long long>(rk, nomin);
+      l.k = (t < L - 1) ? rkm : 0;
+      Nb /= fac;
+      n = fac * rkm;
+      nomin *= fac;
+    }
+  }
+  setup_geometry_common(H);
+  for (int t = 0; t < L; ++t) {
+    Level& l = H.lv[t];
+    const bool root = (t == L - 1);
+    l.kU = root ? l.n : l.k;
+    l.uu_rows = root ? std::max(l.n - rk, 0) : l.n - l.k;
+    const size_t rows = (size_t)l.Nb * l.n;
+    if (!root) {
+      alloc_d(l.U, rows * l.k, st);
+      alloc_d(l.V, rows * l.k, st);
+      if (ulv) alloc_d(l.W, rows * l.n, st);
+    }
+    alloc_d(l.D, rows * l.n, st);
+    if (ulv) {
+      alloc_d(l.Q, rows * l.n, st);
+      alloc_d(l.R, (size_t)l.Nb * l.nu * l.n, st);
+      alloc_d(l.Uu, (size_t)l.Nb * l.uu_rows * l.kU, st);
+    }
+  }
+  H.rk = rk;
+  H.nsamples = s;
+  // ---- workspace
+  size_t Ns = (size_t)N * s;
+  size_t nmax = 0, kmax = 1;
+  for (const Level& l : H.lv) { nmax = std::max<size_t>(nmax, l.n); kmax = std::max<size_t>(kmax, l.k); }
+  size_t need = 8 * (8 * Ns + 4 * Ns + 2 * (size_t)N + 3 * (size_t)N * nmax) + 32 * 256;
+  if (ulv) need += ulv_scratch_bytes(H) + 8 * (2 * (size_t)N * nmax + 4 * (size_t)N * kmax) + 8 * 256;
+  h.ws.reserve(need, st);
+  double* set[2][4];
+  for (int a = 0; a < 2; ++a)
+    for (int b = 0; b < 4; ++b) set[a][b] = h.ws.take<double>(Ns);
+  double* WSA = h.ws.take<double>(2 * Ns);
+  double* WSB = h.ws.take<double>(2 * Ns);
+  double* tauA = h.ws.take<double>(N);
+  double* tauB = h.ws.take<double>(N);
+  double* PB = h.ws.take<double>((size_t)N * nmax);
+  double* T1 = h.ws.take<double>((size_t)N * nmax);
+  double* T2 = h.ws.take<double>((size_t)N * nmax);
+  UlvScratch us{};
+  double *Rhat = nullptr, *Uhat = nullptr, *Ud[2] = {nullptr, nullptr}, *R22[2] = {nullptr, nullptr};
+  if (ulv) {
+    us = carve_ulv(h.ws, H);
+    Rhat = h.ws.take<double>((size_t)N * nmax);
+    Uhat = h.ws.take<double>((size_t)N * nmax);
+    for (int a = 0; a < 2; ++a) {
+      Ud[a] = h.ws.take<double>((size_t)N * kmax);
+      R22[a] = h.ws.take<double>((size_t)N * kmax);
+    }
+  }
+  // leaf sketches: Om/Psi read in place, Y/Z copied (they are updated in place)
+  const double* Om_t = Om;
+  const double* Psi_t = Psi;
+  double* Y_t = set[0][2];
+  double* Z_t = set[0][3];
+  SLU_CHECK_CUDA(cudaMemcpyAsync(Y_t, Y, 8 * Ns, cudaMemcpyDeviceToDevice, st));
+  SLU_CHECK_CUDA(cudaMemcpyAsync(Z_t, Z, 8 * Ns, cudaMemcpyDeviceToDevice, st));
+  int cur = 0;
+  for (int t = 0; t < L; ++t) {
+    Level& l = H.lv[t];
+    const bool root = (t == L - 1);
+    const int Nb = l.Nb, n = l.n, k = l.k;
+    const long long ns = (long long)n * s, nn = (long long)n * n;
+    if (t > 0) {
+      // sketch update from the child level (HBSnew.py:244-251)
+      const Level& c = H.lv[t - 1];
+      const int nc = c.n, kc = c.k, Nbc = c.Nb;
+      const long long ncs = (long long)nc * s, kcs = (long long)kc * s, ncc = (long long)nc * nc;
+      const int nxt = cur ^ 1;
+      double* Om_n = set[nxt][0];
+      double* Psi_n = set[nxt][1];
+      double* Y_n = set[nxt][2];
+      double* Z_n = set[nxt][3];
+      gemm<double>(st, false, false, nc, s, nc, -1.0, dp(c.D), nc, ncc, 0, Om_t, s, ncs, 0, 1.0,
+                   Y_t, s, ncs, 0, Nbc);
+      gemm<double>(st, true, false, kc, s, nc, 1.0, dp(c.U), kc, (long long)nc * kc, 0, Y_t, s,
+                   ncs, 0, 0.0, Y_n, s, kcs, 0, Nbc);
+      gemm<double>(st, true, false, nc, s, nc, -1.0, dp(c.D), nc, ncc, 0, Psi_t, s, ncs, 0, 1.0,
+                   Z_t, s, ncs, 0, Nbc);
+      gemm<double>(st, true, false, kc, s, nc, 1.0, dp(c.V), kc, (long long)nc * kc, 0, Z_t, s,
+                   ncs, 0, 0.0, Z_n, s, kcs, 0, Nbc);
+      gemm<double>(st, true, false, kc, s, nc, 1.0, dp(c.V), kc, (long long)nc * kc, 0, Om_t, s,
+                   ncs, 0, 0.0, Om_n, s, kcs, 0, Nbc);
+      gemm<double>(st, true, false, kc, s, nc, 1.0, dp(c.U), kc, (long long)nc * kc, 0, Psi_t, s,
+                   ncs, 0, 0.0, Psi_n, s, kcs, 0, Nbc);
+      Om_t = Om_n;
+      Psi_t = Psi_n;
+      Y_t = Y_n;
+      Z_t = Z_n;
+      cur = nxt;
+    }
+    // ---- side A: QR of Om_blk^T with Y_blk rows carried along (compute_UV)
+    copy_blocks(st, Nb, 8 * ns, Om_t, 8 * ns, WSA, 16 * ns);
+    copy_blocks(st, Nb, 8 * ns, Y_t, 8 * ns, WSA + ns, 16 * ns);
+    panel_qr(st, s, n, 2 * n, WSA, s, 2 * ns, tauA, n, Nb);
+    const double* YQ1A = WSA + ns;   // row-major n x n (ld s): Y_blk * Q_1
+    if (!root) {
+      copy_blocks(st, Nb, 8 * ns, Psi_t, 8 * ns, WSB, 16 * ns);
+      copy_blocks(st, Nb, 8 * ns, Z_t, 8 * ns, WSB + ns, 16 * ns);
+      panel_qr(st, s, n, 2 * n, WSB, s, 2 * ns, tauB, n, Nb);
+      int* info = h.info.as<int>();
+      // U, V: leading left singular vectors of Y_blk Q[:, s-n:s] (HBSnew.py:26-27)
+      jacobi_left_sv(st, n, n, WSA + ns + (s - n), s, 2 * ns, k, dp(l.U), k, (long long)n * k,
+                     nullptr, 0, Nb, info);
+      jacobi_left_sv(st, n, n, WSB + ns + (s - n), s, 2 * ns, k, dp(l.V), k, (long long)n * k,
+                     nullptr, 0, Nb, info);
+      // D = (Y - U U^T Y) pinv(Om) + U U^T ((Z - V V^T Z) pinv(Psi))^T  (HBSnew.py:48-62)
+      const long long nk = (long long)n * k;
+      copy_batched<double>(st, n, n, YQ1A, s, 2 * ns, 0, dp(l.D), n, nn, 0, Nb);
+      gemm<double>(st, true, false, k, n, n, 1.0, dp(l.U), k, nk, 0, YQ1A, s, 2 * ns, 0, 0.0, T1,
+                   n, nk, 0, Nb);
+      gemm<double>(st, false, false, n, n, k, -1.0, dp(l.U), k, nk, 0, T1, n, nk, 0, 1.0, dp(l.D),
+                   n, nn, 0, Nb);
+      trsm_upper<double>(st, false, n, WSA, 1, s, 2 * ns, dp(l.D), 1, n, nn, n, Nb);
+      const double* YQ1B = WSB + ns;
+      copy_batched<double>(st, n, n, YQ1B, s, 2 * ns, 0, PB, n, nn, 0, Nb);
+      gemm<double>(st, true, false, k, n, n, 1.0, dp(l.V), k, nk, 0, YQ1B, s, 2 * ns, 0, 0.0, T1,
+                   n, nk, 0, Nb);
+      gemm<double>(st, false, false, n, n, k, -1.0, dp(l.V), k, nk, 0, T1, n, nk, 0, 1.0, PB, n,
+                   nn, 0, Nb);
+      trsm_upper<double>(st, false, n, WSB, 1, s, 2 * ns, PB, 1, n, nn, n, Nb);
+      gemm<double>(st, true, true, k, n, n, 1.0, dp(l.U), k, nk, 0, PB, n, nn, 0, 0.0, T2, n, nk,
+                   0, Nb);
+      gemm<double>(st, false, false, n, n, k, 1.0, dp(l.U), k, nk, 0, T2, n, nk, 0, 1.0, dp(l.D),
+                   n, nn, 0, Nb);
+    } else {
+      // root: D = Y pinv(Om)  (HBSnew.py:11-19, 268)
+      copy_batched<double>(st, n, n, YQ1A, s, 2 * ns, 0, dp(l.D), n, nn, 0, Nb);
+      trsm_upper<double>(st, false, n, WSA, 1, s, 2 * ns, dp(l.D), 1, n, nn, n, Nb);
+    }
+    // ---- interleaved ULV (HBSnew.py:273-294)
+    if (ulv) {
+      const int w = t & 1, r = w ^ 1;  // write / read slots of Ud, R22
+      const double* Rh = dp(l.D);
+      const double* Uh = root ? Uhat : dp(l.U);
+      if (t == 0 && root) identity_cols(st, n, 0, n, Uhat, nn, 1);  // single-level tree: U = I
+      if (t > 0) {
+        merge_children(st, H, t, Ud[r], R22[r], Rhat, Uhat, true);
+        Rh = Rhat;
+        Uh = Uhat;
+      }
+      ulv_level(st, l, root, Rh, Uh, l.kU, rk, true, Ud[w], R22[w], us);
+    }
+  }
+  H.has_mats = true;
+  H.has_ulv = ulv;
+  H.has_f32 = false;
+}
+
+// ============================================================== standalone ULV
+void hbs_factor(Handle& h, Hbs& H) {
+  cudaStream_t st = h.stream;
+  SLU_REQUIRE(H.has_mats, "HBS factors not loaded");
+  const int L = H.L;
+  size_t nmax = 0, kmax = 1, N = H.N;
+  for (const Level& l : H.lv) { nmax = std::max<size_t>(nmax, l.n); kmax = std::max<size_t>(kmax, l.k); }
+  for (int t = 0; t < L; ++t) {
+    Level& l = H.lv[t];
+    const bool root = (t == L - 1);
+    l.kU = root ? 0 : l.k;
+    l.uu_rows = root ? 0 : l.n - l.k;
+    const size_t rows = (size_t)l.Nb * l.n;
+    if (!root) alloc_d(l.W, rows * l.n, st);
+    alloc_d(l.Q, rows * l.n, st);
+    alloc_d(l.R, (size_t)l.Nb * l.nu * l.n, st);
+    if (!root) alloc_d(l.Uu, (size_t)l.Nb * l.uu_rows * l.kU, st);
+  }
+  h.ws.reserve(ulv_scratch_bytes(H) + 8 * (2 * N * nmax + 4 * N * kmax) + 8 * 256, st);
+  UlvScratch us = carve_ulv(h.ws, H);
+  double* Rhat = h.ws.take<double>(N * nmax);
+  double* Uhat = h.ws.take<double>(N * nmax);
+  double *Ud[2], *R22[2];
+  for (int a = 0; a < 2; ++a) {
+    Ud[a] = h.ws.take<double>(N * kmax);
+    R22[a] = h.ws.take<double>(N * kmax);
+  }
+  for (int t = 0; t < L; ++t) {
+    Level& l = H.lv[t];
+    const bool root = (t == L - 1);
+    const int w = t & 1, r = w ^ 1;
+    const double* Rh = dp(l.D);
+    const double* Uh = root ? nullptr : dp(l.U);
+    if (t > 0) {
+      merge_children(st, H, t, Ud[r], R22[r], Rhat, Uhat, false);
+      Rh = Rhat;
+      Uh = Uhat;
+    }
+    ulv_level(st, l, root, Rh, Uh, l.kU, l.k, !root, Ud[w], R22[w], us);
+  }
+  H.has_ulv = true;
+  H.has_f32 = false;
+}
+
+// ============================================================== apply
+void hbs_apply(Handle& h, const Hbs& H, bool trans, const double* X, int ldx, double* Yout,
+               int ldy, int c) {
+  cudaStream_t st = h.stream;
+  SLU_REQUIRE(H.has_mats, "HBS factors not loaded");
+  const int L = H.L;
+  const size_t N = H.N;
+  size_t vvrows = N;
+  for (int t = 0; t + 1 < L; ++t) vvrows += (size_t)H.lv[t].Nb * H.lv[t].k;
+  h.ws.reserve(8 * ((vvrows + 2 * N) * c) + 8 * 256, st);
+  double* VVbuf = h.ws.take<double>(vvrows * c);
+  double* u0 = h.ws.take<double>(N * c);
+  double* u1 = h.ws.take<double>(N * c);
+  // VV[t] offsets: VV[0] has N rows, VV[t+1] has Nb_t*k_t rows
+  std::vector<double*> VV(L);
+  VV[0] = VVbuf;
+  {
+    size_t off = N;
+    for (int t = 0; t + 1 < L; ++t) {
+      VV[t + 1] = VVbuf + off * c;
+      off += (size_t)H.lv[t].Nb * H.lv[t].k;
+    }
+  }
+  permute_rows<double>(st, false, (int)N, c, H.perm.as<int64_t>(), X, ldx, VV[0], c);
+  for (int t = 0; t + 1 < L; ++t) {
+    const Level& l = H.lv[t];
+    const double* F = trans ? dp(l.U) : dp(l.V);
+    gemm<double>(st, true, false, l.k, c, l.n, 1.0, F, l.k, (long long)l.n * l.k, 0, VV[t], c,
+                 (long long)l.n * c, 0, 0.0, VV[t + 1], c, (long long)l.k * c, 0, l.Nb);
+  }
+  const Level& r = H.lv[L - 1];
+  double* u = u0;
+  double* un = u1;
+  gemm<double>(st, trans, false, r.n, c, r.n, 1.0, dp(r.D), r.n, 0, 0, VV[L - 1], c, 0, 0, 0.0, u,
+               c, 0, 0, 1);
+  for (int t = L - 2; t >= 0; --t) {
+    const Level& l = H.lv[t];
+    const double* G = trans ? dp(l.V) : dp(l.U);
+    gemm<double>(st, false, false, l.n, c, l.k, 1.0, G, l.k, (long long)l.n * l.k, 0, u, c,
+                 (long long)l.k * c, 0, 0.0, un, c, (long long)l.n * c, 0, l.Nb);
+    gemm<double>(st, trans, false, l.n, c, l.n, 1.0, dp(l.D), l.n, (long long)l.n * l.n, 0, VV[t],
+                 c, (long long)l.n * c, 0, 1.0, un, c, (long long)l.n * c, 0, l.Nb);
+    std::swap(u, un);
+  }
+  permute_rows<double>(st, true, (int)N, c, H.perm.as<int64_t>(), u, c, Yout, ldy);
+}
+
+// ============================================================== solve
+namespace {
+template <typename T> struct Fac;
+template <> struct Fac<double> {
+  static const double* U(const Level& l) { return l.U.as<double>(); }
+  static const double* D(const Level& l) { return l.D.as<double>(); }
+  static const double* Q(const Level& l) { return l.Q.as<double>(); }
+  static const double* W(const Level& l) { return l.W.as<double>(); }
+  static const double* R(const Level& l) { return l.R.as<double>(); }
+  static const double* Uu(const Level& l) { return l.Uu.as<double>(); }
+};
+template <> struct Fac<float> {
+  static const float* U(const Level& l) { return l.Uf.as<float>(); }
+  static const float* D(const Level& l) { return l.Df.as<float>(); }
+  static const float* Q(const Level& l) { return l.Qf.as<float>(); }
+  static const float* W(const Level& l) { return l.Wf.as<float>(); }
+  static const float* R(const Level& l) { return l.Rf.as<float>(); }
+  static const float* Uu(const Level& l) { return l.Uuf.as<float>(); }
+};
+}  // namespace
+
+template <typename T>
+void hbs_solve(Handle& h, const Hbs& H, bool trans, T* B, int ldb, int c) {
+  using F = Fac<T>;
+  cudaStream_t st = h.stream;
+  SLU_REQUIRE(H.has_ulv, "HBS operator has no ULV factorisation");
+  if (sizeof(T) == 4) SLU_REQUIRE(H.has_f32, "single-precision factors not prepared");
+  const int L = H.L;
+  const size_t N = H.N;
+  const std::vector<long long>& NN = H.NN;
+  h.ws.reserve(sizeof(T) * (5 * N * c) + 8 * 256, st);
+  T* r = h.ws.take<T>(N * c);
+  T* y = h.ws.take<T>(N * c);
+  T* tmp = h.ws.take<T>(N * c);
+  T* v = h.ws.take<T>(N * c);
+  T* vn = h.ws.take<T>(N * c);
+  const T one = T(1), zero = T(0), mone = T(-1);
+  const int64_t* perm = H.perm.as<int64_t>();
+  if (!trans) {
+    // ---- mode N (ULVsparse.py:296-327)
+    permute_rows<T>(st, false, (int)N, c, perm, B, ldb, r, c);
+    for (int t = 0; t < L; ++t) {
+      const Level& l = H.lv[t];
+      const int n = l.n, Nb = l.Nb;
+      const long long nn = (long long)n * n;
+      SLU_CHECK_CUDA(cudaMemcpyAsync(tmp, r + NN[t] * c, sizeof(T) * (size_t)Nb * n * c,
+                                     cudaMemcpyDeviceToDevice, st));
+      if (t < L - 1) {
+        const int k = l.k, nu = l.nu;
+        gemm<T>(st, true, false, nu, c, n, one, F::Q(l), n, nn, 0, tmp, c, (long long)n * c, 0,
+                zero, r + NN[t] * c, c, (long long)nu * c, 0, Nb);
+        gemm<T>(st, true, false, k, c, n, one, F::Q(l) + nu, n, nn, 0, tmp, c, (long long)n * c, 0,
+                zero, r + NN[t + 1] * c, c, (long long)k * c, 0, Nb);
+      } else {
+        gemm<T>(st, true, false, n, c, n, one, F::Q(l), n, 0, 0, tmp, c, 0, 0, zero,
+                r + NN[t] * c, c, 0, 0, 1);
+      }
+    }
+    const Level& rt = H.lv[L - 1];
+    T* yr = y + NN[L - 1] * c;
+    SLU_CHECK_CUDA(cudaMemcpyAsync(yr, r + NN[L - 1] * c, sizeof(T) * (size_t)rt.n * c,
+                                   cudaMemcpyDeviceToDevice, st));
+    trsm_upper<T>(st, false, rt.n, F::R(rt), rt.n, 1, 0, yr, c, 1, 0, c, 1);
+    gemm<T>(st, false, false, rt.n, c, rt.n, one, F::D(rt), rt.n, 0, 0, yr, c, 0, 0, zero, v, c,
+            0, 0, 1);
+    for (int t = L - 2; t >= 0; --t) {
+      const Level& l = H.lv[t];
+      const int n = l.n, k = l.k, nu = l.nu, Nb = l.Nb;
+      const long long nn = (long long)n * n;
+      T* yt = y + NN[t] * c;
+      T* ynx = y + NN[t + 1] * c;
+      if (nu > 0) {
+        SLU_CHECK_CUDA(cudaMemcpyAsync(yt, r + NN[t] * c, sizeof(T) * (size_t)Nb * nu * c,
+                                       cudaMemcpyDeviceToDevice, st));
+        gemm<T>(st, false, false, nu, c, k, mone, F::Uu(l), k, (long long)nu * k, 0, v, c,
+                (long long)k * c, 0, one, yt, c, (long long)nu * c, 0, Nb);
+        gemm<T>(st, false, false, nu, c, k, mone, F::R(l) + nu, n, (long long)nu * n, 0, ynx, c,
+                (long long)k * c, 0, one, yt, c, (long long)nu * c, 0, Nb);
+        trsm_upper<T>(st, false, nu, F::R(l), n, 1, (long long)nu * n, yt, c, 1,
+                      (long long)nu * c, c, Nb);
+      }
+      gemm<T>(st, false, false, n, c, nu, one, F::W(l), n, nn, 0, yt, c, (long long)nu * c, 0,
+              zero, tmp, c, (long long)n * c, 0, Nb);
+      gemm<T>(st, false, false, n, c, k, one, F::W(l) + nu, n, nn, 0, ynx, c, (long long)k * c, 0,
+              one, tmp, c, (long long)n * c, 0, Nb);
+      SLU_CHECK_CUDA(cudaMemcpyAsync(yt, tmp, sizeof(T) * (size_t)Nb * n * c,
+                                     cudaMemcpyDeviceToDevice, st));
+      gemm<T>(st, false, false, n, c, k, one, F::U(l), k, (long long)n * k, 0, v, c,
+              (long long)k * c, 0, zero, vn, c, (long long)n * c, 0, Nb);
+      gemm<T>(st, false, false, n, c, n, one, F::D(l), n, nn, 0, yt, c, (long long)n * c, 0, one,
+              vn, c, (long long)n * c, 0, Nb);
+      std::swap(v, vn);
+    }
+    permute_rows<T>(st, true, (int)N, c, perm, y, c, B, ldb);
+  } else {
+    // ---- mode T (ULVsparse.py:328-353); upstream scatters the input and
+    // gathers the output (HBSnew.py:403-411)
+    permute_rows<T>(st, true, (int)N, c, perm, B, ldb, r, c);
+    T* rn = tmp;
+    bool have_v = false;
+    for (int t = 0; t + 1 < L; ++t) {
+      const Level& l = H.lv[t];
+      const Level& l1 = H.lv[t + 1];
+      const int n = l.n, k = l.k, nu = l.nu, Nb = l.Nb;
+      const long long nn = (long long)n * n;
+      T* yt = y + NN[t] * c;
+      gemm<T>(st, true, false, nu, c, n, one, F::W(l), n, nn, 0, r, c, (long long)n * c, 0, zero,
+              yt, c, (long long)nu * c, 0, Nb);
+      gemm<T>(st, true, false, k, c, n, one, F::W(l) + nu, n, nn, 0, r, c, (long long)n * c, 0,
+              zero, rn, c, (long long)k * c, 0, Nb);
+      trsm_upper<T>(st, true, nu, F::R(l), n, 1, (long long)nu * n, yt, c, 1, (long long)nu * c,
+                    c, Nb);
+      gemm<T>(st, true, false, k, c, nu, one, F::Uu(l), k, (long long)nu * k, 0, yt, c,
+              (long long)nu * c, 0, zero, vn, c, (long long)k * c, 0, Nb);
+      if (have_v)
+        gemm<T>(st, true, false, k, c, n, one, F::U(l), k, (long long)n * k, 0, v, c,
+                (long long)n * c, 0, one, vn, c, (long long)k * c, 0, Nb);
+      gemm<T>(st, true, false, k, c, nu, mone, F::R(l) + nu, n, (long long)nu * n, 0, yt, c,
+              (long long)nu * c, 0, one, rn, c, (long long)k * c, 0, Nb);
+      const int n1 = l1.n;
+      gemm<T>(st, true, false, n1, c, n1, mone, F::D(l1), n1, (long long)n1 * n1, 0, vn, c,
+              (long long)n1 * c, 0, one, rn, c, (long long)n1 * c, 0, l1.Nb);
+      std::swap(r, rn);
+      std::swap(v, vn);
+      have_v = true;
+    }
+    const Level& rt = H.lv[L - 1];
+    T* yr = y + NN[L - 1] * c;
+    SLU_CHECK_CUDA(cudaMemcpyAsync(yr, r, sizeof(T) * (size_t)rt.n * c, cudaMemcpyDeviceToDevice, st));
+    trsm_upper<T>(st, true, rt.n, F::R(rt), rt.n, 1, 0, yr, c, 1, 0, c, 1);
+    T* scratch = rn;
+    for (int t = L - 1; t >= 0; --t) {
+      const Level& l = H.lv[t];
+      const int n = l.n, Nb = l.Nb;
+      const long long nn = (long long)n * n;
+      T* yt = y + NN[t] * c;
+      if (t == L - 1) {
+        gemm<T>(st, false, false, n, c, n, one, F::Q(l), n, 0, 0, yt, c, 0, 0, zero, scratch, c, 0,
+                0, 1);
+      } else {
+        const int k = l.k, nu = l.nu;
+        gemm<T>(st, false, false, n, c, nu, one, F::Q(l), n, nn, 0, yt, c, (long long)nu * c, 0,
+                zero, scratch, c, (long long)n * c, 0, Nb);
+        gemm<T>(st, false, false, n, c, k, one, F::Q(l) + nu, n, nn, 0, y + NN[t + 1] * c, c,
+                (long long)k * c, 0, one, scratch, c, (long long)n * c, 0, Nb);
+      }
+      SLU_CHECK_CUDA(cudaMemcpyAsync(yt, scratch, sizeof(T) * (size_t)Nb * n * c,
+                                     cudaMemcpyDeviceToDevice, st));
+    }
+    permute_rows<T>(st, false, (int)N, c, perm, y, c, B, ldb);
+  }
+}
+template void hbs_solve<double>(Handle&, const Hbs&, bool, double*, int, int);
+template void hbs_solve<float>(Handle&, const Hbs&, bool, float*, int, int);
+
+void hbs_make_f32(Handle& h, Hbs& H) {
+  cudaStream_t st = h.stream;
+  SLU_REQUIRE(H.has_ulv, "HBS operator has no ULV factorisation");
+  auto cp = [&](const DevBuf& src, DevBuf& dst) {
+    size_t n = src.bytes / 8;
+    dst.alloc(n * 4, st);
+    cast_f64_f32(st, (long long)n, src.as<double>(), dst.as<float>());
+  };
+  for (Level& l : H.lv) {
+    cp(l.U, l.Uf);
+    cp(l.D, l.Df);
+    cp(l.Q, l.Qf);
+    cp(l.W, l.Wf);
+    cp(l.R, l.Rf);
+    cp(l.Uu, l.Uuf);
+  }
+  H.has_f32 = true;
+}
+
+size_t hbs_nbytes(const Hbs& H, int which) {
+  size_t b = 0;
+  for (const Level& l : H.lv) {
+    if (which == 0) b += l.U.bytes + l.V.bytes + l.D.bytes;
+    else b += l.U.bytes + l.D.bytes + l.Q.bytes + l.W.bytes + l.R.bytes + l.Uu.bytes;
+  }
+  return b;
+}
+
+}  // namespace slu

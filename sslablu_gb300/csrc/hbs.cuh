@@ -1,0 +1,71 @@
+// HBS operator owned by the library: level factors, ULV factors, and the
+// compression / factorisation / apply / solve drivers.
+#pragma once
+#include "slablu_internal.cuh"
+
+namespace slu {
+
+// Per-call scratch arena (grow-only, stream ordered).
+struct Workspace {
+  DevBuf buf;
+  size_t off = 0;
+  void reset() { off = 0; }
+  // Reserve `bytes` total for this call (reallocates if needed; contents lost).
+  void reserve(size_t bytes, cudaStream_t st) {
+    if (buf.bytes < bytes) buf.alloc(bytes + (bytes >> 2), st);
+    off = 0;
+  }
+  template <class T> T* take(size_t count) {
+    size_t b = (count * sizeof(T) + 255) & ~size_t(255);
+    if (off + b > buf.bytes) throw Error(SLU_ERR_ALLOC, "workspace overflow");
+    T* p = reinterpret_cast<T*>(reinterpret_cast<char*>(buf.p) + off);
+    off += b;
+    return p;
+  }
+};
+
+struct Handle {
+  cudaStream_t stream = nullptr;
+  Workspace ws;
+  DevBuf info;  // int[64] device status words
+  std::string last_error;
+};
+
+struct Level {
+  int Nb = 0;   // blocks on this level
+  int n = 0;    // rows (and columns of D) per block
+  int k = 0;    // columns of U and V (0 on the root)
+  int kU = 0;   // columns of the ULV Uu factor
+  int nu = 0;   // rows of Ru per block (n - k; n on the root)
+  int uu_rows = 0;  // rows of Uu per block
+  DevBuf U, V, D;       // Nb*n x k, Nb*n x k, Nb*n x n
+  DevBuf Q, W, R, Uu;   // Nb*n x n, Nb*n x n, Nb*nu x n, Nb*uu_rows x kU
+  // single-precision copies of the solve factors (mixed-precision solve)
+  DevBuf Uf, Df, Qf, Wf, Rf, Uuf;
+};
+
+struct Hbs {
+  int N = 0, L = 0, fac = 2;
+  std::vector<Level> lv;           // lv[0] = leaves, lv[L-1] = root
+  DevBuf perm;                     // int64[N]
+  bool identity_perm = true;
+  std::vector<long long> NN;       // NNvec, L+1 entries
+  bool has_mats = false, has_ulv = false, has_f32 = false;
+  int rk = 0, nsamples = 0;
+};
+
+// compression + interleaved ULV (HBSnew.HBSMAT.constructHBS_ULV)
+void hbs_compress(Handle& h, Hbs& H, int Nb_leaf, int rk, int s, const double* Om,
+                  const double* Psi, const double* Y, const double* Z, bool ulv);
+// standalone ULV of loaded factors (ULVsparse.compute_ULV)
+void hbs_factor(Handle& h, Hbs& H);
+// u = A v (trans = false) or A^T v, tree-ordered input/output when perm_io is false
+void hbs_apply(Handle& h, const Hbs& H, bool trans, const double* X, int ldx, double* Yout,
+               int ldy, int nrhs);
+// ULV solve, reference semantics of HBSMAT.solve (with the permutation)
+template <typename T>
+void hbs_solve(Handle& h, const Hbs& H, bool trans, T* B, int ldb, int nrhs);
+void hbs_make_f32(Handle& h, Hbs& H);
+size_t hbs_nbytes(const Hbs& H, int which);
+
+}  // namespace slu

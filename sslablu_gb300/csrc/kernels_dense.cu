@@ -1,0 +1,607 @@
+// Dense building blocks: batched GEMM, triangular and LU solves, LU with
+// partial pivoting, row permutations and elementwise helpers.
+//
+// These run the block-diagonal products of the HBS tree levels
+// (matAssembly/HBS/HBSnew.py:32-47 block_mult, ULVsparse.py:101-203
+// sparse_block_mult / apply_sparse_block), the block solves of the ULV sweep
+// (ULVsparse.py:213-226) and the pivot-block LU of the red-black elimination
+// (direct_solve/omsdirectsolve.py:211,333 lu_factor / lu_solve).
+#include "slablu_internal.cuh"
+
+namespace slu {
+
+int num_sms() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 1;
+  }
+  return n;
+}
+
+// ============================================================== batched GEMM
+// 64x64 output tile per CTA, 256 threads, 4x4 outputs per thread, K step 16.
+namespace {
+constexpr int GBM = 64, GBN = 64, GBK = 16;
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+gemm_kernel(int M, int N, int K, T alpha, const T* __restrict__ A, int lda, long long sA0,
+            long long sA1, bool ta, const T* __restrict__ B, int ldb, long long sB0,
+            long long sB1, bool tb, T beta, T* __restrict__ C, int ldc, long long sC0,
+            long long sC1, int batch0) {
+  __shared__ T As[GBK][GBM + 1];
+  __shared__ T Bs[GBK][GBN + 1];
+  const int b = blockIdx.z;
+  const int b0 = b % batch0, b1 = b / batch0;
+  A += b0 * sA0 + b1 * sA1;
+  B += b0 * sB0 + b1 * sB1;
+  C += b0 * sC0 + b1 * sC1;
+  const int row0 = blockIdx.y * GBM, col0 = blockIdx.x * GBN;
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  T acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
+
+  for (int k0 = 0; k0 < K; k0 += GBK) {
+#pragma unroll
+    for (int e = tid; e < GBM * GBK; e += 256) {
+      int i, kk;
+      if (!ta) { i = e / GBK; kk = e % GBK; } else { kk = e / GBM; i = e % GBM; }
+      int gi = row0 + i, gk = k0 + kk;
+      T v = T(0);
+      if (gi < M && gk < K) v = ta ? A[(long long)gk * lda + gi] : A[(long long)gi * lda + gk];
+      As[kk][i] = v;
+    }
+#pragma unroll
+    for (int e = tid; e < GBN * GBK; e += 256) {
+      int j, kk;
+      if (!tb) { kk = e / GBN; j = e % GBN; } else { j = e / GBK; kk = e % GBK; }
+      int gj = col0 + j, gk = k0 + kk;
+      T v = T(0);
+      if (gj < N && gk < K) v = tb ? B[(long long)gj * ldb + gk] : B[(long long)gk * ldb + gj];
+      Bs[kk][j] = v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < GBK; ++kk) {
+      T a[4], bb[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) bb[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], bb[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    int gi = row0 + ty + 16 * i;
+    if (gi >= M) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      int gj = col0 + tx + 16 * j;
+      if (gj >= N) continue;
+      T* c = C + (long long)gi * ldc + gj;
+      T v = alpha * acc[i][j];
+      if (beta != T(0)) v = fma(beta, *c, v);
+      *c = v;
+    }
+  }
+}
+}  // namespace
+
+template <typename T>
+void gemm_batched(cudaStream_t st, bool ta, bool tb, int M, int N, int K, T alpha, const T* A,
+                  int lda, long long sA0, long long sA1, const T* B, int ldb, long long sB0,
+                  long long sB1, T beta, T* C, int ldc, long long sC0, long long sC1, int batch0,
+                  int batch1) {
+  if (M <= 0 || N <= 0 || batch0 <= 0 || batch1 <= 0) return;
+  if (K <= 0) {  // C = beta C
+    SLU_REQUIRE(beta == T(0) || beta == T(1), "gemm with K=0 needs beta 0 or 1");
+    if (beta == T(0)) {
+      for (int b1 = 0; b1 < batch1; ++b1)
+        for (int b0 = 0; b0 < batch0; ++b0)
+          SLU_CHECK_CUDA(cudaMemset2DAsync(C + b0 * sC0 + b1 * sC1, sizeof(T) * ldc, 0,
+                                           sizeof(T) * N, M, st));
+    }
+    return;
+  }
+  long long nb = (long long)batch0 * batch1;
+  SLU_REQUIRE(nb <= 65535, "gemm batch too large");
+  dim3 grid((N + GBN - 1) / GBN, (M + GBM - 1) / GBM, (unsigned)nb);
+  gemm_kernel<T><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, sA0, sA1, ta, B, ldb, sB0, sB1,
+                                       tb, beta, C, ldc, sC0, sC1, batch0);
+  check_launch("gemm_kernel");
+}
+
+template void gemm_batched<double>(cudaStream_t, bool, bool, int, int, int, double,
+                                   const double*, int, long long, long long, const double*, int,
+                                   long long, long long, double, double*, int, long long,
+                                   long long, int, int);
+template void gemm_batched<float>(cudaStream_t, bool, bool, int, int, int, float, const float*,
+                                  int, long long, long long, const float*, int, long long,
+                                  long long, float, float*, int, long long, long long, int, int);
+
+// ============================================================== triangular solve
+// One CTA per (matrix, chunk of right-hand sides).  Column-oriented
+// substitution: after x_i is final, every remaining row subtracts R_ri x_i.
+namespace {
+template <typename T>
+__global__ void trsm_upper_kernel(bool trans, int n, const T* __restrict__ R, long long rRs,
+                                  long long rCs, long long sR, T* __restrict__ X, long long xRs,
+                                  long long xCs, long long sX, int nrhs, int chunk) {
+  const int b = blockIdx.y;
+  R += b * sR;
+  X += b * sX;
+  const int c0 = blockIdx.x * chunk;
+  const int nc = min(chunk, nrhs - c0);
+  if (nc <= 0) return;
+  extern __shared__ unsigned char smraw[];
+  T* xs = reinterpret_cast<T*>(smraw);  // n x nc
+  for (int e = threadIdx.x; e < n * nc; e += blockDim.x) {
+    int i = e / nc, c = e % nc;
+    xs[e] = X[i * xRs + (c0 + c) * xCs];
+  }
+  __syncthreads();
+#define RR(i, j) R[(long long)(i) * rRs + (long long)(j) * rCs]
+  if (!trans) {
+    for (int i = n - 1; i >= 0; --i) {
+      T d = RR(i, i);
+      for (int c = threadIdx.x; c < nc; c += blockDim.x) xs[i * nc + c] /= d;
+      __syncthreads();
+      for (int e = threadIdx.x; e < i * nc; e += blockDim.x) {
+        int r = e / nc, c = e % nc;
+        xs[e] -= RR(r, i) * xs[i * nc + c];
+      }
+      __syncthreads();
+    }
+  } else {
+    for (int i = 0; i < n; ++i) {
+      T d = RR(i, i);
+      for (int c = threadIdx.x; c < nc; c += blockDim.x) xs[i * nc + c] /= d;
+      __syncthreads();
+      int rem = (n - i - 1) * nc;
+      for (int e = threadIdx.x; e < rem; e += blockDim.x) {
+        int r = i + 1 + e / nc, c = e % nc;
+        xs[r * nc + c] -= RR(i, r) * xs[i * nc + c];
+      }
+      __syncthreads();
+    }
+  }
+#undef RR
+  for (int e = threadIdx.x; e < n * nc; e += blockDim.x) {
+    int i = e / nc, c = e % nc;
+    X[i * xRs + (c0 + c) * xCs] = xs[e];
+  }
+}
+}  // namespace
+
+template <typename T>
+void trsm_upper(cudaStream_t st, bool trans, int n, const T* R, long long rRs, long long rCs,
+                long long sR, T* X, long long xRs, long long xCs, long long sX, int nrhs,
+                int batch) {
+  if (n <= 0 || nrhs <= 0 || batch <= 0) return;
+  int chunk = nrhs;
+  while ((size_t)n * chunk * sizeof(T) > 96 * 1024 && chunk > 1) chunk = (chunk + 1) / 2;
+  while (chunk > 16 && (long long)batch * ((nrhs + chunk - 1) / chunk) < num_sms()) chunk /= 2;
+  SLU_REQUIRE((size_t)n * chunk * sizeof(T) <= 96 * 1024, "trsm block too large");
+  size_t sm = (size_t)n * chunk * sizeof(T);
+  auto kern = trsm_upper_kernel<T>;
+  if (sm > 48 * 1024)
+    SLU_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  dim3 grid((nrhs + chunk - 1) / chunk, batch);
+  kern<<<grid, 256, sm, st>>>(trans, n, R, rRs, rCs, sR, X, xRs, xCs, sX, nrhs, chunk);
+  check_launch("trsm_upper_kernel");
+}
+template void trsm_upper<double>(cudaStream_t, bool, int, const double*, long long, long long,
+                                 long long, double*, long long, long long, long long, int, int);
+template void trsm_upper<float>(cudaStream_t, bool, int, const float*, long long, long long,
+                                long long, float*, long long, long long, long long, int, int);
+
+// ============================================================== LU (getrf)
+namespace {
+__device__ inline void argmax_abs_block(double v, int idx, double* sv, int* si, double& out_v,
+                                        int& out_i) {
+  // warp reduce
+  for (int o = 16; o > 0; o >>= 1) {
+    double ov = __shfl_down_sync(0xffffffffu, v, o);
+    int oi = __shfl_down_sync(0xffffffffu, idx, o);
+    if (ov > v || (ov == v && oi < idx)) { v = ov; idx = oi; }
+  }
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) { sv[w] = v; si[w] = idx; }
+  __syncthreads();
+  if (w == 0) {
+    int nw = (blockDim.x + 31) >> 5;
+    v = lane < nw ? sv[lane] : -1.0;
+    idx = lane < nw ? si[lane] : 0x7fffffff;
+    for (int o = 16; o > 0; o >>= 1) {
+      double ov = __shfl_down_sync(0xffffffffu, v, o);
+      int oi = __shfl_down_sync(0xffffffffu, idx, o);
+      if (ov > v || (ov == v && oi < idx)) { v = ov; idx = oi; }
+    }
+    if (lane == 0) { sv[0] = v; si[0] = idx; }
+  }
+  __syncthreads();
+  out_v = sv[0];
+  out_i = si[0];
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(1024)
+lu_kernel(int n, double* __restrict__ A, int lda, long long sA, int* __restrict__ piv,
+          long long sP, int* info) {
+  A += blockIdx.x * sA;
+  piv += blockIdx.x * sP;
+  __shared__ double sv[32];
+  __shared__ int si[32];
+  int first_zero = 0;
+  for (int j = 0; j < n; ++j) {
+    double best = -1.0;
+    int bi = j;
+    for (int i = j + threadIdx.x; i < n; i += blockDim.x) {
+      double v = fabs(A[(long long)i * lda + j]);
+      if (v > best) { best = v; bi = i; }
+    }
+    double pv;
+    int p;
+    argmax_abs_block(best, bi, sv, si, pv, p);
+    if (threadIdx.x == 0) piv[j] = p;
+    if (p != j) {
+      for (int c = threadIdx.x; c < n; c += blockDim.x) {
+        double t = A[(long long)j * lda + c];
+        A[(long long)j * lda + c] = A[(long long)p * lda + c];
+        A[(long long)p * lda + c] = t;
+      }
+    }
+    __syncthreads();
+    double d = A[(long long)j * lda + j];
+    if (d == 0.0) {
+      if (!first_zero) first_zero = j + 1;
+      __syncthreads();
+      continue;
+    }
+    double inv = 1.0 / d;
+    for (int i = j + 1 + threadIdx.x; i < n; i += blockDim.x) A[(long long)i * lda + j] *= inv;
+    __syncthreads();
+    int m = n - j - 1;
+    for (long long e = threadIdx.x; e < (long long)m * m; e += blockDim.x) {
+      int i = j + 1 + (int)(e / m), c = j + 1 + (int)(e % m);
+      A[(long long)i * lda + c] -= A[(long long)i * lda + j] * A[(long long)j * lda + c];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && first_zero && info) atomicCAS(info + blockIdx.x, 0, first_zero);
+}
+
+template <typename T>
+__global__ void lu_solve_kernel(bool trans, int n, const T* __restrict__ LU, int lda,
+                                long long sA, const int* __restrict__ piv, long long sP,
+                                T* __restrict__ X, int ldx, long long sX, int nrhs, int chunk) {
+  const int b = blockIdx.y;
+  LU += b * sA;
+  piv += b * sP;
+  X += b * sX;
+  const int c0 = blockIdx.x * chunk;
+  const int nc = min(chunk, nrhs - c0);
+  if (nc <= 0) return;
+  extern __shared__ unsigned char smraw[];
+  T* xs = reinterpret_cast<T*>(smraw);
+  for (int e = threadIdx.x; e < n * nc; e += blockDim.x) {
+    int i = e / nc, c = e % nc;
+    xs[e] = X[(long long)i * ldx + c0 + c];
+  }
+  __syncthreads();
+  if (!trans) {
+    // P: apply swaps in order
+    for (int i = 0; i < n; ++i) {
+      int p = piv[i];
+      if (p != i)
+        for (int c = threadIdx.x; c < nc; c += blockDim.x) {
+          T t = xs[i * nc + c]; xs[i * nc + c] = xs[p * nc + c]; xs[p * nc + c] = t;
+        }
+      __syncthreads();
+    }
+    // L (unit lower)
+    for (int i = 0; i < n; ++i) {
+      int rem = (n - i - 1) * nc;
+      for (int e = threadIdx.x; e < rem; e += blockDim.x) {
+        int r = i + 1 + e / nc, c = e % nc;
+        xs[r * nc + c] -= LU[(long long)r * lda + i] * xs[i * nc + c];
+      }
+      __syncthreads();
+    }
+    // U
+    for (int i = n - 1; i >= 0; --i) {
+      T d = LU[(long long)i * lda + i];
+      for (int c = threadIdx.x; c < nc; c += blockDim.x) xs[i * nc + c] /= d;
+      __syncthreads();
+      for (int e = threadIdx.x; e < i * nc; e += blockDim.x) {
+        int r = e / nc, c = e % nc;
+        xs[e] -= LU[(long long)r * lda + i] * xs[i * nc + c];
+      }
+      __syncthreads();
+    }
+  } else {
+    // U^T (lower)
+    for (int i = 0; i < n; ++i) {
+      T d = LU[(long long)i * lda + i];
+      for (int c = threadIdx.x; c < nc; c += blockDim.x) xs[i * nc + c] /= d;
+      __syncthreads();
+      int rem = (n - i - 1) * nc;
+      for (int e = threadIdx.x; e < rem; e += blockDim.x) {
+        int r = i + 1 + e / nc, c = e % nc;
+        xs[r * nc + c] -= LU[(long long)i * lda + r] * xs[i * nc + c];
+      }
+      __syncthreads();
+    }
+    // L^T (unit upper)
+    for (int i = n - 1; i >= 0; --i) {
+      for (int e = threadIdx.x; e < i * nc; e += blockDim.x) {
+        int r = e / nc, c = e % nc;
+        xs[e] -= LU[(long long)i * lda + r] * xs[i * nc + c];
+      }
+      __syncthreads();
+    }
+    // P^T: swaps in reverse order
+    for (int i = n - 1; i >= 0; --i) {
+      int p = piv[i];
+      if (p != i)
+        for (int c = threadIdx.x; c < nc; c += blockDim.x) {
+          T t = xs[i * nc + c]; xs[i * nc + c] = xs[p * nc + c]; xs[p * nc + c] = t;
+        }
+      __syncthreads();
+    }
+  }
+  for (int e = threadIdx.x; e < n * nc; e += blockDim.x) {
+    int i = e / nc, c = e % nc;
+    X[(long long)i * ldx + c0 + c] = xs[e];
+  }
+}
+}  // namespace
+
+void lu_factor(cudaStream_t st, int n, double* A, int lda, long long sA, int* piv, long long sP,
+               int batch, int* info) {
+  if (n <= 0 || batch <= 0) return;
+  lu_kernel<<<batch, 1024, 0, st>>>(n, A, lda, sA, piv, sP, info);
+  check_launch("lu_kernel");
+}
+
+template <typename T>
+void lu_solve(cudaStream_t st, bool trans, int n, const T* LU, int lda, long long sA,
+              const int* piv, long long sP, T* X, int ldx, long long sX, int nrhs, int batch) {
+  if (n <= 0 || nrhs <= 0 || batch <= 0) return;
+  int chunk = nrhs;
+  while ((size_t)n * chunk * sizeof(T) > 96 * 1024 && chunk > 1) chunk = (chunk + 1) / 2;
+  // spread wide right-hand sides over several CTAs
+  while (chunk > 16 && (long long)batch * ((nrhs + chunk - 1) / chunk) < num_sms()) chunk /= 2;
+  size_t sm = (size_t)n * chunk * sizeof(T);
+  SLU_REQUIRE(sm <= 96 * 1024, "lu_solve block too large");
+  auto kern = lu_solve_kernel<T>;
+  if (sm > 48 * 1024)
+    SLU_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  dim3 grid((nrhs + chunk - 1) / chunk, batch);
+  kern<<<grid, 256, sm, st>>>(trans, n, LU, lda, sA, piv, sP, X, ldx, sX, nrhs, chunk);
+  check_launch("lu_solve_kernel");
+}
+template void lu_solve<double>(cudaStream_t, bool, int, const double*, int, long long, const int*,
+                               long long, double*, int, long long, int, int);
+template void lu_solve<float>(cudaStream_t, bool, int, const float*, int, long long, const int*,
+                              long long, float*, int, long long, int, int);
+
+// ============================================================== permutations etc.
+namespace {
+template <typename T>
+__global__ void permute_rows_kernel(bool scatter, int n, int ncol, const int64_t* __restrict__ perm,
+                                    const T* __restrict__ src, int lds, T* __restrict__ dst,
+                                    int ldd) {
+  long long total = (long long)n * ncol;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    int i = (int)(e / ncol), c = (int)(e % ncol);
+    long long p = perm[i];
+    if (scatter) dst[p * ldd + c] = src[(long long)i * lds + c];
+    else dst[(long long)i * ldd + c] = src[p * lds + c];
+  }
+}
+template <typename T>
+__global__ void axpby_kernel(long long n, T a, const T* __restrict__ x, T b, T* __restrict__ y) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+       e += (long long)gridDim.x * blockDim.x)
+    y[e] = (b == T(0)) ? a * x[e] : fma(a, x[e], b * y[e]);
+}
+__global__ void cast64_32(long long n, const double* __restrict__ x, float* __restrict__ y) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+       e += (long long)gridDim.x * blockDim.x)
+    y[e] = (float)x[e];
+}
+__global__ void cast32_64(long long n, const float* __restrict__ x, double* __restrict__ y) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+       e += (long long)gridDim.x * blockDim.x)
+    y[e] = (double)x[e];
+}
+inline int grid_for(long long n) {
+  long long g = (n + 255) / 256;
+  long long cap = 8LL * num_sms();
+  return (int)(g < 1 ? 1 : (g > cap ? cap : g));
+}
+}  // namespace
+
+template <typename T>
+void permute_rows(cudaStream_t st, bool scatter, int n, int ncol, const int64_t* perm,
+                  const T* src, int lds, T* dst, int ldd) {
+  if (n <= 0 || ncol <= 0) return;
+  permute_rows_kernel<T><<<grid_for((long long)n * ncol), 256, 0, st>>>(scatter, n, ncol, perm,
+                                                                        src, lds, dst, ldd);
+  check_launch("permute_rows_kernel");
+}
+template void permute_rows<double>(cudaStream_t, bool, int, int, const int64_t*, const double*,
+                                   int, double*, int);
+template void permute_rows<float>(cudaStream_t, bool, int, int, const int64_t*, const float*, int,
+                                  float*, int);
+
+template <typename T>
+void axpby(cudaStream_t st, long long n, T a, const T* x, T b, T* y) {
+  if (n <= 0) return;
+  axpby_kernel<T><<<grid_for(n), 256, 0, st>>>(n, a, x, b, y);
+  check_launch("axpby_kernel");
+}
+template void axpby<double>(cudaStream_t, long long, double, const double*, double, double*);
+template void axpby<float>(cudaStream_t, long long, float, const float*, float, float*);
+
+void cast_f64_f32(cudaStream_t st, long long n, const double* x, float* y) {
+  if (n <= 0) return;
+  cast64_32<<<grid_for(n), 256, 0, st>>>(n, x, y);
+  check_launch("cast64_32");
+}
+void cast_f32_f64(cudaStream_t st, long long n, const float* x, double* y) {
+  if (n <= 0) return;
+  cast32_64<<<grid_for(n), 256, 0, st>>>(n, x, y);
+  check_launch("cast32_64");
+}
+void copy2d(cudaStream_t st, int rows, int cols, const double* src, int lds, double* dst,
+            int ldd) {
+  if (rows <= 0 || cols <= 0) return;
+  SLU_CHECK_CUDA(cudaMemcpy2DAsync(dst, sizeof(double) * ldd, src, sizeof(double) * lds,
+                                   sizeof(double) * cols, rows, cudaMemcpyDeviceToDevice, st));
+}
+
+// ============================================================== layout helpers
+namespace {
+__global__ void transpose_kernel(int rows, int cols, const double* __restrict__ src, int lds,
+                                 long long sS0, long long sS1, double* __restrict__ dst, int ldd,
+                                 long long sD0, long long sD1, int batch0) {
+  __shared__ double tile[32][33];
+  const int b = blockIdx.z, b0 = b % batch0, b1 = b / batch0;
+  src += b0 * sS0 + b1 * sS1;
+  dst += b0 * sD0 + b1 * sD1;
+  const int i0 = blockIdx.y * 32, j0 = blockIdx.x * 32;
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    int i = i0 + r, j = j0 + threadIdx.x;
+    if (i < rows && j < cols) tile[r][threadIdx.x] = src[(long long)i * lds + j];
+  }
+  __syncthreads();
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    int j = j0 + r, i = i0 + threadIdx.x;
+    if (i < rows && j < cols) dst[(long long)j * ldd + i] = tile[threadIdx.x][r];
+  }
+}
+template <typename T>
+__global__ void add_kernel(int rows, int cols, T alpha, const T* __restrict__ A, int lda,
+                           long long sA0, long long sA1, T* __restrict__ C, int ldc, long long sC0,
+                           long long sC1, int batch0) {
+  const int b = blockIdx.y, b0 = b % batch0, b1 = b / batch0;
+  A += b0 * sA0 + b1 * sA1;
+  C += b0 * sC0 + b1 * sC1;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < rows * cols; e += gridDim.x * blockDim.x) {
+    int i = e / cols, j = e % cols;
+    C[(long long)i * ldc + j] += alpha * A[(long long)i * lda + j];
+  }
+}
+template <typename T>
+__global__ void copyb_kernel(int rows, int cols, const T* __restrict__ A, int lda, long long sA0,
+                             long long sA1, T* __restrict__ C, int ldc, long long sC0,
+                             long long sC1, int batch0) {
+  const int b = blockIdx.y, b0 = b % batch0, b1 = b / batch0;
+  A += b0 * sA0 + b1 * sA1;
+  C += b0 * sC0 + b1 * sC1;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < rows * cols; e += gridDim.x * blockDim.x) {
+    int i = e / cols, j = e % cols;
+    C[(long long)i * ldc + j] = A[(long long)i * lda + j];
+  }
+}
+__global__ void identity_cols_kernel(int m, int c0, int nc, double* __restrict__ C, long long sC) {
+  C += blockIdx.y * sC;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < m * nc; e += gridDim.x * blockDim.x) {
+    int c = e / m, i = e % m;
+    C[e] = (i == c0 + c) ? 1.0 : 0.0;
+  }
+}
+__global__ void extract_upper_kernel(int r0, int nr, int c0, int nc, const double* __restrict__ src,
+                                     int lds, long long sS, double* __restrict__ dst, int ldd,
+                                     long long sD) {
+  src += blockIdx.y * sS;
+  dst += blockIdx.y * sD;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nr * nc; e += gridDim.x * blockDim.x) {
+    int r = e / nc, c = e % nc;
+    int i = r0 + r, j = c0 + c;
+    dst[(long long)r * ldd + c] = (i <= j) ? src[(long long)j * lds + i] : 0.0;
+  }
+}
+inline int blocks_for(long long n, int cap) {
+  long long g = (n + 255) / 256;
+  return (int)(g < 1 ? 1 : (g > cap ? cap : g));
+}
+}  // namespace
+
+void transpose_batched(cudaStream_t st, int rows, int cols, const double* src, int lds,
+                       long long sS0, long long sS1, double* dst, int ldd, long long sD0,
+                       long long sD1, int batch0, int batch1) {
+  if (rows <= 0 || cols <= 0 || batch0 <= 0 || batch1 <= 0) return;
+  dim3 grid((cols + 31) / 32, (rows + 31) / 32, batch0 * batch1);
+  transpose_kernel<<<grid, dim3(32, 8), 0, st>>>(rows, cols, src, lds, sS0, sS1, dst, ldd, sD0,
+                                                  sD1, batch0);
+  check_launch("transpose_kernel");
+}
+
+template <typename T>
+void add_batched(cudaStream_t st, int rows, int cols, T alpha, const T* A, int lda, long long sA0,
+                 long long sA1, T* C, int ldc, long long sC0, long long sC1, int batch0,
+                 int batch1) {
+  if (rows <= 0 || cols <= 0 || batch0 <= 0 || batch1 <= 0) return;
+  dim3 grid(blocks_for((long long)rows * cols, 64), batch0 * batch1);
+  add_kernel<T><<<grid, 256, 0, st>>>(rows, cols, alpha, A, lda, sA0, sA1, C, ldc, sC0, sC1,
+                                      batch0);
+  check_launch("add_kernel");
+}
+template void add_batched<double>(cudaStream_t, int, int, double, const double*, int, long long,
+                                  long long, double*, int, long long, long long, int, int);
+template void add_batched<float>(cudaStream_t, int, int, float, const float*, int, long long,
+                                 long long, float*, int, long long, long long, int, int);
+
+template <typename T>
+void copy_batched(cudaStream_t st, int rows, int cols, const T* A, int lda, long long sA0,
+                  long long sA1, T* C, int ldc, long long sC0, long long sC1, int batch0,
+                  int batch1) {
+  if (rows <= 0 || cols <= 0 || batch0 <= 0 || batch1 <= 0) return;
+  dim3 grid(blocks_for((long long)rows * cols, 64), batch0 * batch1);
+  copyb_kernel<T><<<grid, 256, 0, st>>>(rows, cols, A, lda, sA0, sA1, C, ldc, sC0, sC1, batch0);
+  check_launch("copyb_kernel");
+}
+template void copy_batched<double>(cudaStream_t, int, int, const double*, int, long long,
+                                   long long, double*, int, long long, long long, int, int);
+template void copy_batched<float>(cudaStream_t, int, int, const float*, int, long long, long long,
+                                  float*, int, long long, long long, int, int);
+
+void identity_cols(cudaStream_t st, int m, int c0, int nc, double* C, long long sC, int batch) {
+  if (m <= 0 || nc <= 0 || batch <= 0) return;
+  dim3 grid(blocks_for((long long)m * nc, 64), batch);
+  identity_cols_kernel<<<grid, 256, 0, st>>>(m, c0, nc, C, sC);
+  check_launch("identity_cols_kernel");
+}
+
+void extract_upper(cudaStream_t st, int r0, int nr, int c0, int nc, const double* src, int lds,
+                   long long sS, double* dst, int ldd, long long sD, int batch) {
+  if (nr <= 0 || nc <= 0 || batch <= 0) return;
+  dim3 grid(blocks_for((long long)nr * nc, 64), batch);
+  extract_upper_kernel<<<grid, 256, 0, st>>>(r0, nr, c0, nc, src, lds, sS, dst, ldd, sD);
+  check_launch("extract_upper_kernel");
+}
+
+void copy_blocks(cudaStream_t st, int nblk, long long width, const void* src, long long spitch,
+                 void* dst, long long dpitch) {
+  if (nblk <= 0 || width <= 0) return;
+  SLU_CHECK_CUDA(cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, nblk,
+                                   cudaMemcpyDeviceToDevice, st));
+}
+
+}  // namespace slu

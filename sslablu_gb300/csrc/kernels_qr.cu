@@ -1,0 +1,299 @@
+// Householder QR panels, reflector application and one-sided Jacobi SVD.
+//
+// These implement the per-block LAPACK work of the HBS compression and ULV
+// factorisation:
+//   * complete QR of each sketch block Om_blk^T and the projection of Y onto
+//     the trailing columns of Q (matAssembly/HBS/HBSnew.py:20-28 compute_UV),
+//     which also yields Y*Q_1 and R for the right pseudo-inverse solves of
+//     construct_D / block_solve_r (HBSnew.py:11-19, 48-62);
+//   * the SVD whose leading left singular vectors become U (HBSnew.py:27);
+//   * complete QR of V (W1, ULVsparse.py:18-25) and square QR of D*W
+//     (ULVsparse.py:51-61).
+// Reflectors follow the LAPACK geqrf convention (beta = -sign(alpha)*norm,
+// v[0] = 1), so the trailing columns of Q match LAPACK's to rounding.
+#include "slablu_internal.cuh"
+
+namespace slu {
+namespace {
+
+__device__ inline double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ inline double block_sum(double v, double* red) {
+  v = warp_sum(v);
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  int nw = (blockDim.x + 31) >> 5;
+  double t = 0.0;
+  for (int i = 0; i < nw; ++i) t += red[i];
+  return t;
+}
+
+// QR of the first nfac columns of an m x ncol column-major work array `a`
+// (leading dimension lda), applying each reflector to every later column.
+__device__ void panel_qr_dev(int m, int nfac, int ncol, double* a, int lda, double* tau) {
+  __shared__ double red[32];
+  __shared__ double s_tau, s_scale;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  for (int j = 0; j < nfac && j < m; ++j) {
+    double* col = a + (long long)j * lda;
+    double ss = 0.0;
+    for (int i = j + 1 + threadIdx.x; i < m; i += blockDim.x) ss += col[i] * col[i];
+    ss = block_sum(ss, red);
+    if (threadIdx.x == 0) {
+      double alpha = col[j];
+      if (ss == 0.0) {
+        s_tau = 0.0;
+        s_scale = 0.0;
+      } else {
+        double beta = -copysign(sqrt(alpha * alpha + ss), alpha);
+        s_tau = (beta - alpha) / beta;
+        s_scale = 1.0 / (alpha - beta);
+        col[j] = beta;
+      }
+      tau[j] = s_tau;
+    }
+    __syncthreads();
+    const double t = s_tau, sc = s_scale;
+    if (t != 0.0)
+      for (int i = j + 1 + threadIdx.x; i < m; i += blockDim.x) col[i] *= sc;
+    __syncthreads();
+    if (t != 0.0) {
+      for (int c = j + 1 + warp; c < ncol; c += nwarps) {
+        double* cc = a + (long long)c * lda;
+        double d = (lane == 0) ? cc[j] : 0.0;
+        for (int i = j + 1 + lane; i < m; i += 32) d += col[i] * cc[i];
+        d = warp_sum(d) * t;
+        if (lane == 0) cc[j] -= d;
+        for (int i = j + 1 + lane; i < m; i += 32) cc[i] -= d * col[i];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(512)
+panel_qr_kernel(int m, int nfac, int ncol, double* __restrict__ W, int ldw, long long sW,
+                double* __restrict__ tau, long long sTau, int use_smem) {
+  extern __shared__ double sm[];
+  double* w = W + blockIdx.x * sW;
+  double* t = tau + blockIdx.x * sTau;
+  if (use_smem) {
+    for (long long e = threadIdx.x; e < (long long)m * ncol; e += blockDim.x) {
+      int c = (int)(e / m), i = (int)(e % m);
+      sm[e] = w[(long long)c * ldw + i];
+    }
+    __syncthreads();
+    panel_qr_dev(m, nfac, ncol, sm, m, t);
+    __syncthreads();
+    for (long long e = threadIdx.x; e < (long long)m * ncol; e += blockDim.x) {
+      int c = (int)(e / m), i = (int)(e % m);
+      w[(long long)c * ldw + i] = sm[e];
+    }
+  } else {
+    panel_qr_dev(m, nfac, ncol, w, ldw, t);
+  }
+}
+
+// C <- Q C (transpose = false) or Q^T C; each warp owns whole columns of C.
+__global__ void __launch_bounds__(256)
+apply_q_kernel(bool transpose, int m, int k, const double* __restrict__ V, int ldv, long long sV,
+               const double* __restrict__ tau, long long sTau, double* __restrict__ C, int ldc,
+               long long sC, int nc) {
+  V += blockIdx.y * sV;
+  tau += blockIdx.y * sTau;
+  C += blockIdx.y * sC;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int c = blockIdx.x * nwarps + warp;
+  if (c >= nc) return;
+  double* cc = C + (long long)c * ldc;
+  for (int s = 0; s < k; ++s) {
+    const int j = transpose ? s : (k - 1 - s);
+    const double t = tau[j];
+    if (t == 0.0) continue;
+    const double* v = V + (long long)j * ldv;
+    double d = (lane == 0) ? cc[j] : 0.0;
+    for (int i = j + 1 + lane; i < m; i += 32) d += v[i] * cc[i];
+    d = warp_sum(d) * t;
+    if (lane == 0) cc[j] -= d;
+    for (int i = j + 1 + lane; i < m; i += 32) cc[i] -= d * v[i];
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------- Jacobi SVD
+// One-sided (Hestenes) Jacobi on the columns of A (m x n), round-robin pair
+// ordering, one warp per column pair.  At convergence the columns are
+// sigma_j u_j; the r largest are normalised and written as U (m x r).
+constexpr int JAC_MAX_SWEEPS = 40;
+
+__global__ void __launch_bounds__(1024)
+jacobi_kernel(int m, int n, const double* __restrict__ A, int lda, long long sA, int r,
+              double* __restrict__ U, int ldu, long long sU, double* __restrict__ sv,
+              long long sS, int* info) {
+  extern __shared__ double sm[];
+  const int np = n + (n & 1);            // even number of columns (a zero pad column)
+  double* a = sm;                        // m x np, column-major, ld = m
+  double* nrm = a + (long long)m * np;   // np
+  int* order = reinterpret_cast<int*>(nrm + np);   // np
+  __shared__ int s_rot;
+  A += blockIdx.x * sA;
+  for (long long e = threadIdx.x; e < (long long)m * np; e += blockDim.x) {
+    int c = (int)(e / m), i = (int)(e % m);
+    a[e] = (c < n) ? A[(long long)i * lda + c] : 0.0;   // A row-major
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const double tol = 2.220446049250313e-16 * (double)m;
+  int sweep = 0;
+  for (; sweep < JAC_MAX_SWEEPS; ++sweep) {
+    if (threadIdx.x == 0) s_rot = 0;
+    __syncthreads();
+    for (int rnd = 0; rnd < np - 1; ++rnd) {
+      for (int pi = warp; pi < np / 2; pi += nwarps) {
+        // circle method: slot 0 fixed, others rotate
+        int s1 = pi, s2 = np - 1 - pi;
+        int p = (s1 == 0) ? 0 : 1 + (s1 - 1 + rnd) % (np - 1);
+        int q = 1 + (s2 - 1 + rnd) % (np - 1);
+        double* ap = a + (long long)p * m;
+        double* aq = a + (long long)q * m;
+        double al = 0.0, be = 0.0, ga = 0.0;
+        for (int i = lane; i < m; i += 32) {
+          double x = ap[i], y = aq[i];
+          al += x * x;
+          be += y * y;
+          ga += x * y;
+        }
+        al = warp_sum(al);
+        be = warp_sum(be);
+        ga = warp_sum(ga);
+        if (ga != 0.0 && fabs(ga) > tol * sqrt(al * be)) {
+          double zeta = (be - al) / (2.0 * ga);
+          double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+          double c = 1.0 / sqrt(1.0 + t * t);
+          double s = c * t;
+          for (int i = lane; i < m; i += 32) {
+            double x = ap[i], y = aq[i];
+            ap[i] = c * x - s * y;
+            aq[i] = s * x + c * y;
+          }
+          if (lane == 0) s_rot = 1;
+        }
+        __syncwarp();
+      }
+      __syncthreads();
+    }
+    __syncthreads();
+    if (!s_rot) break;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && sweep >= JAC_MAX_SWEEPS && info) atomicCAS(info, 0, 1);
+  // column norms
+  for (int c = warp; c < np; c += nwarps) {
+    double s = 0.0;
+    for (int i = lane; i < m; i += 32) s += a[(long long)c * m + i] * a[(long long)c * m + i];
+    s = warp_sum(s);
+    if (lane == 0) nrm[c] = sqrt(s);
+  }
+  __syncthreads();
+  // rank of each column by decreasing norm (ties by index)
+  for (int c = threadIdx.x; c < np; c += blockDim.x) {
+    int rk = 0;
+    double v = nrm[c];
+    for (int o = 0; o < np; ++o) {
+      double w = nrm[o];
+      rk += (w > v) || (w == v && o < c);
+    }
+    order[rk] = c;
+  }
+  __syncthreads();
+  double* Ub = U + blockIdx.x * sU;
+  double* svb = sv ? sv + blockIdx.x * sS : nullptr;
+  const double smax = nrm[order[0]];
+  const double tiny = (smax > 0.0) ? smax * 1e-150 : 1e-300;
+  // normalised leading columns; columns that carry no direction are
+  // completed below by Gram-Schmidt on the unit vectors
+  for (int j = warp; j < r; j += nwarps) {
+    int c = order[j < np ? j : np - 1];
+    double s = nrm[c];
+    if (svb && lane == 0) svb[j] = (j < n) ? s : 0.0;
+    bool ok = (j < n) && s > tiny;
+    for (int i = lane; i < m; i += 32)
+      Ub[(long long)i * ldu + j] = ok ? a[(long long)c * m + i] / s : 0.0;
+  }
+  __syncthreads();
+  // completion (rare: zero or rank-deficient input); serial over columns
+  if (warp == 0) {
+    for (int j = 0; j < r; ++j) {
+      int c = order[j < np ? j : np - 1];
+      bool ok = (j < n) && nrm[c] > tiny;
+      if (ok) continue;
+      for (int e = 0; e < m; ++e) {
+        // candidate e_e, orthogonalise against columns 0..j-1 (twice)
+        for (int i = lane; i < m; i += 32) Ub[(long long)i * ldu + j] = (i == e) ? 1.0 : 0.0;
+        __syncwarp();
+        for (int pass = 0; pass < 2; ++pass)
+          for (int q = 0; q < j; ++q) {
+            double d = 0.0;
+            for (int i = lane; i < m; i += 32) d += Ub[(long long)i * ldu + q] * Ub[(long long)i * ldu + j];
+            d = warp_sum(d);
+            for (int i = lane; i < m; i += 32) Ub[(long long)i * ldu + j] -= d * Ub[(long long)i * ldu + q];
+            __syncwarp();
+          }
+        double s = 0.0;
+        for (int i = lane; i < m; i += 32) s += Ub[(long long)i * ldu + j] * Ub[(long long)i * ldu + j];
+        s = sqrt(warp_sum(s));
+        if (s > 0.5) {
+          for (int i = lane; i < m; i += 32) Ub[(long long)i * ldu + j] /= s;
+          __syncwarp();
+          break;
+        }
+      }
+    }
+  }
+}
+}  // namespace
+
+void panel_qr(cudaStream_t st, int m, int nfac, int ncol, double* W, int ldw, long long sW,
+              double* tau, long long sTau, int batch) {
+  if (batch <= 0 || m <= 0 || nfac <= 0) return;
+  size_t sm = (size_t)m * ncol * sizeof(double);
+  int use_smem = sm <= 200 * 1024;
+  if (!use_smem) sm = 0;
+  if (sm > 48 * 1024)
+    SLU_CHECK_CUDA(cudaFuncSetAttribute(panel_qr_kernel,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  panel_qr_kernel<<<batch, 512, sm, st>>>(m, nfac, ncol, W, ldw, sW, tau, sTau, use_smem);
+  check_launch("panel_qr_kernel");
+}
+
+void apply_q(cudaStream_t st, bool transpose, int m, int k, const double* V, int ldv,
+             long long sV, const double* tau, long long sTau, double* C, int ldc, long long sC,
+             int nc, int batch) {
+  if (batch <= 0 || nc <= 0 || m <= 0) return;
+  dim3 grid((nc + 7) / 8, batch);
+  apply_q_kernel<<<grid, 256, 0, st>>>(transpose, m, k, V, ldv, sV, tau, sTau, C, ldc, sC, nc);
+  check_launch("apply_q_kernel");
+}
+
+void jacobi_left_sv(cudaStream_t st, int m, int n, const double* A, int lda, long long sA, int r,
+                    double* U, int ldu, long long sU, double* sv, long long sS, int batch,
+                    int* info) {
+  if (batch <= 0 || r <= 0) return;
+  SLU_REQUIRE(r <= m, "jacobi: rank larger than rows");
+  int np = n + (n & 1);
+  size_t sm = (size_t)m * np * sizeof(double) + np * sizeof(double) + np * sizeof(int);
+  SLU_REQUIRE(sm <= 220 * 1024, "jacobi: block too large for shared memory");
+  if (sm > 48 * 1024)
+    SLU_CHECK_CUDA(cudaFuncSetAttribute(jacobi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)sm));
+  int threads = 32 * std::min(32, std::max(1, np / 2));
+  jacobi_kernel<<<batch, threads, sm, st>>>(m, n, A, lda, sA, r, U, ldu, sU, sv, sS, info);
+  check_launch("jacobi_kernel");
+}
+
+}  // namespace slu

@@ -1,0 +1,201 @@
+// Dense block-tridiagonal direct solvers on the device.
+//
+//   * red-black cyclic reduction: direct_solve/omsdirectsolve.py:177-333
+//     (RedBlackSolver.factorize / solve / build_block_RB_solver_level)
+//   * block Thomas: direct_solve/omsdirectsolve.py:48-141
+//     (BlockTridiagonalSolver.factorize_helper / solve_helper)
+//
+// Red-black: per level, every odd block o is solved once against the stacked
+// couplings [SiM_o | SiP_o] (one batched LU solve with 2m right-hand sides),
+// then the new diagonal B_i and couplings A_i, C_i of every kept even block i
+// come from two batched GEMMs against those solves:
+//   G1 = SiM_i [T_{i-1}^{-1} SiM_{i-1} | T_{i-1}^{-1} SiP_{i-1}]
+//   G2 = SiP_i [T_{i+1}^{-1} SiM_{i+1} | T_{i+1}^{-1} SiP_{i+1}]
+//   A_i = -G1[:, :m],  B_i = T_i - G1[:, m:] - G2[:, :m],  C_i = -G2[:, m:].
+// Upstream rebuilds each T from its LU factors (omsdirectsolve.py:31-46,314);
+// this keeps T itself, the same matrix up to rounding.
+#include "tridiag.cuh"
+
+#include <algorithm>
+
+namespace slu {
+namespace {
+inline double* dp(const DevBuf& b) { return b.as<double>(); }
+inline int* ip(const DevBuf& b) { return b.as<int>(); }
+}  // namespace
+
+void rb_factor(Handle& h, RbSolver& S, int nblk, int m, const double* SiM, const double* SiP,
+               const double* T) {
+  cudaStream_t st = h.stream;
+  SLU_REQUIRE(nblk >= 1 && (nblk & (nblk - 1)) == 0, "red-black needs a power-of-two block count");
+  SLU_REQUIRE(m >= 1, "bad block size");
+  S.m = m;
+  S.nblk = nblk;
+  S.levels.clear();
+  const size_t mm = (size_t)m * m;
+  // level 0: copies, with the boundary couplings zeroed (omsdirectsolve.py:207-209)
+  S.levels.emplace_back();
+  {
+    RbLevel& L0 = S.levels.back();
+    L0.nS = nblk;
+    L0.SiM.alloc(8 * nblk * mm, st);
+    L0.SiP.alloc(8 * nblk * mm, st);
+    L0.T.alloc(8 * nblk * mm, st);
+    L0.LU.alloc(8 * nblk * mm, st);
+    L0.piv.alloc(4 * (size_t)nblk * m, st);
+    SLU_CHECK_CUDA(cudaMemcpyAsync(dp(L0.SiM), SiM, 8 * nblk * mm, cudaMemcpyDeviceToDevice, st));
+    SLU_CHECK_CUDA(cudaMemcpyAsync(dp(L0.SiP), SiP, 8 * nblk * mm, cudaMemcpyDeviceToDevice, st));
+    SLU_CHECK_CUDA(cudaMemsetAsync(dp(L0.SiM), 0, 8 * mm, st));
+    SLU_CHECK_CUDA(cudaMemsetAsync(dp(L0.SiP) + (nblk - 1) * mm, 0, 8 * mm, st));
+    SLU_CHECK_CUDA(cudaMemcpyAsync(dp(L0.T), T, 8 * nblk * mm, cudaMemcpyDeviceToDevice, st));
+    SLU_CHECK_CUDA(cudaMemcpyAsync(dp(L0.LU), T, 8 * nblk * mm, cudaMemcpyDeviceToDevice, st));
+    lu_factor(st, m, dp(L0.LU), m, mm, ip(L0.piv), m, nblk, h.info.as<int>());
+  }
+  h.ws.reserve(8 * ((size_t)nblk / 2 * 2 * mm * 3) + 8 * 256, st);
+  double* X = h.ws.take<double>(std::max<size_t>(1, (size_t)nblk / 2) * 2 * mm);  // per odd block: m x 2m
+  double* G1 = h.ws.take<double>(std::max<size_t>(1, (size_t)nblk / 2) * 2 * mm);
+  double* G2 = h.ws.take<double>(std::max<size_t>(1, (size_t)nblk / 2) * 2 * mm);
+  int l = nblk;
+  while (l > 1) {
+    const RbLevel& P = S.levels.back();
+    const int nR = l / 2;
+    RbLevel N;
+    N.nS = nR;
+    N.SiM.alloc(8 * nR * mm, st);
+    N.SiP.alloc(8 * nR * mm, st);
+    N.T.alloc(8 * nR * mm, st);
+    N.LU.alloc(8 * nR * mm, st);
+    N.piv.alloc(4 * (size_t)nR * m, st);
+    const long long m2 = 2 * (long long)m;
+    // X_o = T_o^{-1} [SiM_o | SiP_o] for odd o
+    copy_batched<double>(st, m, m, dp(P.SiM) + mm, m, 2 * mm, 0, X, (int)m2, 2 * mm, 0, nR);
+    copy_batched<double>(st, m, m, dp(P.SiP) + mm, m, 2 * mm, 0, X + m, (int)m2, 2 * mm, 0, nR);
+    lu_solve<double>(st, false, m, dp(P.LU) + mm, m, 2 * mm, ip(P.piv) + m, 2 * m, X, (int)m2,
+                     2 * mm, (int)m2, nR);
+    // G1_j = SiM_{2j} X_{2j-1} (j >= 1; SiM_0 is zero), G2_j = SiP_{2j} X_{2j+1}
+    if (nR > 1)
+      gemm_batched<double>(st, false, false, m, (int)m2, m, 1.0, dp(P.SiM) + 2 * mm, m, 2 * mm, 0,
+                           X, (int)m2, 2 * mm, 0, 0.0, G1 + 2 * mm, (int)m2, 2 * mm, 0, nR - 1);
+    SLU_CHECK_CUDA(cudaMemsetAsync(G1, 0, 8 * 2 * mm, st));
+    gemm_batched<double>(st, false, false, m, (int)m2, m, 1.0, dp(P.SiP), m, 2 * mm, 0, X, (int)m2,
+                         2 * mm, 0, 0.0, G2, (int)m2, 2 * mm, 0, nR);
+    // A = -G1[:, :m]; C = -G2[:, m:]; B = T_even - G1[:, m:] - G2[:, :m]
+    copy_batched<double>(st, m, m, dp(P.T), m, 2 * mm, 0, dp(N.T), m, mm, 0, nR);
+    add_batched<double>(st, m, m, -1.0, G1 + m, (int)m2, 2 * mm, 0, dp(N.T), m, mm, 0, nR);
+    add_batched<double>(st, m, m, -1.0, G2, (int)m2, 2 * mm, 0, dp(N.T), m, mm, 0, nR);
+    SLU_CHECK_CUDA(cudaMemsetAsync(dp(N.SiM), 0, 8 * nR * mm, st));
+    SLU_CHECK_CUDA(cudaMemsetAsync(dp(N.SiP), 0, 8 * nR * mm, st));
+    add_batched<double>(st, m, m, -1.0, G1, (int)m2, 2 * mm, 0, dp(N.SiM), m, mm, 0, nR);
+    add_batched<double>(st, m, m, -1.0, G2 + m, (int)m2, 2 * mm, 0, dp(N.SiP), m, mm, 0, nR);
+    SLU_CHECK_CUDA(cudaMemcpyAsync(dp(N.LU), dp(N.T), 8 * nR * mm, cudaMemcpyDeviceToDevice, st));
+    lu_factor(st, m, dp(N.LU), m, mm, ip(N.piv), m, nR, h.info.as<int>());
+    S.levels.push_back(std::move(N));
+    l = nR;
+  }
+}
+
+void rb_solve(Handle& h, const RbSolver& S, double* B, int ldb, int c) {
+  cudaStream_t st = h.stream;
+  const int m = S.m, nblk = S.nblk;
+  const size_t mm = (size_t)m * m, mc = (size_t)m * c;
+  const int nL = (int)S.levels.size();
+  // v[l]: nS_l * m x c
+  size_t tot = 0;
+  for (const RbLevel& L : S.levels) tot += (size_t)L.nS * mc;
+  h.ws.reserve(8 * (tot + (size_t)nblk / 2 * mc + mc) + 8 * 256, st);
+  std::vector<double*> v(nL);
+  for (int l = 0; l < nL; ++l) v[l] = h.ws.take<double>((size_t)S.levels[l].nS * mc);
+  double* z = h.ws.take<double>(std::max<size_t>(1, (size_t)nblk / 2) * mc);
+  copy_batched<double>(st, nblk * m, c, B, ldb, 0, 0, v[0], c, 0, 0, 1);
+  // forward reduction (omsdirectsolve.py:238-258)
+  for (int l = 0; l + 1 < nL; ++l) {
+    const RbLevel& P = S.levels[l];
+    const int nR = P.nS / 2;
+    // z_o = T_o^{-1} v_o (odd o)
+    copy_batched<double>(st, m, c, v[l] + mc, c, 2 * mc, 0, z, c, mc, 0, nR);
+    lu_solve<double>(st, false, m, dp(P.LU) + mm, m, 2 * mm, ip(P.piv) + m, 2 * m, z, c, mc, c, nR);
+    // v'_j = v_{2j} - SiM_{2j} z_{2j-1} - SiP_{2j} z_{2j+1}
+    copy_batched<double>(st, m, c, v[l], c, 2 * mc, 0, v[l + 1], c, mc, 0, nR);
+    if (nR > 1)
+      gemm_batched<double>(st, false, false, m, c, m, -1.0, dp(P.SiM) + 2 * mm, m, 2 * mm, 0, z, c,
+                           mc, 0, 1.0, v[l + 1] + mc, c, mc, 0, nR - 1);
+    gemm_batched<double>(st, false, false, m, c, m, -1.0, dp(P.SiP), m, 2 * mm, 0, z, c, mc, 0,
+                         1.0, v[l + 1], c, mc, 0, nR);
+  }
+  // coarsest block (omsdirectsolve.py:261)
+  lu_solve<double>(st, false, m, dp(S.levels[nL - 1].LU), m, 0, ip(S.levels[nL - 1].piv), 0,
+                   v[nL - 1], c, 0, c, 1);
+  // back substitution (omsdirectsolve.py:263-277)
+  for (int l = nL - 1; l > 0; --l) {
+    const RbLevel& P = S.levels[l - 1];
+    const int nR = P.nS / 2;
+    // odd blocks first use the coarse (even) solution still stored in v[l]
+    // g_o = v_o - SiM_o x_{o-1} - SiP_o x_{o+1}
+    gemm_batched<double>(st, false, false, m, c, m, -1.0, dp(P.SiM) + mm, m, 2 * mm, 0, v[l], c, mc,
+                         0, 1.0, v[l - 1] + mc, c, 2 * mc, 0, nR);
+    if (nR > 1)
+      gemm_batched<double>(st, false, false, m, c, m, -1.0, dp(P.SiP) + mm, m, 2 * mm, 0,
+                           v[l] + mc, c, mc, 0, 1.0, v[l - 1] + mc, c, 2 * mc, 0, nR - 1);
+    lu_solve<double>(st, false, m, dp(P.LU) + mm, m, 2 * mm, ip(P.piv) + m, 2 * m, v[l - 1] + mc,
+                     c, 2 * mc, c, nR);
+    copy_batched<double>(st, m, c, v[l], c, mc, 0, v[l - 1], c, 2 * mc, 0, nR);
+  }
+  copy_batched<double>(st, nblk * m, c, v[0], c, 0, 0, B, ldb, 0, 0, 1);
+}
+
+// ---------------------------------------------------------------- Thomas
+void thomas_factor(Handle& h, RbSolver& S, int nblk, int m, const double* SiM, const double* SiP,
+                   const double* T) {
+  cudaStream_t st = h.stream;
+  SLU_REQUIRE(nblk >= 1 && m >= 1, "bad block-tridiagonal geometry");
+  S.m = m;
+  S.nblk = nblk;
+  S.levels.clear();
+  S.levels.emplace_back();
+  RbLevel& L = S.levels.back();
+  const size_t mm = (size_t)m * m;
+  L.nS = nblk;
+  L.SiM.alloc(8 * nblk * mm, st);  // holds A_i^T = (SiM_i B_{i-1}^{-1})^T
+  L.SiP.alloc(8 * nblk * mm, st);  // C_i
+  L.LU.alloc(8 * nblk * mm, st);   // LU(B_i)
+  L.piv.alloc(4 * (size_t)nblk * m, st);
+  SLU_CHECK_CUDA(cudaMemcpyAsync(dp(L.SiP), SiP, 8 * nblk * mm, cudaMemcpyDeviceToDevice, st));
+  SLU_CHECK_CUDA(cudaMemcpyAsync(dp(L.LU), T, 8 * nblk * mm, cudaMemcpyDeviceToDevice, st));
+  lu_factor(st, m, dp(L.LU), m, mm, ip(L.piv), m, 1, h.info.as<int>());
+  for (int i = 1; i < nblk; ++i) {
+    double* At = dp(L.SiM) + i * mm;
+    // A_i = SiM_i B_{i-1}^{-1}  ->  A_i^T = B_{i-1}^{-T} SiM_i^T  (omsdirectsolve.py:89-91)
+    transpose_batched(st, m, m, SiM + i * mm, m, 0, 0, At, m, 0, 0, 1);
+    lu_solve<double>(st, true, m, dp(L.LU) + (i - 1) * mm, m, 0, ip(L.piv) + (i - 1) * m, 0, At,
+                     m, 0, m, 1);
+    // B_i = T_i - A_i C_{i-1}  (omsdirectsolve.py:94), then LU
+    double* Bi = dp(L.LU) + i * mm;
+    gemm_batched<double>(st, true, false, m, m, m, -1.0, At, m, 0, 0, dp(L.SiP) + (i - 1) * mm, m,
+                         0, 0, 1.0, Bi, m, 0, 0, 1);
+    lu_factor(st, m, Bi, m, 0, ip(L.piv) + i * m, 0, 1, h.info.as<int>());
+  }
+}
+
+void thomas_solve(Handle& h, const RbSolver& S, double* B, int ldb, int c) {
+  cudaStream_t st = h.stream;
+  const int m = S.m, n = S.nblk;
+  const size_t mm = (size_t)m * m;
+  const RbLevel& L = S.levels[0];
+  // d_i -= A_i d_{i-1}  (omsdirectsolve.py:125-126)
+  for (int i = 1; i < n; ++i)
+    gemm_batched<double>(st, true, false, m, c, m, -1.0, dp(L.SiM) + i * mm, m, 0, 0,
+                         B + (size_t)(i - 1) * m * ldb, ldb, 0, 0, 1.0, B + (size_t)i * m * ldb,
+                         ldb, 0, 0, 1);
+  // x_n = B_n^{-1} d_n; x_i = B_i^{-1}(d_i - C_i x_{i+1})  (131-139)
+  lu_solve<double>(st, false, m, dp(L.LU) + (n - 1) * mm, m, 0, ip(L.piv) + (n - 1) * m, 0,
+                   B + (size_t)(n - 1) * m * ldb, ldb, 0, c, 1);
+  for (int i = n - 2; i >= 0; --i) {
+    gemm_batched<double>(st, false, false, m, c, m, -1.0, dp(L.SiP) + i * mm, m, 0, 0,
+                         B + (size_t)(i + 1) * m * ldb, ldb, 0, 0, 1.0, B + (size_t)i * m * ldb,
+                         ldb, 0, 0, 1);
+    lu_solve<double>(st, false, m, dp(L.LU) + i * mm, m, 0, ip(L.piv) + i * m, 0,
+                     B + (size_t)i * m * ldb, ldb, 0, c, 1);
+  }
+}
+
+}  // namespace slu

@@ -1,0 +1,24 @@
+// Dense block-tridiagonal solvers (red-black cyclic reduction, block Thomas).
+#pragma once
+#include "hbs.cuh"
+
+namespace slu {
+
+struct RbLevel {
+  int nS = 0;                      // blocks on this level
+  DevBuf SiM, SiP, T, LU, piv;     // nS m x m blocks each (piv: nS*m int32)
+};
+
+struct RbSolver {
+  int m = 0, nblk = 0;
+  std::vector<RbLevel> levels;     // levels[0] = the input system
+};
+
+void rb_factor(Handle& h, RbSolver& S, int nblk, int m, const double* SiM, const double* SiP,
+               const double* T);
+void rb_solve(Handle& h, const RbSolver& S, double* B, int ldb, int nrhs);
+void thomas_factor(Handle& h, RbSolver& S, int nblk, int m, const double* SiM, const double* SiP,
+                   const double* T);
+void thomas_solve(Handle& h, const RbSolver& S, double* B, int ldb, int nrhs);
+
+}  // namespace slu

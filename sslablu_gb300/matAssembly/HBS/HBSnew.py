@@ -1,0 +1,333 @@
+"""HBSMAT on the GPU -- drop-in for SslabLU matAssembly/HBS/HBSnew.py.
+
+Same constructor, methods, attributes and return shapes as upstream
+HBSnew.HBSMAT (HBSnew.py:65-416).  The operator's factors live on the device
+inside libslablu; the upstream list attributes (Umats, Vmats, Dmats, Qlist,
+Wlist, Rlist, Uulist) are exported to numpy on first access.
+
+Sampling follows upstream exactly (HBSnew.py:211-227): the Gaussian sketches
+are drawn from numpy's global RNG (Om then Psi, shape (N, s) with
+s = 6rk+4nl+5 for quad trees and 4rk+2nl+5 for binary ones), so a seeded run
+reproduces upstream's sketches; ``A.matmat`` / ``A.rmatmat`` of a device
+operator run on the device, a caller's host LinearOperator is evaluated where
+it lives.
+"""
+import ctypes
+import time
+
+import numpy as np
+import torch
+
+from ... import _dev as dv
+from ... import _lib as L
+
+
+def samples_for(rk, nl, fac):
+    """Sample count of HBSnew.py:213-216."""
+    return 6 * rk + 4 * nl + 5 if fac == 4 else 4 * rk + 2 * nl + 5
+
+
+class HBSMAT:
+    """HBS matrix (weak admissibility) with randomized construction and ULV solve."""
+
+    def __init__(self, A=None, tree=None, quad=True):
+        self.mode = "N"
+        self._op = None
+        self._cache = {}
+        self.Nbvec = []
+        self.NNvec = None
+        self.quad = quad
+        self.fac = 4 if quad else 2
+        self.blockSolveTime = 0
+        self.nullTime = 0
+        self.setupTime = 0
+        self.DTime = 0
+        self.tSample = 0
+        self.tConstruct = 0
+        if A is not None:
+            self.A = A
+            self.shape = tuple(A.shape)
+            self.dtype = getattr(A, "dtype", np.float64)
+        if tree is not None:
+            self.perm = np.asarray(tree.perm_leaf, dtype=np.int64)
+            self.Nb = int(tree.nleaves)
+            self.nl = self.A.shape[0] // self.Nb
+            self.L = int(tree.nlevels)
+            self.tree = tree
+
+    # ------------------------------------------------------------ set-up
+    def set_Nbvec(self, Nbvec):
+        """HBSnew.py:119-124."""
+        self.Nbvec = Nbvec
+        self.Nb = Nbvec[0]
+        self.nl = self.A.shape[0] // self.Nb
+        self.L = len(Nbvec)
+        self.perm = np.arange(self.A.shape[0], dtype=np.int64)
+
+    def set_mats(self, Umats, Dmats, Vmats, Nbvec, fac=4):
+        """HBSnew.py:125-133: load given factors (level 0 = leaves)."""
+        N = int(Dmats[0].shape[0])
+        Lv = len(Dmats)
+        self.fac = fac
+        self.quad = fac == 4
+        self.Nb = Nbvec[0]
+        self.Nbvec = list(Nbvec)
+        self.L = Lv
+        self.perm = np.arange(N, dtype=np.int64)
+        self.shape = (N, N)
+        self.dtype = np.float64
+        self._new_op(N, Lv, None)
+        for t in range(Lv):
+            Nb = int(Nbvec[t])
+            D = dv.to_dev(Dmats[t])
+            n = D.shape[0] // Nb
+            if t < Lv - 1:
+                U = dv.to_dev(Umats[t])
+                V = dv.to_dev(Vmats[t])
+                k = U.shape[1]
+            else:
+                U = V = None
+                k = 0
+            L.check(L.lib().slu_hbs_set_level(L.handle(), self._op, t, Nb, n, k, L.ptr(U),
+                                              L.ptr(V), L.ptr(D)))
+        L.sync()
+        self._refresh()
+        return self
+
+    def _new_op(self, N, Lv, perm):
+        self._free()
+        out = ctypes.c_void_p()
+        p = None if perm is None else L.i64(perm)
+        L.check(L.lib().slu_hbs_create(L.handle(), int(N), int(Lv), int(self.fac),
+                                       None if p is None else L.host_ptr(p), ctypes.byref(out)))
+        self._op = out
+        self._perm_keep = p
+
+    def _free(self):
+        if getattr(self, "_op", None) is not None and L._lib is not None:
+            L.lib().slu_hbs_destroy(self._op)
+        self._op = None
+        self._cache = {}
+
+    def __del__(self):
+        try:
+            if getattr(self, "_owner", True):
+                self._free()
+        except Exception:
+            pass
+
+    @property
+    def T(self):
+        """HBSnew.py:134-139: transposed view sharing the factors."""
+        view = object.__new__(self.__class__)
+        view.__dict__ = self.__dict__.copy()
+        view._owner = False
+        view.mode = "T"
+        return view
+
+    # ------------------------------------------------------------ construction
+    def construct(self, rk, compute_ULV=False):
+        """HBSnew.py:140-145."""
+        if compute_ULV:
+            self.constructHBS_ULV(rk)
+        else:
+            self.constructHBS(rk)
+
+    def _sketches(self, rk, rng=None):
+        s = samples_for(rk, self.nl, self.fac)
+        self.nSamples = s
+        if rng is None:
+            Om = np.random.standard_normal(size=(self.shape[1], s))
+            Psi = np.random.standard_normal(size=(self.shape[0], s))
+        else:
+            Om = rng.standard_normal(size=(self.shape[1], s))
+            Psi = rng.standard_normal(size=(self.shape[0], s))
+        return Om, Psi
+
+    def _sample(self, Om, Psi):
+        """Y = A Om', Z = A^T Psi' with Om'[perm] = Om, rows back in tree order."""
+        perm_d = torch.from_numpy(self.perm).to("cuda")
+        Omd = dv.to_dev(Om)
+        Psid = dv.to_dev(Psi)
+        Omp = torch.empty_like(Omd)
+        Omp[perm_d] = Omd
+        Psip = torch.empty_like(Psid)
+        Psip[perm_d] = Psid
+        Y = dv.dev_apply(self.A, Omp, False)[perm_d].contiguous()
+        Z = dv.dev_apply(self.A, Psip, True)[perm_d].contiguous()
+        return Omd, Psid, Y, Z
+
+    def compress_from_sketches(self, rk, Om, Psi, Y, Z, compute_ULV=True):
+        """Compression from given tree-ordered sketches and samples (N x s
+        arrays); the sampling-free entry of HBStorch.HBSMAT.construct
+        (HBStorch.py:163-168) with HBSnew's algorithm."""
+        tic = time.time()
+        Omd, Psid, Yd, Zd = (dv.to_dev(x) for x in (Om, Psi, Y, Z))
+        s = Omd.shape[1]
+        self.nSamples = s
+        N = self.shape[0]
+        self._new_op(N, self.L, self.perm)
+        L.check(L.lib().slu_hbs_compress(L.handle(), self._op, int(self.Nb), int(rk), int(s),
+                                         L.ptr(Omd), L.ptr(Psid), L.ptr(Yd), L.ptr(Zd),
+                                         int(bool(compute_ULV))))
+        L.sync()
+        self._refresh()
+        self.Nbvec += [int(x) for x in self._levels[:, 0]]
+        self.tCompress = time.time() - tic
+        return self
+
+    def constructHBS(self, rk):
+        """HBSnew.py:147-210 (upstream draws from an unseeded default_rng)."""
+        tic = time.time()
+        Om, Psi = self._sketches(rk, np.random.default_rng())
+        Omd, Psid, Y, Z = self._sample(Om, Psi)
+        self.tSample += time.time() - tic
+        self.compress_from_sketches(rk, Omd, Psid, Y, Z, compute_ULV=False)
+
+    def constructHBS_ULV(self, rk):
+        """HBSnew.py:211-295."""
+        tic = time.time()
+        Om, Psi = self._sketches(rk)
+        Omd, Psid, Y, Z = self._sample(Om, Psi)
+        self.tSample += time.time() - tic
+        self.compress_from_sketches(rk, Omd, Psid, Y, Z, compute_ULV=True)
+
+    def compute_ULV(self):
+        """HBSnew.py:390-391."""
+        L.check(L.lib().slu_ulv_factor(L.handle(), self._op))
+        L.sync()
+        self._refresh()
+
+    # ------------------------------------------------------------ metadata
+    def _refresh(self):
+        self._cache = {}
+        Lv = ctypes.c_int()
+        N = ctypes.c_int()
+        ns = ctypes.c_int()
+        lev = np.zeros(4 * 64, dtype=np.int32)
+        NN = np.zeros(65, dtype=np.int64)
+        L.check(L.lib().slu_hbs_info(self._op, ctypes.byref(Lv), ctypes.byref(N),
+                                     L.host_ptr(lev), L.host_ptr(NN), ctypes.byref(ns)))
+        self.L = Lv.value
+        self._levels = lev[:4 * Lv.value].reshape(Lv.value, 4).astype(np.int64)
+        self.NNvec = NN[:Lv.value + 1].copy()
+
+    def _export(self, what, level):
+        key = (what, level)
+        if key not in self._cache:
+            cnt = ctypes.c_size_t()
+            L.check(L.lib().slu_hbs_export(L.handle(), self._op, what, level, None, 0,
+                                           ctypes.byref(cnt)))
+            buf = torch.empty(cnt.value, dtype=torch.float64, device="cuda")
+            L.check(L.lib().slu_hbs_export(L.handle(), self._op, what, level, L.ptr(buf),
+                                           cnt.value, None))
+            Nb, n, k, nu = (int(x) for x in self._levels[level])
+            cols = {0: k, 1: k, 2: n, 3: n, 4: n, 5: n}.get(what)
+            if what == 6:
+                cols = k if level < self.L - 1 else n
+            arr = dv.to_host(buf)
+            self._cache[key] = arr.reshape(-1, cols) if arr.size else np.zeros((0, cols))
+        return self._cache[key]
+
+    def _lists(self, what, levels):
+        return [self._export(what, t) for t in levels]
+
+    @property
+    def Umats(self):
+        return self._lists(0, range(self.L - 1))
+
+    @property
+    def Vmats(self):
+        return self._lists(1, range(self.L - 1))
+
+    @property
+    def Dmats(self):
+        return self._lists(2, range(self.L))
+
+    @property
+    def Qlist(self):
+        return self._lists(3, range(self.L))
+
+    @property
+    def Wlist(self):
+        return [self._export(4, t) if t < self.L - 1 else None for t in range(self.L)]
+
+    @property
+    def Rlist(self):
+        return self._lists(5, range(self.L))
+
+    @property
+    def Uulist(self):
+        lv = [t for t in range(self.L) if self._export_count(6, t) > 0]
+        return self._lists(6, lv)
+
+    def _export_count(self, what, level):
+        cnt = ctypes.c_size_t()
+        L.check(L.lib().slu_hbs_export(L.handle(), self._op, what, level, None, 0,
+                                       ctypes.byref(cnt)))
+        return cnt.value
+
+    @property
+    def nbytes(self):
+        """HBSnew.py:296-302 (U, V, D bytes)."""
+        out = ctypes.c_size_t()
+        L.check(L.lib().slu_hbs_nbytes(self._op, 0, ctypes.byref(out)))
+        return out.value
+
+    # ------------------------------------------------------------ apply / solve
+    def _dev_apply(self, X, trans=False):
+        X = dv.as_2d(X).contiguous()
+        Y = torch.empty_like(X)
+        L.check(L.lib().slu_hbs_apply(L.handle(), self._op, int(trans), L.ptr(X), X.shape[1],
+                                      L.ptr(Y), Y.shape[1], X.shape[1]))
+        return Y
+
+    def _dev_solve(self, X, trans=False):
+        B = dv.as_2d(X).clone().contiguous()
+        L.check(L.lib().slu_ulv_solve(L.handle(), self._op, L.ptr(B), B.shape[1], B.shape[1],
+                                      int(trans)))
+        return B
+
+    def matvec(self, v):
+        return self.matmat(v)
+
+    def rmatvec(self, v):
+        return self.rmatmat(v)
+
+    def matmat(self, v):
+        """HBSnew.py:308-328."""
+        X, one = dv.prepare_rhs(v)
+        return dv.finish(self._dev_apply(X, False), v, one)
+
+    def rmatmat(self, v):
+        """HBSnew.py:330-350."""
+        X, one = dv.prepare_rhs(v)
+        return dv.finish(self._dev_apply(X, True), v, one)
+
+    def __matmul__(self, v):
+        """HBSnew.py:352-388 (honours the .T view)."""
+        if self.mode not in ("N", "T"):
+            raise ValueError("mode not recognized")
+        X, one = dv.prepare_rhs(v)
+        return dv.finish(self._dev_apply(X, self.mode == "T"), v, one)
+
+    def solve(self, b, mode="N"):
+        """HBSnew.py:393-416."""
+        if mode not in ("N", "T"):
+            raise NotImplementedError("mode not recognized")
+        X, one = dv.prepare_rhs(b)
+        return dv.finish(self._dev_solve(X, mode == "T"), b, one)
+
+    # ------------------------------------------------------------ mixed precision
+    def solve_refined(self, b, tol=1e-10, maxit=10):
+        """Mixed-precision solve: float32 ULV sweeps corrected by float64
+        residuals of this operator until ||b - A x|| / ||b|| <= tol per
+        column.  Returns (x, iterations, worst relative residual)."""
+        B, one = dv.prepare_rhs(b)
+        X = torch.empty_like(B)
+        it = ctypes.c_int()
+        rr = ctypes.c_double()
+        L.check(L.lib().slu_refine(L.handle(), self._op, L.ptr(B), B.shape[1], L.ptr(X),
+                                   X.shape[1], B.shape[1], float(tol), int(maxit),
+                                   ctypes.byref(it), ctypes.byref(rr)))
+        return dv.finish(X, b, one), it.value, rr.value

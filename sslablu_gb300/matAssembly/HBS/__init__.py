@@ -1,0 +1,1 @@
+"""Mirror of the upstream package of the same name."""

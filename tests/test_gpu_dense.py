@@ -1,0 +1,64 @@
+"""Dense red-black and Thomas on the GPU vs upstream golden vectors."""
+import numpy as np
+import pytest
+
+from tests._cases import relerr, test_rb_system
+from tests._gpu import need_gpu
+
+pytestmark = pytest.mark.gpu
+
+
+def test_rb_dense_cases(golden):
+    need_gpu()
+    from sslablu_gb300.direct_solve.omsdirectsolve import BlockTridiagonalSolver, RedBlackSolver
+    g = golden("rb_dense")
+    for nS, m in g["cases"]:
+        S, T, mat, rhs = test_rb_system(int(nS), int(m))
+        key = "%d_%d" % (nS, m)
+        rb = RedBlackSolver(int(m))
+        rb.factorize(S, T)
+        x = rb.solve(rhs)
+        assert x.shape == rhs.shape
+        assert relerr(x, g["x_rb_" + key]) < 1e-12
+        assert relerr(x, g["x_np_" + key]) < 1e-8
+        th = BlockTridiagonalSolver(int(m))
+        th.factorize(S, T)
+        assert relerr(th.solve(rhs), g["x_th_" + key]) < 1e-12
+        # multi-RHS through the same factors
+        X = np.stack([rhs, 2 * rhs], axis=1)
+        assert relerr(rb.solve(X)[:, 1], 2 * g["x_rb_" + key]) < 1e-12
+
+
+def test_thomas_cyclic(golden):
+    need_gpu()
+    from sslablu_gb300.direct_solve.omsdirectsolve import BlockTridiagonalSolver
+    g = golden("thomas_cyclic")
+    S = [tuple(p) for p in g["S"]]
+    th = BlockTridiagonalSolver(4, cyclic=True)
+    th.factorize(S, list(g["T"]))
+    assert relerr(th.solve(g["rhs"]), g["x"]) < 1e-12
+
+
+def test_c1_poisson(golden):
+    need_gpu()
+    from sslablu_gb300.direct_solve.omsdirectsolve import BlockTridiagonalSolver, RedBlackSolver
+    g = golden("c1_poisson64")
+    n = g["Sl"].shape[0]
+    nc = int(g["nc"])
+    S = [[g["Sr"][0]]] + [[g["Sl"][i], g["Sr"][i]] for i in range(1, n - 1)] + [[g["Sl"][n - 1]]]
+    th = BlockTridiagonalSolver(nc)
+    th.factorize(S, [np.eye(nc)] * n)
+    assert relerr(th.solve(g["rhs"]), g["x_th"]) < 1e-12
+    Sp = [[g["Sl"][i], g["Sr"][i]] for i in range(n)] + [[np.zeros((nc, nc))] * 2]
+    rb = RedBlackSolver(nc)
+    rb.factorize(Sp, [np.eye(nc)] * (n + 1))
+    xr = rb.solve(np.concatenate([g["rhs"], np.zeros(nc)]))
+    assert relerr(xr, g["x_rb"]) < 1e-12
+
+
+def test_rb_non_power_of_two_raises():
+    need_gpu()
+    from sslablu_gb300.direct_solve.omsdirectsolve import RedBlackSolver
+    S, T, _, _ = test_rb_system(3, 2)
+    with pytest.raises(ValueError):
+        RedBlackSolver(2).factorize(S, T)

@@ -1,0 +1,94 @@
+"""HBS compression, ULV factor/solve and apply on the GPU vs the upstream
+golden vectors (tests/golden/hbs_*.npz) and the CPU oracle."""
+import numpy as np
+import pytest
+
+from tests._cases import hbs_from_fixture, relerr
+from tests._gpu import need_gpu
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12   # plain float64 path vs upstream float64 (relative, per array)
+
+
+def _gpu_hbs_from_oracle(S, Nbvec, fac):
+    from sslablu_gb300.matAssembly.HBS.HBSnew import HBSMAT
+    G = HBSMAT()
+    G.set_mats(S.Umats, S.Dmats, S.Vmats, list(Nbvec), fac=fac)
+    return G
+
+
+@pytest.mark.parametrize("name", ["hbs_binary_k8", "hbs_quad_k8"])
+def test_apply_and_standalone_ulv(golden, name):
+    need_gpu()
+    g = golden(name)
+    S, Nbvec = hbs_from_fixture(g)
+    fac = 4 if g["quad"] else 2
+    G = _gpu_hbs_from_oracle(S, Nbvec, fac)
+    x = g["x"]
+    assert relerr(G.matmat(x), g["Ax_true"]) < TOL
+    assert relerr(G.rmatmat(x), g["ATx_true"]) < TOL
+    assert relerr(G @ x, g["Ax_true"]) < TOL
+    assert relerr(G.T @ x, g["ATx_true"]) < TOL
+    G.compute_ULV()
+    assert np.array_equal(G.NNvec, g["ulv_NNvec"])
+    assert relerr(G.solve(x), g["ulv_sol"]) < TOL
+    assert relerr(G.solve(x, mode="T"), g["ulv_solT"]) < TOL
+    # 1-D in, 1-D out
+    y1 = G.solve(x[:, 0])
+    assert y1.shape == (x.shape[0],)
+    assert relerr(y1, g["ulv_sol"][:, 0]) < TOL
+
+
+@pytest.mark.parametrize("name", ["hbs_binary_k8", "hbs_quad_k8", "hbs_c2_n512"])
+def test_construct_ulv(golden, name):
+    """HBSMAT(A).construct(k, True) with upstream's seeded sketches."""
+    need_gpu()
+    from sslablu_gb300.matAssembly.HBS.HBSnew import HBSMAT
+    g = golden(name)
+    S, Nbvec = hbs_from_fixture(g)      # leaves the global RNG where upstream drew from
+    fac = 4 if g["quad"] else 2
+    import numpy.random as npr
+    state = npr.get_state()
+    A = _gpu_hbs_from_oracle(S, Nbvec, fac)
+    npr.set_state(state)
+    H = HBSMAT(A, tree=None, quad=bool(g["quad"]))
+    H.set_Nbvec(list(Nbvec))
+    H.construct(int(g["k"]), True)
+    assert H.nSamples == int(g["nSamples"])
+    assert np.array_equal(H.NNvec, g["NNvec"])
+    x = g["x"]
+    assert relerr(H.matmat(x), g["mm"]) < TOL
+    assert relerr(H.rmatmat(x), g["rmm"]) < TOL
+    assert relerr(H.solve(x), g["sol"]) < TOL
+    assert relerr(H.solve(x, mode="T"), g["solT"]) < TOL
+    assert relerr(H.solve(x[:, 0]), g["sol1"]) < TOL
+
+
+def test_construct_factors_match(golden):
+    """Stored factors equal upstream's up to column signs of U/V."""
+    need_gpu()
+    from sslablu_gb300.matAssembly.HBS.HBSnew import HBSMAT
+    g = golden("hbs_binary_k8")
+    S, Nbvec = hbs_from_fixture(g)
+    import numpy.random as npr
+    state = npr.get_state()
+    A = _gpu_hbs_from_oracle(S, Nbvec, 2)
+    npr.set_state(state)
+    H = HBSMAT(A, tree=None, quad=False)
+    H.set_Nbvec(list(Nbvec))
+    H.construct(int(g["k"]), True)
+    # leaf D is basis independent; above the leaves D is written in the
+    # children's U/V bases, whose column signs are the SVD's free choice
+    Ds = H.Dmats
+    assert relerr(Ds[0], g["Dmats_0"]) < 1e-11
+    for t in range(1, len(Ds)):
+        assert relerr(np.abs(Ds[t]), np.abs(g["Dmats_%d" % t])) < 1e-11
+    for t, U in enumerate(H.Umats):
+        Ur = g["Umats_%d" % t]
+        Nb = Nbvec[t]
+        n = U.shape[0] // Nb
+        for b in range(Nb):
+            Pg = U[b * n:(b + 1) * n] @ U[b * n:(b + 1) * n].T
+            Pr = Ur[b * n:(b + 1) * n] @ Ur[b * n:(b + 1) * n].T
+            assert np.abs(Pg - Pr).max() < 1e-11
