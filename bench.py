@@ -1,0 +1,332 @@
+"""Benchmark of the slab direct-solve hot path on one GB300.
+
+Workload (the HBS configuration the headline metric is quoted on): a
+synthetic exact HBS matrix, N = 4096, leaf 64, binary tree of 7 levels
+(6 below the root), off-diagonal rank 32, leaf generators scaled so the
+singular values decay geometrically from 1 to 1e-12; compressed with the
+upstream randomized scheme (s = 4*32 + 2*64 + 5 = 261 Gaussian samples, the
+count the upstream algorithm fixes) and ULV-factored on the GPU once, outside
+the timed region (factor time reported separately).
+
+A step is one batch of 16 right-hand sides ~ N(0, 1) solved to a relative
+residual <= 1e-10 against the stored float64 HBS operator:
+  plain : float64 ULV solve (slu_ulv_solve)
+  mixed : float32 ULV solves + float64 residual refinement (slu_refine)
+`value` is the plain float64 path's RHS solves/s; the mixed path is reported
+beside it under "mixed".  Inputs (factors ~ 20 MB) fit in L2, so L2 is
+flushed (a 256 MB write) before every timed step, outside the timed events.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+--impl reference times the CPU restatement of the upstream numpy solve
+(oracle/, a port: the upstream package does not travel) on the host cores.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "RHS solves/sec + p50/p99 latency at 1e-10 rel residual, mixed vs plain FP64"
+UNIT = "RHS/s"
+N, LEAF, LEVELS, RANK, NRHS = 4096, 64, 7, 32, 16
+SEED = 20261205
+TOL = 1e-10
+
+
+def workload_config(extra=None):
+    cfg = {"workload": "synthetic exact HBS N=4096 leaf=64 levels=7 rank=32 "
+                       "sigma 1->1e-12, 16 RHS per step",
+           "N": N, "leaf": LEAF, "levels": LEVELS, "rank": RANK, "nrhs": NRHS,
+           "samples": 4 * RANK + 2 * LEAF + 5, "tol": TOL, "l2": "flushed before each step",
+           "parallelism": "replicas"}
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+def sigma():
+    return 10.0 ** (-12.0 * np.arange(RANK) / (RANK - 1))
+
+
+def make_problem():
+    from oracle.hbs import gen_random_hbs
+    np.random.seed(SEED)
+    S, Nbvec = gen_random_hbs(RANK, LEAF, LEVELS, quad=False, sigma=sigma())
+    rhs = np.random.default_rng(SEED + 1).standard_normal((N, NRHS))
+    return S, Nbvec, rhs
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, dev=0):
+        self.dev = dev
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.QUERY,
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = float(p[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------- CPU leg
+def cpu_time_solve(O, rhs, reps):
+    ts = []
+    O.solve(rhs)
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        O.solve(rhs)
+        ts.append(time.perf_counter() - t0)
+    return ts
+
+
+def cpu_baseline(S, Nbvec, rhs, budget_s=15.0):
+    """The CPU restatement of the upstream numpy ULV solve on the host cores."""
+    from oracle.hbs import OracleHBS
+    np.random.seed(SEED + 7)
+    t0 = time.perf_counter()
+    O = OracleHBS(S, None, Nbvec[0], len(Nbvec), 2).construct(RANK)
+    t_factor = time.perf_counter() - t0
+    one = cpu_time_solve(O, rhs, 1)[0]
+    reps = max(3, min(200, int(budget_s / max(one, 1e-4))))
+    ts = cpu_time_solve(O, rhs, reps)
+    med = statistics.median(ts)
+    return {"value": NRHS / med, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+            "sample": "%d solves of the 16-RHS batch (upstream ULVsparse.solve restated in "
+                      "numpy), median; factor (compress+ULV) %.2f s" % (reps, t_factor),
+            "p50_ms": 1e3 * med, "p99_ms": 1e3 * float(np.percentile(ts, 99)),
+            "factor_s": t_factor}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    S, Nbvec, rhs = make_problem()
+    base = cpu_baseline(S, Nbvec, rhs, budget_s=max(5.0, 2.0 * args.steps / 10))
+    line = {"metric": METRIC, "value": base["value"], "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": base["p50_ms"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference", "config": workload_config(),
+            "cpu_baseline": base,
+            "e2e": {"value": base["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------- GPU leg
+def run_gpu(args, rank, world):
+    import torch
+    import torch.distributed as dist
+    from sslablu_gb300 import _lib
+    from sslablu_gb300.matAssembly.HBS.HBSnew import HBSMAT
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    S, Nbvec, rhs = make_problem()
+    # operator to compress: the exact HBS matrix, resident on the device
+    A = HBSMAT().set_mats(S.Umats, S.Dmats, S.Vmats, list(Nbvec), fac=2)
+    np.random.seed(SEED + 7)
+    H = HBSMAT(A, tree=None, quad=False)
+    H.set_Nbvec(list(Nbvec))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    H.construct(RANK, True)
+    torch.cuda.synchronize()
+    t_factor = time.perf_counter() - t0
+    H.solve_refined(rhs[:, :1], tol=TOL, maxit=10)   # prepares float32 factors
+    torch.cuda.synchronize()
+
+    B = torch.from_numpy(rhs).cuda()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def plain_step():
+        return H._dev_solve(B, False)
+
+    def mixed_step():
+        return H.solve_refined(B, tol=TOL, maxit=10)
+
+    def residual(X):
+        R = B - H._dev_apply(X, False)
+        return float((R.norm(dim=0) / B.norm(dim=0)).max())
+
+    def timed(fn, steps, warmup):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        ts = []
+        n0 = _lib.launch_count()
+        for _ in range(steps):
+            flush.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            out = fn()
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1) * 1e-3)
+        launches = _lib.launch_count() - n0
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        return ts, launches, out
+
+    clocks = ClockSampler(dev)
+    clocks.start()
+    ts_plain, launches_plain, Xp = timed(plain_step, args.steps, args.warmup)
+    ts_mixed, launches_mixed, mixed_out = timed(mixed_step, args.steps, args.warmup)
+    # end-to-end through the public API: pinned host -> device -> solve -> host
+    hp = torch.from_numpy(rhs).pin_memory()
+    out_h = torch.empty_like(hp).pin_memory()
+    e2e = []
+    for i in range(args.warmup + args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        xd = hp.to("cuda", non_blocking=True)
+        y = H.solve(xd)
+        out_h.copy_(y, non_blocking=True)
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            e2e.append(time.perf_counter() - t0)
+    clk = clocks.stop()
+
+    res_plain = residual(Xp)
+    Xm, iters, relres = mixed_out
+    res_mixed = residual(Xm)
+    tot_plain = sum(ts_plain)
+    tot_mixed = sum(ts_mixed)
+    if world > 1:
+        t = torch.tensor([tot_plain, tot_mixed, sum(e2e)], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        tot_plain, tot_mixed, tot_e2e = t.tolist()
+    else:
+        tot_e2e = sum(e2e)
+    value = world * NRHS * args.steps / tot_plain
+    # roofline: the whole float64 solve step as one unit (algorithmic bytes:
+    # every solve factor read once + 4 passes over the right-hand sides)
+    import ctypes
+    fb = ctypes.c_size_t()
+    _lib.check(_lib.lib().slu_hbs_nbytes(H._op, 1, ctypes.byref(fb)))
+    alg_bytes = fb.value + 8 * N * NRHS * 4
+    p50 = statistics.median(ts_plain)
+    hbm, src = peaks()
+    achieved = alg_bytes / p50 / 1e9
+    line = None
+    if rank == 0:
+        base = cpu_baseline(S, Nbvec, rhs)
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * tot_plain / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": workload_config({"factor_s": t_factor, "arm": "plain float64 ULV solve"}),
+            "p50_ms": 1e3 * p50, "p99_ms": 1e3 * float(np.percentile(ts_plain, 99)),
+            "relres": res_plain,
+            "mixed": {"value": world * NRHS * args.steps / tot_mixed, "unit": UNIT,
+                      "dtype": "f32 solve + f64 residual refinement",
+                      "p50_ms": 1e3 * statistics.median(ts_mixed),
+                      "p99_ms": 1e3 * float(np.percentile(ts_mixed, 99)),
+                      "iters": iters, "relres": res_mixed,
+                      "speedup_vs_plain": tot_plain / tot_mixed,
+                      "gpu_launches": launches_mixed},
+            "e2e": {"value": world * NRHS * args.steps / tot_e2e, "unit": UNIT,
+                    "h2d_bytes_per_step": int(rhs.nbytes), "d2h_bytes_per_step": int(rhs.nbytes),
+                    "p50_ms": 1e3 * statistics.median(e2e)},
+            "gpu_launches": launches_plain,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "traffic": None,
+                         "kernel": "float64 ULV solve step (all launches of one solve)",
+                         "alg_bytes_per_launch": alg_bytes, "peak_source": src},
+            "cpu_baseline": {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "clocks": clk,
+        }
+        print(json.dumps(line))
+    return line
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1 and args.impl == "native":
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_gpu(args, rank, world)
+    if world > 1 and args.impl == "native":
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -43,6 +43,9 @@ typedef struct slu_dense_rb_s* slu_rb_t;
 
 /* ---------------------------------------------------------------- runtime */
 int slu_version(void);
+/* Kernels launched by this library so far in this process (host-side count,
+ * all streams); a diagnostic for benchmarks. */
+long long slu_launch_count(void);
 /* Copies the last error message of this thread into buf (NUL terminated). */
 int slu_last_error(char* buf, size_t len);
 /* stream: a cudaStream_t (NULL = legacy default stream). */

@@ -76,7 +76,13 @@ def load_cdll(path=LIB_PATH):
         f = getattr(dll, name)
         f.argtypes = args
         f.restype = c_int
+    dll.slu_launch_count.argtypes = []
+    dll.slu_launch_count.restype = c_longlong
     return dll
+
+
+def launch_count():
+    return int(lib().slu_launch_count())
 
 
 def lib():

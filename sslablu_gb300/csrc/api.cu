@@ -105,6 +105,8 @@ extern "C" {
 
 int slu_version(void) { return 1; }
 
+long long slu_launch_count(void) { return slu::launch_counter(); }
+
 int slu_last_error(char* buf, size_t len) {
   if (!buf || len == 0) return SLU_ERR_ARG;
   std::strncpy(buf, g_err.c_str(), len - 1);
@@ -310,20 +312,20 @@ int slu_refine(slu_handle_t h, slu_hbs_t op, const double* B, int ldb, double* X
     float* f = fbuf.as<float>();
     double* bn = nbuf.as<double>();
     double* rn = bn + c;
-    colnorm2_kernel<<<c, 256, 0, st>>>(N, c, B, ldb, bn);
+    colnorm2_kernel<<<c, 256, 0, st>>>(N, c, B, ldb, bn); ++slu::launch_counter();
     std::vector<double> hb(c), hr(c);
     SLU_CHECK_CUDA(cudaMemcpyAsync(hb.data(), bn, 8 * c, cudaMemcpyDeviceToHost, st));
     const long long nel = (long long)N * c;
-    tofloat_kernel<<<gsz(nel), 256, 0, st>>>(N, c, B, ldb, f);
+    tofloat_kernel<<<gsz(nel), 256, 0, st>>>(N, c, B, ldb, f); ++slu::launch_counter();
     int it = 0;
     double worst = 0.0;
     for (;;) {
       slu::hbs_solve<float>(h->h, H, false, f, c, c);
-      accum_kernel<<<gsz(nel), 256, 0, st>>>(N, c, f, X, ldx, it == 0);
+      accum_kernel<<<gsz(nel), 256, 0, st>>>(N, c, f, X, ldx, it == 0); ++slu::launch_counter();
       ++it;
       slu::hbs_apply(h->h, H, false, X, ldx, r, c, c);
-      residual_kernel<<<gsz(nel), 256, 0, st>>>(N, c, B, ldb, r, c);
-      colnorm2_kernel<<<c, 256, 0, st>>>(N, c, r, c, rn);
+      residual_kernel<<<gsz(nel), 256, 0, st>>>(N, c, B, ldb, r, c); ++slu::launch_counter();
+      colnorm2_kernel<<<c, 256, 0, st>>>(N, c, r, c, rn); ++slu::launch_counter();
       SLU_CHECK_CUDA(cudaMemcpyAsync(hr.data(), rn, 8 * c, cudaMemcpyDeviceToHost, st));
       SLU_CHECK_CUDA(cudaStreamSynchronize(st));
       worst = 0.0;
@@ -332,7 +334,7 @@ int slu_refine(slu_handle_t h, slu_hbs_t op, const double* B, int ldb, double* X
         worst = std::max(worst, std::sqrt(hr[j]) / den);
       }
       if (worst <= tol || it >= maxit) break;
-      tofloat_kernel<<<gsz(nel), 256, 0, st>>>(N, c, r, c, f);
+      tofloat_kernel<<<gsz(nel), 256, 0, st>>>(N, c, r, c, f); ++slu::launch_counter();
     }
     slu::check_launch("refine kernels");
     if (iters_out) *iters_out = it;

@@ -10,6 +10,11 @@
 
 namespace slu {
 
+long long& launch_counter() {
+  static long long n = 0;
+  return n;
+}
+
 int num_sms() {
   static int n = 0;
   if (!n) {

@@ -36,7 +36,12 @@ struct Error : std::runtime_error {
     if (!(cond)) throw ::slu::Error(SLU_ERR_ARG, msg);                  \
   } while (0)
 
+// Number of kernels this library has launched (host-side count; reported by
+// slu_launch_count so benchmarks can state how many of their kernels ran).
+long long& launch_counter();
+
 inline void check_launch(const char* what) {
+  ++launch_counter();
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess)
     throw Error(SLU_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
