@@ -92,6 +92,24 @@ int slu_hbs_apply(slu_handle_t h, slu_hbs_t op, int trans, const double* X, int 
  * trans = 1 reproduces upstream's mode 'T' handling of the permutation. */
 int slu_ulv_solve(slu_handle_t h, slu_hbs_t op, double* B, int ldb, int nrhs, int trans);
 
+/* Allocation-free variant of slu_ulv_solve (same float64 solve, same result).
+ * It has no counterpart in the upstream code.  It exists for callers that
+ * cannot let a library allocate device memory while they solve: a serving
+ * runtime that owns the GPU's memory under a fixed budget, or a latency-
+ * critical loop where cudaMalloc's implicit synchronisation is not
+ * acceptable.  Scratch comes from a fixed 16 MiB array compiled into the
+ * library (held on every GPU that loads it until the process exits); the
+ * call makes no cudaMalloc / cudaFree or other allocation.  Limit: five
+ * N x nrhs float64 buffers must fit, i.e. 5 * roundup(8*N*nrhs, 256) <=
+ * 16 MiB (N = 4096: up to 102 right-hand sides); larger sizes are rejected
+ * with SLU_ERR_ARG.  The first call on a device (with that device current)
+ * looks up the array's device address with cudaGetSymbolAddress; make that
+ * first call before any stream capture.  All calls on a device share the
+ * array: calls that overlap on the GPU race and must be serialised by the
+ * caller.  The operator must already be factored (slu_hbs_compress with
+ * compute_ulv or slu_ulv_factor). */
+int slu_ulv_solve_noalloc(slu_handle_t h, slu_hbs_t op, double* B, int ldb, int nrhs, int trans);
+
 /* Single-precision copy of the ULV factors and a float32 solve with the same
  * sweep; used inside iterative refinement (no upstream counterpart: the
  * mixed-precision path of this library). */

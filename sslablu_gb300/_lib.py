@@ -34,6 +34,7 @@ SIGNATURES = {
     "slu_ulv_factor": [P, P],
     "slu_hbs_apply": [P, P, c_int, P, c_int, P, c_int, c_int],
     "slu_ulv_solve": [P, P, P, c_int, c_int, c_int],
+    "slu_ulv_solve_noalloc": [P, P, P, c_int, c_int, c_int],
     "slu_hbs_prepare_f32": [P, P],
     "slu_ulv_solve_f32": [P, P, P, c_int, c_int, c_int],
     "slu_refine": [P, P, P, c_int, P, c_int, c_int, c_double, c_int, P, P],

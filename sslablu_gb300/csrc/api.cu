@@ -5,42 +5,21 @@
 #include <memory>
 #include <string>
 
-#include "../../include/slablu.h"
-#include "tridiag.cuh"
+#include "abi_types.cuh"
 
-struct slu_handle_s {
-  slu::Handle h;
-};
-struct slu_hbs_s {
-  slu::Hbs H;
-};
-struct slu_dense_rb_s {
-  slu::RbSolver S;
-  bool thomas = false;
-};
+namespace slu {
+std::string& thread_error() {
+  static thread_local std::string msg;
+  return msg;
+}
+}  // namespace slu
 
 namespace {
-thread_local std::string g_err;
+#define g_err (slu::thread_error())
 
 template <class F>
 int guard(slu_handle_t h, F&& f) {
-  try {
-    f();
-    return SLU_OK;
-  } catch (const slu::Error& e) {
-    g_err = e.what();
-    if (h) h->h.last_error = g_err;
-    return e.code;
-  } catch (const std::bad_alloc&) {
-    g_err = "host allocation failed";
-    return SLU_ERR_ALLOC;
-  } catch (const std::exception& e) {
-    g_err = e.what();
-    return SLU_ERR_ARG;
-  } catch (...) {
-    g_err = "unknown error";
-    return SLU_ERR_ARG;
-  }
+  return slu::guard_call(h, static_cast<F&&>(f));
 }
 
 // per-column squared 2-norms of an rows x cols row-major array

@@ -464,21 +464,33 @@ template <> struct Fac<float> {
 };
 }  // namespace
 
+size_t hbs_solve_scratch_bytes(const Hbs& H, int c, size_t elem) {
+  return 5 * ((elem * (size_t)H.N * c + 255) & ~size_t(255));
+}
+
 template <typename T>
 void hbs_solve(Handle& h, const Hbs& H, bool trans, T* B, int ldb, int c) {
+  h.ws.reserve(hbs_solve_scratch_bytes(H, c, sizeof(T)) + 256, h.stream);
+  T* scratch = h.ws.take<T>(hbs_solve_scratch_bytes(H, c, sizeof(T)) / sizeof(T));
+  hbs_solve_scratch<T>(h.stream, H, trans, B, ldb, c, scratch);
+}
+
+template <typename T>
+void hbs_solve_scratch(cudaStream_t st, const Hbs& H, bool trans, T* B, int ldb, int c,
+                       T* scratch) {
   using F = Fac<T>;
-  cudaStream_t st = h.stream;
   SLU_REQUIRE(H.has_ulv, "HBS operator has no ULV factorisation");
   if (sizeof(T) == 4) SLU_REQUIRE(H.has_f32, "single-precision factors not prepared");
   const int L = H.L;
   const size_t N = H.N;
   const std::vector<long long>& NN = H.NN;
-  h.ws.reserve(sizeof(T) * (5 * N * c) + 8 * 256, st);
-  T* r = h.ws.take<T>(N * c);
-  T* y = h.ws.take<T>(N * c);
-  T* tmp = h.ws.take<T>(N * c);
-  T* v = h.ws.take<T>(N * c);
-  T* vn = h.ws.take<T>(N * c);
+  // five (N x c) buffers, each starting on a 256-byte boundary
+  const size_t stride = ((sizeof(T) * N * c + 255) & ~size_t(255)) / sizeof(T);
+  T* r = scratch;
+  T* y = scratch + stride;
+  T* tmp = scratch + 2 * stride;
+  T* v = scratch + 3 * stride;
+  T* vn = scratch + 4 * stride;
   const T one = T(1), zero = T(0), mone = T(-1);
   const int64_t* perm = H.perm.as<int64_t>();
   if (!trans) {
@@ -597,6 +609,8 @@ void hbs_solve(Handle& h, const Hbs& H, bool trans, T* B, int ldb, int c) {
 }
 template void hbs_solve<double>(Handle&, const Hbs&, bool, double*, int, int);
 template void hbs_solve<float>(Handle&, const Hbs&, bool, float*, int, int);
+template void hbs_solve_scratch<double>(cudaStream_t, const Hbs&, bool, double*, int, int, double*);
+template void hbs_solve_scratch<float>(cudaStream_t, const Hbs&, bool, float*, int, int, float*);
 
 void hbs_make_f32(Handle& h, Hbs& H) {
   cudaStream_t st = h.stream;

@@ -65,6 +65,12 @@ void hbs_apply(Handle& h, const Hbs& H, bool trans, const double* X, int ldx, do
 // ULV solve, reference semantics of HBSMAT.solve (with the permutation)
 template <typename T>
 void hbs_solve(Handle& h, const Hbs& H, bool trans, T* B, int ldb, int nrhs);
+// The same solve with caller-provided scratch of hbs_solve_scratch_bytes()
+// bytes (256-byte aligned); it makes no allocation of its own.
+template <typename T>
+void hbs_solve_scratch(cudaStream_t st, const Hbs& H, bool trans, T* B, int ldb, int nrhs,
+                       T* scratch);
+size_t hbs_solve_scratch_bytes(const Hbs& H, int nrhs, size_t elem);
 void hbs_make_f32(Handle& h, Hbs& H);
 size_t hbs_nbytes(const Hbs& H, int which);
 
