@@ -74,9 +74,19 @@ int slu_hbs_compress(slu_handle_t h, slu_hbs_t op, int nleaves, int rk, int s, c
 
 /* Replaces HBSMAT.set_mats (matAssembly/HBS/HBSnew.py:125-133) one level at a
  * time: level 0 = leaves.  U, V: (Nb*n) x k, D: (Nb*n) x n (device); on the
- * root pass k = 0 and U = V = NULL.  Every level must be set before use. */
+ * root pass k = 0 and U = V = NULL.  Every level must be set before use.
+ * V may be NULL for an operator that is only solved with loaded ULV factors
+ * (slu_hbs_set_ulv_level); apply and factorisation then report an error. */
 int slu_hbs_set_level(slu_handle_t h, slu_hbs_t op, int level, int Nb, int n, int k,
                       const double* U, const double* V, const double* D);
+
+/* Loads given ULV factors of one level (ULVsparse.solve's Qlist[level],
+ * Wlist[level], Rlist[level], Uulist[level]; ULVsparse.py:295), after every
+ * level was set with slu_hbs_set_level (V may be NULL there for an operator
+ * that is only solved).  Q, W: (Nb*n) x n; R: (Nb*(n-k)) x n (root: n x n);
+ * Uu: (Nb*(n-k)) x k.  W and Uu are ignored (may be NULL) on the root. */
+int slu_hbs_set_ulv_level(slu_handle_t h, slu_hbs_t op, int level, const double* Q,
+                          const double* W, const double* R, const double* Uu);
 
 /* Replaces ULVsparse.compute_ULV (matAssembly/HBS/ULVsparse.py:231-293) /
  * HBSMAT.compute_ULV (HBSnew.py:390-391) for loaded factors. */

@@ -32,6 +32,7 @@ SIGNATURES = {
     "slu_hbs_compress": [P, P, c_int, c_int, c_int, P, P, P, P, c_int],
     "slu_hbs_set_level": [P, P, c_int, c_int, c_int, c_int, P, P, P],
     "slu_ulv_factor": [P, P],
+    "slu_hbs_set_ulv_level": [P, P, c_int, P, P, P, P],
     "slu_hbs_apply": [P, P, c_int, P, c_int, P, c_int, c_int],
     "slu_ulv_solve": [P, P, P, c_int, c_int, c_int],
     "slu_ulv_solve_noalloc": [P, P, P, c_int, c_int, c_int],

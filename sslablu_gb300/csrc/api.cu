@@ -195,7 +195,7 @@ int slu_hbs_set_level(slu_handle_t h, slu_hbs_t op, int level, int Nb, int n, in
     SLU_REQUIRE(level >= 0 && level < H.L, "level out of range");
     const bool root = (level == H.L - 1);
     SLU_REQUIRE(Nb >= 1 && n >= 1 && k >= 0 && k <= n, "bad level geometry");
-    SLU_REQUIRE(root ? (k == 0 && Nb == 1) : (k >= 1 && U && V), "root takes k = 0, others U/V");
+    SLU_REQUIRE(root ? (k == 0 && Nb == 1) : (k >= 1 && U), "root takes k = 0, others U (and V)");
     if (level == 0) SLU_REQUIRE((long long)Nb * n == H.N, "leaf level must cover N rows");
     cudaStream_t st = h->h.stream;
     slu::Level& l = H.lv[level];
@@ -206,9 +206,11 @@ int slu_hbs_set_level(slu_handle_t h, slu_hbs_t op, int level, int Nb, int n, in
     const size_t rows = (size_t)Nb * n;
     if (!root) {
       l.U.alloc(8 * rows * k, st);
-      l.V.alloc(8 * rows * k, st);
       SLU_CHECK_CUDA(cudaMemcpyAsync(l.U.p, U, 8 * rows * k, cudaMemcpyDeviceToDevice, st));
-      SLU_CHECK_CUDA(cudaMemcpyAsync(l.V.p, V, 8 * rows * k, cudaMemcpyDeviceToDevice, st));
+      if (V) {  // V is needed for apply and factorisation, not for a solve of loaded factors
+        l.V.alloc(8 * rows * k, st);
+        SLU_CHECK_CUDA(cudaMemcpyAsync(l.V.p, V, 8 * rows * k, cudaMemcpyDeviceToDevice, st));
+      }
     }
     l.D.alloc(8 * rows * n, st);
     SLU_CHECK_CUDA(cudaMemcpyAsync(l.D.p, D, 8 * rows * n, cudaMemcpyDeviceToDevice, st));
@@ -231,6 +233,38 @@ int slu_hbs_set_level(slu_handle_t h, slu_hbs_t op, int level, int Nb, int n, in
       H.has_ulv = false;
       H.has_f32 = false;
     }
+  });
+}
+
+int slu_hbs_set_ulv_level(slu_handle_t h, slu_hbs_t op, int level, const double* Q,
+                          const double* W, const double* R, const double* Uu) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h && op && Q && R, "null argument");
+    slu::Hbs& H = op->H;
+    SLU_REQUIRE(H.has_mats, "set every level with slu_hbs_set_level first");
+    SLU_REQUIRE(level >= 0 && level < H.L, "level out of range");
+    const bool root = (level == H.L - 1);
+    SLU_REQUIRE(root || (W && Uu), "non-root levels need W and Uu");
+    cudaStream_t st = h->h.stream;
+    slu::Level& l = H.lv[level];
+    const size_t rows = (size_t)l.Nb * l.n;
+    l.kU = root ? 0 : l.k;
+    l.uu_rows = root ? 0 : l.n - l.k;
+    auto put = [&](slu::DevBuf& b, const double* src, size_t count) {
+      b.alloc(8 * count, st);
+      if (count) SLU_CHECK_CUDA(cudaMemcpyAsync(b.p, src, 8 * count, cudaMemcpyDeviceToDevice, st));
+    };
+    put(l.Q, Q, rows * l.n);
+    put(l.R, R, (size_t)l.Nb * l.nu * l.n);
+    if (!root) {
+      put(l.W, W, rows * l.n);
+      put(l.Uu, Uu, (size_t)l.Nb * l.uu_rows * l.kU);
+    }
+    l.Uf.release(); l.Df.release(); l.Qf.release(); l.Wf.release(); l.Rf.release(); l.Uuf.release();
+    bool all = true;
+    for (int t = 0; t < H.L; ++t) all = all && H.lv[t].Q.p && H.lv[t].R.p;
+    H.has_ulv = all;
+    H.has_f32 = false;
   });
 }
 

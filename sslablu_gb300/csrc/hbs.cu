@@ -185,8 +185,6 @@ void hbs_compress(Handle& h, Hbs& H, int Nb0, int rk, int s, const double* Om, c
   const int nl = N / Nb0;
   SLU_REQUIRE((long long)nl * Nb0 == N, "N must be a multiple of the leaf count");
   SLU_REQUIRE(rk >= 1, "rank must be positive");
-  SLU_REQUIRE(L == 1 || nl >= rk,
-              "leaf size smaller than the rank is not supported (upstream slices Q by rk)");
   // ---- level geometry (HBSnew.py:234-256)
   H.lv.clear();
   H.lv.resize(L);
@@ -344,7 +342,11 @@ void hbs_compress(Handle& h, Hbs& H, int Nb0, int rk, int s, const double* Om, c
         Rh = Rhat;
         Uh = Uhat;
       }
-      ulv_level(st, l, root, Rh, Uh, l.kU, rk, true, Ud[w], R22[w], us);
+      // upstream slices Q[:, :-rk] / Q[:, -rk:] (HBSnew.py:291-292); Python
+      // slicing saturates, so the split is min(rk, n) = the level rank below
+      // the root
+      const int kslice = root ? std::min(rk, n) : l.k;
+      ulv_level(st, l, root, Rh, Uh, l.kU, kslice, true, Ud[w], R22[w], us);
     }
   }
   H.has_mats = true;
@@ -356,6 +358,8 @@ void hbs_compress(Handle& h, Hbs& H, int Nb0, int rk, int s, const double* Om, c
 void hbs_factor(Handle& h, Hbs& H) {
   cudaStream_t st = h.stream;
   SLU_REQUIRE(H.has_mats, "HBS factors not loaded");
+  for (int t = 0; t + 1 < H.L; ++t)
+    SLU_REQUIRE(H.lv[t].V.p, "factorisation needs V factors (loaded without V)");
   const int L = H.L;
   size_t nmax = 0, kmax = 1, N = H.N;
   for (const Level& l : H.lv) { nmax = std::max<size_t>(nmax, l.n); kmax = std::max<size_t>(kmax, l.k); }
@@ -401,6 +405,8 @@ void hbs_apply(Handle& h, const Hbs& H, bool trans, const double* X, int ldx, do
                int ldy, int c) {
   cudaStream_t st = h.stream;
   SLU_REQUIRE(H.has_mats, "HBS factors not loaded");
+  for (int t = 0; t + 1 < H.L; ++t)
+    SLU_REQUIRE(H.lv[t].V.p, "apply needs V factors (loaded without V)");
   const int L = H.L;
   const size_t N = H.N;
   size_t vvrows = N;

@@ -54,3 +54,29 @@ def kernel_system(m=64, nS=4):
         C = blk(-0.2 - 0.01 * i) if i < nS - 1 else np.zeros((m, m))
         S.append((A, C))
     return S
+
+
+def gauss_system(m=128, nS=4, c=20.0):
+    """Gaussian-kernel couplings (tests/golden/make_golden.py)."""
+    x = np.linspace(0, 1, m)
+
+    def blk(shift):
+        return 0.3 * np.exp(-c * (x[:, None] - x[None, :] - shift) ** 2)
+    S = []
+    for i in range(nS):
+        A = blk(0.2 + 0.01 * i) if i > 0 else np.zeros((m, m))
+        C = blk(-0.2 - 0.01 * i) if i < nS - 1 else np.zeros((m, m))
+        S.append((A, C))
+    return S
+
+
+def tridiag_matrix(S, m):
+    """Assemble I + block off-diagonals of a coupling list."""
+    nS = len(S)
+    M = np.eye(nS * m)
+    for i in range(nS):
+        if i > 0:
+            M[i * m:(i + 1) * m, (i - 1) * m:i * m] = S[i][0]
+        if i < nS - 1:
+            M[i * m:(i + 1) * m, (i + 1) * m:(i + 2) * m] = S[i][1]
+    return M

@@ -19,8 +19,10 @@ the large outputs are stored.  Fixtures written (all small):
   c1_poisson64.npz   multislab.oms + stencil 2D Poisson, 8 slabs, 64-point
                      interfaces (the C1 layout at reduced size): S blocks, rhs
                      and the Thomas / red-black / functional-Thomas solutions
-  rbhbs_kernel.npz   RedBlackSolverHBS / ThomasSolverHBS on a smooth-kernel
-                     block-tridiagonal system
+  rbhbs_kernel.npz   RedBlackSolverHBS / ThomasSolverHBS on an exponential-
+                     kernel block-tridiagonal system (truncation dominated)
+  rbhbs_gauss.npz    the same on a Gaussian-kernel system that rank 16
+                     resolves to a ~1e-13 residual
 """
 import contextlib
 import io
@@ -167,6 +169,45 @@ def kernel_system(m=64, nS=4):
     return S
 
 
+def gauss_system(m=128, nS=4, c=20.0):
+    x = np.linspace(0, 1, m)
+
+    def blk(shift):
+        return 0.3 * np.exp(-c * (x[:, None] - x[None, :] - shift) ** 2)
+    S = []
+    for i in range(nS):
+        A = blk(0.2 + 0.01 * i) if i > 0 else np.zeros((m, m))
+        C = blk(-0.2 - 0.01 * i) if i < nS - 1 else np.zeros((m, m))
+        S.append((A, C))
+    return S
+
+
+def rbhbs_gauss(ref):
+    """Well-resolved HBS red-black / Thomas (residual ~1e-13 at rank 16)."""
+    m, nS, leaf, nlev, rk = 128, 4, 32, 3, 16
+    tree = types.SimpleNamespace(perm_leaf=np.arange(m), nleaves=m // leaf, nlevels=nlev)
+    S = gauss_system(m, nS)
+
+    def lo(A):
+        o = ref.omsdirectsolveHBS.dense_to_linop(A)
+        o.tree, o.quad = tree, False
+        return o
+    Slo = [(lo(a), lo(c)) for a, c in S]
+    b = np.random.default_rng(7).standard_normal(nS * m)
+    out = dict(m=m, nS=nS, leaf=leaf, nlev=nlev, rk=rk, b=b)
+    np.random.seed(11)
+    with contextlib.redirect_stdout(QUIET):
+        R = ref.omsdirectsolveHBS.RedBlackSolverHBS(m, rk, tree, False)
+        R.factorize(Slo)
+        out["x_rb"] = R.solve(b)
+    np.random.seed(12)
+    with contextlib.redirect_stdout(QUIET):
+        T = ref.omsdirectsolveHBS.ThomasSolverHBS(m, rk)
+        T.factorize(Slo)
+        out["x_th"] = T.solve(b)
+    np.savez_compressed(os.path.join(HERE, "rbhbs_gauss.npz"), **out)
+
+
 def rbhbs(ref):
     m, nS, leaf, nlev = 64, 4, 16, 3
     tree = types.SimpleNamespace(perm_leaf=np.arange(m), nleaves=m // leaf, nlevels=nlev)
@@ -204,6 +245,7 @@ def main():
     hbs_case(ref, "hbs_c2_n512", 32, 64, 4, False, 103, sigma=sig, nrhs=4, store_factors=False)
     c1_poisson(ref, P)
     rbhbs(ref)
+    rbhbs_gauss(ref)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

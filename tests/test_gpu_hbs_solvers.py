@@ -1,0 +1,84 @@
+"""HBS red-black and Thomas solvers on the GPU vs upstream golden vectors.
+
+rbhbs_gauss: rank 16 resolves the Schur complements to a ~1e-13 residual, so
+the GPU result must match upstream to 1e-10 (float64 rounding of the two
+implementations, amplified only by the conditioning of the compressions).
+rbhbs_kernel: the exponential-kernel couplings are truncation dominated at
+ranks 16/24 (upstream residual 4e-5 / 1e-5).  The singular values near the
+cut decay slowly, so the retained subspace of each truncated SVD is fixed only
+up to the near-degenerate cluster at the cut: float64 rounding differences
+between any two implementations (LAPACK vs this library) move the truncated
+approximation within its own error.  There parity is equal solution quality:
+the GPU residual within 2x of upstream's, and the two solutions no further
+apart than 100x that residual.  (Thomas-HBS at these ranks is well resolved
+and must match to 1e-10.)
+"""
+import numpy as np
+import pytest
+import types
+
+from tests._cases import gauss_system, kernel_system, relerr, tridiag_matrix
+from tests._gpu import need_gpu
+
+pytestmark = pytest.mark.gpu
+
+
+def _ops(S, tree):
+    from sslablu_gb300.direct_solve.omsdirectsolveHBS import dense_to_linop
+    out = []
+    for a, c in S:
+        la, lc = dense_to_linop(a), dense_to_linop(c)
+        la.tree = lc.tree = tree
+        la.quad = lc.quad = False
+        out.append((la, lc))
+    return out
+
+
+def test_rbhbs_gauss(golden):
+    need_gpu()
+    from sslablu_gb300.direct_solve.omsdirectsolveHBS import RedBlackSolverHBS, ThomasSolverHBS
+    g = golden("rbhbs_gauss")
+    m, nS, leaf, nlev, rk = (int(g[k]) for k in ("m", "nS", "leaf", "nlev", "rk"))
+    tree = types.SimpleNamespace(perm_leaf=np.arange(m), nleaves=m // leaf, nlevels=nlev)
+    S = gauss_system(m, nS)
+    M = tridiag_matrix(S, m)
+    np.random.seed(11)
+    R = RedBlackSolverHBS(m, rk, tree, False)
+    R.factorize(_ops(S, tree))
+    x = R.solve(g["b"])
+    assert x.shape == g["b"].shape
+    assert relerr(x, g["x_rb"]) < 1e-10
+    assert relerr(M @ x, g["b"]) < 1e-11
+    np.random.seed(12)
+    T = ThomasSolverHBS(m, rk)
+    T.factorize(_ops(S, tree))
+    y = T.solve(g["b"])
+    assert relerr(y, g["x_th"]) < 1e-10
+    assert relerr(M @ y, g["b"]) < 1e-11
+    # multi-RHS through the same factors
+    B = np.stack([g["b"], -g["b"]], axis=1)
+    X = R.solve(B)
+    assert relerr(X[:, 1], -x) < 1e-12
+
+
+@pytest.mark.parametrize("rk", [16, 24])
+def test_rbhbs_kernel(golden, rk):
+    need_gpu()
+    from sslablu_gb300.direct_solve.omsdirectsolveHBS import RedBlackSolverHBS, ThomasSolverHBS
+    g = golden("rbhbs_kernel")
+    m, nS, leaf, nlev = int(g["m"]), int(g["nS"]), int(g["leaf"]), int(g["nlev"])
+    tree = types.SimpleNamespace(perm_leaf=np.arange(m), nleaves=m // leaf, nlevels=nlev)
+    S = kernel_system(m, nS)
+    M = tridiag_matrix(S, m)
+    np.random.seed(11)
+    R = RedBlackSolverHBS(m, rk, tree, False)
+    R.factorize(_ops(S, tree))
+    x = R.solve(g["b"])
+    res_ref = relerr(M @ g["x_rb_%d" % rk], g["b"])
+    assert relerr(M @ x, g["b"]) < 2 * res_ref
+    assert relerr(x, g["x_rb_%d" % rk]) < 100 * res_ref
+    np.random.seed(12)
+    T = ThomasSolverHBS(m, rk)
+    T.factorize(_ops(S, tree))
+    y = T.solve(g["b"])
+    assert relerr(y, g["x_th_%d" % rk]) < 1e-10

@@ -99,3 +99,20 @@ def test_rbhbs_kernel(golden, rk):
     np.random.seed(12)
     y = od.ThomasHBS(m, rk, td, False).factorize(S).solve(g["b"])
     assert relerr(y, g["x_th_%d" % rk]) < 1e-12
+
+
+def test_rbhbs_gauss(golden):
+    from tests._cases import gauss_system, tridiag_matrix
+    g = golden("rbhbs_gauss")
+    m, nS, leaf, nlev, rk = (int(g[k]) for k in ("m", "nS", "leaf", "nlev", "rk"))
+    S = gauss_system(m, nS)
+    Sop = [(od.dense_op(a), od.dense_op(c)) for a, c in S]
+    td = (np.arange(m), m // leaf, nlev)
+    np.random.seed(11)
+    x = od.RedBlackHBS(m, rk, td, False).factorize(Sop).solve(g["b"])
+    assert relerr(x, g["x_rb"]) < 1e-12
+    np.random.seed(12)
+    y = od.ThomasHBS(m, rk, td, False).factorize(Sop).solve(g["b"])
+    assert relerr(y, g["x_th"]) < 1e-12
+    M = tridiag_matrix(S, m)
+    assert relerr(M @ g["x_rb"], g["b"]) < 1e-12
