@@ -407,46 +407,10 @@ void hbs_apply(Handle& h, const Hbs& H, bool trans, const double* X, int ldx, do
   SLU_REQUIRE(H.has_mats, "HBS factors not loaded");
   for (int t = 0; t + 1 < H.L; ++t)
     SLU_REQUIRE(H.lv[t].V.p, "apply needs V factors (loaded without V)");
-  const int L = H.L;
-  const size_t N = H.N;
-  size_t vvrows = N;
-  for (int t = 0; t + 1 < L; ++t) vvrows += (size_t)H.lv[t].Nb * H.lv[t].k;
-  h.ws.reserve(8 * ((vvrows + 2 * N) * c) + 8 * 256, st);
-  double* VVbuf = h.ws.take<double>(vvrows * c);
-  double* u0 = h.ws.take<double>(N * c);
-  double* u1 = h.ws.take<double>(N * c);
-  // VV[t] offsets: VV[0] has N rows, VV[t+1] has Nb_t*k_t rows
-  std::vector<double*> VV(L);
-  VV[0] = VVbuf;
-  {
-    size_t off = N;
-    for (int t = 0; t + 1 < L; ++t) {
-      VV[t + 1] = VVbuf + off * c;
-      off += (size_t)H.lv[t].Nb * H.lv[t].k;
-    }
-  }
-  permute_rows<double>(st, false, (int)N, c, H.perm.as<int64_t>(), X, ldx, VV[0], c);
-  for (int t = 0; t + 1 < L; ++t) {
-    const Level& l = H.lv[t];
-    const double* F = trans ? dp(l.U) : dp(l.V);
-    gemm<double>(st, true, false, l.k, c, l.n, 1.0, F, l.k, (long long)l.n * l.k, 0, VV[t], c,
-                 (long long)l.n * c, 0, 0.0, VV[t + 1], c, (long long)l.k * c, 0, l.Nb);
-  }
-  const Level& r = H.lv[L - 1];
-  double* u = u0;
-  double* un = u1;
-  gemm<double>(st, trans, false, r.n, c, r.n, 1.0, dp(r.D), r.n, 0, 0, VV[L - 1], c, 0, 0, 0.0, u,
-               c, 0, 0, 1);
-  for (int t = L - 2; t >= 0; --t) {
-    const Level& l = H.lv[t];
-    const double* G = trans ? dp(l.V) : dp(l.U);
-    gemm<double>(st, false, false, l.n, c, l.k, 1.0, G, l.k, (long long)l.n * l.k, 0, u, c,
-                 (long long)l.k * c, 0, 0.0, un, c, (long long)l.n * c, 0, l.Nb);
-    gemm<double>(st, trans, false, l.n, c, l.n, 1.0, dp(l.D), l.n, (long long)l.n * l.n, 0, VV[t],
-                 c, (long long)l.n * c, 0, 1.0, un, c, (long long)l.n * c, 0, l.Nb);
-    std::swap(u, un);
-  }
-  permute_rows<double>(st, true, (int)N, c, H.perm.as<int64_t>(), u, c, Yout, ldy);
+  const size_t elems = hbs_apply_scratch_elems(H, c);
+  h.ws.reserve(8 * elems + 256, st);
+  double* scratch = h.ws.take<double>(elems);
+  hbs_apply_fused(st, H, trans, X, ldx, Yout, ldy, c, scratch);
 }
 
 // ============================================================== solve
@@ -500,62 +464,11 @@ void hbs_solve_scratch(cudaStream_t st, const Hbs& H, bool trans, T* B, int ldb,
   const T one = T(1), zero = T(0), mone = T(-1);
   const int64_t* perm = H.perm.as<int64_t>();
   if (!trans) {
-    // ---- mode N (ULVsparse.py:296-327)
-    permute_rows<T>(st, false, (int)N, c, perm, B, ldb, r, c);
-    for (int t = 0; t < L; ++t) {
-      const Level& l = H.lv[t];
-      const int n = l.n, Nb = l.Nb;
-      const long long nn = (long long)n * n;
-      SLU_CHECK_CUDA(cudaMemcpyAsync(tmp, r + NN[t] * c, sizeof(T) * (size_t)Nb * n * c,
-                                     cudaMemcpyDeviceToDevice, st));
-      if (t < L - 1) {
-        const int k = l.k, nu = l.nu;
-        gemm<T>(st, true, false, nu, c, n, one, F::Q(l), n, nn, 0, tmp, c, (long long)n * c, 0,
-                zero, r + NN[t] * c, c, (long long)nu * c, 0, Nb);
-        gemm<T>(st, true, false, k, c, n, one, F::Q(l) + nu, n, nn, 0, tmp, c, (long long)n * c, 0,
-                zero, r + NN[t + 1] * c, c, (long long)k * c, 0, Nb);
-      } else {
-        gemm<T>(st, true, false, n, c, n, one, F::Q(l), n, 0, 0, tmp, c, 0, 0, zero,
-                r + NN[t] * c, c, 0, 0, 1);
-      }
-    }
-    const Level& rt = H.lv[L - 1];
-    T* yr = y + NN[L - 1] * c;
-    SLU_CHECK_CUDA(cudaMemcpyAsync(yr, r + NN[L - 1] * c, sizeof(T) * (size_t)rt.n * c,
-                                   cudaMemcpyDeviceToDevice, st));
-    trsm_upper<T>(st, false, rt.n, F::R(rt), rt.n, 1, 0, yr, c, 1, 0, c, 1);
-    gemm<T>(st, false, false, rt.n, c, rt.n, one, F::D(rt), rt.n, 0, 0, yr, c, 0, 0, zero, v, c,
-            0, 0, 1);
-    for (int t = L - 2; t >= 0; --t) {
-      const Level& l = H.lv[t];
-      const int n = l.n, k = l.k, nu = l.nu, Nb = l.Nb;
-      const long long nn = (long long)n * n;
-      T* yt = y + NN[t] * c;
-      T* ynx = y + NN[t + 1] * c;
-      if (nu > 0) {
-        SLU_CHECK_CUDA(cudaMemcpyAsync(yt, r + NN[t] * c, sizeof(T) * (size_t)Nb * nu * c,
-                                       cudaMemcpyDeviceToDevice, st));
-        gemm<T>(st, false, false, nu, c, k, mone, F::Uu(l), k, (long long)nu * k, 0, v, c,
-                (long long)k * c, 0, one, yt, c, (long long)nu * c, 0, Nb);
-        gemm<T>(st, false, false, nu, c, k, mone, F::R(l) + nu, n, (long long)nu * n, 0, ynx, c,
-                (long long)k * c, 0, one, yt, c, (long long)nu * c, 0, Nb);
-        trsm_upper<T>(st, false, nu, F::R(l), n, 1, (long long)nu * n, yt, c, 1,
-                      (long long)nu * c, c, Nb);
-      }
-      gemm<T>(st, false, false, n, c, nu, one, F::W(l), n, nn, 0, yt, c, (long long)nu * c, 0,
-              zero, tmp, c, (long long)n * c, 0, Nb);
-      gemm<T>(st, false, false, n, c, k, one, F::W(l) + nu, n, nn, 0, ynx, c, (long long)k * c, 0,
-              one, tmp, c, (long long)n * c, 0, Nb);
-      SLU_CHECK_CUDA(cudaMemcpyAsync(yt, tmp, sizeof(T) * (size_t)Nb * n * c,
-                                     cudaMemcpyDeviceToDevice, st));
-      gemm<T>(st, false, false, n, c, k, one, F::U(l), k, (long long)n * k, 0, v, c,
-              (long long)k * c, 0, zero, vn, c, (long long)n * c, 0, Nb);
-      gemm<T>(st, false, false, n, c, n, one, F::D(l), n, nn, 0, yt, c, (long long)n * c, 0, one,
-              vn, c, (long long)n * c, 0, Nb);
-      std::swap(v, vn);
-    }
-    permute_rows<T>(st, true, (int)N, c, perm, y, c, B, ldb);
-  } else {
+    // ---- mode N (ULVsparse.py:296-327): fused per-level kernels
+    ulv_solve_fused<T>(st, H, B, ldb, c, scratch, stride);
+    return;
+  }
+  {
     // ---- mode T (ULVsparse.py:328-353); upstream scatters the input and
     // gathers the output (HBSnew.py:403-411)
     permute_rows<T>(st, true, (int)N, c, perm, B, ldb, r, c);

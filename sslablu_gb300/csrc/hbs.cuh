@@ -71,6 +71,15 @@ template <typename T>
 void hbs_solve_scratch(cudaStream_t st, const Hbs& H, bool trans, T* B, int ldb, int nrhs,
                        T* scratch);
 size_t hbs_solve_scratch_bytes(const Hbs& H, int nrhs, size_t elem);
+// Mode-N solve with one fused kernel per level and sweep (ulv_solve.cu);
+// scratch: five buffers of `stride` elements.
+template <typename T>
+void ulv_solve_fused(cudaStream_t st, const Hbs& H, T* B, int ldb, int c, T* scratch,
+                     size_t stride);
+// Fused per-level apply (hbs_apply.cu); scratch of hbs_apply_scratch_elems doubles.
+size_t hbs_apply_scratch_elems(const Hbs& H, int c);
+void hbs_apply_fused(cudaStream_t st, const Hbs& H, bool trans, const double* X, int ldx,
+                     double* Y, int ldy, int c, double* scratch);
 void hbs_make_f32(Handle& h, Hbs& H);
 size_t hbs_nbytes(const Hbs& H, int which);
 
