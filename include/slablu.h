@@ -165,6 +165,16 @@ int slu_gemm_batched(slu_handle_t h, int transa, int transb, int M, int N, int K
                      const double* A, int lda, long long sA, const double* B, int ldb,
                      long long sB, double beta, double* C, int ldc, long long sC, int nb);
 
+/* C = alpha A B + beta C (A M x K, B K x N, C M x N; row-major float64) on the
+ * tcgen05 tensor cores as a split-BF16x3 product with float32 accumulation
+ * (relative accuracy of a float32 GEMM).  For the mixed-precision path's
+ * dense sampling and Schur products (matAssembly/matAssembler.py:115-116,
+ * direct_solve/omsdirectsolve.py:316-324); the float64 path does not use it.
+ * A wait timeout inside the kernel is reported by slu_sync as
+ * SLU_ERR_TIMEOUT. */
+int slu_gemm_split3(slu_handle_t h, int M, int N, int K, double alpha, const double* A, int lda,
+                    const double* B, int ldb, double beta, double* C, int ldc);
+
 /* ---------------------------------------------------------------- block tridiagonal
  * Dense red-black cyclic reduction (direct_solve/omsdirectsolve.py:177-333,
  * RedBlackSolver.factorize / solve) of nblk blocks of size m: SiM[i] couples

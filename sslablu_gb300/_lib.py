@@ -47,6 +47,7 @@ SIGNATURES = {
                      c_int, c_int],
     "slu_gemm_batched": [P, c_int, c_int, c_int, c_int, c_int, c_double, P, c_int, c_longlong, P,
                          c_int, c_longlong, c_double, P, c_int, c_longlong, c_int],
+    "slu_gemm_split3": [P, c_int, c_int, c_int, c_double, P, c_int, P, c_int, c_double, P, c_int],
     "slu_rb_factor": [P, c_int, c_int, P, P, P, ctypes.POINTER(c_void_p)],
     "slu_rb_solve": [P, P, P, c_int, c_int],
     "slu_rb_destroy": [P],

@@ -131,6 +131,12 @@ int slu_sync(slu_handle_t h) {
     SLU_CHECK_CUDA(cudaMemcpy(info, h->h.info.p, sizeof(info), cudaMemcpyDeviceToHost));
   });
   if (st != SLU_OK) return st;
+  if (info[1] != 0) {
+    cudaMemset(h->h.info.p, 0, sizeof(info));
+    g_err = "a tensor-core GEMM gave up waiting on its TMA / MMA pipeline";
+    h->h.last_error = g_err;
+    return SLU_ERR_TIMEOUT;
+  }
   if (info[0] != 0) {
     cudaMemset(h->h.info.p, 0, sizeof(info));
     g_err = "a device-side factorisation reported a failure (zero pivot or Jacobi sweep limit)";
@@ -441,6 +447,18 @@ int slu_gemm_batched(slu_handle_t h, int transa, int transb, int M, int N, int K
     SLU_REQUIRE(h && A && B && C, "null argument");
     slu::gemm_batched<double>(h->h.stream, transa != 0, transb != 0, M, N, K, alpha, A, lda, sA,
                               0, B, ldb, sB, 0, beta, C, ldc, sC, 0, nb, 1);
+  });
+}
+
+int slu_gemm_split3(slu_handle_t h, int M, int N, int K, double alpha, const double* A, int lda,
+                    const double* B, int ldb, double beta, double* C, int ldc) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h && A && B && C, "null argument");
+    SLU_REQUIRE(M >= 0 && N >= 0 && K >= 1 && lda >= K && ldb >= N && ldc >= N, "bad shape");
+    h->h.ws.reserve(slu::tc_gemm_workspace_bytes(M, N, K), h->h.stream);
+    void* ws = h->h.ws.take<char>(slu::tc_gemm_workspace_bytes(M, N, K) - 256);
+    slu::tc_gemm_split3(h->h.stream, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, ws,
+                        reinterpret_cast<unsigned int*>(h->h.info.as<int>()) + 1);
   });
 }
 

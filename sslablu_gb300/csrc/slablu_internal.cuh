@@ -175,6 +175,13 @@ void extract_upper(cudaStream_t st, int r0, int nr, int c0, int nc, const double
 void copy_blocks(cudaStream_t st, int nblk, long long width, const void* src, long long spitch,
                  void* dst, long long dpitch);  // bytes
 
+// Split-BF16x3 tensor-core GEMM (tc_gemm.cu): C = alpha A B + beta C, row-major
+// float64 in and out, float32 accumulation; ws of tc_gemm_workspace_bytes.
+size_t tc_gemm_workspace_bytes(int M, int N, int K);
+void tc_gemm_split3(cudaStream_t st, int M, int N, int K, double alpha, const double* A, int lda,
+                    const double* B, int ldb, double beta, double* C, int ldc, void* ws,
+                    unsigned int* err);
+
 int num_sms();
 
 }  // namespace slu
