@@ -185,6 +185,19 @@ int slu_rb_factor(slu_handle_t h, int nblk, int m, const double* SiM, const doub
                   const double* T, slu_rb_t* out);
 /* B (nblk*m x nrhs, ldb) <- solution, in place. */
 int slu_rb_solve(slu_handle_t h, slu_rb_t rb, double* B, int ldb, int nrhs);
+/* Mixed-precision variant of slu_rb_factor: the Schur-complement products of
+ * every level (SiM_i T^{-1} [SiM|SiP], omsdirectsolve.py:316-324) run on the
+ * tcgen05 tensor cores (slu_gemm_split3); pivot-block LU factors and solves
+ * stay float64.  Use with slu_rb_refine. */
+int slu_rb_factor_mixed(slu_handle_t h, int nblk, int m, const double* SiM, const double* SiP,
+                        const double* T, slu_rb_t* out);
+/* Iterative refinement of A x = b with the red-black factors and a float64
+ * residual of the stored block-tridiagonal system (no upstream counterpart:
+ * the mixed path's outer loop).  X (nblk*m x nrhs) receives the solution;
+ * stops when every column has ||b - A x|| / ||b|| <= tol or after maxit
+ * solves (then SLU_ERR_NOT_CONVERGED). */
+int slu_rb_refine(slu_handle_t h, slu_rb_t rb, const double* B, int ldb, double* X, int ldx,
+                  int nrhs, double tol, int maxit, int* iters_out, double* relres_out);
 int slu_rb_destroy(slu_rb_t rb);
 
 /* Dense block Thomas (direct_solve/omsdirectsolve.py:48-141,

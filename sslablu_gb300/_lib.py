@@ -50,6 +50,8 @@ SIGNATURES = {
     "slu_gemm_split3": [P, c_int, c_int, c_int, c_double, P, c_int, P, c_int, c_double, P, c_int],
     "slu_rb_factor": [P, c_int, c_int, P, P, P, ctypes.POINTER(c_void_p)],
     "slu_rb_solve": [P, P, P, c_int, c_int],
+    "slu_rb_factor_mixed": [P, c_int, c_int, P, P, P, ctypes.POINTER(c_void_p)],
+    "slu_rb_refine": [P, P, P, c_int, P, c_int, c_int, c_double, c_int, P, P],
     "slu_rb_destroy": [P],
     "slu_thomas_factor": [P, c_int, c_int, P, P, P, ctypes.POINTER(c_void_p)],
     "slu_thomas_solve": [P, P, P, c_int, c_int],
@@ -122,20 +124,19 @@ _handles = _HandleCache()
 
 
 def handle():
-    """Per-thread, per-device handle bound to torch's current stream."""
+    """Per-thread handle for torch's current device and stream (one handle per
+    stream, so work on different streams never shares a scratch arena)."""
     import torch
     dev = torch.cuda.current_device()
     stream = torch.cuda.current_stream(dev).cuda_stream
-    h = _handles.handles.get(dev)
+    key = (dev, stream)
+    h = _handles.handles.get(key)
     if h is None:
         out = c_void_p()
         check(lib().slu_create(c_void_p(stream), ctypes.byref(out)))
-        h = [out, stream]
-        _handles.handles[dev] = h
-    elif h[1] != stream:
-        check(lib().slu_set_stream(h[0], c_void_p(stream)))
-        h[1] = stream
-    return h[0]
+        h = out
+        _handles.handles[key] = h
+    return h
 
 
 def sync():

@@ -473,6 +473,26 @@ int slu_rb_factor(slu_handle_t h, int nblk, int m, const double* SiM, const doub
   });
 }
 
+int slu_rb_factor_mixed(slu_handle_t h, int nblk, int m, const double* SiM, const double* SiP,
+                        const double* T, slu_rb_t* out) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h && SiM && SiP && T && out, "null argument");
+    auto p = std::make_unique<slu_dense_rb_s>();
+    slu::rb_factor(h->h, p->S, nblk, m, SiM, SiP, T, true);
+    *out = p.release();
+  });
+}
+
+int slu_rb_refine(slu_handle_t h, slu_rb_t rb, const double* B, int ldb, double* X, int ldx,
+                  int nrhs, double tol, int maxit, int* iters_out, double* relres_out) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h && rb && B && X, "null argument");
+    SLU_REQUIRE(!rb->thomas, "handle was made by slu_thomas_factor");
+    SLU_REQUIRE(nrhs >= 1 && ldb >= nrhs && ldx >= nrhs && maxit >= 1, "bad arguments");
+    slu::rb_refine(h->h, rb->S, B, ldb, X, ldx, nrhs, tol, maxit, iters_out, relres_out);
+  });
+}
+
 int slu_rb_solve(slu_handle_t h, slu_rb_t rb, double* B, int ldb, int nrhs) {
   return guard(h, [&] {
     SLU_REQUIRE(h && rb && B, "null argument");

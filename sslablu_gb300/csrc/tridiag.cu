@@ -17,6 +17,7 @@
 #include "tridiag.cuh"
 
 #include <algorithm>
+#include <cmath>
 
 namespace slu {
 namespace {
@@ -25,12 +26,15 @@ inline int* ip(const DevBuf& b) { return b.as<int>(); }
 }  // namespace
 
 void rb_factor(Handle& h, RbSolver& S, int nblk, int m, const double* SiM, const double* SiP,
-               const double* T) {
+               const double* T, bool mixed) {
   cudaStream_t st = h.stream;
   SLU_REQUIRE(nblk >= 1 && (nblk & (nblk - 1)) == 0, "red-black needs a power-of-two block count");
   SLU_REQUIRE(m >= 1, "bad block size");
   S.m = m;
   S.nblk = nblk;
+  S.mixed = mixed;
+  DevBuf tcws;
+  if (mixed) tcws.alloc(tc_gemm_workspace_bytes(m, 2 * m, m), st);
   S.levels.clear();
   const size_t mm = (size_t)m * m;
   // level 0: copies, with the boundary couplings zeroed (omsdirectsolve.py:207-209)
@@ -73,12 +77,24 @@ void rb_factor(Handle& h, RbSolver& S, int nblk, int m, const double* SiM, const
     lu_solve<double>(st, false, m, dp(P.LU) + mm, m, 2 * mm, ip(P.piv) + m, 2 * m, X, (int)m2,
                      2 * mm, (int)m2, nR);
     // G1_j = SiM_{2j} X_{2j-1} (j >= 1; SiM_0 is zero), G2_j = SiP_{2j} X_{2j+1}
-    if (nR > 1)
-      gemm_batched<double>(st, false, false, m, (int)m2, m, 1.0, dp(P.SiM) + 2 * mm, m, 2 * mm, 0,
-                           X, (int)m2, 2 * mm, 0, 0.0, G1 + 2 * mm, (int)m2, 2 * mm, 0, nR - 1);
+    if (!mixed) {
+      if (nR > 1)
+        gemm_batched<double>(st, false, false, m, (int)m2, m, 1.0, dp(P.SiM) + 2 * mm, m, 2 * mm,
+                             0, X, (int)m2, 2 * mm, 0, 0.0, G1 + 2 * mm, (int)m2, 2 * mm, 0,
+                             nR - 1);
+      gemm_batched<double>(st, false, false, m, (int)m2, m, 1.0, dp(P.SiP), m, 2 * mm, 0, X,
+                           (int)m2, 2 * mm, 0, 0.0, G2, (int)m2, 2 * mm, 0, nR);
+    } else {
+      // Schur products on the tensor cores (split-BF16x3, float32 accumulation)
+      unsigned int* err = reinterpret_cast<unsigned int*>(h.info.as<int>()) + 1;
+      for (int j = 1; j < nR; ++j)
+        tc_gemm_split3(st, m, (int)m2, m, 1.0, dp(P.SiM) + 2 * j * mm, m, X + 2 * (j - 1) * mm,
+                       (int)m2, 0.0, G1 + 2 * j * mm, (int)m2, tcws.p, err);
+      for (int j = 0; j < nR; ++j)
+        tc_gemm_split3(st, m, (int)m2, m, 1.0, dp(P.SiP) + 2 * j * mm, m, X + 2 * j * mm,
+                       (int)m2, 0.0, G2 + 2 * j * mm, (int)m2, tcws.p, err);
+    }
     SLU_CHECK_CUDA(cudaMemsetAsync(G1, 0, 8 * 2 * mm, st));
-    gemm_batched<double>(st, false, false, m, (int)m2, m, 1.0, dp(P.SiP), m, 2 * mm, 0, X, (int)m2,
-                         2 * mm, 0, 0.0, G2, (int)m2, 2 * mm, 0, nR);
     // A = -G1[:, :m]; C = -G2[:, m:]; B = T_even - G1[:, m:] - G2[:, :m]
     copy_batched<double>(st, m, m, dp(P.T), m, 2 * mm, 0, dp(N.T), m, mm, 0, nR);
     add_batched<double>(st, m, m, -1.0, G1 + m, (int)m2, 2 * mm, 0, dp(N.T), m, mm, 0, nR);
@@ -141,6 +157,88 @@ void rb_solve(Handle& h, const RbSolver& S, double* B, int ldb, int c) {
     copy_batched<double>(st, m, c, v[l], c, mc, 0, v[l - 1], c, 2 * mc, 0, nR);
   }
   copy_batched<double>(st, nblk * m, c, v[0], c, 0, 0, B, ldb, 0, 0, 1);
+}
+
+// ---------------------------------------------------------------- apply / refine
+void rb_apply(Handle& h, const RbSolver& S, const double* X, int ldx, double* Y, int ldy, int c) {
+  cudaStream_t st = h.stream;
+  const int m = S.m, n = S.nblk;
+  const size_t mm = (size_t)m * m;
+  const RbLevel& L0 = S.levels[0];
+  const long long bx = (long long)m * ldx, by = (long long)m * ldy;
+  // Y_i = T_i X_i + SiM_i X_{i-1} + SiP_i X_{i+1}  (SiM_0 = SiP_{n-1} = 0)
+  gemm_batched<double>(st, false, false, m, c, m, 1.0, dp(L0.T), m, mm, 0, X, ldx, bx, 0, 0.0, Y,
+                       ldy, by, 0, n);
+  if (n > 1) {
+    gemm_batched<double>(st, false, false, m, c, m, 1.0, dp(L0.SiM) + mm, m, mm, 0, X, ldx, bx, 0,
+                         1.0, Y + by, ldy, by, 0, n - 1);
+    gemm_batched<double>(st, false, false, m, c, m, 1.0, dp(L0.SiP), m, mm, 0, X + bx, ldx, bx, 0,
+                         1.0, Y, ldy, by, 0, n - 1);
+  }
+}
+
+namespace {
+__global__ void colnorm2_rb(int rows, int cols, const double* __restrict__ A, int lda,
+                            double* __restrict__ out) {
+  const int c = blockIdx.x;
+  double s = 0.0;
+  for (int i = threadIdx.x; i < rows; i += blockDim.x) {
+    double v = A[(long long)i * lda + c];
+    s += v * v;
+  }
+  __shared__ double red[32];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    out[c] = t;
+  }
+}
+}  // namespace
+
+void rb_refine(Handle& h, const RbSolver& S, const double* B, int ldb, double* X, int ldx, int c,
+               double tol, int maxit, int* iters, double* relres) {
+  cudaStream_t st = h.stream;
+  const int N = S.m * S.nblk;
+  DevBuf rb, db, nb;
+  rb.alloc(8 * (size_t)N * c, st);
+  db.alloc(8 * (size_t)N * c, st);
+  nb.alloc(8 * 2 * (size_t)c, st);
+  double* r = rb.as<double>();
+  double* d = db.as<double>();
+  double* bn = nb.as<double>();
+  double* rn = bn + c;
+  colnorm2_rb<<<c, 256, 0, st>>>(N, c, B, ldb, bn);
+  check_launch("colnorm2_rb");
+  std::vector<double> hb(c), hr(c);
+  SLU_CHECK_CUDA(cudaMemcpyAsync(hb.data(), bn, 8 * c, cudaMemcpyDeviceToHost, st));
+  // x0 = A~^{-1} b
+  copy_batched<double>(st, N, c, B, ldb, 0, 0, X, ldx, 0, 0, 1);
+  rb_solve(h, S, X, ldx, c);
+  int it = 1;
+  double worst = 0.0;
+  for (;;) {
+    rb_apply(h, S, X, ldx, r, c, c);                 // r = A x
+    add_batched<double>(st, N, c, -1.0, B, ldb, 0, 0, r, c, 0, 0, 1);   // r = A x - b
+    colnorm2_rb<<<c, 256, 0, st>>>(N, c, r, c, rn);
+    check_launch("colnorm2_rb");
+    SLU_CHECK_CUDA(cudaMemcpyAsync(hr.data(), rn, 8 * c, cudaMemcpyDeviceToHost, st));
+    SLU_CHECK_CUDA(cudaStreamSynchronize(st));
+    worst = 0.0;
+    for (int j = 0; j < c; ++j)
+      worst = std::max(worst, std::sqrt(hr[j]) / (hb[j] > 0 ? std::sqrt(hb[j]) : 1.0));
+    if (worst <= tol || it >= maxit) break;
+    // x -= A~^{-1} (A x - b)
+    copy_batched<double>(st, N, c, r, c, 0, 0, d, c, 0, 0, 1);
+    rb_solve(h, S, d, c, c);
+    add_batched<double>(st, N, c, -1.0, d, c, 0, 0, X, ldx, 0, 0, 1);
+    ++it;
+  }
+  if (iters) *iters = it;
+  if (relres) *relres = worst;
+  if (worst > tol) throw Error(SLU_ERR_NOT_CONVERGED, "red-black refinement did not reach the tolerance");
 }
 
 // ---------------------------------------------------------------- Thomas

@@ -152,10 +152,25 @@ class BlockTridiagonalSolver(_DeviceTridiag, DirectSolver):
 
 
 class RedBlackSolver(_DeviceTridiag, DirectSolver):
-    """Red-black cyclic reduction, omsdirectsolve.py:177-333 (non-cyclic)."""
+    """Red-black cyclic reduction, omsdirectsolve.py:177-333 (non-cyclic).
+
+    precision='mixed' (beyond upstream): the Schur-complement products of the
+    elimination run on the tensor cores (split-BF16x3, slu_rb_factor_mixed),
+    pivot blocks stay float64, and solve() refines against the float64 system
+    until ||b - A x|| / ||b|| <= tol per column (slu_rb_refine); the last
+    iteration count and relative residual are kept in .iters / .relres.
+    """
 
     _factor_fn = "slu_rb_factor"
     _solve_fn = "slu_rb_solve"
+
+    def __init__(self, m, cyclic=False, precision="f64", tol=1e-10, maxit=20):
+        super().__init__(m, cyclic)
+        if precision not in ("f64", "mixed"):
+            raise ValueError("precision must be 'f64' or 'mixed'")
+        self.precision, self.tol, self.maxit = precision, tol, maxit
+        if precision == "mixed":
+            self._factor_fn = "slu_rb_factor_mixed"
 
     def factorize(self, S_rk_list, T):
         n = len(S_rk_list)
@@ -169,4 +184,13 @@ class RedBlackSolver(_DeviceTridiag, DirectSolver):
 
     def solve(self, rhs):
         B, one = dv.prepare_rhs(rhs)
+        if self.precision == "mixed":
+            import ctypes
+            X = torch.empty_like(B)
+            it, rr = ctypes.c_int(), ctypes.c_double()
+            L.check(L.lib().slu_rb_refine(L.handle(), self._h, L.ptr(B), B.shape[1], L.ptr(X),
+                                          X.shape[1], B.shape[1], float(self.tol),
+                                          int(self.maxit), ctypes.byref(it), ctypes.byref(rr)))
+            self.iters, self.relres = it.value, rr.value
+            return dv.finish(X, rhs, one)
         return dv.finish(self._solve_dev(B.clone()), rhs, one)

@@ -62,3 +62,33 @@ def test_rb_non_power_of_two_raises():
     S, T, _, _ = test_rb_system(3, 2)
     with pytest.raises(ValueError):
         RedBlackSolver(2).factorize(S, T)
+
+
+def test_rb_mixed_c1_poisson(golden):
+    """Mixed red-black (tensor-core Schur products, float64 pivots, float64
+    refinement) reaches 1e-10 and matches the upstream float64 solution."""
+    need_gpu()
+    from sslablu_gb300.direct_solve.omsdirectsolve import RedBlackSolver
+    g = golden("c1_poisson64")
+    n = g["Sl"].shape[0]
+    nc = int(g["nc"])
+    Sp = [[g["Sl"][i], g["Sr"][i]] for i in range(n)] + [[np.zeros((nc, nc))] * 2]
+    rb = RedBlackSolver(nc, precision="mixed", tol=1e-10)
+    rb.factorize(Sp, [np.eye(nc)] * (n + 1))
+    b = np.concatenate([g["rhs"], np.zeros(nc)])
+    x = rb.solve(b)
+    assert rb.relres <= 1e-10
+    assert relerr(x, g["x_rb"]) < 1e-10
+
+
+def test_rb_mixed_cases(golden):
+    need_gpu()
+    from sslablu_gb300.direct_solve.omsdirectsolve import RedBlackSolver
+    g = golden("rb_dense")
+    for nS, m in g["cases"]:
+        S, T, mat, rhs = test_rb_system(int(nS), int(m))
+        rb = RedBlackSolver(int(m), precision="mixed")
+        rb.factorize(S, T)
+        x = rb.solve(rhs)
+        assert rb.relres <= 1e-10
+        assert relerr(x, g["x_np_%d_%d" % (nS, m)]) < 1e-10
