@@ -126,9 +126,11 @@ int slu_ulv_solve_noalloc(slu_handle_t h, slu_hbs_t op, double* B, int ldb, int 
 int slu_hbs_prepare_f32(slu_handle_t h, slu_hbs_t op);
 int slu_ulv_solve_f32(slu_handle_t h, slu_hbs_t op, float* B, int ldb, int nrhs, int trans);
 
-/* Iterative refinement of A x = b with float32 ULV solves and a float64
- * residual r = b - A x computed with the stored HBS factors (the operator the
- * upstream solve inverts).  X holds the result (N x nrhs); iterations stop
+/* Iterative refinement of A x = b with float32 ULV solves and a float64-
+ * accurate residual r = b - A x of the stored HBS factors (the operator the
+ * upstream solve inverts), evaluated in double-float arithmetic (factors as
+ * float32 hi/lo pairs, error-free products and sums: ~1e-14 relative) on the
+ * float32 units.  X holds the result (N x nrhs); iterations stop
  * when every column reaches ||r||/||b|| <= tol or after maxit corrections.
  * iters_out / relres_out (host pointers, may be NULL) receive the iteration
  * count and the largest final relative residual. */

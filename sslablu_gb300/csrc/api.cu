@@ -22,62 +22,6 @@ int guard(slu_handle_t h, F&& f) {
   return slu::guard_call(h, static_cast<F&&>(f));
 }
 
-// per-column squared 2-norms of an rows x cols row-major array
-__global__ void colnorm2_kernel(int rows, int cols, const double* __restrict__ A, int lda,
-                                double* __restrict__ out) {
-  const int c = blockIdx.x;
-  double s = 0.0;
-  for (int i = threadIdx.x; i < rows; i += blockDim.x) {
-    double v = A[(long long)i * lda + c];
-    s += v * v;
-  }
-  __shared__ double red[32];
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
-    out[c] = t;
-  }
-}
-
-// y = b - y  (rows x cols, leading dims)
-__global__ void residual_kernel(int rows, int cols, const double* __restrict__ b, int ldb,
-                                double* __restrict__ y, int ldy) {
-  long long n = (long long)rows * cols;
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
-       e += (long long)gridDim.x * blockDim.x) {
-    int i = (int)(e / cols), j = (int)(e % cols);
-    y[(long long)i * ldy + j] = b[(long long)i * ldb + j] - y[(long long)i * ldy + j];
-  }
-}
-// x += (double) d ; d float rows x cols dense (ld cols)
-__global__ void accum_kernel(int rows, int cols, const float* __restrict__ d, double* __restrict__ x,
-                             int ldx, int init) {
-  long long n = (long long)rows * cols;
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
-       e += (long long)gridDim.x * blockDim.x) {
-    int i = (int)(e / cols), j = (int)(e % cols);
-    double v = (double)d[e];
-    double* p = x + (long long)i * ldx + j;
-    *p = init ? v : *p + v;
-  }
-}
-// f = (float) r  (r ld ldr -> f dense)
-__global__ void tofloat_kernel(int rows, int cols, const double* __restrict__ r, int ldr,
-                               float* __restrict__ f) {
-  long long n = (long long)rows * cols;
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
-       e += (long long)gridDim.x * blockDim.x) {
-    int i = (int)(e / cols), j = (int)(e % cols);
-    f[e] = (float)r[(long long)i * ldr + j];
-  }
-}
-inline int gsz(long long n) {
-  long long g = (n + 255) / 256;
-  return (int)(g < 1 ? 1 : (g > 4096 ? 4096 : g));
-}
 }  // namespace
 
 extern "C" {
@@ -238,6 +182,8 @@ int slu_hbs_set_level(slu_handle_t h, slu_hbs_t op, int level, int Nb, int n, in
       H.has_mats = true;
       H.has_ulv = false;
       H.has_f32 = false;
+      H.has_df = false;
+      H.invalidate_plans();
     }
   });
 }
@@ -271,6 +217,7 @@ int slu_hbs_set_ulv_level(slu_handle_t h, slu_hbs_t op, int level, const double*
     for (int t = 0; t < H.L; ++t) all = all && H.lv[t].Q.p && H.lv[t].R.p;
     H.has_ulv = all;
     H.has_f32 = false;
+    H.invalidate_plans();
   });
 }
 
@@ -318,52 +265,7 @@ int slu_refine(slu_handle_t h, slu_hbs_t op, const double* B, int ldb, double* X
   return guard(h, [&] {
     SLU_REQUIRE(h && op && B && X, "null argument");
     SLU_REQUIRE(nrhs >= 1 && ldb >= nrhs && ldx >= nrhs && maxit >= 1, "bad arguments");
-    slu::Hbs& H = op->H;
-    if (!H.has_f32) slu::hbs_make_f32(h->h, H);
-    cudaStream_t st = h->h.stream;
-    const int N = H.N, c = nrhs;
-    // own buffers: the apply/solve calls reuse the handle workspace
-    slu::DevBuf rbuf, fbuf, nbuf;
-    rbuf.alloc(8 * (size_t)N * c, st);
-    fbuf.alloc(4 * (size_t)N * c, st);
-    nbuf.alloc(8 * 2 * (size_t)c, st);
-    double* r = rbuf.as<double>();
-    float* f = fbuf.as<float>();
-    double* bn = nbuf.as<double>();
-    double* rn = bn + c;
-    colnorm2_kernel<<<c, 256, 0, st>>>(N, c, B, ldb, bn); ++slu::launch_counter();
-    std::vector<double> hb(c), hr(c);
-    SLU_CHECK_CUDA(cudaMemcpyAsync(hb.data(), bn, 8 * c, cudaMemcpyDeviceToHost, st));
-    const long long nel = (long long)N * c;
-    tofloat_kernel<<<gsz(nel), 256, 0, st>>>(N, c, B, ldb, f); ++slu::launch_counter();
-    int it = 0;
-    double worst = 0.0;
-    for (;;) {
-      slu::hbs_solve<float>(h->h, H, false, f, c, c);
-      accum_kernel<<<gsz(nel), 256, 0, st>>>(N, c, f, X, ldx, it == 0); ++slu::launch_counter();
-      ++it;
-      slu::hbs_apply(h->h, H, false, X, ldx, r, c, c);
-      residual_kernel<<<gsz(nel), 256, 0, st>>>(N, c, B, ldb, r, c); ++slu::launch_counter();
-      // the first correction never meets a float64-level tolerance from a
-      // float32 solve, so the host looks at the residual from the second
-      // correction on (one synchronisation per check)
-      if (it >= 2 || it >= maxit || tol >= 1e-6) {
-        colnorm2_kernel<<<c, 256, 0, st>>>(N, c, r, c, rn); ++slu::launch_counter();
-        SLU_CHECK_CUDA(cudaMemcpyAsync(hr.data(), rn, 8 * c, cudaMemcpyDeviceToHost, st));
-        SLU_CHECK_CUDA(cudaStreamSynchronize(st));
-        worst = 0.0;
-        for (int j = 0; j < c; ++j) {
-          double den = hb[j] > 0 ? std::sqrt(hb[j]) : 1.0;
-          worst = std::max(worst, std::sqrt(hr[j]) / den);
-        }
-        if (worst <= tol || it >= maxit) break;
-      }
-      tofloat_kernel<<<gsz(nel), 256, 0, st>>>(N, c, r, c, f); ++slu::launch_counter();
-    }
-    slu::check_launch("refine kernels");
-    if (iters_out) *iters_out = it;
-    if (relres_out) *relres_out = worst;
-    if (worst > tol) throw slu::Error(SLU_ERR_NOT_CONVERGED, "refinement did not reach the tolerance");
+    slu::hbs_refine(h->h, op->H, B, ldb, X, ldx, nrhs, tol, maxit, iters_out, relres_out);
   });
 }
 

@@ -352,6 +352,8 @@ void hbs_compress(Handle& h, Hbs& H, int Nb0, int rk, int s, const double* Om, c
   H.has_mats = true;
   H.has_ulv = ulv;
   H.has_f32 = false;
+  H.has_df = false;
+  H.invalidate_plans();
 }
 
 // ============================================================== standalone ULV
@@ -398,6 +400,7 @@ void hbs_factor(Handle& h, Hbs& H) {
   }
   H.has_ulv = true;
   H.has_f32 = false;
+  H.invalidate_plans();
 }
 
 // ============================================================== apply
@@ -533,6 +536,7 @@ template void hbs_solve_scratch<float>(cudaStream_t, const Hbs&, bool, float*, i
 
 void hbs_make_f32(Handle& h, Hbs& H) {
   cudaStream_t st = h.stream;
+  H.invalidate_plans();
   SLU_REQUIRE(H.has_ulv, "HBS operator has no ULV factorisation");
   auto cp = [&](const DevBuf& src, DevBuf& dst) {
     size_t n = src.bytes / 8;

@@ -42,7 +42,11 @@ struct Level {
   DevBuf Q, W, R, Uu;   // Nb*n x n, Nb*n x n, Nb*nu x n, Nb*uu_rows x kU
   // single-precision copies of the solve factors (mixed-precision solve)
   DevBuf Uf, Df, Qf, Wf, Rf, Uuf;
+  // (hi, lo) float32 pairs of U, V, D (double-float residual apply)
+  DevBuf Uh, Ul, Vh, Vl, Dh, Dl;
 };
+
+struct RefinePlan;  // refine.cu: buffers + CUDA graphs of one refinement iteration
 
 struct Hbs {
   int N = 0, L = 0, fac = 2;
@@ -50,8 +54,12 @@ struct Hbs {
   DevBuf perm;                     // int64[N]
   bool identity_perm = true;
   std::vector<long long> NN;       // NNvec, L+1 entries
-  bool has_mats = false, has_ulv = false, has_f32 = false;
+  bool has_mats = false, has_ulv = false, has_f32 = false, has_df = false;
   int rk = 0, nsamples = 0;
+  // refinement plans per right-hand-side count; they capture factor pointers,
+  // so every change of the factors clears them (invalidate_plans)
+  std::map<int, std::shared_ptr<RefinePlan>> refine_plans;
+  void invalidate_plans() { refine_plans.clear(); }
 };
 
 // compression + interleaved ULV (HBSnew.HBSMAT.constructHBS_ULV)
@@ -81,6 +89,14 @@ size_t hbs_apply_scratch_elems(const Hbs& H, int c);
 void hbs_apply_fused(cudaStream_t st, const Hbs& H, bool trans, const double* X, int ldx,
                      double* Y, int ldy, int c, double* scratch);
 void hbs_make_f32(Handle& h, Hbs& H);
+// Mixed-precision refinement replayed as CUDA graphs (refine.cu).
+void hbs_refine(Handle& h, Hbs& H, const double* B, int ldb, double* X, int ldx, int c,
+                double tol, int maxit, int* iters, double* relres);
+// Double-float apply (hbs_apply_df.cu): factors split once by hbs_make_df.
+void hbs_make_df(Handle& h, Hbs& H);
+size_t hbs_apply_df_scratch_bytes(const Hbs& H, int c);
+void hbs_apply_df(cudaStream_t st, const Hbs& H, const double* X, int ldx, double* Y, int ldy,
+                  int c, void* scratch);
 size_t hbs_nbytes(const Hbs& H, int which);
 
 }  // namespace slu

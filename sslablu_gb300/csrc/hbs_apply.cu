@@ -131,9 +131,7 @@ int chunk64(int Nb, int c) {
 
 template <typename K>
 void set_smem(K kern, size_t bytes) {
-  if (bytes > 48 * 1024)
-    SLU_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)bytes));
+  ensure_smem(reinterpret_cast<const void*>(kern), bytes);
 }
 
 }  // namespace

@@ -8,11 +8,25 @@
 // (direct_solve/omsdirectsolve.py:211,333 lu_factor / lu_solve).
 #include "slablu_internal.cuh"
 
+#include <mutex>
+
 namespace slu {
 
 long long& launch_counter() {
   static long long n = 0;
   return n;
+}
+
+void ensure_smem(const void* kernel, size_t bytes) {
+  static std::mutex mu;
+  static std::map<const void*, size_t> done;
+  if (bytes <= 48 * 1024) return;
+  std::lock_guard<std::mutex> lock(mu);
+  size_t& cur = done[kernel];
+  if (cur >= bytes) return;
+  SLU_CHECK_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)bytes));
+  cur = bytes;
 }
 
 int num_sms() {
@@ -201,8 +215,7 @@ void trsm_upper(cudaStream_t st, bool trans, int n, const T* R, long long rRs, l
   SLU_REQUIRE((size_t)n * chunk * sizeof(T) <= 96 * 1024, "trsm block too large");
   size_t sm = (size_t)n * chunk * sizeof(T);
   auto kern = trsm_upper_kernel<T>;
-  if (sm > 48 * 1024)
-    SLU_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  ensure_smem((const void*)kern, sm);
   dim3 grid((nrhs + chunk - 1) / chunk, batch);
   kern<<<grid, 256, sm, st>>>(trans, n, R, rRs, rCs, sR, X, xRs, xCs, sX, nrhs, chunk);
   check_launch("trsm_upper_kernel");
@@ -392,8 +405,7 @@ void lu_solve(cudaStream_t st, bool trans, int n, const T* LU, int lda, long lon
   size_t sm = (size_t)n * chunk * sizeof(T);
   SLU_REQUIRE(sm <= 96 * 1024, "lu_solve block too large");
   auto kern = lu_solve_kernel<T>;
-  if (sm > 48 * 1024)
-    SLU_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  ensure_smem((const void*)kern, sm);
   dim3 grid((nrhs + chunk - 1) / chunk, batch);
   kern<<<grid, 256, sm, st>>>(trans, n, LU, lda, sA, piv, sP, X, ldx, sX, nrhs, chunk);
   check_launch("lu_solve_kernel");

@@ -1,0 +1,209 @@
+// Mixed-precision refinement of the HBS solve, replayed as CUDA graphs.
+//
+//   x0 = float32 ULV solve of b;  r = b - A x  (double-float apply)
+//   x += float32 ULV solve of r;  r = b - A x  ...
+// until ||r_j|| / ||b_j|| <= tol for every column j.
+//
+// One refinement iteration (cast, float32 fused ULV sweep, correction, double-
+// float residual, column norms, device-to-host copy of the norms) is captured
+// once per (operator, nrhs) into a CUDA graph over buffers that the plan owns,
+// and replayed; the host looks at the norms only from the second correction on
+// (a float32 solve alone never reaches a float64 tolerance), so a typical
+// refinement is two or three graph launches and one or two synchronisations.
+#include <cmath>
+
+#include "abi_types.cuh"
+
+namespace slu {
+namespace {
+
+__global__ void colnorm2_k(int rows, int cols, const double* __restrict__ A, int lda,
+                           double* __restrict__ out) {
+  const int c = blockIdx.x;
+  double s = 0.0;
+  for (int i = threadIdx.x; i < rows; i += blockDim.x) {
+    double v = A[(long long)i * lda + c];
+    s += v * v;
+  }
+  __shared__ double red[32];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    out[c] = t;
+  }
+}
+
+// f = (float) src (dense, ld cols)
+__global__ void to_f32_k(long long n, const double* __restrict__ src, float* __restrict__ f) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+       e += (long long)gridDim.x * blockDim.x)
+    f[e] = (float)src[e];
+}
+
+// x = f (init) or x += f
+__global__ void accum_k(long long n, const float* __restrict__ f, double* __restrict__ x, int init) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+       e += (long long)gridDim.x * blockDim.x)
+    x[e] = init ? (double)f[e] : x[e] + (double)f[e];
+}
+
+// r = b - r
+__global__ void resid_k(long long n, const double* __restrict__ b, double* __restrict__ r) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+       e += (long long)gridDim.x * blockDim.x)
+    r[e] = b[e] - r[e];
+}
+
+inline int gsz(long long n) {
+  long long g = (n + 255) / 256;
+  return (int)(g < 1 ? 1 : (g > 4096 ? 4096 : g));
+}
+
+}  // namespace
+
+struct RefinePlan {
+  int c = 0;
+  DevBuf B, X, r, f, bn, rn, solve_ws, df_ws;
+  double* host_norms = nullptr;   // pinned: [bn (c) | rn (c)]
+  cudaGraphExec_t first = nullptr, next = nullptr;
+  long long first_kernels = 0, next_kernels = 0;   // kernel nodes per graph
+  ~RefinePlan() {
+    if (first) cudaGraphExecDestroy(first);
+    if (next) cudaGraphExecDestroy(next);
+    if (host_norms) cudaFreeHost(host_norms);
+  }
+};
+
+namespace {
+
+void enqueue_iteration(cudaStream_t st, const Hbs& H, RefinePlan& P, bool first) {
+  const int N = H.N, c = P.c;
+  const long long n = (long long)N * c;
+  double* B = P.B.as<double>();
+  double* X = P.X.as<double>();
+  double* r = P.r.as<double>();
+  float* f = P.f.as<float>();
+  if (first) {
+    colnorm2_k<<<c, 256, 0, st>>>(N, c, B, c, P.bn.as<double>());
+    check_launch("colnorm2_k");
+    SLU_CHECK_CUDA(cudaMemcpyAsync(P.host_norms, P.bn.p, 8 * c, cudaMemcpyDeviceToHost, st));
+    to_f32_k<<<gsz(n), 256, 0, st>>>(n, B, f);
+  } else {
+    to_f32_k<<<gsz(n), 256, 0, st>>>(n, r, f);
+  }
+  check_launch("to_f32_k");
+  hbs_solve_scratch<float>(st, H, false, f, c, c, P.solve_ws.as<float>());
+  accum_k<<<gsz(n), 256, 0, st>>>(n, f, X, first ? 1 : 0);
+  check_launch("accum_k");
+  hbs_apply_df(st, H, X, c, r, c, c, P.df_ws.p);
+  resid_k<<<gsz(n), 256, 0, st>>>(n, B, r);
+  check_launch("resid_k");
+  colnorm2_k<<<c, 256, 0, st>>>(N, c, r, c, P.rn.as<double>());
+  check_launch("colnorm2_k");
+  SLU_CHECK_CUDA(cudaMemcpyAsync(P.host_norms + c, P.rn.p, 8 * c, cudaMemcpyDeviceToHost, st));
+}
+
+cudaGraphExec_t capture(cudaStream_t st, const Hbs& H, RefinePlan& P, bool first) {
+  cudaGraph_t g = nullptr;
+  SLU_CHECK_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  const long long n0 = launch_counter();
+  try {
+    enqueue_iteration(st, H, P, first);
+    // captured launches run when the graph is replayed: count them there
+    (first ? P.first_kernels : P.next_kernels) = launch_counter() - n0;
+    launch_counter() = n0;
+  } catch (...) {
+    cudaStreamEndCapture(st, &g);
+    if (g) cudaGraphDestroy(g);
+    throw;
+  }
+  SLU_CHECK_CUDA(cudaStreamEndCapture(st, &g));
+  cudaGraphExec_t ex = nullptr;
+  cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess)
+    throw Error(SLU_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+  return ex;
+}
+
+RefinePlan& plan_for(Handle& h, Hbs& H, int c) {
+  auto it = H.refine_plans.find(c);
+  if (it != H.refine_plans.end()) return *it->second;
+  cudaStream_t st = h.stream;
+  auto P = std::make_shared<RefinePlan>();
+  P->c = c;
+  const size_t n = (size_t)H.N * c;
+  P->B.alloc(8 * n, st);
+  P->X.alloc(8 * n, st);
+  P->r.alloc(8 * n, st);
+  P->f.alloc(4 * n, st);
+  P->bn.alloc(8 * (size_t)c, st);
+  P->rn.alloc(8 * (size_t)c, st);
+  P->solve_ws.alloc(hbs_solve_scratch_bytes(H, c, sizeof(float)), st);
+  P->df_ws.alloc(hbs_apply_df_scratch_bytes(H, c), st);
+  SLU_CHECK_CUDA(cudaMallocHost(&P->host_norms, 16 * (size_t)c));
+  SLU_CHECK_CUDA(cudaStreamSynchronize(st));
+  // an uncaptured run first: sets kernel attributes and validates the sequence
+  SLU_CHECK_CUDA(cudaMemsetAsync(P->B.p, 0, 8 * n, st));
+  enqueue_iteration(st, H, *P, true);
+  SLU_CHECK_CUDA(cudaStreamSynchronize(st));
+  // capture on a private stream (the caller's may be the legacy default
+  // stream, which cannot be captured); the graphs launch on the caller's
+  cudaStream_t cs = nullptr;
+  SLU_CHECK_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  try {
+    P->first = capture(cs, H, *P, true);
+    P->next = capture(cs, H, *P, false);
+  } catch (...) {
+    cudaStreamDestroy(cs);
+    throw;
+  }
+  SLU_CHECK_CUDA(cudaStreamDestroy(cs));
+  RefinePlan& ref = *P;
+  H.refine_plans[c] = P;
+  return ref;
+}
+
+}  // namespace
+
+void hbs_refine(Handle& h, Hbs& H, const double* B, int ldb, double* X, int ldx, int c,
+                double tol, int maxit, int* iters, double* relres) {
+  cudaStream_t st = h.stream;
+  if (!H.has_f32) hbs_make_f32(h, H);
+  if (!H.has_df) hbs_make_df(h, H);
+  RefinePlan& P = plan_for(h, H, c);
+  SLU_CHECK_CUDA(cudaMemcpy2DAsync(P.B.p, 8 * (size_t)c, B, 8 * (size_t)ldb, 8 * (size_t)c,
+                                   H.N, cudaMemcpyDeviceToDevice, st));
+  SLU_CHECK_CUDA(cudaGraphLaunch(P.first, st));
+  launch_counter() += P.first_kernels;
+  int it = 1;
+  double worst = 0.0;
+  for (;;) {
+    if (it < 2 && it < maxit && tol < 1e-6) {  // first correction without a check
+      SLU_CHECK_CUDA(cudaGraphLaunch(P.next, st));
+      launch_counter() += P.next_kernels;
+      ++it;
+      continue;
+    }
+    SLU_CHECK_CUDA(cudaStreamSynchronize(st));
+    worst = 0.0;
+    for (int j = 0; j < c; ++j) {
+      const double bj = P.host_norms[j], rj = P.host_norms[c + j];
+      worst = std::max(worst, std::sqrt(rj) / (bj > 0 ? std::sqrt(bj) : 1.0));
+    }
+    if (worst <= tol || it >= maxit) break;
+    SLU_CHECK_CUDA(cudaGraphLaunch(P.next, st));
+    launch_counter() += P.next_kernels;
+    ++it;
+  }
+  SLU_CHECK_CUDA(cudaMemcpy2DAsync(X, 8 * (size_t)ldx, P.X.p, 8 * (size_t)c, 8 * (size_t)c, H.N,
+                                   cudaMemcpyDeviceToDevice, st));
+  if (iters) *iters = it;
+  if (relres) *relres = worst;
+  if (worst > tol) throw Error(SLU_ERR_NOT_CONVERGED, "refinement did not reach the tolerance");
+}
+
+}  // namespace slu

@@ -8,6 +8,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string>
+#include <map>
+#include <memory>
 #include <vector>
 #include <stdexcept>
 
@@ -183,5 +185,9 @@ void tc_gemm_split3(cudaStream_t st, int M, int N, int K, double alpha, const do
                     unsigned int* err);
 
 int num_sms();
+
+// cudaFuncSetAttribute(MaxDynamicSharedMemorySize) only when a kernel needs
+// more than it was last given (cached; safe to call while a stream captures).
+void ensure_smem(const void* kernel, size_t bytes);
 
 }  // namespace slu

@@ -247,9 +247,7 @@ int chunk_for(int Nb, int c) {
 
 template <typename K>
 void set_smem(K kern, size_t bytes) {
-  if (bytes > 48 * 1024)
-    SLU_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)bytes));
+  ensure_smem(reinterpret_cast<const void*>(kern), bytes);
 }
 
 }  // namespace

@@ -94,3 +94,18 @@ def test_construct_factors_match(golden):
             if t > 0:   # rows are child skeleton coordinates (sign choice of the child SVD)
                 Pg, Pr = np.abs(Pg), np.abs(Pr)
             assert np.abs(Pg - Pr).max() < 1e-11
+
+
+def test_mixed_refinement_reaches_tolerance(golden):
+    """float32 ULV sweeps + double-float residuals reach 1e-10 (checked with the
+    float64 apply) and agree with the float64 solve."""
+    need_gpu()
+    g = golden("hbs_c2_n512")
+    S, Nbvec = hbs_from_fixture(g)
+    G = _gpu_hbs_from_oracle(S, Nbvec, 2)
+    G.compute_ULV()
+    x = g["x"]
+    xm, iters, rr = G.solve_refined(x, tol=1e-10, maxit=10)
+    assert rr <= 1e-10 and iters >= 2
+    assert relerr(G.matmat(xm), x) <= 1e-10
+    assert relerr(xm, G.solve(x)) < 1e-9
