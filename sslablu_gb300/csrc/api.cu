@@ -28,7 +28,7 @@ extern "C" {
 
 int slu_version(void) { return 1; }
 
-long long slu_launch_count(void) { return slu::launch_counter(); }
+long long slu_launch_count(void) { return slu::launch_total().load(); }
 
 int slu_last_error(char* buf, size_t len) {
   if (!buf || len == 0) return SLU_ERR_ARG;

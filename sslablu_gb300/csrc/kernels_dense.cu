@@ -12,8 +12,12 @@
 
 namespace slu {
 
-long long& launch_counter() {
-  static long long n = 0;
+std::atomic<long long>& launch_total() {
+  static std::atomic<long long> n{0};
+  return n;
+}
+long long& launch_thread() {
+  static thread_local long long n = 0;
   return n;
 }
 

@@ -109,12 +109,14 @@ void enqueue_iteration(cudaStream_t st, const Hbs& H, RefinePlan& P, bool first)
 cudaGraphExec_t capture(cudaStream_t st, const Hbs& H, RefinePlan& P, bool first) {
   cudaGraph_t g = nullptr;
   SLU_CHECK_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-  const long long n0 = launch_counter();
+  const long long n0 = launch_thread();
   try {
     enqueue_iteration(st, H, P, first);
     // captured launches run when the graph is replayed: count them there
-    (first ? P.first_kernels : P.next_kernels) = launch_counter() - n0;
-    launch_counter() = n0;
+    const long long d = launch_thread() - n0;
+    (first ? P.first_kernels : P.next_kernels) = d;
+    launch_thread() = n0;
+    launch_total() -= d;
   } catch (...) {
     cudaStreamEndCapture(st, &g);
     if (g) cudaGraphDestroy(g);
@@ -178,13 +180,13 @@ void hbs_refine(Handle& h, Hbs& H, const double* B, int ldb, double* X, int ldx,
   SLU_CHECK_CUDA(cudaMemcpy2DAsync(P.B.p, 8 * (size_t)c, B, 8 * (size_t)ldb, 8 * (size_t)c,
                                    H.N, cudaMemcpyDeviceToDevice, st));
   SLU_CHECK_CUDA(cudaGraphLaunch(P.first, st));
-  launch_counter() += P.first_kernels;
+  count_launches(P.first_kernels);
   int it = 1;
   double worst = 0.0;
   for (;;) {
     if (it < 2 && it < maxit && tol < 1e-6) {  // first correction without a check
       SLU_CHECK_CUDA(cudaGraphLaunch(P.next, st));
-      launch_counter() += P.next_kernels;
+      count_launches(P.next_kernels);
       ++it;
       continue;
     }
@@ -196,7 +198,7 @@ void hbs_refine(Handle& h, Hbs& H, const double* B, int ldb, double* X, int ldx,
     }
     if (worst <= tol || it >= maxit) break;
     SLU_CHECK_CUDA(cudaGraphLaunch(P.next, st));
-    launch_counter() += P.next_kernels;
+    count_launches(P.next_kernels);
     ++it;
   }
   SLU_CHECK_CUDA(cudaMemcpy2DAsync(X, 8 * (size_t)ldx, P.X.p, 8 * (size_t)c, 8 * (size_t)c, H.N,

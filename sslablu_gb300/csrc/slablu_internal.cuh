@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string>
+#include <atomic>
 #include <map>
 #include <memory>
 #include <vector>
@@ -40,10 +41,17 @@ struct Error : std::runtime_error {
 
 // Number of kernels this library has launched (host-side count; reported by
 // slu_launch_count so benchmarks can state how many of their kernels ran).
-long long& launch_counter();
+// launch_total() is process wide; launch_thread() is the calling thread's
+// share, used to discount launches recorded into a CUDA graph capture.
+std::atomic<long long>& launch_total();
+long long& launch_thread();
+inline void count_launches(long long n) {
+  launch_total() += n;
+  launch_thread() += n;
+}
 
 inline void check_launch(const char* what) {
-  ++launch_counter();
+  count_launches(1);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess)
     throw Error(SLU_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));

@@ -1,0 +1,266 @@
+"""Serving loop for resident factored slab operators.
+
+Factored operators (HBS ULV factors or red-black factors) stay resident in
+device memory under a byte budget; solve requests (an operator key and a host
+block of right-hand sides) arrive over time and are batched per operator.
+
+    srv = SolveServer(budget_bytes=8 << 30, workers=4, max_batch_rhs=64)
+    srv.admit("op0", factory, footprint)      # factory() -> factored operator
+    srv.run(requests)                         # requests: [Request(key, B, t_arrival)]
+    srv.stats()                               # latency p50/p99, RHS/s
+
+Scheduling (continuous batching):
+  * a dispatcher thread admits requests at their arrival time into per-
+    operator queues;
+  * whenever a worker is idle, the operator whose oldest pending request is
+    the oldest gets a batch: its pending requests concatenated up to
+    ``max_batch_rhs`` columns; requests that arrive while that batch runs join
+    a later one;
+  * at most one batch per operator is in flight (a factored operator's
+    solve plan is not shared between streams), different operators overlap
+    on different CUDA streams;
+  * each worker owns one CUDA stream and one library handle; a batch is
+    pinned host -> device copy, solve, device -> pinned host copy.
+
+Admission by footprint: ``admit`` factors an operator only when the resident
+footprint plus its own fits the budget; otherwise it waits (in FIFO order)
+until ``retire`` frees memory.
+
+A request's result is its block of the batch's solution: columns do not mix,
+so it equals a solve of the request alone (bit for bit on the float64 path,
+within the refinement tolerance on the mixed path, where the batch iterates
+until its worst column converges).
+"""
+import collections
+import queue
+import threading
+import time
+
+import numpy as np
+import torch
+
+
+class Request:
+    __slots__ = ("key", "B", "t_arrival", "t_start", "t_done", "X", "rid", "error")
+
+    def __init__(self, key, B, t_arrival=0.0, rid=None):
+        self.key = key
+        self.B = np.ascontiguousarray(B, dtype=np.float64)
+        if self.B.ndim == 1:
+            self.B = self.B[:, None]
+        self.t_arrival = float(t_arrival)
+        self.t_start = self.t_done = None
+        self.X = None
+        self.rid = rid
+        self.error = None
+
+    @property
+    def latency(self):
+        return None if self.t_done is None else self.t_done - self.t_arrival
+
+
+class Resident:
+    def __init__(self, key, op, footprint, solve):
+        self.key, self.op, self.footprint, self.solve = key, op, footprint, solve
+        self.busy = False
+        self.last_used = 0.0
+
+
+def hbs_solver(H, precision="f64", tol=1e-10, maxit=10):
+    """Device solve callable for a factored HBSMAT (ULV).  The mixed path pads
+    a batch to a power-of-two column count (zero columns converge at once) so
+    each operator keeps only a few refinement plans (CUDA graphs)."""
+    if precision == "f64":
+        return lambda X: H._dev_solve(X, False)
+
+    def mixed(X):
+        c = X.shape[1]
+        w = 1 << (c - 1).bit_length()
+        if w != c:
+            X = torch.cat([X, torch.zeros((X.shape[0], w - c), dtype=X.dtype, device=X.device)], 1)
+        x, _, _ = H.solve_refined(X.contiguous(), tol=tol, maxit=maxit)
+        return x[:, :c]
+    return mixed
+
+
+def rb_solver(rb):
+    """Device solve callable for a factored RedBlackSolver (either precision)."""
+    return lambda X: rb.solve(X)
+
+
+class SolveServer:
+    def __init__(self, budget_bytes, workers=4, max_batch_rhs=64):
+        self.budget = int(budget_bytes)
+        self.max_batch = int(max_batch_rhs)
+        self.resident = collections.OrderedDict()
+        self.waiting_admissions = collections.deque()
+        self.pending = collections.defaultdict(collections.deque)
+        self.done = []
+        self._lock = threading.Condition()
+        self._jobs = queue.Queue()
+        self._nworkers = workers
+        self._idle = workers
+        self._threads = []
+        self._stop = False
+        self._t0 = None
+        self.batches = 0
+        self.batch_rhs = []
+        for w in range(workers):
+            t = threading.Thread(target=self._worker, args=(w,), daemon=True)
+            t.start()
+            self._threads.append(t)
+
+    # ---------------------------------------------------------- admission
+    @property
+    def resident_bytes(self):
+        return sum(r.footprint for r in self.resident.values())
+
+    def admit(self, key, factory, footprint, solve_factory):
+        """Factor and keep `key` resident when the budget allows, else queue it.
+        factory() returns the factored operator; solve_factory(op) returns its
+        device solve callable X -> A^{-1} X."""
+        with self._lock:
+            self.waiting_admissions.append((key, factory, int(footprint), solve_factory))
+            self._admit_waiting()
+
+    def _admit_waiting(self):
+        while self.waiting_admissions:
+            key, factory, fp, sf = self.waiting_admissions[0]
+            if self.resident_bytes + fp > self.budget and self.resident:
+                return
+            self.waiting_admissions.popleft()
+            op = factory()
+            self.resident[key] = Resident(key, op, fp, sf(op))
+
+    def retire(self, key):
+        with self._lock:
+            r = self.resident.pop(key, None)
+            if r is not None:
+                del r.op
+            torch.cuda.empty_cache()
+            self._admit_waiting()
+
+    # ---------------------------------------------------------- scheduling
+    def _now(self):
+        return time.perf_counter() - self._t0
+
+    def _pick_batch(self):
+        best, best_t = None, None
+        for key, dq in self.pending.items():
+            if not dq:
+                continue
+            r = self.resident.get(key)
+            if r is None or r.busy:
+                continue
+            if best_t is None or dq[0].t_arrival < best_t:
+                best, best_t = key, dq[0].t_arrival
+        if best is None:
+            return None
+        dq = self.pending[best]
+        reqs, cols = [], 0
+        while dq and (not reqs or cols + dq[0].B.shape[1] <= self.max_batch):
+            r = dq.popleft()
+            reqs.append(r)
+            cols += r.B.shape[1]
+        self.resident[best].busy = True
+        return best, reqs
+
+    def _worker(self, w):
+        stream = torch.cuda.Stream()
+        while True:
+            job = self._jobs.get()
+            if job is None:
+                return
+            key, reqs = job
+            res = self.resident[key]
+            t_start = self._now()
+            try:
+                with torch.cuda.stream(stream):
+                    Bh = torch.from_numpy(np.concatenate([r.B for r in reqs], axis=1)).pin_memory()
+                    Bd = Bh.to("cuda", non_blocking=True)
+                    Xd = res.solve(Bd)
+                    Xh = torch.empty(Xd.shape, dtype=Xd.dtype, pin_memory=True)
+                    Xh.copy_(Xd, non_blocking=True)
+                    stream.synchronize()
+                X, err = Xh.numpy(), None
+            except Exception as e:   # the requests complete with the error
+                X, err = None, e
+            t_done = self._now()
+            c = 0
+            for r in reqs:
+                k = r.B.shape[1]
+                r.X = None if X is None else X[:, c:c + k].copy()
+                r.error = err
+                r.t_start, r.t_done = t_start, t_done
+                c += k
+            with self._lock:
+                res.busy = False
+                res.last_used = t_done
+                self.done.extend(reqs)
+                self.batches += 1
+                self.batch_rhs.append(c)
+                self._idle += 1
+                self._lock.notify_all()
+
+    def run(self, requests):
+        """Serve `requests` (sorted by t_arrival, seconds from the start);
+        returns when every request is done."""
+        reqs = sorted(requests, key=lambda r: r.t_arrival)
+        for r in reqs:
+            if r.key not in self.resident:
+                raise KeyError("operator %r is not resident" % (r.key,))
+        self.done = []
+        self.batches = 0
+        self.batch_rhs = []
+        self._t0 = time.perf_counter()
+        i, n = 0, len(reqs)
+        with self._lock:
+            while len(self.done) < n:
+                now = self._now()
+                while i < n and reqs[i].t_arrival <= now:
+                    self.pending[reqs[i].key].append(reqs[i])
+                    i += 1
+                dispatched = False
+                while self._idle > 0:
+                    b = self._pick_batch()
+                    if b is None:
+                        break
+                    self._idle -= 1
+                    self._jobs.put(b)
+                    dispatched = True
+                if dispatched:
+                    continue
+                wait = (reqs[i].t_arrival - now) if i < n else 0.05
+                self._lock.wait(timeout=max(1e-4, min(wait, 0.05)))
+        self.makespan = self._now()
+        return self.done
+
+    def stats(self):
+        lat = np.array([r.latency for r in self.done])
+        rhs = sum(r.B.shape[1] for r in self.done)
+        return {"requests": len(self.done), "rhs": int(rhs),
+                "makespan_s": self.makespan, "rhs_per_s": rhs / self.makespan,
+                "p50_ms": 1e3 * float(np.percentile(lat, 50)),
+                "p99_ms": 1e3 * float(np.percentile(lat, 99)),
+                "batches": self.batches,
+                "mean_batch_rhs": float(np.mean(self.batch_rhs)) if self.batch_rhs else 0.0}
+
+    def close(self):
+        for _ in self._threads:
+            self._jobs.put(None)
+        for t in self._threads:
+            t.join(timeout=10)
+
+
+def poisson_trace(keys, rate, count, rhs_range=(1, 64), seed=0, sizes=None):
+    """Seeded Poisson arrivals: `count` requests at `rate` req/s, each on a
+    uniformly chosen operator with U{rhs_range} right-hand sides ~ N(0, 1)."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, size=count))
+    out = []
+    for j in range(count):
+        key = keys[int(rng.integers(len(keys)))]
+        r = int(rng.integers(rhs_range[0], rhs_range[1] + 1))
+        n = sizes[key]
+        out.append(Request(key, rng.standard_normal((n, r)), t[j], rid=j))
+    return out
