@@ -264,3 +264,88 @@ def poisson_trace(keys, rate, count, rhs_range=(1, 64), seed=0, sizes=None):
         n = sizes[key]
         out.append(Request(key, rng.standard_normal((n, r)), t[j], rid=j))
     return out
+
+
+# ---------------------------------------------------------------------------
+# benchmark: python -m sslablu_gb300.serving [--operators 16 --requests 2000 ...]
+# ---------------------------------------------------------------------------
+def _build_hbs_ops(count, seed, sizes=(2048, 4096, 8192), shift=16.0):
+    """Exact synthetic HBS operators (leaf 64, rank 32, singular values 1 -> 1e-12),
+    compressed + ULV-factored on the device with the upstream sampling.  The
+    leaf diagonal blocks get `shift` * I (like the I + S interface systems of
+    the slab method) so that a 1e-10 relative residual is attainable in
+    float64 for every size."""
+    from .matAssembly.HBS.HBSnew import HBSMAT
+    import sys
+    import os
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    from oracle.hbs import gen_random_hbs
+    sigma = 10.0 ** (-12.0 * np.arange(32) / 31.0)
+    ops = []
+    for j in range(count):
+        N = sizes[j % len(sizes)]
+        L = int(np.log2(N // 64)) + 1
+        np.random.seed(seed + j)
+        S, Nbvec = gen_random_hbs(32, 64, L, quad=False, sigma=sigma)
+        D0 = S.Dmats[0].copy()
+        D0.reshape(-1, 64, 64)[:] += shift * np.eye(64)
+        A = HBSMAT().set_mats(S.Umats, [D0] + S.Dmats[1:], S.Vmats, list(Nbvec), fac=2)
+        H = HBSMAT(A, tree=None, quad=False)
+        H.set_Nbvec(list(Nbvec))
+        H.construct(32, True)
+        ops.append(("hbs%d_N%d" % (j, N), H, N))
+    return ops
+
+
+def main():
+    import argparse
+    import json
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--operators", type=int, default=16)
+    ap.add_argument("--requests", type=int, default=2000)
+    ap.add_argument("--rate", type=float, default=20000.0)
+    ap.add_argument("--workers", type=int, default=8)
+    ap.add_argument("--shift", type=float, default=16.0)
+    ap.add_argument("--max-batch", type=int, default=64)
+    ap.add_argument("--seed", type=int, default=20261205)
+    a = ap.parse_args()
+    ops = _build_hbs_ops(a.operators, a.seed, shift=a.shift)
+    sizes = {k: n for k, _, n in ops}
+    out = {"workload": "%d resident exact-HBS operators (N in 2048/4096/8192, leaf 64, rank 32, "
+                       "leaf shift %g), Poisson arrivals %.0f req/s, %d requests, 1-64 RHS each, "
+                       "%d worker streams" % (a.operators, a.shift, a.rate, a.requests, a.workers)}
+    # the plain trace warms the device first, then each arm serves the same trace
+    for precision in ("f64", "mixed"):
+        srv = SolveServer(budget_bytes=64 << 30, workers=a.workers, max_batch_rhs=a.max_batch)
+        try:
+            for key, H, n in ops:
+                srv.admit(key, lambda H=H: H, H.nbytes, lambda op, p=precision: hbs_solver(op, p))
+            warm = poisson_trace(list(sizes), a.rate, min(200, a.requests), seed=a.seed + 1,
+                                 sizes=sizes)
+            srv.run(warm)
+            trace = poisson_trace(list(sizes), a.rate, a.requests, seed=a.seed, sizes=sizes)
+            done = srv.run(trace)
+            st = srv.stats()
+            # relative residual of every served result against its operator
+            worst = 0.0
+            errs = [r.error for r in done if r.error is not None]
+            if errs:
+                st["first_error"] = repr(errs[0])
+            for r in done:
+                if r.error is not None:
+                    continue
+                H = dict((k, h) for k, h, _ in ops)[r.key]
+                R = r.B - H.matmat(r.X)
+                worst = max(worst, float(np.max(np.linalg.norm(R, axis=0) /
+                                                np.linalg.norm(r.B, axis=0))))
+            st["worst_relres"] = worst
+            st["errors"] = sum(r.error is not None for r in done)
+            out[precision] = st
+        finally:
+            srv.close()
+    out["mixed_vs_f64_rhs_per_s"] = out["mixed"]["rhs_per_s"] / out["f64"]["rhs_per_s"]
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()
