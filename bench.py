@@ -57,11 +57,12 @@ def sigma():
 
 
 def make_problem():
-    from oracle.hbs import gen_random_hbs
+    """(Umats, Dmats, Vmats), Nbvec and the right-hand sides of the workload."""
+    from sslablu_gb300.synthetic import random_hbs_factors
     np.random.seed(SEED)
-    S, Nbvec = gen_random_hbs(RANK, LEAF, LEVELS, quad=False, sigma=sigma())
+    U, D, V, Nbvec = random_hbs_factors(RANK, LEAF, LEVELS, quad=False, sigma=sigma())
     rhs = np.random.default_rng(SEED + 1).standard_normal((N, NRHS))
-    return S, Nbvec, rhs
+    return (U, D, V), Nbvec, rhs
 
 
 # ---------------------------------------------------------------- clocks
@@ -135,9 +136,10 @@ def cpu_time_solve(O, rhs, reps):
     return ts
 
 
-def cpu_baseline(S, Nbvec, rhs, budget_s=15.0):
+def cpu_baseline(mats, Nbvec, rhs, budget_s=15.0):
     """The CPU restatement of the upstream numpy ULV solve on the host cores."""
     from oracle.hbs import OracleHBS
+    S = OracleHBS().set_mats(mats[0], mats[1], mats[2], list(Nbvec), fac=2)
     np.random.seed(SEED + 7)
     t0 = time.perf_counter()
     O = OracleHBS(S, None, Nbvec[0], len(Nbvec), 2).construct(RANK)
@@ -156,8 +158,8 @@ def cpu_baseline(S, Nbvec, rhs, budget_s=15.0):
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    S, Nbvec, rhs = make_problem()
-    base = cpu_baseline(S, Nbvec, rhs, budget_s=max(5.0, 2.0 * args.steps / 10))
+    mats, Nbvec, rhs = make_problem()
+    base = cpu_baseline(mats, Nbvec, rhs, budget_s=max(5.0, 2.0 * args.steps / 10))
     line = {"metric": METRIC, "value": base["value"], "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": base["p50_ms"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -177,9 +179,9 @@ def run_gpu(args, rank, world):
 
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
-    S, Nbvec, rhs = make_problem()
+    mats, Nbvec, rhs = make_problem()
     # operator to compress: the exact HBS matrix, resident on the device
-    A = HBSMAT().set_mats(S.Umats, S.Dmats, S.Vmats, list(Nbvec), fac=2)
+    A = HBSMAT().set_mats(mats[0], mats[1], mats[2], list(Nbvec), fac=2)
     np.random.seed(SEED + 7)
     H = HBSMAT(A, tree=None, quad=False)
     H.set_Nbvec(list(Nbvec))
@@ -272,7 +274,7 @@ def run_gpu(args, rank, world):
     achieved = alg_bytes / p50 / 1e9
     line = None
     if rank == 0:
-        base = cpu_baseline(S, Nbvec, rhs)
+        base = cpu_baseline(mats, Nbvec, rhs)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup,

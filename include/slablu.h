@@ -137,6 +137,25 @@ int slu_ulv_solve_f32(slu_handle_t h, slu_hbs_t op, float* B, int ldb, int nrhs,
 int slu_refine(slu_handle_t h, slu_hbs_t op, const double* B, int ldb, double* X, int ldx,
                int nrhs, double tol, int maxit, int* iters_out, double* relres_out);
 
+/* Grouped solves over `count` operators of any sizes and depths, one kernel
+ * launch per tree step for the whole group (the batched form of calling
+ * HBSnew.HBSMAT.solve, matAssembly/HBS/HBSnew.py:393-416, once per operator;
+ * the reference has no grouped call).  Arrays are host arrays of `count`
+ * entries; B[i] / X[i] are device pointers to N_i x nrhs[i] row-major blocks
+ * with leading dimensions ldb[i] / ldx[i]; members with nrhs[i] == 0 are
+ * skipped.  Each member's result equals its own slu_ulv_solve (mode N) /
+ * slu_refine result: every member runs the same per-level arithmetic.
+ *   slu_ulv_solve_grouped: B[i] <- A_i^{-1} B[i] in float64.
+ *   slu_refine_grouped: X[i] from float32 sweeps refined by double-float
+ *     residuals until every column of every member reaches tol; iters_out
+ *     (may be NULL) receives the common iteration count and relres_out (may
+ *     be NULL, else count entries) each member's worst relative residual. */
+int slu_ulv_solve_grouped(slu_handle_t h, int count, const slu_hbs_t* ops, double* const* B,
+                          const int* ldb, const int* nrhs);
+int slu_refine_grouped(slu_handle_t h, int count, const slu_hbs_t* ops, const double* const* B,
+                       const int* ldb, double* const* X, const int* ldx, const int* nrhs,
+                       double tol, int maxit, int* iters_out, double* relres_out);
+
 /* Geometry: L, N and per level (Nb, n, k, nu) into levels[4*L]; NNvec[L+1]
  * (ULVsparse.compute_ULV's NNvec).  Host pointers, any may be NULL. */
 int slu_hbs_info(slu_hbs_t op, int* L, int* N, int* levels, long long* NNvec, int* nsamples);

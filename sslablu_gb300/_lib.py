@@ -39,6 +39,8 @@ SIGNATURES = {
     "slu_hbs_prepare_f32": [P, P],
     "slu_ulv_solve_f32": [P, P, P, c_int, c_int, c_int],
     "slu_refine": [P, P, P, c_int, P, c_int, c_int, c_double, c_int, P, P],
+    "slu_ulv_solve_grouped": [P, c_int, P, P, P, P],
+    "slu_refine_grouped": [P, c_int, P, P, P, P, P, P, c_double, c_int, P, P],
     "slu_hbs_info": [P, P, P, P, P, P],
     "slu_hbs_export": [P, P, c_int, c_int, P, c_size_t, P],
     "slu_hbs_nbytes": [P, c_int, P],

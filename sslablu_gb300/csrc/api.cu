@@ -269,6 +269,38 @@ int slu_refine(slu_handle_t h, slu_hbs_t op, const double* B, int ldb, double* X
   });
 }
 
+namespace {
+std::vector<slu::Hbs*> group_ops(int count, const slu_hbs_t* ops) {
+  SLU_REQUIRE(count >= 0 && (count == 0 || ops), "null argument");
+  std::vector<slu::Hbs*> H(count);
+  for (int i = 0; i < count; ++i) {
+    SLU_REQUIRE(ops[i], "null operator");
+    H[i] = &ops[i]->H;
+  }
+  return H;
+}
+}  // namespace
+
+int slu_ulv_solve_grouped(slu_handle_t h, int count, const slu_hbs_t* ops, double* const* B,
+                          const int* ldb, const int* nrhs) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h, "null argument");
+    std::vector<slu::Hbs*> H = group_ops(count, ops);
+    slu::hbs_solve_grouped(h->h, count, H.data(), B, ldb, nrhs);
+  });
+}
+
+int slu_refine_grouped(slu_handle_t h, int count, const slu_hbs_t* ops, const double* const* B,
+                       const int* ldb, double* const* X, const int* ldx, const int* nrhs,
+                       double tol, int maxit, int* iters_out, double* relres_out) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h, "null argument");
+    std::vector<slu::Hbs*> H = group_ops(count, ops);
+    slu::hbs_refine_grouped(h->h, count, H.data(), B, ldb, X, ldx, nrhs, tol, maxit, iters_out,
+                            relres_out);
+  });
+}
+
 int slu_hbs_info(slu_hbs_t op, int* L, int* N, int* levels, long long* NNvec, int* nsamples) {
   return guard(nullptr, [&] {
     SLU_REQUIRE(op, "null argument");

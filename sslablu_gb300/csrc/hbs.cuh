@@ -24,9 +24,43 @@ struct Workspace {
   }
 };
 
+// Pinned host memory for per-call uploads (task tables) and small read-backs
+// (residual norms).  acquire() waits until the copy issued after the previous
+// acquire has completed, so the buffer can be rewritten.
+struct HostStage {
+  char* p = nullptr;
+  size_t bytes = 0;
+  cudaEvent_t done = nullptr;
+  HostStage() = default;
+  HostStage(const HostStage&) = delete;
+  HostStage& operator=(const HostStage&) = delete;
+  ~HostStage() {
+    if (done) cudaEventDestroy(done);
+    if (p) cudaFreeHost(p);
+  }
+  char* acquire(size_t n) {
+    if (done) SLU_CHECK_CUDA(cudaEventSynchronize(done));
+    if (bytes < n) {
+      if (p) SLU_CHECK_CUDA(cudaFreeHost(p));
+      p = nullptr;
+      bytes = 0;
+      const size_t want = n + (n >> 2) + 4096;
+      SLU_CHECK_CUDA(cudaMallocHost(reinterpret_cast<void**>(&p), want));
+      bytes = want;
+    }
+    return p;
+  }
+  // Marks the point on `st` after which the contents may be overwritten.
+  void release(cudaStream_t st) {
+    if (!done) SLU_CHECK_CUDA(cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
+    SLU_CHECK_CUDA(cudaEventRecord(done, st));
+  }
+};
+
 struct Handle {
   cudaStream_t stream = nullptr;
   Workspace ws;
+  HostStage upload, readback;
   DevBuf info;  // int[64] device status words
   std::string last_error;
 };
@@ -98,5 +132,38 @@ size_t hbs_apply_df_scratch_bytes(const Hbs& H, int c);
 void hbs_apply_df(cudaStream_t st, const Hbs& H, const double* X, int ldx, double* Y, int ldy,
                   int c, void* scratch);
 size_t hbs_nbytes(const Hbs& H, int which);
+
+// Factor pointers of one level by arithmetic type (float64 factors or their
+// float32 copies).
+template <typename T>
+struct FacPtr;
+template <>
+struct FacPtr<double> {
+  static const double* U(const Level& l) { return l.U.as<double>(); }
+  static const double* D(const Level& l) { return l.D.as<double>(); }
+  static const double* Q(const Level& l) { return l.Q.as<double>(); }
+  static const double* W(const Level& l) { return l.W.as<double>(); }
+  static const double* R(const Level& l) { return l.R.as<double>(); }
+  static const double* Uu(const Level& l) { return l.Uu.as<double>(); }
+};
+template <>
+struct FacPtr<float> {
+  static const float* U(const Level& l) { return l.Uf.as<float>(); }
+  static const float* D(const Level& l) { return l.Df.as<float>(); }
+  static const float* Q(const Level& l) { return l.Qf.as<float>(); }
+  static const float* W(const Level& l) { return l.Wf.as<float>(); }
+  static const float* R(const Level& l) { return l.Rf.as<float>(); }
+  static const float* Uu(const Level& l) { return l.Uuf.as<float>(); }
+};
+
+// Grouped solves over many operators (group.cu): one launch per tree step for
+// the whole group.  B[i] is N_i x c[i] row-major with leading dimension ldb[i].
+void hbs_solve_grouped(Handle& h, int count, Hbs* const* ops, double* const* B, const int* ldb,
+                       const int* c);
+// Mixed-precision refinement of the group; iters is the common iteration
+// count, relres[i] the worst column residual of member i.
+void hbs_refine_grouped(Handle& h, int count, Hbs* const* ops, const double* const* B,
+                        const int* ldb, double* const* X, const int* ldx, const int* c,
+                        double tol, int maxit, int* iters, double* relres);
 
 }  // namespace slu

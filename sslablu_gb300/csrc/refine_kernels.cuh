@@ -1,0 +1,54 @@
+// Column norms and elementwise steps of the mixed-precision refinement,
+// shared by the per-operator (refine.cu) and grouped (group.cu) loops.
+#pragma once
+
+namespace slu {
+namespace {
+
+__global__ void colnorm2_k(int rows, int cols, const double* __restrict__ A, int lda,
+                           double* __restrict__ out) {
+  const int c = blockIdx.x;
+  double s = 0.0;
+  for (int i = threadIdx.x; i < rows; i += blockDim.x) {
+    double v = A[(long long)i * lda + c];
+    s += v * v;
+  }
+  __shared__ double red[32];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    out[c] = t;
+  }
+}
+
+// f = (float) src (dense, ld cols)
+__global__ void to_f32_k(long long n, const double* __restrict__ src, float* __restrict__ f) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+       e += (long long)gridDim.x * blockDim.x)
+    f[e] = (float)src[e];
+}
+
+// x = f (init) or x += f
+__global__ void accum_k(long long n, const float* __restrict__ f, double* __restrict__ x, int init) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+       e += (long long)gridDim.x * blockDim.x)
+    x[e] = init ? (double)f[e] : x[e] + (double)f[e];
+}
+
+// r = b - r
+__global__ void resid_k(long long n, const double* __restrict__ b, double* __restrict__ r) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+       e += (long long)gridDim.x * blockDim.x)
+    r[e] = b[e] - r[e];
+}
+
+inline int gsz(long long n) {
+  long long g = (n + 255) / 256;
+  return (int)(g < 1 ? 1 : (g > 4096 ? 4096 : g));
+}
+
+}  // namespace
+}  // namespace slu

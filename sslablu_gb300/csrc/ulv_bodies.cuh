@@ -1,0 +1,217 @@
+// Device bodies of the fused ULV solve (mode N), shared by the per-level
+// kernels (ulv_solve.cu) and the grouped kernels over many operators
+// (group.cu).  Arithmetic of ULVsparse.solve (matAssembly/HBS/
+// ULVsparse.py:296-327):
+//   forward, level t (leaf -> root-1):  z = Q_b^T x_b, the leading nu rows are
+//     kept (ru), the trailing k rows form the parent's input;
+//   root:  y = R^{-1} (Q^T x),  v = D y;
+//   backward, level t (root-1 -> leaf):
+//     y_u  = R11^{-1} (ru - Uu v - R12 y_next)
+//     ynew = W [y_u; y_next],  vnew = U v + D ynew
+// Each body is run by one CTA on block b and right-hand-side columns
+// [c0, c0 + nc); shared memory is laid out per body (see the comments).
+#pragma once
+
+#include <cstdint>
+
+namespace slu {
+namespace ulvk {
+
+
+template <typename T>
+__device__ inline void stage(T* S, int ld, const T* __restrict__ A, int rows, int cols) {
+  for (int e = threadIdx.x; e < rows * cols; e += blockDim.x) {
+    int i = e / cols, j = e - i * cols;
+    S[i * ld + j] = A[e];
+  }
+}
+
+// out[i][c] (+)= sign * sum_j S[i][j0 + j] * x[j][c]   i < rows, j < cols
+template <typename T>
+__device__ inline void mv(const T* S, int ld, int j0, int rows, int cols, const T* x, int ldx,
+                          T* out, int ldo, int nc, T sign, bool accumulate) {
+  for (int e = threadIdx.x; e < rows * nc; e += blockDim.x) {
+    int i = e / nc, cc = e - i * nc;
+    const T* s = S + i * ld + j0;
+    T acc = T(0);
+#pragma unroll 4
+    for (int j = 0; j < cols; ++j) acc = fma(s[j], x[j * ldx + cc], acc);
+    T* o = out + i * ldo + cc;
+    *o = accumulate ? fma(sign, acc, *o) : sign * acc;
+  }
+}
+
+// out[i][c] = sum_j S[j][i] * x[j][c]   (transposed product)
+template <typename T>
+__device__ inline void mvt(const T* S, int ld, int rows_out, int cols_in, const T* x, int ldx,
+                           T* out, int ldo, int nc) {
+  for (int e = threadIdx.x; e < rows_out * nc; e += blockDim.x) {
+    int i = e / nc, cc = e - i * nc;
+    T acc = T(0);
+#pragma unroll 4
+    for (int j = 0; j < cols_in; ++j) acc = fma(S[j * ld + i], x[j * ldx + cc], acc);
+    out[i * ldo + cc] = acc;
+  }
+}
+
+// x <- R^{-1} x for the leading m x m upper triangle of staged R (pitch ld).
+template <typename T>
+__device__ inline void trsv_upper(const T* R, int ld, int m, T* x, int ldx, int nc) {
+  for (int i = m - 1; i >= 0; --i) {
+    __syncthreads();
+    const T d = R[i * ld + i];
+    for (int cc = threadIdx.x; cc < nc; cc += blockDim.x) x[i * ldx + cc] /= d;
+    __syncthreads();
+    for (int e = threadIdx.x; e < i * nc; e += blockDim.x) {
+      int r = e / nc, cc = e - r * nc;
+      x[r * ldx + cc] -= R[r * ld + i] * x[i * ldx + cc];
+    }
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------- forward
+template <typename T>
+__device__ __forceinline__ void ulv_fwd_body(unsigned char* sm_raw, int b, int c0, int nc, int n,
+                                             int nu, int k, const T* __restrict__ Q,
+                                             const T* __restrict__ src, int lds,
+                                             const int64_t* __restrict__ perm, T* __restrict__ ru,
+                                             T* __restrict__ dst, int c, int cpb) {
+  T* S = reinterpret_cast<T*>(sm_raw);       // n x (n+1)
+  T* x = S + n * (n + 1);                     // n x cpb
+  T* z = x + n * cpb;                         // n x cpb
+  for (int e = threadIdx.x; e < n * nc; e += blockDim.x) {
+    int i = e / nc, cc = e - i * nc;
+    long long row = (long long)b * n + i;
+    if (perm) row = perm[row];
+    x[i * cpb + cc] = src[row * lds + c0 + cc];
+  }
+  stage(S, n + 1, Q + (size_t)b * n * n, n, n);
+  __syncthreads();
+  mvt(S, n + 1, n, n, x, cpb, z, cpb, nc);
+  __syncthreads();
+  for (int e = threadIdx.x; e < n * nc; e += blockDim.x) {
+    int i = e / nc, cc = e - i * nc;
+    T v = z[i * cpb + cc];
+    if (i < nu) ru[((size_t)b * nu + i) * c + c0 + cc] = v;
+    else dst[((size_t)b * k + (i - nu)) * c + c0 + cc] = v;
+  }
+}
+
+// ---------------------------------------------------------------- root
+// y = R^{-1} Q^T x, v = D y.  When the tree has one level the root is also
+// the leaf: input gathered through perm, solution scattered through perm.
+template <typename T>
+__device__ __forceinline__ void ulv_root_body(unsigned char* sm_raw, int c0, int nc, int n,
+                                              const T* __restrict__ Q, const T* __restrict__ R,
+                                              const T* __restrict__ D, const T* __restrict__ src,
+                                              int lds, const int64_t* __restrict__ perm,
+                                              T* __restrict__ Yout, T* __restrict__ Vout,
+                                              T* __restrict__ B, int ldb, int c, int cpb) {
+  T* S = reinterpret_cast<T*>(sm_raw);
+  T* x = S + n * (n + 1);
+  T* y = x + n * cpb;
+  for (int e = threadIdx.x; e < n * nc; e += blockDim.x) {
+    int i = e / nc, cc = e - i * nc;
+    long long row = perm ? perm[i] : i;
+    x[i * cpb + cc] = src[row * lds + c0 + cc];
+  }
+  stage(S, n + 1, Q, n, n);
+  __syncthreads();
+  mvt(S, n + 1, n, n, x, cpb, y, cpb, nc);
+  __syncthreads();
+  stage(S, n + 1, R, n, n);
+  trsv_upper(S, n + 1, n, y, cpb, nc);
+  if (perm) {  // single-level tree: y is the solution
+    for (int e = threadIdx.x; e < n * nc; e += blockDim.x) {
+      int i = e / nc, cc = e - i * nc;
+      B[perm[i] * ldb + c0 + cc] = y[i * cpb + cc];
+    }
+    return;
+  }
+  stage(S, n + 1, D, n, n);
+  __syncthreads();
+  mv(S, n + 1, 0, n, n, y, cpb, x, cpb, nc, T(1), false);   // x <- D y
+  __syncthreads();
+  for (int e = threadIdx.x; e < n * nc; e += blockDim.x) {
+    int i = e / nc, cc = e - i * nc;
+    Yout[(size_t)i * c + c0 + cc] = y[i * cpb + cc];
+    Vout[(size_t)i * c + c0 + cc] = x[i * cpb + cc];
+  }
+}
+
+// ---------------------------------------------------------------- backward
+template <typename T>
+__device__ __forceinline__ void ulv_bwd_body(unsigned char* sm_raw, int b, int c0, int nc, int n,
+                                             int nu, int k, const T* __restrict__ ru,
+                                             const T* __restrict__ Uu, const T* __restrict__ R,
+                                             const T* __restrict__ W, const T* __restrict__ U,
+                                             const T* __restrict__ D, const T* __restrict__ Vin,
+                                             const T* __restrict__ Yin, T* __restrict__ Yout,
+                                             T* __restrict__ Vout, const int64_t* __restrict__ perm,
+                                             T* __restrict__ B, int ldb, int c, int cpb) {
+  T* S = reinterpret_cast<T*>(sm_raw);        // n x (n+1) staging
+  T* vb = S + n * (n + 1);                     // k  x cpb
+  T* yn = vb + k * cpb;                        // k  x cpb
+  T* yu = yn + k * cpb;                        // nu x cpb
+  T* ynew = yu + nu * cpb;                     // n  x cpb
+  for (int e = threadIdx.x; e < k * nc; e += blockDim.x) {
+    int i = e / nc, cc = e - i * nc;
+    vb[i * cpb + cc] = Vin[((size_t)b * k + i) * c + c0 + cc];
+    yn[i * cpb + cc] = Yin[((size_t)b * k + i) * c + c0 + cc];
+  }
+  for (int e = threadIdx.x; e < nu * nc; e += blockDim.x) {
+    int i = e / nc, cc = e - i * nc;
+    yu[i * cpb + cc] = ru[((size_t)b * nu + i) * c + c0 + cc];
+  }
+  if (nu > 0) {
+    // yu = ru - Uu v - R12 y_next ; then R11^{-1}
+    stage(S, k + 1, Uu + (size_t)b * nu * k, nu, k);
+    __syncthreads();
+    mv(S, k + 1, 0, nu, k, vb, cpb, yu, cpb, nc, T(-1), true);
+    __syncthreads();
+    stage(S, n + 1, R + (size_t)b * nu * n, nu, n);
+    __syncthreads();
+    mv(S, n + 1, nu, nu, k, yn, cpb, yu, cpb, nc, T(-1), true);
+    trsv_upper(S, n + 1, nu, yu, cpb, nc);
+  }
+  // ynew = W [yu; y_next]
+  stage(S, n + 1, W + (size_t)b * n * n, n, n);
+  __syncthreads();
+  mv(S, n + 1, 0, n, nu, yu, cpb, ynew, cpb, nc, T(1), false);
+  mv(S, n + 1, nu, n, k, yn, cpb, ynew, cpb, nc, T(1), true);
+  __syncthreads();
+  if (perm) {  // leaf level: scatter the solution to the caller's ordering
+    for (int e = threadIdx.x; e < n * nc; e += blockDim.x) {
+      int i = e / nc, cc = e - i * nc;
+      B[perm[(size_t)b * n + i] * ldb + c0 + cc] = ynew[i * cpb + cc];
+    }
+    return;
+  }
+  // vnew = U v + D ynew (written straight to Vout)
+  stage(S, k + 1, U + (size_t)b * n * k, n, k);
+  __syncthreads();
+  for (int e = threadIdx.x; e < n * nc; e += blockDim.x) {
+    int i = e / nc, cc = e - i * nc;
+    const T* s = S + i * (k + 1);
+    T acc = T(0);
+    for (int j = 0; j < k; ++j) acc = fma(s[j], vb[j * cpb + cc], acc);
+    Vout[((size_t)b * n + i) * c + c0 + cc] = acc;
+    Yout[((size_t)b * n + i) * c + c0 + cc] = ynew[i * cpb + cc];
+  }
+  __syncthreads();
+  stage(S, n + 1, D + (size_t)b * n * n, n, n);
+  __syncthreads();
+  for (int e = threadIdx.x; e < n * nc; e += blockDim.x) {
+    int i = e / nc, cc = e - i * nc;
+    const T* s = S + i * (n + 1);
+    T acc = T(0);
+#pragma unroll 4
+    for (int j = 0; j < n; ++j) acc = fma(s[j], ynew[j * cpb + cc], acc);
+    Vout[((size_t)b * n + i) * c + c0 + cc] += acc;
+  }
+}
+
+
+}  // namespace ulvk
+}  // namespace slu

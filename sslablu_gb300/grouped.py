@@ -1,0 +1,63 @@
+"""Grouped solves over many HBS operators.
+
+The reference solves one operator per call (``HBSnew.HBSMAT.solve``,
+matAssembly/HBS/HBSnew.py:393-416); a batch of slab systems calls it once
+per operator.  ``solve_grouped`` hands the whole batch to the library, which
+runs one kernel launch per tree step for every member together
+(``slu_ulv_solve_grouped`` / ``slu_refine_grouped``).  Each member's result is
+the result of its own ``HBSMAT.solve`` (float64) or ``HBSMAT.solve_refined``
+(mixed precision).
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _dev as dv
+from . import _lib as L
+
+
+def _arrays(items):
+    n = len(items)
+    ops = (ctypes.c_void_p * n)(*[H._op for H, _ in items])
+    return n, ops
+
+
+def solve_grouped(systems, precision="f64", tol=1e-10, maxit=10):
+    """Solve A_i x_i = b_i for every (HBSMAT A_i, b_i) in ``systems``.
+
+    ``b_i`` is 1-D or 2-D, numpy or torch; each x_i comes back in the form of
+    its b_i.  ``precision='f64'`` runs the float64 ULV sweep (mode N);
+    ``'mixed'`` runs float32 sweeps refined against float64 residuals until
+    ||b - A x|| / ||b|| <= tol per column, and returns
+    ``(xs, iterations, relres)`` with one worst residual per member.
+    """
+    if precision not in ("f64", "mixed"):
+        raise ValueError("precision must be 'f64' or 'mixed'")
+    items = []
+    for H, b in systems:
+        if getattr(H, "mode", "N") != "N":
+            raise NotImplementedError("grouped solves are mode N only")
+        B, one = dv.prepare_rhs(b)
+        if B.shape[0] != H.shape[0]:
+            raise ValueError("right-hand side has %d rows, operator %d" % (B.shape[0], H.shape[0]))
+        items.append((H, (B.clone().contiguous(), one, b)))
+    if not items:
+        return ([], 0, []) if precision == "mixed" else []
+    n, ops = _arrays(items)
+    Bs = [t for _, (t, _, _) in items]
+    bp = (ctypes.c_void_p * n)(*[t.data_ptr() for t in Bs])
+    ld = (ctypes.c_int * n)(*[t.shape[1] for t in Bs])
+    nr = (ctypes.c_int * n)(*[t.shape[1] for t in Bs])
+    lib = L.lib()
+    if precision == "f64":
+        L.check(lib.slu_ulv_solve_grouped(L.handle(), n, ops, bp, ld, nr))
+        return [dv.finish(t, ref, one) for t, (_, (_, one, ref)) in zip(Bs, items)]
+    Xs = [torch.empty_like(t) for t in Bs]
+    xp = (ctypes.c_void_p * n)(*[t.data_ptr() for t in Xs])
+    it = ctypes.c_int()
+    rr = (ctypes.c_double * n)()
+    L.check(lib.slu_refine_grouped(L.handle(), n, ops, bp, ld, xp, ld, nr, float(tol),
+                                   int(maxit), ctypes.byref(it), rr))
+    xs = [dv.finish(t, ref, one) for t, (_, (_, one, ref)) in zip(Xs, items)]
+    return xs, it.value, list(np.frombuffer(rr, dtype=np.float64))

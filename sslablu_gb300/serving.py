@@ -276,20 +276,15 @@ def _build_hbs_ops(count, seed, sizes=(2048, 4096, 8192), shift=16.0):
     the slab method) so that a 1e-10 relative residual is attainable in
     float64 for every size."""
     from .matAssembly.HBS.HBSnew import HBSMAT
-    import sys
-    import os
-    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
-    from oracle.hbs import gen_random_hbs
-    sigma = 10.0 ** (-12.0 * np.arange(32) / 31.0)
+    from .synthetic import decaying_sigma, random_hbs_factors
+    sigma = decaying_sigma(32)
     ops = []
     for j in range(count):
         N = sizes[j % len(sizes)]
         L = int(np.log2(N // 64)) + 1
         np.random.seed(seed + j)
-        S, Nbvec = gen_random_hbs(32, 64, L, quad=False, sigma=sigma)
-        D0 = S.Dmats[0].copy()
-        D0.reshape(-1, 64, 64)[:] += shift * np.eye(64)
-        A = HBSMAT().set_mats(S.Umats, [D0] + S.Dmats[1:], S.Vmats, list(Nbvec), fac=2)
+        U, D, V, Nbvec = random_hbs_factors(32, 64, L, quad=False, sigma=sigma, shift=shift)
+        A = HBSMAT().set_mats(U, D, V, list(Nbvec), fac=2)
         H = HBSMAT(A, tree=None, quad=False)
         H.set_Nbvec(list(Nbvec))
         H.construct(32, True)

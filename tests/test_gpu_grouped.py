@@ -1,0 +1,97 @@
+"""Grouped solves over many HBS operators of uneven sizes and depths
+(slu_ulv_solve_grouped / slu_refine_grouped through sslablu_gb300.grouped):
+every member's result equals the result of its own solve.
+
+Float64: each column runs the same sequence of operations as the
+per-operator solve, whatever the column chunking, so the bound is 1e-15
+(relative).  Mixed: every member reaches the 1e-10 relative residual against
+its float64 operator and agrees with its own refined solve to 1e-8."""
+import numpy as np
+import pytest
+
+from tests._cases import relerr
+from tests._gpu import need_gpu
+
+pytestmark = pytest.mark.gpu
+
+# (k, leaf, levels, quad): N = leaf * fac**(levels-1)
+SHAPES = [(8, 16, 5, False), (16, 32, 4, False), (8, 32, 3, False), (16, 16, 6, False),
+          (32, 64, 5, False), (8, 16, 3, True), (12, 24, 2, False)]
+
+
+def _operators(shift=4.0, compress=False):
+    from sslablu_gb300.matAssembly.HBS.HBSnew import HBSMAT
+    from sslablu_gb300.synthetic import random_hbs_factors
+    ops = []
+    for j, (k, nl, L, quad) in enumerate(SHAPES):
+        np.random.seed(300 + j)
+        U, D, V, Nbvec = random_hbs_factors(k, nl, L, quad=quad, shift=shift)
+        fac = 4 if quad else 2
+        A = HBSMAT().set_mats(U, D, V, list(Nbvec), fac=fac)
+        nsamp = (6 * k + 4 * nl + 5) if quad else (4 * k + 2 * nl + 5)
+        if compress and nsamp < A.shape[0]:
+            H = HBSMAT(A, tree=None, quad=quad)
+            H.set_Nbvec(list(Nbvec))
+            H.construct(k, True)
+        else:
+            A.compute_ULV()
+            H = A
+        ops.append(H)
+    return ops
+
+
+def _rhs(ops, counts, seed):
+    rng = np.random.default_rng(seed)
+    return [rng.standard_normal((H.shape[0], c)) for H, c in zip(ops, counts)]
+
+
+@pytest.mark.parametrize("compress", [False, True])
+def test_grouped_f64_equals_solo(compress):
+    need_gpu()
+    from sslablu_gb300.grouped import solve_grouped
+    ops = _operators(compress=compress)
+    counts = [1, 3, 8, 16, 5, 2, 7]
+    bs = _rhs(ops, counts, 1)
+    xs = solve_grouped(list(zip(ops, bs)))
+    for H, b, x in zip(ops, bs, xs):
+        assert x.shape == b.shape
+        assert relerr(x, H.solve(b)) <= 1e-15
+
+
+def test_grouped_f64_repeated_members_and_edges():
+    """The same operator several times with different right-hand sides, a 1-D
+    right-hand side, a member with no columns and an empty group."""
+    need_gpu()
+    from sslablu_gb300.grouped import solve_grouped
+    ops = _operators()
+    group = []
+    rng = np.random.default_rng(2)
+    for rep in range(9):
+        for H in ops:
+            c = int(rng.integers(1, 24))
+            group.append((H, rng.standard_normal((H.shape[0], c))))
+    group.append((ops[0], rng.standard_normal(ops[0].shape[0])))     # 1-D
+    group.append((ops[1], np.zeros((ops[1].shape[0], 0))))           # no columns
+    xs = solve_grouped(group)
+    assert len(xs) == len(group)
+    for (H, b), x in zip(group, xs):
+        assert x.shape == b.shape
+        if b.size:
+            assert relerr(x, H.solve(b)) <= 1e-15
+    assert solve_grouped([]) == []
+
+
+def test_grouped_mixed_refinement():
+    need_gpu()
+    from sslablu_gb300.grouped import solve_grouped
+    ops = _operators(compress=True)
+    counts = [4, 1, 16, 8, 3, 5, 2]
+    bs = _rhs(ops, counts, 3)
+    xs, iters, rr = solve_grouped(list(zip(ops, bs)), precision="mixed", tol=1e-10)
+    assert 1 <= iters <= 10 and len(rr) == len(ops)
+    for H, b, x, r in zip(ops, bs, xs, rr):
+        assert r <= 1e-10
+        assert relerr(H.matmat(x), b) <= 1e-10
+        solo, _, rs = H.solve_refined(b, tol=1e-10)
+        assert rs <= 1e-10
+        assert relerr(x, solo) < 1e-8

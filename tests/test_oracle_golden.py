@@ -116,3 +116,19 @@ def test_rbhbs_gauss(golden):
     assert relerr(y, g["x_th"]) < 1e-12
     M = tridiag_matrix(S, m)
     assert relerr(M @ g["x_rb"], g["b"]) < 1e-12
+
+
+def test_package_generator_matches_oracle_generator():
+    """sslablu_gb300.synthetic (benchmarks, serving CLI) draws the same
+    operator as the oracle's generator for the same seed."""
+    from oracle.hbs import gen_random_hbs
+    from sslablu_gb300.synthetic import decaying_sigma, random_hbs_factors
+    for k, nl, L, quad in [(8, 16, 4, False), (4, 8, 3, True)]:
+        sig = decaying_sigma(k)
+        np.random.seed(5)
+        S, nb = gen_random_hbs(k, nl, L, quad=quad, sigma=sig)
+        np.random.seed(5)
+        U, D, V, nb2 = random_hbs_factors(k, nl, L, quad=quad, sigma=sig)
+        assert list(nb) == list(nb2)
+        for a, b in zip(S.Umats + S.Vmats + S.Dmats, U + V + D):
+            assert np.array_equal(a, b)
