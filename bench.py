@@ -170,6 +170,75 @@ def run_reference(args, rank, world):
     print(json.dumps(line))
 
 
+# ---------------------------------------------------------------- roofline
+# DRAM bytes (read + written) of one launch of the leaf backward kernel
+# (ulv_bwd_kernel<double>, level 0) of this workload, from the ncu launch list
+# of `python bench.py --steps 2 --warmup 3` (profiles/ulv_solve_c2_launches.txt);
+# None until measured.
+NCU_TRAFFIC = {"ulv_bwd_kernel<double> level 0": None}
+FP64_NOMINAL_TFLOPS = 1.25   # GB300 float64 (no measured figure in the peaks file)
+
+
+def launch_cost(kind, Nb, n, k, nu, c, leaf):
+    """Algorithmic (bytes, flops) of one fused solve launch: every factor block
+    read once, the right-hand-side blocks read and written once."""
+    if kind == 0:      # z = Q^T x: Q, x in; ru, parent part out
+        return 8 * Nb * (n * n + 2 * n * c), 2 * Nb * n * n * c
+    if kind == 1:      # y = R^-1 Q^T x, v = D y
+        return 8 * (3 * n * n + 3 * n * c), 5 * n * n * c
+    fac = nu * k + nu * n + n * n + (0 if leaf else n * k + n * n)
+    vec = c * (nu + 2 * k) + (n * c if leaf else 2 * n * c)
+    fl = c * (4 * nu * k + nu * nu + 2 * n * n + (0 if leaf else 2 * n * k + 2 * n * n))
+    return 8 * Nb * (fac + vec), Nb * fl
+
+
+def launch_roofline(H, B, flush, hbm, src, reps):
+    """Per-launch device times of the float64 solve (event pairs around each
+    launch, inside the library), the dominant launch, and its roofline."""
+    import ctypes
+    import torch
+    from sslablu_gb300 import _lib
+    lib = _lib.lib()
+    nl, nn = ctypes.c_int(), ctypes.c_int()
+    geo = (ctypes.c_int * 256)()
+    _lib.check(lib.slu_hbs_info(H._op, ctypes.byref(nl), ctypes.byref(nn), geo, None, None))
+    cap = 64
+    runs, meta = [], None
+    c = B.shape[1]
+    for _ in range(reps):
+        flush.fill_(1.0)
+        W = B.clone()
+        ms = (ctypes.c_float * cap)()
+        lvl = (ctypes.c_int * cap)()
+        kind = (ctypes.c_int * cap)()
+        cnt = ctypes.c_int()
+        _lib.check(lib.slu_ulv_solve_timed(_lib.handle(), H._op, _lib.ptr(W), c, c, ms, lvl, kind,
+                                           cap, ctypes.byref(cnt)))
+        runs.append([ms[i] for i in range(cnt.value)])
+        meta = [(lvl[i], kind[i]) for i in range(cnt.value)]
+    med = np.median(np.array(runs), axis=0)
+    names = {0: "ulv_fwd_kernel", 1: "ulv_root_kernel", 2: "ulv_bwd_kernel"}
+    launches = []
+    for (t, kd), m in zip(meta, med):
+        Nb, n, k, nu = (geo[4 * t + j] for j in range(4))
+        by, fl = launch_cost(kd, Nb, n, k, nu, c, t == 0)
+        launches.append({"kernel": "%s<double> level %d" % (names[kd], t), "ms": float(m),
+                         "alg_bytes": int(by), "alg_flops": int(fl)})
+    top = max(launches, key=lambda x: x["ms"])
+    sec = top["ms"] * 1e-3
+    achieved = top["alg_bytes"] / sec / 1e9
+    tflops = top["alg_flops"] / sec / 1e12
+    return {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+            "frac": achieved / hbm, "traffic": NCU_TRAFFIC.get(top["kernel"]),
+            "kernel": top["kernel"], "alg_bytes_per_launch": top["alg_bytes"],
+            "launch_ms": top["ms"], "share_of_solve": top["ms"] / float(np.sum(med)),
+            "peak_source": ("hbm_gbs of measured peaks" if src == "measured"
+                            else "6.8 TB/s of fallback"),
+            "fp64": {"achieved_tflops": tflops, "nominal_peak_tflops": FP64_NOMINAL_TFLOPS,
+                     "frac_nominal": tflops / FP64_NOMINAL_TFLOPS},
+            "launches": launches}
+
+
 # ---------------------------------------------------------------- GPU leg
 def run_gpu(args, rank, world):
     import torch
@@ -263,15 +332,9 @@ def run_gpu(args, rank, world):
     else:
         tot_e2e = sum(e2e)
     value = world * NRHS * args.steps / tot_plain
-    # roofline: the whole float64 solve step as one unit (algorithmic bytes:
-    # every solve factor read once + 4 passes over the right-hand sides)
-    import ctypes
-    fb = ctypes.c_size_t()
-    _lib.check(_lib.lib().slu_hbs_nbytes(H._op, 1, ctypes.byref(fb)))
-    alg_bytes = fb.value + 8 * N * NRHS * 4
     p50 = statistics.median(ts_plain)
     hbm, src = peaks()
-    achieved = alg_bytes / p50 / 1e9
+    roof = launch_roofline(H, B, flush, hbm, src, reps=max(5, args.steps))
     line = None
     if rank == 0:
         base = cpu_baseline(mats, Nbvec, rhs)
@@ -295,10 +358,7 @@ def run_gpu(args, rank, world):
                     "h2d_bytes_per_step": int(rhs.nbytes), "d2h_bytes_per_step": int(rhs.nbytes),
                     "p50_ms": 1e3 * statistics.median(e2e)},
             "gpu_launches": launches_plain,
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                         "frac": achieved / hbm, "traffic": None,
-                         "kernel": "float64 ULV solve step (all launches of one solve)",
-                         "alg_bytes_per_launch": alg_bytes, "peak_source": src},
+            "roofline": roof,
             "cpu_baseline": {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")},
             "clocks": clk,
         }

@@ -137,6 +137,14 @@ int slu_ulv_solve_f32(slu_handle_t h, slu_hbs_t op, float* B, int ldb, int nrhs,
 int slu_refine(slu_handle_t h, slu_hbs_t op, const double* B, int ldb, double* X, int ldx,
                int nrhs, double tol, int maxit, int* iters_out, double* relres_out);
 
+/* Null-space rule of the next slu_hbs_compress of `op`: mode 0 projects each
+ * block's sketch on the last n columns of the complete Q of Om_blk^T
+ * (HBSnew.compute_UV, matAssembly/HBS/HBSnew.py:20-28; the default), mode 1
+ * on every column after the first n (HBStorch.compute_UV,
+ * matAssembly/HBS/HBStorch.py:73-82, the rkHBS assembler's engine).  Mode 0
+ * spans the null space only when s >= 2n; mode 1 does for every s > n. */
+int slu_hbs_set_null_space(slu_hbs_t op, int mode);
+
 /* Grouped solves over `count` operators of any sizes and depths, one kernel
  * launch per tree step for the whole group (the batched form of calling
  * HBSnew.HBSMAT.solve, matAssembly/HBS/HBSnew.py:393-416, once per operator;
@@ -155,6 +163,17 @@ int slu_ulv_solve_grouped(slu_handle_t h, int count, const slu_hbs_t* ops, doubl
 int slu_refine_grouped(slu_handle_t h, int count, const slu_hbs_t* ops, const double* const* B,
                        const int* ldb, double* const* X, const int* ldx, const int* nrhs,
                        double tol, int maxit, int* iters_out, double* relres_out);
+
+/* Diagnostics: one float64 mode-N solve (as slu_ulv_solve) with a CUDA event
+ * pair around each kernel launch; returns after the solve completes.
+ * ms_out[k] is the device time of launch k (launch order), level_out[k] its
+ * tree level and kind_out[k] its sweep (0 forward, 1 root, 2 backward), for
+ * k < cap (host arrays, each may be NULL); *nlaunch receives the number of
+ * launches.  The reference keeps host-side timers on HBSMAT
+ * (matAssembly/HBS/HBSnew.py:108-111, 155-200); this is their device-side
+ * counterpart for the solve. */
+int slu_ulv_solve_timed(slu_handle_t h, slu_hbs_t op, double* B, int ldb, int nrhs,
+                        float* ms_out, int* level_out, int* kind_out, int cap, int* nlaunch);
 
 /* Geometry: L, N and per level (Nb, n, k, nu) into levels[4*L]; NNvec[L+1]
  * (ULVsparse.compute_ULV's NNvec).  Host pointers, any may be NULL. */

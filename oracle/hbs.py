@@ -98,13 +98,15 @@ def block_solve(A, B, Nb, mode="N"):
 # --------------------------------------------------------------------------
 # compression kernels
 # --------------------------------------------------------------------------
-def compute_UV(Om, Y, rk, Nb):
+def compute_UV(Om, Y, rk, Nb, after_n=False):
     """HBSnew.py:20-28: complete QR of each Om block^T, project Y onto the
-    trailing n columns of Q, keep the rk leading left singular vectors."""
+    trailing n columns of Q, keep the rk leading left singular vectors.
+    ``after_n`` projects on every column after the first n instead
+    (HBStorch.py:73-82)."""
     Omb = bv(Om, Nb)                 # (Nb, n, s)
     n = Omb.shape[1]
     Q = np.linalg.qr(tr(Omb), mode="complete")[0]   # (Nb, s, s)
-    M = bv(Y, Nb) @ Q[:, :, -n:]
+    M = bv(Y, Nb) @ (Q[:, :, n:] if after_n else Q[:, :, -n:])
     U = np.linalg.svd(M)[0][:, :, :rk]
     return ub(np.ascontiguousarray(U))
 
@@ -318,8 +320,10 @@ class OracleHBS:
         self.compress_from_sketches(rk, Om, Psi, Y, Z)
         return self
 
-    def compress_from_sketches(self, rk, Om, Psi, Y, Z):
-        """Levels leaf -> root (HBSnew.py:234-294), sketches in tree order."""
+    def compress_from_sketches(self, rk, Om, Psi, Y, Z, null_after_n=False):
+        """Levels leaf -> root (HBSnew.py:234-294), sketches in tree order;
+        ``null_after_n`` selects HBStorch's null-space rule (HBStorch.py:73-82,
+        its level loop 184-229 being the same)."""
         fac, L, nl = self.fac, self.L, self.nl
         Nb = self.Nb
         self.Nbvec = []
@@ -343,8 +347,8 @@ class OracleHBS:
                 rkm = min(rk, nl * fac ** (L - 1 - lvl))
             self.Nbvec.append(Nb)
             if lvl > 0:
-                U_l = compute_UV(Om_l, Y_l, rkm, Nb)
-                V_l = compute_UV(Psi_l, Z_l, rkm, Nb)
+                U_l = compute_UV(Om_l, Y_l, rkm, Nb, null_after_n)
+                V_l = compute_UV(Psi_l, Z_l, rkm, Nb, null_after_n)
                 D_l = construct_D(U_l, V_l, Y_l, Z_l, Om_l, Psi_l, Nb)
                 self.Umats.append(U_l)
                 self.Vmats.append(V_l)

@@ -40,6 +40,8 @@ SIGNATURES = {
     "slu_ulv_solve_f32": [P, P, P, c_int, c_int, c_int],
     "slu_refine": [P, P, P, c_int, P, c_int, c_int, c_double, c_int, P, P],
     "slu_ulv_solve_grouped": [P, c_int, P, P, P, P],
+    "slu_hbs_set_null_space": [P, c_int],
+    "slu_ulv_solve_timed": [P, P, P, c_int, c_int, P, P, P, c_int, P],
     "slu_refine_grouped": [P, c_int, P, P, P, P, P, P, c_double, c_int, P, P],
     "slu_hbs_info": [P, P, P, P, P, P],
     "slu_hbs_export": [P, P, c_int, c_int, P, c_size_t, P],

@@ -301,6 +301,41 @@ int slu_refine_grouped(slu_handle_t h, int count, const slu_hbs_t* ops, const do
   });
 }
 
+int slu_ulv_solve_timed(slu_handle_t h, slu_hbs_t op, double* B, int ldb, int nrhs,
+                        float* ms_out, int* level_out, int* kind_out, int cap, int* nlaunch) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h && op && B && nlaunch, "null argument");
+    SLU_REQUIRE(nrhs >= 1 && ldb >= nrhs && cap >= 0, "bad arguments");
+    const slu::Hbs& H = op->H;
+    SLU_REQUIRE(H.has_ulv, "HBS operator has no ULV factorisation");
+    cudaStream_t st = h->h.stream;
+    const size_t bytes = slu::hbs_solve_scratch_bytes(H, nrhs, sizeof(double));
+    h->h.ws.reserve(bytes, st);
+    double* scratch = h->h.ws.take<double>(bytes / sizeof(double));
+    const size_t stride = ((sizeof(double) * (size_t)H.N * nrhs + 255) & ~size_t(255)) / 8;
+    slu::LaunchTimes lt;
+    slu::ulv_solve_fused<double>(st, H, B, ldb, nrhs, scratch, stride, &lt);
+    SLU_CHECK_CUDA(cudaStreamSynchronize(st));
+    const int n = (int)lt.level.size();
+    *nlaunch = n;
+    for (int k = 0; k < n && k < cap; ++k) {
+      float ms = 0.f;
+      SLU_CHECK_CUDA(cudaEventElapsedTime(&ms, lt.ev[2 * k], lt.ev[2 * k + 1]));
+      if (ms_out) ms_out[k] = ms;
+      if (level_out) level_out[k] = lt.level[k];
+      if (kind_out) kind_out[k] = lt.kind[k];
+    }
+  });
+}
+
+int slu_hbs_set_null_space(slu_hbs_t op, int mode) {
+  return guard(nullptr, [&] {
+    SLU_REQUIRE(op, "null argument");
+    SLU_REQUIRE(mode == 0 || mode == 1, "null-space mode must be 0 or 1");
+    op->H.null_after_n = (mode == 1);
+  });
+}
+
 int slu_hbs_info(slu_hbs_t op, int* L, int* N, int* levels, long long* NNvec, int* nsamples) {
   return guard(nullptr, [&] {
     SLU_REQUIRE(op, "null argument");

@@ -303,10 +303,26 @@ void hbs_compress(Handle& h, Hbs& H, int Nb0, int rk, int s, const double* Om, c
       panel_qr(st, s, n, 2 * n, WSB, s, 2 * ns, tauB, n, Nb);
       int* info = h.info.as<int>();
       // U, V: leading left singular vectors of Y_blk Q[:, s-n:s] (HBSnew.py:26-27)
-      jacobi_left_sv(st, n, n, WSA + ns + (s - n), s, 2 * ns, k, dp(l.U), k, (long long)n * k,
-                     nullptr, 0, Nb, info);
-      jacobi_left_sv(st, n, n, WSB + ns + (s - n), s, 2 * ns, k, dp(l.V), k, (long long)n * k,
-                     nullptr, 0, Nb, info);
+      // or of Y_blk Q[:, n:s] (HBStorch.py:73-82)
+      const int jc = H.null_after_n ? s - n : n;
+      const int j0 = H.null_after_n ? n : s - n;
+      SLU_REQUIRE(k <= std::min(n, jc), "rank exceeds the columns of the projected sketch");
+      if (jc > n) {
+        // wide n x jc block: its left singular vectors are those of R^T from
+        // the QR of its transpose, which the panels already hold column-major
+        // (column i = row i of the block); R^T is n x n lower triangular
+        panel_qr(st, jc, n, n, WSA + ns + j0, s, 2 * ns, tauA, n, Nb);
+        panel_qr(st, jc, n, n, WSB + ns + j0, s, 2 * ns, tauB, n, Nb);
+        jacobi_left_sv(st, n, n, WSA + ns + j0, s, 2 * ns, k, dp(l.U), k, (long long)n * k,
+                       nullptr, 0, Nb, info, true);
+        jacobi_left_sv(st, n, n, WSB + ns + j0, s, 2 * ns, k, dp(l.V), k, (long long)n * k,
+                       nullptr, 0, Nb, info, true);
+      } else {
+        jacobi_left_sv(st, n, jc, WSA + ns + j0, s, 2 * ns, k, dp(l.U), k, (long long)n * k,
+                       nullptr, 0, Nb, info);
+        jacobi_left_sv(st, n, jc, WSB + ns + j0, s, 2 * ns, k, dp(l.V), k, (long long)n * k,
+                       nullptr, 0, Nb, info);
+      }
       // D = (Y - U U^T Y) pinv(Om) + U U^T ((Z - V V^T Z) pinv(Psi))^T  (HBSnew.py:48-62)
       const long long nk = (long long)n * k;
       copy_batched<double>(st, n, n, YQ1A, s, 2 * ns, 0, dp(l.D), n, nn, 0, Nb);

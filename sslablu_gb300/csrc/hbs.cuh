@@ -90,6 +90,10 @@ struct Hbs {
   std::vector<long long> NN;       // NNvec, L+1 entries
   bool has_mats = false, has_ulv = false, has_f32 = false, has_df = false;
   int rk = 0, nsamples = 0;
+  // null space of a sketch block's Om^T used by compression: false takes the
+  // last n columns of the complete Q (HBSnew.compute_UV), true every column
+  // after the first n (HBStorch.compute_UV)
+  bool null_after_n = false;
   // refinement plans per right-hand-side count; they capture factor pointers,
   // so every change of the factors clears them (invalidate_plans)
   std::map<int, std::shared_ptr<RefinePlan>> refine_plans;
@@ -113,11 +117,35 @@ template <typename T>
 void hbs_solve_scratch(cudaStream_t st, const Hbs& H, bool trans, T* B, int ldb, int nrhs,
                        T* scratch);
 size_t hbs_solve_scratch_bytes(const Hbs& H, int nrhs, size_t elem);
+// Device time of every launch of one fused solve (diagnostics): an event
+// pair around each launch, with the launch's level and kind (0 forward,
+// 1 root, 2 backward).
+struct LaunchTimes {
+  std::vector<cudaEvent_t> ev;
+  std::vector<int> level, kind;
+  LaunchTimes() = default;
+  LaunchTimes(const LaunchTimes&) = delete;
+  LaunchTimes& operator=(const LaunchTimes&) = delete;
+  ~LaunchTimes() {
+    for (cudaEvent_t e : ev) cudaEventDestroy(e);
+  }
+  void mark(cudaStream_t st) {
+    cudaEvent_t e = nullptr;
+    SLU_CHECK_CUDA(cudaEventCreate(&e));
+    ev.push_back(e);
+    SLU_CHECK_CUDA(cudaEventRecord(e, st));
+  }
+  void done(int lvl, int k) {
+    level.push_back(lvl);
+    kind.push_back(k);
+  }
+};
+
 // Mode-N solve with one fused kernel per level and sweep (ulv_solve.cu);
 // scratch: five buffers of `stride` elements.
 template <typename T>
 void ulv_solve_fused(cudaStream_t st, const Hbs& H, T* B, int ldb, int c, T* scratch,
-                     size_t stride);
+                     size_t stride, LaunchTimes* times = nullptr);
 // Fused per-level apply (hbs_apply.cu); scratch of hbs_apply_scratch_elems doubles.
 size_t hbs_apply_scratch_elems(const Hbs& H, int c);
 void hbs_apply_fused(cudaStream_t st, const Hbs& H, bool trans, const double* X, int ldx,

@@ -127,67 +127,100 @@ apply_q_kernel(bool transpose, int m, int k, const double* __restrict__ V, int l
 
 // ---------------------------------------------------------------- Jacobi SVD
 // One-sided (Hestenes) Jacobi on the columns of A (m x n), round-robin pair
-// ordering, one warp per column pair.  At convergence the columns are
-// sigma_j u_j; the r largest are normalised and written as U (m x r).
+// ordering.  One thread per column pair: it forms the three inner products of
+// its pair, the rotation, and applies it, so the scalar work (square roots,
+// divisions) runs once per pair instead of once per lane; the float64 pipe
+// then does only the 7m multiply-adds of each pair.  Each inner product is
+// summed in JAC_ACC interleaved partial sums combined pairwise, which keeps
+// its rounding error well below the m*eps rotation threshold (a single
+// running sum reaches that threshold on noise-level columns, which then
+// never stop rotating).  Columns live in shared memory with an odd leading
+// dimension, so the 32 threads of a warp, each on its own column, read
+// different banks.  At convergence the columns are sigma_j u_j; the r largest
+// are normalised and written as U (m x r).
 constexpr int JAC_MAX_SWEEPS = 40;
+constexpr int JAC_ACC = 8;
 
 __global__ void __launch_bounds__(1024)
 jacobi_kernel(int m, int n, const double* __restrict__ A, int lda, long long sA, int r,
               double* __restrict__ U, int ldu, long long sU, double* __restrict__ sv,
-              long long sS, int* info) {
+              long long sS, int* info, int lower) {
   extern __shared__ double sm[];
   const int np = n + (n & 1);            // even number of columns (a zero pad column)
-  double* a = sm;                        // m x np, column-major, ld = m
-  double* nrm = a + (long long)m * np;   // np
+  const int lda_s = m | 1;               // odd column stride
+  double* a = sm;                        // column-major, column c at a + c * lda_s
+  double* nrm = a + (long long)lda_s * np;   // np
   int* order = reinterpret_cast<int*>(nrm + np);   // np
   __shared__ int s_rot;
   A += blockIdx.x * sA;
   for (long long e = threadIdx.x; e < (long long)m * np; e += blockDim.x) {
     int c = (int)(e / m), i = (int)(e % m);
-    a[e] = (c < n) ? A[(long long)i * lda + c] : 0.0;   // A row-major
+    // A row-major; with `lower`, only its lower triangle (c <= i) is read
+    a[(long long)c * lda_s + i] =
+        (c < n && (!lower || c <= i)) ? A[(long long)i * lda + c] : 0.0;
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const double tol = 2.220446049250313e-16 * (double)m;
+  const int npairs = np / 2;
   int sweep = 0;
   for (; sweep < JAC_MAX_SWEEPS; ++sweep) {
     if (threadIdx.x == 0) s_rot = 0;
     __syncthreads();
     for (int rnd = 0; rnd < np - 1; ++rnd) {
-      for (int pi = warp; pi < np / 2; pi += nwarps) {
+      for (int pi = threadIdx.x; pi < npairs; pi += blockDim.x) {
         // circle method: slot 0 fixed, others rotate
-        int s1 = pi, s2 = np - 1 - pi;
-        int p = (s1 == 0) ? 0 : 1 + (s1 - 1 + rnd) % (np - 1);
-        int q = 1 + (s2 - 1 + rnd) % (np - 1);
-        double* ap = a + (long long)p * m;
-        double* aq = a + (long long)q * m;
-        double al = 0.0, be = 0.0, ga = 0.0;
-        for (int i = lane; i < m; i += 32) {
-          double x = ap[i], y = aq[i];
-          al += x * x;
-          be += y * y;
-          ga += x * y;
-        }
-        al = warp_sum(al);
-        be = warp_sum(be);
-        ga = warp_sum(ga);
-        if (ga != 0.0 && fabs(ga) > tol * sqrt(al * be)) {
-          double zeta = (be - al) / (2.0 * ga);
-          double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-          double c = 1.0 / sqrt(1.0 + t * t);
-          double s = c * t;
-          for (int i = lane; i < m; i += 32) {
-            double x = ap[i], y = aq[i];
-            ap[i] = c * x - s * y;
-            aq[i] = s * x + c * y;
+        const int s1 = pi, s2 = np - 1 - pi;
+        const int p = (s1 == 0) ? 0 : 1 + (s1 - 1 + rnd) % (np - 1);
+        const int q = 1 + (s2 - 1 + rnd) % (np - 1);
+        double* ap = a + (long long)p * lda_s;
+        double* aq = a + (long long)q * lda_s;
+        double pa[JAC_ACC], pb[JAC_ACC], pg[JAC_ACC];
+#pragma unroll
+        for (int u = 0; u < JAC_ACC; ++u) pa[u] = pb[u] = pg[u] = 0.0;
+        int i = 0;
+        for (; i + JAC_ACC <= m; i += JAC_ACC) {
+#pragma unroll
+          for (int u = 0; u < JAC_ACC; ++u) {
+            const double x = ap[i + u], y = aq[i + u];
+            pa[u] = fma(x, x, pa[u]);
+            pb[u] = fma(y, y, pb[u]);
+            pg[u] = fma(x, y, pg[u]);
           }
-          if (lane == 0) s_rot = 1;
         }
-        __syncwarp();
+#pragma unroll
+        for (int u = 0; u < JAC_ACC; ++u) {
+          if (i + u < m) {
+            const double x = ap[i + u], y = aq[i + u];
+            pa[u] = fma(x, x, pa[u]);
+            pb[u] = fma(y, y, pb[u]);
+            pg[u] = fma(x, y, pg[u]);
+          }
+        }
+#pragma unroll
+        for (int w = JAC_ACC / 2; w > 0; w >>= 1)
+#pragma unroll
+          for (int u = 0; u < w; ++u) {
+            pa[u] += pa[u + w];
+            pb[u] += pb[u + w];
+            pg[u] += pg[u + w];
+          }
+        const double al = pa[0], be = pb[0], ga = pg[0];
+        if (ga != 0.0 && fabs(ga) > tol * sqrt(al * be)) {
+          const double zeta = (be - al) / (2.0 * ga);
+          const double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+          const double c = 1.0 / sqrt(1.0 + t * t);
+          const double s = c * t;
+          for (int j = 0; j < m; ++j) {
+            const double x = ap[j], y = aq[j];
+            ap[j] = c * x - s * y;
+            aq[j] = s * x + c * y;
+          }
+          s_rot = 1;
+        }
       }
       __syncthreads();
     }
-    __syncthreads();
     if (!s_rot) break;
     __syncthreads();
   }
@@ -195,7 +228,7 @@ jacobi_kernel(int m, int n, const double* __restrict__ A, int lda, long long sA,
   // column norms
   for (int c = warp; c < np; c += nwarps) {
     double s = 0.0;
-    for (int i = lane; i < m; i += 32) s += a[(long long)c * m + i] * a[(long long)c * m + i];
+    for (int i = lane; i < m; i += 32) s += a[(long long)c * lda_s + i] * a[(long long)c * lda_s + i];
     s = warp_sum(s);
     if (lane == 0) nrm[c] = sqrt(s);
   }
@@ -223,7 +256,7 @@ jacobi_kernel(int m, int n, const double* __restrict__ A, int lda, long long sA,
     if (svb && lane == 0) svb[j] = (j < n) ? s : 0.0;
     bool ok = (j < n) && s > tiny;
     for (int i = lane; i < m; i += 32)
-      Ub[(long long)i * ldu + j] = ok ? a[(long long)c * m + i] / s : 0.0;
+      Ub[(long long)i * ldu + j] = ok ? a[(long long)c * lda_s + i] / s : 0.0;
   }
   __syncthreads();
   // completion (rare: zero or rank-deficient input); serial over columns
@@ -282,17 +315,18 @@ void apply_q(cudaStream_t st, bool transpose, int m, int k, const double* V, int
 
 void jacobi_left_sv(cudaStream_t st, int m, int n, const double* A, int lda, long long sA, int r,
                     double* U, int ldu, long long sU, double* sv, long long sS, int batch,
-                    int* info) {
+                    int* info, bool lower) {
   if (batch <= 0 || r <= 0) return;
   SLU_REQUIRE(r <= m, "jacobi: rank larger than rows");
   int np = n + (n & 1);
-  size_t sm = (size_t)m * np * sizeof(double) + np * sizeof(double) + np * sizeof(int);
+  size_t sm = (size_t)(m | 1) * np * sizeof(double) + np * sizeof(double) + np * sizeof(int);
   SLU_REQUIRE(sm <= 220 * 1024, "jacobi: block too large for shared memory");
   if (sm > 48 * 1024)
     SLU_CHECK_CUDA(cudaFuncSetAttribute(jacobi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)sm));
-  int threads = 32 * std::min(32, std::max(1, np / 2));
-  jacobi_kernel<<<batch, threads, sm, st>>>(m, n, A, lda, sA, r, U, ldu, sU, sv, sS, info);
+  int threads = 32 * std::min(32, std::max(2, (np / 2 + 31) / 32));
+  jacobi_kernel<<<batch, threads, sm, st>>>(m, n, A, lda, sA, r, U, ldu, sU, sv, sS, info,
+                                            lower ? 1 : 0);
   check_launch("jacobi_kernel");
 }
 

@@ -124,9 +124,10 @@ void apply_q(cudaStream_t st, bool transpose, int m, int k, const double* V, int
 // One-sided Jacobi SVD of A_b (m x n, row-major with leading dimension lda):
 // writes the leading r left singular vectors (sorted by decreasing singular
 // value) as an m x r row-major array U_b (ldu), and the singular values.
+// `lower` reads only the lower triangle of A (the rest taken as zero).
 void jacobi_left_sv(cudaStream_t st, int m, int n, const double* A, int lda, long long sA,
                     int r, double* U, int ldu, long long sU, double* sv, long long sS,
-                    int batch, int* info);
+                    int batch, int* info, bool lower = false);
 
 // Batched triangular solve with an upper-triangular R_b (n x n): element
 // (i, j) of R_b at R_b[i*rRs + j*rCs] (row-major: rRs = ld, rCs = 1;

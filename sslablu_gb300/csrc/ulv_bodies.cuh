@@ -55,16 +55,27 @@ __device__ inline void mvt(const T* S, int ld, int rows_out, int cols_in, const 
 }
 
 // x <- R^{-1} x for the leading m x m upper triangle of staged R (pitch ld).
+// The diagonal of the staged copy is replaced by its reciprocals (all threads,
+// once), then one warp per right-hand-side column runs the back substitution:
+// lane (i mod 32) finishes x_i and broadcasts it, each lane updates the rows
+// it owns (r = lane + 32 q).  Rows never change owner, so the sweep needs no
+// block barrier.
 template <typename T>
-__device__ inline void trsv_upper(const T* R, int ld, int m, T* x, int ldx, int nc) {
-  for (int i = m - 1; i >= 0; --i) {
-    __syncthreads();
-    const T d = R[i * ld + i];
-    for (int cc = threadIdx.x; cc < nc; cc += blockDim.x) x[i * ldx + cc] /= d;
-    __syncthreads();
-    for (int e = threadIdx.x; e < i * nc; e += blockDim.x) {
-      int r = e / nc, cc = e - r * nc;
-      x[r * ldx + cc] -= R[r * ld + i] * x[i * ldx + cc];
+__device__ inline void trsv_upper(T* R, int ld, int m, T* x, int ldx, int nc) {
+  __syncthreads();
+  for (int i = threadIdx.x; i < m; i += blockDim.x) R[i * ld + i] = T(1) / R[i * ld + i];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int cc = threadIdx.x >> 5; cc < nc; cc += nw) {
+    for (int i = m - 1; i >= 0; --i) {
+      const int owner = i & 31;
+      T xi = T(0);
+      if (lane == owner) {
+        xi = x[i * ldx + cc] * R[i * ld + i];
+        x[i * ldx + cc] = xi;
+      }
+      xi = __shfl_sync(0xffffffffu, xi, owner);
+      for (int r = lane; r < i; r += 32) x[r * ldx + cc] -= R[r * ld + i] * xi;
     }
   }
   __syncthreads();

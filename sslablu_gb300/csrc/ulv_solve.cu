@@ -95,7 +95,7 @@ void set_smem(K kern, size_t bytes) {
 // B (N x c, caller ordering) <- A^{-1} B; scratch: 5 buffers of stride elements.
 template <typename T>
 void ulv_solve_fused(cudaStream_t st, const Hbs& H, T* B, int ldb, int c, T* scratch,
-                     size_t stride) {
+                     size_t stride, LaunchTimes* lt) {
   using F = FacPtr<T>;
   const int L = H.L;
   const int64_t* perm = H.perm.as<int64_t>();
@@ -117,9 +117,14 @@ void ulv_solve_fused(cudaStream_t st, const Hbs& H, T* B, int ldb, int c, T* scr
     set_smem(kern, sm);
     T* dst = P[t & 1];
     dim3 grid(l.Nb, (c + cpb - 1) / cpb);
+    if (lt) lt->mark(st);
     kern<<<grid, kThreads, sm, st>>>(l.n, l.nu, l.k, F::Q(l), src, lds, gperm, ru + NN[t] * c,
                                      dst, c, cpb);
     check_launch("ulv_fwd_kernel");
+    if (lt) {
+      lt->mark(st);
+      lt->done(t, 0);
+    }
     src = dst;
     lds = c;
     gperm = nullptr;
@@ -132,9 +137,14 @@ void ulv_solve_fused(cudaStream_t st, const Hbs& H, T* B, int ldb, int c, T* scr
     auto kern = ulv_root_kernel<T>;
     set_smem(kern, sm);
     dim3 grid(1, (c + cpr - 1) / cpr);
+    if (lt) lt->mark(st);
     kern<<<grid, kThreads, sm, st>>>(r.n, F::Q(r), F::R(r), F::D(r), src, lds,
                                      L == 1 ? perm : nullptr, P[2], P[3], B, ldb, c, cpr);
     check_launch("ulv_root_kernel");
+    if (lt) {
+      lt->mark(st);
+      lt->done(L - 1, 1);
+    }
   }
   // backward sweep
   int in = 2;
@@ -146,15 +156,22 @@ void ulv_solve_fused(cudaStream_t st, const Hbs& H, T* B, int ldb, int c, T* scr
     set_smem(kern, sm);
     const int out = (in == 2) ? 0 : 2;
     dim3 grid(l.Nb, (c + cpb - 1) / cpb);
+    if (lt) lt->mark(st);
     kern<<<grid, kThreads, sm, st>>>(l.n, l.nu, l.k, ru + NN[t] * c, F::Uu(l), F::R(l), F::W(l),
                                      F::U(l), F::D(l), P[in + 1], P[in], P[out], P[out + 1],
                                      t == 0 ? perm : nullptr, B, ldb, c, cpb);
     check_launch("ulv_bwd_kernel");
+    if (lt) {
+      lt->mark(st);
+      lt->done(t, 2);
+    }
     in = out;
   }
 }
 
-template void ulv_solve_fused<double>(cudaStream_t, const Hbs&, double*, int, int, double*, size_t);
-template void ulv_solve_fused<float>(cudaStream_t, const Hbs&, float*, int, int, float*, size_t);
+template void ulv_solve_fused<double>(cudaStream_t, const Hbs&, double*, int, int, double*, size_t,
+                                      LaunchTimes*);
+template void ulv_solve_fused<float>(cudaStream_t, const Hbs&, float*, int, int, float*, size_t,
+                                     LaunchTimes*);
 
 }  // namespace slu

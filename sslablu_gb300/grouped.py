@@ -17,10 +17,36 @@ from . import _dev as dv
 from . import _lib as L
 
 
-def _arrays(items):
-    n = len(items)
-    ops = (ctypes.c_void_p * n)(*[H._op for H, _ in items])
-    return n, ops
+def solve_grouped_device(ops, Bs, precision="f64", tol=1e-10, maxit=10, Xs=None):
+    """Grouped solve on contiguous float64 CUDA tensors Bs[i] (N_i x c_i).
+
+    ``'f64'`` solves every Bs[i] in place and returns Bs.  ``'mixed'`` writes
+    Xs[i] (allocated when None) and returns ``(Xs, iterations, relres)``."""
+    n = len(ops)
+    if n == 0:
+        return ([], 0, []) if precision == "mixed" else []
+    for H, B in zip(ops, Bs):
+        if B.dtype != torch.float64 or not B.is_cuda or not B.is_contiguous() or B.dim() != 2:
+            raise ValueError("right-hand sides must be contiguous 2-D float64 CUDA tensors")
+        if B.shape[0] != H.shape[0]:
+            raise ValueError("right-hand side has %d rows, operator %d" % (B.shape[0], H.shape[0]))
+    op_arr = (ctypes.c_void_p * n)(*[H._op for H in ops])
+    bp = (ctypes.c_void_p * n)(*[t.data_ptr() for t in Bs])
+    ld = (ctypes.c_int * n)(*[t.shape[1] for t in Bs])
+    lib = L.lib()
+    if precision == "f64":
+        L.check(lib.slu_ulv_solve_grouped(L.handle(), n, op_arr, bp, ld, ld))
+        return Bs
+    if precision != "mixed":
+        raise ValueError("precision must be 'f64' or 'mixed'")
+    if Xs is None:
+        Xs = [torch.empty_like(t) for t in Bs]
+    xp = (ctypes.c_void_p * n)(*[t.data_ptr() for t in Xs])
+    it = ctypes.c_int()
+    rr = (ctypes.c_double * n)()
+    L.check(lib.slu_refine_grouped(L.handle(), n, op_arr, bp, ld, xp, ld, ld, float(tol),
+                                   int(maxit), ctypes.byref(it), rr))
+    return Xs, it.value, list(np.frombuffer(rr, dtype=np.float64))
 
 
 def solve_grouped(systems, precision="f64", tol=1e-10, maxit=10):
@@ -34,30 +60,16 @@ def solve_grouped(systems, precision="f64", tol=1e-10, maxit=10):
     """
     if precision not in ("f64", "mixed"):
         raise ValueError("precision must be 'f64' or 'mixed'")
-    items = []
+    ops, Bs, meta = [], [], []
     for H, b in systems:
         if getattr(H, "mode", "N") != "N":
             raise NotImplementedError("grouped solves are mode N only")
         B, one = dv.prepare_rhs(b)
-        if B.shape[0] != H.shape[0]:
-            raise ValueError("right-hand side has %d rows, operator %d" % (B.shape[0], H.shape[0]))
-        items.append((H, (B.clone().contiguous(), one, b)))
-    if not items:
-        return ([], 0, []) if precision == "mixed" else []
-    n, ops = _arrays(items)
-    Bs = [t for _, (t, _, _) in items]
-    bp = (ctypes.c_void_p * n)(*[t.data_ptr() for t in Bs])
-    ld = (ctypes.c_int * n)(*[t.shape[1] for t in Bs])
-    nr = (ctypes.c_int * n)(*[t.shape[1] for t in Bs])
-    lib = L.lib()
+        ops.append(H)
+        Bs.append(B.clone().contiguous())
+        meta.append((one, b))
     if precision == "f64":
-        L.check(lib.slu_ulv_solve_grouped(L.handle(), n, ops, bp, ld, nr))
-        return [dv.finish(t, ref, one) for t, (_, (_, one, ref)) in zip(Bs, items)]
-    Xs = [torch.empty_like(t) for t in Bs]
-    xp = (ctypes.c_void_p * n)(*[t.data_ptr() for t in Xs])
-    it = ctypes.c_int()
-    rr = (ctypes.c_double * n)()
-    L.check(lib.slu_refine_grouped(L.handle(), n, ops, bp, ld, xp, ld, nr, float(tol),
-                                   int(maxit), ctypes.byref(it), rr))
-    xs = [dv.finish(t, ref, one) for t, (_, (_, one, ref)) in zip(Xs, items)]
-    return xs, it.value, list(np.frombuffer(rr, dtype=np.float64))
+        out = solve_grouped_device(ops, Bs)
+        return [dv.finish(t, ref, one) for t, (one, ref) in zip(out, meta)]
+    Xs, it, rr = solve_grouped_device(ops, Bs, "mixed", tol, maxit)
+    return [dv.finish(t, ref, one) for t, (one, ref) in zip(Xs, meta)], it, rr

@@ -30,6 +30,10 @@ def samples_for(rk, nl, fac):
 class HBSMAT:
     """HBS matrix (weak admissibility) with randomized construction and ULV solve."""
 
+    # null-space rule of the compression (slu_hbs_set_null_space): 0 is
+    # HBSnew.compute_UV's Q[:, -n:]
+    _null_mode = 0
+
     def __init__(self, A=None, tree=None, quad=True):
         self.mode = "N"
         self._op = None
@@ -167,6 +171,7 @@ class HBSMAT:
         self.nSamples = s
         N = self.shape[0]
         self._new_op(N, self.L, self.perm)
+        L.check(L.lib().slu_hbs_set_null_space(self._op, int(self._null_mode)))
         L.check(L.lib().slu_hbs_compress(L.handle(), self._op, int(self.Nb), int(rk), int(s),
                                          L.ptr(Omd), L.ptr(Psid), L.ptr(Yd), L.ptr(Zd),
                                          int(bool(compute_ULV))))

@@ -3,12 +3,18 @@
     python -m sslablu_gb300.microbench tc_gemm [--m 4096 --n 261 --k 4096 --reps 20]
     python -m sslablu_gb300.microbench f64_gemm [...]
 
+    python -m sslablu_gb300.microbench compress [--m 4096 --reps 5]
+
 tc_gemm : slu_gemm_split3 (tcgen05 split-BF16x3, float32 accumulation)
 f64_gemm: slu_gemm_batched (float64 CUDA-core GEMM) on the same shape
 The default shape is the sketch product of an N = 4096 dense block with the
 261 Gaussian samples of the rank-32 / leaf-64 HBS compression.  Prints one
 JSON line with the median time, the tensor FLOP rate (6 split products) and
 the effective rate (2 m n k).
+compress: HBSMAT.construct(32, compute_ULV=True) of a synthetic exact HBS
+operator of size m (leaf 64, rank 32, singular values 1 -> 1e-12), the
+sketches sampled through the resident operator; prints the median time and
+the relative error of the compressed operator's apply.
 """
 import argparse
 import json
@@ -22,13 +28,15 @@ from . import _lib
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("kernel", choices=["tc_gemm", "f64_gemm"])
+    ap.add_argument("kernel", choices=["tc_gemm", "f64_gemm", "compress"])
     ap.add_argument("--m", type=int, default=4096)
     ap.add_argument("--n", type=int, default=261)
     ap.add_argument("--k", type=int, default=4096)
     ap.add_argument("--reps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     a = ap.parse_args()
+    if a.kernel == "compress":
+        return compress(a)
     m, n, k = a.m, a.n, a.k
     rng = np.random.default_rng(0)
     A = torch.from_numpy(rng.standard_normal((m, k))).cuda()
@@ -65,6 +73,33 @@ def main():
     print(json.dumps({"kernel": a.kernel, "m": m, "n": n, "k": k, "median_ms": 1e3 * t,
                       "tensor_tflops": tensor / t / 1e12, "effective_tflops": eff / t / 1e12,
                       "relerr": err}))
+
+
+def compress(a):
+    import time
+    from .matAssembly.HBS.HBSnew import HBSMAT
+    from .synthetic import decaying_sigma, random_hbs_factors
+    N = a.m
+    Lv = int(np.log2(N // 64)) + 1
+    np.random.seed(1)
+    U, D, V, Nbvec = random_hbs_factors(32, 64, Lv, quad=False, sigma=decaying_sigma(32))
+    A = HBSMAT().set_mats(U, D, V, list(Nbvec), fac=2)
+    ts = []
+    H = None
+    for i in range(a.warmup + a.reps):
+        H = HBSMAT(A, tree=None, quad=False)
+        H.set_Nbvec(list(Nbvec))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        H.construct(32, True)
+        torch.cuda.synchronize()
+        if i >= a.warmup:
+            ts.append(time.perf_counter() - t0)
+    x = np.random.default_rng(2).standard_normal((N, 4))
+    err = float(np.linalg.norm(H.matmat(x) - A.matmat(x)) / np.linalg.norm(A.matmat(x)))
+    print(json.dumps({"kernel": "compress", "N": N, "levels": Lv, "rank": 32,
+                      "samples": H.nSamples, "median_ms": 1e3 * statistics.median(ts),
+                      "apply_relerr": err}))
 
 
 if __name__ == "__main__":

@@ -22,6 +22,13 @@ Scheduling (continuous batching):
   * each worker owns one CUDA stream and one library handle; a batch is
     pinned host -> device copy, solve, device -> pinned host copy.
 
+Grouped dispatch (``group_solve`` given): an idle worker takes the pending
+requests of every resident operator that has no batch in flight (each up to
+``max_batch_rhs`` columns, oldest operators first, up to ``max_group_rhs``
+columns in all) and solves them in one grouped call, whose launches serve all
+of those operators at once (sslablu_gb300.grouped).  The group's right-hand
+sides travel as one flat pinned block each way.
+
 Admission by footprint: ``admit`` factors an operator only when the resident
 footprint plus its own fits the budget; otherwise it waits (in FIFO order)
 until ``retire`` frees memory.
@@ -83,15 +90,36 @@ def hbs_solver(H, precision="f64", tol=1e-10, maxit=10):
     return mixed
 
 
+def hbs_group_solver(precision="f64", tol=1e-10, maxit=10):
+    """Grouped device solve for SolveServer(group_solve=...): given HBSMATs,
+    one flat float64 device block and its layout [(offset, N, c)], returns
+    the flat block of solutions in the same layout."""
+    from .grouped import solve_grouped_device
+
+    def run(ops, flat, layout):
+        Bs = [flat[o:o + n * c].view(n, c) for o, n, c in layout]
+        if precision == "f64":
+            solve_grouped_device(ops, Bs)
+            return flat
+        out = torch.empty_like(flat)
+        Xs = [out[o:o + n * c].view(n, c) for o, n, c in layout]
+        solve_grouped_device(ops, Bs, "mixed", tol, maxit, Xs=Xs)
+        return out
+    return run
+
+
 def rb_solver(rb):
     """Device solve callable for a factored RedBlackSolver (either precision)."""
     return lambda X: rb.solve(X)
 
 
 class SolveServer:
-    def __init__(self, budget_bytes, workers=4, max_batch_rhs=64):
+    def __init__(self, budget_bytes, workers=4, max_batch_rhs=64, group_solve=None,
+                 max_group_rhs=4096):
         self.budget = int(budget_bytes)
         self.max_batch = int(max_batch_rhs)
+        self.group_solve = group_solve
+        self.max_group = int(max_group_rhs)
         self.resident = collections.OrderedDict()
         self.waiting_admissions = collections.deque()
         self.pending = collections.defaultdict(collections.deque)
@@ -144,7 +172,34 @@ class SolveServer:
     def _now(self):
         return time.perf_counter() - self._t0
 
+    def _take(self, key):
+        dq = self.pending[key]
+        reqs, cols = [], 0
+        while dq and (not reqs or cols + dq[0].B.shape[1] <= self.max_batch):
+            r = dq.popleft()
+            reqs.append(r)
+            cols += r.B.shape[1]
+        self.resident[key].busy = True
+        return reqs, cols
+
+    def _pick_group(self):
+        keys = [k for k, dq in self.pending.items()
+                if dq and k in self.resident and not self.resident[k].busy]
+        if not keys:
+            return None
+        keys.sort(key=lambda k: self.pending[k][0].t_arrival)
+        job, total = [], 0
+        for k in keys:
+            if job and total >= self.max_group:
+                break
+            reqs, cols = self._take(k)
+            job.append((k, reqs))
+            total += cols
+        return job
+
     def _pick_batch(self):
+        if self.group_solve is not None:
+            return self._pick_group()
         best, best_t = None, None
         for key, dq in self.pending.items():
             if not dq:
@@ -156,14 +211,35 @@ class SolveServer:
                 best, best_t = key, dq[0].t_arrival
         if best is None:
             return None
-        dq = self.pending[best]
-        reqs, cols = [], 0
-        while dq and (not reqs or cols + dq[0].B.shape[1] <= self.max_batch):
-            r = dq.popleft()
-            reqs.append(r)
-            cols += r.B.shape[1]
-        self.resident[best].busy = True
-        return best, reqs
+        return [(best, self._take(best)[0])]
+
+    def _solve_one(self, key, reqs, stream):
+        res = self.resident[key]
+        with torch.cuda.stream(stream):
+            Bh = torch.from_numpy(np.concatenate([r.B for r in reqs], axis=1)).pin_memory()
+            Bd = Bh.to("cuda", non_blocking=True)
+            Xd = res.solve(Bd)
+            Xh = torch.empty(Xd.shape, dtype=Xd.dtype, pin_memory=True)
+            Xh.copy_(Xd, non_blocking=True)
+            stream.synchronize()
+        return [Xh.numpy()]
+
+    def _solve_group(self, job, stream):
+        blocks = [np.concatenate([r.B for r in reqs], axis=1) for _, reqs in job]
+        layout, off = [], 0
+        for b in blocks:
+            layout.append((off, b.shape[0], b.shape[1]))
+            off += b.size
+        ops = [self.resident[k].op for k, _ in job]
+        with torch.cuda.stream(stream):
+            Bh = torch.from_numpy(np.concatenate([b.ravel() for b in blocks])).pin_memory()
+            Bd = Bh.to("cuda", non_blocking=True)
+            Xd = self.group_solve(ops, Bd, layout)
+            Xh = torch.empty(Xd.shape, dtype=Xd.dtype, pin_memory=True)
+            Xh.copy_(Xd, non_blocking=True)
+            stream.synchronize()
+        flat = Xh.numpy()
+        return [flat[o:o + n * c].reshape(n, c) for o, n, c in layout]
 
     def _worker(self, w):
         stream = torch.cuda.Stream()
@@ -171,34 +247,34 @@ class SolveServer:
             job = self._jobs.get()
             if job is None:
                 return
-            key, reqs = job
-            res = self.resident[key]
             t_start = self._now()
             try:
-                with torch.cuda.stream(stream):
-                    Bh = torch.from_numpy(np.concatenate([r.B for r in reqs], axis=1)).pin_memory()
-                    Bd = Bh.to("cuda", non_blocking=True)
-                    Xd = res.solve(Bd)
-                    Xh = torch.empty(Xd.shape, dtype=Xd.dtype, pin_memory=True)
-                    Xh.copy_(Xd, non_blocking=True)
-                    stream.synchronize()
-                X, err = Xh.numpy(), None
+                if self.group_solve is not None:
+                    Xs, err = self._solve_group(job, stream), None
+                else:
+                    Xs, err = self._solve_one(job[0][0], job[0][1], stream), None
             except Exception as e:   # the requests complete with the error
-                X, err = None, e
+                Xs, err = [None] * len(job), e
             t_done = self._now()
-            c = 0
-            for r in reqs:
-                k = r.B.shape[1]
-                r.X = None if X is None else X[:, c:c + k].copy()
-                r.error = err
-                r.t_start, r.t_done = t_start, t_done
-                c += k
+            done, ncols = [], 0
+            for (key, reqs), X in zip(job, Xs):
+                c = 0
+                for r in reqs:
+                    k = r.B.shape[1]
+                    r.X = None if X is None else X[:, c:c + k].copy()
+                    r.error = err
+                    r.t_start, r.t_done = t_start, t_done
+                    c += k
+                done.extend(reqs)
+                ncols += c
             with self._lock:
-                res.busy = False
-                res.last_used = t_done
-                self.done.extend(reqs)
+                for key, _ in job:
+                    res = self.resident[key]
+                    res.busy = False
+                    res.last_used = t_done
+                self.done.extend(done)
                 self.batches += 1
-                self.batch_rhs.append(c)
+                self.batch_rhs.append(ncols)
                 self._idle += 1
                 self._lock.notify_all()
 
@@ -302,16 +378,22 @@ def main():
     ap.add_argument("--workers", type=int, default=8)
     ap.add_argument("--shift", type=float, default=16.0)
     ap.add_argument("--max-batch", type=int, default=64)
+    ap.add_argument("--group-workers", type=int, default=2)
     ap.add_argument("--seed", type=int, default=20261205)
     a = ap.parse_args()
     ops = _build_hbs_ops(a.operators, a.seed, shift=a.shift)
     sizes = {k: n for k, _, n in ops}
     out = {"workload": "%d resident exact-HBS operators (N in 2048/4096/8192, leaf 64, rank 32, "
                        "leaf shift %g), Poisson arrivals %.0f req/s, %d requests, 1-64 RHS each, "
-                       "%d worker streams" % (a.operators, a.shift, a.rate, a.requests, a.workers)}
-    # the plain trace warms the device first, then each arm serves the same trace
-    for precision in ("f64", "mixed"):
-        srv = SolveServer(budget_bytes=64 << 30, workers=a.workers, max_batch_rhs=a.max_batch)
+                       "%d worker streams per-operator, %d grouped"
+                       % (a.operators, a.shift, a.rate, a.requests, a.workers, a.group_workers)}
+    # a short trace warms each arm first, then every arm serves the same trace
+    arms = [("f64", False), ("mixed", False), ("f64", True), ("mixed", True)]
+    for precision, grouped in arms:
+        name = ("grouped_" if grouped else "") + precision
+        gs = hbs_group_solver(precision) if grouped else None
+        srv = SolveServer(budget_bytes=64 << 30, workers=a.group_workers if grouped else a.workers,
+                          max_batch_rhs=a.max_batch, group_solve=gs)
         try:
             for key, H, n in ops:
                 srv.admit(key, lambda H=H: H, H.nbytes, lambda op, p=precision: hbs_solver(op, p))
@@ -335,10 +417,12 @@ def main():
                                                 np.linalg.norm(r.B, axis=0))))
             st["worst_relres"] = worst
             st["errors"] = sum(r.error is not None for r in done)
-            out[precision] = st
+            out[name] = st
         finally:
             srv.close()
     out["mixed_vs_f64_rhs_per_s"] = out["mixed"]["rhs_per_s"] / out["f64"]["rhs_per_s"]
+    out["grouped_mixed_vs_f64_rhs_per_s"] = (out["grouped_mixed"]["rhs_per_s"] /
+                                             out["f64"]["rhs_per_s"])
     print(json.dumps(out))
 
 

@@ -23,6 +23,19 @@ the large outputs are stored.  Fixtures written (all small):
                      kernel block-tridiagonal system (truncation dominated)
   rbhbs_gauss.npz    the same on a Gaussian-kernel system that rank 16
                      resolves to a ~1e-13 residual
+  slab_trees.npz     slabTree on lines, rectangles (binary and quad) and a plane
+                     in 3-D: perm_leaf, nleaves, nlevels, leaf boundary DOFs and
+                     interface DOFs
+  hbstorch.npz       HBStorch.HBSMAT(tree=slabTree).construct(k, Om, Psi, Y, Z)
+                     of an exact HBS matrix in a rectangle tree's ordering, with
+                     the rkHBS assembler's sample count (s < 2n at the leaves):
+                     factors, matmat / rmatmat, and the ULVsparse solution of
+                     the compressed operator (HBStorch's own compute_ULV and
+                     solve do not run upstream)
+  assembler.npz      matAssembler rkHBS and dense assembly of a stMap-like
+                     operator (exact HBS in tree order on a 16 x 16 grid)
+
+Run one group with ``python tests/golden/make_golden.py <name> ...``.
 """
 import contextlib
 import io
@@ -234,7 +247,151 @@ def rbhbs(ref):
     np.savez_compressed(os.path.join(HERE, "rbhbs_kernel.npz"), **out)
 
 
+SLAB_TREE_CASES = [
+    ("line256", "line", 256, False, 32),
+    ("rect16_bin", "rect16", 0, False, 16),
+    ("rect16_quad", "rect16", 0, True, 16),
+    ("plane3d_bin", "plane32", 0, False, 128),
+    ("plane3d_quad", "plane32", 0, True, 64),
+    ("line2d", "line2d", 128, False, 8),
+    ("rect17_bin", "rect17", 0, False, 20),
+    ("rect17_quad", "rect17", 0, True, 20),
+]
+
+
+def slab_cloud(kind, n=0):
+    """Point clouds of the slab tree cases (regenerated by the tests)."""
+    if kind == "line":
+        return np.linspace(0, 1, n)
+    if kind == "line2d":
+        return np.stack([np.linspace(0, 1, n), np.full(n, 0.25)], 1)
+    if kind == "rect16":
+        return np.stack(np.meshgrid(np.linspace(0, 1, 16), np.linspace(0, 2, 16), indexing="ij"),
+                        -1).reshape(-1, 2)
+    if kind == "rect17":
+        return np.stack(np.meshgrid(np.linspace(0, 1, 17), np.linspace(0, 1, 17), indexing="ij"),
+                        -1).reshape(-1, 2)
+    if kind == "plane32":
+        g = np.stack(np.meshgrid(np.linspace(0, 1, 32), np.linspace(0, 1, 32), indexing="ij"),
+                     -1).reshape(-1, 2)
+        return np.concatenate([np.full((g.shape[0], 1), 0.5), g], 1)
+    raise ValueError(kind)
+
+
+def tree_record(t, prefix, out):
+    """perm/nleaves/nlevels and the DOF lists of a built slabTree."""
+    out[prefix + "perm"] = np.asarray(t.perm_leaf)
+    out[prefix + "shape"] = np.array([t.nleaves, t.nlevels])
+    bd, bl, idofs, il = [], [], [], []
+    for b in t.get_leaves():
+        node = t.get_node(b)
+        for side in ("left", "down", "up", "right"):
+            v = np.asarray(node.bDOFs[side]) if node.bDOFs is not None else np.zeros(0, int)
+            bd.append(v)
+            bl.append(len(v))
+    for b in sorted(t._boxes):
+        node = t.get_node(b)
+        v = np.asarray(node.iDOFs) if node.iDOFs is not None else np.zeros(0, int)
+        idofs.append(v)
+        il.append(len(v) if node.iDOFs is not None else -1)
+    out[prefix + "bdofs"] = np.concatenate(bd).astype(np.int64)
+    out[prefix + "blen"] = np.array(bl)
+    out[prefix + "idofs"] = np.concatenate(idofs).astype(np.int64)
+    out[prefix + "ilen"] = np.array(il)
+
+
+def slab_trees(ref):
+    import matAssembly.HBS.slabTree as ST
+    out = {}
+    for name, kind, n, quad, leaf in SLAB_TREE_CASES:
+        with contextlib.redirect_stdout(QUIET):
+            t = ST.slabTree(slab_cloud(kind, n), quad, leaf)
+        tree_record(t, name + "_", out)
+    np.savez_compressed(os.path.join(HERE, "slab_trees.npz"), **out)
+
+
+def exact_in_tree_order(k, nl, L, seed, perm):
+    """Dense A with A[perm][:, perm] equal to an exact random HBS matrix."""
+    np.random.seed(seed)
+    S, _ = gen_random_hbs(k, nl, L, quad=False)
+    M = S.matmat(np.eye(S.shape[0]))
+    A = np.zeros_like(M)
+    A[np.ix_(perm, perm)] = M
+    return A
+
+
+def hbstorch(ref):
+    import torch
+    import matAssembly.HBS.slabTree as ST
+    import matAssembly.HBS.HBStorch as HT
+    import matAssembly.HBS.ULVsparse as US
+    with contextlib.redirect_stdout(QUIET):
+        tree = ST.slabTree(slab_cloud("rect16"), False, 16)
+    perm = np.asarray(tree.perm_leaf)
+    k, leaf = 4, 16
+    A = exact_in_tree_order(k, leaf, tree.nlevels, 7, perm)
+    s = max(2 * k, leaf) + k + 10
+    rng = np.random.default_rng(5)
+    Om = rng.standard_normal((256, s))
+    Psi = rng.standard_normal((256, s))
+    x = rng.standard_normal((256, 3))
+    H = HT.HBSMAT(device="cpu", tree=tree, quad=False)
+    with contextlib.redirect_stdout(QUIET):
+        H.construct(k, Om, Psi, A @ Om, A.T @ Psi)
+    out = {"perm": perm, "k": k, "s": s, "Om": Om, "Psi": Psi, "x": x,
+           "Nbvec": np.array(H.Nbvec), "nSamples": H.nSamples, "nbytes": H.nbytes,
+           "Ax": H.matmat(x), "ATx": H.rmatmat(x)}
+    for name, lst in (("U", H.Umats), ("V", H.Vmats), ("D", H.Dmats)):
+        for t, m in enumerate(lst):
+            out["%s%d" % (name, t)] = np.asarray(m.detach().cpu().numpy())
+    # ULV solve of the compressed operator through upstream ULVsparse (numpy)
+    flat = lambda m: m.detach().cpu().numpy().reshape(-1, m.shape[2])
+    Umats = [flat(u) for u in H.Umats]
+    Vmats = [flat(v) for v in H.Vmats]
+    Dmats = [flat(d) for d in H.Dmats]
+    Nbvec = [int(d.shape[0]) for d in H.Dmats]
+    with contextlib.redirect_stdout(QUIET):
+        Q, W, Uu, R, NN = US.compute_ULV(Umats, Dmats, Vmats, Nbvec)
+        b = A @ x
+        uh = US.solve(Umats, Dmats, Q, W, Uu, R, NN, Nbvec, b[perm, :])
+    u = np.zeros_like(uh)
+    u[perm, :] = uh
+    out["b"] = b
+    out["sol"] = u
+    np.savez_compressed(os.path.join(HERE, "hbstorch.npz"), **out)
+
+
+def assembler(ref):
+    import scipy.sparse.linalg as sla
+    import matAssembly.matAssembler as MA
+    import matAssembly.HBS.slabTree as ST
+    XX = slab_cloud("rect16")
+    with contextlib.redirect_stdout(QUIET):
+        tree = ST.slabTree(XX, False, 8)
+    perm = np.asarray(tree.perm_leaf)
+    A = exact_in_tree_order(3, 8, tree.nlevels, 9, perm)
+    lin = sla.aslinearoperator(A)
+    stmap = types.SimpleNamespace(A=lin, XXI=XX)
+    np.random.seed(11)
+    with contextlib.redirect_stdout(QUIET):
+        H = MA.rkHMatAssembler(8, 3).assemble(stmap)
+    x = np.random.default_rng(12).standard_normal((256, 2))
+    with contextlib.redirect_stdout(QUIET):
+        M = MA.denseMatAssembler().assemble(stmap)
+    np.savez_compressed(os.path.join(HERE, "assembler.npz"), perm=perm, x=x, Ax=H.matmat(x),
+                        ATx=H.rmatmat(x), nSamples=H.nSamples, nbytes=H.nbytes,
+                        dense_ok=np.array(np.array_equal(M, A)))
+
+
 def main():
+    only = sys.argv[1:]
+    if only:
+        refshim.install()
+        with contextlib.redirect_stdout(QUIET):
+            P = refshim.import_pipeline()
+        for name in only:
+            globals()[name](P)
+        return
     ref = refshim.import_hot_path()
     P = refshim.import_pipeline()
     rb_dense(ref)
@@ -246,6 +403,9 @@ def main():
     c1_poisson(ref, P)
     rbhbs(ref)
     rbhbs_gauss(ref)
+    slab_trees(ref)
+    hbstorch(ref)
+    assembler(ref)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -1,7 +1,8 @@
 """Serving loop: each request's result equals a solve of that request alone
 (float64 path: to rounding, 1e-14; mixed path: both meet the 1e-10 relative
 residual and agree to 1e-8), with requests batched across arrivals and
-operators overlapping on several streams; admission by footprint."""
+operators overlapping on several streams or grouped into shared launches;
+admission by footprint."""
 import numpy as np
 import pytest
 
@@ -25,12 +26,15 @@ def _operators(precision):
     return ops
 
 
+@pytest.mark.parametrize("grouped", [False, True])
 @pytest.mark.parametrize("precision", ["f64", "mixed"])
-def test_served_results_equal_solo(precision):
+def test_served_results_equal_solo(precision, grouped):
     need_gpu()
-    from sslablu_gb300.serving import SolveServer, poisson_trace
+    from sslablu_gb300.serving import SolveServer, hbs_group_solver, poisson_trace
     ops = _operators(precision)
-    srv = SolveServer(budget_bytes=1 << 34, workers=3, max_batch_rhs=24)
+    gs = hbs_group_solver(precision) if grouped else None
+    srv = SolveServer(budget_bytes=1 << 34, workers=2 if grouped else 3, max_batch_rhs=24,
+                      group_solve=gs)
     try:
         for key, (H, solve, n) in ops.items():
             srv.admit(key, lambda H=H: H, H.nbytes, lambda op, s=solve: s)

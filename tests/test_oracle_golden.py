@@ -132,3 +132,91 @@ def test_package_generator_matches_oracle_generator():
         assert list(nb) == list(nb2)
         for a, b in zip(S.Umats + S.Vmats + S.Dmats, U + V + D):
             assert np.array_equal(a, b)
+
+
+def _exact_in_tree_order(k, nl, L, seed, perm):
+    """The operator of the hbstorch / assembler fixtures (see make_golden.py)."""
+    np.random.seed(seed)
+    S, _ = oh.gen_random_hbs(k, nl, L, quad=False)
+    M = S.matmat(np.eye(S.shape[0]))
+    A = np.zeros_like(M)
+    A[np.ix_(perm, perm)] = M
+    return A
+
+
+def test_slab_tree_mirror_matches_upstream(golden):
+    """sslablu_gb300's slabTree (host code of the tree protocol) against
+    upstream slabTree: perm_leaf, nleaves, nlevels, leaf boundary DOFs and
+    interface DOFs, on lines, rectangles (binary, quad) and a plane in 3-D,
+    including split lines that hold points (which both halves keep)."""
+    from sslablu_gb300.matAssembly.HBS.slabTree import slabTree
+    g = golden("slab_trees")
+    cases = [("line256", "line", 256, False, 32), ("rect16_bin", "rect16", 0, False, 16),
+             ("rect16_quad", "rect16", 0, True, 16), ("plane3d_bin", "plane32", 0, False, 128),
+             ("plane3d_quad", "plane32", 0, True, 64), ("line2d", "line2d", 128, False, 8),
+             ("rect17_bin", "rect17", 0, False, 20), ("rect17_quad", "rect17", 0, True, 20)]
+    for name, kind, n, quad, leaf in cases:
+        t = slabTree(_cloud(kind, n), quad, leaf)
+        p = name + "_"
+        assert np.array_equal(t.perm_leaf, g[p + "perm"]), name
+        assert [t.nleaves, t.nlevels] == list(g[p + "shape"]), name
+        sides = [np.asarray(t.get_node(b).bDOFs[sd]) if t.get_node(b).bDOFs is not None
+                 else np.zeros(0, np.int64)
+                 for b in t.get_leaves() for sd in ("left", "down", "up", "right")]
+        bd = np.concatenate(sides).astype(np.int64)
+        assert np.array_equal(bd, g[p + "bdofs"]), name
+        il = [len(t.get_node(b).iDOFs) if t.get_node(b).iDOFs is not None else -1
+              for b in sorted(t._boxes)]
+        assert il == list(g[p + "ilen"]), name
+        idofs = [np.asarray(t.get_node(b).iDOFs) for b in sorted(t._boxes)
+                 if t.get_node(b).iDOFs is not None]
+        cat = np.concatenate(idofs).astype(np.int64) if idofs else np.zeros(0, np.int64)
+        assert np.array_equal(cat, g[p + "idofs"]), name
+
+
+def _cloud(kind, n=0):
+    if kind == "line":
+        return np.linspace(0, 1, n)
+    if kind == "line2d":
+        return np.stack([np.linspace(0, 1, n), np.full(n, 0.25)], 1)
+    if kind == "rect16":
+        return np.stack(np.meshgrid(np.linspace(0, 1, 16), np.linspace(0, 2, 16), indexing="ij"),
+                        -1).reshape(-1, 2)
+    if kind == "rect17":
+        return np.stack(np.meshgrid(np.linspace(0, 1, 17), np.linspace(0, 1, 17), indexing="ij"),
+                        -1).reshape(-1, 2)
+    g = np.stack(np.meshgrid(np.linspace(0, 1, 32), np.linspace(0, 1, 32), indexing="ij"),
+                 -1).reshape(-1, 2)
+    return np.concatenate([np.full((g.shape[0], 1), 0.5), g], 1)
+
+
+def test_oracle_hbstorch_rule_matches_upstream(golden):
+    """The oracle with HBStorch's null-space rule (s < 2n at the leaves)
+    reproduces upstream HBStorch's factors (D, and U/V up to column signs) and
+    outputs; the ULV solve of those factors matches upstream ULVsparse."""
+    g = golden("hbstorch")
+    perm = g["perm"]
+    k = int(g["k"])
+    A = _exact_in_tree_order(k, 16, 5, 7, perm)
+    O = oh.OracleHBS(A, perm, 16, 5, 2)
+    Om, Psi = g["Om"], g["Psi"]
+    O.compress_from_sketches(k, Om[perm], Psi[perm], (A @ Om)[perm], (A.T @ Psi)[perm],
+                             null_after_n=True)
+    # leaf D exactly; above the leaves the blocks are expressed in the child
+    # bases, which an SVD fixes only up to column signs
+    for t in range(5):
+        ref = g["D%d" % t].reshape(O.Dmats[t].shape)
+        got = O.Dmats[t] if t == 0 else np.abs(O.Dmats[t])
+        assert relerr(got, ref if t == 0 else np.abs(ref)) < 1e-12
+    for t in range(4):
+        for nm, mats in (("U", O.Umats), ("V", O.Vmats)):
+            ref = g["%s%d" % (nm, t)].reshape(mats[t].shape)
+            assert relerr(np.abs(mats[t]), np.abs(ref)) < 1e-12
+    x = g["x"]
+    assert relerr(O.matmat(x), g["Ax"]) < 1e-13
+    assert relerr(O.rmatmat(x), g["ATx"]) < 1e-13
+    assert relerr(O.solve(g["b"]), g["sol"]) < 1e-12
+    # HBSnew's rule spans part of the sketch's range here (s < 2n): different factors
+    O2 = oh.OracleHBS(A, perm, 16, 5, 2)
+    O2.compress_from_sketches(k, Om[perm], Psi[perm], (A @ Om)[perm], (A.T @ Psi)[perm])
+    assert relerr(O2.matmat(x), g["Ax"]) > 1e-8
