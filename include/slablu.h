@@ -165,7 +165,10 @@ int slu_refine_grouped(slu_handle_t h, int count, const slu_hbs_t* ops, const do
                        double tol, int maxit, int* iters_out, double* relres_out);
 
 /* Diagnostics: one float64 mode-N solve (as slu_ulv_solve) with a CUDA event
- * pair around each kernel launch; returns after the solve completes.
+ * pair around each kernel launch; returns after the solve completes.  The
+ * solve is queued behind a ~0.5 ms device-side sleep, so every launch is
+ * already queued when the device reaches it and the event pairs measure
+ * device time only.
  * ms_out[k] is the device time of launch k (launch order), level_out[k] its
  * tree level and kind_out[k] its sweep (0 forward, 1 root, 2 backward), for
  * k < cap (host arrays, each may be NULL); *nlaunch receives the number of

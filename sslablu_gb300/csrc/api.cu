@@ -314,6 +314,8 @@ int slu_ulv_solve_timed(slu_handle_t h, slu_hbs_t op, double* B, int ldb, int nr
     double* scratch = h->h.ws.take<double>(bytes / sizeof(double));
     const size_t stride = ((sizeof(double) * (size_t)H.N * nrhs + 255) & ~size_t(255)) / 8;
     slu::LaunchTimes lt;
+    lt.reserve(2 * (size_t)H.L);
+    slu::enqueue_device_lead(st, 500);
     slu::ulv_solve_fused<double>(st, H, B, ldb, nrhs, scratch, stride, &lt);
     SLU_CHECK_CUDA(cudaStreamSynchronize(st));
     const int n = (int)lt.level.size();

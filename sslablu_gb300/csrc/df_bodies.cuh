@@ -34,13 +34,67 @@ __device__ __forceinline__ DF split_d(double x) {
   return r;
 }
 
+constexpr int kBatch = 8;   // global loads in flight per thread in the copies
+
 // Stage a rows x cols (hi, lo) block into shared memory with pitch ld.
 __device__ inline void stage2(float* Sh, float* Sl, int ld, const float* __restrict__ Ah,
                               const float* __restrict__ Al, int rows, int cols) {
-  for (int e = threadIdx.x; e < rows * cols; e += blockDim.x) {
-    int i = e / cols, j = e - i * cols;
-    Sh[i * ld + j] = Ah[e];
-    Sl[i * ld + j] = Al[e];
+  const int total = rows * cols, step = blockDim.x;
+  for (int e0 = threadIdx.x; e0 < total; e0 += kBatch * step) {
+    float h[kBatch], l[kBatch];
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      const int e = e0 + u * step;
+      if (e < total) {
+        h[u] = __ldg(Ah + e);
+        l[u] = __ldg(Al + e);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      const int e = e0 + u * step;
+      if (e < total) {
+        const int i = e / cols, j = e - i * cols;
+        Sh[i * ld + j] = h[u];
+        Sl[i * ld + j] = l[u];
+      }
+    }
+  }
+}
+
+// (xh, xl)[i * ldx + cc] for i < rows, cc < nc: from the float64 X (rows
+// perm[row0 + i], or row0 + i without perm), split into (hi, lo), or from the
+// (hi, lo) pairs `in` (rows row0 + i, leading dimension c) when X is null.
+__device__ inline void gather2(float* xh, float* xl, int ldx, const double* X, long long ldX,
+                               const int64_t* __restrict__ perm, const DF* in, int c,
+                               long long row0, int rows, int c0, int nc) {
+  const int total = rows * nc, step = blockDim.x;
+  for (int e0 = threadIdx.x; e0 < total; e0 += kBatch * step) {
+    long long r[kBatch];
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      const int e = e0 + u * step;
+      const long long row = row0 + (e < total ? e / nc : 0);
+      r[u] = (e < total && X && perm) ? __ldg(perm + row) : row;
+    }
+    DF v[kBatch];
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      const int e = e0 + u * step;
+      if (e < total) {
+        const int cc = e % nc;
+        v[u] = X ? split_d(X[r[u] * ldX + c0 + cc]) : in[r[u] * c + c0 + cc];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      const int e = e0 + u * step;
+      if (e < total) {
+        const int i = e / nc, cc = e - i * nc;
+        xh[i * ldx + cc] = v[u].h;
+        xl[i * ldx + cc] = v[u].l;
+      }
+    }
   }
 }
 
@@ -56,18 +110,7 @@ __device__ __forceinline__ void df_up_body(float* smf, int b, int c0, int nc, in
   float* Sl = Sh + n * (k + 1);
   float* xh = Sl + n * (k + 1);           // n x cpb
   float* xl = xh + n * cpb;
-  for (int e = threadIdx.x; e < n * nc; e += blockDim.x) {
-    int i = e / nc, cc = e - i * nc;
-    long long row = (long long)b * n + i;
-    DF v;
-    if (X) {
-      v = split_d(X[(perm ? perm[row] : row) * ldx + c0 + cc]);
-    } else {
-      v = in[row * c + c0 + cc];
-    }
-    xh[i * cpb + cc] = v.h;
-    xl[i * cpb + cc] = v.l;
-  }
+  gather2(xh, xl, cpb, X, ldx, perm, in, c, (long long)b * n, n, c0, nc);
   stage2(Sh, Sl, k + 1, Fh + (size_t)b * n * k, Fl + (size_t)b * n * k, n, k);
   __syncthreads();
   for (int e = threadIdx.x; e < k * nc; e += blockDim.x) {
@@ -103,20 +146,8 @@ __device__ __forceinline__ void df_down_body(float* smf, int b, int c0, int nc, 
   float* ul = uh + k * cpb;
   float* ah = ul + k * cpb;               // n x cpb accumulators
   float* al = ah + n * cpb;
-  for (int e = threadIdx.x; e < n * nc; e += blockDim.x) {
-    int i = e / nc, cc = e - i * nc;
-    long long row = (long long)b * n + i;
-    DF v = X ? split_d(X[(perm ? perm[row] : row) * ldx + c0 + cc]) : vv[row * c + c0 + cc];
-    xh[i * cpb + cc] = v.h;
-    xl[i * cpb + cc] = v.l;
-  }
-  if (Gh)
-    for (int e = threadIdx.x; e < k * nc; e += blockDim.x) {
-      int i = e / nc, cc = e - i * nc;
-      DF v = uin[((size_t)b * k + i) * c + c0 + cc];
-      uh[i * cpb + cc] = v.h;
-      ul[i * cpb + cc] = v.l;
-    }
+  gather2(xh, xl, cpb, X, ldx, perm, vv, c, (long long)b * n, n, c0, nc);
+  if (Gh) gather2(uh, ul, cpb, nullptr, 0, nullptr, uin, c, (long long)b * k, k, c0, nc);
   stage2(Sh, Sl, n + 1, Dh + (size_t)b * n * n, Dl + (size_t)b * n * n, n, n);
   __syncthreads();
   for (int e = threadIdx.x; e < n * nc; e += blockDim.x) {

@@ -129,11 +129,17 @@ struct LaunchTimes {
   ~LaunchTimes() {
     for (cudaEvent_t e : ev) cudaEventDestroy(e);
   }
+  size_t next = 0;   // events are created up front (reserve), recorded in order
+  void reserve(size_t launches) {
+    while (ev.size() < 2 * launches) {
+      cudaEvent_t e = nullptr;
+      SLU_CHECK_CUDA(cudaEventCreate(&e));
+      ev.push_back(e);
+    }
+  }
   void mark(cudaStream_t st) {
-    cudaEvent_t e = nullptr;
-    SLU_CHECK_CUDA(cudaEventCreate(&e));
-    ev.push_back(e);
-    SLU_CHECK_CUDA(cudaEventRecord(e, st));
+    if (next == ev.size()) reserve(ev.size() / 2 + 1);
+    SLU_CHECK_CUDA(cudaEventRecord(ev[next++], st));
   }
   void done(int lvl, int k) {
     level.push_back(lvl);
@@ -146,6 +152,11 @@ struct LaunchTimes {
 template <typename T>
 void ulv_solve_fused(cudaStream_t st, const Hbs& H, T* B, int ldb, int c, T* scratch,
                      size_t stride, LaunchTimes* times = nullptr);
+// Enqueues a kernel that only sleeps for about `us` microseconds (a fixed
+// number of __nanosleep calls, no waiting on anything), so that the host can
+// queue the launches that follow before the device reaches them: their event
+// timestamps then measure device time, not host enqueue gaps.
+void enqueue_device_lead(cudaStream_t st, int us);
 // Fused per-level apply (hbs_apply.cu); scratch of hbs_apply_scratch_elems doubles.
 size_t hbs_apply_scratch_elems(const Hbs& H, int c);
 void hbs_apply_fused(cudaStream_t st, const Hbs& H, bool trans, const double* X, int ldx,

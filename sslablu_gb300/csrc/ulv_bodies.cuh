@@ -18,11 +18,89 @@ namespace slu {
 namespace ulvk {
 
 
+// Global -> shared copies keep kBatch loads in flight per thread: issued as
+// one group, then stored, so a copy of e elements costs about
+// e / (kBatch * blockDim) memory round trips instead of e / blockDim.
+constexpr int kBatch = 8;
+
+// S[i * ld + j] = A[i * cols + j], a rows x cols block.
 template <typename T>
 __device__ inline void stage(T* S, int ld, const T* __restrict__ A, int rows, int cols) {
-  for (int e = threadIdx.x; e < rows * cols; e += blockDim.x) {
-    int i = e / cols, j = e - i * cols;
-    S[i * ld + j] = A[e];
+  const int total = rows * cols, step = blockDim.x;
+  for (int e0 = threadIdx.x; e0 < total; e0 += kBatch * step) {
+    T v[kBatch];
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      const int e = e0 + u * step;
+      if (e < total) v[u] = __ldg(A + e);
+    }
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      const int e = e0 + u * step;
+      if (e < total) {
+        const int i = e / cols;
+        S[i * ld + (e - i * cols)] = v[u];
+      }
+    }
+  }
+}
+
+// x[i * ldx + cc] = src[r_i * lds + c0 + cc] for i < rows, cc < nc, with
+// r_i = perm[row0 + i] when perm is given, else row0 + i.
+template <typename T>
+__device__ inline void gather(T* x, int ldx, const T* src, long long lds,
+                              const int64_t* __restrict__ perm, long long row0, int rows,
+                              int c0, int nc) {
+  const int total = rows * nc, step = blockDim.x;
+  for (int e0 = threadIdx.x; e0 < total; e0 += kBatch * step) {
+    long long r[kBatch];
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      const int e = e0 + u * step;
+      r[u] = 0;
+      if (e < total) {
+        const long long row = row0 + e / nc;
+        r[u] = perm ? __ldg(perm + row) : row;
+      }
+    }
+    T v[kBatch];
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      const int e = e0 + u * step;
+      if (e < total) v[u] = src[r[u] * lds + c0 + (e % nc)];
+    }
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      const int e = e0 + u * step;
+      if (e < total) {
+        const int i = e / nc;
+        x[i * ldx + (e - i * nc)] = v[u];
+      }
+    }
+  }
+}
+
+// B[perm[row0 + i] * ldb + c0 + cc] = y[i * ldy + cc] for i < rows, cc < nc,
+// with the permutation loads batched.
+template <typename T>
+__device__ inline void scatter(T* B, long long ldb, const int64_t* __restrict__ perm,
+                               long long row0, const T* y, int ldy, int rows, int c0, int nc) {
+  const int total = rows * nc, step = blockDim.x;
+  for (int e0 = threadIdx.x; e0 < total; e0 += kBatch * step) {
+    long long r[kBatch];
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      const int e = e0 + u * step;
+      r[u] = (e < total) ? __ldg(perm + row0 + e / nc) : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      const int e = e0 + u * step;
+      if (e < total) {
+        const int i = e / nc, cc = e - i * nc;
+        B[r[u] * ldb + c0 + cc] = y[i * ldy + cc];
+      }
+    }
   }
 }
 
@@ -91,12 +169,7 @@ __device__ __forceinline__ void ulv_fwd_body(unsigned char* sm_raw, int b, int c
   T* S = reinterpret_cast<T*>(sm_raw);       // n x (n+1)
   T* x = S + n * (n + 1);                     // n x cpb
   T* z = x + n * cpb;                         // n x cpb
-  for (int e = threadIdx.x; e < n * nc; e += blockDim.x) {
-    int i = e / nc, cc = e - i * nc;
-    long long row = (long long)b * n + i;
-    if (perm) row = perm[row];
-    x[i * cpb + cc] = src[row * lds + c0 + cc];
-  }
+  gather(x, cpb, src, lds, perm, (long long)b * n, n, c0, nc);
   stage(S, n + 1, Q + (size_t)b * n * n, n, n);
   __syncthreads();
   mvt(S, n + 1, n, n, x, cpb, z, cpb, nc);
@@ -122,11 +195,7 @@ __device__ __forceinline__ void ulv_root_body(unsigned char* sm_raw, int c0, int
   T* S = reinterpret_cast<T*>(sm_raw);
   T* x = S + n * (n + 1);
   T* y = x + n * cpb;
-  for (int e = threadIdx.x; e < n * nc; e += blockDim.x) {
-    int i = e / nc, cc = e - i * nc;
-    long long row = perm ? perm[i] : i;
-    x[i * cpb + cc] = src[row * lds + c0 + cc];
-  }
+  gather(x, cpb, src, lds, perm, 0, n, c0, nc);
   stage(S, n + 1, Q, n, n);
   __syncthreads();
   mvt(S, n + 1, n, n, x, cpb, y, cpb, nc);
@@ -134,10 +203,7 @@ __device__ __forceinline__ void ulv_root_body(unsigned char* sm_raw, int c0, int
   stage(S, n + 1, R, n, n);
   trsv_upper(S, n + 1, n, y, cpb, nc);
   if (perm) {  // single-level tree: y is the solution
-    for (int e = threadIdx.x; e < n * nc; e += blockDim.x) {
-      int i = e / nc, cc = e - i * nc;
-      B[perm[i] * ldb + c0 + cc] = y[i * cpb + cc];
-    }
+    scatter(B, ldb, perm, 0, y, cpb, n, c0, nc);
     return;
   }
   stage(S, n + 1, D, n, n);
@@ -166,15 +232,9 @@ __device__ __forceinline__ void ulv_bwd_body(unsigned char* sm_raw, int b, int c
   T* yn = vb + k * cpb;                        // k  x cpb
   T* yu = yn + k * cpb;                        // nu x cpb
   T* ynew = yu + nu * cpb;                     // n  x cpb
-  for (int e = threadIdx.x; e < k * nc; e += blockDim.x) {
-    int i = e / nc, cc = e - i * nc;
-    vb[i * cpb + cc] = Vin[((size_t)b * k + i) * c + c0 + cc];
-    yn[i * cpb + cc] = Yin[((size_t)b * k + i) * c + c0 + cc];
-  }
-  for (int e = threadIdx.x; e < nu * nc; e += blockDim.x) {
-    int i = e / nc, cc = e - i * nc;
-    yu[i * cpb + cc] = ru[((size_t)b * nu + i) * c + c0 + cc];
-  }
+  gather(vb, cpb, Vin, c, nullptr, (long long)b * k, k, c0, nc);
+  gather(yn, cpb, Yin, c, nullptr, (long long)b * k, k, c0, nc);
+  gather(yu, cpb, ru, c, nullptr, (long long)b * nu, nu, c0, nc);
   if (nu > 0) {
     // yu = ru - Uu v - R12 y_next ; then R11^{-1}
     stage(S, k + 1, Uu + (size_t)b * nu * k, nu, k);
@@ -193,10 +253,7 @@ __device__ __forceinline__ void ulv_bwd_body(unsigned char* sm_raw, int b, int c
   mv(S, n + 1, nu, n, k, yn, cpb, ynew, cpb, nc, T(1), true);
   __syncthreads();
   if (perm) {  // leaf level: scatter the solution to the caller's ordering
-    for (int e = threadIdx.x; e < n * nc; e += blockDim.x) {
-      int i = e / nc, cc = e - i * nc;
-      B[perm[(size_t)b * n + i] * ldb + c0 + cc] = ynew[i * cpb + cc];
-    }
+    scatter(B, ldb, perm, (long long)b * n, ynew, cpb, n, c0, nc);
     return;
   }
   // vnew = U v + D ynew (written straight to Vout)

@@ -169,6 +169,17 @@ void ulv_solve_fused(cudaStream_t st, const Hbs& H, T* B, int ldb, int c, T* scr
   }
 }
 
+namespace {
+__global__ void lead_kernel(int us) {
+  for (int i = 0; i < us; ++i) __nanosleep(1000);
+}
+}  // namespace
+
+void enqueue_device_lead(cudaStream_t st, int us) {
+  lead_kernel<<<1, 32, 0, st>>>(us);
+  check_launch("lead_kernel");
+}
+
 template void ulv_solve_fused<double>(cudaStream_t, const Hbs&, double*, int, int, double*, size_t,
                                       LaunchTimes*);
 template void ulv_solve_fused<float>(cudaStream_t, const Hbs&, float*, int, int, float*, size_t,

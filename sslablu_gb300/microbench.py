@@ -4,6 +4,7 @@
     python -m sslablu_gb300.microbench f64_gemm [...]
 
     python -m sslablu_gb300.microbench compress [--m 4096 --reps 5]
+    python -m sslablu_gb300.microbench solve [--m 4096 --n 16 --reps 20]
 
 tc_gemm : slu_gemm_split3 (tcgen05 split-BF16x3, float32 accumulation)
 f64_gemm: slu_gemm_batched (float64 CUDA-core GEMM) on the same shape
@@ -11,6 +12,9 @@ The default shape is the sketch product of an N = 4096 dense block with the
 261 Gaussian samples of the rank-32 / leaf-64 HBS compression.  Prints one
 JSON line with the median time, the tensor FLOP rate (6 split products) and
 the effective rate (2 m n k).
+solve: the float64 ULV solve (slu_ulv_solve, mode N) of a synthetic exact
+HBS operator of size m (leaf 64, rank 32, ULV from the given factors) with n
+right-hand sides; prints the median time per solve.
 compress: HBSMAT.construct(32, compute_ULV=True) of a synthetic exact HBS
 operator of size m (leaf 64, rank 32, singular values 1 -> 1e-12), the
 sketches sampled through the resident operator; prints the median time and
@@ -28,7 +32,7 @@ from . import _lib
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("kernel", choices=["tc_gemm", "f64_gemm", "compress"])
+    ap.add_argument("kernel", choices=["tc_gemm", "f64_gemm", "compress", "solve"])
     ap.add_argument("--m", type=int, default=4096)
     ap.add_argument("--n", type=int, default=261)
     ap.add_argument("--k", type=int, default=4096)
@@ -37,6 +41,8 @@ def main():
     a = ap.parse_args()
     if a.kernel == "compress":
         return compress(a)
+    if a.kernel == "solve":
+        return solve(a)
     m, n, k = a.m, a.n, a.k
     rng = np.random.default_rng(0)
     A = torch.from_numpy(rng.standard_normal((m, k))).cuda()
@@ -73,6 +79,39 @@ def main():
     print(json.dumps({"kernel": a.kernel, "m": m, "n": n, "k": k, "median_ms": 1e3 * t,
                       "tensor_tflops": tensor / t / 1e12, "effective_tflops": eff / t / 1e12,
                       "relerr": err}))
+
+
+def solve(a):
+    from .matAssembly.HBS.HBSnew import HBSMAT
+    from .synthetic import decaying_sigma, random_hbs_factors
+    N, c = a.m, a.n
+    Lv = int(np.log2(N // 64)) + 1
+    np.random.seed(1)
+    U, D, V, Nbvec = random_hbs_factors(32, 64, Lv, quad=False, sigma=decaying_sigma(32),
+                                        shift=16.0)
+    H = HBSMAT().set_mats(U, D, V, list(Nbvec), fac=2)
+    H.compute_ULV()
+    B = torch.from_numpy(np.random.default_rng(2).standard_normal((N, c))).cuda()
+    W = B.clone()
+    L, h = _lib.lib(), _lib.handle()
+
+    def run():
+        _lib.check(L.slu_ulv_solve(h, H._op, _lib.ptr(W), c, c, 0))
+
+    for _ in range(a.warmup):
+        run()
+    torch.cuda.synchronize()
+    st = torch.cuda.current_stream()
+    ts = []
+    for _ in range(a.reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        run()
+        e1.record(st)
+        e1.synchronize()
+        ts.append(e0.elapsed_time(e1) * 1e-3)
+    print(json.dumps({"kernel": "solve", "N": N, "nrhs": c, "levels": Lv,
+                      "median_ms": 1e3 * statistics.median(ts)}))
 
 
 def compress(a):
