@@ -36,10 +36,32 @@ __device__ __forceinline__ DF split_d(double x) {
 
 constexpr int kBatch = 8;   // global loads in flight per thread in the copies
 
+// Row/column of e = threadIdx.x + u * blockDim.x in a row-major array of
+// `cols` columns, advanced without a division per element.
+struct FlatIdx {
+  int i, j, qs, rs, cols;
+  __device__ FlatIdx(int cols_) : cols(cols_) {
+    qs = blockDim.x / cols;
+    rs = blockDim.x - qs * cols;
+    i = threadIdx.x / cols;
+    j = threadIdx.x - i * cols;
+  }
+  __device__ void next() {
+    i += qs;
+    j += rs;
+    if (j >= cols) {
+      j -= cols;
+      ++i;
+    }
+  }
+};
+
 // Stage a rows x cols (hi, lo) block into shared memory with pitch ld.
 __device__ inline void stage2(float* Sh, float* Sl, int ld, const float* __restrict__ Ah,
                               const float* __restrict__ Al, int rows, int cols) {
   const int total = rows * cols, step = blockDim.x;
+  if (total == 0) return;
+  FlatIdx ix(cols);
   for (int e0 = threadIdx.x; e0 < total; e0 += kBatch * step) {
     float h[kBatch], l[kBatch];
 #pragma unroll
@@ -52,12 +74,11 @@ __device__ inline void stage2(float* Sh, float* Sl, int ld, const float* __restr
     }
 #pragma unroll
     for (int u = 0; u < kBatch; ++u) {
-      const int e = e0 + u * step;
-      if (e < total) {
-        const int i = e / cols, j = e - i * cols;
-        Sh[i * ld + j] = h[u];
-        Sl[i * ld + j] = l[u];
+      if (e0 + u * step < total) {
+        Sh[ix.i * ld + ix.j] = h[u];
+        Sl[ix.i * ld + ix.j] = l[u];
       }
+      ix.next();
     }
   }
 }
@@ -69,31 +90,32 @@ __device__ inline void gather2(float* xh, float* xl, int ldx, const double* X, l
                                const int64_t* __restrict__ perm, const DF* in, int c,
                                long long row0, int rows, int c0, int nc) {
   const int total = rows * nc, step = blockDim.x;
+  if (total == 0) return;
+  FlatIdx ix(nc);
   for (int e0 = threadIdx.x; e0 < total; e0 += kBatch * step) {
+    FlatIdx at = ix;
     long long r[kBatch];
 #pragma unroll
     for (int u = 0; u < kBatch; ++u) {
-      const int e = e0 + u * step;
-      const long long row = row0 + (e < total ? e / nc : 0);
-      r[u] = (e < total && X && perm) ? __ldg(perm + row) : row;
+      const long long row = row0 + at.i;
+      r[u] = (e0 + u * step < total && X && perm) ? __ldg(perm + row) : row;
+      at.next();
     }
     DF v[kBatch];
+    at = ix;
 #pragma unroll
     for (int u = 0; u < kBatch; ++u) {
-      const int e = e0 + u * step;
-      if (e < total) {
-        const int cc = e % nc;
-        v[u] = X ? split_d(X[r[u] * ldX + c0 + cc]) : in[r[u] * c + c0 + cc];
-      }
+      if (e0 + u * step < total)
+        v[u] = X ? split_d(X[r[u] * ldX + c0 + at.j]) : in[r[u] * c + c0 + at.j];
+      at.next();
     }
 #pragma unroll
     for (int u = 0; u < kBatch; ++u) {
-      const int e = e0 + u * step;
-      if (e < total) {
-        const int i = e / nc, cc = e - i * nc;
-        xh[i * ldx + cc] = v[u].h;
-        xl[i * ldx + cc] = v[u].l;
+      if (e0 + u * step < total) {
+        xh[ix.i * ldx + ix.j] = v[u].h;
+        xl[ix.i * ldx + ix.j] = v[u].l;
       }
+      ix.next();
     }
   }
 }

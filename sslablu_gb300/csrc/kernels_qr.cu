@@ -127,19 +127,24 @@ apply_q_kernel(bool transpose, int m, int k, const double* __restrict__ V, int l
 
 // ---------------------------------------------------------------- Jacobi SVD
 // One-sided (Hestenes) Jacobi on the columns of A (m x n), round-robin pair
-// ordering.  One thread per column pair: it forms the three inner products of
-// its pair, the rotation, and applies it, so the scalar work (square roots,
-// divisions) runs once per pair instead of once per lane; the float64 pipe
-// then does only the 7m multiply-adds of each pair.  Each inner product is
-// summed in JAC_ACC interleaved partial sums combined pairwise, which keeps
-// its rounding error well below the m*eps rotation threshold (a single
-// running sum reaches that threshold on noise-level columns, which then
-// never stop rotating).  Columns live in shared memory with an odd leading
-// dimension, so the 32 threads of a warp, each on its own column, read
-// different banks.  At convergence the columns are sigma_j u_j; the r largest
-// are normalised and written as U (m x r).
+// ordering.  Each column pair belongs to JAC_LANES consecutive lanes of a
+// warp; a lane owns rows part, part + JAC_LANES, ...  The lanes form the
+// three inner products of the pair over their rows (two partial sums each,
+// then a shuffle butterfly -- the pair's sums are combined the same way on
+// every lane), compute the rotation redundantly and rotate their own rows,
+// so no shared-memory traffic beyond the columns themselves and one block
+// barrier per round.  The rotation is orthogonal in float64 whatever its
+// angle, so the angle is computed in float32 from the float64 quotient
+// zeta = (beta - alpha) / (2 gamma) and the float64 (c, s) are renormalised
+// to c^2 + s^2 = 1 to float64 rounding; an angle good to ~1e-7 still cuts
+// gamma by that factor per rotation, and the sweep test (|gamma| <= m eps
+// sqrt(alpha beta) for every pair) is unchanged.  Small angles
+// (|zeta| > 1e7, where zeta^2 would leave float32 range) take t = 1/(2 zeta)
+// in float64 instead.  Columns live in shared
+// memory with an odd leading dimension.  At convergence the columns are
+// sigma_j u_j; the r largest are normalised and written as U (m x r).
 constexpr int JAC_MAX_SWEEPS = 40;
-constexpr int JAC_ACC = 8;
+constexpr int JAC_LANES = 4;
 
 __global__ void __launch_bounds__(1024)
 jacobi_kernel(int m, int n, const double* __restrict__ A, int lda, long long sA, int r,
@@ -163,60 +168,81 @@ jacobi_kernel(int m, int n, const double* __restrict__ A, int lda, long long sA,
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const double tol = 2.220446049250313e-16 * (double)m;
   const int npairs = np / 2;
+  const int part = threadIdx.x & (JAC_LANES - 1);
+  // every lane of a warp runs the pair loop the same number of times, so the
+  // shuffles below always see the whole warp
+  const int slots = (npairs * JAC_LANES + blockDim.x - 1) / blockDim.x * blockDim.x;
   int sweep = 0;
   for (; sweep < JAC_MAX_SWEEPS; ++sweep) {
     if (threadIdx.x == 0) s_rot = 0;
     __syncthreads();
     for (int rnd = 0; rnd < np - 1; ++rnd) {
-      for (int pi = threadIdx.x; pi < npairs; pi += blockDim.x) {
+      for (int t = threadIdx.x; t < slots; t += blockDim.x) {
+        const int pi = t / JAC_LANES;
+        const bool on = pi < npairs;
         // circle method: slot 0 fixed, others rotate
         const int s1 = pi, s2 = np - 1 - pi;
         const int p = (s1 == 0) ? 0 : 1 + (s1 - 1 + rnd) % (np - 1);
         const int q = 1 + (s2 - 1 + rnd) % (np - 1);
-        double* ap = a + (long long)p * lda_s;
-        double* aq = a + (long long)q * lda_s;
-        double pa[JAC_ACC], pb[JAC_ACC], pg[JAC_ACC];
-#pragma unroll
-        for (int u = 0; u < JAC_ACC; ++u) pa[u] = pb[u] = pg[u] = 0.0;
-        int i = 0;
-        for (; i + JAC_ACC <= m; i += JAC_ACC) {
-#pragma unroll
-          for (int u = 0; u < JAC_ACC; ++u) {
-            const double x = ap[i + u], y = aq[i + u];
-            pa[u] = fma(x, x, pa[u]);
-            pb[u] = fma(y, y, pb[u]);
-            pg[u] = fma(x, y, pg[u]);
+        double* ap = a + (long long)(on ? p : 0) * lda_s;
+        double* aq = a + (long long)(on ? q : 0) * lda_s;
+        double a0 = 0.0, b0 = 0.0, g0 = 0.0, a1 = 0.0, b1 = 0.0, g1 = 0.0;
+        if (on) {
+          int i = part;
+          for (; i + JAC_LANES < m; i += 2 * JAC_LANES) {
+            const double x0 = ap[i], y0 = aq[i];
+            const double x1 = ap[i + JAC_LANES], y1 = aq[i + JAC_LANES];
+            a0 = fma(x0, x0, a0);
+            b0 = fma(y0, y0, b0);
+            g0 = fma(x0, y0, g0);
+            a1 = fma(x1, x1, a1);
+            b1 = fma(y1, y1, b1);
+            g1 = fma(x1, y1, g1);
+          }
+          if (i < m) {
+            const double x0 = ap[i], y0 = aq[i];
+            a0 = fma(x0, x0, a0);
+            b0 = fma(y0, y0, b0);
+            g0 = fma(x0, y0, g0);
           }
         }
+        double al = a0 + a1, be = b0 + b1, ga = g0 + g1;
 #pragma unroll
-        for (int u = 0; u < JAC_ACC; ++u) {
-          if (i + u < m) {
-            const double x = ap[i + u], y = aq[i + u];
-            pa[u] = fma(x, x, pa[u]);
-            pb[u] = fma(y, y, pb[u]);
-            pg[u] = fma(x, y, pg[u]);
-          }
+        for (int o = 1; o < JAC_LANES; o <<= 1) {
+          al += __shfl_xor_sync(0xffffffffu, al, o);
+          be += __shfl_xor_sync(0xffffffffu, be, o);
+          ga += __shfl_xor_sync(0xffffffffu, ga, o);
         }
-#pragma unroll
-        for (int w = JAC_ACC / 2; w > 0; w >>= 1)
-#pragma unroll
-          for (int u = 0; u < w; ++u) {
-            pa[u] += pa[u + w];
-            pb[u] += pb[u + w];
-            pg[u] += pg[u + w];
-          }
-        const double al = pa[0], be = pb[0], ga = pg[0];
-        if (ga != 0.0 && fabs(ga) > tol * sqrt(al * be)) {
+        if (on && ga != 0.0 && fabs(ga) > tol * sqrt(al * be)) {
           const double zeta = (be - al) / (2.0 * ga);
-          const double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-          const double c = 1.0 / sqrt(1.0 + t * t);
-          const double s = c * t;
-          for (int j = 0; j < m; ++j) {
-            const double x = ap[j], y = aq[j];
-            ap[j] = c * x - s * y;
-            aq[j] = s * x + c * y;
+          double c, s;
+          float tf;
+          if (fabs(zeta) > 1e7) {
+            // small angle: t = 1 / (2 zeta) to relative 1e-14, c^2 + s^2 = 1 + O(t^4)
+            const double t = 0.5 / zeta;
+            c = fma(-0.5 * t, t, 1.0);
+            s = t * c;
+            tf = (float)t;
+          } else {
+            const float zf = (float)zeta;
+            tf = copysignf(1.0f, zf) / (fabsf(zf) + sqrtf(fmaf(zf, zf, 1.0f)));
+            const float cf = rsqrtf(fmaf(tf, tf, 1.0f));
+            c = (double)cf;
+            s = (double)cf * (double)tf;
+            // renormalise: (c, s) /= sqrt(1 + d), d = c^2 + s^2 - 1 ~ 1e-7
+            const double d = fma(c, c, fma(s, s, -1.0));
+            const double f = fma(d, fma(0.375, d, -0.5), 1.0);
+            c *= f;
+            s *= f;
           }
-          s_rot = 1;
+          if (s != 0.0) {
+            for (int i = part; i < m; i += JAC_LANES) {
+              const double x = ap[i], y = aq[i];
+              ap[i] = c * x - s * y;
+              aq[i] = s * x + c * y;
+            }
+            s_rot = 1;
+          }
         }
       }
       __syncthreads();
@@ -324,7 +350,7 @@ void jacobi_left_sv(cudaStream_t st, int m, int n, const double* A, int lda, lon
   if (sm > 48 * 1024)
     SLU_CHECK_CUDA(cudaFuncSetAttribute(jacobi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)sm));
-  int threads = 32 * std::min(32, std::max(2, (np / 2 + 31) / 32));
+  int threads = 32 * std::min(32, std::max(2, (np / 2 * JAC_LANES + 31) / 32));
   jacobi_kernel<<<batch, threads, sm, st>>>(m, n, A, lda, sA, r, U, ldu, sU, sv, sS, info,
                                             lower ? 1 : 0);
   check_launch("jacobi_kernel");

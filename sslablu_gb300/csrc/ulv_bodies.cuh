@@ -23,10 +23,33 @@ namespace ulvk {
 // e / (kBatch * blockDim) memory round trips instead of e / blockDim.
 constexpr int kBatch = 8;
 
+// Row/column of the flat index e = threadIdx.x + u * blockDim.x, u = 0, 1,
+// ..., in a row-major array of `cols` columns, advanced without a division
+// per element (one division per thread at the start).
+struct FlatIdx {
+  int i, j, qs, rs, cols;
+  __device__ FlatIdx(int cols_) : cols(cols_) {
+    qs = blockDim.x / cols;
+    rs = blockDim.x - qs * cols;
+    i = threadIdx.x / cols;
+    j = threadIdx.x - i * cols;
+  }
+  __device__ void next() {
+    i += qs;
+    j += rs;
+    if (j >= cols) {
+      j -= cols;
+      ++i;
+    }
+  }
+};
+
 // S[i * ld + j] = A[i * cols + j], a rows x cols block.
 template <typename T>
 __device__ inline void stage(T* S, int ld, const T* __restrict__ A, int rows, int cols) {
   const int total = rows * cols, step = blockDim.x;
+  if (total == 0) return;
+  FlatIdx ix(cols);
   for (int e0 = threadIdx.x; e0 < total; e0 += kBatch * step) {
     T v[kBatch];
 #pragma unroll
@@ -36,11 +59,8 @@ __device__ inline void stage(T* S, int ld, const T* __restrict__ A, int rows, in
     }
 #pragma unroll
     for (int u = 0; u < kBatch; ++u) {
-      const int e = e0 + u * step;
-      if (e < total) {
-        const int i = e / cols;
-        S[i * ld + (e - i * cols)] = v[u];
-      }
+      if (e0 + u * step < total) S[ix.i * ld + ix.j] = v[u];
+      ix.next();
     }
   }
 }
@@ -52,30 +72,28 @@ __device__ inline void gather(T* x, int ldx, const T* src, long long lds,
                               const int64_t* __restrict__ perm, long long row0, int rows,
                               int c0, int nc) {
   const int total = rows * nc, step = blockDim.x;
+  if (total == 0) return;
+  FlatIdx ix(nc);
   for (int e0 = threadIdx.x; e0 < total; e0 += kBatch * step) {
+    FlatIdx at = ix;
     long long r[kBatch];
 #pragma unroll
     for (int u = 0; u < kBatch; ++u) {
-      const int e = e0 + u * step;
-      r[u] = 0;
-      if (e < total) {
-        const long long row = row0 + e / nc;
-        r[u] = perm ? __ldg(perm + row) : row;
-      }
+      const long long row = row0 + at.i;
+      r[u] = (e0 + u * step < total && perm) ? __ldg(perm + row) : row;
+      at.next();
     }
     T v[kBatch];
+    at = ix;
 #pragma unroll
     for (int u = 0; u < kBatch; ++u) {
-      const int e = e0 + u * step;
-      if (e < total) v[u] = src[r[u] * lds + c0 + (e % nc)];
+      if (e0 + u * step < total) v[u] = src[r[u] * lds + c0 + at.j];
+      at.next();
     }
 #pragma unroll
     for (int u = 0; u < kBatch; ++u) {
-      const int e = e0 + u * step;
-      if (e < total) {
-        const int i = e / nc;
-        x[i * ldx + (e - i * nc)] = v[u];
-      }
+      if (e0 + u * step < total) x[ix.i * ldx + ix.j] = v[u];
+      ix.next();
     }
   }
 }
@@ -86,36 +104,54 @@ template <typename T>
 __device__ inline void scatter(T* B, long long ldb, const int64_t* __restrict__ perm,
                                long long row0, const T* y, int ldy, int rows, int c0, int nc) {
   const int total = rows * nc, step = blockDim.x;
+  if (total == 0) return;
+  FlatIdx ix(nc);
   for (int e0 = threadIdx.x; e0 < total; e0 += kBatch * step) {
+    FlatIdx at = ix;
     long long r[kBatch];
 #pragma unroll
     for (int u = 0; u < kBatch; ++u) {
-      const int e = e0 + u * step;
-      r[u] = (e < total) ? __ldg(perm + row0 + e / nc) : 0;
+      r[u] = (e0 + u * step < total) ? __ldg(perm + row0 + at.i) : 0;
+      at.next();
     }
 #pragma unroll
     for (int u = 0; u < kBatch; ++u) {
-      const int e = e0 + u * step;
-      if (e < total) {
-        const int i = e / nc, cc = e - i * nc;
-        B[r[u] * ldb + c0 + cc] = y[i * ldy + cc];
-      }
+      if (e0 + u * step < total) B[r[u] * ldb + c0 + ix.j] = y[ix.i * ldy + ix.j];
+      ix.next();
     }
   }
 }
+
+// Dot products of the matrix-vector steps are split over ks consecutive lanes
+// (each sums every ks-th term, then a butterfly of shuffles adds the ks
+// partial sums): the dependent multiply-add chain is ks times shorter and
+// more lanes work when there are few columns.  ks depends only on the
+// length of the dot product, so the summation order -- and the result --
+// does not depend on how the right-hand sides are chunked over CTAs.
+__device__ __forceinline__ int dot_split(int len) { return len >= 32 ? 4 : (len >= 8 ? 2 : 1); }
 
 // out[i][c] (+)= sign * sum_j S[i][j0 + j] * x[j][c]   i < rows, j < cols
 template <typename T>
 __device__ inline void mv(const T* S, int ld, int j0, int rows, int cols, const T* x, int ldx,
                           T* out, int ldo, int nc, T sign, bool accumulate) {
-  for (int e = threadIdx.x; e < rows * nc; e += blockDim.x) {
-    int i = e / nc, cc = e - i * nc;
-    const T* s = S + i * ld + j0;
+  const int ks = dot_split(cols), lks = ks == 4 ? 2 : (ks == 2 ? 1 : 0);
+  const int work = rows * nc * ks, lane = threadIdx.x & 31;
+  for (int base = threadIdx.x - lane; base < work; base += blockDim.x) {
+    const int t = base + lane;
+    const bool on = t < work;
+    const int e = t >> lks, part = t & (ks - 1);
+    const int i = on ? e / nc : 0, cc = on ? e - i * nc : 0;
     T acc = T(0);
+    if (on) {
+      const T* s = S + i * ld + j0;
 #pragma unroll 4
-    for (int j = 0; j < cols; ++j) acc = fma(s[j], x[j * ldx + cc], acc);
-    T* o = out + i * ldo + cc;
-    *o = accumulate ? fma(sign, acc, *o) : sign * acc;
+      for (int j = part; j < cols; j += ks) acc = fma(s[j], x[j * ldx + cc], acc);
+    }
+    for (int o = ks >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (on && part == 0) {
+      T* op = out + i * ldo + cc;
+      *op = accumulate ? fma(sign, acc, *op) : sign * acc;
+    }
   }
 }
 
@@ -123,12 +159,20 @@ __device__ inline void mv(const T* S, int ld, int j0, int rows, int cols, const 
 template <typename T>
 __device__ inline void mvt(const T* S, int ld, int rows_out, int cols_in, const T* x, int ldx,
                            T* out, int ldo, int nc) {
-  for (int e = threadIdx.x; e < rows_out * nc; e += blockDim.x) {
-    int i = e / nc, cc = e - i * nc;
+  const int ks = dot_split(cols_in), lks = ks == 4 ? 2 : (ks == 2 ? 1 : 0);
+  const int work = rows_out * nc * ks, lane = threadIdx.x & 31;
+  for (int base = threadIdx.x - lane; base < work; base += blockDim.x) {
+    const int t = base + lane;
+    const bool on = t < work;
+    const int e = t >> lks, part = t & (ks - 1);
+    const int i = on ? e / nc : 0, cc = on ? e - i * nc : 0;
     T acc = T(0);
+    if (on) {
 #pragma unroll 4
-    for (int j = 0; j < cols_in; ++j) acc = fma(S[j * ld + i], x[j * ldx + cc], acc);
-    out[i * ldo + cc] = acc;
+      for (int j = part; j < cols_in; j += ks) acc = fma(S[j * ld + i], x[j * ldx + cc], acc);
+    }
+    for (int o = ks >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (on && part == 0) out[i * ldo + cc] = acc;
   }
 }
 
