@@ -97,10 +97,10 @@ group_solve_kernel(const SolveSeg<T>* __restrict__ segs, int nseg) {
     ulvk::ulv_fwd_body<T>(sm_raw, b, c0, nc, s.n, s.nu, s.k, s.Q, s.src, s.lds, s.perm, s.ru,
                           s.dst, s.c, s.cpb);
   else if (s.kind == 1)
-    ulvk::ulv_root_body<T>(sm_raw, c0, nc, s.n, s.Q, s.R, s.D, s.src, s.lds, s.perm, s.Yout,
+    ulvk::ulv_root_body<T, false>(sm_raw, c0, nc, s.n, s.Q, s.R, s.D, s.src, s.lds, s.perm, s.Yout,
                            s.Vout, s.B, s.ldb, s.c, s.cpb);
   else
-    ulvk::ulv_bwd_body<T>(sm_raw, b, c0, nc, s.n, s.nu, s.k, s.ru, s.Uu, s.R, s.W, s.U, s.D,
+    ulvk::ulv_bwd_body<T, false>(sm_raw, b, c0, nc, s.n, s.nu, s.k, s.ru, s.Uu, s.R, s.W, s.U, s.D,
                           s.Vin, s.Yin, s.Yout, s.Vout, s.perm, s.B, s.ldb, s.c, s.cpb);
 }
 
@@ -244,7 +244,7 @@ void build_solve(const std::vector<const Hbs*>& H, const std::vector<int>& c,
       s.ru = buf[i].ru + H[i]->NN[t] * c[i];
       s.dst = buf[i].P[t & 1];
       st.segs.push_back(s);
-      st.g.push_back({l.Nb, c[i], e * l.n * (l.n + 1), e * 2 * l.n});
+      st.g.push_back({l.Nb, c[i], e * ulvk::ulv_fwd_smem(l.n, 0), e * 2 * l.n});
     }
     st.end(mstart, mmin, target);
   }
@@ -264,7 +264,7 @@ void build_solve(const std::vector<const Hbs*>& H, const std::vector<int>& c,
     s.B = B[i];
     s.ldb = ldb[i];
     st.segs.push_back(s);
-    st.g.push_back({1, c[i], e * r.n * (r.n + 1), e * 2 * r.n});
+    st.g.push_back({1, c[i], e * ulvk::ulv_root_smem(r.n, 0, false), e * 2 * r.n});
   }
   st.end(mstart, mmin, target);
   for (int t = maxL - 2; t >= 0; --t) {
@@ -287,7 +287,8 @@ void build_solve(const std::vector<const Hbs*>& H, const std::vector<int>& c,
       s.B = B[i];
       s.ldb = ldb[i];
       st.segs.push_back(s);
-      st.g.push_back({l.Nb, c[i], e * l.n * (l.n + 1), e * (2 * l.k + l.nu + l.n)});
+      st.g.push_back({l.Nb, c[i], e * ulvk::ulv_bwd_smem(l.n, l.nu, l.k, 0, false, t == 0),
+                      e * (2 * l.k + l.nu + 2 * l.n)});
     }
     st.end(mstart, mmin, target);
   }

@@ -87,7 +87,9 @@ __device__ inline void gather(T* x, int ldx, const T* src, long long lds,
     at = ix;
 #pragma unroll
     for (int u = 0; u < kBatch; ++u) {
-      if (e0 + u * step < total) v[u] = src[r[u] * lds + c0 + at.j];
+      // L2-only loads: in a persistent kernel the same buffer is rewritten
+      // by other SMs between steps, so no stale L1 line may be used
+      if (e0 + u * step < total) v[u] = __ldcg(src + r[u] * lds + c0 + at.j);
       at.next();
     }
 #pragma unroll
@@ -119,6 +121,36 @@ __device__ inline void scatter(T* B, long long ldb, const int64_t* __restrict__ 
       if (e0 + u * step < total) B[r[u] * ldb + c0 + ix.j] = y[ix.i * ldy + ix.j];
       ix.next();
     }
+  }
+}
+
+// Asynchronous global -> shared copies (cp.async, Ampere and later): every
+// element of every block matrix a CTA needs can be in flight at once, and one
+// wait covers them all.  The wait is the hardware's completion of the
+// thread's own copies.
+template <typename T>
+__device__ __forceinline__ void cp_async_elem(T* dst, const T* src) {
+  const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
+  if (sizeof(T) == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
+// S[i * ld + j] <- A[i * cols + j] as asynchronous copies (complete after
+// cp_async_wait_all and a barrier).
+template <typename T>
+__device__ inline void stage_async(T* S, int ld, const T* A, int rows, int cols) {
+  const int total = rows * cols;
+  if (total == 0) return;
+  FlatIdx ix(cols);
+  for (int e = threadIdx.x; e < total; e += blockDim.x) {
+    cp_async_elem(S + ix.i * ld + ix.j, A + e);
+    ix.next();
   }
 }
 
@@ -213,8 +245,9 @@ __device__ __forceinline__ void ulv_fwd_body(unsigned char* sm_raw, int b, int c
   T* S = reinterpret_cast<T*>(sm_raw);       // n x (n+1)
   T* x = S + n * (n + 1);                     // n x cpb
   T* z = x + n * cpb;                         // n x cpb
+  stage_async(S, n + 1, Q + (size_t)b * n * n, n, n);
   gather(x, cpb, src, lds, perm, (long long)b * n, n, c0, nc);
-  stage(S, n + 1, Q + (size_t)b * n * n, n, n);
+  cp_async_wait_all();
   __syncthreads();
   mvt(S, n + 1, n, n, x, cpb, z, cpb, nc);
   __syncthreads();
@@ -229,30 +262,44 @@ __device__ __forceinline__ void ulv_fwd_body(unsigned char* sm_raw, int b, int c
 // ---------------------------------------------------------------- root
 // y = R^{-1} Q^T x, v = D y.  When the tree has one level the root is also
 // the leaf: input gathered through perm, solution scattered through perm.
-template <typename T>
+// Shared memory: with PF, Q, R and D (n x (n+1) each) copied in one
+// asynchronous batch; without PF one n x (n+1) region restaged per matrix.
+// Then x, y (n x cpb each).
+template <typename T, bool PF>
 __device__ __forceinline__ void ulv_root_body(unsigned char* sm_raw, int c0, int nc, int n,
                                               const T* __restrict__ Q, const T* __restrict__ R,
                                               const T* __restrict__ D, const T* __restrict__ src,
                                               int lds, const int64_t* __restrict__ perm,
                                               T* __restrict__ Yout, T* __restrict__ Vout,
                                               T* __restrict__ B, int ldb, int c, int cpb) {
-  T* S = reinterpret_cast<T*>(sm_raw);
-  T* x = S + n * (n + 1);
+  T* SQ = reinterpret_cast<T*>(sm_raw);
+  T* SR = PF ? SQ + n * (n + 1) : SQ;
+  T* SD = PF ? SR + n * (n + 1) : SQ;
+  T* x = (PF ? SD : SQ) + n * (n + 1);
   T* y = x + n * cpb;
+  stage_async(SQ, n + 1, Q, n, n);
+  if (PF) {
+    stage_async(SR, n + 1, R, n, n);
+    if (!perm) stage_async(SD, n + 1, D, n, n);
+  }
   gather(x, cpb, src, lds, perm, 0, n, c0, nc);
-  stage(S, n + 1, Q, n, n);
+  cp_async_wait_all();
   __syncthreads();
-  mvt(S, n + 1, n, n, x, cpb, y, cpb, nc);
-  __syncthreads();
-  stage(S, n + 1, R, n, n);
-  trsv_upper(S, n + 1, n, y, cpb, nc);
+  mvt(SQ, n + 1, n, n, x, cpb, y, cpb, nc);
+  if (!PF) {
+    __syncthreads();
+    stage(SR, n + 1, R, n, n);
+  }
+  trsv_upper(SR, n + 1, n, y, cpb, nc);   // begins and ends with a barrier
   if (perm) {  // single-level tree: y is the solution
     scatter(B, ldb, perm, 0, y, cpb, n, c0, nc);
     return;
   }
-  stage(S, n + 1, D, n, n);
-  __syncthreads();
-  mv(S, n + 1, 0, n, n, y, cpb, x, cpb, nc, T(1), false);   // x <- D y
+  if (!PF) {
+    stage(SD, n + 1, D, n, n);
+    __syncthreads();
+  }
+  mv(SD, n + 1, 0, n, n, y, cpb, x, cpb, nc, T(1), false);   // x <- D y
   __syncthreads();
   for (int e = threadIdx.x; e < n * nc; e += blockDim.x) {
     int i = e / nc, cc = e - i * nc;
@@ -262,7 +309,12 @@ __device__ __forceinline__ void ulv_root_body(unsigned char* sm_raw, int c0, int
 }
 
 // ---------------------------------------------------------------- backward
-template <typename T>
+// Shared memory (elements of T): with PF every block matrix has its own
+// region -- Uu nu x (k+1), R nu x (n+1), W n x (n+1) and, above the leaves,
+// U n x (k+1), D n x (n+1) -- all copied in one asynchronous batch; without
+// PF one n x (n+1) region is restaged per matrix.  Then vb, yn (k x cpb),
+// yu (nu x cpb), ynew and vt (n x cpb).
+template <typename T, bool PF>
 __device__ __forceinline__ void ulv_bwd_body(unsigned char* sm_raw, int b, int c0, int nc, int n,
                                              int nu, int k, const T* __restrict__ ru,
                                              const T* __restrict__ Uu, const T* __restrict__ R,
@@ -271,59 +323,96 @@ __device__ __forceinline__ void ulv_bwd_body(unsigned char* sm_raw, int b, int c
                                              const T* __restrict__ Yin, T* __restrict__ Yout,
                                              T* __restrict__ Vout, const int64_t* __restrict__ perm,
                                              T* __restrict__ B, int ldb, int c, int cpb) {
-  T* S = reinterpret_cast<T*>(sm_raw);        // n x (n+1) staging
-  T* vb = S + n * (n + 1);                     // k  x cpb
-  T* yn = vb + k * cpb;                        // k  x cpb
-  T* yu = yn + k * cpb;                        // nu x cpb
-  T* ynew = yu + nu * cpb;                     // n  x cpb
+  const bool leaf = perm != nullptr;
+  T* base = reinterpret_cast<T*>(sm_raw);
+  T *SUu = base, *SR = base, *SW = base, *SU = base, *SD = base, *vec;
+  if (PF) {
+    SR = SUu + nu * (k + 1);
+    SW = SR + nu * (n + 1);
+    SU = SW + n * (n + 1);
+    SD = SU + (leaf ? 0 : n * (k + 1));
+    vec = SD + (leaf ? 0 : n * (n + 1));
+    if (nu > 0) {
+      stage_async(SUu, k + 1, Uu + (size_t)b * nu * k, nu, k);
+      stage_async(SR, n + 1, R + (size_t)b * nu * n, nu, n);
+    }
+    stage_async(SW, n + 1, W + (size_t)b * n * n, n, n);
+    if (!leaf) {
+      stage_async(SU, k + 1, U + (size_t)b * n * k, n, k);
+      stage_async(SD, n + 1, D + (size_t)b * n * n, n, n);
+    }
+  } else {
+    vec = base + n * (n + 1);
+  }
+  T* vb = vec;                 // k  x cpb
+  T* yn = vb + k * cpb;        // k  x cpb
+  T* yu = yn + k * cpb;        // nu x cpb
+  T* ynew = yu + nu * cpb;     // n  x cpb
+  T* vt = ynew + n * cpb;      // n  x cpb
   gather(vb, cpb, Vin, c, nullptr, (long long)b * k, k, c0, nc);
   gather(yn, cpb, Yin, c, nullptr, (long long)b * k, k, c0, nc);
   gather(yu, cpb, ru, c, nullptr, (long long)b * nu, nu, c0, nc);
+  if (PF) cp_async_wait_all();
   if (nu > 0) {
     // yu = ru - Uu v - R12 y_next ; then R11^{-1}
-    stage(S, k + 1, Uu + (size_t)b * nu * k, nu, k);
+    if (!PF) stage(SUu, k + 1, Uu + (size_t)b * nu * k, nu, k);
     __syncthreads();
-    mv(S, k + 1, 0, nu, k, vb, cpb, yu, cpb, nc, T(-1), true);
+    mv(SUu, k + 1, 0, nu, k, vb, cpb, yu, cpb, nc, T(-1), true);
     __syncthreads();
-    stage(S, n + 1, R + (size_t)b * nu * n, nu, n);
-    __syncthreads();
-    mv(S, n + 1, nu, nu, k, yn, cpb, yu, cpb, nc, T(-1), true);
-    trsv_upper(S, n + 1, nu, yu, cpb, nc);
+    if (!PF) {
+      stage(SR, n + 1, R + (size_t)b * nu * n, nu, n);
+      __syncthreads();
+    }
+    mv(SR, n + 1, nu, nu, k, yn, cpb, yu, cpb, nc, T(-1), true);
+    trsv_upper(SR, n + 1, nu, yu, cpb, nc);   // begins and ends with a barrier
   }
   // ynew = W [yu; y_next]
-  stage(S, n + 1, W + (size_t)b * n * n, n, n);
+  if (!PF) stage(SW, n + 1, W + (size_t)b * n * n, n, n);
   __syncthreads();
-  mv(S, n + 1, 0, n, nu, yu, cpb, ynew, cpb, nc, T(1), false);
-  mv(S, n + 1, nu, n, k, yn, cpb, ynew, cpb, nc, T(1), true);
+  mv(SW, n + 1, 0, n, nu, yu, cpb, ynew, cpb, nc, T(1), false);
+  // the two products split their dot products differently (lengths nu and
+  // k), so an output element is finished by a different lane: barrier
   __syncthreads();
-  if (perm) {  // leaf level: scatter the solution to the caller's ordering
+  mv(SW, n + 1, nu, n, k, yn, cpb, ynew, cpb, nc, T(1), true);
+  __syncthreads();
+  if (leaf) {  // leaf level: scatter the solution to the caller's ordering
     scatter(B, ldb, perm, (long long)b * n, ynew, cpb, n, c0, nc);
     return;
   }
-  // vnew = U v + D ynew (written straight to Vout)
-  stage(S, k + 1, U + (size_t)b * n * k, n, k);
-  __syncthreads();
-  for (int e = threadIdx.x; e < n * nc; e += blockDim.x) {
-    int i = e / nc, cc = e - i * nc;
-    const T* s = S + i * (k + 1);
-    T acc = T(0);
-    for (int j = 0; j < k; ++j) acc = fma(s[j], vb[j * cpb + cc], acc);
-    Vout[((size_t)b * n + i) * c + c0 + cc] = acc;
-    Yout[((size_t)b * n + i) * c + c0 + cc] = ynew[i * cpb + cc];
+  // vnew = U v + D ynew
+  if (!PF) {
+    stage(SU, k + 1, U + (size_t)b * n * k, n, k);
+    __syncthreads();
   }
+  mv(SU, k + 1, 0, n, k, vb, cpb, vt, cpb, nc, T(1), false);
   __syncthreads();
-  stage(S, n + 1, D + (size_t)b * n * n, n, n);
+  if (!PF) {
+    stage(SD, n + 1, D + (size_t)b * n * n, n, n);
+    __syncthreads();
+  }
+  mv(SD, n + 1, 0, n, n, ynew, cpb, vt, cpb, nc, T(1), true);
   __syncthreads();
   for (int e = threadIdx.x; e < n * nc; e += blockDim.x) {
-    int i = e / nc, cc = e - i * nc;
-    const T* s = S + i * (n + 1);
-    T acc = T(0);
-#pragma unroll 4
-    for (int j = 0; j < n; ++j) acc = fma(s[j], ynew[j * cpb + cc], acc);
-    Vout[((size_t)b * n + i) * c + c0 + cc] += acc;
+    const int i = e / nc, cc = e - i * nc;
+    Yout[((size_t)b * n + i) * c + c0 + cc] = ynew[i * cpb + cc];
+    Vout[((size_t)b * n + i) * c + c0 + cc] = vt[i * cpb + cc];
   }
 }
 
+// Shared-memory elements of the three bodies (see the layouts above).
+__host__ __device__ inline size_t ulv_fwd_smem(int n, int cpb) {
+  return (size_t)n * (n + 1) + 2 * (size_t)n * cpb;
+}
+__host__ __device__ inline size_t ulv_root_smem(int n, int cpb, bool pf) {
+  return (pf ? 3 : 1) * (size_t)n * (n + 1) + 2 * (size_t)n * cpb;
+}
+__host__ __device__ inline size_t ulv_bwd_smem(int n, int nu, int k, int cpb, bool pf, bool leaf) {
+  const size_t vec = (2 * (size_t)k + nu + 2 * (size_t)n) * cpb;
+  if (!pf) return (size_t)n * (n + 1) + vec;
+  size_t m = (size_t)nu * (k + 1) + (size_t)nu * (n + 1) + (size_t)n * (n + 1);
+  if (!leaf) m += (size_t)n * (k + 1) + (size_t)n * (n + 1);
+  return m + vec;
+}
 
 }  // namespace ulvk
 }  // namespace slu

@@ -30,6 +30,7 @@ namespace slu {
 namespace {
 
 constexpr int kThreads = 256;
+constexpr size_t kSmemPrefetch = 200 * 1024;
 
 using namespace ulvk;
 
@@ -45,7 +46,7 @@ ulv_fwd_kernel(int n, int nu, int k, const T* __restrict__ Q, const T* __restric
   ulv_fwd_body<T>(sm_raw, b, c0, nc, n, nu, k, Q, src, lds, perm, ru, dst, c, cpb);
 }
 
-template <typename T>
+template <typename T, bool PF>
 __global__ void __launch_bounds__(kThreads)
 ulv_root_kernel(int n, const T* __restrict__ Q, const T* __restrict__ R, const T* __restrict__ D,
                 const T* __restrict__ src, int lds, const int64_t* __restrict__ perm,
@@ -54,10 +55,10 @@ ulv_root_kernel(int n, const T* __restrict__ Q, const T* __restrict__ R, const T
   extern __shared__ unsigned char sm_raw[];
   const int c0 = blockIdx.y * cpb, nc = min(cpb, c - c0);
   if (nc <= 0) return;
-  ulv_root_body<T>(sm_raw, c0, nc, n, Q, R, D, src, lds, perm, Yout, Vout, B, ldb, c, cpb);
+  ulv_root_body<T, PF>(sm_raw, c0, nc, n, Q, R, D, src, lds, perm, Yout, Vout, B, ldb, c, cpb);
 }
 
-template <typename T>
+template <typename T, bool PF>
 __global__ void __launch_bounds__(kThreads)
 ulv_bwd_kernel(int n, int nu, int k, const T* __restrict__ ru, const T* __restrict__ Uu,
                const T* __restrict__ R, const T* __restrict__ W, const T* __restrict__ U,
@@ -67,21 +68,31 @@ ulv_bwd_kernel(int n, int nu, int k, const T* __restrict__ ru, const T* __restri
   extern __shared__ unsigned char sm_raw[];
   const int b = blockIdx.x, c0 = blockIdx.y * cpb, nc = min(cpb, c - c0);
   if (nc <= 0) return;
-  ulv_bwd_body<T>(sm_raw, b, c0, nc, n, nu, k, ru, Uu, R, W, U, D, Vin, Yin, Yout, Vout, perm, B,
-                  ldb, c, cpb);
+  ulv_bwd_body<T, PF>(sm_raw, b, c0, nc, n, nu, k, ru, Uu, R, W, U, D, Vin, Yin, Yout, Vout, perm,
+                      B, ldb, c, cpb);
 }
 
+// Column chunk per CTA.  float64: the widest chunk that still spreads the
+// level over ~2 CTAs per SM (the FP64 pipe bounds the large levels); float32
+// (latency bound): chunks of at most 16 columns.
 template <typename T>
 int chunk_for(int Nb, int c) {
   if (sizeof(T) == 8) {
-    // spread the float64 work over ~2 CTAs per SM
-    int target = 2 * num_sms();
+    const int target = 2 * num_sms();
     int cpb = c;
     while (cpb > 1 && (long long)Nb * ((c + cpb - 1) / cpb) < target) cpb = (cpb + 1) / 2;
     return cpb;
   }
   int cpb = c < 16 ? c : 16;
   while (cpb > 4 && (long long)Nb * ((c + cpb - 1) / cpb) < num_sms()) cpb /= 2;
+  return cpb;
+}
+
+// Narrows a chunk until its CTA's shared memory (elements of T per column
+// `per_col`, fixed part `fixed`) fits in `limit` bytes.
+template <typename T>
+int fit_chunk(int cpb, size_t fixed, size_t per_col, size_t limit) {
+  while (cpb > 1 && sizeof(T) * (fixed + per_col * cpb) > limit) cpb = (cpb + 1) / 2;
   return cpb;
 }
 
@@ -111,8 +122,9 @@ void ulv_solve_fused(cudaStream_t st, const Hbs& H, T* B, int ldb, int c, T* scr
   const int64_t* gperm = perm;
   for (int t = 0; t + 1 < L; ++t) {
     const Level& l = H.lv[t];
-    const int cpb = chunk_for<T>(l.Nb, c);
-    size_t sm = sizeof(T) * ((size_t)l.n * (l.n + 1) + 2 * (size_t)l.n * cpb);
+    const int cpb = fit_chunk<T>(chunk_for<T>(l.Nb, c), ulv_fwd_smem(l.n, 0), 2 * (size_t)l.n,
+                                 kSmemPrefetch);
+    size_t sm = sizeof(T) * ulv_fwd_smem(l.n, cpb);
     auto kern = ulv_fwd_kernel<T>;
     set_smem(kern, sm);
     T* dst = P[t & 1];
@@ -131,10 +143,14 @@ void ulv_solve_fused(cudaStream_t st, const Hbs& H, T* B, int ldb, int c, T* scr
   }
   // root
   const Level& r = H.lv[L - 1];
-  const int cpr = chunk_for<T>(1, c);
+  const int cpr = fit_chunk<T>(chunk_for<T>(1, c), ulv_root_smem(r.n, 0, false),
+                               2 * (size_t)r.n, kSmemPrefetch);
   {
-    size_t sm = sizeof(T) * ((size_t)r.n * (r.n + 1) + 2 * (size_t)r.n * cpr);
-    auto kern = ulv_root_kernel<T>;
+    // one CTA per column chunk: every block matrix in one asynchronous batch
+    // when it fits
+    const bool pf = sizeof(T) * ulv_root_smem(r.n, cpr, true) <= kSmemPrefetch;
+    size_t sm = sizeof(T) * ulv_root_smem(r.n, cpr, pf);
+    auto kern = pf ? ulv_root_kernel<T, true> : ulv_root_kernel<T, false>;
     set_smem(kern, sm);
     dim3 grid(1, (c + cpr - 1) / cpr);
     if (lt) lt->mark(st);
@@ -150,12 +166,20 @@ void ulv_solve_fused(cudaStream_t st, const Hbs& H, T* B, int ldb, int c, T* scr
   int in = 2;
   for (int t = L - 2; t >= 0; --t) {
     const Level& l = H.lv[t];
-    const int cpb = chunk_for<T>(l.Nb, c);
-    size_t sm = sizeof(T) * ((size_t)l.n * (l.n + 1) + (2 * (size_t)l.k + l.nu + l.n) * cpb);
-    auto kern = ulv_bwd_kernel<T>;
+    const size_t per_col = 2 * (size_t)l.k + l.nu + 2 * (size_t)l.n;
+    const int cpb = fit_chunk<T>(chunk_for<T>(l.Nb, c),
+                                 ulv_bwd_smem(l.n, l.nu, l.k, 0, false, t == 0), per_col,
+                                 kSmemPrefetch);
+    dim3 grid(l.Nb, (c + cpb - 1) / cpb);
+    // levels that fit in one wave copy all their block matrices in one
+    // asynchronous batch (larger shared memory, fewer CTAs per SM)
+    const bool leaf = t == 0;
+    const bool pf = (long long)grid.x * grid.y <= num_sms() &&
+                    sizeof(T) * ulv_bwd_smem(l.n, l.nu, l.k, cpb, true, leaf) <= kSmemPrefetch;
+    size_t sm = sizeof(T) * ulv_bwd_smem(l.n, l.nu, l.k, cpb, pf, leaf);
+    auto kern = pf ? ulv_bwd_kernel<T, true> : ulv_bwd_kernel<T, false>;
     set_smem(kern, sm);
     const int out = (in == 2) ? 0 : 2;
-    dim3 grid(l.Nb, (c + cpb - 1) / cpb);
     if (lt) lt->mark(st);
     kern<<<grid, kThreads, sm, st>>>(l.n, l.nu, l.k, ru + NN[t] * c, F::Uu(l), F::R(l), F::W(l),
                                      F::U(l), F::D(l), P[in + 1], P[in], P[out], P[out + 1],

@@ -12,9 +12,10 @@ The default shape is the sketch product of an N = 4096 dense block with the
 261 Gaussian samples of the rank-32 / leaf-64 HBS compression.  Prints one
 JSON line with the median time, the tensor FLOP rate (6 split products) and
 the effective rate (2 m n k).
-solve: the float64 ULV solve (slu_ulv_solve, mode N) of a synthetic exact
-HBS operator of size m (leaf 64, rank 32, ULV from the given factors) with n
-right-hand sides; prints the median time per solve.
+solve: the float64 ULV solve (mode N) of a synthetic exact HBS operator of
+size m (leaf 64, rank 32, ULV from the given factors) with n right-hand
+sides, two ways: per-level launches (slu_ulv_solve) and the grouped sweep of
+a one-member group; prints the median time per solve of each.
 compress: HBSMAT.construct(32, compute_ULV=True) of a synthetic exact HBS
 operator of size m (leaf 64, rank 32, singular values 1 -> 1e-12), the
 sketches sampled through the resident operator; prints the median time and
@@ -95,23 +96,34 @@ def solve(a):
     W = B.clone()
     L, h = _lib.lib(), _lib.handle()
 
-    def run():
+    import ctypes
+    ops = (ctypes.c_void_p * 1)(H._op)
+    bp = (ctypes.c_void_p * 1)(W.data_ptr())
+    ld = (ctypes.c_int * 1)(c)
+
+    def per_level():
         _lib.check(L.slu_ulv_solve(h, H._op, _lib.ptr(W), c, c, 0))
 
-    for _ in range(a.warmup):
-        run()
-    torch.cuda.synchronize()
+    def grouped():
+        _lib.check(L.slu_ulv_solve_grouped(h, 1, ops, bp, ld, ld))
+
+    out = {"kernel": "solve", "N": N, "nrhs": c, "levels": Lv}
     st = torch.cuda.current_stream()
-    ts = []
-    for _ in range(a.reps):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(st)
-        run()
-        e1.record(st)
-        e1.synchronize()
-        ts.append(e0.elapsed_time(e1) * 1e-3)
-    print(json.dumps({"kernel": "solve", "N": N, "nrhs": c, "levels": Lv,
-                      "median_ms": 1e3 * statistics.median(ts)}))
+    for name, run in (("per_level", per_level), ("grouped", grouped)):
+        for _ in range(a.warmup):
+            run()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(a.reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            run()
+            e1.record(st)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1) * 1e-3)
+        _lib.sync()
+        out[name + "_ms"] = 1e3 * statistics.median(ts)
+    print(json.dumps(out))
 
 
 def compress(a):

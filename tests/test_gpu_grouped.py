@@ -95,3 +95,25 @@ def test_grouped_mixed_refinement():
         solo, _, rs = H.solve_refined(b, tol=1e-10)
         assert rs <= 1e-10
         assert relerr(x, solo) < 1e-8
+
+
+@pytest.mark.parametrize("k", [16, 24, 33, 40, 48])
+def test_per_level_solve_equals_grouped_for_uneven_ranks(k):
+    """Ranks up to 3/4 of the leaf size and levels of 1-3 blocks: the
+    per-level kernels (which switch to one-batch prefetching of the block
+    matrices on small levels) agree with the grouped sweep to rounding."""
+    need_gpu()
+    from sslablu_gb300.grouped import solve_grouped
+    from sslablu_gb300.matAssembly.HBS.HBSnew import HBSMAT
+    from sslablu_gb300.synthetic import random_hbs_factors
+    for N in (128, 256, 512):
+        Lv = int(np.log2(N // 64)) + 1
+        U, D, V, Nbvec = random_hbs_factors(k, 64, Lv, quad=False,
+                                            rng=np.random.default_rng(N + k), shift=16.0)
+        H = HBSMAT().set_mats(U, D, V, list(Nbvec), fac=2)
+        H.compute_ULV()
+        b = np.random.default_rng(k).standard_normal((N, 8))
+        x_solo = H.solve(b)
+        x_grp = solve_grouped([(H, b)])[0]
+        assert relerr(H.matmat(x_grp), b) < 1e-12, (N, k)
+        assert relerr(x_solo, x_grp) < 1e-13, (N, k)
