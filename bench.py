@@ -375,14 +375,130 @@ def run_gpu(args, rank, world):
     return line
 
 
+# ---------------------------------------------------------------- other rows
+# `--workload` measures the other slab-solver rows, one JSON line each, with
+# the oracle (the numpy restatement of the upstream solver) timed beside the
+# GPU path on the host cores.  Single GPU; the headline remains the default.
+def run_other(args):
+    import types
+    import torch
+    from oracle import direct as od
+    torch.cuda.set_device(0)
+    base = {"n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic"}
+    if args.workload == "c1_dense":
+        from sslablu_gb300 import slabbench
+        from sslablu_gb300.synthetic import slab_couplings
+        m, nS = 256, 8
+        g = slabbench.dense(types.SimpleNamespace(m=m, slabs=nS, reps=args.steps))
+        S = slab_couplings(m, nS)
+        T = [np.eye(m) for _ in range(nS)]
+        B = np.random.default_rng(1).standard_normal((nS * m, 64))
+        cpu = {}
+        for name, cls in (("rb_f64", od.RedBlackDense), ("thomas_f64", od.ThomasDense)):
+            t0 = time.perf_counter()
+            sv = cls(m).factorize(S, T)
+            t_f = time.perf_counter() - t0
+            ts = []
+            for _ in range(3):
+                t0 = time.perf_counter()
+                sv.solve(B)
+                ts.append(time.perf_counter() - t0)
+            cpu[name] = {"factor_ms": 1e3 * t_f, "rhs_per_s_64rhs": 64 / statistics.median(ts)}
+        line = dict(base, metric="dense red-black RHS solves/sec, 64 RHS", unit="RHS/s",
+                    value=g["rb_f64"]["rhs_per_s_64rhs"],
+                    ms_per_step=g["rb_f64"]["solve_64rhs_ms"],
+                    config={"workload": g["workload"], "slabs": nS, "m": m, "nrhs": 64},
+                    arms=g,
+                    cpu_baseline={"value": cpu["rb_f64"]["rhs_per_s_64rhs"], "unit": "RHS/s",
+                                  "cores": os.cpu_count(), "kind": "port",
+                                  "sample": "upstream RedBlackSolver / BlockTridiagonalSolver "
+                                            "restated in numpy, same system, 64 RHS",
+                                  "arms": cpu})
+    elif args.workload == "c3_hbs":
+        from sslablu_gb300 import slabbench
+        from sslablu_gb300.synthetic import slab_couplings
+        m, nS, leaf, rk, m_cpu = 1024, 8, 64, 24, 256
+        ns = types.SimpleNamespace(m=m, slabs=nS, leaf=leaf, rank=rk, reps=max(3, args.steps // 5))
+        g = slabbench.hbs(ns)
+        g_small = slabbench.hbs(types.SimpleNamespace(m=m_cpu, slabs=nS, leaf=leaf, rank=rk,
+                                                      reps=ns.reps))
+        S = slab_couplings(m_cpu, nS)
+        B = np.random.default_rng(2).standard_normal((nS * m_cpu, 64))
+        td = (np.arange(m_cpu), m_cpu // leaf, int(np.log2(m_cpu // leaf)) + 1)
+        Sop = [(od.dense_op(x), od.dense_op(y)) for x, y in S]
+        cpu = {}
+        for name, cls in (("rb_hbs", od.RedBlackHBS), ("thomas_hbs", od.ThomasHBS)):
+            np.random.seed(11)
+            t0 = time.perf_counter()
+            sv = cls(m_cpu, rk, td, False).factorize(Sop)
+            t_f = time.perf_counter() - t0
+            t0 = time.perf_counter()
+            try:
+                sv.solve(B)
+            except ValueError:   # the upstream red-black HBS solve takes one column
+                for j in range(B.shape[1]):
+                    sv.solve(B[:, j])
+            t_s = time.perf_counter() - t0
+            cpu[name] = {"m": m_cpu, "factor_ms": 1e3 * t_f, "rhs_per_s_64rhs": 64 / t_s,
+                         "gpu_same_size": g_small[name]}
+        line = dict(base, metric="HBS red-black RHS solves/sec, 64 RHS", unit="RHS/s",
+                    value=g["rb_hbs"]["rhs_per_s_64rhs"],
+                    ms_per_step=g["rb_hbs"]["solve_64rhs_ms"],
+                    config={"workload": g["workload"], "slabs": nS, "m": m, "leaf": leaf,
+                            "rank": rk, "nrhs": 64},
+                    arms=g,
+                    cpu_baseline={"value": cpu["rb_hbs"]["rhs_per_s_64rhs"], "unit": "RHS/s",
+                                  "cores": os.cpu_count(), "kind": "port",
+                                  "sample": "upstream RedBlackSolverHBS / ThomasSolverHBS "
+                                            "restated in numpy at %d-point interfaces (the GPU "
+                                            "at the same size is in arms.gpu_same_size)" % m_cpu,
+                                  "arms": cpu})
+    else:   # c4_batch
+        import subprocess
+        out = subprocess.run([sys.executable, "-m", "sslablu_gb300.batchbench", "--reps",
+                              str(args.steps)], capture_output=True, text=True, check=True)
+        g = json.loads(out.stdout.strip().splitlines()[-1])
+        # CPU: the oracle's per-system ULV solve over a sample of the systems
+        from sslablu_gb300.batchbench import system_factors
+        sample = system_factors(32, 20261205)
+        ts = 0.0
+        nrhs = 0
+        for U, D, V, Nbvec in sample:
+            O = od_hbs().set_mats(U, D, V, list(Nbvec), fac=2)
+            O.compute_ULV()
+            b = np.random.default_rng(3).standard_normal((O.shape[0], 8))
+            t0 = time.perf_counter()
+            O.solve(b)
+            ts += time.perf_counter() - t0
+            nrhs += 8
+        line = dict(base, metric="batched HBS RHS solves/sec (512 uneven systems x 8 RHS)",
+                    unit="RHS/s", value=g["grouped_f64"]["rhs_per_s"],
+                    ms_per_step=g["grouped_f64"]["ms_per_step"],
+                    config={"workload": g["workload"], "sizes": g["sizes"]}, arms=g,
+                    cpu_baseline={"value": nrhs / ts, "unit": "RHS/s", "cores": os.cpu_count(),
+                                  "kind": "port",
+                                  "sample": "upstream ULVsparse.solve restated in numpy, the "
+                                            "first 32 of the 512 systems, 8 RHS each"})
+    print(json.dumps(line))
+
+
+def od_hbs():
+    from oracle.hbs import OracleHBS
+    return OracleHBS()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c1_dense", "c3_hbs", "c4_batch"])
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
+    if args.workload != "c2":
+        return run_other(args)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if world > 1 and args.impl == "native":

@@ -27,18 +27,25 @@ import torch
 from . import _lib as L
 
 
-def build_batch(systems, seed, sizes=(128, 256, 512, 1024, 2048), ranks=(16, 48), shift=16.0):
-    from .matAssembly.HBS.HBSnew import HBSMAT
+def system_factors(systems, seed, sizes=(128, 256, 512, 1024, 2048), ranks=(16, 48),
+                   shift=16.0):
+    """(Umats, Dmats, Vmats, Nbvec) of the first `systems` systems of the batch."""
     from .synthetic import random_hbs_factors
     rng = np.random.default_rng(seed)
-    ops = []
+    out = []
     for j in range(systems):
         N = int(rng.choice(sizes))
         k = int(rng.integers(ranks[0], ranks[1] + 1))
         Lv = int(np.log2(N // 64)) + 1
-        U, D, V, Nbvec = random_hbs_factors(k, 64, Lv, quad=False,
-                                            rng=np.random.default_rng(seed + 1000 + j),
-                                            shift=shift)
+        out.append(random_hbs_factors(k, 64, Lv, quad=False,
+                                      rng=np.random.default_rng(seed + 1000 + j), shift=shift))
+    return out
+
+
+def build_batch(systems, seed):
+    from .matAssembly.HBS.HBSnew import HBSMAT
+    ops = []
+    for U, D, V, Nbvec in system_factors(systems, seed):
         H = HBSMAT().set_mats(U, D, V, list(Nbvec), fac=2)
         H.compute_ULV()
         ops.append(H)

@@ -47,44 +47,47 @@ int num_sms() {
 // ============================================================== batched GEMM
 // 64x64 output tile per CTA, 256 threads, 4x4 outputs per thread, K step 16.
 namespace {
-constexpr int GBM = 64, GBN = 64, GBK = 16;
+constexpr int GBK = 16;
 
-template <typename T>
+// TM x TM output tile per CTA (TM = 64, or 32 when 64-tiles would leave most
+// SMs idle); 16 x 16 threads, each (TM/16) x (TM/16) outputs.
+template <typename T, int TM>
 __global__ void __launch_bounds__(256)
 gemm_kernel(int M, int N, int K, T alpha, const T* __restrict__ A, int lda, long long sA0,
             long long sA1, bool ta, const T* __restrict__ B, int ldb, long long sB0,
             long long sB1, bool tb, T beta, T* __restrict__ C, int ldc, long long sC0,
             long long sC1, int batch0) {
-  __shared__ T As[GBK][GBM + 1];
-  __shared__ T Bs[GBK][GBN + 1];
+  constexpr int R = TM / 16;
+  __shared__ T As[GBK][TM + 1];
+  __shared__ T Bs[GBK][TM + 1];
   const int b = blockIdx.z;
   const int b0 = b % batch0, b1 = b / batch0;
   A += b0 * sA0 + b1 * sA1;
   B += b0 * sB0 + b1 * sB1;
   C += b0 * sC0 + b1 * sC1;
-  const int row0 = blockIdx.y * GBM, col0 = blockIdx.x * GBN;
+  const int row0 = blockIdx.y * TM, col0 = blockIdx.x * TM;
   const int tid = threadIdx.x;
   const int tx = tid & 15, ty = tid >> 4;
-  T acc[4][4];
+  T acc[R][R];
 #pragma unroll
-  for (int i = 0; i < 4; ++i)
+  for (int i = 0; i < R; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
+    for (int j = 0; j < R; ++j) acc[i][j] = T(0);
 
   for (int k0 = 0; k0 < K; k0 += GBK) {
 #pragma unroll
-    for (int e = tid; e < GBM * GBK; e += 256) {
+    for (int e = tid; e < TM * GBK; e += 256) {
       int i, kk;
-      if (!ta) { i = e / GBK; kk = e % GBK; } else { kk = e / GBM; i = e % GBM; }
+      if (!ta) { i = e / GBK; kk = e % GBK; } else { kk = e / TM; i = e % TM; }
       int gi = row0 + i, gk = k0 + kk;
       T v = T(0);
       if (gi < M && gk < K) v = ta ? A[(long long)gk * lda + gi] : A[(long long)gi * lda + gk];
       As[kk][i] = v;
     }
 #pragma unroll
-    for (int e = tid; e < GBN * GBK; e += 256) {
+    for (int e = tid; e < TM * GBK; e += 256) {
       int j, kk;
-      if (!tb) { kk = e / GBN; j = e % GBN; } else { j = e / GBK; kk = e % GBK; }
+      if (!tb) { kk = e / TM; j = e % TM; } else { j = e / GBK; kk = e % GBK; }
       int gj = col0 + j, gk = k0 + kk;
       T v = T(0);
       if (gj < N && gk < K) v = tb ? B[(long long)gj * ldb + gk] : B[(long long)gk * ldb + gj];
@@ -93,24 +96,24 @@ gemm_kernel(int M, int N, int K, T alpha, const T* __restrict__ A, int lda, long
     __syncthreads();
 #pragma unroll
     for (int kk = 0; kk < GBK; ++kk) {
-      T a[4], bb[4];
+      T a[R], bb[R];
 #pragma unroll
-      for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
+      for (int i = 0; i < R; ++i) a[i] = As[kk][ty + 16 * i];
 #pragma unroll
-      for (int j = 0; j < 4; ++j) bb[j] = Bs[kk][tx + 16 * j];
+      for (int j = 0; j < R; ++j) bb[j] = Bs[kk][tx + 16 * j];
 #pragma unroll
-      for (int i = 0; i < 4; ++i)
+      for (int i = 0; i < R; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], bb[j], acc[i][j]);
+        for (int j = 0; j < R; ++j) acc[i][j] = fma(a[i], bb[j], acc[i][j]);
     }
     __syncthreads();
   }
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
+  for (int i = 0; i < R; ++i) {
     int gi = row0 + ty + 16 * i;
     if (gi >= M) continue;
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
+    for (int j = 0; j < R; ++j) {
       int gj = col0 + tx + 16 * j;
       if (gj >= N) continue;
       T* c = C + (long long)gi * ldc + gj;
@@ -120,6 +123,65 @@ gemm_kernel(int M, int N, int K, T alpha, const T* __restrict__ A, int lda, long
     }
   }
 }
+// Skinny products (N <= kSkinny columns, B not transposed): the 64 x 64 tile
+// kernel would compute 64 output columns per tile regardless of N.  Here each
+// output row is one warp (A row-major: lanes stride over K, coalesced, then a
+// shuffle reduction per column) or one thread (A transposed: threads over
+// rows read A[k][i] coalesced while looping over K); B rows are broadcast.
+constexpr int kSkinny = 16;
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+gemm_skinny_kernel(int M, int N, int K, T alpha, const T* __restrict__ A, int lda,
+                   long long sA0, long long sA1, bool ta, const T* __restrict__ B, int ldb,
+                   long long sB0, long long sB1, T beta, T* __restrict__ C, int ldc,
+                   long long sC0, long long sC1, int batch0) {
+  const int b = blockIdx.z;
+  const int b0 = b % batch0, b1 = b / batch0;
+  A += b0 * sA0 + b1 * sA1;
+  B += b0 * sB0 + b1 * sB1;
+  C += b0 * sC0 + b1 * sC1;
+  T acc[kSkinny];
+#pragma unroll
+  for (int j = 0; j < kSkinny; ++j) acc[j] = T(0);
+  int row;
+  if (!ta) {
+    const int lane = threadIdx.x & 31;
+    row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (row >= M) return;   // whole warp
+    const T* a = A + (long long)row * lda;
+    for (int k = lane; k < K; k += 32) {
+      const T av = a[k];
+      const T* bk = B + (long long)k * ldb;
+#pragma unroll
+      for (int j = 0; j < kSkinny; ++j)
+        if (j < N) acc[j] = fma(av, bk[j], acc[j]);
+    }
+#pragma unroll
+    for (int j = 0; j < kSkinny; ++j)
+      for (int o = 16; o > 0; o >>= 1) acc[j] += __shfl_xor_sync(0xffffffffu, acc[j], o);
+    if (lane != 0) return;
+  } else {
+    row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= M) return;
+    for (int k = 0; k < K; ++k) {
+      const T av = A[(long long)k * lda + row];
+      const T* bk = B + (long long)k * ldb;
+#pragma unroll
+      for (int j = 0; j < kSkinny; ++j)
+        if (j < N) acc[j] = fma(av, bk[j], acc[j]);
+    }
+  }
+  T* c = C + (long long)row * ldc;
+#pragma unroll
+  for (int j = 0; j < kSkinny; ++j)
+    if (j < N) {
+      T v = alpha * acc[j];
+      if (beta != T(0)) v = fma(beta, c[j], v);
+      c[j] = v;
+    }
+}
+
 }  // namespace
 
 template <typename T>
@@ -140,9 +202,24 @@ void gemm_batched(cudaStream_t st, bool ta, bool tb, int M, int N, int K, T alph
   }
   long long nb = (long long)batch0 * batch1;
   SLU_REQUIRE(nb <= 65535, "gemm batch too large");
-  dim3 grid((N + GBN - 1) / GBN, (M + GBM - 1) / GBM, (unsigned)nb);
-  gemm_kernel<T><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, sA0, sA1, ta, B, ldb, sB0, sB1,
-                                       tb, beta, C, ldc, sC0, sC1, batch0);
+  if (N <= kSkinny && !tb) {
+    const int rows_per_cta = ta ? 256 : 8;
+    dim3 g((M + rows_per_cta - 1) / rows_per_cta, 1, (unsigned)nb);
+    gemm_skinny_kernel<T><<<g, 256, 0, st>>>(M, N, K, alpha, A, lda, sA0, sA1, ta, B, ldb, sB0,
+                                             sB1, beta, C, ldc, sC0, sC1, batch0);
+    check_launch("gemm_skinny_kernel");
+    return;
+  }
+  const long long tiles64 = (long long)((N + 63) / 64) * ((M + 63) / 64) * nb;
+  if (tiles64 < num_sms()) {
+    dim3 grid((N + 31) / 32, (M + 31) / 32, (unsigned)nb);
+    gemm_kernel<T, 32><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, sA0, sA1, ta, B, ldb, sB0,
+                                             sB1, tb, beta, C, ldc, sC0, sC1, batch0);
+  } else {
+    dim3 grid((N + 63) / 64, (M + 63) / 64, (unsigned)nb);
+    gemm_kernel<T, 64><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, sA0, sA1, ta, B, ldb, sB0,
+                                             sB1, tb, beta, C, ldc, sC0, sC1, batch0);
+  }
   check_launch("gemm_kernel");
 }
 
@@ -389,6 +466,121 @@ __global__ void lu_solve_kernel(bool trans, int n, const T* __restrict__ LU, int
     X[(long long)i * ldx + c0 + c] = xs[e];
   }
 }
+// X <- A^{-1} X from LAPACK-style LU factors, blocked by 32-row tiles: the
+// row swaps are composed into one permutation (one thread) and applied as a
+// gather; each diagonal tile is swept by one warp per right-hand-side column
+// (lane l holds row l of the tile; the finished x_i is broadcast by shuffle);
+// the rows outside the tile are then updated in parallel.  Two block barriers
+// per tile instead of one or two per row.  Arithmetic per element as in the
+// row-by-row kernel (the same divisions by the pivots).
+constexpr int kLuTile = 32;
+
+template <typename T>
+__global__ void lu_solve_tiled_kernel(int n, const T* __restrict__ LU, int lda, long long sA,
+                                      const int* __restrict__ piv, long long sP,
+                                      T* __restrict__ X, int ldx, long long sX, int nrhs,
+                                      int chunk) {
+  const int b = blockIdx.y;
+  LU += b * sA;
+  piv += b * sP;
+  X += b * sX;
+  const int c0 = blockIdx.x * chunk;
+  const int nc = min(chunk, nrhs - c0);
+  if (nc <= 0) return;
+  extern __shared__ unsigned char smraw[];
+  T* xs = reinterpret_cast<T*>(smraw);                         // n x nc
+  T* dt = xs + (size_t)n * nc;                                 // diagonal tile, 32 x 33
+  int* perm = reinterpret_cast<int*>(dt + kLuTile * (kLuTile + 1));   // n
+  int* pv = perm + n;                                          // n
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) pv[i] = piv[i];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < n; ++i) perm[i] = i;
+    for (int i = 0; i < n; ++i) {
+      const int p = pv[i];
+      const int t = perm[i];
+      perm[i] = perm[p];
+      perm[p] = t;
+    }
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < n * nc; e += blockDim.x) {
+    const int i = e / nc, c = e - i * nc;
+    xs[e] = X[(long long)perm[i] * ldx + c0 + c];
+  }
+  // forward: unit lower L
+  for (int t0 = 0; t0 < n; t0 += kLuTile) {
+    const int tn = min(kLuTile, n - t0);
+    for (int e = threadIdx.x; e < tn * tn; e += blockDim.x) {
+      const int i = e / tn, j = e - i * tn;
+      dt[i * (kLuTile + 1) + j] = LU[(long long)(t0 + i) * lda + t0 + j];
+    }
+    __syncthreads();
+    for (int c = warp; c < nc; c += nw) {
+      T xl = lane < tn ? xs[(t0 + lane) * nc + c] : T(0);
+      for (int i = 0; i < tn; ++i) {
+        const T xi = __shfl_sync(0xffffffffu, xl, i);
+        if (lane > i && lane < tn) xl -= dt[lane * (kLuTile + 1) + i] * xi;
+      }
+      if (lane < tn) xs[(t0 + lane) * nc + c] = xl;
+    }
+    __syncthreads();
+    const int below = n - t0 - tn;
+    for (int e = threadIdx.x; e < below * nc; e += blockDim.x) {
+      const int r = t0 + tn + e / nc, c = e % nc;
+      const T* l = LU + (long long)r * lda + t0;
+      T acc = xs[r * nc + c];
+      if (tn == kLuTile) {   // full tile: all 32 loads of the row segment in flight
+#pragma unroll
+        for (int i = 0; i < kLuTile; ++i) acc -= __ldg(l + i) * xs[(t0 + i) * nc + c];
+      } else {
+        for (int i = 0; i < tn; ++i) acc -= l[i] * xs[(t0 + i) * nc + c];
+      }
+      xs[r * nc + c] = acc;
+    }
+    __syncthreads();
+  }
+  // backward: upper U; each lane inverts its row's pivot up front (all lanes
+  // at once) and the sweep multiplies -- a division per row on one lane
+  // would serialise the float64 pipe through the whole sweep
+  for (int t1 = n; t1 > 0; t1 -= kLuTile) {
+    const int t0 = max(0, t1 - kLuTile), tn = t1 - t0;
+    for (int e = threadIdx.x; e < tn * tn; e += blockDim.x) {
+      const int i = e / tn, j = e - i * tn;
+      dt[i * (kLuTile + 1) + j] = LU[(long long)(t0 + i) * lda + t0 + j];
+    }
+    __syncthreads();
+    for (int c = warp; c < nc; c += nw) {
+      const T rl = lane < tn ? T(1) / dt[lane * (kLuTile + 1) + lane] : T(0);
+      T xl = lane < tn ? xs[(t0 + lane) * nc + c] : T(0);
+      for (int i = tn - 1; i >= 0; --i) {
+        if (lane == i) xl *= rl;
+        const T xi = __shfl_sync(0xffffffffu, xl, i);
+        if (lane < i) xl -= dt[lane * (kLuTile + 1) + i] * xi;
+      }
+      if (lane < tn) xs[(t0 + lane) * nc + c] = xl;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < t0 * nc; e += blockDim.x) {
+      const int r = e / nc, c = e % nc;
+      const T* u = LU + (long long)r * lda + t0;
+      T acc = xs[r * nc + c];
+      if (tn == kLuTile) {
+#pragma unroll
+        for (int i = 0; i < kLuTile; ++i) acc -= __ldg(u + i) * xs[(t0 + i) * nc + c];
+      } else {
+        for (int i = 0; i < tn; ++i) acc -= u[i] * xs[(t0 + i) * nc + c];
+      }
+      xs[r * nc + c] = acc;
+    }
+    __syncthreads();
+  }
+  for (int e = threadIdx.x; e < n * nc; e += blockDim.x) {
+    const int i = e / nc, c = e - i * nc;
+    X[(long long)i * ldx + c0 + c] = xs[e];
+  }
+}
 }  // namespace
 
 void lu_factor(cudaStream_t st, int n, double* A, int lda, long long sA, int* piv, long long sP,
@@ -404,13 +596,23 @@ void lu_solve(cudaStream_t st, bool trans, int n, const T* LU, int lda, long lon
   if (n <= 0 || nrhs <= 0 || batch <= 0) return;
   int chunk = nrhs;
   while ((size_t)n * chunk * sizeof(T) > 96 * 1024 && chunk > 1) chunk = (chunk + 1) / 2;
-  // spread wide right-hand sides over several CTAs
-  while (chunk > 16 && (long long)batch * ((nrhs + chunk - 1) / chunk) < num_sms()) chunk /= 2;
+  // spread the right-hand sides over ~2 CTAs per SM (the substitutions of
+  // different columns are independent)
+  while (chunk > (trans ? 16 : 1) && (long long)batch * ((nrhs + chunk - 1) / chunk) < 2 * num_sms())
+    chunk = (chunk + 1) / 2;
   size_t sm = (size_t)n * chunk * sizeof(T);
   SLU_REQUIRE(sm <= 96 * 1024, "lu_solve block too large");
+  dim3 grid((nrhs + chunk - 1) / chunk, batch);
+  if (!trans) {
+    auto kern = lu_solve_tiled_kernel<T>;
+    const size_t smt = sm + sizeof(T) * kLuTile * (kLuTile + 1) + 2 * sizeof(int) * (size_t)n;
+    ensure_smem((const void*)kern, smt);
+    kern<<<grid, 256, smt, st>>>(n, LU, lda, sA, piv, sP, X, ldx, sX, nrhs, chunk);
+    check_launch("lu_solve_tiled_kernel");
+    return;
+  }
   auto kern = lu_solve_kernel<T>;
   ensure_smem((const void*)kern, sm);
-  dim3 grid((nrhs + chunk - 1) / chunk, batch);
   kern<<<grid, 256, sm, st>>>(trans, n, LU, lda, sA, piv, sP, X, ldx, sX, nrhs, chunk);
   check_launch("lu_solve_kernel");
 }

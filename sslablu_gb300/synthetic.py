@@ -55,3 +55,34 @@ def random_hbs_factors(k, nl, L, quad=False, sigma=None, rng=None, shift=0.0):
 def decaying_sigma(k, smallest=1e-12):
     """Singular values 1 -> smallest, geometric over k columns."""
     return 10.0 ** (np.log10(smallest) * np.arange(k) / max(k - 1, 1))
+
+
+def slab_couplings(m, nS, c=20.0):
+    """Block-tridiagonal interface couplings of nS slabs with m-point
+    interfaces: S_{i,i-1} and S_{i,i+1} are Gaussian kernels of the interface
+    coordinate, shifted by +-0.2 (+-0.01 per slab), scaled by 0.3, so that
+    I + S is well conditioned and its blocks are HBS compressible.  Returns
+    [(S_{i,i-1}, S_{i,i+1})], with zero outer blocks."""
+    x = np.linspace(0, 1, m)
+
+    def blk(shift):
+        return 0.3 * np.exp(-c * (x[:, None] - x[None, :] - shift) ** 2)
+    out = []
+    for i in range(nS):
+        A = blk(0.2 + 0.01 * i) if i > 0 else np.zeros((m, m))
+        C = blk(-0.2 - 0.01 * i) if i < nS - 1 else np.zeros((m, m))
+        out.append((A, C))
+    return out
+
+
+def tridiag_apply(S, X):
+    """(I + block off-diagonals of S) X for X of shape (nS * m, r), numpy."""
+    nS = len(S)
+    m = S[0][0].shape[0]
+    Y = X.copy()
+    for i in range(nS):
+        if i > 0:
+            Y[i * m:(i + 1) * m] += S[i][0] @ X[(i - 1) * m:i * m]
+        if i < nS - 1:
+            Y[i * m:(i + 1) * m] += S[i][1] @ X[(i + 1) * m:(i + 2) * m]
+    return Y
