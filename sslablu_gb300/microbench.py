@@ -5,6 +5,7 @@
 
     python -m sslablu_gb300.microbench compress [--m 4096 --reps 5]
     python -m sslablu_gb300.microbench solve [--m 4096 --n 16 --reps 20]
+    python -m sslablu_gb300.microbench refine [--m 4096 --reps 10]
 
 tc_gemm : slu_gemm_split3 (tcgen05 split-BF16x3, float32 accumulation)
 f64_gemm: slu_gemm_batched (float64 CUDA-core GEMM) on the same shape
@@ -16,6 +17,9 @@ solve: the float64 ULV solve (mode N) of a synthetic exact HBS operator of
 size m (leaf 64, rank 32, ULV from the given factors) with n right-hand
 sides, two ways: per-level launches (slu_ulv_solve) and the grouped sweep of
 a one-member group; prints the median time per solve of each.
+refine: float64 ULV solve against mixed-precision refinement to 1e-10
+(float32 sweeps + double-float residuals) on the same operator, for 16, 64,
+256 and 1024 right-hand sides; prints both times and the ratio.
 compress: HBSMAT.construct(32, compute_ULV=True) of a synthetic exact HBS
 operator of size m (leaf 64, rank 32, singular values 1 -> 1e-12), the
 sketches sampled through the resident operator; prints the median time and
@@ -33,7 +37,7 @@ from . import _lib
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("kernel", choices=["tc_gemm", "f64_gemm", "compress", "solve"])
+    ap.add_argument("kernel", choices=["tc_gemm", "f64_gemm", "compress", "solve", "refine"])
     ap.add_argument("--m", type=int, default=4096)
     ap.add_argument("--n", type=int, default=261)
     ap.add_argument("--k", type=int, default=4096)
@@ -44,6 +48,8 @@ def main():
         return compress(a)
     if a.kernel == "solve":
         return solve(a)
+    if a.kernel == "refine":
+        return refine(a)
     m, n, k = a.m, a.n, a.k
     rng = np.random.default_rng(0)
     A = torch.from_numpy(rng.standard_normal((m, k))).cuda()
@@ -123,6 +129,43 @@ def solve(a):
             ts.append(e0.elapsed_time(e1) * 1e-3)
         _lib.sync()
         out[name + "_ms"] = 1e3 * statistics.median(ts)
+    print(json.dumps(out))
+
+
+def refine(a):
+    from .matAssembly.HBS.HBSnew import HBSMAT
+    from .synthetic import decaying_sigma, random_hbs_factors
+    N = a.m
+    Lv = int(np.log2(N // 64)) + 1
+    np.random.seed(1)
+    U, D, V, Nbvec = random_hbs_factors(32, 64, Lv, quad=False, sigma=decaying_sigma(32),
+                                        shift=16.0)
+    H = HBSMAT().set_mats(U, D, V, list(Nbvec), fac=2)
+    H.compute_ULV()
+    st = torch.cuda.current_stream()
+    out = {"kernel": "refine", "N": N}
+
+    def timed(fn):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(a.reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            fn()
+            e1.record(st)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1) * 1e-3)
+        return statistics.median(ts)
+
+    for c in (16, 64, 256, 1024):
+        B = torch.from_numpy(np.random.default_rng(c).standard_normal((N, c))).cuda()
+        t64 = timed(lambda: H._dev_solve(B, False))
+        res = {}
+        tmx = timed(lambda: res.update(r=H.solve_refined(B, tol=1e-10)))
+        out["c%d" % c] = {"f64_ms": 1e3 * t64, "mixed_ms": 1e3 * tmx, "mixed_speedup": t64 / tmx,
+                          "iters": res["r"][1], "relres": res["r"][2]}
     print(json.dumps(out))
 
 
