@@ -248,6 +248,25 @@ def launch_roofline(H, B, flush, hbm, src, reps):
             "device_ms_per_solve": total, "launches": launches}
 
 
+# ---------------------------------------------------------------- replicas
+def max_over_ranks(values, world, device):
+    """Element-wise maximum over the ranks of a torch.distributed job (the
+    slowest replica's times); the values themselves when world == 1."""
+    if world <= 1:
+        return list(values)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor(list(values), dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.tolist()
+
+
+def replica_throughput(world, units_per_rank, slowest_seconds):
+    """Whole-job throughput of `world` independent replicas that each process
+    `units_per_rank` units, timed by the slowest one."""
+    return world * units_per_rank / slowest_seconds
+
+
 # ---------------------------------------------------------------- GPU leg
 def run_gpu(args, rank, world):
     import torch
@@ -334,13 +353,9 @@ def run_gpu(args, rank, world):
     res_mixed = residual(Xm)
     tot_plain = sum(ts_plain)
     tot_mixed = sum(ts_mixed)
-    if world > 1:
-        t = torch.tensor([tot_plain, tot_mixed, sum(e2e)], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        tot_plain, tot_mixed, tot_e2e = t.tolist()
-    else:
-        tot_e2e = sum(e2e)
-    value = world * NRHS * args.steps / tot_plain
+    tot_plain, tot_mixed, tot_e2e = max_over_ranks([tot_plain, tot_mixed, sum(e2e)], world,
+                                                   "cuda")
+    value = replica_throughput(world, NRHS * args.steps, tot_plain)
     p50 = statistics.median(ts_plain)
     hbm, src = peaks()
     roof = launch_roofline(H, B, flush, hbm, src, reps=max(5, args.steps))
