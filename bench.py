@@ -174,22 +174,20 @@ def run_reference(args, rank, world):
 # DRAM bytes (read + written) per launch of each solve kernel, averaged over
 # the launches of that kernel in the ncu launch list of
 # `python bench.py --steps 2 --warmup 3` (profiles/ulv_solve_c2_launches.txt).
-NCU_TRAFFIC = {"ulv_bwd_kernel<double>": 2007214, "ulv_fwd_kernel<double>": 875736,
-               "ulv_root_kernel<double>": None}
+NCU_TRAFFIC = {}
 FP64_NOMINAL_TFLOPS = 1.25   # GB300 float64 (no measured figure in the peaks file)
 
 
-def launch_cost(kind, Nb, n, k, nu, c, leaf):
-    """Algorithmic (bytes, flops) of one fused solve launch: every factor block
-    read once, the right-hand-side blocks read and written once."""
-    if kind == 0:      # z = Q^T x: Q, x in; ru, parent part out
-        return 8 * Nb * (n * n + 2 * n * c), 2 * Nb * n * n * c
-    if kind == 1:      # y = R^-1 Q^T x, v = D y
-        return 8 * (3 * n * n + 3 * n * c), 5 * n * n * c
-    fac = nu * k + nu * n + n * n + (0 if leaf else n * k + n * n)
-    vec = c * (nu + 2 * k) + (n * c if leaf else 2 * n * c)
-    fl = c * (4 * nu * k + nu * nu + 2 * n * n + (0 if leaf else 2 * n * k + 2 * n * n))
-    return 8 * Nb * (fac + vec), Nb * fl
+def launch_cost(kind, Nb, n, k, nu, c, leaf, single=False):
+    """Algorithmic (bytes, flops) of one fused solve launch: the block
+    operators read once, the right-hand-side blocks read and written once."""
+    if kind == 0:      # [ru; x_parent] = Q^T x
+        rows, w = n, n
+    elif kind == 1:    # [y; v] = [R^-1 Q^T; D R^-1 Q^T] x
+        rows, w = (n if single else 2 * n), n
+    else:              # [y_new; v_new] = [G; H] [ru; v; y_next]
+        rows, w = (n if leaf else 2 * n), nu + 2 * k
+    return 8 * Nb * (rows * w + w * c + rows * c), 2 * Nb * rows * w * c
 
 
 def launch_roofline(H, B, flush, hbm, src, reps):
@@ -217,13 +215,13 @@ def launch_roofline(H, B, flush, hbm, src, reps):
         runs.append([ms[i] for i in range(cnt.value)])
         meta = [(lvl[i], kind[i]) for i in range(cnt.value)]
     med = np.median(np.array(runs), axis=0)
-    names = {0: "ulv_fwd_kernel", 1: "ulv_root_kernel", 2: "ulv_bwd_kernel"}
+    names = {0: "forward", 1: "root", 2: "backward"}
     launches = []
     for (t, kd), m in zip(meta, med):
         Nb, n, k, nu = (geo[4 * t + j] for j in range(4))
-        by, fl = launch_cost(kd, Nb, n, k, nu, c, t == 0)
-        launches.append({"kernel": "%s<double>" % names[kd], "level": t, "ms": float(m),
-                         "alg_bytes": int(by), "alg_flops": int(fl)})
+        by, fl = launch_cost(kd, Nb, n, k, nu, c, t == 0, nl.value == 1)
+        launches.append({"kernel": "step_kernel<double> (%s)" % names[kd], "level": t,
+                         "ms": float(m), "alg_bytes": int(by), "alg_flops": int(fl)})
     # the dominant kernel: the one with the largest share of the solve; its
     # roofline uses per-launch averages over its launches (one per level)
     groups = {}

@@ -126,16 +126,32 @@ int slu_ulv_solve_noalloc(slu_handle_t h, slu_hbs_t op, double* B, int ldb, int 
 int slu_hbs_prepare_f32(slu_handle_t h, slu_hbs_t op);
 int slu_ulv_solve_f32(slu_handle_t h, slu_hbs_t op, float* B, int ldb, int nrhs, int trans);
 
-/* Iterative refinement of A x = b with float32 ULV solves and a float64-
- * accurate residual r = b - A x of the stored HBS factors (the operator the
- * upstream solve inverts), evaluated in double-float arithmetic (factors as
- * float32 hi/lo pairs, error-free products and sums: ~1e-14 relative) on the
- * float32 units.  X holds the result (N x nrhs); iterations stop
- * when every column reaches ||r||/||b|| <= tol or after maxit corrections.
- * iters_out / relres_out (host pointers, may be NULL) receive the iteration
- * count and the largest final relative residual. */
+/* Double-float copy of the ULV factors (each float64 split into a float32
+ * pair hi + lo, interleaved) and a mode-N solve with the same fused sweep in
+ * double-float arithmetic on the float32 units: B (N x nrhs float64, device)
+ * <- A^{-1} B to ~1e-14 relative accuracy (48-bit significands, float32
+ * exponent range).  slu_ulv_solve_dfloat prepares the copy on first use;
+ * slu_hbs_prepare_dfloat does it ahead.  No upstream counterpart: a solve
+ * mode of the mixed-precision path of this library. */
+int slu_hbs_prepare_dfloat(slu_handle_t h, slu_hbs_t op);
+int slu_ulv_solve_dfloat(slu_handle_t h, slu_hbs_t op, double* B, int ldb, int nrhs);
+
+/* Iterative refinement of A x = b with ULV solves on the float32 units and a
+ * float64-accurate residual r = b - A x of the stored HBS factors (the
+ * operator the upstream solve inverts), evaluated in double-float arithmetic
+ * (factors as float32 hi/lo pairs, error-free products and sums: ~1e-14
+ * relative).  The inner solve is the double-float sweep (default; one
+ * iteration reaches 1e-10 on well-conditioned operators) or the float32
+ * sweep, chosen by slu_hbs_set_refine_inner.  X holds the result
+ * (N x nrhs); iterations stop when every column reaches ||r||/||b|| <= tol or
+ * after maxit corrections.  iters_out / relres_out (host pointers, may be
+ * NULL) receive the iteration count and the largest final relative
+ * residual. */
 int slu_refine(slu_handle_t h, slu_hbs_t op, const double* B, int ldb, double* X, int ldx,
                int nrhs, double tol, int maxit, int* iters_out, double* relres_out);
+/* Inner solve of slu_refine for `op`: mode 1 double-float sweep (default),
+ * mode 0 float32 sweep. */
+int slu_hbs_set_refine_inner(slu_hbs_t op, int mode);
 
 /* Null-space rule of the next slu_hbs_compress of `op`: mode 0 projects each
  * block's sketch on the last n columns of the complete Q of Om_blk^T

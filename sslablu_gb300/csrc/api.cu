@@ -181,7 +181,9 @@ int slu_hbs_set_level(slu_handle_t h, slu_hbs_t op, int level, int Nb, int n, in
       }
       H.has_mats = true;
       H.has_ulv = false;
+      H.has_sweep = false;
       H.has_f32 = false;
+      H.has_dfs = false;
       H.has_df = false;
       H.invalidate_plans();
     }
@@ -217,7 +219,10 @@ int slu_hbs_set_ulv_level(slu_handle_t h, slu_hbs_t op, int level, const double*
     for (int t = 0; t < H.L; ++t) all = all && H.lv[t].Q.p && H.lv[t].R.p;
     H.has_ulv = all;
     H.has_f32 = false;
+    H.has_dfs = false;
+    H.has_sweep = false;
     H.invalidate_plans();
+    if (all) slu::hbs_make_sweep(h->h, H);
   });
 }
 
@@ -257,6 +262,36 @@ int slu_ulv_solve_f32(slu_handle_t h, slu_hbs_t op, float* B, int ldb, int nrhs,
     SLU_REQUIRE(h && op && B, "null argument");
     SLU_REQUIRE(nrhs >= 1 && ldb >= nrhs, "bad right-hand side shape");
     slu::hbs_solve<float>(h->h, op->H, trans != 0, B, ldb, nrhs);
+  });
+}
+
+int slu_hbs_prepare_dfloat(slu_handle_t h, slu_hbs_t op) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h && op, "null argument");
+    slu::hbs_make_dfs(h->h, op->H);
+  });
+}
+
+int slu_ulv_solve_dfloat(slu_handle_t h, slu_hbs_t op, double* B, int ldb, int nrhs) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h && op && B, "null argument");
+    SLU_REQUIRE(nrhs >= 1 && ldb >= nrhs, "bad right-hand side shape");
+    slu::Hbs& H = op->H;
+    SLU_REQUIRE(H.has_ulv, "HBS operator has no ULV factorisation");
+    if (!H.has_dfs) slu::hbs_make_dfs(h->h, H);
+    const size_t bytes = slu::hbs_solve_df_scratch_bytes(H, nrhs);
+    h->h.ws.reserve(bytes + 256, h->h.stream);
+    void* scratch = h->h.ws.take<char>(bytes);
+    slu::hbs_solve_df(h->h.stream, H, B, ldb, nrhs, scratch);
+  });
+}
+
+int slu_hbs_set_refine_inner(slu_hbs_t op, int mode) {
+  return guard(nullptr, [&] {
+    SLU_REQUIRE(op, "null argument");
+    SLU_REQUIRE(mode == 0 || mode == 1, "refine inner mode must be 0 or 1");
+    if (op->H.refine_inner != mode) op->H.invalidate_plans();
+    op->H.refine_inner = mode;
   });
 }
 

@@ -9,7 +9,7 @@
 // task table lists, per segment, the member's factors, buffers and column
 // chunking, and the CTA range it owns; a CTA finds its segment by binary
 // search over the range starts and runs the same device body as the
-// per-operator kernel (ulv_bodies.cuh, df_bodies.cuh).  The schedule is
+// per-operator kernel (sweep.cuh, df_bodies.cuh).  The schedule is
 //   forward  t = 0 .. maxL-2   (members with L_i >= t + 2)
 //   root                         (every member)
 //   backward t = maxL-2 .. 0   (members with L_i >= t + 2)
@@ -18,8 +18,9 @@
 //
 // Mixed-precision refinement of a group (hbs_refine_grouped) runs the same
 // loop as refine.cu over concatenated buffers: one launch per elementwise step
-// for the whole group, the float32 grouped sweep, the grouped double-float
-// apply, and segmented column norms.
+// for the whole group, the grouped inner sweep (double-float, or float32 when
+// every member asks for it), the grouped double-float apply, and segmented
+// column norms.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -27,7 +28,7 @@
 #include "df_bodies.cuh"
 #include "hbs.cuh"
 #include "refine_kernels.cuh"
-#include "ulv_bodies.cuh"
+#include "sweep_host.cuh"
 
 namespace slu {
 namespace {
@@ -37,15 +38,12 @@ constexpr size_t kSmemLimit = 200 * 1024;
 
 using dfk::DF;
 
-// One tree step of one member in a grouped ULV sweep.
+// One tree step of one member in a grouped ULV sweep: its step (sweep.cuh),
+// the first CTA of its range and its column chunks per row slice.
 template <typename T>
-struct SolveSeg {
-  int kind;  // 0 forward, 1 root, 2 backward
-  int n, nu, k, c, cpb, nchunk, cta0, lds, ldb;
-  const T *Q, *R, *W, *U, *D, *Uu;
-  const T* src;
-  const int64_t* perm;
-  T *ru, *dst, *Yin, *Vin, *Yout, *Vout, *B;
+struct StepSeg {
+  sweep::Step<T> s;
+  int cta0, ncch;
 };
 
 // One tree step of one member in a grouped double-float apply.
@@ -84,24 +82,12 @@ __device__ __forceinline__ int find_seg(const S* __restrict__ segs, int nseg) {
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kThreads)
-group_solve_kernel(const SolveSeg<T>* __restrict__ segs, int nseg) {
+__global__ void __launch_bounds__(sweep::kMaxThreads)
+group_step_kernel(const StepSeg<T>* __restrict__ segs, int nseg) {
   extern __shared__ __align__(16) unsigned char sm_raw[];
-  const SolveSeg<T>& s = segs[find_seg(segs, nseg)];
-  const int local = blockIdx.x - s.cta0;
-  const int b = local / s.nchunk;
-  const int c0 = (local - b * s.nchunk) * s.cpb;
-  const int nc = min(s.cpb, s.c - c0);
-  if (nc <= 0) return;
-  if (s.kind == 0)
-    ulvk::ulv_fwd_body<T>(sm_raw, b, c0, nc, s.n, s.nu, s.k, s.Q, s.src, s.lds, s.perm, s.ru,
-                          s.dst, s.c, s.cpb);
-  else if (s.kind == 1)
-    ulvk::ulv_root_body<T, false>(sm_raw, c0, nc, s.n, s.Q, s.R, s.D, s.src, s.lds, s.perm, s.Yout,
-                           s.Vout, s.B, s.ldb, s.c, s.cpb);
-  else
-    ulvk::ulv_bwd_body<T, false>(sm_raw, b, c0, nc, s.n, s.nu, s.k, s.ru, s.Uu, s.R, s.W, s.U, s.D,
-                          s.Vin, s.Yin, s.Yout, s.Vout, s.perm, s.B, s.ldb, s.c, s.cpb);
+  const StepSeg<T>& g = segs[find_seg(segs, nseg)];
+  const int local = blockIdx.x - g.cta0;
+  sweep::step_body<T>(g.s, sm_raw, local / g.ncch, local - (local / g.ncch) * g.ncch);
 }
 
 __global__ void __launch_bounds__(kThreads)
@@ -213,84 +199,72 @@ struct SolveBufs {
   T* P[4];
 };
 
-// Builds the step tables of a grouped mode-N ULV sweep; B[i] is solved in place.
+// Step tables of a grouped sweep: the segments of every launch, back to back.
+template <typename T>
+struct StepTable {
+  std::vector<StepSeg<T>> segs;
+  std::vector<int> off, cnt;
+  std::vector<sweep::LaunchPlan> plan;
+  void add(std::vector<sweep::Step<T>>& v) {
+    if (v.empty()) return;
+    std::vector<sweep::Step<T>*> ptr;
+    for (auto& x : v) ptr.push_back(&x);
+    const sweep::LaunchPlan p = sweep::plan_steps(ptr.data(), (int)ptr.size());
+    off.push_back((int)segs.size());
+    cnt.push_back((int)v.size());
+    plan.push_back(p);
+    long long cta = 0;
+    for (auto& x : v) {
+      StepSeg<T> g{};
+      g.s = x;
+      g.ncch = (x.c + x.cpb - 1) / x.cpb;
+      g.cta0 = (int)cta;
+      cta += (long long)x.nb * x.nrch * g.ncch;
+      segs.push_back(g);
+    }
+  }
+};
+
+// Builds the step tables of a grouped mode-N ULV sweep; B[i] is solved in
+// place.  Member i runs exactly its solo sequence of steps and buffers.
 template <typename T>
 void build_solve(const std::vector<const Hbs*>& H, const std::vector<int>& c,
                  const std::vector<T*>& B, const std::vector<int>& ldb,
-                 const std::vector<SolveBufs<T>>& buf, Steps<SolveSeg<T>>& st) {
-  using F = FacPtr<T>;
+                 const std::vector<SolveBufs<T>>& buf, StepTable<T>& tab) {
   const int m = (int)H.size();
-  int maxL = 0, maxc = 1;
-  for (int i = 0; i < m; ++i) {
-    maxL = std::max(maxL, H[i]->L);
-    maxc = std::max(maxc, c[i]);
-  }
-  const bool f64 = sizeof(T) == 8;
-  const long long target = (f64 ? 2 : 1) * (long long)num_sms();
-  const int mstart = f64 ? maxc : std::min(maxc, 16), mmin = f64 ? 1 : 4;
-  const size_t e = sizeof(T);
+  int maxL = 0;
+  for (int i = 0; i < m; ++i) maxL = std::max(maxL, H[i]->L);
+  std::vector<sweep::Step<T>> v;
   for (int t = 0; t + 1 < maxL; ++t) {
-    st.begin();
+    v.clear();
     for (int i = 0; i < m; ++i) {
       if (H[i]->L < t + 2) continue;
-      const Level& l = H[i]->lv[t];
-      SolveSeg<T> s{};
-      s.kind = 0;
-      s.n = l.n; s.nu = l.nu; s.k = l.k; s.c = c[i];
-      s.Q = F::Q(l);
-      s.src = t == 0 ? B[i] : buf[i].P[(t - 1) & 1];
-      s.lds = t == 0 ? ldb[i] : c[i];
-      s.perm = t == 0 ? H[i]->perm.as<int64_t>() : nullptr;
-      s.ru = buf[i].ru + H[i]->NN[t] * c[i];
-      s.dst = buf[i].P[t & 1];
-      st.segs.push_back(s);
-      st.g.push_back({l.Nb, c[i], e * ulvk::ulv_fwd_smem(l.n, 0), e * 2 * l.n});
+      v.push_back(sweep::forward_step<T>(
+          *H[i], t, t == 0 ? B[i] : buf[i].P[(t - 1) & 1], t == 0 ? ldb[i] : c[i],
+          t == 0 ? H[i]->perm.as<int64_t>() : nullptr, buf[i].ru + H[i]->NN[t] * c[i],
+          buf[i].P[t & 1], c[i]));
     }
-    st.end(mstart, mmin, target);
+    tab.add(v);
   }
-  st.begin();
+  v.clear();
   for (int i = 0; i < m; ++i) {
     const int L = H[i]->L;
-    const Level& r = H[i]->lv[L - 1];
-    SolveSeg<T> s{};
-    s.kind = 1;
-    s.n = r.n; s.c = c[i];
-    s.Q = F::Q(r); s.R = F::R(r); s.D = F::D(r);
-    s.src = L == 1 ? B[i] : buf[i].P[(L - 2) & 1];
-    s.lds = L == 1 ? ldb[i] : c[i];
-    s.perm = L == 1 ? H[i]->perm.as<int64_t>() : nullptr;
-    s.Yout = buf[i].P[2];
-    s.Vout = buf[i].P[3];
-    s.B = B[i];
-    s.ldb = ldb[i];
-    st.segs.push_back(s);
-    st.g.push_back({1, c[i], e * ulvk::ulv_root_smem(r.n, 0, false), e * 2 * r.n});
+    v.push_back(sweep::root_step<T>(*H[i], L == 1 ? B[i] : buf[i].P[(L - 2) & 1],
+                                    L == 1 ? ldb[i] : c[i], B[i], ldb[i], buf[i].P[2],
+                                    buf[i].P[3], c[i]));
   }
-  st.end(mstart, mmin, target);
+  tab.add(v);
   for (int t = maxL - 2; t >= 0; --t) {
-    st.begin();
+    v.clear();
     for (int i = 0; i < m; ++i) {
       const int L = H[i]->L;
       if (L < t + 2) continue;
-      const Level& l = H[i]->lv[t];
       const int in = ((L - 2 - t) % 2 == 0) ? 2 : 0, out = in == 2 ? 0 : 2;
-      SolveSeg<T> s{};
-      s.kind = 2;
-      s.n = l.n; s.nu = l.nu; s.k = l.k; s.c = c[i];
-      s.ru = buf[i].ru + H[i]->NN[t] * c[i];
-      s.Uu = F::Uu(l); s.R = F::R(l); s.W = F::W(l); s.U = F::U(l); s.D = F::D(l);
-      s.Vin = buf[i].P[in + 1];
-      s.Yin = buf[i].P[in];
-      s.Yout = buf[i].P[out];
-      s.Vout = buf[i].P[out + 1];
-      s.perm = t == 0 ? H[i]->perm.as<int64_t>() : nullptr;
-      s.B = B[i];
-      s.ldb = ldb[i];
-      st.segs.push_back(s);
-      st.g.push_back({l.Nb, c[i], e * ulvk::ulv_bwd_smem(l.n, l.nu, l.k, 0, false, t == 0),
-                      e * (2 * l.k + l.nu + 2 * l.n)});
+      v.push_back(sweep::backward_step<T>(*H[i], t, buf[i].ru + H[i]->NN[t] * c[i],
+                                          buf[i].P[in + 1], buf[i].P[in], buf[i].P[out],
+                                          buf[i].P[out + 1], B[i], ldb[i], c[i]));
     }
-    st.end(mstart, mmin, target);
+    tab.add(v);
   }
 }
 
@@ -404,13 +378,13 @@ void set_smem(K kern, size_t bytes) {
 }
 
 template <typename T>
-void launch_solve(cudaStream_t st, const Steps<SolveSeg<T>>& s, const SolveSeg<T>* dsegs) {
-  auto kern = group_solve_kernel<T>;
-  for (int i = 0; i < s.nsteps(); ++i) {
-    if (s.ctas[i] == 0) continue;
-    set_smem(kern, s.smem[i]);
-    kern<<<s.ctas[i], kThreads, s.smem[i], st>>>(dsegs + s.off[i], s.count(i));
-    check_launch("group_solve_kernel");
+void launch_solve(cudaStream_t st, const StepTable<T>& tab, const StepSeg<T>* dsegs) {
+  auto kern = group_step_kernel<T>;
+  for (size_t i = 0; i < tab.plan.size(); ++i) {
+    const sweep::LaunchPlan& p = tab.plan[i];
+    if (p.ctas == 0) continue;
+    ensure_smem(reinterpret_cast<const void*>(kern), p.smem);
+    sweep::launch_pdl(kern, p, st, "group_step_kernel", dsegs + tab.off[i], tab.cnt[i]);
   }
 }
 
@@ -488,7 +462,7 @@ void hbs_solve_grouped(Handle& h, int count, Hbs* const* ops, double* const* B, 
   size_t nseg = 0;
   for (const Hbs* x : H) nseg += 2 * (size_t)x->L;
   Plan plan;
-  plan.add(blob_bound(nseg * sizeof(SolveSeg<double>), 1));
+  plan.add(blob_bound(nseg * sizeof(StepSeg<double>), 1));
   std::vector<size_t> stride(m);
   for (int i = 0; i < m; ++i) {
     stride[i] = round64((size_t)H[i]->N * cm[i]);
@@ -502,21 +476,40 @@ void hbs_solve_grouped(Handle& h, int count, Hbs* const* ops, double* const* B, 
     buf[i].ru = s;
     for (int j = 0; j < 4; ++j) buf[i].P[j] = s + (j + 1) * stride[i];
   }
-  Steps<SolveSeg<double>> steps;
+  StepTable<double> steps;
   build_solve<double>(H, cm, Bm, ldm, buf, steps);
   Blob blob;
   const size_t at = blob.put(steps.segs);
   SLU_REQUIRE(blob.host.size() <= plan.bytes[0], "task table overflow");
   upload(h, blob, dtab);
-  launch_solve<double>(st, steps, reinterpret_cast<const SolveSeg<double>*>(dtab + at));
+  launch_solve<double>(st, steps, reinterpret_cast<const StepSeg<double>*>(dtab + at));
 }
 
-void hbs_refine_grouped(Handle& h, int count, Hbs* const* ops, const double* const* B,
-                        const int* ldb, double* const* X, const int* ldx, const int* c,
-                        double tol, int maxit, int* iters, double* relres) {
-  SLU_REQUIRE(count >= 0 && (count == 0 || (ops && B && ldb && X && ldx && c)),
-              "null argument");
-  SLU_REQUIRE(maxit >= 1, "bad iteration limit");
+namespace {
+
+// Inner sweep of the grouped refinement in T (dfloat or float).
+inline void to_inner(cudaStream_t st, long long n, const double* x, dfloat* y) {
+  to_dfs_k<<<gsz(n), 256, 0, st>>>(n, x, y);
+  check_launch("to_dfs_k");
+}
+inline void to_inner(cudaStream_t st, long long n, const double* x, float* y) {
+  to_f32_k<<<gsz(n), 256, 0, st>>>(n, x, y);
+  check_launch("to_f32_k");
+}
+inline void accum_inner(cudaStream_t st, long long n, const dfloat* y, double* x, int init) {
+  accum_dfs_k<<<gsz(n), 256, 0, st>>>(n, y, x, init);
+  check_launch("accum_dfs_k");
+}
+inline void accum_inner(cudaStream_t st, long long n, const float* y, double* x, int init) {
+  accum_k<<<gsz(n), 256, 0, st>>>(n, y, x, init);
+  check_launch("accum_k");
+}
+
+template <typename T>
+void refine_grouped(Handle& h, int count, Hbs* const* ops, const double* const* B,
+                    const int* ldb, double* const* X, const int* ldx, const int* c, double tol,
+                    int maxit, int* iters, double* relres) {
+  constexpr bool kDf = sizeof(T) == 8;
   std::vector<int> idx;
   for (int i = 0; i < count; ++i) {
     SLU_REQUIRE(ops[i], "null operator");
@@ -532,7 +525,8 @@ void hbs_refine_grouped(Handle& h, int count, Hbs* const* ops, const double* con
   if (m == 0) return;
   cudaStream_t st = h.stream;
   for (int i : idx) {
-    if (!ops[i]->has_f32) hbs_make_f32(h, *ops[i]);
+    if (kDf && !ops[i]->has_dfs) hbs_make_dfs(h, *ops[i]);
+    if (!kDf && !ops[i]->has_f32) hbs_make_f32(h, *ops[i]);
     if (!ops[i]->has_df) hbs_make_df(h, *ops[i]);
   }
   std::vector<const Hbs*> H(m);
@@ -552,27 +546,27 @@ void hbs_refine_grouped(Handle& h, int count, Hbs* const* ops, const double* con
   }
   // device regions
   Plan plan;
-  const size_t tab_bytes = blob_bound(nseg * (sizeof(SolveSeg<float>) + sizeof(DfSeg)) +
+  const size_t tab_bytes = blob_bound(nseg * (sizeof(StepSeg<T>) + sizeof(DfSeg)) +
                                           (size_t)C * sizeof(ColSeg) + 2 * m * sizeof(CopySeg),
                                       5);
   plan.add(tab_bytes);
   plan.add(8 * E);  // B
   plan.add(8 * E);  // X
   plan.add(8 * E);  // r
-  plan.add(4 * E);  // f
+  plan.add(sizeof(T) * E);  // inner right-hand sides / corrections
   plan.add(16 * (size_t)C);  // [bn | rn]
-  for (int j = 0; j < m; ++j) plan.add(5 * stride[j] * sizeof(float));
+  for (int j = 0; j < m; ++j) plan.add(5 * stride[j] * sizeof(T));
   for (int j = 0; j < m; ++j) plan.add(hbs_apply_df_scratch_bytes(*H[j], cm[j]));
   h.ws.reserve(plan.total(), st);
   char* dtab = h.ws.take<char>(plan.bytes[0]);
   double* dB = h.ws.take<double>(E);
   double* dX = h.ws.take<double>(E);
   double* dr = h.ws.take<double>(E);
-  float* df = h.ws.take<float>(E);
+  T* df = h.ws.take<T>(E);
   double* norms = h.ws.take<double>(2 * (size_t)C);
-  std::vector<SolveBufs<float>> sbuf(m);
+  std::vector<SolveBufs<T>> sbuf(m);
   for (int j = 0; j < m; ++j) {
-    float* s = h.ws.take<float>(5 * stride[j]);
+    T* s = h.ws.take<T>(5 * stride[j]);
     sbuf[j].ru = s;
     for (int q = 0; q < 4; ++q) sbuf[j].P[q] = s + (q + 1) * stride[j];
   }
@@ -580,7 +574,7 @@ void hbs_refine_grouped(Handle& h, int count, Hbs* const* ops, const double* con
   for (int j = 0; j < m; ++j)
     dbuf[j] = carve_df(*H[j], cm[j], h.ws.take<char>(plan.bytes[6 + m + j]));
   // task tables
-  std::vector<float*> fB(m);
+  std::vector<T*> fB(m);
   std::vector<const double*> xX(m);
   std::vector<double*> rY(m);
   for (int j = 0; j < m; ++j) {
@@ -588,8 +582,8 @@ void hbs_refine_grouped(Handle& h, int count, Hbs* const* ops, const double* con
     xX[j] = dX + off[j];
     rY[j] = dr + off[j];
   }
-  Steps<SolveSeg<float>> ssteps;
-  build_solve<float>(H, cm, fB, cm, sbuf, ssteps);
+  StepTable<T> ssteps;
+  build_solve<T>(H, cm, fB, cm, sbuf, ssteps);
   Steps<DfSeg> dsteps;
   build_df(H, cm, xX, cm, rY, cm, dbuf, dsteps);
   std::vector<ColSeg> cols;
@@ -607,7 +601,7 @@ void hbs_refine_grouped(Handle& h, int count, Hbs* const* ops, const double* con
                a_i = blob.put(cin), a_o = blob.put(cpy_out);
   SLU_REQUIRE(blob.host.size() <= tab_bytes, "task table overflow");
   upload(h, blob, dtab);
-  const auto* d_s = reinterpret_cast<const SolveSeg<float>*>(dtab + a_s);
+  const auto* d_s = reinterpret_cast<const StepSeg<T>*>(dtab + a_s);
   const auto* d_d = reinterpret_cast<const DfSeg*>(dtab + a_d);
   const auto* d_c = reinterpret_cast<const ColSeg*>(dtab + a_c);
   const auto* d_i = reinterpret_cast<const CopySeg*>(dtab + a_i);
@@ -623,11 +617,9 @@ void hbs_refine_grouped(Handle& h, int count, Hbs* const* ops, const double* con
       SLU_CHECK_CUDA(
           cudaMemcpyAsync(host, norms, 8 * (size_t)C, cudaMemcpyDeviceToHost, st));
     }
-    to_f32_k<<<gsz(En), 256, 0, st>>>(En, first ? dB : dr, df);
-    check_launch("to_f32_k");
-    launch_solve<float>(st, ssteps, d_s);
-    accum_k<<<gsz(En), 256, 0, st>>>(En, df, dX, first ? 1 : 0);
-    check_launch("accum_k");
+    to_inner(st, En, first ? dB : dr, df);
+    launch_solve<T>(st, ssteps, d_s);
+    accum_inner(st, En, df, dX, first ? 1 : 0);
     launch_df(st, dsteps, d_d);
     resid_k<<<gsz(En), 256, 0, st>>>(En, dB, dr);
     check_launch("resid_k");
@@ -644,7 +636,7 @@ void hbs_refine_grouped(Handle& h, int count, Hbs* const* ops, const double* con
   double worst = 0.0;
   std::vector<double> member(m, 0.0);
   for (;;) {
-    if (it < 2 && it < maxit && tol < 1e-6) {  // first correction without a check
+    if (!kDf && it < 2 && it < maxit && tol < 1e-6) {  // float32: no check yet
       iteration(false);
       ++it;
       continue;
@@ -672,6 +664,21 @@ void hbs_refine_grouped(Handle& h, int count, Hbs* const* ops, const double* con
   if (relres)
     for (int j = 0; j < m; ++j) relres[idx[j]] = member[j];
   if (worst > tol) throw Error(SLU_ERR_NOT_CONVERGED, "refinement did not reach the tolerance");
+}
+
+}  // namespace
+
+void hbs_refine_grouped(Handle& h, int count, Hbs* const* ops, const double* const* B,
+                        const int* ldb, double* const* X, const int* ldx, const int* c,
+                        double tol, int maxit, int* iters, double* relres) {
+  SLU_REQUIRE(count >= 0 && (count == 0 || (ops && B && ldb && X && ldx && c)),
+              "null argument");
+  SLU_REQUIRE(maxit >= 1, "bad iteration limit");
+  // double-float inner sweeps unless every member asks for float32
+  bool f32 = count > 0;
+  for (int i = 0; i < count; ++i) f32 = f32 && ops[i] && ops[i]->refine_inner == 0;
+  if (f32) refine_grouped<float>(h, count, ops, B, ldb, X, ldx, c, tol, maxit, iters, relres);
+  else refine_grouped<dfloat>(h, count, ops, B, ldb, X, ldx, c, tol, maxit, iters, relres);
 }
 
 }  // namespace slu

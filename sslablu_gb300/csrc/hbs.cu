@@ -368,8 +368,11 @@ void hbs_compress(Handle& h, Hbs& H, int Nb0, int rk, int s, const double* Om, c
   H.has_mats = true;
   H.has_ulv = ulv;
   H.has_f32 = false;
+  H.has_dfs = false;
   H.has_df = false;
+  H.has_sweep = false;
   H.invalidate_plans();
+  if (ulv) hbs_make_sweep(h, H);
 }
 
 // ============================================================== standalone ULV
@@ -416,7 +419,9 @@ void hbs_factor(Handle& h, Hbs& H) {
   }
   H.has_ulv = true;
   H.has_f32 = false;
+  H.has_dfs = false;
   H.invalidate_plans();
+  hbs_make_sweep(h, H);
 }
 
 // ============================================================== apply
@@ -559,6 +564,7 @@ void hbs_make_f32(Handle& h, Hbs& H) {
     dst.alloc(n * 4, st);
     cast_f64_f32(st, (long long)n, src.as<double>(), dst.as<float>());
   };
+  SLU_REQUIRE(H.has_sweep, "step operators not composed");
   for (Level& l : H.lv) {
     cp(l.U, l.Uf);
     cp(l.D, l.Df);
@@ -566,6 +572,8 @@ void hbs_make_f32(Handle& h, Hbs& H) {
     cp(l.W, l.Wf);
     cp(l.R, l.Rf);
     cp(l.Uu, l.Uuf);
+    cp(l.Qt, l.Qtf);
+    cp(l.Sw, l.Swf);
   }
   H.has_f32 = true;
 }

@@ -1,6 +1,7 @@
 // HBS operator owned by the library: level factors, ULV factors, and the
 // compression / factorisation / apply / solve drivers.
 #pragma once
+#include "dfloat.cuh"
 #include "slablu_internal.cuh"
 
 namespace slu {
@@ -78,6 +79,11 @@ struct Level {
   DevBuf Uf, Df, Qf, Wf, Rf, Uuf;
   // (hi, lo) float32 pairs of U, V, D (double-float residual apply)
   DevBuf Uh, Ul, Vh, Vl, Dh, Dl;
+  // step operators of the mode-N solve (sweep_ops.cu): Qt = Q^T per block,
+  // Sw = [G; H] per block (G only on the leaves; the root: [R^-1 Q^T; D R^-1 Q^T])
+  DevBuf Qt, Sw;
+  DevBuf Qtf, Swf;     // float32 copies
+  DevBuf Qtdf, Swdf;   // double-float copies (interleaved hi/lo pairs)
 };
 
 struct RefinePlan;  // refine.cu: buffers + CUDA graphs of one refinement iteration
@@ -88,7 +94,10 @@ struct Hbs {
   DevBuf perm;                     // int64[N]
   bool identity_perm = true;
   std::vector<long long> NN;       // NNvec, L+1 entries
-  bool has_mats = false, has_ulv = false, has_f32 = false, has_df = false;
+  bool has_mats = false, has_ulv = false, has_f32 = false, has_df = false, has_dfs = false;
+  bool has_sweep = false;   // step operators composed (hbs_make_sweep)
+  // inner sweep of the mixed-precision refinement: 0 float32, 1 double-float
+  int refine_inner = 1;
   int rk = 0, nsamples = 0;
   // null space of a sketch block's Om^T used by compression: false takes the
   // last n columns of the complete Q (HBSnew.compute_UV), true every column
@@ -162,6 +171,14 @@ size_t hbs_apply_scratch_elems(const Hbs& H, int c);
 void hbs_apply_fused(cudaStream_t st, const Hbs& H, bool trans, const double* X, int ldx,
                      double* Y, int ldy, int c, double* scratch);
 void hbs_make_f32(Handle& h, Hbs& H);
+// Composes the step operators of the mode-N solve from the ULV factors.
+void hbs_make_sweep(Handle& h, Hbs& H);
+// Double-float copies of the step operators (dfloat ULV sweep).
+void hbs_make_dfs(Handle& h, Hbs& H);
+// B (N x c float64, caller ordering) <- A^{-1} B with the double-float sweep;
+// scratch of hbs_solve_df_scratch_bytes() bytes.
+size_t hbs_solve_df_scratch_bytes(const Hbs& H, int c);
+void hbs_solve_df(cudaStream_t st, const Hbs& H, double* B, int ldb, int c, void* scratch);
 // Mixed-precision refinement replayed as CUDA graphs (refine.cu).
 void hbs_refine(Handle& h, Hbs& H, const double* B, int ldb, double* X, int ldx, int c,
                 double tol, int maxit, int* iters, double* relres);
@@ -184,6 +201,8 @@ struct FacPtr<double> {
   static const double* W(const Level& l) { return l.W.as<double>(); }
   static const double* R(const Level& l) { return l.R.as<double>(); }
   static const double* Uu(const Level& l) { return l.Uu.as<double>(); }
+  static const double* Qt(const Level& l) { return l.Qt.as<double>(); }
+  static const double* Sw(const Level& l) { return l.Sw.as<double>(); }
 };
 template <>
 struct FacPtr<float> {
@@ -193,6 +212,14 @@ struct FacPtr<float> {
   static const float* W(const Level& l) { return l.Wf.as<float>(); }
   static const float* R(const Level& l) { return l.Rf.as<float>(); }
   static const float* Uu(const Level& l) { return l.Uuf.as<float>(); }
+  static const float* Qt(const Level& l) { return l.Qtf.as<float>(); }
+  static const float* Sw(const Level& l) { return l.Swf.as<float>(); }
+};
+
+template <>
+struct FacPtr<dfloat> {
+  static const dfloat* Qt(const Level& l) { return l.Qtdf.as<dfloat>(); }
+  static const dfloat* Sw(const Level& l) { return l.Swdf.as<dfloat>(); }
 };
 
 // Grouped solves over many operators (group.cu): one launch per tree step for

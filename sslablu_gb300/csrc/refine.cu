@@ -1,15 +1,18 @@
 // Mixed-precision refinement of the HBS solve, replayed as CUDA graphs.
 //
-//   x0 = float32 ULV solve of b;  r = b - A x  (double-float apply)
-//   x += float32 ULV solve of r;  r = b - A x  ...
-// until ||r_j|| / ||b_j|| <= tol for every column j.
+//   x0 = inner ULV solve of b;  r = b - A x  (double-float apply)
+//   x += inner ULV solve of r;  r = b - A x  ...
+// until ||r_j|| / ||b_j|| <= tol for every column j.  The inner sweep runs on
+// the float32 pipe: either in double-float arithmetic (the default; ~1e-14
+// relative, so one iteration usually reaches the tolerance) or in plain
+// float32 (two or three iterations).
 //
-// One refinement iteration (cast, float32 fused ULV sweep, correction, double-
+// One refinement iteration (cast, inner fused ULV sweep, correction, double-
 // float residual, column norms, device-to-host copy of the norms) is captured
 // once per (operator, nrhs) into a CUDA graph over buffers that the plan owns,
-// and replayed; the host looks at the norms only from the second correction on
-// (a float32 solve alone never reaches a float64 tolerance), so a typical
-// refinement is two or three graph launches and one or two synchronisations.
+// and replayed.  With the float32 inner sweep the host looks at the norms only
+// from the second correction on (a float32 solve alone never reaches a
+// float64 tolerance).
 #include <cmath>
 
 #include "abi_types.cuh"
@@ -19,7 +22,8 @@ namespace slu {
 
 struct RefinePlan {
   int c = 0;
-  DevBuf B, X, r, f, bn, rn, solve_ws, df_ws;
+  int inner = 0;   // 0 float32 sweep (f), 1 double-float sweep (d)
+  DevBuf B, X, r, f, d, bn, rn, solve_ws, df_ws;
   double* host_norms = nullptr;   // pinned: [bn (c) | rn (c)]
   cudaGraphExec_t first = nullptr, next = nullptr;
   long long first_kernels = 0, next_kernels = 0;   // kernel nodes per graph
@@ -38,19 +42,29 @@ void enqueue_iteration(cudaStream_t st, const Hbs& H, RefinePlan& P, bool first)
   double* B = P.B.as<double>();
   double* X = P.X.as<double>();
   double* r = P.r.as<double>();
-  float* f = P.f.as<float>();
   if (first) {
     colnorm2_k<<<c, 256, 0, st>>>(N, c, B, c, P.bn.as<double>());
     check_launch("colnorm2_k");
     SLU_CHECK_CUDA(cudaMemcpyAsync(P.host_norms, P.bn.p, 8 * c, cudaMemcpyDeviceToHost, st));
-    to_f32_k<<<gsz(n), 256, 0, st>>>(n, B, f);
-  } else {
-    to_f32_k<<<gsz(n), 256, 0, st>>>(n, r, f);
   }
-  check_launch("to_f32_k");
-  hbs_solve_scratch<float>(st, H, false, f, c, c, P.solve_ws.as<float>());
-  accum_k<<<gsz(n), 256, 0, st>>>(n, f, X, first ? 1 : 0);
-  check_launch("accum_k");
+  const double* rhs = first ? B : r;
+  if (P.inner == 1) {
+    dfloat* d = P.d.as<dfloat>();
+    to_dfs_k<<<gsz(n), 256, 0, st>>>(n, rhs, d);
+    check_launch("to_dfs_k");
+    const size_t stride =
+        ((sizeof(dfloat) * (size_t)N * c + 255) & ~size_t(255)) / sizeof(dfloat);
+    ulv_solve_fused<dfloat>(st, H, d, c, c, P.solve_ws.as<dfloat>(), stride);
+    accum_dfs_k<<<gsz(n), 256, 0, st>>>(n, d, X, first ? 1 : 0);
+    check_launch("accum_dfs_k");
+  } else {
+    float* f = P.f.as<float>();
+    to_f32_k<<<gsz(n), 256, 0, st>>>(n, rhs, f);
+    check_launch("to_f32_k");
+    hbs_solve_scratch<float>(st, H, false, f, c, c, P.solve_ws.as<float>());
+    accum_k<<<gsz(n), 256, 0, st>>>(n, f, X, first ? 1 : 0);
+    check_launch("accum_k");
+  }
   hbs_apply_df(st, H, X, c, r, c, c, P.df_ws.p);
   resid_k<<<gsz(n), 256, 0, st>>>(n, B, r);
   check_launch("resid_k");
@@ -90,14 +104,16 @@ RefinePlan& plan_for(Handle& h, Hbs& H, int c) {
   cudaStream_t st = h.stream;
   auto P = std::make_shared<RefinePlan>();
   P->c = c;
+  P->inner = H.refine_inner;
   const size_t n = (size_t)H.N * c;
   P->B.alloc(8 * n, st);
   P->X.alloc(8 * n, st);
   P->r.alloc(8 * n, st);
-  P->f.alloc(4 * n, st);
+  if (P->inner == 1) P->d.alloc(8 * n, st);
+  else P->f.alloc(4 * n, st);
   P->bn.alloc(8 * (size_t)c, st);
   P->rn.alloc(8 * (size_t)c, st);
-  P->solve_ws.alloc(hbs_solve_scratch_bytes(H, c, sizeof(float)), st);
+  P->solve_ws.alloc(hbs_solve_scratch_bytes(H, c, P->inner == 1 ? 8 : 4), st);
   P->df_ws.alloc(hbs_apply_df_scratch_bytes(H, c), st);
   SLU_CHECK_CUDA(cudaMallocHost(&P->host_norms, 16 * (size_t)c));
   SLU_CHECK_CUDA(cudaStreamSynchronize(st));
@@ -127,7 +143,8 @@ RefinePlan& plan_for(Handle& h, Hbs& H, int c) {
 void hbs_refine(Handle& h, Hbs& H, const double* B, int ldb, double* X, int ldx, int c,
                 double tol, int maxit, int* iters, double* relres) {
   cudaStream_t st = h.stream;
-  if (!H.has_f32) hbs_make_f32(h, H);
+  if (H.refine_inner == 1 && !H.has_dfs) hbs_make_dfs(h, H);
+  if (H.refine_inner == 0 && !H.has_f32) hbs_make_f32(h, H);
   if (!H.has_df) hbs_make_df(h, H);
   RefinePlan& P = plan_for(h, H, c);
   SLU_CHECK_CUDA(cudaMemcpy2DAsync(P.B.p, 8 * (size_t)c, B, 8 * (size_t)ldb, 8 * (size_t)c,
@@ -137,7 +154,7 @@ void hbs_refine(Handle& h, Hbs& H, const double* B, int ldb, double* X, int ldx,
   int it = 1;
   double worst = 0.0;
   for (;;) {
-    if (it < 2 && it < maxit && tol < 1e-6) {  // first correction without a check
+    if (P.inner == 0 && it < 2 && it < maxit && tol < 1e-6) {  // float32: no check yet
       SLU_CHECK_CUDA(cudaGraphLaunch(P.next, st));
       count_launches(P.next_kernels);
       ++it;

@@ -2,6 +2,8 @@
 // shared by the per-operator (refine.cu) and grouped (group.cu) loops.
 #pragma once
 
+#include "dfloat.cuh"
+
 namespace slu {
 namespace {
 
@@ -36,6 +38,23 @@ __global__ void accum_k(long long n, const float* __restrict__ f, double* __rest
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
        e += (long long)gridDim.x * blockDim.x)
     x[e] = init ? (double)f[e] : x[e] + (double)f[e];
+}
+
+// d = (double-float) src
+__global__ void to_dfs_k(long long n, const double* __restrict__ src, dfloat* __restrict__ d) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+       e += (long long)gridDim.x * blockDim.x)
+    d[e] = to_dfloat(src[e]);
+}
+
+// x = d (init) or x += d
+__global__ void accum_dfs_k(long long n, const dfloat* __restrict__ d, double* __restrict__ x,
+                            int init) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+       e += (long long)gridDim.x * blockDim.x) {
+    const double v = to_double(d[e]);
+    x[e] = init ? v : x[e] + v;
+  }
 }
 
 // r = b - r

@@ -324,10 +324,26 @@ class HBSMAT:
         return dv.finish(self._dev_solve(X, mode == "T"), b, one)
 
     # ------------------------------------------------------------ mixed precision
-    def solve_refined(self, b, tol=1e-10, maxit=10):
-        """Mixed-precision solve: float32 ULV sweeps corrected by float64
-        residuals of this operator until ||b - A x|| / ||b|| <= tol per
-        column.  Returns (x, iterations, worst relative residual)."""
+    def solve_dfloat(self, b):
+        """Mode-N solve in double-float arithmetic on the float32 units (the
+        fused sweep of solve(), every factor a float32 pair hi + lo): about
+        1e-14 relative accuracy without refinement."""
+        X, one = dv.prepare_rhs(b)
+        B = dv.as_2d(X).clone().contiguous()
+        L.check(L.lib().slu_ulv_solve_dfloat(L.handle(), self._op, L.ptr(B), B.shape[1],
+                                             B.shape[1]))
+        return dv.finish(B, b, one)
+
+    def solve_refined(self, b, tol=1e-10, maxit=10, inner="dfloat"):
+        """Mixed-precision solve: ULV sweeps on the float32 units
+        (``inner='dfloat'``: double-float, usually one iteration;
+        ``'float32'``: plain float32, two or three) corrected by float64-
+        accurate residuals of this operator until ||b - A x|| / ||b|| <= tol
+        per column.  Returns (x, iterations, worst relative residual)."""
+        modes = {"float32": 0, "dfloat": 1}
+        if inner not in modes:
+            raise ValueError("inner must be 'dfloat' or 'float32'")
+        L.check(L.lib().slu_hbs_set_refine_inner(self._op, modes[inner]))
         B, one = dv.prepare_rhs(b)
         X = torch.empty_like(B)
         it = ctypes.c_int()

@@ -17,9 +17,10 @@ solve: the float64 ULV solve (mode N) of a synthetic exact HBS operator of
 size m (leaf 64, rank 32, ULV from the given factors) with n right-hand
 sides, two ways: per-level launches (slu_ulv_solve) and the grouped sweep of
 a one-member group; prints the median time per solve of each.
-refine: float64 ULV solve against mixed-precision refinement to 1e-10
-(float32 sweeps + double-float residuals) on the same operator, for 16, 64,
-256 and 1024 right-hand sides; prints both times and the ratio.
+refine: float64 ULV solve against the double-float sweep alone and against
+mixed-precision refinement to 1e-10 with double-float and with float32 inner
+sweeps (double-float residuals) on the same operator, for 16, 64, 256 and
+1024 right-hand sides; prints the times, iterations and ratios.
 compress: HBSMAT.construct(32, compute_ULV=True) of a synthetic exact HBS
 operator of size m (leaf 64, rank 32, singular values 1 -> 1e-12), the
 sketches sampled through the resident operator; prints the median time and
@@ -162,10 +163,19 @@ def refine(a):
     for c in (16, 64, 256, 1024):
         B = torch.from_numpy(np.random.default_rng(c).standard_normal((N, c))).cuda()
         t64 = timed(lambda: H._dev_solve(B, False))
-        res = {}
-        tmx = timed(lambda: res.update(r=H.solve_refined(B, tol=1e-10)))
-        out["c%d" % c] = {"f64_ms": 1e3 * t64, "mixed_ms": 1e3 * tmx, "mixed_speedup": t64 / tmx,
-                          "iters": res["r"][1], "relres": res["r"][2]}
+        x64 = H._dev_solve(B, False)
+        tdf = timed(lambda: H.solve_dfloat(B))
+        xdf = H.solve_dfloat(B)
+        row = {"f64_ms": 1e3 * t64, "dfloat_ms": 1e3 * tdf, "dfloat_speedup": t64 / tdf,
+               "dfloat_vs_f64": float(torch.linalg.norm(xdf - x64) / torch.linalg.norm(x64))}
+        for inner in ("dfloat", "float32"):
+            res = {}
+            tmx = timed(lambda: res.update(r=H.solve_refined(B, tol=1e-10, inner=inner)))
+            row["mixed_%s_ms" % inner] = 1e3 * tmx
+            row["mixed_%s_speedup" % inner] = t64 / tmx
+            row["mixed_%s_iters" % inner] = res["r"][1]
+            row["mixed_%s_relres" % inner] = res["r"][2]
+        out["c%d" % c] = row
     print(json.dumps(out))
 
 

@@ -96,16 +96,55 @@ def test_construct_factors_match(golden):
             assert np.abs(Pg - Pr).max() < 1e-11
 
 
-def test_mixed_refinement_reaches_tolerance(golden):
-    """float32 ULV sweeps + double-float residuals reach 1e-10 (checked with the
-    float64 apply) and agree with the float64 solve."""
+@pytest.mark.parametrize("inner", ["dfloat", "float32"])
+def test_mixed_refinement_reaches_tolerance(golden, inner):
+    """ULV sweeps on the float32 units + double-float residuals reach 1e-10
+    (checked with the float64 apply) and agree with the float64 solve: one
+    iteration with the double-float sweep, two or more with float32."""
     need_gpu()
     g = golden("hbs_c2_n512")
     S, Nbvec = hbs_from_fixture(g)
     G = _gpu_hbs_from_oracle(S, Nbvec, 2)
     G.compute_ULV()
     x = g["x"]
-    xm, iters, rr = G.solve_refined(x, tol=1e-10, maxit=10)
-    assert rr <= 1e-10 and iters >= 2
+    xm, iters, rr = G.solve_refined(x, tol=1e-10, maxit=10, inner=inner)
+    assert rr <= 1e-10
+    assert iters == 1 if inner == "dfloat" else iters >= 2
     assert relerr(G.matmat(xm), x) <= 1e-10
     assert relerr(xm, G.solve(x)) < 1e-9
+
+
+def test_dfloat_solve_matches_float64(golden):
+    """The double-float sweep (float32 pairs, 48-bit significands) against
+    the float64 sweep and the oracle's solution of the golden C2 operator:
+    within 1e-12 relative (the operator's condition number times 2^-47)."""
+    need_gpu()
+    g = golden("hbs_c2_n512")
+    S, Nbvec = hbs_from_fixture(g)
+    G = _gpu_hbs_from_oracle(S, Nbvec, 2)
+    G.compute_ULV()
+    x = g["x"]
+    xd = G.solve_dfloat(x)
+    assert relerr(xd, G.solve(x)) < 1e-12
+    assert relerr(G.matmat(xd), x) < 1e-12
+    x1 = G.solve_dfloat(x[:, 0])
+    assert x1.ndim == 1 and relerr(x1, G.solve(x[:, 0])) < 1e-12
+
+
+@pytest.mark.parametrize("k", [16, 33, 48])
+def test_dfloat_solve_uneven_ranks_and_chunks(k):
+    """Uneven ranks (odd pitches, the one-batch prefetch variants on small
+    levels) and right-hand-side counts that split into ragged column chunks."""
+    need_gpu()
+    from sslablu_gb300.matAssembly.HBS.HBSnew import HBSMAT
+    from sslablu_gb300.synthetic import random_hbs_factors
+    for N, c in ((128, 1), (256, 7), (512, 300)):
+        Lv = int(np.log2(N // 64)) + 1
+        U, D, V, Nbvec = random_hbs_factors(k, 64, Lv, quad=False,
+                                            rng=np.random.default_rng(N + k), shift=16.0)
+        H = HBSMAT().set_mats(U, D, V, list(Nbvec), fac=2)
+        H.compute_ULV()
+        b = np.random.default_rng(k + c).standard_normal((N, c))
+        xd = H.solve_dfloat(b)
+        assert relerr(xd, H.solve(b)) < 1e-12, (N, k, c)
+        assert relerr(H.matmat(xd), b) < 1e-12, (N, k, c)
