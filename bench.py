@@ -10,11 +10,15 @@ the timed region (factor time reported separately).
 
 A step is one batch of 16 right-hand sides ~ N(0, 1) solved to a relative
 residual <= 1e-10 against the stored float64 HBS operator:
-  plain : float64 ULV solve (slu_ulv_solve)
-  mixed : float32 ULV solves + float64 residual refinement (slu_refine)
-`value` is the plain float64 path's RHS solves/s; the mixed path is reported
-beside it under "mixed".  Inputs (factors ~ 20 MB) fit in L2, so L2 is
-flushed (a 256 MB write) before every timed step, outside the timed events.
+  plain  : float64 ULV solve (slu_ulv_solve)
+  mixed  : ULV sweeps on the float32 units (double-float arithmetic) refined
+           against a float64-accurate residual until every column reaches
+           1e-10, the residual check inside every step (slu_refine)
+  dfloat : the double-float ULV sweep alone (slu_ulv_solve_dfloat), its
+           residual checked after the timed region as for plain
+`value` is the plain float64 path's RHS solves/s; the other arms are reported
+beside it.  Inputs (factors ~ 20 MB) fit in L2, so L2 is flushed (a 256 MB
+write) before every timed step, outside the timed events.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -171,10 +175,12 @@ def run_reference(args, rank, world):
 
 
 # ---------------------------------------------------------------- roofline
-# DRAM bytes (read + written) per launch of each solve kernel, averaged over
-# the launches of that kernel in the ncu launch list of
-# `python bench.py --steps 2 --warmup 3` (profiles/ulv_solve_c2_launches.txt).
-NCU_TRAFFIC = {}
+# DRAM bytes (read + written) per launch of each solve step group, averaged
+# over the group's launches in the ncu launch list of
+# `python bench.py --steps 2 --warmup 3` (profiles/ulv_step_c2_launches.txt).
+NCU_TRAFFIC = {"step_kernel<double> (backward)": 1864917,
+               "step_kernel<double> (forward)": 926635,
+               "step_kernel<double> (root)": 134400}
 FP64_NOMINAL_TFLOPS = 1.25   # GB300 float64 (no measured figure in the peaks file)
 
 
@@ -285,7 +291,7 @@ def run_gpu(args, rank, world):
     H.construct(RANK, True)
     torch.cuda.synchronize()
     t_factor = time.perf_counter() - t0
-    H.solve_refined(rhs[:, :1], tol=TOL, maxit=10)   # prepares float32 factors
+    H.solve_refined(rhs[:, :1], tol=TOL, maxit=10)   # prepares the double-float factors
     torch.cuda.synchronize()
 
     B = torch.from_numpy(rhs).cuda()
@@ -297,6 +303,9 @@ def run_gpu(args, rank, world):
 
     def mixed_step():
         return H.solve_refined(B, tol=TOL, maxit=10)
+
+    def dfloat_step():
+        return H.solve_dfloat(B)
 
     def residual(X):
         R = B - H._dev_apply(X, False)
@@ -330,6 +339,7 @@ def run_gpu(args, rank, world):
     clocks.start()
     ts_plain, launches_plain, Xp = timed(plain_step, args.steps, args.warmup)
     ts_mixed, launches_mixed, mixed_out = timed(mixed_step, args.steps, args.warmup)
+    ts_df, launches_df, Xd = timed(dfloat_step, args.steps, args.warmup)
     # end-to-end through the public API: pinned host -> device -> solve -> host
     hp = torch.from_numpy(rhs).pin_memory()
     out_h = torch.empty_like(hp).pin_memory()
@@ -349,10 +359,9 @@ def run_gpu(args, rank, world):
     res_plain = residual(Xp)
     Xm, iters, relres = mixed_out
     res_mixed = residual(Xm)
-    tot_plain = sum(ts_plain)
-    tot_mixed = sum(ts_mixed)
-    tot_plain, tot_mixed, tot_e2e = max_over_ranks([tot_plain, tot_mixed, sum(e2e)], world,
-                                                   "cuda")
+    res_df = residual(Xd)
+    tot_plain, tot_mixed, tot_df, tot_e2e = max_over_ranks(
+        [sum(ts_plain), sum(ts_mixed), sum(ts_df), sum(e2e)], world, "cuda")
     value = replica_throughput(world, NRHS * args.steps, tot_plain)
     p50 = statistics.median(ts_plain)
     hbm, src = peaks()
@@ -370,12 +379,18 @@ def run_gpu(args, rank, world):
             "p50_ms": 1e3 * p50, "p99_ms": 1e3 * float(np.percentile(ts_plain, 99)),
             "relres": res_plain,
             "mixed": {"value": world * NRHS * args.steps / tot_mixed, "unit": UNIT,
-                      "dtype": "f32 solve + f64 residual refinement",
+                      "dtype": "double-float (f32 pairs) ULV sweep + f64-accurate residual "
+                               "refinement to 1e-10",
                       "p50_ms": 1e3 * statistics.median(ts_mixed),
                       "p99_ms": 1e3 * float(np.percentile(ts_mixed, 99)),
                       "iters": iters, "relres": res_mixed,
                       "speedup_vs_plain": tot_plain / tot_mixed,
                       "gpu_launches": launches_mixed},
+            "dfloat": {"value": world * NRHS * args.steps / tot_df, "unit": UNIT,
+                       "dtype": "double-float (f32 pairs) ULV sweep, no refinement",
+                       "p50_ms": 1e3 * statistics.median(ts_df),
+                       "p99_ms": 1e3 * float(np.percentile(ts_df, 99)), "relres": res_df,
+                       "speedup_vs_plain": tot_plain / tot_df, "gpu_launches": launches_df},
             "e2e": {"value": world * NRHS * args.steps / tot_e2e, "unit": UNIT,
                     "h2d_bytes_per_step": int(rhs.nbytes), "d2h_bytes_per_step": int(rhs.nbytes),
                     "p50_ms": 1e3 * statistics.median(e2e)},

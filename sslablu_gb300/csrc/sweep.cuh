@@ -47,11 +47,18 @@ struct Step {
 };
 
 // Lanes per dot product: each sums every ks-th term of its row, then a
-// butterfly of shuffles adds the ks partial sums.  Depends only on the dot
-// product length, so the summation order of an output does not depend on the
-// right-hand-side count or on the chunking.
+// butterfly of shuffles adds the ks partial sums.  Depends only on the
+// element type and the dot product length, so the summation order of an
+// output does not depend on the right-hand-side count or on the chunking.
+// float64: two lanes (the butterfly's adds run on the FP64 pipe, which
+// bounds the large levels); float32 and double-float: four.
+template <typename T>
 __host__ __device__ inline int split_for(int w) {
-  return w >= 64 ? 8 : (w >= 32 ? 4 : (w >= 8 ? 2 : 1));
+  return w >= 32 ? 4 : (w >= 8 ? 2 : 1);
+}
+template <>
+__host__ __device__ inline int split_for<double>(int w) {
+  return w >= 16 ? 2 : 1;
 }
 
 // Pitch of the transposed z tile (zT[cc][j]): congruent to ks modulo the
@@ -118,14 +125,19 @@ __device__ __forceinline__ void copy_contig(T* dst, const T* src, size_t count) 
 }
 
 // Products of R interleaved items per thread (independent accumulation
-// chains): item t -> output (i, cc), lane part t % ks.
-template <typename T, int R>
-__device__ __forceinline__ void product(const Step<T>& s, const T* Ss, const T* zT, int pz,
-                                        int ks, int b, int r0, int nr, int c0, int nc) {
-  const int w = s.w, items = nr * nc * ks, lane = threadIdx.x & 31;
-  const int lks = ks == 8 ? 3 : (ks == 4 ? 2 : (ks == 2 ? 1 : 0));
+// chains): item t -> output (i, cc), lane part t % KS.  The full-width case
+// (all R items of the warp present) runs without per-item guards.
+template <typename T, int R, int KS>
+__device__ __forceinline__ void product(const Step<T>& s, const T* Ss, const T* zT, int pz, int b,
+                                        int r0, int nr, int c0, int nc) {
+  constexpr int LKS = KS == 8 ? 3 : (KS == 4 ? 2 : (KS == 2 ? 1 : 0));
+  const int w = s.w, items = nr * nc * KS, lane = threadIdx.x & 31;
+  const int part = lane & (KS - 1);
+  const int nterm = (w - part + KS - 1) / KS;
   const int stride = blockDim.x;
   for (int base = threadIdx.x - lane; base < items; base += R * stride) {
+    const T* sp[R];
+    const T* zp[R];
     int i[R], cc[R];
     bool on[R];
     int nact = 0;
@@ -133,26 +145,35 @@ __device__ __forceinline__ void product(const Step<T>& s, const T* Ss, const T* 
     for (int r = 0; r < R; ++r) {
       const int t = base + r * stride + lane;
       on[r] = t < items;
-      const int e = t >> lks;
+      const int e = t >> LKS;
       const int ii = on[r] ? e / nc : 0;
       i[r] = ii;
       cc[r] = on[r] ? e - ii * nc : 0;
+      sp[r] = Ss + ii * w + part;
+      zp[r] = zT + cc[r] * pz + part;
       if (base + r * stride < items) nact = r + 1;   // warp-uniform
     }
-    const int part = (base + lane) & (ks - 1);
     T acc[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) acc[r] = T(0);
-#pragma unroll 2
-    for (int j = part; j < w; j += ks) {
+    if (nact == R) {
+#pragma unroll 4
+      for (int m = 0; m < nterm; ++m) {
 #pragma unroll
-      for (int r = 0; r < R; ++r)
-        if (r < nact) acc[r] = fma(Ss[i[r] * w + j], zT[cc[r] * pz + j], acc[r]);
+        for (int r = 0; r < R; ++r) acc[r] = fma(sp[r][m * KS], zp[r][m * KS], acc[r]);
+      }
+    } else {
+      for (int m = 0; m < nterm; ++m) {
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+          if (r < nact) acc[r] = fma(sp[r][m * KS], zp[r][m * KS], acc[r]);
+      }
     }
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       if (r < nact) {
-        for (int o = ks >> 1; o > 0; o >>= 1) acc[r] += __shfl_xor_sync(0xffffffffu, acc[r], o);
+#pragma unroll
+        for (int o = KS >> 1; o > 0; o >>= 1) acc[r] += __shfl_xor_sync(0xffffffffu, acc[r], o);
         if (on[r] && part == 0) {
           const int row = r0 + i[r];
           const int col = c0 + cc[r];
@@ -170,6 +191,15 @@ __device__ __forceinline__ void product(const Step<T>& s, const T* Ss, const T* 
   }
 }
 
+template <typename T, int KS>
+__device__ __forceinline__ void product_ks(const Step<T>& s, const T* Ss, const T* zT, int pz,
+                                           int b, int r0, int nr, int c0, int nc) {
+  const int per = (nr * nc * KS + blockDim.x - 1) / blockDim.x;
+  if (per >= 4) product<T, 4, KS>(s, Ss, zT, pz, b, r0, nr, c0, nc);
+  else if (per >= 2) product<T, 2, KS>(s, Ss, zT, pz, b, r0, nr, c0, nc);
+  else product<T, 1, KS>(s, Ss, zT, pz, b, r0, nr, c0, nc);
+}
+
 // CTA (xb, cy) of a step: block b = xb / nrch, row slice xb % nrch, column
 // chunk cy.
 template <typename T>
@@ -179,7 +209,7 @@ __device__ __forceinline__ void step_body(const Step<T>& s, unsigned char* sm_ra
   const int nr = min(s.rch, s.rows - r0);
   const int c0 = cy * s.cpb, nc = min(s.cpb, s.c - c0);
   if (nr <= 0 || nc <= 0) return;   // uniform over the CTA
-  const int w = s.w, ks = split_for(w), pz = z_pitch(w, ks, (int)sizeof(T));
+  const int w = s.w, ks = split_for<T>(w), pz = z_pitch(w, ks, (int)sizeof(T));
   T* Ss = reinterpret_cast<T*>(sm_raw);      // nr x w (rows r0.. of S_b)
   T* zT = Ss + (size_t)s.rch * w;            // nc x pz, zT[cc][j] = z[j][c0 + cc]
   // the block operator is constant: its copy starts before the wait for the
@@ -206,10 +236,9 @@ __device__ __forceinline__ void step_body(const Step<T>& s, unsigned char* sm_ra
   __syncthreads();
   // inputs staged: the next launch may start its own operator copies
   launch_dependents();
-  const int per = (nr * nc * ks + blockDim.x - 1) / blockDim.x;
-  if (per >= 4) product<T, 4>(s, Ss, zT, pz, ks, b, r0, nr, c0, nc);
-  else if (per >= 2) product<T, 2>(s, Ss, zT, pz, ks, b, r0, nr, c0, nc);
-  else product<T, 1>(s, Ss, zT, pz, ks, b, r0, nr, c0, nc);
+  if (ks == 4) product_ks<T, 4>(s, Ss, zT, pz, b, r0, nr, c0, nc);
+  else if (ks == 2) product_ks<T, 2>(s, Ss, zT, pz, b, r0, nr, c0, nc);
+  else product_ks<T, 1>(s, Ss, zT, pz, b, r0, nr, c0, nc);
 }
 
 }  // namespace sweep

@@ -163,7 +163,7 @@ LaunchPlan plan_steps(Step<T>* const* steps, int count) {
   for (int i = 0; i < count; ++i) {
     Step<T>& s = *steps[i];
     const bool wh = whole(&s);
-    const int ks = split_for(s.w);
+    const int ks = split_for<T>(s.w);
     int rch = wh ? s.rows : std::min(s.rows, rmax);
     int cpb = std::min(s.c, cmax);
     auto bytes = [&] { return sizeof(T) * step_smem_elems<T>(rch, s.w, cpb, ks); };

@@ -16,7 +16,8 @@ the effective rate (2 m n k).
 solve: the float64 ULV solve (mode N) of a synthetic exact HBS operator of
 size m (leaf 64, rank 32, ULV from the given factors) with n right-hand
 sides, two ways: per-level launches (slu_ulv_solve) and the grouped sweep of
-a one-member group; prints the median time per solve of each.
+a one-member group; prints the median time per solve of each.  With
+--precision dfloat: the double-float sweep (slu_ulv_solve_dfloat) instead.
 refine: float64 ULV solve against the double-float sweep alone and against
 mixed-precision refinement to 1e-10 with double-float and with float32 inner
 sweeps (double-float residuals) on the same operator, for 16, 64, 256 and
@@ -44,6 +45,8 @@ def main():
     ap.add_argument("--k", type=int, default=4096)
     ap.add_argument("--reps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--precision", default="f64", choices=["f64", "dfloat"],
+                    help="solve: float64 (per-level and grouped) or the double-float sweep")
     a = ap.parse_args()
     if a.kernel == "compress":
         return compress(a)
@@ -114,9 +117,14 @@ def solve(a):
     def grouped():
         _lib.check(L.slu_ulv_solve_grouped(h, 1, ops, bp, ld, ld))
 
+    def dfloat():
+        _lib.check(L.slu_ulv_solve_dfloat(h, H._op, _lib.ptr(W), c, c))
+
     out = {"kernel": "solve", "N": N, "nrhs": c, "levels": Lv}
     st = torch.cuda.current_stream()
-    for name, run in (("per_level", per_level), ("grouped", grouped)):
+    arms = {"f64": (("per_level", per_level), ("grouped", grouped)),
+            "dfloat": (("dfloat", dfloat),)}[a.precision]
+    for name, run in arms:
         for _ in range(a.warmup):
             run()
         torch.cuda.synchronize()
