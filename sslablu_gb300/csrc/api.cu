@@ -185,6 +185,7 @@ int slu_hbs_set_level(slu_handle_t h, slu_hbs_t op, int level, int Nb, int n, in
       H.has_f32 = false;
       H.has_dfs = false;
       H.has_df = false;
+      H.has_apply[0] = H.has_apply[1] = false;
       H.invalidate_plans();
     }
   });

@@ -9,7 +9,7 @@
 // task table lists, per segment, the member's factors, buffers and column
 // chunking, and the CTA range it owns; a CTA finds its segment by binary
 // search over the range starts and runs the same device body as the
-// per-operator kernel (sweep.cuh, df_bodies.cuh).  The schedule is
+// per-operator kernel (sweep.cuh).  The schedule is
 //   forward  t = 0 .. maxL-2   (members with L_i >= t + 2)
 //   root                         (every member)
 //   backward t = maxL-2 .. 0   (members with L_i >= t + 2)
@@ -19,13 +19,12 @@
 // Mixed-precision refinement of a group (hbs_refine_grouped) runs the same
 // loop as refine.cu over concatenated buffers: one launch per elementwise step
 // for the whole group, the grouped inner sweep (double-float, or float32 when
-// every member asks for it), the grouped double-float apply, and segmented
-// column norms.
+// every member asks for it), the grouped double-float apply (the apply steps
+// of hbs_apply.cu on float32 pairs), and segmented column norms.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
 
-#include "df_bodies.cuh"
 #include "hbs.cuh"
 #include "refine_kernels.cuh"
 #include "sweep_host.cuh"
@@ -33,29 +32,12 @@
 namespace slu {
 namespace {
 
-constexpr int kThreads = 256;
-constexpr size_t kSmemLimit = 200 * 1024;
-
-using dfk::DF;
-
 // One tree step of one member in a grouped ULV sweep: its step (sweep.cuh),
 // the first CTA of its range and its column chunks per row slice.
 template <typename T>
 struct StepSeg {
   sweep::Step<T> s;
   int cta0, ncch;
-};
-
-// One tree step of one member in a grouped double-float apply.
-struct DfSeg {
-  int kind;  // 0 upward, 1 root or downward
-  int n, k, c, cpb, nchunk, cta0, ldx, ldy;
-  const float *Fh, *Fl, *Dh, *Dl;  // upward: V; downward: U (Fh/Fl) and D
-  const DF *in, *uin, *vv;
-  const double* X;
-  const int64_t* perm;
-  DF* out;
-  double* Y;
 };
 
 struct ColSeg {  // one right-hand-side column of a concatenated buffer
@@ -90,23 +72,6 @@ group_step_kernel(const StepSeg<T>* __restrict__ segs, int nseg) {
   sweep::step_body<T>(g.s, sm_raw, local / g.ncch, local - (local / g.ncch) * g.ncch);
 }
 
-__global__ void __launch_bounds__(kThreads)
-group_df_kernel(const DfSeg* __restrict__ segs, int nseg) {
-  extern __shared__ __align__(16) float smf[];
-  const DfSeg& s = segs[find_seg(segs, nseg)];
-  const int local = blockIdx.x - s.cta0;
-  const int b = local / s.nchunk;
-  const int c0 = (local - b * s.nchunk) * s.cpb;
-  const int nc = min(s.cpb, s.c - c0);
-  if (nc <= 0) return;
-  if (s.kind == 0)
-    dfk::df_up_body(smf, b, c0, nc, s.n, s.k, s.Fh, s.Fl, s.X, s.ldx, s.perm, s.in, s.out, s.c,
-                    s.cpb);
-  else
-    dfk::df_down_body(smf, b, c0, nc, s.n, s.k, s.Fh, s.Fl, s.Dh, s.Dl, s.uin, s.vv, s.X, s.ldx,
-                      s.perm, s.out, s.Y, s.ldy, s.c, s.cpb);
-}
-
 // out[j] = sum_i A[cols[j].off + i * cols[j].ld]^2
 __global__ void colnorm_seg_k(const ColSeg* __restrict__ cols, const double* __restrict__ A,
                               double* __restrict__ out) {
@@ -138,60 +103,6 @@ __global__ void seg_copy_k(const CopySeg* __restrict__ segs) {
 }
 
 // ------------------------------------------------------------------ host side
-struct Geom {
-  int Nb, c;
-  size_t a, b;  // shared memory bytes of a CTA = a + b * cpb
-};
-
-// Step tables: segments of every step, back to back.
-template <class S>
-struct Steps {
-  std::vector<S> segs;
-  std::vector<int> off, ctas;
-  std::vector<size_t> smem;
-  std::vector<Geom> g;  // geometry of the step being built
-  void begin() {
-    off.push_back((int)segs.size());
-    g.clear();
-  }
-  // Column chunks for the step just built: the widest chunk m (at most
-  // mstart) that still gives `target` CTAs, halving down to mmin; each
-  // segment then narrows its own chunk until its CTA fits in shared memory.
-  void end(int mstart, int mmin, long long target) {
-    auto count = [&](int m) {
-      long long t = 0;
-      for (const Geom& x : g) {
-        const int cp = std::min(x.c, m);
-        t += (long long)x.Nb * ((x.c + cp - 1) / cp);
-      }
-      return t;
-    };
-    int m = std::max(mstart, 1);
-    while (m > mmin && count(m) < target) m = (m + 1) / 2;
-    long long cta = 0;
-    size_t sm = 0;
-    const size_t first = off.back();
-    for (size_t i = 0; i < g.size(); ++i) {
-      S& s = segs[first + i];
-      int cpb = std::min(g[i].c, m);
-      while (cpb > 1 && g[i].a + g[i].b * cpb > kSmemLimit) cpb = (cpb + 1) / 2;
-      SLU_REQUIRE(g[i].a + g[i].b * cpb <= kSmemLimit, "block too large for the grouped solve");
-      s.cpb = cpb;
-      s.nchunk = (g[i].c + cpb - 1) / cpb;
-      s.cta0 = (int)cta;
-      cta += (long long)g[i].Nb * s.nchunk;
-      sm = std::max(sm, g[i].a + g[i].b * cpb);
-    }
-    SLU_REQUIRE(cta < (1LL << 31), "grouped step too large");
-    ctas.push_back((int)cta);
-    smem.push_back(sm);
-  }
-  int nsteps() const { return (int)ctas.size(); }
-  int count(int s) const {
-    return (s + 1 < (int)off.size() ? off[s + 1] : (int)segs.size()) - off[s];
-  }
-};
-
 // Per-member device buffers of a grouped ULV sweep (five of `stride`).
 template <typename T>
 struct SolveBufs {
@@ -268,113 +179,76 @@ void build_solve(const std::vector<const Hbs*>& H, const std::vector<int>& c,
   }
 }
 
-// Per-member device buffers of a grouped double-float apply.
-struct DfBufs {
-  std::vector<DF*> VV;  // VV[t] for t >= 1
-  DF* u[2];
+// Per-member buffers of a grouped apply: VV[t] for t >= 1 and u[2]
+// (hbs_apply_scratch_elems elements).
+template <typename T>
+struct ApplyBufs {
+  std::vector<T*> VV;
+  T* u[2];
 };
 
-DfBufs carve_df(const Hbs& H, int c, void* scratch) {
-  DfBufs d;
-  DF* base = reinterpret_cast<DF*>(scratch);
+template <typename T>
+ApplyBufs<T> carve_apply(const Hbs& H, int c, T* base) {
+  ApplyBufs<T> d;
   d.VV.assign(H.L, nullptr);
   size_t off = 0;
   for (int t = 0; t + 1 < H.L; ++t) {
     d.VV[t + 1] = base + off;
-    off += ((size_t)H.lv[t].Nb * H.lv[t].k * c + 31) & ~size_t(31);
+    off += ((size_t)H.lv[t].Nb * H.lv[t].k * c + 63) & ~size_t(63);
   }
   d.u[0] = base + off;
-  d.u[1] = base + off + (((size_t)H.N * c + 31) & ~size_t(31));
+  d.u[1] = base + off + (((size_t)H.N * c + 63) & ~size_t(63));
   return d;
 }
 
-// Step tables of a grouped double-float apply Y[i] = A_i X[i] (the recursion
-// of hbs_apply_df.cu).
-void build_df(const std::vector<const Hbs*>& H, const std::vector<int>& c,
-              const std::vector<const double*>& X, const std::vector<int>& ldx,
-              const std::vector<double*>& Y, const std::vector<int>& ldy,
-              const std::vector<DfBufs>& buf, Steps<DfSeg>& st) {
+// Step tables of a grouped double-float apply Y[i] = A_i X[i] (the steps of
+// hbs_apply_fused, tree-step by tree-step across members).
+void build_apply_df(const std::vector<const Hbs*>& H, const std::vector<int>& c,
+                    const std::vector<const dfloat*>& X, const std::vector<dfloat*>& Y,
+                    const std::vector<ApplyBufs<dfloat>>& buf, StepTable<dfloat>& tab) {
   const int m = (int)H.size();
-  int maxL = 0, maxc = 1;
-  for (int i = 0; i < m; ++i) {
-    maxL = std::max(maxL, H[i]->L);
-    maxc = std::max(maxc, c[i]);
-  }
-  const long long target = num_sms();
-  const int mstart = std::min(maxc, 16), mmin = 2;
+  int maxL = 0;
+  for (int i = 0; i < m; ++i) maxL = std::max(maxL, H[i]->L);
+  std::vector<sweep::Step<dfloat>> v;
   for (int t = 0; t + 1 < maxL; ++t) {
-    st.begin();
+    v.clear();
     for (int i = 0; i < m; ++i) {
       if (H[i]->L < t + 2) continue;
       const Level& l = H[i]->lv[t];
-      DfSeg s{};
-      s.kind = 0;
-      s.n = l.n; s.k = l.k; s.c = c[i];
-      s.Fh = l.Vh.as<float>(); s.Fl = l.Vl.as<float>();
-      s.X = t == 0 ? X[i] : nullptr;
-      s.ldx = ldx[i];
-      s.perm = t == 0 ? H[i]->perm.as<int64_t>() : nullptr;
-      s.in = buf[i].VV[t];
-      s.out = buf[i].VV[t + 1];
-      st.segs.push_back(s);
-      st.g.push_back({l.Nb, c[i], 4 * 2 * (size_t)l.n * (l.k + 1), 4 * 2 * (size_t)l.n});
+      v.push_back(sweep::up_step<dfloat>(l, l.Aupdf.as<dfloat>(), t == 0 ? X[i] : buf[i].VV[t],
+                                         c[i], t == 0 ? H[i]->perm.as<int64_t>() : nullptr,
+                                         buf[i].VV[t + 1], c[i]));
     }
-    st.end(mstart, mmin, target);
+    tab.add(v);
   }
-  st.begin();
+  v.clear();
   for (int i = 0; i < m; ++i) {
     const int L = H[i]->L;
     const Level& r = H[i]->lv[L - 1];
-    DfSeg s{};
-    s.kind = 1;
-    s.n = r.n; s.k = 0; s.c = c[i];
-    s.Dh = r.Dh.as<float>(); s.Dl = r.Dl.as<float>();
-    if (L == 1) {
-      s.X = X[i];
-      s.ldx = ldx[i];
-      s.perm = H[i]->perm.as<int64_t>();
-      s.Y = Y[i];
-      s.ldy = ldy[i];
-    } else {
-      s.vv = buf[i].VV[L - 1];
-      s.out = buf[i].u[0];
-    }
-    st.segs.push_back(s);
-    st.g.push_back({1, c[i], 4 * 2 * (size_t)r.n * (r.n + 1), 4 * 4 * (size_t)r.n});
+    const int64_t* perm = H[i]->perm.as<int64_t>();
+    if (L == 1)
+      v.push_back(sweep::down_step<dfloat>(r, r.Adndf.as<dfloat>(), true, X[i], c[i], perm,
+                                           nullptr, Y[i], c[i], perm, c[i]));
+    else
+      v.push_back(sweep::down_step<dfloat>(r, r.Adndf.as<dfloat>(), true, buf[i].VV[L - 1], c[i],
+                                           nullptr, nullptr, buf[i].u[0], c[i], nullptr, c[i]));
   }
-  st.end(mstart, mmin, target);
+  tab.add(v);
   for (int t = maxL - 2; t >= 0; --t) {
-    st.begin();
+    v.clear();
     for (int i = 0; i < m; ++i) {
       const int L = H[i]->L;
       if (L < t + 2) continue;
       const Level& l = H[i]->lv[t];
       const int cur = (L - 2 - t) & 1;
       const bool leaf = t == 0;
-      DfSeg s{};
-      s.kind = 1;
-      s.n = l.n; s.k = l.k; s.c = c[i];
-      s.Fh = l.Uh.as<float>(); s.Fl = l.Ul.as<float>();
-      s.Dh = l.Dh.as<float>(); s.Dl = l.Dl.as<float>();
-      s.uin = buf[i].u[cur];
-      s.vv = leaf ? nullptr : buf[i].VV[t];
-      s.X = leaf ? X[i] : nullptr;
-      s.ldx = ldx[i];
-      s.perm = leaf ? H[i]->perm.as<int64_t>() : nullptr;
-      s.out = leaf ? nullptr : buf[i].u[cur ^ 1];
-      s.Y = leaf ? Y[i] : nullptr;
-      s.ldy = ldy[i];
-      st.segs.push_back(s);
-      st.g.push_back({l.Nb, c[i], 4 * 2 * (size_t)l.n * (l.n + 1),
-                      4 * (4 * (size_t)l.n + 2 * (size_t)l.k)});
+      const int64_t* perm = leaf ? H[i]->perm.as<int64_t>() : nullptr;
+      v.push_back(sweep::down_step<dfloat>(l, l.Adndf.as<dfloat>(), false,
+                                           leaf ? X[i] : buf[i].VV[t], c[i], perm, buf[i].u[cur],
+                                           leaf ? Y[i] : buf[i].u[cur ^ 1], c[i], perm, c[i]));
     }
-    st.end(mstart, mmin, target);
+    tab.add(v);
   }
-}
-
-template <typename K>
-void set_smem(K kern, size_t bytes) {
-  ensure_smem(reinterpret_cast<const void*>(kern), bytes);
 }
 
 template <typename T>
@@ -385,16 +259,6 @@ void launch_solve(cudaStream_t st, const StepTable<T>& tab, const StepSeg<T>* ds
     if (p.ctas == 0) continue;
     ensure_smem(reinterpret_cast<const void*>(kern), p.smem);
     sweep::launch_pdl(kern, p, st, "group_step_kernel", dsegs + tab.off[i], tab.cnt[i]);
-  }
-}
-
-void launch_df(cudaStream_t st, const Steps<DfSeg>& s, const DfSeg* dsegs) {
-  auto kern = group_df_kernel;
-  for (int i = 0; i < s.nsteps(); ++i) {
-    if (s.ctas[i] == 0) continue;
-    set_smem(kern, s.smem[i]);
-    kern<<<s.ctas[i], kThreads, s.smem[i], st>>>(dsegs + s.off[i], s.count(i));
-    check_launch("group_df_kernel");
   }
 }
 
@@ -546,7 +410,7 @@ void refine_grouped(Handle& h, int count, Hbs* const* ops, const double* const* 
   }
   // device regions
   Plan plan;
-  const size_t tab_bytes = blob_bound(nseg * (sizeof(StepSeg<T>) + sizeof(DfSeg)) +
+  const size_t tab_bytes = blob_bound(nseg * (sizeof(StepSeg<T>) + sizeof(StepSeg<dfloat>)) +
                                           (size_t)C * sizeof(ColSeg) + 2 * m * sizeof(CopySeg),
                                       5);
   plan.add(tab_bytes);
@@ -555,8 +419,11 @@ void refine_grouped(Handle& h, int count, Hbs* const* ops, const double* const* 
   plan.add(8 * E);  // r
   plan.add(sizeof(T) * E);  // inner right-hand sides / corrections
   plan.add(16 * (size_t)C);  // [bn | rn]
+  plan.add(sizeof(dfloat) * E);  // X as double-float pairs (residual apply input)
+  plan.add(sizeof(dfloat) * E);  // A X as double-float pairs
   for (int j = 0; j < m; ++j) plan.add(5 * stride[j] * sizeof(T));
-  for (int j = 0; j < m; ++j) plan.add(hbs_apply_df_scratch_bytes(*H[j], cm[j]));
+  for (int j = 0; j < m; ++j)
+    plan.add(sizeof(dfloat) * hbs_apply_scratch_elems(*H[j], cm[j]));
   h.ws.reserve(plan.total(), st);
   char* dtab = h.ws.take<char>(plan.bytes[0]);
   double* dB = h.ws.take<double>(E);
@@ -564,28 +431,30 @@ void refine_grouped(Handle& h, int count, Hbs* const* ops, const double* const* 
   double* dr = h.ws.take<double>(E);
   T* df = h.ws.take<T>(E);
   double* norms = h.ws.take<double>(2 * (size_t)C);
+  dfloat* xdf = h.ws.take<dfloat>(E);
+  dfloat* ydf = h.ws.take<dfloat>(E);
   std::vector<SolveBufs<T>> sbuf(m);
   for (int j = 0; j < m; ++j) {
     T* s = h.ws.take<T>(5 * stride[j]);
     sbuf[j].ru = s;
     for (int q = 0; q < 4; ++q) sbuf[j].P[q] = s + (q + 1) * stride[j];
   }
-  std::vector<DfBufs> dbuf(m);
+  std::vector<ApplyBufs<dfloat>> abuf(m);
   for (int j = 0; j < m; ++j)
-    dbuf[j] = carve_df(*H[j], cm[j], h.ws.take<char>(plan.bytes[6 + m + j]));
+    abuf[j] = carve_apply(*H[j], cm[j], h.ws.take<dfloat>(hbs_apply_scratch_elems(*H[j], cm[j])));
   // task tables
   std::vector<T*> fB(m);
-  std::vector<const double*> xX(m);
-  std::vector<double*> rY(m);
+  std::vector<const dfloat*> xX(m);
+  std::vector<dfloat*> rY(m);
   for (int j = 0; j < m; ++j) {
     fB[j] = df + off[j];
-    xX[j] = dX + off[j];
-    rY[j] = dr + off[j];
+    xX[j] = xdf + off[j];
+    rY[j] = ydf + off[j];
   }
   StepTable<T> ssteps;
   build_solve<T>(H, cm, fB, cm, sbuf, ssteps);
-  Steps<DfSeg> dsteps;
-  build_df(H, cm, xX, cm, rY, cm, dbuf, dsteps);
+  StepTable<dfloat> dsteps;
+  build_apply_df(H, cm, xX, rY, abuf, dsteps);
   std::vector<ColSeg> cols;
   cols.reserve(C);
   std::vector<CopySeg> cin(m), cpy_out(m);
@@ -602,7 +471,7 @@ void refine_grouped(Handle& h, int count, Hbs* const* ops, const double* const* 
   SLU_REQUIRE(blob.host.size() <= tab_bytes, "task table overflow");
   upload(h, blob, dtab);
   const auto* d_s = reinterpret_cast<const StepSeg<T>*>(dtab + a_s);
-  const auto* d_d = reinterpret_cast<const DfSeg*>(dtab + a_d);
+  const auto* d_d = reinterpret_cast<const StepSeg<dfloat>*>(dtab + a_d);
   const auto* d_c = reinterpret_cast<const ColSeg*>(dtab + a_c);
   const auto* d_i = reinterpret_cast<const CopySeg*>(dtab + a_i);
   const auto* d_o = reinterpret_cast<const CopySeg*>(dtab + a_o);
@@ -620,9 +489,11 @@ void refine_grouped(Handle& h, int count, Hbs* const* ops, const double* const* 
     to_inner(st, En, first ? dB : dr, df);
     launch_solve<T>(st, ssteps, d_s);
     accum_inner(st, En, df, dX, first ? 1 : 0);
-    launch_df(st, dsteps, d_d);
-    resid_k<<<gsz(En), 256, 0, st>>>(En, dB, dr);
-    check_launch("resid_k");
+    to_dfs_k<<<gsz(En), 256, 0, st>>>(En, dX, xdf);
+    check_launch("to_dfs_k");
+    launch_solve<dfloat>(st, dsteps, d_d);
+    resid_dfs_k<<<gsz(En), 256, 0, st>>>(En, dB, ydf, dr);
+    check_launch("resid_dfs_k");
     colnorm_seg_k<<<C, 256, 0, st>>>(d_c, dr, norms + C);
     check_launch("colnorm_seg_k");
     SLU_CHECK_CUDA(

@@ -371,6 +371,7 @@ void hbs_compress(Handle& h, Hbs& H, int Nb0, int rk, int s, const double* Om, c
   H.has_dfs = false;
   H.has_df = false;
   H.has_sweep = false;
+  H.has_apply[0] = H.has_apply[1] = false;
   H.invalidate_plans();
   if (ulv) hbs_make_sweep(h, H);
 }
@@ -425,16 +426,15 @@ void hbs_factor(Handle& h, Hbs& H) {
 }
 
 // ============================================================== apply
-void hbs_apply(Handle& h, const Hbs& H, bool trans, const double* X, int ldx, double* Yout,
+void hbs_apply(Handle& h, Hbs& H, bool trans, const double* X, int ldx, double* Yout,
                int ldy, int c) {
   cudaStream_t st = h.stream;
   SLU_REQUIRE(H.has_mats, "HBS factors not loaded");
-  for (int t = 0; t + 1 < H.L; ++t)
-    SLU_REQUIRE(H.lv[t].V.p, "apply needs V factors (loaded without V)");
+  if (!H.has_apply[trans ? 1 : 0]) hbs_make_apply(h, H, trans);
   const size_t elems = hbs_apply_scratch_elems(H, c);
   h.ws.reserve(8 * elems + 256, st);
   double* scratch = h.ws.take<double>(elems);
-  hbs_apply_fused(st, H, trans, X, ldx, Yout, ldy, c, scratch);
+  hbs_apply_fused<double>(st, H, trans, X, ldx, Yout, ldy, c, scratch);
 }
 
 // ============================================================== solve

@@ -77,8 +77,11 @@ struct Level {
   DevBuf Q, W, R, Uu;   // Nb*n x n, Nb*n x n, Nb*nu x n, Nb*uu_rows x kU
   // single-precision copies of the solve factors (mixed-precision solve)
   DevBuf Uf, Df, Qf, Wf, Rf, Uuf;
-  // (hi, lo) float32 pairs of U, V, D (double-float residual apply)
-  DevBuf Uh, Ul, Vh, Vl, Dh, Dl;
+  // step operators of the HBS apply (hbs_apply.cu), composed on first use:
+  // mode N Aup = V^T, Adn = [D | U] per block (the root: D); mode T
+  // AupT = U^T, AdnT = [D^T | V] (the root: D^T); Aupdf / Adndf: double-float
+  // copies of the mode-N ones (the refinement residual)
+  DevBuf Aup, Adn, AupT, AdnT, Aupdf, Adndf;
   // step operators of the mode-N solve (sweep_ops.cu): Qt = Q^T per block,
   // Sw = [G; H] per block (G only on the leaves; the root: [R^-1 Q^T; D R^-1 Q^T])
   DevBuf Qt, Sw;
@@ -96,6 +99,7 @@ struct Hbs {
   std::vector<long long> NN;       // NNvec, L+1 entries
   bool has_mats = false, has_ulv = false, has_f32 = false, has_df = false, has_dfs = false;
   bool has_sweep = false;   // step operators composed (hbs_make_sweep)
+  bool has_apply[2] = {false, false};   // apply operators, mode N / T (hbs_make_apply)
   // inner sweep of the mixed-precision refinement: 0 float32, 1 double-float
   int refine_inner = 1;
   int rk = 0, nsamples = 0;
@@ -114,8 +118,8 @@ void hbs_compress(Handle& h, Hbs& H, int Nb_leaf, int rk, int s, const double* O
                   const double* Psi, const double* Y, const double* Z, bool ulv);
 // standalone ULV of loaded factors (ULVsparse.compute_ULV)
 void hbs_factor(Handle& h, Hbs& H);
-// u = A v (trans = false) or A^T v, tree-ordered input/output when perm_io is false
-void hbs_apply(Handle& h, const Hbs& H, bool trans, const double* X, int ldx, double* Yout,
+// u = A v (trans = false) or A^T v, caller ordering (through the tree permutation)
+void hbs_apply(Handle& h, Hbs& H, bool trans, const double* X, int ldx, double* Yout,
                int ldy, int nrhs);
 // ULV solve, reference semantics of HBSMAT.solve (with the permutation)
 template <typename T>
@@ -166,10 +170,14 @@ void ulv_solve_fused(cudaStream_t st, const Hbs& H, T* B, int ldb, int c, T* scr
 // queue the launches that follow before the device reaches them: their event
 // timestamps then measure device time, not host enqueue gaps.
 void enqueue_device_lead(cudaStream_t st, int us);
-// Fused per-level apply (hbs_apply.cu); scratch of hbs_apply_scratch_elems doubles.
+// Apply as step kernels (hbs_apply.cu): scratch of hbs_apply_scratch_elems
+// elements of T; the operators of the direction must have been composed
+// (hbs_make_apply; for T = dfloat, hbs_make_df).
 size_t hbs_apply_scratch_elems(const Hbs& H, int c);
-void hbs_apply_fused(cudaStream_t st, const Hbs& H, bool trans, const double* X, int ldx,
-                     double* Y, int ldy, int c, double* scratch);
+void hbs_make_apply(Handle& h, Hbs& H, bool trans);
+template <typename T>
+void hbs_apply_fused(cudaStream_t st, const Hbs& H, bool trans, const T* X, int ldx, T* Y,
+                     int ldy, int c, T* scratch);
 void hbs_make_f32(Handle& h, Hbs& H);
 // Composes the step operators of the mode-N solve from the ULV factors.
 void hbs_make_sweep(Handle& h, Hbs& H);
@@ -182,7 +190,8 @@ void hbs_solve_df(cudaStream_t st, const Hbs& H, double* B, int ldb, int c, void
 // Mixed-precision refinement replayed as CUDA graphs (refine.cu).
 void hbs_refine(Handle& h, Hbs& H, const double* B, int ldb, double* X, int ldx, int c,
                 double tol, int maxit, int* iters, double* relres);
-// Double-float apply (hbs_apply_df.cu): factors split once by hbs_make_df.
+// Double-float apply Y = A X (mode N; float64 in and out, double-float
+// arithmetic): the mode-N apply operators split once by hbs_make_df.
 void hbs_make_df(Handle& h, Hbs& H);
 size_t hbs_apply_df_scratch_bytes(const Hbs& H, int c);
 void hbs_apply_df(cudaStream_t st, const Hbs& H, const double* X, int ldx, double* Y, int ldy,

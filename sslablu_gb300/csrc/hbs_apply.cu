@@ -1,212 +1,221 @@
-// Fused HBS apply: one kernel per tree level and sweep.
+// HBS apply Y = A X or A^T X as step kernels (sweep.cuh / sweep_host.cuh).
 //
-// u = A v (or A^T v) for the stored HBS factors, the recursion of
-// HBSnew.HBSMAT.matmat / rmatmat (matAssembly/HBS/HBSnew.py:308-350):
+// The recursion of HBSnew.HBSMAT.matmat / rmatmat (matAssembly/HBS/
+// HBSnew.py:308-350):
 //   upward   VV[t+1]_b = F_b^T VV[t]_b          (F = V for A, U for A^T)
-//   root     u = D_root VV[L-1]                  (D_root^T for A^T)
-//   downward u_b = G_b u_parent(b) + D_b VV[t]_b (G = U for A, V for A^T;
-//                                                 D_b^T for A^T)
-// The permutation gather of v and scatter of u are folded into the leaf
-// kernels.  CTA (b, j) handles block b and a chunk of right-hand-side
-// columns, staging each block matrix in shared memory (as ulv_solve.cu).
+//   root     u = op(D_root) VV[L-1]              (op(D) = D^T for A^T)
+//   downward u_b = op(D_b) VV[t]_b + G_b u_parent(b)   (G = U for A, V for A^T)
+// Each step is one block product with an operator composed from the stored
+// factors on first use (hbs_make_apply): F_b^T for the up steps and
+// [op(D_b) | G_b] for the down steps, so a down step is a single product
+// over [VV[t]_b; u_parent(b)].  The permutation gather of X and scatter of Y
+// are folded into the leaf steps.
+//
+// The double-float apply (the refinement residual of the mixed path) runs the
+// same steps on float32 pairs: X is split into pairs, the steps run in
+// double-float arithmetic, Y is rounded back to float64.
 #include "hbs.cuh"
+#include "sweep_host.cuh"
 
 #include <algorithm>
 
 namespace slu {
 namespace {
 
-constexpr int kThreads = 256;
+// out_b (n x (n+k)) = [op(D_b) | G_b]
+__global__ void compose_down_kernel(int nb, int n, int k, bool transD, const double* __restrict__ D,
+                                    const double* __restrict__ G, double* __restrict__ out) {
+  const int w = n + k;
+  const long long total = (long long)nb * n * w;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long b = e / ((long long)n * w);
+    const int r = (int)(e - b * n * w);
+    const int i = r / w, j = r - i * w;
+    double v;
+    if (j < n) v = transD ? D[(b * n + j) * n + i] : D[(b * n + i) * n + j];
+    else v = G[(b * n + i) * k + (j - n)];
+    out[e] = v;
+  }
+}
+
+__global__ void split_pairs_kernel(long long n, const double* __restrict__ x,
+                                   dfloat* __restrict__ y) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+       e += (long long)gridDim.x * blockDim.x)
+    y[e] = to_dfloat(x[e]);
+}
+
+// Y (rows x c, ld c) <- X (ld ldx) as double-float, and back
+__global__ void rows_to_pairs_kernel(int rows, int c, const double* __restrict__ X, int ldx,
+                                     dfloat* __restrict__ Y) {
+  const long long n = (long long)rows * c;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long i = e / c, j = e - i * c;
+    Y[e] = to_dfloat(X[i * ldx + j]);
+  }
+}
+__global__ void rows_from_pairs_kernel(int rows, int c, const dfloat* __restrict__ Y,
+                                       double* __restrict__ X, int ldx) {
+  const long long n = (long long)rows * c;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long i = e / c, j = e - i * c;
+    X[i * ldx + j] = to_double(Y[e]);
+  }
+}
+
+int grid_for(long long n) {
+  return (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, 8LL * num_sms()));
+}
+
+void split_pairs(cudaStream_t st, const DevBuf& src, DevBuf& dst) {
+  const long long n = (long long)(src.bytes / 8);
+  dst.alloc(8 * n, st);
+  if (n == 0) return;
+  split_pairs_kernel<<<grid_for(n), 256, 0, st>>>(n, src.as<double>(), dst.as<dfloat>());
+  check_launch("split_pairs_kernel");
+}
 
 template <typename T>
-__device__ inline void stage(T* S, int ld, const T* __restrict__ A, int rows, int cols) {
-  for (int e = threadIdx.x; e < rows * cols; e += blockDim.x) {
-    int i = e / cols, j = e - i * cols;
-    S[i * ld + j] = A[e];
+struct ApplyOps;
+template <>
+struct ApplyOps<double> {
+  static bool ready(const Hbs& H, bool trans) { return H.has_apply[trans ? 1 : 0]; }
+  static const double* up(const Level& l, bool trans) {
+    return (trans ? l.AupT : l.Aup).as<double>();
   }
-}
-
-// Upward step: out_b (k x c) = F_b^T in_b, in_b n x c (gathered through perm
-// on the leaf level).
-template <typename T>
-__global__ void __launch_bounds__(kThreads)
-apply_up_kernel(int n, int k, const T* __restrict__ F, const T* __restrict__ in, int ldi,
-                const int64_t* __restrict__ perm, T* __restrict__ out, int c, int cpb) {
-  extern __shared__ unsigned char sm_raw[];
-  T* S = reinterpret_cast<T*>(sm_raw);   // n x (k+1)
-  T* x = S + n * (k + 1);                 // n x cpb
-  const int b = blockIdx.x, c0 = blockIdx.y * cpb, nc = min(cpb, c - c0);
-  if (nc <= 0) return;
-  for (int e = threadIdx.x; e < n * nc; e += blockDim.x) {
-    int i = e / nc, cc = e - i * nc;
-    long long row = (long long)b * n + i;
-    if (perm) row = perm[row];
-    x[i * cpb + cc] = in[row * ldi + c0 + cc];
+  static const double* down(const Level& l, bool trans) {
+    return (trans ? l.AdnT : l.Adn).as<double>();
   }
-  stage(S, k + 1, F + (size_t)b * n * k, n, k);
-  __syncthreads();
-  for (int e = threadIdx.x; e < k * nc; e += blockDim.x) {
-    int i = e / nc, cc = e - i * nc;
-    T acc = T(0);
-#pragma unroll 4
-    for (int j = 0; j < n; ++j) acc = fma(S[j * (k + 1) + i], x[j * cpb + cc], acc);
-    out[((size_t)b * k + i) * c + c0 + cc] = acc;
-  }
-}
-
-// Downward step (and the root when G == nullptr):
-//   out_b = G_b uin_b + op(D_b) vv_b   (n x c); on the leaf level the rows
-//   are scattered through perm into Y (ld ldy), and the leaf input vv is
-//   gathered through perm from X (ld ldx).
-template <typename T>
-__global__ void __launch_bounds__(kThreads)
-apply_down_kernel(int n, int k, bool transD, const T* __restrict__ G, const T* __restrict__ D,
-                  const T* __restrict__ uin, const T* __restrict__ vv, int ldv,
-                  const int64_t* __restrict__ perm, T* __restrict__ out, int ldo, int c,
-                  int cpb) {
-  extern __shared__ unsigned char sm_raw[];
-  T* S = reinterpret_cast<T*>(sm_raw);   // n x (n+1)
-  T* x = S + n * (n + 1);                 // n x cpb : vv_b
-  T* ub = x + n * cpb;                    // k x cpb : uin_b
-  T* acc_s = ub + k * cpb;                // n x cpb
-  const int b = blockIdx.x, c0 = blockIdx.y * cpb, nc = min(cpb, c - c0);
-  if (nc <= 0) return;
-  for (int e = threadIdx.x; e < n * nc; e += blockDim.x) {
-    int i = e / nc, cc = e - i * nc;
-    long long row = (long long)b * n + i;
-    if (perm) row = perm[row];
-    x[i * cpb + cc] = vv[row * ldv + c0 + cc];
-  }
-  if (G)
-    for (int e = threadIdx.x; e < k * nc; e += blockDim.x) {
-      int i = e / nc, cc = e - i * nc;
-      ub[i * cpb + cc] = uin[((size_t)b * k + i) * c + c0 + cc];
-    }
-  stage(S, n + 1, D + (size_t)b * n * n, n, n);
-  __syncthreads();
-  for (int e = threadIdx.x; e < n * nc; e += blockDim.x) {
-    int i = e / nc, cc = e - i * nc;
-    T a = T(0);
-    if (!transD) {
-      const T* s = S + i * (n + 1);
-#pragma unroll 4
-      for (int j = 0; j < n; ++j) a = fma(s[j], x[j * cpb + cc], a);
-    } else {
-#pragma unroll 4
-      for (int j = 0; j < n; ++j) a = fma(S[j * (n + 1) + i], x[j * cpb + cc], a);
-    }
-    acc_s[i * cpb + cc] = a;
-  }
-  if (G) {
-    __syncthreads();
-    stage(S, k + 1, G + (size_t)b * n * k, n, k);
-    __syncthreads();
-    for (int e = threadIdx.x; e < n * nc; e += blockDim.x) {
-      int i = e / nc, cc = e - i * nc;
-      const T* s = S + i * (k + 1);
-      T a = acc_s[i * cpb + cc];
-#pragma unroll 4
-      for (int j = 0; j < k; ++j) a = fma(s[j], ub[j * cpb + cc], a);
-      acc_s[i * cpb + cc] = a;
-    }
-  }
-  // write (each thread owns its own acc_s entries: no barrier needed)
-  for (int e = threadIdx.x; e < n * nc; e += blockDim.x) {
-    int i = e / nc, cc = e - i * nc;
-    long long row = (long long)b * n + i;
-    if (perm) {
-      out[perm[row] * ldo + c0 + cc] = acc_s[i * cpb + cc];
-    } else {
-      out[row * c + c0 + cc] = acc_s[i * cpb + cc];
-    }
-  }
-}
-
-int chunk64(int Nb, int c) {
-  int target = 2 * num_sms();
-  int cpb = c;
-  while (cpb > 1 && (long long)Nb * ((c + cpb - 1) / cpb) < target) cpb = (cpb + 1) / 2;
-  return cpb;
-}
-
-template <typename K>
-void set_smem(K kern, size_t bytes) {
-  ensure_smem(reinterpret_cast<const void*>(kern), bytes);
-}
+};
+template <>
+struct ApplyOps<dfloat> {
+  static bool ready(const Hbs& H, bool trans) { return H.has_df && !trans; }
+  static const dfloat* up(const Level& l, bool) { return l.Aupdf.as<dfloat>(); }
+  static const dfloat* down(const Level& l, bool) { return l.Adndf.as<dfloat>(); }
+};
 
 }  // namespace
 
-size_t hbs_apply_scratch_elems(const Hbs& H, int c) {
-  size_t vv = H.N;
-  for (int t = 0; t + 1 < H.L; ++t) vv += (size_t)H.lv[t].Nb * H.lv[t].k;
-  return (vv + 2 * (size_t)H.N) * c + 3 * 64;
+void hbs_make_apply(Handle& h, Hbs& H, bool trans) {
+  SLU_REQUIRE(H.has_mats, "HBS factors not loaded");
+  cudaStream_t st = h.stream;
+  const int L = H.L;
+  for (int t = 0; t + 1 < L; ++t) {
+    Level& l = H.lv[t];
+    SLU_REQUIRE(trans ? l.U.p : l.V.p, "apply needs V factors (loaded without V)");
+    SLU_REQUIRE(trans ? l.V.p : l.U.p, "apply needs U and V factors");
+    const int n = l.n, k = l.k, Nb = l.Nb;
+    DevBuf& up = trans ? l.AupT : l.Aup;
+    DevBuf& dn = trans ? l.AdnT : l.Adn;
+    up.alloc(8 * (size_t)Nb * k * n, st);
+    transpose_batched(st, n, k, (trans ? l.U : l.V).as<double>(), k, (long long)n * k, 0,
+                      up.as<double>(), n, (long long)k * n, 0, Nb);
+    dn.alloc(8 * (size_t)Nb * n * (n + k), st);
+    const long long ne = (long long)Nb * n * (n + k);
+    compose_down_kernel<<<grid_for(ne), 256, 0, st>>>(Nb, n, k, trans, l.D.as<double>(),
+                                                       (trans ? l.V : l.U).as<double>(),
+                                                       dn.as<double>());
+    check_launch("compose_down_kernel");
+  }
+  Level& r = H.lv[L - 1];
+  DevBuf& dn = trans ? r.AdnT : r.Adn;
+  dn.alloc(8 * (size_t)r.n * r.n, st);
+  compose_down_kernel<<<grid_for((long long)r.n * r.n), 256, 0, st>>>(
+      1, r.n, 0, trans, r.D.as<double>(), nullptr, dn.as<double>());
+  check_launch("compose_down_kernel");
+  H.has_apply[trans ? 1 : 0] = true;
 }
 
-// Y (N x c, ld ldy) = A X or A^T X; scratch of hbs_apply_scratch_elems doubles.
-void hbs_apply_fused(cudaStream_t st, const Hbs& H, bool trans, const double* X, int ldx,
-                     double* Y, int ldy, int c, double* scratch) {
+size_t hbs_apply_scratch_elems(const Hbs& H, int c) {
+  size_t vv = 0;
+  for (int t = 0; t + 1 < H.L; ++t) vv += ((size_t)H.lv[t].Nb * H.lv[t].k * c + 63) & ~size_t(63);
+  return vv + 2 * (((size_t)H.N * c + 63) & ~size_t(63)) + 64;
+}
+
+// Y (N x c, ld ldy) = op(A) X; scratch of hbs_apply_scratch_elems elements.
+template <typename T>
+void hbs_apply_fused(cudaStream_t st, const Hbs& H, bool trans, const T* X, int ldx, T* Y,
+                     int ldy, int c, T* scratch) {
+  using A = ApplyOps<T>;
+  SLU_REQUIRE(A::ready(H, trans), "apply operators not composed");
   const int L = H.L;
   const int64_t* perm = H.perm.as<int64_t>();
-  // VV[t] for t >= 1 (VV[0] is X read through perm)
-  std::vector<double*> VV(L, nullptr);
+  std::vector<T*> VV(L, nullptr);
   size_t off = 0;
   for (int t = 0; t + 1 < L; ++t) {
     VV[t + 1] = scratch + off;
     off += ((size_t)H.lv[t].Nb * H.lv[t].k * c + 63) & ~size_t(63);
   }
-  double* u[2] = {scratch + off, scratch + off + (((size_t)H.N * c + 63) & ~size_t(63))};
+  T* u[2] = {scratch + off, scratch + off + (((size_t)H.N * c + 63) & ~size_t(63))};
   if (L == 1) {
     const Level& r = H.lv[0];
-    size_t sm = 8 * ((size_t)r.n * (r.n + 1) + 2 * (size_t)r.n * c);
-    auto kern = apply_down_kernel<double>;
-    set_smem(kern, sm);
-    int cpb = chunk64(1, c);
-    sm = 8 * ((size_t)r.n * (r.n + 1) + 2 * (size_t)r.n * cpb);
-    set_smem(kern, sm);
-    kern<<<dim3(1, (c + cpb - 1) / cpb), kThreads, sm, st>>>(
-        r.n, 0, trans, nullptr, r.D.as<double>(), nullptr, X, ldx, perm, Y, ldy, c, cpb);
-    check_launch("apply_down_kernel");
+    sweep::launch_step(st, sweep::down_step<T>(r, A::down(r, trans), true, X, ldx, perm, nullptr,
+                                               Y, ldy, perm, c),
+                       "apply_root_step");
     return;
   }
   for (int t = 0; t + 1 < L; ++t) {
     const Level& l = H.lv[t];
-    const double* F = trans ? l.U.as<double>() : l.V.as<double>();
-    const int cpb = chunk64(l.Nb, c);
-    size_t sm = 8 * ((size_t)l.n * (l.k + 1) + (size_t)l.n * cpb);
-    auto kern = apply_up_kernel<double>;
-    set_smem(kern, sm);
-    const double* in = t == 0 ? X : VV[t];
-    int ldi = t == 0 ? ldx : c;
-    kern<<<dim3(l.Nb, (c + cpb - 1) / cpb), kThreads, sm, st>>>(
-        l.n, l.k, F, in, ldi, t == 0 ? perm : nullptr, VV[t + 1], c, cpb);
-    check_launch("apply_up_kernel");
+    sweep::launch_step(st, sweep::up_step<T>(l, A::up(l, trans), t == 0 ? X : VV[t],
+                                             t == 0 ? ldx : c, t == 0 ? perm : nullptr,
+                                             VV[t + 1], c),
+                       "apply_up_step");
   }
   const Level& r = H.lv[L - 1];
-  {
-    const int cpb = chunk64(1, c);
-    size_t sm = 8 * ((size_t)r.n * (r.n + 1) + 2 * (size_t)r.n * cpb);
-    auto kern = apply_down_kernel<double>;
-    set_smem(kern, sm);
-    kern<<<dim3(1, (c + cpb - 1) / cpb), kThreads, sm, st>>>(
-        r.n, 0, trans, nullptr, r.D.as<double>(), nullptr, VV[L - 1], c, nullptr, u[0], c, c,
-        cpb);
-    check_launch("apply_down_kernel");
-  }
+  sweep::launch_step(st, sweep::down_step<T>(r, A::down(r, trans), true, VV[L - 1], c, nullptr,
+                                             nullptr, u[0], c, nullptr, c),
+                     "apply_root_step");
   int cur = 0;
   for (int t = L - 2; t >= 0; --t) {
     const Level& l = H.lv[t];
-    const double* G = trans ? l.V.as<double>() : l.U.as<double>();
-    const int cpb = chunk64(l.Nb, c);
-    size_t sm = 8 * ((size_t)l.n * (l.n + 1) + (2 * (size_t)l.n + l.k) * cpb);
-    auto kern = apply_down_kernel<double>;
-    set_smem(kern, sm);
-    const bool leaf = (t == 0);
-    kern<<<dim3(l.Nb, (c + cpb - 1) / cpb), kThreads, sm, st>>>(
-        l.n, l.k, trans, G, l.D.as<double>(), u[cur], leaf ? X : VV[t], leaf ? ldx : c,
-        leaf ? perm : nullptr, leaf ? Y : u[cur ^ 1], leaf ? ldy : c, c, cpb);
-    check_launch("apply_down_kernel");
+    const bool leaf = t == 0;
+    sweep::launch_step(st, sweep::down_step<T>(l, A::down(l, trans), false, leaf ? X : VV[t],
+                                               leaf ? ldx : c, leaf ? perm : nullptr, u[cur],
+                                               leaf ? Y : u[cur ^ 1], leaf ? ldy : c,
+                                               leaf ? perm : nullptr, c),
+                       "apply_down_step");
     cur ^= 1;
   }
+}
+template void hbs_apply_fused<double>(cudaStream_t, const Hbs&, bool, const double*, int, double*,
+                                      int, int, double*);
+template void hbs_apply_fused<dfloat>(cudaStream_t, const Hbs&, bool, const dfloat*, int, dfloat*,
+                                      int, int, dfloat*);
+
+// ---------------------------------------------------------------- double-float
+void hbs_make_df(Handle& h, Hbs& H) {
+  SLU_REQUIRE(H.has_mats, "HBS factors not loaded");
+  H.invalidate_plans();
+  if (!H.has_apply[0]) hbs_make_apply(h, H, false);
+  for (Level& l : H.lv) {
+    if (l.Aup.p) split_pairs(h.stream, l.Aup, l.Aupdf);
+    split_pairs(h.stream, l.Adn, l.Adndf);
+  }
+  H.has_df = true;
+}
+
+size_t hbs_apply_df_scratch_bytes(const Hbs& H, int c) {
+  const size_t nc = ((size_t)H.N * c + 63) & ~size_t(63);
+  return sizeof(dfloat) * (2 * nc + hbs_apply_scratch_elems(H, c)) + 256;
+}
+
+// Y (N x c, float64, ld ldy) = A X with double-float arithmetic.
+void hbs_apply_df(cudaStream_t st, const Hbs& H, const double* X, int ldx, double* Y, int ldy,
+                  int c, void* scratch) {
+  SLU_REQUIRE(H.has_df, "double-float factors not prepared");
+  const size_t nc = ((size_t)H.N * c + 63) & ~size_t(63);
+  dfloat* xd = static_cast<dfloat*>(scratch);
+  dfloat* yd = xd + nc;
+  dfloat* ws = yd + nc;
+  const long long n = (long long)H.N * c;
+  rows_to_pairs_kernel<<<grid_for(n), 256, 0, st>>>(H.N, c, X, ldx, xd);
+  check_launch("rows_to_pairs_kernel");
+  hbs_apply_fused<dfloat>(st, H, false, xd, c, yd, c, c, ws);
+  rows_from_pairs_kernel<<<grid_for(n), 256, 0, st>>>(H.N, c, yd, Y, ldy);
+  check_launch("rows_from_pairs_kernel");
 }
 
 }  // namespace slu

@@ -57,6 +57,16 @@ __global__ void accum_dfs_k(long long n, const dfloat* __restrict__ d, double* _
   }
 }
 
+// r = b - y (y double-float)
+__global__ void resid_dfs_k(long long n, const double* __restrict__ b, const dfloat* __restrict__ y,
+                            double* __restrict__ r) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+       e += (long long)gridDim.x * blockDim.x) {
+    const dfloat v = y[e];
+    r[e] = (b[e] - (double)v.h) - (double)v.l;
+  }
+}
+
 // r = b - r
 __global__ void resid_k(long long n, const double* __restrict__ b, double* __restrict__ r) {
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;

@@ -207,5 +207,96 @@ void launch_pdl(void (*kern)(Args...), const LaunchPlan& p, cudaStream_t st,
   check_launch(what);
 }
 
+// ---------------------------------------------------------------- apply steps
+// The HBS apply Y = op(A) X (HBSnew.HBSMAT.matmat / rmatmat,
+// matAssembly/HBS/HBSnew.py:308-350) as the same step kernels:
+//   up, level t:   VV[t+1]_b = F_b^T VV[t]_b       S = F_b^T (k x n)
+//   root:          u = op(D_root) VV[L-1]           S = op(D_root) (n x n)
+//   down, level t: u_b = op(D_b) VV[t]_b + G_b u_parent(b)
+//                                                   S = [op(D_b) | G_b] (n x (n+k))
+// (F = V, G = U for A; F = U, G = V, op(D) = D^T for A^T).  VV[0] is X read
+// through the tree permutation; the leaf down step writes Y through it.
+template <typename T>
+Step<T> up_step(const Level& l, const T* S, const T* in, int ldi, const int64_t* perm, T* out,
+                int c) {
+  Step<T> s{};
+  s.S = S;
+  s.sS = (long long)l.k * l.n;
+  s.rows = l.k;
+  s.w = l.n;
+  s.nb = l.Nb;
+  s.c = c;
+  s.nin = 1;
+  s.in_p[0] = in;
+  s.in_ld[0] = ldi;
+  s.in_blk[0] = l.n;
+  s.in_rows[0] = l.n;
+  s.in_perm = perm;
+  s.split = l.k;
+  s.out_p[0] = out;
+  s.out_ld[0] = c;
+  s.out_blk[0] = l.k;
+  return s;
+}
+
+// Down step of level l (root: uin == nullptr, S = op(D) only).
+template <typename T>
+Step<T> down_step(const Level& l, const T* S, bool root, const T* vv, int ldv,
+                  const int64_t* vperm, const T* uin, T* out, int ldo, const int64_t* operm,
+                  int c) {
+  Step<T> s{};
+  s.S = S;
+  s.rows = l.n;
+  s.w = root ? l.n : l.n + l.k;
+  s.sS = (long long)s.rows * s.w;
+  s.nb = root ? 1 : l.Nb;
+  s.c = c;
+  s.nin = root ? 1 : 2;
+  s.in_p[0] = vv;
+  s.in_ld[0] = ldv;
+  s.in_blk[0] = l.n;
+  s.in_rows[0] = l.n;
+  s.in_perm = vperm;
+  if (!root) {
+    s.in_p[1] = uin;
+    s.in_ld[1] = c;
+    s.in_blk[1] = l.k;
+    s.in_rows[1] = l.k;
+  }
+  s.split = l.n;
+  s.out_p[0] = out;
+  s.out_ld[0] = ldo;
+  s.out_blk[0] = l.n;
+  s.out_perm = operm;
+  return s;
+}
+
+// ---------------------------------------------------------------- launches
+namespace {
+template <typename T>
+__global__ void __launch_bounds__(kMaxThreads) step_kernel(const Step<T> s) {
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  const int ncch = (s.c + s.cpb - 1) / s.cpb;
+  step_body<T>(s, sm_raw, blockIdx.x / ncch, blockIdx.x % ncch);
+}
+}  // namespace
+
+// One step as one launch (programmatic dependent launch); with `lt` the
+// launch is bracketed by timing events.
+template <typename T>
+void launch_step(cudaStream_t st, Step<T> s, const char* what, LaunchTimes* lt = nullptr,
+                 int lvl = 0, int kind = 0) {
+  Step<T>* one = &s;
+  const LaunchPlan p = plan_steps(&one, 1);
+  auto kern = step_kernel<T>;
+  ensure_smem(reinterpret_cast<const void*>(kern), p.smem);
+  if (lt) lt->mark(st);
+  launch_pdl(kern, p, st, what, s);
+  if (lt) {
+    lt->mark(st);
+    lt->done(lvl, kind);
+  }
+}
+
 }  // namespace sweep
 }  // namespace slu

@@ -23,31 +23,8 @@
 #include <algorithm>
 
 namespace slu {
-namespace {
 
-template <typename T>
-__global__ void __launch_bounds__(sweep::kMaxThreads) step_kernel(const sweep::Step<T> s) {
-  extern __shared__ __align__(16) unsigned char sm_raw[];
-  sweep::step_body<T>(s, sm_raw, blockIdx.x / ((s.c + s.cpb - 1) / s.cpb),
-                      blockIdx.x % ((s.c + s.cpb - 1) / s.cpb));
-}
-
-template <typename T>
-void launch_step(cudaStream_t st, sweep::Step<T> s, const char* what, LaunchTimes* lt, int lvl,
-                 int kind) {
-  sweep::Step<T>* one = &s;
-  const sweep::LaunchPlan p = sweep::plan_steps(&one, 1);
-  auto kern = step_kernel<T>;
-  ensure_smem(reinterpret_cast<const void*>(kern), p.smem);
-  if (lt) lt->mark(st);
-  sweep::launch_pdl(kern, p, st, what, s);
-  if (lt) {
-    lt->mark(st);
-    lt->done(lvl, kind);
-  }
-}
-
-}  // namespace
+using sweep::launch_step;
 
 // B (N x c, caller ordering) <- A^{-1} B; scratch: 5 buffers of stride elements.
 template <typename T>
