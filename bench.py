@@ -292,6 +292,8 @@ def run_gpu(args, rank, world):
     torch.cuda.synchronize()
     t_factor = time.perf_counter() - t0
     H.solve_refined(rhs[:, :1], tol=TOL, maxit=10)   # prepares the double-float factors
+    # launch plans of the 16-column solves picked by the autotuner (untimed)
+    tuned = {"f64": H.autotune(NRHS), "dfloat": H.autotune(NRHS, "dfloat")}
     torch.cuda.synchronize()
 
     B = torch.from_numpy(rhs).cuda()
@@ -375,7 +377,10 @@ def run_gpu(args, rank, world):
             "ms_per_step": 1e3 * tot_plain / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic",
-            "config": workload_config({"factor_s": t_factor, "arm": "plain float64 ULV solve"}),
+            "config": workload_config({"factor_s": t_factor, "arm": "plain float64 ULV solve",
+                                       "launch_plans": "autotuned per launch (target CTAs/SM, "
+                                                       "row floor, column cap)",
+                                       "tuned": tuned}),
             "p50_ms": 1e3 * p50, "p99_ms": 1e3 * float(np.percentile(ts_plain, 99)),
             "relres": res_plain,
             "mixed": {"value": world * NRHS * args.steps / tot_mixed, "unit": UNIT,

@@ -194,6 +194,20 @@ int slu_refine_grouped(slu_handle_t h, int count, const slu_hbs_t* ops, const do
 int slu_ulv_solve_timed(slu_handle_t h, slu_hbs_t op, double* B, int ldb, int nrhs,
                         float* ms_out, int* level_out, int* kind_out, int cap, int* nlaunch);
 
+/* Autotuner of the mode-N solve's launch plans for `nrhs` right-hand sides:
+ * every launch of the solve is timed under a set of plan caps (CTAs per SM
+ * aimed for, the row-slice floor, the widest column chunk), `reps` times
+ * each, and the fastest caps are kept on `op` for that right-hand-side count
+ * and precision (0 float64 slu_ulv_solve, 2 double-float
+ * slu_ulv_solve_dfloat); later solves of that width use them.  Results do
+ * not change: the caps move work between CTAs, never the order of terms.
+ * knobs_out (host, may be NULL) receives 3 ints per launch (target, row
+ * floor, column cap) for up to cap launches; *nlaunch the launch count.
+ * The tuning is dropped when the operator is refactored.  No upstream
+ * counterpart. */
+int slu_ulv_autotune(slu_handle_t h, slu_hbs_t op, int nrhs, int precision, int reps,
+                     int* knobs_out, int cap, int* nlaunch);
+
 /* Geometry: L, N and per level (Nb, n, k, nu) into levels[4*L]; NNvec[L+1]
  * (ULVsparse.compute_ULV's NNvec).  Host pointers, any may be NULL. */
 int slu_hbs_info(slu_hbs_t op, int* L, int* N, int* levels, long long* NNvec, int* nsamples);

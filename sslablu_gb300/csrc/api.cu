@@ -366,6 +366,24 @@ int slu_ulv_solve_timed(slu_handle_t h, slu_hbs_t op, double* B, int ldb, int nr
   });
 }
 
+int slu_ulv_autotune(slu_handle_t h, slu_hbs_t op, int nrhs, int precision, int reps,
+                     int* knobs_out, int cap, int* nlaunch) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h && op, "null argument");
+    SLU_REQUIRE(nrhs >= 1 && reps >= 1 && cap >= 0, "bad arguments");
+    slu::Hbs& H = op->H;
+    SLU_REQUIRE(H.has_ulv, "HBS operator has no ULV factorisation");
+    slu::hbs_autotune_solve(h->h, H, nrhs, precision, reps);
+    const std::vector<slu::PlanKnobs>& k = H.tuned[{precision, nrhs}];
+    if (nlaunch) *nlaunch = (int)k.size();
+    for (int i = 0; knobs_out && i < (int)k.size() && i < cap; ++i) {
+      knobs_out[3 * i] = k[i].target;
+      knobs_out[3 * i + 1] = k[i].rmin;
+      knobs_out[3 * i + 2] = k[i].cmax;
+    }
+  });
+}
+
 int slu_hbs_set_null_space(slu_hbs_t op, int mode) {
   return guard(nullptr, [&] {
     SLU_REQUIRE(op, "null argument");

@@ -91,6 +91,16 @@ struct Level {
 
 struct RefinePlan;  // refine.cu: buffers + CUDA graphs of one refinement iteration
 
+// Caps of a step launch plan (sweep_host.cuh plan_steps): the CTAs per SM a
+// launch aims for, the row-slice floor it halves down to first, the widest
+// column chunk.  The defaults serve untuned solves; hbs_autotune_solve picks
+// them per step by timing.
+struct PlanKnobs {
+  int target = 2;
+  int rmin = 16;
+  int cmax = 64;
+};
+
 struct Hbs {
   int N = 0, L = 0, fac = 2;
   std::vector<Level> lv;           // lv[0] = leaves, lv[L-1] = root
@@ -110,6 +120,10 @@ struct Hbs {
   // refinement plans per right-hand-side count; they capture factor pointers,
   // so every change of the factors clears them (invalidate_plans)
   std::map<int, std::shared_ptr<RefinePlan>> refine_plans;
+  // tuned launch caps of the mode-N solve per (element type: 0 float64,
+  // 1 float32, 2 double-float; right-hand-side count), one per launch;
+  // dropped whenever the step operators are recomposed
+  std::map<std::pair<int, int>, std::vector<PlanKnobs>> tuned;
   void invalidate_plans() { refine_plans.clear(); }
 };
 
@@ -165,6 +179,11 @@ struct LaunchTimes {
 template <typename T>
 void ulv_solve_fused(cudaStream_t st, const Hbs& H, T* B, int ldb, int c, T* scratch,
                      size_t stride, LaunchTimes* times = nullptr);
+// Times every launch of the mode-N solve for `c` right-hand sides under a set
+// of plan caps and keeps the fastest per launch (H.tuned); precision 0
+// float64, 2 double-float.  Results are unchanged: the caps only move work
+// between CTAs, never the order of a dot product's terms.
+void hbs_autotune_solve(Handle& h, Hbs& H, int c, int precision, int reps);
 // Enqueues a kernel that only sleeps for about `us` microseconds (a fixed
 // number of __nanosleep calls, no waiting on anything), so that the host can
 // queue the launches that follow before the device reaches them: their event

@@ -134,13 +134,13 @@ struct LaunchPlan {
 // any of them.  Each step then narrows its own slice / chunk until its CTA
 // fits in shared memory.
 template <typename T>
-LaunchPlan plan_steps(Step<T>* const* steps, int count) {
+LaunchPlan plan_steps(Step<T>* const* steps, int count, const PlanKnobs& kn = PlanKnobs()) {
   int rmax = 1, cmax = 1;
   for (int i = 0; i < count; ++i) {
     rmax = std::max(rmax, steps[i]->rows);
     cmax = std::max(cmax, steps[i]->c);
   }
-  cmax = std::min(cmax, 64);
+  cmax = std::min(cmax, std::max(1, kn.cmax));
   auto whole = [](const Step<T>* s) { return s->out_p[0] == s->in_p[0]; };
   auto total = [&](int rm, int cm) {
     long long t = 0;
@@ -152,9 +152,9 @@ LaunchPlan plan_steps(Step<T>* const* steps, int count) {
     }
     return t;
   };
-  const long long target = 2LL * num_sms();
+  const long long target = (long long)std::max(1, kn.target) * num_sms();
   while (total(rmax, cmax) < target) {
-    if (rmax > 16) rmax = (rmax + 1) / 2;
+    if (rmax > std::max(8, kn.rmin)) rmax = (rmax + 1) / 2;
     else if (cmax > 1) cmax = (cmax + 1) / 2;
     else if (rmax > 8) rmax = (rmax + 1) / 2;
     else break;
@@ -285,9 +285,9 @@ __global__ void __launch_bounds__(kMaxThreads) step_kernel(const Step<T> s) {
 // launch is bracketed by timing events.
 template <typename T>
 void launch_step(cudaStream_t st, Step<T> s, const char* what, LaunchTimes* lt = nullptr,
-                 int lvl = 0, int kind = 0) {
+                 int lvl = 0, int kind = 0, const PlanKnobs& kn = PlanKnobs()) {
   Step<T>* one = &s;
-  const LaunchPlan p = plan_steps(&one, 1);
+  const LaunchPlan p = plan_steps(&one, 1, kn);
   auto kern = step_kernel<T>;
   ensure_smem(reinterpret_cast<const void*>(kern), p.smem);
   if (lt) lt->mark(st);

@@ -48,6 +48,7 @@ void hbs_make_sweep(Handle& h, Hbs& H) {
   SLU_REQUIRE(H.has_ulv, "HBS operator has no ULV factorisation");
   cudaStream_t st = h.stream;
   H.invalidate_plans();
+  H.tuned.clear();
   const int L = H.L;
   size_t mmax = 0;
   for (int t = 0; t + 1 < L; ++t) {

@@ -21,39 +21,166 @@
 #include "sweep_host.cuh"
 
 #include <algorithm>
+#include <array>
 
 namespace slu {
 
 using sweep::launch_step;
+
+namespace {
+
+template <typename T>
+struct StepRec {
+  sweep::Step<T> s;
+  const char* what;
+  int level, kind;
+};
+
+template <typename T> constexpr int type_code();
+template <> constexpr int type_code<double>() { return 0; }
+template <> constexpr int type_code<float>() { return 1; }
+template <> constexpr int type_code<dfloat>() { return 2; }
+
+// The 2L-1 launches of a mode-N solve, in order.
+template <typename T>
+std::vector<StepRec<T>> solve_steps(const Hbs& H, T* B, int ldb, int c, T* scratch,
+                                    size_t stride) {
+  const int L = H.L;
+  const int64_t* perm = H.perm.as<int64_t>();
+  T* ru = scratch;
+  T* P[4] = {scratch + stride, scratch + 2 * stride, scratch + 3 * stride, scratch + 4 * stride};
+  const std::vector<long long>& NN = H.NN;
+  std::vector<StepRec<T>> v;
+  const T* src = B;
+  int lds = ldb;
+  for (int t = 0; t + 1 < L; ++t) {
+    v.push_back({sweep::forward_step<T>(H, t, src, lds, t == 0 ? perm : nullptr, ru + NN[t] * c,
+                                        P[t & 1], c),
+                 "ulv_fwd_step", t, 0});
+    src = P[t & 1];
+    lds = c;
+  }
+  v.push_back({sweep::root_step<T>(H, src, lds, B, ldb, P[2], P[3], c), "ulv_root_step", L - 1,
+               1});
+  int in = 2;
+  for (int t = L - 2; t >= 0; --t) {
+    const int out = (in == 2) ? 0 : 2;
+    v.push_back({sweep::backward_step<T>(H, t, ru + NN[t] * c, P[in + 1], P[in], P[out],
+                                         P[out + 1], B, ldb, c),
+                 "ulv_bwd_step", t, 2});
+    in = out;
+  }
+  return v;
+}
+
+}  // namespace
 
 // B (N x c, caller ordering) <- A^{-1} B; scratch: 5 buffers of stride elements.
 template <typename T>
 void ulv_solve_fused(cudaStream_t st, const Hbs& H, T* B, int ldb, int c, T* scratch,
                      size_t stride, LaunchTimes* lt) {
   SLU_REQUIRE(H.has_sweep, "step operators not composed");
-  const int L = H.L;
-  const int64_t* perm = H.perm.as<int64_t>();
-  T* ru = scratch;
-  T* P[4] = {scratch + stride, scratch + 2 * stride, scratch + 3 * stride, scratch + 4 * stride};
-  const std::vector<long long>& NN = H.NN;
-  const T* src = B;
-  int lds = ldb;
-  for (int t = 0; t + 1 < L; ++t) {
-    launch_step(st, sweep::forward_step<T>(H, t, src, lds, t == 0 ? perm : nullptr,
-                                           ru + NN[t] * c, P[t & 1], c),
-                "ulv_fwd_step", lt, t, 0);
-    src = P[t & 1];
-    lds = c;
+  const std::vector<StepRec<T>> steps = solve_steps<T>(H, B, ldb, c, scratch, stride);
+  auto it = H.tuned.find({type_code<T>(), c});
+  const std::vector<PlanKnobs>* kn =
+      (it != H.tuned.end() && it->second.size() == steps.size()) ? &it->second : nullptr;
+  for (size_t i = 0; i < steps.size(); ++i)
+    launch_step(st, steps[i].s, steps[i].what, lt, steps[i].level, steps[i].kind,
+                kn ? (*kn)[i] : PlanKnobs());
+}
+
+namespace {
+
+// Coordinate descent on the whole solve: starting from the default caps,
+// each launch in turn tries every candidate cap set that changes its plan;
+// a candidate is kept when the median time of `reps` full solves (CUDA events
+// around the solve, programmatic dependent launch as in use) drops by more
+// than 0.5%.  Timing whole solves keeps the overlap between consecutive
+// launches in the measurement.  The buffers hold zeros: every launch reads
+// and writes finite values, and timing does not depend on the data.
+template <typename T>
+void autotune(Handle& h, Hbs& H, int c, int reps) {
+  cudaStream_t st = h.stream;
+  const size_t n = (size_t)H.N * c;
+  const size_t stride = ((sizeof(T) * n + 255) & ~size_t(255)) / sizeof(T);
+  DevBuf buf;
+  buf.alloc(sizeof(T) * 6 * stride, st);
+  SLU_CHECK_CUDA(cudaMemsetAsync(buf.p, 0, sizeof(T) * 6 * stride, st));
+  T* B = buf.as<T>();
+  const std::vector<StepRec<T>> steps = solve_steps<T>(H, B, c, c, B + stride, stride);
+  std::vector<PlanKnobs> cand;
+  for (int target : {1, 2, 4})
+    for (int rmin : {8, 16, 32, 64})
+      for (int cmax : {8, 16, 32, 64}) cand.push_back({target, rmin, cmax});
+  cudaEvent_t e0, e1;
+  SLU_CHECK_CUDA(cudaEventCreate(&e0));
+  SLU_CHECK_CUDA(cudaEventCreate(&e1));
+  std::vector<PlanKnobs> cur(steps.size());
+  auto measure = [&](const std::vector<PlanKnobs>& kn) {
+    std::vector<float> ms;
+    for (int r = 0; r < reps; ++r) {
+      SLU_CHECK_CUDA(cudaEventRecord(e0, st));
+      for (size_t i = 0; i < steps.size(); ++i)
+        launch_step(st, steps[i].s, steps[i].what, nullptr, 0, 0, kn[i]);
+      SLU_CHECK_CUDA(cudaEventRecord(e1, st));
+      SLU_CHECK_CUDA(cudaEventSynchronize(e1));
+      float x = 0.f;
+      SLU_CHECK_CUDA(cudaEventElapsedTime(&x, e0, e1));
+      ms.push_back(x);
+    }
+    std::nth_element(ms.begin(), ms.begin() + ms.size() / 2, ms.end());
+    return ms[ms.size() / 2];
+  };
+  try {
+    measure(cur);   // warm-up (kernel attributes, caches)
+    float best = measure(cur);
+    for (size_t i = 0; i < steps.size(); ++i) {
+      std::vector<std::array<long long, 4>> seen;
+      {
+        sweep::Step<T> t = steps[i].s;
+        sweep::Step<T>* one = &t;
+        const sweep::LaunchPlan p = sweep::plan_steps(&one, 1, cur[i]);
+        seen.push_back({t.rch, t.cpb, p.threads, p.ctas});
+      }
+      for (const PlanKnobs& k : cand) {
+        sweep::Step<T> t = steps[i].s;
+        sweep::Step<T>* one = &t;
+        const sweep::LaunchPlan p = sweep::plan_steps(&one, 1, k);
+        const std::array<long long, 4> key{t.rch, t.cpb, p.threads, p.ctas};
+        if (std::find(seen.begin(), seen.end(), key) != seen.end()) continue;
+        seen.push_back(key);
+        std::vector<PlanKnobs> trial = cur;
+        trial[i] = k;
+        const float ms = measure(trial);
+        if (ms < 0.995f * best) {
+          best = ms;
+          cur = trial;
+        }
+      }
+    }
+  } catch (...) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    throw;
   }
-  launch_step(st, sweep::root_step<T>(H, src, lds, B, ldb, P[2], P[3], c), "ulv_root_step", lt,
-              L - 1, 1);
-  int in = 2;
-  for (int t = L - 2; t >= 0; --t) {
-    const int out = (in == 2) ? 0 : 2;
-    launch_step(st, sweep::backward_step<T>(H, t, ru + NN[t] * c, P[in + 1], P[in], P[out],
-                                            P[out + 1], B, ldb, c),
-                "ulv_bwd_step", lt, t, 2);
-    in = out;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  SLU_CHECK_CUDA(cudaStreamSynchronize(st));
+  H.tuned[{type_code<T>(), c}] = cur;
+}
+
+}  // namespace
+
+void hbs_autotune_solve(Handle& h, Hbs& H, int c, int precision, int reps) {
+  SLU_REQUIRE(H.has_sweep, "step operators not composed");
+  SLU_REQUIRE(c >= 1 && reps >= 1, "bad arguments");
+  if (precision == 0) {
+    autotune<double>(h, H, c, reps);
+  } else if (precision == 2) {
+    if (!H.has_dfs) hbs_make_dfs(h, H);
+    autotune<dfloat>(h, H, c, reps);
+  } else {
+    throw Error(SLU_ERR_ARG, "autotune precision must be 0 (float64) or 2 (double-float)");
   }
 }
 

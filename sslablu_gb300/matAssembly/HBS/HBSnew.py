@@ -323,6 +323,20 @@ class HBSMAT:
         X, one = dv.prepare_rhs(b)
         return dv.finish(self._dev_solve(X, mode == "T"), b, one)
 
+    def autotune(self, nrhs, precision="f64", reps=9):
+        """Times the launches of a mode-N solve of `nrhs` columns under a set
+        of launch-plan caps and keeps the fastest per launch for later solves
+        of that width (results unchanged).  precision 'f64' (solve) or
+        'dfloat' (solve_dfloat).  Returns the caps chosen per launch as
+        (target CTAs per SM, row-slice floor, column cap) triples."""
+        code = {"f64": 0, "dfloat": 2}[precision]
+        cap = 256
+        knobs = (ctypes.c_int * (3 * cap))()
+        n = ctypes.c_int()
+        L.check(L.lib().slu_ulv_autotune(L.handle(), self._op, int(nrhs), code, int(reps), knobs,
+                                         cap, ctypes.byref(n)))
+        return [tuple(knobs[3 * i:3 * i + 3]) for i in range(min(n.value, cap))]
+
     # ------------------------------------------------------------ mixed precision
     def solve_dfloat(self, b):
         """Mode-N solve in double-float arithmetic on the float32 units (the

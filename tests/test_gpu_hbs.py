@@ -148,3 +148,24 @@ def test_dfloat_solve_uneven_ranks_and_chunks(k):
         xd = H.solve_dfloat(b)
         assert relerr(xd, H.solve(b)) < 1e-12, (N, k, c)
         assert relerr(H.matmat(xd), b) < 1e-12, (N, k, c)
+
+
+def test_autotuned_plans_keep_results():
+    """The launch-plan autotuner moves work between CTAs only: solves after
+    tuning (float64 and double-float) are bitwise equal to untuned ones."""
+    need_gpu()
+    from sslablu_gb300.matAssembly.HBS.HBSnew import HBSMAT
+    from sslablu_gb300.synthetic import random_hbs_factors
+    U, D, V, Nbvec = random_hbs_factors(32, 64, 4, quad=False, rng=np.random.default_rng(4),
+                                        shift=16.0)
+    H = HBSMAT().set_mats(U, D, V, list(Nbvec), fac=2)
+    H.compute_ULV()
+    b = np.random.default_rng(5).standard_normal((H.shape[0], 16))
+    x0, xd0 = H.solve(b), H.solve_dfloat(b)
+    kn = H.autotune(16, reps=3)
+    assert len(kn) == 2 * len(Nbvec) - 1 and all(len(k) == 3 and min(k) >= 1 for k in kn)
+    H.autotune(16, "dfloat", reps=3)
+    assert np.array_equal(H.solve(b), x0)
+    assert np.array_equal(H.solve_dfloat(b), xd0)
+    # a column's result does not depend on how many columns are solved with it
+    assert np.array_equal(H.solve(b[:, :7]), x0[:, :7])
