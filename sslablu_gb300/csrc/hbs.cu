@@ -430,7 +430,10 @@ void hbs_apply(Handle& h, Hbs& H, bool trans, const double* X, int ldx, double* 
                int ldy, int c) {
   cudaStream_t st = h.stream;
   SLU_REQUIRE(H.has_mats, "HBS factors not loaded");
-  if (!H.has_apply[trans ? 1 : 0]) hbs_make_apply(h, H, trans);
+  if (!H.has_apply[trans ? 1 : 0]) {
+    std::lock_guard<std::mutex> lock(H.lazy_mu);
+    if (!H.has_apply[trans ? 1 : 0]) hbs_make_apply(h, H, trans);
+  }
   const size_t elems = hbs_apply_scratch_elems(H, c);
   h.ws.reserve(8 * elems + 256, st);
   double* scratch = h.ws.take<double>(elems);

@@ -4,6 +4,8 @@
 #include "dfloat.cuh"
 #include "slablu_internal.cuh"
 
+#include <mutex>
+
 namespace slu {
 
 // Per-call scratch arena (grow-only, stream ordered).
@@ -109,7 +111,11 @@ struct Hbs {
   std::vector<long long> NN;       // NNvec, L+1 entries
   bool has_mats = false, has_ulv = false, has_f32 = false, has_df = false, has_dfs = false;
   bool has_sweep = false;   // step operators composed (hbs_make_sweep)
-  bool has_apply[2] = {false, false};   // apply operators, mode N / T (hbs_make_apply)
+  // apply operators, mode N / T (hbs_make_apply); composed on first use, so
+  // set only after the composing stream has finished (other threads may read
+  // them from their own streams right after)
+  std::atomic<bool> has_apply[2] = {false, false};
+  std::mutex lazy_mu;   // serialises first-use composition across threads
   // inner sweep of the mixed-precision refinement: 0 float32, 1 double-float
   int refine_inner = 1;
   int rk = 0, nsamples = 0;

@@ -14,8 +14,13 @@ from numpy's global RNG per compression, compressions in upstream's loop
 order), so seeded runs reproduce upstream's sketches.
 
 Beyond upstream: solve accepts (N,) and (N, nrhs) right-hand sides (upstream
-RB-HBS is 1-D only, omsdirectsolveHBS.py:503).
+RB-HBS is 1-D only, omsdirectsolveHBS.py:503); the compressions of one
+red-black level, which are independent, run concurrently on worker streams
+(sketches still drawn in upstream's order on the calling thread).
 """
+import concurrent.futures as cf
+import threading
+
 import numpy as np
 import torch
 
@@ -174,6 +179,10 @@ def _shape0(op):
     return int(op.shape[0])
 
 
+# concurrent compressions per red-black level (worker threads, one stream each)
+_LEVEL_WORKERS = 12
+
+
 # ---------------------------------------------------------------------------
 # HBS Thomas, omsdirectsolveHBS.py:189-351
 # ---------------------------------------------------------------------------
@@ -287,6 +296,36 @@ class RedBlackSolverHBS(DirectSolver):
         h.construct(self.rk if rk is None else rk, compute_ULV=True)
         return h
 
+    def _hbs_many(self, linops, rk):
+        """_hbs of every operator of a level: sketches drawn here in list
+        order (upstream's draw order), then sampling + compression + ULV of
+        all of them concurrently, one worker stream each."""
+        rk = self.rk if rk is None else rk
+        jobs = []
+        for op in linops:
+            h = HBSnew.HBSMAT(op, self.tree, self.quad)
+            jobs.append((h,) + h._sketches(rk))
+        if len(jobs) == 1:
+            h, Om, Psi = jobs[0]
+            h.construct_drawn(rk, Om, Psi)
+            return [h]
+        dev = torch.cuda.current_device()
+        torch.cuda.current_stream(dev).synchronize()   # inputs ready for every stream
+        local = threading.local()
+
+        def run(job):
+            h, Om, Psi = job
+            if getattr(local, "stream", None) is None:
+                local.stream = torch.cuda.Stream(dev)
+            torch.cuda.set_device(dev)
+            with torch.cuda.stream(local.stream):
+                h.construct_drawn(rk, Om, Psi)
+            local.stream.synchronize()
+            return h
+
+        with cf.ThreadPoolExecutor(max_workers=min(len(jobs), _LEVEL_WORKERS)) as ex:
+            return list(ex.map(run, jobs))
+
     def factorize(self, S_rk_list, T=None):
         """omsdirectsolveHBS.py:397-430."""
         m = _shape0(S_rk_list[0][0])
@@ -312,19 +351,20 @@ class RedBlackSolverHBS(DirectSolver):
     def _build_level(self, m, nS, lev, rk):
         """omsdirectsolveHBS.py:436-483 (same compression order)."""
         SiM, T, Th, SiP = lev
-        B_lin, T_new = [], []
+        B_lin = []
         for i in range(0, nS, 2):
             spm = SiP[(i - 1) % nS] if i > 0 else None
             smp = SiM[(i + 1) % nS] if i < nS - 1 else None
             tm = Th[(i - 1) % nS] if spm is not None else None
             tp = Th[(i + 1) % nS] if smp is not None else None
-            op = RB_linop(T[i], tm, tp, SiP[i], SiM[i], smp, spm)
-            T_new.append(self._hbs(op, rk))
-            B_lin.append(op)
-        A = [self._hbs(STS_linop(SiM[i], Th[(i - 1) % nS], SiM[(i - 1) % nS]), rk)
-             for i in range(0, nS, 2)]
-        C = [self._hbs(STS_linop(SiP[i], Th[(i + 1) % nS], SiP[(i + 1) % nS]), rk)
-             for i in range(0, nS, 2)]
+            B_lin.append(RB_linop(T[i], tm, tp, SiP[i], SiM[i], smp, spm))
+        A_lin = [STS_linop(SiM[i], Th[(i - 1) % nS], SiM[(i - 1) % nS]) for i in range(0, nS, 2)]
+        C_lin = [STS_linop(SiP[i], Th[(i + 1) % nS], SiP[(i + 1) % nS]) for i in range(0, nS, 2)]
+        # upstream compresses T_new, then A, then C (one sketch pair each, in
+        # that order); the compressions are independent of one another
+        hs = self._hbs_many(B_lin + A_lin + C_lin, rk)
+        k = len(B_lin)
+        T_new, A, C = hs[:k], hs[k:2 * k], hs[2 * k:]
         return (A, B_lin, T_new, C)
 
     def solve(self, rhs):

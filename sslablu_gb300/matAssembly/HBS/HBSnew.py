@@ -191,11 +191,18 @@ class HBSMAT:
 
     def constructHBS_ULV(self, rk):
         """HBSnew.py:211-295."""
-        tic = time.time()
         Om, Psi = self._sketches(rk)
+        self.construct_drawn(rk, Om, Psi)
+
+    def construct_drawn(self, rk, Om, Psi, compute_ULV=True):
+        """constructHBS_ULV with sketches already drawn (by _sketches): the
+        sampling Y = A Om, Z = A^T Psi and the compression, on torch's current
+        stream.  Lets a caller draw the sketches of several operators in the
+        upstream order and construct them concurrently."""
+        tic = time.time()
         Omd, Psid, Y, Z = self._sample(Om, Psi)
         self.tSample += time.time() - tic
-        self.compress_from_sketches(rk, Omd, Psid, Y, Z, compute_ULV=True)
+        self.compress_from_sketches(rk, Omd, Psid, Y, Z, compute_ULV=compute_ULV)
 
     def compute_ULV(self):
         """HBSnew.py:390-391."""
