@@ -293,14 +293,16 @@ void hbs_compress(Handle& h, Hbs& H, int Nb0, int rk, int s, const double* Om, c
       cur = nxt;
     }
     // ---- side A: QR of Om_blk^T with Y_blk rows carried along (compute_UV)
+    // (sides A and B run as one launch each: independent problems of the
+    // same shapes, so a level with few blocks fills twice as many SMs)
     copy_blocks(st, Nb, 8 * ns, Om_t, 8 * ns, WSA, 16 * ns);
     copy_blocks(st, Nb, 8 * ns, Y_t, 8 * ns, WSA + ns, 16 * ns);
-    panel_qr(st, s, n, 2 * n, WSA, s, 2 * ns, tauA, n, Nb);
+    if (root) panel_qr(st, s, n, 2 * n, WSA, s, 2 * ns, tauA, n, Nb);
     const double* YQ1A = WSA + ns;   // row-major n x n (ld s): Y_blk * Q_1
     if (!root) {
       copy_blocks(st, Nb, 8 * ns, Psi_t, 8 * ns, WSB, 16 * ns);
       copy_blocks(st, Nb, 8 * ns, Z_t, 8 * ns, WSB + ns, 16 * ns);
-      panel_qr(st, s, n, 2 * n, WSB, s, 2 * ns, tauB, n, Nb);
+      panel_qr2(st, s, n, 2 * n, WSA, WSB, s, 2 * ns, tauA, tauB, n, Nb);
       int* info = h.info.as<int>();
       // U, V: leading left singular vectors of Y_blk Q[:, s-n:s] (HBSnew.py:26-27)
       // or of Y_blk Q[:, n:s] (HBStorch.py:73-82)
@@ -311,17 +313,12 @@ void hbs_compress(Handle& h, Hbs& H, int Nb0, int rk, int s, const double* Om, c
         // wide n x jc block: its left singular vectors are those of R^T from
         // the QR of its transpose, which the panels already hold column-major
         // (column i = row i of the block); R^T is n x n lower triangular
-        panel_qr(st, jc, n, n, WSA + ns + j0, s, 2 * ns, tauA, n, Nb);
-        panel_qr(st, jc, n, n, WSB + ns + j0, s, 2 * ns, tauB, n, Nb);
-        jacobi_left_sv(st, n, n, WSA + ns + j0, s, 2 * ns, k, dp(l.U), k, (long long)n * k,
-                       nullptr, 0, Nb, info, true);
-        jacobi_left_sv(st, n, n, WSB + ns + j0, s, 2 * ns, k, dp(l.V), k, (long long)n * k,
-                       nullptr, 0, Nb, info, true);
+        panel_qr2(st, jc, n, n, WSA + ns + j0, WSB + ns + j0, s, 2 * ns, tauA, tauB, n, Nb);
+        jacobi_left_sv2(st, n, n, WSA + ns + j0, WSB + ns + j0, s, 2 * ns, k, dp(l.U), dp(l.V),
+                        k, (long long)n * k, Nb, info, true);
       } else {
-        jacobi_left_sv(st, n, jc, WSA + ns + j0, s, 2 * ns, k, dp(l.U), k, (long long)n * k,
-                       nullptr, 0, Nb, info);
-        jacobi_left_sv(st, n, jc, WSB + ns + j0, s, 2 * ns, k, dp(l.V), k, (long long)n * k,
-                       nullptr, 0, Nb, info);
+        jacobi_left_sv2(st, n, jc, WSA + ns + j0, WSB + ns + j0, s, 2 * ns, k, dp(l.U), dp(l.V),
+                        k, (long long)n * k, Nb, info);
       }
       // D = (Y - U U^T Y) pinv(Om) + U U^T ((Z - V V^T Z) pinv(Psi))^T  (HBSnew.py:48-62)
       const long long nk = (long long)n * k;

@@ -78,10 +78,14 @@ __device__ void panel_qr_dev(int m, int nfac, int ncol, double* a, int lda, doub
 
 __global__ void __launch_bounds__(512)
 panel_qr_kernel(int m, int nfac, int ncol, double* __restrict__ W, int ldw, long long sW,
-                double* __restrict__ tau, long long sTau, int use_smem) {
+                double* __restrict__ tau, long long sTau, int use_smem, double* __restrict__ W2,
+                double* __restrict__ tau2, int nsplit) {
   extern __shared__ double sm[];
-  double* w = W + blockIdx.x * sW;
-  double* t = tau + blockIdx.x * sTau;
+  // blocks nsplit.. work on the second batch (W2, tau2), same shapes
+  const bool second = (int)blockIdx.x >= nsplit;
+  const long long b = second ? blockIdx.x - nsplit : blockIdx.x;
+  double* w = (second ? W2 : W) + b * sW;
+  double* t = (second ? tau2 : tau) + b * sTau;
   if (use_smem) {
     for (long long e = threadIdx.x; e < (long long)m * ncol; e += blockDim.x) {
       int c = (int)(e / m), i = (int)(e % m);
@@ -149,7 +153,8 @@ constexpr int JAC_LANES = 4;
 __global__ void __launch_bounds__(1024)
 jacobi_kernel(int m, int n, const double* __restrict__ A, int lda, long long sA, int r,
               double* __restrict__ U, int ldu, long long sU, double* __restrict__ sv,
-              long long sS, int* info, int lower) {
+              long long sS, int* info, int lower, const double* __restrict__ A2,
+              double* __restrict__ U2, int nsplit) {
   extern __shared__ double sm[];
   const int np = n + (n & 1);            // even number of columns (a zero pad column)
   const int lda_s = m | 1;               // odd column stride
@@ -157,7 +162,10 @@ jacobi_kernel(int m, int n, const double* __restrict__ A, int lda, long long sA,
   double* nrm = a + (long long)lda_s * np;   // np
   int* order = reinterpret_cast<int*>(nrm + np);   // np
   __shared__ int s_rot;
-  A += blockIdx.x * sA;
+  // blocks nsplit.. work on the second batch (A2 -> U2), same shapes
+  const bool second = (int)blockIdx.x >= nsplit;
+  const long long bi = second ? blockIdx.x - nsplit : blockIdx.x;
+  A = (second ? A2 : A) + bi * sA;
   for (long long e = threadIdx.x; e < (long long)m * np; e += blockDim.x) {
     int c = (int)(e / m), i = (int)(e % m);
     // A row-major; with `lower`, only its lower triangle (c <= i) is read
@@ -270,8 +278,8 @@ jacobi_kernel(int m, int n, const double* __restrict__ A, int lda, long long sA,
     order[rk] = c;
   }
   __syncthreads();
-  double* Ub = U + blockIdx.x * sU;
-  double* svb = sv ? sv + blockIdx.x * sS : nullptr;
+  double* Ub = (second ? U2 : U) + bi * sU;
+  double* svb = (sv && !second) ? sv + bi * sS : nullptr;
   const double smax = nrm[order[0]];
   const double tiny = (smax > 0.0) ? smax * 1e-150 : 1e-300;
   // normalised leading columns; columns that carry no direction are
@@ -326,7 +334,22 @@ void panel_qr(cudaStream_t st, int m, int nfac, int ncol, double* W, int ldw, lo
   if (sm > 48 * 1024)
     SLU_CHECK_CUDA(cudaFuncSetAttribute(panel_qr_kernel,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-  panel_qr_kernel<<<batch, 512, sm, st>>>(m, nfac, ncol, W, ldw, sW, tau, sTau, use_smem);
+  panel_qr_kernel<<<batch, 512, sm, st>>>(m, nfac, ncol, W, ldw, sW, tau, sTau, use_smem, W,
+                                          tau, batch);
+  check_launch("panel_qr_kernel");
+}
+
+void panel_qr2(cudaStream_t st, int m, int nfac, int ncol, double* W, double* W2, int ldw,
+               long long sW, double* tau, double* tau2, long long sTau, int batch) {
+  if (batch <= 0 || m <= 0 || nfac <= 0) return;
+  size_t sm = (size_t)m * ncol * sizeof(double);
+  int use_smem = sm <= 200 * 1024;
+  if (!use_smem) sm = 0;
+  if (sm > 48 * 1024)
+    SLU_CHECK_CUDA(cudaFuncSetAttribute(panel_qr_kernel,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  panel_qr_kernel<<<2 * batch, 512, sm, st>>>(m, nfac, ncol, W, ldw, sW, tau, sTau, use_smem,
+                                              W2, tau2, batch);
   check_launch("panel_qr_kernel");
 }
 
@@ -352,7 +375,24 @@ void jacobi_left_sv(cudaStream_t st, int m, int n, const double* A, int lda, lon
                                         (int)sm));
   int threads = 32 * std::min(32, std::max(2, (np / 2 * JAC_LANES + 31) / 32));
   jacobi_kernel<<<batch, threads, sm, st>>>(m, n, A, lda, sA, r, U, ldu, sU, sv, sS, info,
-                                            lower ? 1 : 0);
+                                            lower ? 1 : 0, A, U, batch);
+  check_launch("jacobi_kernel");
+}
+
+void jacobi_left_sv2(cudaStream_t st, int m, int n, const double* A, const double* A2, int lda,
+                     long long sA, int r, double* U, double* U2, int ldu, long long sU, int batch,
+                     int* info, bool lower) {
+  if (batch <= 0 || r <= 0) return;
+  SLU_REQUIRE(r <= m, "jacobi: rank larger than rows");
+  int np = n + (n & 1);
+  size_t sm = (size_t)(m | 1) * np * sizeof(double) + np * sizeof(double) + np * sizeof(int);
+  SLU_REQUIRE(sm <= 220 * 1024, "jacobi: block too large for shared memory");
+  if (sm > 48 * 1024)
+    SLU_CHECK_CUDA(cudaFuncSetAttribute(jacobi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)sm));
+  int threads = 32 * std::min(32, std::max(2, (np / 2 * JAC_LANES + 31) / 32));
+  jacobi_kernel<<<2 * batch, threads, sm, st>>>(m, n, A, lda, sA, r, U, ldu, sU, nullptr, 0, info,
+                                                lower ? 1 : 0, A2, U2, batch);
   check_launch("jacobi_kernel");
 }
 

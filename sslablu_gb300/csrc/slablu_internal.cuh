@@ -114,6 +114,11 @@ void gemm_batched(cudaStream_t st, bool ta, bool tb, int M, int N, int K, T alph
 void panel_qr(cudaStream_t st, int m, int nfac, int ncol, double* W, int ldw,
               long long sW, double* tau, long long sTau, int batch);
 
+// Two panel factorisations of the same shapes in one launch (W, tau and
+// W2, tau2, batch blocks each).
+void panel_qr2(cudaStream_t st, int m, int nfac, int ncol, double* W, double* W2, int ldw,
+               long long sW, double* tau, double* tau2, long long sTau, int batch);
+
 // Apply the reflectors of a factored panel (m x k, column-major, ldv) to the
 // columns of C (m x nc, column-major, ldc): C <- Q C (left = false means
 // Q^T C).  Used to form Q explicitly from the identity.
@@ -128,6 +133,12 @@ void apply_q(cudaStream_t st, bool transpose, int m, int k, const double* V, int
 void jacobi_left_sv(cudaStream_t st, int m, int n, const double* A, int lda, long long sA,
                     int r, double* U, int ldu, long long sU, double* sv, long long sS,
                     int batch, int* info, bool lower = false);
+
+// Two Jacobi SVDs of the same shapes in one launch (A -> U and A2 -> U2,
+// batch blocks each; no singular values).
+void jacobi_left_sv2(cudaStream_t st, int m, int n, const double* A, const double* A2, int lda,
+                     long long sA, int r, double* U, double* U2, int ldu, long long sU, int batch,
+                     int* info, bool lower = false);
 
 // Batched triangular solve with an upper-triangular R_b (n x n): element
 // (i, j) of R_b at R_b[i*rRs + j*rCs] (row-major: rRs = ld, rCs = 1;
