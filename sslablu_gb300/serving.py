@@ -19,8 +19,11 @@ Scheduling (continuous batching):
   * at most one batch per operator is in flight (a factored operator's
     solve plan is not shared between streams), different operators overlap
     on different CUDA streams;
-  * each worker owns one CUDA stream and one library handle; a batch is
-    pinned host -> device copy, solve, device -> pinned host copy.
+  * each worker owns one CUDA stream, one library handle and two grow-only
+    pinned staging buffers; a batch is assembled column by column straight
+    into the input buffer (one host pass), copied host -> device, solved,
+    copied device -> the output buffer, and each request's columns are
+    copied out of it (one host pass).
 
 Grouped dispatch (``group_solve`` given): an idle worker takes the pending
 requests of every resident operator that has no batch in flight (each up to
@@ -213,29 +216,57 @@ class SolveServer:
             return None
         return [(best, self._take(best)[0])]
 
-    def _solve_one(self, key, reqs, stream):
+    @staticmethod
+    def _staging(stage, which, n):
+        """The worker's pinned float64 buffer `which` with room for n values
+        (grow-only)."""
+        buf = stage.get(which)
+        if buf is None or buf.numel() < n:
+            buf = torch.empty(max(n, 1 << 16), dtype=torch.float64, pin_memory=True)
+            stage[which] = buf
+        return buf[:n]
+
+    @staticmethod
+    def _assemble(dst, reqs):
+        """Writes the requests' blocks side by side into dst (N x cols)."""
+        if len(reqs) == 1:
+            dst[...] = reqs[0].B
+            return
+        c = 0
+        for r in reqs:
+            k = r.B.shape[1]
+            dst[:, c:c + k] = r.B
+            c += k
+
+    def _solve_one(self, key, reqs, stream, stage):
         res = self.resident[key]
+        N = reqs[0].B.shape[0]
+        cols = sum(r.B.shape[1] for r in reqs)
+        Bh = self._staging(stage, "in", N * cols).view(N, cols)
+        self._assemble(Bh.numpy(), reqs)
         with torch.cuda.stream(stream):
-            Bh = torch.from_numpy(np.concatenate([r.B for r in reqs], axis=1)).pin_memory()
             Bd = Bh.to("cuda", non_blocking=True)
             Xd = res.solve(Bd)
-            Xh = torch.empty(Xd.shape, dtype=Xd.dtype, pin_memory=True)
+            Xh = self._staging(stage, "out", N * cols).view(N, cols)
             Xh.copy_(Xd, non_blocking=True)
             stream.synchronize()
         return [Xh.numpy()]
 
-    def _solve_group(self, job, stream):
-        blocks = [np.concatenate([r.B for r in reqs], axis=1) for _, reqs in job]
+    def _solve_group(self, job, stream, stage):
         layout, off = [], 0
-        for b in blocks:
-            layout.append((off, b.shape[0], b.shape[1]))
-            off += b.size
+        for _, reqs in job:
+            n, c = reqs[0].B.shape[0], sum(r.B.shape[1] for r in reqs)
+            layout.append((off, n, c))
+            off += n * c
+        flat_in = self._staging(stage, "in", off)
+        fin = flat_in.numpy()
+        for (o, n, c), (_, reqs) in zip(layout, job):
+            self._assemble(fin[o:o + n * c].reshape(n, c), reqs)
         ops = [self.resident[k].op for k, _ in job]
         with torch.cuda.stream(stream):
-            Bh = torch.from_numpy(np.concatenate([b.ravel() for b in blocks])).pin_memory()
-            Bd = Bh.to("cuda", non_blocking=True)
+            Bd = flat_in.to("cuda", non_blocking=True)
             Xd = self.group_solve(ops, Bd, layout)
-            Xh = torch.empty(Xd.shape, dtype=Xd.dtype, pin_memory=True)
+            Xh = self._staging(stage, "out", off)
             Xh.copy_(Xd, non_blocking=True)
             stream.synchronize()
         flat = Xh.numpy()
@@ -243,6 +274,7 @@ class SolveServer:
 
     def _worker(self, w):
         stream = torch.cuda.Stream()
+        stage = {}
         while True:
             job = self._jobs.get()
             if job is None:
@@ -250,9 +282,9 @@ class SolveServer:
             t_start = self._now()
             try:
                 if self.group_solve is not None:
-                    Xs, err = self._solve_group(job, stream), None
+                    Xs, err = self._solve_group(job, stream, stage), None
                 else:
-                    Xs, err = self._solve_one(job[0][0], job[0][1], stream), None
+                    Xs, err = self._solve_one(job[0][0], job[0][1], stream, stage), None
             except Exception as e:   # the requests complete with the error
                 Xs, err = [None] * len(job), e
             t_done = self._now()
