@@ -251,6 +251,22 @@ int slu_ulv_solve(slu_handle_t h, slu_hbs_t op, double* B, int ldb, int nrhs, in
   });
 }
 
+int slu_ulv_solve_into(slu_handle_t h, slu_hbs_t op, const double* X, int ldx, double* Y,
+                       int ldy, int nrhs) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h && op && X && Y, "null argument");
+    SLU_REQUIRE(nrhs >= 1 && ldx >= nrhs && ldy >= nrhs, "bad right-hand side shape");
+    const slu::Hbs& H = op->H;
+    SLU_REQUIRE(H.has_ulv, "HBS operator has no ULV factorisation");
+    cudaStream_t st = h->h.stream;
+    const size_t bytes = slu::hbs_solve_scratch_bytes(H, nrhs, sizeof(double));
+    h->h.ws.reserve(bytes + 256, st);
+    double* scratch = h->h.ws.take<double>(bytes / sizeof(double));
+    const size_t stride = ((sizeof(double) * (size_t)H.N * nrhs + 255) & ~size_t(255)) / 8;
+    slu::ulv_solve_fused<double>(st, H, Y, ldy, nrhs, scratch, stride, nullptr, X, ldx);
+  });
+}
+
 int slu_hbs_prepare_f32(slu_handle_t h, slu_hbs_t op) {
   return guard(h, [&] {
     SLU_REQUIRE(h && op, "null argument");

@@ -181,10 +181,12 @@ struct LaunchTimes {
 };
 
 // Mode-N solve with one fused kernel per level and sweep (ulv_solve.cu);
-// scratch: five buffers of `stride` elements.
+// scratch: five buffers of `stride` elements.  With X given, the right-hand
+// sides are read from X (ld ldx) and B only receives the solution.
 template <typename T>
 void ulv_solve_fused(cudaStream_t st, const Hbs& H, T* B, int ldb, int c, T* scratch,
-                     size_t stride, LaunchTimes* times = nullptr);
+                     size_t stride, LaunchTimes* times = nullptr, const T* X = nullptr,
+                     int ldx = 0);
 // Times every launch of the mode-N solve for `c` right-hand sides under a set
 // of plan caps and keeps the fastest per launch (H.tuned); precision 0
 // float64, 2 double-float.  Results are unchanged: the caps only move work

@@ -41,18 +41,20 @@ template <> constexpr int type_code<double>() { return 0; }
 template <> constexpr int type_code<float>() { return 1; }
 template <> constexpr int type_code<dfloat>() { return 2; }
 
-// The 2L-1 launches of a mode-N solve, in order.
+// The 2L-1 launches of a mode-N solve, in order: the right-hand sides are
+// read from X (ld ldx) and the solution written to B (ld ldb); X == B solves
+// in place.
 template <typename T>
-std::vector<StepRec<T>> solve_steps(const Hbs& H, T* B, int ldb, int c, T* scratch,
-                                    size_t stride) {
+std::vector<StepRec<T>> solve_steps(const Hbs& H, const T* X, int ldx, T* B, int ldb, int c,
+                                    T* scratch, size_t stride) {
   const int L = H.L;
   const int64_t* perm = H.perm.as<int64_t>();
   T* ru = scratch;
   T* P[4] = {scratch + stride, scratch + 2 * stride, scratch + 3 * stride, scratch + 4 * stride};
   const std::vector<long long>& NN = H.NN;
   std::vector<StepRec<T>> v;
-  const T* src = B;
-  int lds = ldb;
+  const T* src = X;
+  int lds = ldx;
   for (int t = 0; t + 1 < L; ++t) {
     v.push_back({sweep::forward_step<T>(H, t, src, lds, t == 0 ? perm : nullptr, ru + NN[t] * c,
                                         P[t & 1], c),
@@ -62,6 +64,11 @@ std::vector<StepRec<T>> solve_steps(const Hbs& H, T* B, int ldb, int c, T* scrat
   }
   v.push_back({sweep::root_step<T>(H, src, lds, B, ldb, P[2], P[3], c), "ulv_root_step", L - 1,
                1});
+  if (L == 1 && X != B) {   // one-level tree: the root reads X, writes B
+    sweep::Step<T>& r = v.back().s;
+    r.in_p[0] = X;
+    r.in_ld[0] = ldx;
+  }
   int in = 2;
   for (int t = L - 2; t >= 0; --t) {
     const int out = (in == 2) ? 0 : 2;
@@ -78,9 +85,13 @@ std::vector<StepRec<T>> solve_steps(const Hbs& H, T* B, int ldb, int c, T* scrat
 // B (N x c, caller ordering) <- A^{-1} B; scratch: 5 buffers of stride elements.
 template <typename T>
 void ulv_solve_fused(cudaStream_t st, const Hbs& H, T* B, int ldb, int c, T* scratch,
-                     size_t stride, LaunchTimes* lt) {
+                     size_t stride, LaunchTimes* lt, const T* X, int ldx) {
   SLU_REQUIRE(H.has_sweep, "step operators not composed");
-  const std::vector<StepRec<T>> steps = solve_steps<T>(H, B, ldb, c, scratch, stride);
+  if (!X) {
+    X = B;
+    ldx = ldb;
+  }
+  const std::vector<StepRec<T>> steps = solve_steps<T>(H, X, ldx, B, ldb, c, scratch, stride);
   auto it = H.tuned.find({type_code<T>(), c});
   const std::vector<PlanKnobs>* kn =
       (it != H.tuned.end() && it->second.size() == steps.size()) ? &it->second : nullptr;
@@ -107,7 +118,7 @@ void autotune(Handle& h, Hbs& H, int c, int reps) {
   buf.alloc(sizeof(T) * 6 * stride, st);
   SLU_CHECK_CUDA(cudaMemsetAsync(buf.p, 0, sizeof(T) * 6 * stride, st));
   T* B = buf.as<T>();
-  const std::vector<StepRec<T>> steps = solve_steps<T>(H, B, c, c, B + stride, stride);
+  const std::vector<StepRec<T>> steps = solve_steps<T>(H, B, c, B, c, c, B + stride, stride);
   std::vector<PlanKnobs> cand;
   for (int target : {1, 2, 4})
     for (int rmin : {8, 16, 32, 64})
@@ -196,11 +207,11 @@ void enqueue_device_lead(cudaStream_t st, int us) {
 }
 
 template void ulv_solve_fused<double>(cudaStream_t, const Hbs&, double*, int, int, double*, size_t,
-                                      LaunchTimes*);
+                                      LaunchTimes*, const double*, int);
 template void ulv_solve_fused<float>(cudaStream_t, const Hbs&, float*, int, int, float*, size_t,
-                                     LaunchTimes*);
+                                     LaunchTimes*, const float*, int);
 template void ulv_solve_fused<dfloat>(cudaStream_t, const Hbs&, dfloat*, int, int, dfloat*, size_t,
-                                      LaunchTimes*);
+                                      LaunchTimes*, const dfloat*, int);
 
 // ---------------------------------------------------------------- double-float sweep
 namespace {

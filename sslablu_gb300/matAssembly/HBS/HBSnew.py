@@ -295,7 +295,13 @@ class HBSMAT:
         return Y
 
     def _dev_solve(self, X, trans=False):
-        B = dv.as_2d(X).clone().contiguous()
+        X = dv.as_2d(X).contiguous()
+        if not trans:   # out of place: no copy of the right-hand sides
+            Y = torch.empty_like(X)
+            L.check(L.lib().slu_ulv_solve_into(L.handle(), self._op, L.ptr(X), X.shape[1],
+                                               L.ptr(Y), Y.shape[1], X.shape[1]))
+            return Y
+        B = X.clone()
         L.check(L.lib().slu_ulv_solve(L.handle(), self._op, L.ptr(B), B.shape[1], B.shape[1],
                                       int(trans)))
         return B

@@ -169,3 +169,29 @@ def test_autotuned_plans_keep_results():
     assert np.array_equal(H.solve_dfloat(b), xd0)
     # a column's result does not depend on how many columns are solved with it
     assert np.array_equal(H.solve(b[:, :7]), x0[:, :7])
+
+
+def test_out_of_place_solve_matches_in_place():
+    """slu_ulv_solve_into reads X and writes Y (leading dimensions wider than
+    the column count; one-level and multi-level trees): X is unchanged and Y
+    equals the in-place solve bitwise."""
+    need_gpu()
+    import torch
+    from sslablu_gb300 import _lib as L
+    from sslablu_gb300.matAssembly.HBS.HBSnew import HBSMAT
+    from sslablu_gb300.synthetic import random_hbs_factors
+    for Lv in (1, 4):
+        U, D, V, Nbvec = random_hbs_factors(16, 64, Lv, quad=False,
+                                            rng=np.random.default_rng(Lv), shift=16.0)
+        H = HBSMAT().set_mats(U, D, V, list(Nbvec), fac=2)
+        H.compute_ULV()
+        N, c = H.shape[0], 5
+        Xw = torch.from_numpy(np.random.default_rng(9).standard_normal((N, 8))).cuda()
+        X0 = Xw.clone()
+        Yw = torch.full((N, 7), 7.0, dtype=torch.float64, device="cuda")
+        L.check(L.lib().slu_ulv_solve_into(L.handle(), H._op, L.ptr(Xw), 8, L.ptr(Yw), 7, c))
+        B = Xw[:, :c].clone().contiguous()
+        L.check(L.lib().slu_ulv_solve(L.handle(), H._op, L.ptr(B), c, c, 0))
+        torch.cuda.synchronize()
+        assert torch.equal(Xw, X0)
+        assert torch.equal(Yw[:, :c], B) and bool((Yw[:, c:] == 7.0).all())
