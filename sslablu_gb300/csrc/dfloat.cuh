@@ -104,6 +104,40 @@ __device__ __forceinline__ dfloat __ldcg(const dfloat* p) {
   return dfloat(v.x, v.y);
 }
 
+// Dot-product accumulators.  For float and double the accumulator is the
+// value itself.  For double-float, the sum is kept unnormalised (Ogita, Rump
+// and Oishi's Dot2 scheme, with the cross terms of double-float inputs): the
+// exact product's high part goes through TwoSum into h, every error term
+// into l, and one renormalisation at the end gives the double-float result
+// -- 12 float32 operations per term instead of 15.
+template <typename T>
+struct DotAcc {
+  T v;
+  __device__ __forceinline__ void zero() { v = T(0); }
+  __device__ __forceinline__ void add(T a, T b) { v = fma(a, b, v); }
+  __device__ __forceinline__ T value() const { return v; }
+};
+template <>
+struct DotAcc<dfloat> {
+  float h, l;
+  __device__ __forceinline__ void zero() { h = l = 0.f; }
+  __device__ __forceinline__ void add(dfloat a, dfloat b) {
+    const float p = __fmul_rn(a.h, b.h);
+    float pe = __fmaf_rn(a.h, b.h, -p);
+    pe = __fmaf_rn(a.h, b.l, __fmaf_rn(a.l, b.h, pe));
+    float s, e;
+    dfops::two_sum(h, p, s, e);
+    h = s;
+    l = __fadd_rn(l, __fadd_rn(e, pe));
+  }
+  // TwoSum, not the fast form: after cancellation |l| may exceed |h|
+  __device__ __forceinline__ dfloat value() const {
+    float hh, ll;
+    dfops::two_sum(h, l, hh, ll);
+    return dfloat(hh, ll);
+  }
+};
+
 __device__ __forceinline__ dfloat to_dfloat(double x) {
   const float h = __double2float_rn(x);
   return dfloat(h, __double2float_rn(x - (double)h));

@@ -25,6 +25,8 @@
 
 #include <cstdint>
 
+#include "dfloat.cuh"
+
 namespace slu {
 namespace sweep {
 
@@ -153,22 +155,25 @@ __device__ __forceinline__ void product(const Step<T>& s, const T* Ss, const T* 
       zp[r] = zT + cc[r] * pz + part;
       if (base + r * stride < items) nact = r + 1;   // warp-uniform
     }
-    T acc[R];
+    DotAcc<T> da[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) acc[r] = T(0);
+    for (int r = 0; r < R; ++r) da[r].zero();
     if (nact == R) {
 #pragma unroll 4
       for (int m = 0; m < nterm; ++m) {
 #pragma unroll
-        for (int r = 0; r < R; ++r) acc[r] = fma(sp[r][m * KS], zp[r][m * KS], acc[r]);
+        for (int r = 0; r < R; ++r) da[r].add(sp[r][m * KS], zp[r][m * KS]);
       }
     } else {
       for (int m = 0; m < nterm; ++m) {
 #pragma unroll
         for (int r = 0; r < R; ++r)
-          if (r < nact) acc[r] = fma(sp[r][m * KS], zp[r][m * KS], acc[r]);
+          if (r < nact) da[r].add(sp[r][m * KS], zp[r][m * KS]);
       }
     }
+    T acc[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) acc[r] = da[r].value();
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       if (r < nact) {
