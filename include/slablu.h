@@ -185,6 +185,14 @@ int slu_hbs_set_null_space(slu_hbs_t op, int mode);
  *     be NULL, else count entries) each member's worst relative residual. */
 int slu_ulv_solve_grouped(slu_handle_t h, int count, const slu_hbs_t* ops, double* const* B,
                           const int* ldb, const int* nrhs);
+/* Grouped apply: Y[i] (N_i x nrhs[i], ld ldy[i]) <- A_i X[i] (trans[i] = 0)
+ * or A_i^T X[i] (trans[i] = 1), one launch per tree step for the whole group
+ * (the batched form of HBSMAT.matmat / rmatmat, matAssembly/HBS/
+ * HBSnew.py:308-350); every member's result equals its own slu_hbs_apply
+ * bitwise.  Host arrays of count entries; nrhs[i] == 0 skips a member. */
+int slu_hbs_apply_grouped(slu_handle_t h, int count, const slu_hbs_t* ops, const int* trans,
+                          const double* const* X, const int* ldx, double* const* Y,
+                          const int* ldy, const int* nrhs);
 int slu_refine_grouped(slu_handle_t h, int count, const slu_hbs_t* ops, const double* const* B,
                        const int* ldb, double* const* X, const int* ldx, const int* nrhs,
                        double tol, int maxit, int* iters_out, double* relres_out);

@@ -47,6 +47,7 @@ SIGNATURES = {
     "slu_ulv_autotune": [P, P, c_int, c_int, c_int, P, c_int, P],
     "slu_hbs_set_refine_inner": [P, c_int],
     "slu_ulv_solve_timed": [P, P, P, c_int, c_int, P, P, P, c_int, P],
+    "slu_hbs_apply_grouped": [P, c_int, P, P, P, P, P, P, P],
     "slu_refine_grouped": [P, c_int, P, P, P, P, P, P, c_double, c_int, P, P],
     "slu_hbs_info": [P, P, P, P, P, P],
     "slu_hbs_export": [P, P, c_int, c_int, P, c_size_t, P],

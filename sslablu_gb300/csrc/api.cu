@@ -342,6 +342,16 @@ int slu_ulv_solve_grouped(slu_handle_t h, int count, const slu_hbs_t* ops, doubl
   });
 }
 
+int slu_hbs_apply_grouped(slu_handle_t h, int count, const slu_hbs_t* ops, const int* trans,
+                          const double* const* X, const int* ldx, double* const* Y,
+                          const int* ldy, const int* nrhs) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h, "null argument");
+    std::vector<slu::Hbs*> H = group_ops(count, ops);
+    slu::hbs_apply_grouped(h->h, count, H.data(), trans, X, ldx, Y, ldy, nrhs);
+  });
+}
+
 int slu_refine_grouped(slu_handle_t h, int count, const slu_hbs_t* ops, const double* const* B,
                        const int* ldb, double* const* X, const int* ldx, const int* nrhs,
                        double tol, int maxit, int* iters_out, double* relres_out) {

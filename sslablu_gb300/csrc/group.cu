@@ -300,6 +300,62 @@ size_t blob_bound(size_t payload, int arrays) { return payload + 256 * (size_t)(
 
 inline size_t round64(size_t n) { return (n + 63) & ~size_t(63); }
 
+// Step tables of a grouped float64 apply Y[i] = op_i(A_i) X[i] (mode N or T
+// per member; the steps of hbs_apply_fused, tree step by tree step).
+void build_apply64(const std::vector<const Hbs*>& H, const std::vector<int>& tr,
+                   const std::vector<int>& c, const std::vector<const double*>& X,
+                   const std::vector<int>& ldx, const std::vector<double*>& Y,
+                   const std::vector<int>& ldy, const std::vector<ApplyBufs<double>>& buf,
+                   StepTable<double>& tab) {
+  const int m = (int)H.size();
+  int maxL = 0;
+  for (int i = 0; i < m; ++i) maxL = std::max(maxL, H[i]->L);
+  auto up = [&](const Level& l, int i) { return (tr[i] ? l.AupT : l.Aup).as<double>(); };
+  auto dn = [&](const Level& l, int i) { return (tr[i] ? l.AdnT : l.Adn).as<double>(); };
+  std::vector<sweep::Step<double>> v;
+  for (int t = 0; t + 1 < maxL; ++t) {
+    v.clear();
+    for (int i = 0; i < m; ++i) {
+      if (H[i]->L < t + 2) continue;
+      const Level& l = H[i]->lv[t];
+      v.push_back(sweep::up_step<double>(l, up(l, i), t == 0 ? X[i] : buf[i].VV[t],
+                                         t == 0 ? ldx[i] : c[i],
+                                         t == 0 ? H[i]->perm.as<int64_t>() : nullptr,
+                                         buf[i].VV[t + 1], c[i]));
+    }
+    tab.add(v);
+  }
+  v.clear();
+  for (int i = 0; i < m; ++i) {
+    const int L = H[i]->L;
+    const Level& r = H[i]->lv[L - 1];
+    const int64_t* perm = H[i]->perm.as<int64_t>();
+    if (L == 1)
+      v.push_back(sweep::down_step<double>(r, dn(r, i), true, X[i], ldx[i], perm, nullptr, Y[i],
+                                           ldy[i], perm, c[i]));
+    else
+      v.push_back(sweep::down_step<double>(r, dn(r, i), true, buf[i].VV[L - 1], c[i], nullptr,
+                                           nullptr, buf[i].u[0], c[i], nullptr, c[i]));
+  }
+  tab.add(v);
+  for (int t = maxL - 2; t >= 0; --t) {
+    v.clear();
+    for (int i = 0; i < m; ++i) {
+      const int L = H[i]->L;
+      if (L < t + 2) continue;
+      const Level& l = H[i]->lv[t];
+      const int cur = (L - 2 - t) & 1;
+      const bool leaf = t == 0;
+      const int64_t* perm = leaf ? H[i]->perm.as<int64_t>() : nullptr;
+      v.push_back(sweep::down_step<double>(l, dn(l, i), false, leaf ? X[i] : buf[i].VV[t],
+                                           leaf ? ldx[i] : c[i], perm, buf[i].u[cur],
+                                           leaf ? Y[i] : buf[i].u[cur ^ 1], leaf ? ldy[i] : c[i],
+                                           perm, c[i]));
+    }
+    tab.add(v);
+  }
+}
+
 }  // namespace
 
 void hbs_solve_grouped(Handle& h, int count, Hbs* const* ops, double* const* B, const int* ldb,
@@ -342,6 +398,57 @@ void hbs_solve_grouped(Handle& h, int count, Hbs* const* ops, double* const* B, 
   }
   StepTable<double> steps;
   build_solve<double>(H, cm, Bm, ldm, buf, steps);
+  Blob blob;
+  const size_t at = blob.put(steps.segs);
+  SLU_REQUIRE(blob.host.size() <= plan.bytes[0], "task table overflow");
+  upload(h, blob, dtab);
+  launch_solve<double>(st, steps, reinterpret_cast<const StepSeg<double>*>(dtab + at));
+}
+
+void hbs_apply_grouped(Handle& h, int count, Hbs* const* ops, const int* trans,
+                       const double* const* X, const int* ldx, double* const* Y, const int* ldy,
+                       const int* c) {
+  SLU_REQUIRE(count >= 0 && (count == 0 || (ops && trans && X && ldx && Y && ldy && c)),
+              "null argument");
+  std::vector<const Hbs*> H;
+  std::vector<int> tr, cm, lx, ly;
+  std::vector<const double*> Xm;
+  std::vector<double*> Ym;
+  for (int i = 0; i < count; ++i) {
+    SLU_REQUIRE(ops[i], "null operator");
+    SLU_REQUIRE(c[i] >= 0, "bad right-hand-side count");
+    if (c[i] == 0) continue;
+    SLU_REQUIRE(X[i] && Y[i] && ldx[i] >= c[i] && ldy[i] >= c[i], "bad right-hand side");
+    Hbs& Hi = *ops[i];
+    SLU_REQUIRE(Hi.has_mats, "HBS factors not loaded");
+    const int t = trans[i] ? 1 : 0;
+    if (!Hi.has_apply[t]) {
+      std::lock_guard<std::mutex> lock(Hi.lazy_mu);
+      if (!Hi.has_apply[t]) hbs_make_apply(h, Hi, t == 1);
+    }
+    H.push_back(&Hi);
+    tr.push_back(t);
+    cm.push_back(c[i]);
+    Xm.push_back(X[i]);
+    lx.push_back(ldx[i]);
+    Ym.push_back(Y[i]);
+    ly.push_back(ldy[i]);
+  }
+  const int m = (int)H.size();
+  if (m == 0) return;
+  cudaStream_t st = h.stream;
+  size_t nseg = 0;
+  for (const Hbs* x : H) nseg += 2 * (size_t)x->L;
+  Plan plan;
+  plan.add(blob_bound(nseg * sizeof(StepSeg<double>), 1));
+  for (int i = 0; i < m; ++i) plan.add(8 * hbs_apply_scratch_elems(*H[i], cm[i]));
+  h.ws.reserve(plan.total(), st);
+  char* dtab = h.ws.take<char>(plan.bytes[0]);
+  std::vector<ApplyBufs<double>> buf(m);
+  for (int i = 0; i < m; ++i)
+    buf[i] = carve_apply(*H[i], cm[i], h.ws.take<double>(hbs_apply_scratch_elems(*H[i], cm[i])));
+  StepTable<double> steps;
+  build_apply64(H, tr, cm, Xm, lx, Ym, ly, buf, steps);
   Blob blob;
   const size_t at = blob.put(steps.segs);
   SLU_REQUIRE(blob.host.size() <= plan.bytes[0], "task table overflow");

@@ -260,6 +260,11 @@ struct FacPtr<dfloat> {
 
 // Grouped solves over many operators (group.cu): one launch per tree step for
 // the whole group.  B[i] is N_i x c[i] row-major with leading dimension ldb[i].
+// Grouped apply Y[i] = A_i X[i] (trans[i] = 0) or A_i^T X[i]: one launch per
+// tree step for the whole group.
+void hbs_apply_grouped(Handle& h, int count, Hbs* const* ops, const int* trans,
+                       const double* const* X, const int* ldx, double* const* Y, const int* ldy,
+                       const int* c);
 void hbs_solve_grouped(Handle& h, int count, Hbs* const* ops, double* const* B, const int* ldb,
                        const int* c);
 // Mixed-precision refinement of the group; iters is the common iteration

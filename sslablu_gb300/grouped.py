@@ -49,6 +49,32 @@ def solve_grouped_device(ops, Bs, precision="f64", tol=1e-10, maxit=10, Xs=None)
     return Xs, it.value, list(np.frombuffer(rr, dtype=np.float64))
 
 
+def apply_grouped(ops, Xs, trans=False, Ys=None):
+    """Grouped apply on contiguous float64 CUDA tensors: Ys[i] = A_i Xs[i]
+    (or A_i^T Xs[i] where ``trans`` -- one flag, or one per member -- is
+    true), one kernel launch per tree step for the whole group.  Each result
+    equals the member's own HBSMAT.matmat / rmatmat.  Returns Ys."""
+    n = len(ops)
+    if Ys is None:
+        Ys = [torch.empty_like(t) for t in Xs]
+    if n == 0:
+        return Ys
+    tr = list(trans) if isinstance(trans, (list, tuple)) else [bool(trans)] * n
+    for H, X, Y in zip(ops, Xs, Ys):
+        for t in (X, Y):
+            if t.dtype != torch.float64 or not t.is_cuda or not t.is_contiguous() or t.dim() != 2:
+                raise ValueError("operands must be contiguous 2-D float64 CUDA tensors")
+        if X.shape[0] != H.shape[1] or Y.shape != X.shape:
+            raise ValueError("operand shape does not match the operator")
+    op_arr = (ctypes.c_void_p * n)(*[H._op for H in ops])
+    tra = (ctypes.c_int * n)(*[int(bool(t)) for t in tr])
+    xp = (ctypes.c_void_p * n)(*[t.data_ptr() for t in Xs])
+    yp = (ctypes.c_void_p * n)(*[t.data_ptr() for t in Ys])
+    ld = (ctypes.c_int * n)(*[t.shape[1] for t in Xs])
+    L.check(L.lib().slu_hbs_apply_grouped(L.handle(), n, op_arr, tra, xp, ld, yp, ld, ld))
+    return Ys
+
+
 def solve_grouped(systems, precision="f64", tol=1e-10, maxit=10):
     """Solve A_i x_i = b_i for every (HBSMAT A_i, b_i) in ``systems``.
 

@@ -117,3 +117,27 @@ def test_per_level_solve_equals_grouped_for_uneven_ranks(k):
         x_grp = solve_grouped([(H, b)])[0]
         assert relerr(H.matmat(x_grp), b) < 1e-12, (N, k)
         assert relerr(x_solo, x_grp) < 1e-13, (N, k)
+
+
+def test_grouped_apply_equals_solo():
+    """Grouped applies (mode N and T mixed, uneven sizes and depths, a
+    one-level member) equal each member's own matmat / rmatmat bitwise."""
+    need_gpu()
+    import torch
+    from sslablu_gb300.grouped import apply_grouped
+    from sslablu_gb300.matAssembly.HBS.HBSnew import HBSMAT
+    from sslablu_gb300.synthetic import random_hbs_factors
+    ops = []
+    for N, k in ((64, 16), (256, 24), (1024, 32), (512, 16)):
+        Lv = int(np.log2(N // 64)) + 1
+        U, D, V, Nbvec = random_hbs_factors(k, 64, Lv, quad=False,
+                                            rng=np.random.default_rng(N + k), shift=4.0)
+        ops.append(HBSMAT().set_mats(U, D, V, list(Nbvec), fac=2))
+    rng = np.random.default_rng(3)
+    Xs = [torch.from_numpy(rng.standard_normal((H.shape[0], c))).cuda()
+          for H, c in zip(ops, (3, 8, 1, 5))]
+    trans = [False, True, False, True]
+    Ys = apply_grouped(ops, Xs, trans)
+    for H, X, Y, t in zip(ops, Xs, Ys, trans):
+        ref = H._dev_apply(X, t)
+        assert torch.equal(Y, ref)
