@@ -13,7 +13,10 @@
 //   G2 = SiP_i [T_{i+1}^{-1} SiM_{i+1} | T_{i+1}^{-1} SiP_{i+1}]
 //   A_i = -G1[:, :m],  B_i = T_i - G1[:, m:] - G2[:, :m],  C_i = -G2[:, m:].
 // Upstream rebuilds each T from its LU factors (omsdirectsolve.py:31-46,314);
-// this keeps T itself, the same matrix up to rounding.
+// this keeps T itself, the same matrix up to rounding.  The solve phase
+// applies the pivot-block inverses (formed once from the LU factors) as
+// GEMMs instead of triangular sweeps: the same result to rounding, and every
+// block solve parallel over the block's rows.
 #include "tridiag.cuh"
 
 #include <algorithm>
@@ -23,6 +26,17 @@ namespace slu {
 namespace {
 inline double* dp(const DevBuf& b) { return b.as<double>(); }
 inline int* ip(const DevBuf& b) { return b.as<int>(); }
+
+// Inv_b = T_b^{-1} from the LU factors of nS blocks (m x m each): a batched
+// LU solve against the identity.
+void make_inverses(cudaStream_t st, int m, const DevBuf& LU, const DevBuf& piv, int nS,
+                   DevBuf& Inv) {
+  const size_t mm = (size_t)m * m;
+  Inv.alloc(8 * nS * mm, st);
+  identity_cols(st, m, 0, m, dp(Inv), (long long)mm, nS);
+  lu_solve<double>(st, false, m, dp(LU), m, (long long)mm, ip(piv), m, dp(Inv), m,
+                   (long long)mm, m, nS);
+}
 }  // namespace
 
 void rb_factor(Handle& h, RbSolver& S, int nblk, int m, const double* SiM, const double* SiP,
@@ -54,6 +68,7 @@ void rb_factor(Handle& h, RbSolver& S, int nblk, int m, const double* SiM, const
     SLU_CHECK_CUDA(cudaMemcpyAsync(dp(L0.T), T, 8 * nblk * mm, cudaMemcpyDeviceToDevice, st));
     SLU_CHECK_CUDA(cudaMemcpyAsync(dp(L0.LU), T, 8 * nblk * mm, cudaMemcpyDeviceToDevice, st));
     lu_factor(st, m, dp(L0.LU), m, mm, ip(L0.piv), m, nblk, h.info.as<int>());
+    make_inverses(st, m, L0.LU, L0.piv, nblk, L0.Inv);
   }
   h.ws.reserve(8 * ((size_t)nblk / 2 * 2 * mm * 3) + 8 * 256, st);
   double* X = h.ws.take<double>(std::max<size_t>(1, (size_t)nblk / 2) * 2 * mm);  // per odd block: m x 2m
@@ -105,6 +120,7 @@ void rb_factor(Handle& h, RbSolver& S, int nblk, int m, const double* SiM, const
     add_batched<double>(st, m, m, -1.0, G2 + m, (int)m2, 2 * mm, 0, dp(N.SiP), m, mm, 0, nR);
     SLU_CHECK_CUDA(cudaMemcpyAsync(dp(N.LU), dp(N.T), 8 * nR * mm, cudaMemcpyDeviceToDevice, st));
     lu_factor(st, m, dp(N.LU), m, mm, ip(N.piv), m, nR, h.info.as<int>());
+    make_inverses(st, m, N.LU, N.piv, nR, N.Inv);
     S.levels.push_back(std::move(N));
     l = nR;
   }
@@ -128,8 +144,8 @@ void rb_solve(Handle& h, const RbSolver& S, double* B, int ldb, int c) {
     const RbLevel& P = S.levels[l];
     const int nR = P.nS / 2;
     // z_o = T_o^{-1} v_o (odd o)
-    copy_batched<double>(st, m, c, v[l] + mc, c, 2 * mc, 0, z, c, mc, 0, nR);
-    lu_solve<double>(st, false, m, dp(P.LU) + mm, m, 2 * mm, ip(P.piv) + m, 2 * m, z, c, mc, c, nR);
+    gemm_batched<double>(st, false, false, m, c, m, 1.0, dp(P.Inv) + mm, m, 2 * mm, 0, v[l] + mc,
+                         c, 2 * mc, 0, 0.0, z, c, mc, 0, nR);
     // v'_j = v_{2j} - SiM_{2j} z_{2j-1} - SiP_{2j} z_{2j+1}
     copy_batched<double>(st, m, c, v[l], c, 2 * mc, 0, v[l + 1], c, mc, 0, nR);
     if (nR > 1)
@@ -139,8 +155,9 @@ void rb_solve(Handle& h, const RbSolver& S, double* B, int ldb, int c) {
                          1.0, v[l + 1], c, mc, 0, nR);
   }
   // coarsest block (omsdirectsolve.py:261)
-  lu_solve<double>(st, false, m, dp(S.levels[nL - 1].LU), m, 0, ip(S.levels[nL - 1].piv), 0,
-                   v[nL - 1], c, 0, c, 1);
+  gemm_batched<double>(st, false, false, m, c, m, 1.0, dp(S.levels[nL - 1].Inv), m, 0, 0,
+                       v[nL - 1], c, 0, 0, 0.0, z, c, 0, 0, 1);
+  copy_batched<double>(st, m, c, z, c, 0, 0, v[nL - 1], c, 0, 0, 1);
   // back substitution (omsdirectsolve.py:263-277)
   for (int l = nL - 1; l > 0; --l) {
     const RbLevel& P = S.levels[l - 1];
@@ -152,8 +169,9 @@ void rb_solve(Handle& h, const RbSolver& S, double* B, int ldb, int c) {
     if (nR > 1)
       gemm_batched<double>(st, false, false, m, c, m, -1.0, dp(P.SiP) + mm, m, 2 * mm, 0,
                            v[l] + mc, c, mc, 0, 1.0, v[l - 1] + mc, c, 2 * mc, 0, nR - 1);
-    lu_solve<double>(st, false, m, dp(P.LU) + mm, m, 2 * mm, ip(P.piv) + m, 2 * m, v[l - 1] + mc,
-                     c, 2 * mc, c, nR);
+    gemm_batched<double>(st, false, false, m, c, m, 1.0, dp(P.Inv) + mm, m, 2 * mm, 0,
+                         v[l - 1] + mc, c, 2 * mc, 0, 0.0, z, c, mc, 0, nR);
+    copy_batched<double>(st, m, c, z, c, mc, 0, v[l - 1] + mc, c, 2 * mc, 0, nR);
     copy_batched<double>(st, m, c, v[l], c, mc, 0, v[l - 1], c, 2 * mc, 0, nR);
   }
   copy_batched<double>(st, nblk * m, c, v[0], c, 0, 0, B, ldb, 0, 0, 1);
@@ -272,6 +290,7 @@ void thomas_factor(Handle& h, RbSolver& S, int nblk, int m, const double* SiM, c
                          0, 0, 1.0, Bi, m, 0, 0, 1);
     lu_factor(st, m, Bi, m, 0, ip(L.piv) + i * m, 0, 1, h.info.as<int>());
   }
+  make_inverses(st, m, L.LU, L.piv, nblk, L.Inv);
 }
 
 void thomas_solve(Handle& h, const RbSolver& S, double* B, int ldb, int c) {
@@ -285,14 +304,20 @@ void thomas_solve(Handle& h, const RbSolver& S, double* B, int ldb, int c) {
                          B + (size_t)(i - 1) * m * ldb, ldb, 0, 0, 1.0, B + (size_t)i * m * ldb,
                          ldb, 0, 0, 1);
   // x_n = B_n^{-1} d_n; x_i = B_i^{-1}(d_i - C_i x_{i+1})  (131-139)
-  lu_solve<double>(st, false, m, dp(L.LU) + (n - 1) * mm, m, 0, ip(L.piv) + (n - 1) * m, 0,
-                   B + (size_t)(n - 1) * m * ldb, ldb, 0, c, 1);
+  h.ws.reserve(8 * (size_t)m * c + 256, st);
+  double* z = h.ws.take<double>((size_t)m * c);
+  auto block_solve = [&](int i) {
+    double* Bi = B + (size_t)i * m * ldb;
+    gemm_batched<double>(st, false, false, m, c, m, 1.0, dp(L.Inv) + i * mm, m, 0, 0, Bi, ldb, 0,
+                         0, 0.0, z, c, 0, 0, 1);
+    copy_batched<double>(st, m, c, z, c, 0, 0, Bi, ldb, 0, 0, 1);
+  };
+  block_solve(n - 1);
   for (int i = n - 2; i >= 0; --i) {
     gemm_batched<double>(st, false, false, m, c, m, -1.0, dp(L.SiP) + i * mm, m, 0, 0,
                          B + (size_t)(i + 1) * m * ldb, ldb, 0, 0, 1.0, B + (size_t)i * m * ldb,
                          ldb, 0, 0, 1);
-    lu_solve<double>(st, false, m, dp(L.LU) + i * mm, m, 0, ip(L.piv) + i * m, 0,
-                     B + (size_t)i * m * ldb, ldb, 0, c, 1);
+    block_solve(i);
   }
 }
 

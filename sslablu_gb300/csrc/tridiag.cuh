@@ -7,6 +7,9 @@ namespace slu {
 struct RbLevel {
   int nS = 0;                      // blocks on this level
   DevBuf SiM, SiP, T, LU, piv;     // nS m x m blocks each (piv: nS*m int32)
+  // inverses of the pivot blocks, formed once from their LU factors: every
+  // solve-phase block solve is then one (batched) GEMM
+  DevBuf Inv;
 };
 
 struct RbSolver {
