@@ -271,7 +271,7 @@ void thomas_factor(Handle& h, RbSolver& S, int nblk, int m, const double* SiM, c
   RbLevel& L = S.levels.back();
   const size_t mm = (size_t)m * m;
   L.nS = nblk;
-  L.SiM.alloc(8 * nblk * mm, st);  // holds A_i^T = (SiM_i B_{i-1}^{-1})^T
+  L.SiM.alloc(8 * nblk * mm, st);  // holds A_i^T = (SiM_i B_{i-1}^{-1})^T (T: A_i)
   L.SiP.alloc(8 * nblk * mm, st);  // C_i
   L.LU.alloc(8 * nblk * mm, st);   // LU(B_i)
   L.piv.alloc(4 * (size_t)nblk * m, st);
@@ -291,6 +291,12 @@ void thomas_factor(Handle& h, RbSolver& S, int nblk, int m, const double* SiM, c
     lu_factor(st, m, Bi, m, 0, ip(L.piv) + i * m, 0, 1, h.info.as<int>());
   }
   make_inverses(st, m, L.LU, L.piv, nblk, L.Inv);
+  // A_i itself (the solve multiplies by it; block 0 is unused)
+  L.T.alloc(8 * nblk * mm, st);
+  SLU_CHECK_CUDA(cudaMemsetAsync(dp(L.T), 0, 8 * mm, st));
+  if (nblk > 1)
+    transpose_batched(st, m, m, dp(L.SiM) + mm, m, (long long)mm, 0, dp(L.T) + mm, m,
+                      (long long)mm, 0, nblk - 1);
 }
 
 void thomas_solve(Handle& h, const RbSolver& S, double* B, int ldb, int c) {
@@ -300,7 +306,7 @@ void thomas_solve(Handle& h, const RbSolver& S, double* B, int ldb, int c) {
   const RbLevel& L = S.levels[0];
   // d_i -= A_i d_{i-1}  (omsdirectsolve.py:125-126)
   for (int i = 1; i < n; ++i)
-    gemm_batched<double>(st, true, false, m, c, m, -1.0, dp(L.SiM) + i * mm, m, 0, 0,
+    gemm_batched<double>(st, false, false, m, c, m, -1.0, dp(L.T) + i * mm, m, 0, 0,
                          B + (size_t)(i - 1) * m * ldb, ldb, 0, 0, 1.0, B + (size_t)i * m * ldb,
                          ldb, 0, 0, 1);
   // x_n = B_n^{-1} d_n; x_i = B_i^{-1}(d_i - C_i x_{i+1})  (131-139)
