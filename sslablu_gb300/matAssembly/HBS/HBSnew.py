@@ -329,10 +329,25 @@ class HBSMAT:
         X, one = dv.prepare_rhs(v)
         return dv.finish(self._dev_apply(X, self.mode == "T"), v, one)
 
-    def solve(self, b, mode="N"):
-        """HBSnew.py:393-416."""
+    def solve(self, b, mode="N", out=None):
+        """HBSnew.py:393-416.  Beyond upstream: a pinned host tensor b (2-D,
+        float64, contiguous) is solved in mode N without staging copies --
+        the first solve step reads b from host memory and the last writes the
+        solution into ``out`` (a pinned host tensor of b's shape, allocated
+        when None) -- and the call returns once ``out`` holds the result."""
         if mode not in ("N", "T"):
             raise NotImplementedError("mode not recognized")
+        if (mode == "N" and isinstance(b, torch.Tensor) and not b.is_cuda and b.is_pinned()
+                and b.dim() == 2 and b.dtype == torch.float64 and b.is_contiguous()):
+            if out is None:
+                out = torch.empty(b.shape, dtype=torch.float64, pin_memory=True)
+            if out.shape != b.shape or not out.is_pinned() or not out.is_contiguous():
+                raise ValueError("out must be a contiguous pinned host tensor of b's shape")
+            c = b.shape[1]
+            L.check(L.lib().slu_ulv_solve_into(L.handle(), self._op, L.ptr(b), c, L.ptr(out), c,
+                                               c))
+            torch.cuda.current_stream().synchronize()
+            return out
         X, one = dv.prepare_rhs(b)
         return dv.finish(self._dev_solve(X, mode == "T"), b, one)
 

@@ -195,3 +195,22 @@ def test_out_of_place_solve_matches_in_place():
         torch.cuda.synchronize()
         assert torch.equal(Xw, X0)
         assert torch.equal(Yw[:, :c], B) and bool((Yw[:, c:] == 7.0).all())
+
+
+def test_pinned_host_solve_reads_and_writes_host_memory():
+    """HBSMAT.solve on a pinned host block: the solve steps read the block and
+    write the result in host memory directly; equal to the device solve."""
+    need_gpu()
+    import torch
+    from sslablu_gb300.matAssembly.HBS.HBSnew import HBSMAT
+    from sslablu_gb300.synthetic import random_hbs_factors
+    U, D, V, Nbvec = random_hbs_factors(16, 64, 4, quad=False, rng=np.random.default_rng(6),
+                                        shift=16.0)
+    H = HBSMAT().set_mats(U, D, V, list(Nbvec), fac=2)
+    H.compute_ULV()
+    hp = torch.from_numpy(np.random.default_rng(7).standard_normal((H.shape[0], 6))).pin_memory()
+    out = torch.empty_like(hp).pin_memory()
+    y = H.solve(hp, out=out)
+    assert y is out and not y.is_cuda
+    assert torch.equal(y, H.solve(hp.cuda()).cpu())
+    assert torch.equal(H.solve(hp), y)     # output allocated when not given
