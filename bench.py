@@ -178,9 +178,9 @@ def run_reference(args, rank, world):
 # DRAM bytes (read + written) per launch of each solve step group, averaged
 # over the group's launches in the ncu launch list of
 # `python bench.py --steps 2 --warmup 3` (profiles/ulv_step_c2_launches.txt).
-NCU_TRAFFIC = {"step_kernel<double> (backward)": 1864917,
-               "step_kernel<double> (forward)": 926635,
-               "step_kernel<double> (root)": 134400}
+NCU_TRAFFIC = {"step_kernel<double> (backward)": 1864064,
+               "step_kernel<double> (forward)": 926037,
+               "step_kernel<double> (root)": 134016}
 FP64_NOMINAL_TFLOPS = 1.25   # GB300 float64 (no measured figure in the peaks file)
 
 
