@@ -488,7 +488,7 @@ void hbs_solve_scratch(cudaStream_t st, const Hbs& H, bool trans, T* B, int ldb,
   const T one = T(1), zero = T(0), mone = T(-1);
   const int64_t* perm = H.perm.as<int64_t>();
   if (!trans) {
-    // ---- mode N (ULVsparse.py:296-327): fused per-level kernels
+    // ---- mode N (ULVsparse.py:296-327): one step kernel per tree step
     ulv_solve_fused<T>(st, H, B, ldb, c, scratch, stride);
     return;
   }
