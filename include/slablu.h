@@ -120,14 +120,14 @@ int slu_ulv_solve(slu_handle_t h, slu_hbs_t op, double* B, int ldb, int nrhs, in
  * compute_ulv or slu_ulv_factor). */
 int slu_ulv_solve_noalloc(slu_handle_t h, slu_hbs_t op, double* B, int ldb, int nrhs, int trans);
 
-/* Out-of-place mode-N solve: Y (N x nrhs, ld ldy) <- A^{-1} X (ld ldx), X
- * unchanged (X == Y with equal leading dimensions solves in place).  The
- * same arithmetic as slu_ulv_solve(trans = 0); the first launch reads X and
- * the last writes Y, so no copy of the right-hand sides is made.  Beyond
- * upstream (HBSMAT.solve returns a new array: this is that solve without
- * the copy). */
+/* Out-of-place solve: Y (N x nrhs, ld ldy) <- A^{-1} X (trans = 0) or
+ * A^{-T} X (trans = 1) (ld ldx), X unchanged (X == Y with equal leading
+ * dimensions solves in place).  The same arithmetic as slu_ulv_solve with
+ * the same trans; the first launch reads X and the last writes Y, so no copy
+ * of the right-hand sides is made.  Beyond upstream (HBSMAT.solve returns a
+ * new array: this is that solve without the copy). */
 int slu_ulv_solve_into(slu_handle_t h, slu_hbs_t op, const double* X, int ldx, double* Y,
-                       int ldy, int nrhs);
+                       int ldy, int nrhs, int trans);
 
 /* Single-precision copy of the ULV factors and a float32 solve with the same
  * sweep; used inside iterative refinement (no upstream counterpart: the

@@ -43,7 +43,7 @@ SIGNATURES = {
     "slu_hbs_set_null_space": [P, c_int],
     "slu_hbs_prepare_dfloat": [P, P],
     "slu_ulv_solve_dfloat": [P, P, P, c_int, c_int],
-    "slu_ulv_solve_into": [P, P, P, c_int, P, c_int, c_int],
+    "slu_ulv_solve_into": [P, P, P, c_int, P, c_int, c_int, c_int],
     "slu_ulv_autotune": [P, P, c_int, c_int, c_int, P, c_int, P],
     "slu_hbs_set_refine_inner": [P, c_int],
     "slu_ulv_solve_timed": [P, P, P, c_int, c_int, P, P, P, c_int, P],

@@ -118,6 +118,13 @@ int slu_hbs_create(slu_handle_t h, int N, int L, int fac, const int64_t* perm_ho
     p->H.perm.alloc(sizeof(int64_t) * N, h->h.stream);
     SLU_CHECK_CUDA(cudaMemcpyAsync(p->H.perm.p, perm.data(), sizeof(int64_t) * N,
                                    cudaMemcpyHostToDevice, h->h.stream));
+    // the mode-T solve scatters its input and gathers its output through perm
+    // (HBSnew.py:403-411): as step gathers / scatters that is the inverse
+    std::vector<int64_t> iperm(N);
+    for (int i = 0; i < N; ++i) iperm[perm[i]] = i;
+    p->H.iperm.alloc(sizeof(int64_t) * N, h->h.stream);
+    SLU_CHECK_CUDA(cudaMemcpyAsync(p->H.iperm.p, iperm.data(), sizeof(int64_t) * N,
+                                   cudaMemcpyHostToDevice, h->h.stream));
     SLU_CHECK_CUDA(cudaStreamSynchronize(h->h.stream));
     p->H.lv.resize(L);
     *out = p.release();
@@ -252,7 +259,7 @@ int slu_ulv_solve(slu_handle_t h, slu_hbs_t op, double* B, int ldb, int nrhs, in
 }
 
 int slu_ulv_solve_into(slu_handle_t h, slu_hbs_t op, const double* X, int ldx, double* Y,
-                       int ldy, int nrhs) {
+                       int ldy, int nrhs, int trans) {
   return guard(h, [&] {
     SLU_REQUIRE(h && op && X && Y, "null argument");
     SLU_REQUIRE(nrhs >= 1 && ldx >= nrhs && ldy >= nrhs, "bad right-hand side shape");
@@ -263,7 +270,8 @@ int slu_ulv_solve_into(slu_handle_t h, slu_hbs_t op, const double* X, int ldx, d
     h->h.ws.reserve(bytes + 256, st);
     double* scratch = h->h.ws.take<double>(bytes / sizeof(double));
     const size_t stride = ((sizeof(double) * (size_t)H.N * nrhs + 255) & ~size_t(255)) / 8;
-    slu::ulv_solve_fused<double>(st, H, Y, ldy, nrhs, scratch, stride, nullptr, X, ldx);
+    if (trans) slu::ulv_solve_T<double>(st, H, Y, ldy, nrhs, scratch, stride, X, ldx);
+    else slu::ulv_solve_fused<double>(st, H, Y, ldy, nrhs, scratch, stride, nullptr, X, ldx);
   });
 }
 

@@ -438,26 +438,6 @@ void hbs_apply(Handle& h, Hbs& H, bool trans, const double* X, int ldx, double* 
 }
 
 // ============================================================== solve
-namespace {
-template <typename T> struct Fac;
-template <> struct Fac<double> {
-  static const double* U(const Level& l) { return l.U.as<double>(); }
-  static const double* D(const Level& l) { return l.D.as<double>(); }
-  static const double* Q(const Level& l) { return l.Q.as<double>(); }
-  static const double* W(const Level& l) { return l.W.as<double>(); }
-  static const double* R(const Level& l) { return l.R.as<double>(); }
-  static const double* Uu(const Level& l) { return l.Uu.as<double>(); }
-};
-template <> struct Fac<float> {
-  static const float* U(const Level& l) { return l.Uf.as<float>(); }
-  static const float* D(const Level& l) { return l.Df.as<float>(); }
-  static const float* Q(const Level& l) { return l.Qf.as<float>(); }
-  static const float* W(const Level& l) { return l.Wf.as<float>(); }
-  static const float* R(const Level& l) { return l.Rf.as<float>(); }
-  static const float* Uu(const Level& l) { return l.Uuf.as<float>(); }
-};
-}  // namespace
-
 size_t hbs_solve_scratch_bytes(const Hbs& H, int c, size_t elem) {
   return 5 * ((elem * (size_t)H.N * c + 255) & ~size_t(255));
 }
@@ -472,82 +452,17 @@ void hbs_solve(Handle& h, const Hbs& H, bool trans, T* B, int ldb, int c) {
 template <typename T>
 void hbs_solve_scratch(cudaStream_t st, const Hbs& H, bool trans, T* B, int ldb, int c,
                        T* scratch) {
-  using F = Fac<T>;
   SLU_REQUIRE(H.has_ulv, "HBS operator has no ULV factorisation");
   if (sizeof(T) == 4) SLU_REQUIRE(H.has_f32, "single-precision factors not prepared");
-  const int L = H.L;
-  const size_t N = H.N;
-  const std::vector<long long>& NN = H.NN;
   // five (N x c) buffers, each starting on a 256-byte boundary
-  const size_t stride = ((sizeof(T) * N * c + 255) & ~size_t(255)) / sizeof(T);
-  T* r = scratch;
-  T* y = scratch + stride;
-  T* tmp = scratch + 2 * stride;
-  T* v = scratch + 3 * stride;
-  T* vn = scratch + 4 * stride;
-  const T one = T(1), zero = T(0), mone = T(-1);
-  const int64_t* perm = H.perm.as<int64_t>();
+  const size_t stride = ((sizeof(T) * (size_t)H.N * c + 255) & ~size_t(255)) / sizeof(T);
   if (!trans) {
-    // ---- mode N (ULVsparse.py:296-327): one step kernel per tree step
+    // mode N (ULVsparse.py:296-327): one step kernel per tree step
     ulv_solve_fused<T>(st, H, B, ldb, c, scratch, stride);
-    return;
-  }
-  {
-    // ---- mode T (ULVsparse.py:328-353); upstream scatters the input and
-    // gathers the output (HBSnew.py:403-411)
-    permute_rows<T>(st, true, (int)N, c, perm, B, ldb, r, c);
-    T* rn = tmp;
-    bool have_v = false;
-    for (int t = 0; t + 1 < L; ++t) {
-      const Level& l = H.lv[t];
-      const Level& l1 = H.lv[t + 1];
-      const int n = l.n, k = l.k, nu = l.nu, Nb = l.Nb;
-      const long long nn = (long long)n * n;
-      T* yt = y + NN[t] * c;
-      gemm<T>(st, true, false, nu, c, n, one, F::W(l), n, nn, 0, r, c, (long long)n * c, 0, zero,
-              yt, c, (long long)nu * c, 0, Nb);
-      gemm<T>(st, true, false, k, c, n, one, F::W(l) + nu, n, nn, 0, r, c, (long long)n * c, 0,
-              zero, rn, c, (long long)k * c, 0, Nb);
-      trsm_upper<T>(st, true, nu, F::R(l), n, 1, (long long)nu * n, yt, c, 1, (long long)nu * c,
-                    c, Nb);
-      gemm<T>(st, true, false, k, c, nu, one, F::Uu(l), k, (long long)nu * k, 0, yt, c,
-              (long long)nu * c, 0, zero, vn, c, (long long)k * c, 0, Nb);
-      if (have_v)
-        gemm<T>(st, true, false, k, c, n, one, F::U(l), k, (long long)n * k, 0, v, c,
-                (long long)n * c, 0, one, vn, c, (long long)k * c, 0, Nb);
-      gemm<T>(st, true, false, k, c, nu, mone, F::R(l) + nu, n, (long long)nu * n, 0, yt, c,
-              (long long)nu * c, 0, one, rn, c, (long long)k * c, 0, Nb);
-      const int n1 = l1.n;
-      gemm<T>(st, true, false, n1, c, n1, mone, F::D(l1), n1, (long long)n1 * n1, 0, vn, c,
-              (long long)n1 * c, 0, one, rn, c, (long long)n1 * c, 0, l1.Nb);
-      std::swap(r, rn);
-      std::swap(v, vn);
-      have_v = true;
-    }
-    const Level& rt = H.lv[L - 1];
-    T* yr = y + NN[L - 1] * c;
-    SLU_CHECK_CUDA(cudaMemcpyAsync(yr, r, sizeof(T) * (size_t)rt.n * c, cudaMemcpyDeviceToDevice, st));
-    trsm_upper<T>(st, true, rt.n, F::R(rt), rt.n, 1, 0, yr, c, 1, 0, c, 1);
-    T* scratch = rn;
-    for (int t = L - 1; t >= 0; --t) {
-      const Level& l = H.lv[t];
-      const int n = l.n, Nb = l.Nb;
-      const long long nn = (long long)n * n;
-      T* yt = y + NN[t] * c;
-      if (t == L - 1) {
-        gemm<T>(st, false, false, n, c, n, one, F::Q(l), n, 0, 0, yt, c, 0, 0, zero, scratch, c, 0,
-                0, 1);
-      } else {
-        const int k = l.k, nu = l.nu;
-        gemm<T>(st, false, false, n, c, nu, one, F::Q(l), n, nn, 0, yt, c, (long long)nu * c, 0,
-                zero, scratch, c, (long long)n * c, 0, Nb);
-        gemm<T>(st, false, false, n, c, k, one, F::Q(l) + nu, n, nn, 0, y + NN[t + 1] * c, c,
-                (long long)k * c, 0, one, scratch, c, (long long)n * c, 0, Nb);
-      }
-      SLU_CHECK_CUDA(cudaMemcpyAsync(yt, scratch, sizeof(T) * (size_t)Nb * n * c,
-                                     cudaMemcpyDeviceToDevice, st));
-    }
-    permute_rows<T>(st, false, (int)N, c, perm, y, c, B, ldb);
+  } else {
+    // mode T (ULVsparse.py:328-353): the transposed steps, in reverse order;
+    // upstream scatters the input and gathers the output (HBSnew.py:403-411)
+    ulv_solve_T<T>(st, H, B, ldb, c, scratch, stride);
   }
 }
 template void hbs_solve<double>(Handle&, const Hbs&, bool, double*, int, int);
@@ -574,6 +489,7 @@ void hbs_make_f32(Handle& h, Hbs& H) {
     cp(l.Uu, l.Uuf);
     cp(l.Qt, l.Qtf);
     cp(l.Sw, l.Swf);
+    cp(l.SwT, l.SwTf);
   }
   H.has_f32 = true;
 }

@@ -88,6 +88,10 @@ struct Level {
   // Sw = [G; H] per block (G only on the leaves; the root: [R^-1 Q^T; D R^-1 Q^T])
   DevBuf Qt, Sw;
   DevBuf Qtf, Swf;     // float32 copies
+  // step operators of the mode-T solve: SwT = Sw^T per block, its columns
+  // (the rows of Sw above the leaves) reordered to the children's [v; y]
+  // ranges, child after child; the transposed forward steps use Q itself
+  DevBuf SwT, SwTf;
   DevBuf Qtdf, Swdf;   // double-float copies (interleaved hi/lo pairs)
 };
 
@@ -107,6 +111,7 @@ struct Hbs {
   int N = 0, L = 0, fac = 2;
   std::vector<Level> lv;           // lv[0] = leaves, lv[L-1] = root
   DevBuf perm;                     // int64[N]
+  DevBuf iperm;                    // int64[N], iperm[perm[i]] = i
   bool identity_perm = true;
   std::vector<long long> NN;       // NNvec, L+1 entries
   bool has_mats = false, has_ulv = false, has_f32 = false, has_df = false, has_dfs = false;
@@ -187,6 +192,11 @@ template <typename T>
 void ulv_solve_fused(cudaStream_t st, const Hbs& H, T* B, int ldb, int c, T* scratch,
                      size_t stride, LaunchTimes* times = nullptr, const T* X = nullptr,
                      int ldx = 0);
+// Mode-T solve B <- A^{-T} B (reading X when given) with the transposed
+// step operators; scratch as ulv_solve_fused.
+template <typename T>
+void ulv_solve_T(cudaStream_t st, const Hbs& H, T* B, int ldb, int c, T* scratch, size_t stride,
+                 const T* X = nullptr, int ldx = 0);
 // Times every launch of the mode-N solve for `c` right-hand sides under a set
 // of plan caps and keeps the fastest per launch (H.tuned); precision 0
 // float64, 2 double-float.  Results are unchanged: the caps only move work
@@ -239,6 +249,7 @@ struct FacPtr<double> {
   static const double* Uu(const Level& l) { return l.Uu.as<double>(); }
   static const double* Qt(const Level& l) { return l.Qt.as<double>(); }
   static const double* Sw(const Level& l) { return l.Sw.as<double>(); }
+  static const double* SwT(const Level& l) { return l.SwT.as<double>(); }
 };
 template <>
 struct FacPtr<float> {
@@ -250,6 +261,7 @@ struct FacPtr<float> {
   static const float* Uu(const Level& l) { return l.Uuf.as<float>(); }
   static const float* Qt(const Level& l) { return l.Qtf.as<float>(); }
   static const float* Sw(const Level& l) { return l.Swf.as<float>(); }
+  static const float* SwT(const Level& l) { return l.SwTf.as<float>(); }
 };
 
 template <>

@@ -115,6 +115,95 @@ Step<T> backward_step(const Hbs& H, int t, const T* ru, const T* Vin, const T* Y
   return s;
 }
 
+// ---------------------------------------------------------------- mode T
+// The mode-T solve (ULVsparse.py:328-353) is the transpose of the mode-N
+// map, so it runs the mode-N steps transposed and in reverse order.  Every
+// vector of the mode-N solve has one producer and one consumer, so no
+// transposed step accumulates into another's output:
+//   backward^T, leaf -> root-1:  [ru'; v'; y'] = [G; H]^T z      (SwT)
+//   root^T:                      x' = [R^{-1} Q^T; D R^{-1} Q^T]^T z
+//   forward^T, root-1 -> leaf:   x_b' = Q_b [ru'; x_parent']
+// A backward^T step writes the [v'; y'] rows of a block as one 2k-row range,
+// so a parent reads its children's ranges as one input (SwT's columns are
+// ordered to match).  The caller's rows enter and leave through iperm.
+template <typename T>
+Step<T> backwardT_step(const Hbs& H, int t, const T* src, int lds, const int64_t* perm, T* ru,
+                       T* dst, int c) {
+  const Level& l = H.lv[t];
+  const int cols = t == 0 ? l.n : 2 * l.n;
+  Step<T> s{};
+  s.S = FacPtr<T>::SwT(l);
+  s.rows = l.nu + 2 * l.k;
+  s.w = cols;
+  s.sS = (long long)s.rows * s.w;
+  s.nb = l.Nb;
+  s.c = c;
+  s.nin = 1;
+  s.in_p[0] = src;
+  s.in_ld[0] = lds;
+  s.in_blk[0] = cols;
+  s.in_rows[0] = cols;
+  s.in_perm = perm;
+  s.split = l.nu;
+  s.out_p[0] = ru;
+  s.out_ld[0] = c;
+  s.out_blk[0] = l.nu;
+  s.out_p[1] = dst;
+  s.out_ld[1] = c;
+  s.out_blk[1] = 2 * l.k;
+  return s;
+}
+
+template <typename T>
+Step<T> rootT_step(const Hbs& H, const T* src, int lds, const int64_t* iperm, T* out, int ldo,
+                   const int64_t* operm, int c) {
+  const Level& r = H.lv[H.L - 1];
+  Step<T> s{};
+  s.S = FacPtr<T>::SwT(r);
+  s.rows = r.n;
+  s.w = H.L == 1 ? r.n : 2 * r.n;
+  s.nb = 1;
+  s.c = c;
+  s.nin = 1;
+  s.in_p[0] = src;
+  s.in_ld[0] = lds;
+  s.in_rows[0] = s.w;
+  s.in_perm = iperm;
+  s.split = r.n;
+  s.out_p[0] = out;
+  s.out_ld[0] = ldo;
+  s.out_perm = operm;
+  return s;
+}
+
+template <typename T>
+Step<T> forwardT_step(const Hbs& H, int t, const T* ru, const T* xp, T* out, int ldo,
+                      const int64_t* operm, int c) {
+  const Level& l = H.lv[t];
+  Step<T> s{};
+  s.S = FacPtr<T>::Q(l);
+  s.sS = (long long)l.n * l.n;
+  s.rows = l.n;
+  s.w = l.n;
+  s.nb = l.Nb;
+  s.c = c;
+  s.nin = 2;
+  s.in_p[0] = ru;
+  s.in_ld[0] = c;
+  s.in_blk[0] = l.nu;
+  s.in_rows[0] = l.nu;
+  s.in_p[1] = xp;
+  s.in_ld[1] = c;
+  s.in_blk[1] = l.k;
+  s.in_rows[1] = l.k;
+  s.split = l.n;
+  s.out_p[0] = out;
+  s.out_ld[0] = ldo;
+  s.out_blk[0] = l.n;
+  s.out_perm = operm;
+  return s;
+}
+
 constexpr int kMaxThreads = 256;
 constexpr size_t kStepSmem = 96 * 1024;
 

@@ -38,6 +38,26 @@ __global__ void zero_kernel(long long n, double* __restrict__ x) {
     x[e] = 0.0;
 }
 
+// ST_b (w x rows) = Sw_b^T with column j taken from row sig(j) of Sw_b:
+// sig(j) = j when kc == 0; otherwise j = c*2kc + i runs over child c's
+// [v; y] range: i < kc -> v row n + c*kc + i, else y row c*kc + i - kc.
+__global__ void transpose_children_kernel(int nb, int rows, int w, int n, int kc,
+                                          const double* __restrict__ Sw, double* __restrict__ ST) {
+  const long long total = (long long)nb * rows * w;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long b = e / ((long long)rows * w);
+    const int q = (int)(e - b * rows * w);
+    const int r = q / rows, j = q - r * rows;
+    int src = j;
+    if (kc > 0) {
+      const int c = j / (2 * kc), i = j - c * 2 * kc;
+      src = i < kc ? n + c * kc + i : c * kc + i - kc;
+    }
+    ST[e] = Sw[(b * rows + src) * w + r];
+  }
+}
+
 int grid_for(long long n) {
   return (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, 8LL * num_sms()));
 }
@@ -100,6 +120,22 @@ void hbs_make_sweep(Handle& h, Hbs& H) {
   if (L > 1)
     gemm_batched<double>(st, false, false, n, n, n, 1.0, r.D.as<double>(), n, 0, 0, S, n, 0, 0,
                          0.0, S + nn, n, 0, 0, 1);
+  // mode-T operators: every Sw transposed, the columns above the leaves in
+  // the order the children's transposed backward steps write [v; y]
+  for (int t = 0; t < L; ++t) {
+    Level& l = H.lv[t];
+    const bool root = t == L - 1;
+    const int rows = t == 0 ? l.n : 2 * l.n;
+    const int w = root ? l.n : l.nu + 2 * l.k;
+    const int nb = root ? 1 : l.Nb;
+    const int kc = t == 0 ? 0 : H.lv[t - 1].k;
+    SLU_REQUIRE(kc == 0 || l.n % kc == 0, "level size is not a multiple of the children's rank");
+    const long long ne = (long long)nb * rows * w;
+    l.SwT.alloc(8 * (size_t)ne, st);
+    transpose_children_kernel<<<grid_for(ne), 256, 0, st>>>(nb, rows, w, l.n, kc,
+                                                            l.Sw.as<double>(), l.SwT.as<double>());
+    check_launch("transpose_children_kernel");
+  }
   H.has_sweep = true;
   H.has_f32 = false;
   H.has_dfs = false;

@@ -80,7 +80,59 @@ std::vector<StepRec<T>> solve_steps(const Hbs& H, const T* X, int ldx, T* B, int
   return v;
 }
 
+// The 2L-1 launches of a mode-T solve (sweep_host.cuh): right-hand sides
+// read from X, solution written to B.  Scratch: ru' (one stride, at the
+// mode-N offsets) and two ping-pong buffers of two strides each (a
+// backward^T step writes 2k rows per block: at most 2N).
+template <typename T>
+std::vector<StepRec<T>> solve_steps_T(const Hbs& H, const T* X, int ldx, T* B, int ldb, int c,
+                                      T* scratch, size_t stride) {
+  const int L = H.L;
+  const int64_t* ip = H.iperm.as<int64_t>();
+  T* ru = scratch;
+  T* P[2] = {scratch + stride, scratch + 3 * stride};
+  const std::vector<long long>& NN = H.NN;
+  std::vector<StepRec<T>> v;
+  if (L == 1) {
+    v.push_back({sweep::rootT_step<T>(H, X, ldx, ip, B, ldb, ip, c), "ulvT_root_step", 0, 1});
+    return v;
+  }
+  for (int t = 0; t + 1 < L; ++t)
+    v.push_back({sweep::backwardT_step<T>(H, t, t == 0 ? X : P[(t - 1) & 1], t == 0 ? ldx : c,
+                                          t == 0 ? ip : nullptr, ru + NN[t] * c, P[t & 1], c),
+                 "ulvT_bwd_step", t, 2});
+  int cur = (L - 1) & 1;
+  v.push_back({sweep::rootT_step<T>(H, P[(L - 2) & 1], c, nullptr, P[cur], c, nullptr, c),
+               "ulvT_root_step", L - 1, 1});
+  for (int t = L - 2; t >= 0; --t) {
+    const bool leaf = t == 0;
+    v.push_back({sweep::forwardT_step<T>(H, t, ru + NN[t] * c, P[cur], leaf ? B : P[cur ^ 1],
+                                         leaf ? ldb : c, leaf ? ip : nullptr, c),
+                 "ulvT_fwd_step", t, 0});
+    cur ^= 1;
+  }
+  return v;
+}
+
 }  // namespace
+
+// B (N x c, caller ordering) <- A^{-T} B with the transposed steps; X as in
+// ulv_solve_fused.
+template <typename T>
+void ulv_solve_T(cudaStream_t st, const Hbs& H, T* B, int ldb, int c, T* scratch, size_t stride,
+                 const T* X, int ldx) {
+  SLU_REQUIRE(H.has_sweep, "step operators not composed");
+  if (!X) {
+    X = B;
+    ldx = ldb;
+  }
+  for (const StepRec<T>& r : solve_steps_T<T>(H, X, ldx, B, ldb, c, scratch, stride))
+    launch_step(st, r.s, r.what);
+}
+template void ulv_solve_T<double>(cudaStream_t, const Hbs&, double*, int, int, double*, size_t,
+                                  const double*, int);
+template void ulv_solve_T<float>(cudaStream_t, const Hbs&, float*, int, int, float*, size_t,
+                                 const float*, int);
 
 // B (N x c, caller ordering) <- A^{-1} B; scratch: 5 buffers of stride elements.
 template <typename T>

@@ -295,16 +295,12 @@ class HBSMAT:
         return Y
 
     def _dev_solve(self, X, trans=False):
+        # out of place: no copy of the right-hand sides
         X = dv.as_2d(X).contiguous()
-        if not trans:   # out of place: no copy of the right-hand sides
-            Y = torch.empty_like(X)
-            L.check(L.lib().slu_ulv_solve_into(L.handle(), self._op, L.ptr(X), X.shape[1],
-                                               L.ptr(Y), Y.shape[1], X.shape[1]))
-            return Y
-        B = X.clone()
-        L.check(L.lib().slu_ulv_solve(L.handle(), self._op, L.ptr(B), B.shape[1], B.shape[1],
-                                      int(trans)))
-        return B
+        Y = torch.empty_like(X)
+        L.check(L.lib().slu_ulv_solve_into(L.handle(), self._op, L.ptr(X), X.shape[1],
+                                           L.ptr(Y), Y.shape[1], X.shape[1], int(trans)))
+        return Y
 
     def matvec(self, v):
         return self.matmat(v)
@@ -331,13 +327,13 @@ class HBSMAT:
 
     def solve(self, b, mode="N", out=None):
         """HBSnew.py:393-416.  Beyond upstream: a pinned host tensor b (2-D,
-        float64, contiguous) is solved in mode N without staging copies --
+        float64, contiguous) is solved without staging copies --
         the first solve step reads b from host memory and the last writes the
         solution into ``out`` (a pinned host tensor of b's shape, allocated
         when None) -- and the call returns once ``out`` holds the result."""
         if mode not in ("N", "T"):
             raise NotImplementedError("mode not recognized")
-        if (mode == "N" and isinstance(b, torch.Tensor) and not b.is_cuda and b.is_pinned()
+        if (isinstance(b, torch.Tensor) and not b.is_cuda and b.is_pinned()
                 and b.dim() == 2 and b.dtype == torch.float64 and b.is_contiguous()):
             if out is None:
                 out = torch.empty(b.shape, dtype=torch.float64, pin_memory=True)
@@ -345,7 +341,7 @@ class HBSMAT:
                 raise ValueError("out must be a contiguous pinned host tensor of b's shape")
             c = b.shape[1]
             L.check(L.lib().slu_ulv_solve_into(L.handle(), self._op, L.ptr(b), c, L.ptr(out), c,
-                                               c))
+                                               c, int(mode == "T")))
             torch.cuda.current_stream().synchronize()
             return out
         X, one = dv.prepare_rhs(b)

@@ -15,8 +15,9 @@ JSON line with the median time, the tensor FLOP rate (6 split products) and
 the effective rate (2 m n k).
 solve: the float64 ULV solve (mode N) of a synthetic exact HBS operator of
 size m (leaf 64, rank 32, ULV from the given factors) with n right-hand
-sides, two ways: per-level launches (slu_ulv_solve) and the grouped sweep of
-a one-member group; prints the median time per solve of each.  With
+sides, three ways: per-step launches (slu_ulv_solve), the mode-T solve
+(the transposed steps) and the grouped sweep of a one-member group; prints
+the median time per solve of each.  With
 --precision dfloat: the double-float sweep (slu_ulv_solve_dfloat) instead.
 refine: float64 ULV solve against the double-float sweep alone and against
 mixed-precision refinement to 1e-10 with double-float and with float32 inner
@@ -114,6 +115,9 @@ def solve(a):
     def per_level():
         _lib.check(L.slu_ulv_solve(h, H._op, _lib.ptr(W), c, c, 0))
 
+    def mode_T():
+        _lib.check(L.slu_ulv_solve(h, H._op, _lib.ptr(W), c, c, 1))
+
     def grouped():
         _lib.check(L.slu_ulv_solve_grouped(h, 1, ops, bp, ld, ld))
 
@@ -122,7 +126,7 @@ def solve(a):
 
     out = {"kernel": "solve", "N": N, "nrhs": c, "levels": Lv}
     st = torch.cuda.current_stream()
-    arms = {"f64": (("per_level", per_level), ("grouped", grouped)),
+    arms = {"f64": (("per_level", per_level), ("mode_T", mode_T), ("grouped", grouped)),
             "dfloat": (("dfloat", dfloat),)}[a.precision]
     for name, run in arms:
         for _ in range(a.warmup):

@@ -173,8 +173,8 @@ def test_autotuned_plans_keep_results():
 
 def test_out_of_place_solve_matches_in_place():
     """slu_ulv_solve_into reads X and writes Y (leading dimensions wider than
-    the column count; one-level and multi-level trees): X is unchanged and Y
-    equals the in-place solve bitwise."""
+    the column count; one-level and multi-level trees; modes N and T): X is
+    unchanged and Y equals the in-place solve bitwise."""
     need_gpu()
     import torch
     from sslablu_gb300 import _lib as L
@@ -188,13 +188,15 @@ def test_out_of_place_solve_matches_in_place():
         N, c = H.shape[0], 5
         Xw = torch.from_numpy(np.random.default_rng(9).standard_normal((N, 8))).cuda()
         X0 = Xw.clone()
-        Yw = torch.full((N, 7), 7.0, dtype=torch.float64, device="cuda")
-        L.check(L.lib().slu_ulv_solve_into(L.handle(), H._op, L.ptr(Xw), 8, L.ptr(Yw), 7, c))
-        B = Xw[:, :c].clone().contiguous()
-        L.check(L.lib().slu_ulv_solve(L.handle(), H._op, L.ptr(B), c, c, 0))
-        torch.cuda.synchronize()
-        assert torch.equal(Xw, X0)
-        assert torch.equal(Yw[:, :c], B) and bool((Yw[:, c:] == 7.0).all())
+        for trans in (0, 1):
+            Yw = torch.full((N, 7), 7.0, dtype=torch.float64, device="cuda")
+            L.check(L.lib().slu_ulv_solve_into(L.handle(), H._op, L.ptr(Xw), 8, L.ptr(Yw), 7, c,
+                                               trans))
+            B = Xw[:, :c].clone().contiguous()
+            L.check(L.lib().slu_ulv_solve(L.handle(), H._op, L.ptr(B), c, c, trans))
+            torch.cuda.synchronize()
+            assert torch.equal(Xw, X0)
+            assert torch.equal(Yw[:, :c], B) and bool((Yw[:, c:] == 7.0).all())
 
 
 def test_pinned_host_solve_reads_and_writes_host_memory():
@@ -214,3 +216,86 @@ def test_pinned_host_solve_reads_and_writes_host_memory():
     assert y is out and not y.is_cuda
     assert torch.equal(y, H.solve(hp.cuda()).cpu())
     assert torch.equal(H.solve(hp), y)     # output allocated when not given
+
+
+def _hbs_with_perm(U, D, V, Nbvec, perm, fac=2):
+    """An HBSMAT over the given factors whose tree ordering is `perm`
+    (the ordering construct() takes from a slabTree's perm_leaf)."""
+    from sslablu_gb300 import _lib as L
+    from sslablu_gb300 import _dev as dv
+    from sslablu_gb300.matAssembly.HBS.HBSnew import HBSMAT
+    H = HBSMAT().set_mats(U, D, V, list(Nbvec), fac=fac)
+    N, Lv = H.shape[0], len(D)
+    H._new_op(N, Lv, perm)
+    H.perm = np.asarray(perm, dtype=np.int64)
+    for t in range(Lv):
+        Nb = int(Nbvec[t])
+        Dd = dv.to_dev(D[t])
+        n = Dd.shape[0] // Nb
+        Ud = dv.to_dev(U[t]) if t < Lv - 1 else None
+        Vd = dv.to_dev(V[t]) if t < Lv - 1 else None
+        k = Ud.shape[1] if Ud is not None else 0
+        L.check(L.lib().slu_hbs_set_level(L.handle(), H._op, t, Nb, n, k, L.ptr(Ud), L.ptr(Vd),
+                                          L.ptr(Dd)))
+    L.sync()
+    H.compute_ULV()
+    return H
+
+
+@pytest.mark.parametrize("k,nl,Lv,quad,c", [(16, 64, 4, False, 3), (16, 64, 3, True, 5),
+                                            (33, 64, 3, False, 70), (16, 64, 1, False, 2),
+                                            (48, 64, 2, False, 1)])
+def test_mode_T_solve_matches_oracle_with_permutation(k, nl, Lv, quad, c):
+    """Mode-T solve (the transposed steps) vs the oracle's ULVsparse.solve
+    mode T, through a random non-involutory tree ordering applied as
+    HBSnew.solve does (scatter in, gather out); one-level trees, quad trees,
+    uneven ranks, ragged column counts.  Mode N
+    on the same operator as a check of the ordering."""
+    need_gpu()
+    from oracle import hbs as oh
+    from sslablu_gb300.synthetic import random_hbs_factors
+    U, D, V, Nbvec = random_hbs_factors(k, nl, Lv, quad=quad,
+                                        rng=np.random.default_rng(k + Lv), shift=16.0)
+    N = D[0].shape[0]
+    rng = np.random.default_rng(N + k)
+    perm = rng.permutation(N)
+    while np.array_equal(perm[perm], np.arange(N)):
+        perm = rng.permutation(N)
+    H = _hbs_with_perm(U, D, V, Nbvec, perm, fac=4 if quad else 2)
+    Ql, Wl, Uul, Rl, NNv = oh.compute_ULV(U, D, V, list(Nbvec))
+    b = rng.standard_normal((N, c))
+    rhs = np.zeros_like(b)
+    rhs[perm] = b
+    refT = oh.ulv_solve(U, D, Ql, Wl, Uul, Rl, NNv, list(Nbvec), rhs, "T")[perm]
+    assert relerr(H.solve(b, mode="T"), refT) < TOL
+    refN = np.zeros_like(b)
+    refN[perm] = oh.ulv_solve(U, D, Ql, Wl, Uul, Rl, NNv, list(Nbvec), b[perm])
+    assert relerr(H.solve(b), refN) < TOL
+    # 1-D in, 1-D out
+    assert relerr(H.solve(b[:, 0], mode="T"), refT[:, 0]) < TOL
+
+
+def test_mode_T_float32_and_pinned_host():
+    """The float32 mode-T solve (the same transposed steps on the float32
+    operator copies) is within float32 accuracy of float64, and a pinned host
+    block solved in mode T equals the device solve bitwise."""
+    need_gpu()
+    import torch
+    from sslablu_gb300 import _lib as L
+    from sslablu_gb300.synthetic import random_hbs_factors
+    U, D, V, Nbvec = random_hbs_factors(16, 64, 4, quad=False, rng=np.random.default_rng(3),
+                                        shift=16.0)
+    N = D[0].shape[0]
+    H = _hbs_with_perm(U, D, V, Nbvec, np.random.default_rng(4).permutation(N))
+    b = np.random.default_rng(5).standard_normal((N, 6))
+    x64 = H.solve(b, mode="T")
+    L.check(L.lib().slu_hbs_prepare_f32(L.handle(), H._op))
+    B32 = torch.from_numpy(b).float().cuda().contiguous()
+    L.check(L.lib().slu_ulv_solve_f32(L.handle(), H._op, L.ptr(B32), 6, 6, 1))
+    torch.cuda.synchronize()
+    assert relerr(B32.double().cpu().numpy(), x64) < 1e-5
+    hp = torch.from_numpy(b).pin_memory()
+    y = H.solve(hp, mode="T")
+    assert not y.is_cuda and y.is_pinned()
+    assert torch.equal(y, H.solve(hp.cuda(), mode="T").cpu())
+    assert relerr(y.numpy(), x64) < TOL
