@@ -8,22 +8,31 @@
 // evaluated as a split-BF16x3 product: each float64 operand is split into
 // three bfloat16 slices x = x0 + x1 + x2 (24 significant bits), and the six
 // cross products x0y0 + x0y1 + x1y0 + x0y2 + x1y1 + x2y0 are accumulated by
-// one tcgen05 GEMM over the concatenated K: float32 inside 512-term chunks,
-// double-float (float32 pairs, error-free TwoSum) across chunks.  Relative accuracy is that of a float32 GEMM of depth
-// 512, which is what the refinement-driven mixed path needs; the float64 path
-// never uses this kernel.
+// one tcgen05 GEMM over the concatenated K, in float32.  Relative accuracy is
+// that of a float32 GEMM of depth 512, which is what the refinement-driven
+// mixed path needs; the float64 path never uses this kernel.
 //
-// Kernel: one CTA per 128 x 128 output tile, 192 threads.
-//   warp 4 lane 0 : TMA producer, 3-stage ring of (A, B) 128 x 64 bf16 slabs
-//                   (128B-swizzled, one mbarrier per stage, complete_tx)
-//   warp 5 lane 0 : MMA issuer, tcgen05.mma.cta_group::1.kind::f16
-//                   (M=128, N=128, K=16 per instruction); K runs in chunks of
-//                   512 into two ping-pong float32 TMEM accumulators, and
-//                   tcgen05.commit frees each stage / publishes each chunk;
-//                   warp 5 also allocates and frees the 256 TMEM columns
-//   warps 0-3     : epilogue, tcgen05.ld 32x32b rows of each finished chunk
-//                   added (error-free TwoSum, float32 ops) into a
-//                   double-float tile in shared memory, then C in float64
+// Kernel: one CTA per 128 x BN output tile (BN = 256 when the grid still
+// fills the GPU, else 128), 320 threads, one CTA per SM.
+//   warp 8 lane 0 : TMA producer, ring of (A 128 x 64, B BN x 64) bf16 slabs
+//                   (128B-swizzled, one mbarrier per stage, complete_tx); the
+//                   slice of each product is picked by the TMA coordinate
+//   warp 9 lane 0 : MMA issuer, tcgen05.mma.cta_group::1.kind::f16
+//                   (M=128, N=BN, K=16 per instruction) into two ping-pong
+//                   float32 TMEM accumulators of BN columns; tcgen05.commit
+//                   frees each stage and publishes each chunk; warp 9 also
+//                   allocates and frees the 2 BN TMEM columns
+//   warps 0-7     : epilogue; warp w reads TMEM lanes 32 (w % 4) .. + 31
+//                   (its tile rows) and columns (w / 4) BN/2 .. + BN/2, adds
+//                   each finished chunk into float32 sums (BN = 128: held in
+//                   registers while the MMA fills the other accumulator;
+//                   BN = 256: held in the second half of TMEM, the MMA waiting
+//                   for each drain), stages the tile in the freed operand
+//                   ring and writes C in float64, coalesced
+// The product x0 y0 runs in chunks of 512 terms (1024 at BN = 256): float32
+// rounding acts within a chunk; the float32 sums take ceil(K / 512) + 1 chunk
+// additions.  The five smaller products (magnitudes <= 2^-8 of the result)
+// form one last chunk.
 // Every mbarrier wait is bounded; on timeout the kernel records an error word,
 // drains what it issued (again bounded), frees its TMEM and returns.
 #include <cuda.h>
@@ -36,15 +45,32 @@
 namespace slu {
 namespace {
 
-constexpr int BM = 128, BN = 128, BK = 64, STAGES = 3;
-constexpr int TILE_BYTES = BM * BK * 2;          // 16 KB per operand slab
-constexpr int STAGE_BYTES = 2 * TILE_BYTES;      // A + B
-constexpr int ACC_BYTES = BM * BN * 8;           // (hi, lo) float pair tile accumulator
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + ACC_BYTES + 1024;
-constexpr uint32_t TMEM_COLS = 2 * BN;           // two float32 accumulators (ping-pong)
-constexpr int CHUNK = 8;                         // k-tiles (of BK) per float32 chunk
-constexpr int kThreadsTC = 192;                  // warps 0-3 epilogue, 4 TMA, 5 MMA
+constexpr int BM = 128, BK = 64;
+constexpr int A_BYTES = BM * BK * 2;             // 16 KB per A slab
+constexpr int CHUNK = 8;                         // k-tiles (of BK) per x0 y0 chunk
+constexpr int kEpiWarps = 8;
+constexpr int kThreadsTC = 32 * (kEpiWarps + 2); // warps 0-7 epilogue, 8 TMA, 9 MMA
 constexpr long long kWaitLimit = 1LL << 22;      // try_wait rounds before giving up
+
+template <int BN>
+struct TcCfg {
+  // BN = 128: two ping-pong accumulators, float32 sums in the epilogue's
+  // registers.  BN = 256: one accumulator and the float32 sums in the other
+  // half of TMEM (128 register sums per thread do not fit beside 10 warps);
+  // the MMA waits for each drain, so chunks are twice as long.
+  static constexpr bool kTmemSum = BN == 256;
+  static constexpr int kChunk = kTmemSum ? 2 * CHUNK : CHUNK;
+  static constexpr int kStages = BN == 256 ? 4 : 6;
+  static constexpr int kStageBytes = A_BYTES + BN * BK * 2;
+  static constexpr int kSmem = kStages * kStageBytes + 1024;   // + 1024 B alignment slack
+  static constexpr uint32_t kTmemCols = 2 * BN;                // two accumulators
+  static constexpr int kCols = BN / 2;                         // columns per epilogue thread
+  // instruction descriptor, kind::f16: D f32, A/B bf16, both K-major, M = 128, N = BN
+  static constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) |
+                                     ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+  static_assert(kSmem <= 227 * 1024, "shared memory");
+  static_assert(BM * (BN + 1) * 4 <= kStages * kStageBytes, "epilogue staging fits the ring");
+};
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -102,17 +128,13 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
   return d;
 }
 
-// Instruction descriptor, kind::f16: D f32, A/B bf16, both K-major, M = 128, N = 128.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
-                            ((uint32_t)(BM >> 4) << 24);
-
 __device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
-                                         uint32_t accumulate) {
+                                         uint32_t idesc, uint32_t accumulate) {
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
       "setp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
-      "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate)
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
       : "memory");
 }
 
@@ -123,29 +145,44 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
       : "memory");
 }
 
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
         "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
-        "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
-        "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
-        "=r"(r[31])
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
       : "r"(taddr));
 }
 
-// K is consumed in chunks of CHUNK k-tiles.  Chunk c accumulates in float32
-// TMEM accumulator c % 2; the epilogue warps add each finished chunk into a
-// double-float tile in shared memory while the MMA warp fills the other
-// accumulator, so float32 rounding acts only within 512-term chunks.  (The
-// drain uses float32 arithmetic: GB300's float64 pipe is ~1/64 of it.)
-__global__ void __launch_bounds__(kThreadsTC, 1)
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
+      "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]),
+      "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]),
+      "r"(r[15])
+      : "memory");
+}
+
+// Chunks of the K stream (k-tiles kt of KT = 6 KT1): the x0 y0 product
+// (kt < KT1) in chunks of `chunk` k-tiles, the other five products as one.
+__device__ __forceinline__ int chunk_count(int KT1, int chunk) {
+  return (KT1 + chunk - 1) / chunk + 1;
+}
+
+// BN = 128: chunk c accumulates in float32 TMEM accumulator c % 2; the
+// epilogue warps add each finished chunk into their register sums while the
+// MMA warp fills the other accumulator.  BN = 256: every chunk uses the one
+// accumulator, and the epilogue adds it into the TMEM sums before the next.
+// (10 warps put 3 on some SM sub-partitions: 168 registers per thread at most)
+template <int BN>
+__global__ void __maxnreg__(168)
 tc_gemm_bf16_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                     int M, int N, int Kp, double alpha, double beta, double* __restrict__ C,
                     int ldc, unsigned int* __restrict__ err) {
+  using G = TcCfg<BN>;
+  constexpr int STAGES = G::kStages;
   extern __shared__ unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t full_bar[STAGES];
   __shared__ __align__(8) uint64_t empty_bar[STAGES];
@@ -156,14 +193,11 @@ tc_gemm_bf16_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_consta
   __shared__ volatile int s_issued;   // TMA stages issued by the producer
   unsigned char* smem = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  // double-float accumulator, [BN][BM] column-major so a warp's 32 rows are
-  // consecutive: hi at acc_hi, lo at acc_lo
-  float* acc_hi = reinterpret_cast<float*>(smem + STAGES * STAGE_BYTES);
-  float* acc_lo = acc_hi + BM * BN;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
-  const int KT = Kp / BK;
-  const int NC = (KT + CHUNK - 1) / CHUNK;
+  const int KT1 = Kp / BK;          // k-tiles of one product
+  const int KT = 6 * KT1;
+  const int NC = chunk_count(KT1, G::kChunk);
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -172,16 +206,16 @@ tc_gemm_bf16_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_consta
     }
     for (int a = 0; a < 2; ++a) {
       mbar_init(&ready_bar[a], 1);
-      mbar_init(&drained_bar[a], 128);
+      mbar_init(&drained_bar[a], 32 * kEpiWarps);
     }
     s_fail = 0;
     s_issued = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 5) {
+  if (warp == kEpiWarps + 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(&tmem_slot)),
-                 "r"(TMEM_COLS)
+                 "r"(G::kTmemCols)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -189,7 +223,7 @@ tc_gemm_bf16_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_consta
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_slot;
 
-  if (warp == 4) {
+  if (warp == kEpiWarps) {
     // ---------------- TMA producer
     if (lane == 0) {
       for (int kt = 0; kt < KT; ++kt) {
@@ -198,39 +232,48 @@ tc_gemm_bf16_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_consta
           s_fail = 1;
           break;
         }
-        unsigned char* a = smem + s * STAGE_BYTES;
-        unsigned char* b = a + TILE_BYTES;
-        mbar_expect_tx(&full_bar[s], STAGE_BYTES);
-        tma_load_2d(a, &tmA, kt * BK, m0, &full_bar[s]);
-        tma_load_2d(b, &tmB, kt * BK, n0, &full_bar[s]);
+        // product t = A slice sa x B slice sb: (0,0) (0,1) (1,0) (0,2) (1,1) (2,0)
+        const int t = kt / KT1, kk = kt - t * KT1;
+        const int sa = t == 0 ? 0 : (t == 1 ? 0 : (t == 2 ? 1 : (t == 3 ? 0 : (t == 4 ? 1 : 2))));
+        const int sb = t == 0 ? 0 : (t == 1 ? 1 : (t == 2 ? 0 : (t == 3 ? 2 : (t == 4 ? 1 : 0))));
+        unsigned char* a = smem + s * G::kStageBytes;
+        unsigned char* b = a + A_BYTES;
+        mbar_expect_tx(&full_bar[s], G::kStageBytes);
+        tma_load_2d(a, &tmA, sa * Kp + kk * BK, m0, &full_bar[s]);
+        tma_load_2d(b, &tmB, sb * Kp + kk * BK, n0, &full_bar[s]);
         s_issued = kt + 1;
       }
     }
-  } else if (warp == 5) {
+  } else if (warp == kEpiWarps + 1) {
     // ---------------- MMA issuer
     if (lane == 0) {
       int kt = 0;
       bool fail = false;
       for (int c = 0; c < NC && !fail; ++c) {
-        const int a = c & 1;
-        if (c >= 2 && !mbar_wait(&drained_bar[a], ((c >> 1) - 1) & 1)) {
+        // accumulator of chunk c, and the drain it must wait for
+        const int a = G::kTmemSum ? 0 : (c & 1);
+        const bool reuse = G::kTmemSum ? c >= 1 : c >= 2;
+        const uint32_t par = G::kTmemSum ? ((c - 1) & 1) : (((c >> 1) - 1) & 1);
+        if (reuse && !mbar_wait(&drained_bar[a], par)) {
           fail = true;
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t dacc = tmem + (uint32_t)(a * BN);
-        for (int j = 0; j < CHUNK && kt < KT; ++j, ++kt) {
+        const int kend = kt < KT1 ? min(kt + G::kChunk, KT1) : KT;
+        for (int j = 0; kt < kend; ++j, ++kt) {
           const int s = kt % STAGES;
           if (!mbar_wait(&full_bar[s], (kt / STAGES) & 1)) {
             fail = true;
             break;
           }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-          const uint32_t sa = smem_u32(smem + s * STAGE_BYTES);
-          const uint32_t sb = sa + TILE_BYTES;
+          const uint32_t sa = smem_u32(smem + s * G::kStageBytes);
+          const uint32_t sb = sa + A_BYTES;
 #pragma unroll
           for (int kk = 0; kk < BK / 16; ++kk)
-            mma_bf16(dacc, smem_desc(sa + kk * 32), smem_desc(sb + kk * 32), (j | kk) != 0);
+            mma_bf16(dacc, smem_desc(sa + kk * 32), smem_desc(sb + kk * 32), G::kIdesc,
+                     (j | kk) != 0);
           mma_commit(&empty_bar[s]);
         }
         mma_commit(&ready_bar[a]);
@@ -245,116 +288,186 @@ tc_gemm_bf16_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_consta
       }
     }
   } else {
-    // ---------------- epilogue warps 0-3: TMEM lanes 32*warp .. 32*warp+31
-    const int r = warp * 32 + lane;  // tile row owned by this thread
-    for (int cidx = 0; cidx < BN; ++cidx) acc_hi[cidx * BM + r] = acc_lo[cidx * BM + r] = 0.0f;
+    // ---------------- epilogue warps: TMEM lanes 32 (warp % 4) .., columns half (warp / 4)
+    const int q = warp & 3, half = warp >> 2;
+    const int r = q * 32 + lane;       // tile row owned by this thread
+    constexpr int P = BN + 1;          // staging pitch (odd: no bank conflicts)
+    float* tile = reinterpret_cast<float*>(smem);
+    float run[G::kTmemSum ? 1 : G::kCols];
+    if constexpr (!G::kTmemSum) {
+#pragma unroll
+      for (int j = 0; j < G::kCols; ++j) run[j] = 0.f;
+    }
     bool fail = false;
     for (int c = 0; c < NC; ++c) {
-      const int a = c & 1;
-      if (!mbar_wait(&ready_bar[a], (c >> 1) & 1)) {
-        fail = true;
-        break;
-      }
-      if (s_fail) {
+      const int a = G::kTmemSum ? 0 : (c & 1);
+      const uint32_t par = G::kTmemSum ? (c & 1) : ((c >> 1) & 1);
+      // warp-uniform: the TMEM loads below are warp-collective
+      const bool ok = mbar_wait(&ready_bar[a], par) && !s_fail;
+      if (!__all_sync(0xffffffffu, ok)) {
         fail = true;
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t lanes = (uint32_t)(q * 32) << 16;
+      const uint32_t base = tmem + lanes + (uint32_t)(a * BN + half * G::kCols);
+      if constexpr (G::kTmemSum) {
+        // sums at columns BN ..: sum += chunk; the last chunk goes (with
+        // the sums) straight to the staging tile, as every MMA has completed
+        const uint32_t sbase = tmem + lanes + (uint32_t)(BN + half * G::kCols);
+        const bool last = c == NC - 1;
 #pragma unroll 1
-      for (int c0 = 0; c0 < BN; c0 += 32) {
-        uint32_t v[32];
-        tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(a * BN + c0), v);
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        for (int c0 = 0; c0 < G::kCols; c0 += 32) {
+          uint32_t v0[16], v1[16], u0[16], u1[16];
+          tmem_ld16(base + (uint32_t)c0, v0);
+          tmem_ld16(base + (uint32_t)c0 + 16, v1);
+          if (c > 0) {
+            tmem_ld16(sbase + (uint32_t)c0, u0);
+            tmem_ld16(sbase + (uint32_t)c0 + 16, u1);
+          }
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          // error-free TwoSum of (hi, v); the rounding error goes to lo
-          const int idx = (c0 + j) * BM + r;
-          const float x = __uint_as_float(v[j]);
-          const float h = acc_hi[idx];
-          const float sum = h + x;
-          const float bb = sum - h;
-          const float e = (h - (sum - bb)) + (x - bb);
-          acc_hi[idx] = sum;
-          acc_lo[idx] += e;
+          for (int j = 0; j < 16; ++j) {
+            const float x0 = __uint_as_float(v0[j]), x1 = __uint_as_float(v1[j]);
+            u0[j] = __float_as_uint(c > 0 ? __uint_as_float(u0[j]) + x0 : x0);
+            u1[j] = __float_as_uint(c > 0 ? __uint_as_float(u1[j]) + x1 : x1);
+          }
+          if (!last) {
+            tmem_st16(sbase + (uint32_t)c0, u0);
+            tmem_st16(sbase + (uint32_t)c0 + 16, u1);
+          } else {
+            float* t = tile + r * P + half * G::kCols + c0;
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+              t[j] = __uint_as_float(u0[j]);
+              t[16 + j] = __uint_as_float(u1[j]);
+            }
+          }
+        }
+        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+      } else {
+#pragma unroll
+        for (int c0 = 0; c0 < G::kCols; c0 += 16) {
+          uint32_t v[16];
+          tmem_ld16(base + (uint32_t)c0, v);
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+          for (int j = 0; j < 16; ++j) run[c0 + j] += __uint_as_float(v[j]);
         }
       }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       mbar_arrive(&drained_bar[a]);
     }
-    if (fail) {
+    // one decision for all epilogue threads (each gave up, or not, on its
+    // own bounded waits): they all pass this barrier, so the staging
+    // barrier below is reached by all 256 or by none
+    uint32_t any_fail;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "barrier.cta.red.or.pred q, 1, %2, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(any_fail)
+        : "r"((uint32_t)fail), "r"(32 * kEpiWarps)
+        : "memory");
+    if (any_fail) {
       if (lane == 0 && err) atomicOr(err, 1u);
     } else {
-      const int row = m0 + r;
-      if (row < M) {
-        double* crow = C + (long long)row * ldc;
-        for (int cidx = 0; cidx < BN; ++cidx) {
-          const int col = n0 + cidx;
-          if (col < N) {
-            const double v =
-                alpha * ((double)acc_hi[cidx * BM + r] + (double)acc_lo[cidx * BM + r]);
-            crow[col] = (beta == 0.0) ? v : fma(beta, crow[col], v);
-          }
+      // every MMA has completed (the last chunk's commit), so the operand
+      // ring is free: the sums are staged there (odd pitch: no bank
+      // conflicts in either direction), then C is written row by row,
+      // coalesced
+      if constexpr (!G::kTmemSum) {
+#pragma unroll
+        for (int j = 0; j < G::kCols; ++j) tile[r * P + half * G::kCols + j] = run[j];
+      }
+      asm volatile("barrier.cta.sync 1, %0;" ::"r"(32 * kEpiWarps) : "memory");
+      for (int e = threadIdx.x; e < BM * BN; e += 32 * kEpiWarps) {
+        const int i = e / BN, j = e - i * BN;
+        const int row = m0 + i, col = n0 + j;
+        if (row < M && col < N) {
+          double* cp = C + (long long)row * ldc + col;
+          const double v = alpha * (double)tile[i * P + j];
+          *cp = (beta == 0.0) ? v : fma(beta, *cp, v);
         }
       }
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if (warp == 5)
+  if (warp == kEpiWarps + 1)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
-                 "r"(TMEM_COLS)
+                 "r"(G::kTmemCols)
                  : "memory");
 }
 
 // ---------------------------------------------------------------- splitting
-// Slices of x: s0 = bf16(x), s1 = bf16(x - s0), s2 = bf16(x - s0 - s1).
+// Slices of x: f = float32(x), s0 = bf16(f), s1 = bf16(f - s0),
+// s2 = bf16(f - s0 - s1).  The differences are exact in float32 (each drops
+// the leading 8 significant bits), so s0 + s1 + s2 carries the 24 bits of f:
+// one float64 operation per element (GB300's float64 pipe is ~1/64 of the
+// float32 one).
 __device__ __forceinline__ void split3(double x, __nv_bfloat16& s0, __nv_bfloat16& s1,
                                        __nv_bfloat16& s2) {
-  s0 = __double2bfloat16(x);
-  double r = x - (double)__bfloat162float(s0);
-  s1 = __double2bfloat16(r);
-  r -= (double)__bfloat162float(s1);
-  s2 = __double2bfloat16(r);
+  const float f = __double2float_rn(x);
+  s0 = __float2bfloat16_rn(f);
+  const float r1 = f - __bfloat162float(s0);
+  s1 = __float2bfloat16_rn(r1);
+  s2 = __float2bfloat16_rn(r1 - __bfloat162float(s1));
 }
 
-// Slice order of the six cross products along the concatenated K.
-__constant__ int kTermA[6] = {0, 0, 1, 0, 1, 2};
-__constant__ int kTermB[6] = {0, 1, 0, 2, 1, 0};
-
-// A (M x K row-major, float64) -> Acat (M x 6*Kp bf16): block t holds slice kTermA[t].
+// A (M x K row-major, float64) -> Asl (M x 3*Kp bf16): slice t at columns
+// t*Kp ..; one row per blockIdx.y, four consecutive k per thread (8-byte
+// stores; Kp is a multiple of 64).
 __global__ void split_a_kernel(int M, int K, int Kp, const double* __restrict__ A, int lda,
                                __nv_bfloat16* __restrict__ out) {
-  const long long total = (long long)M * Kp;
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
-       e += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(e / Kp), k = (int)(e % Kp);
-    __nv_bfloat16 s[3];
-    if (k < K) split3(A[(long long)i * lda + k], s[0], s[1], s[2]);
-    else s[0] = s[1] = s[2] = __double2bfloat16(0.0);
-    __nv_bfloat16* row = out + (long long)i * 6 * Kp;
+  const int i = blockIdx.y;
+  const int k = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
+  if (i >= M || k >= Kp) return;
+  const double* a = A + (long long)i * lda;
+  __align__(8) __nv_bfloat16 s[3][4];
 #pragma unroll
-    for (int t = 0; t < 6; ++t) row[t * Kp + k] = s[kTermA[t]];
+  for (int u = 0; u < 4; ++u) {
+    if (k + u < K) split3(a[k + u], s[0][u], s[1][u], s[2][u]);
+    else s[0][u] = s[1][u] = s[2][u] = __float2bfloat16_rn(0.f);
   }
+  __nv_bfloat16* row = out + (long long)i * 3 * Kp + k;
+#pragma unroll
+  for (int t = 0; t < 3; ++t)
+    *reinterpret_cast<uint2*>(row + (long long)t * Kp) = *reinterpret_cast<const uint2*>(s[t]);
 }
 
-// B (K x N row-major, float64) -> Bcat (N x 6*Kp bf16, K-major): block t holds slice kTermB[t].
+// B (K x N row-major, float64) -> Bsl (N x 3*Kp bf16, K-major): slice t at
+// columns t*Kp ..; 64 x 64 tiles transposed through shared memory (one
+// float32 per element: the conversion happens on the way in).
 __global__ void split_b_kernel(int K, int N, int Kp, const double* __restrict__ B, int ldb,
                                __nv_bfloat16* __restrict__ out) {
-  __shared__ double tile[32][33];
-  const int k0 = blockIdx.y * 32, n0 = blockIdx.x * 32;
-  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
-    const int k = k0 + r, n = n0 + threadIdx.x;
-    tile[r][threadIdx.x] = (k < K && n < N) ? B[(long long)k * ldb + n] : 0.0;
+  __shared__ float tile[64][65];
+  const int k0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
+  const int tx = threadIdx.x & 63, ty = threadIdx.x >> 6;   // 256 threads: 64 x 4
+  for (int r = ty; r < 64; r += 4) {
+    const int k = k0 + r, n = n0 + tx;
+    tile[r][tx] = (k < K && n < N) ? __double2float_rn(B[(long long)k * ldb + n]) : 0.f;
   }
   __syncthreads();
-  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
-    const int n = n0 + r, k = k0 + threadIdx.x;
+  // each thread: 4 consecutive k of one column n (8-byte stores)
+  const int kq = 4 * (threadIdx.x & 15), nr = threadIdx.x >> 4;   // 16 x 16
+  for (int c = nr; c < 64; c += 16) {
+    const int n = n0 + c, k = k0 + kq;
     if (n >= N || k >= Kp) continue;
-    __nv_bfloat16 s[3];
-    split3(tile[threadIdx.x][r], s[0], s[1], s[2]);
-    __nv_bfloat16* row = out + (long long)n * 6 * Kp;
+    __align__(8) __nv_bfloat16 s[3][4];
 #pragma unroll
-    for (int t = 0; t < 6; ++t) row[t * Kp + k] = s[kTermB[t]];
+    for (int u = 0; u < 4; ++u) {
+      const float f = tile[kq + u][c];
+      s[0][u] = __float2bfloat16_rn(f);
+      const float r1 = f - __bfloat162float(s[0][u]);
+      s[1][u] = __float2bfloat16_rn(r1);
+      s[2][u] = __float2bfloat16_rn(r1 - __bfloat162float(s[1][u]));
+    }
+    __nv_bfloat16* row = out + (long long)n * 3 * Kp + k;
+#pragma unroll
+    for (int t = 0; t < 3; ++t)
+      *reinterpret_cast<uint2*>(row + (long long)t * Kp) = *reinterpret_cast<const uint2*>(s[t]);
   }
 }
 
@@ -379,14 +492,14 @@ EncodeTiledFn encode_fn() {
   return fn;
 }
 
-// rows x cols bf16 matrix, row pitch cols (K-major), box 64 x 128, 128B swizzle.
-CUtensorMap make_map(const void* base, int rows, long long cols) {
+// rows x cols bf16 matrix, row pitch cols (K-major), box 64 x box_rows, 128B swizzle.
+CUtensorMap make_map(const void* base, int rows, long long cols, int box_rows) {
   SLU_REQUIRE((reinterpret_cast<uintptr_t>(base) & 15) == 0, "TMA base must be 16-byte aligned");
   SLU_REQUIRE((cols * 2) % 16 == 0, "TMA row pitch must be a multiple of 16 bytes");
   CUtensorMap m;
   cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
   cuuint64_t strides[1] = {(cuuint64_t)cols * 2};
-  cuuint32_t box[2] = {BK, 128};
+  cuuint32_t box[2] = {BK, (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1, 1};
   CUresult r = encode_fn()(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims,
                            strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -396,11 +509,28 @@ CUtensorMap make_map(const void* base, int rows, long long cols) {
   return m;
 }
 
+template <int BN>
+void launch_tc(cudaStream_t st, const __nv_bfloat16* Asl, const __nv_bfloat16* Bsl, int M, int N,
+               int Kp, double alpha, double beta, double* C, int ldc, unsigned int* err) {
+  using G = TcCfg<BN>;
+  CUtensorMap ma = make_map(Asl, M, 3LL * Kp, BM);
+  CUtensorMap mb = make_map(Bsl, N, 3LL * Kp, BN);
+  static std::once_flag once;
+  std::call_once(once, [] {
+    SLU_CHECK_CUDA(cudaFuncSetAttribute(tc_gemm_bf16_kernel<BN>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, G::kSmem));
+  });
+  dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM);
+  tc_gemm_bf16_kernel<BN><<<grid, kThreadsTC, G::kSmem, st>>>(ma, mb, M, N, Kp, alpha, beta, C,
+                                                                ldc, err);
+  check_launch("tc_gemm_bf16_kernel");
+}
+
 }  // namespace
 
 size_t tc_gemm_workspace_bytes(int M, int N, int K) {
   const long long Kp = ((long long)K + BK - 1) / BK * BK;
-  return (size_t)(6 * Kp * 2) * ((size_t)M + N) + 2 * 256;
+  return (size_t)(3 * Kp * 2) * ((size_t)M + N) + 2 * 256;
 }
 
 // C = alpha A B + beta C with split-BF16x3 tcgen05 products (float32 accumulation).
@@ -411,32 +541,24 @@ void tc_gemm_split3(cudaStream_t st, int M, int N, int K, double alpha, const do
   if (M <= 0 || N <= 0) return;
   SLU_REQUIRE(K >= 1, "K must be positive");
   const int Kp = (K + BK - 1) / BK * BK;
-  const long long Kc = 6LL * Kp;
-  SLU_REQUIRE(Kc < (1LL << 31), "K too large");
-  __nv_bfloat16* Acat = reinterpret_cast<__nv_bfloat16*>(ws);
-  size_t abytes = ((size_t)M * Kc * 2 + 255) & ~size_t(255);
-  __nv_bfloat16* Bcat = reinterpret_cast<__nv_bfloat16*>(reinterpret_cast<char*>(ws) + abytes);
+  SLU_REQUIRE(6LL * Kp < (1LL << 31), "K too large");
+  __nv_bfloat16* Asl = reinterpret_cast<__nv_bfloat16*>(ws);
+  size_t abytes = ((size_t)M * 3 * Kp * 2 + 255) & ~size_t(255);
+  __nv_bfloat16* Bsl = reinterpret_cast<__nv_bfloat16*>(reinterpret_cast<char*>(ws) + abytes);
   {
-    long long total = (long long)M * Kp;
-    int g = (int)std::min<long long>((total + 255) / 256, 8LL * num_sms());
-    split_a_kernel<<<g, 256, 0, st>>>(M, K, Kp, A, lda, Acat);
+    SLU_REQUIRE(M <= 65535 && Kp / 64 <= 65535, "split grid too large");
+    split_a_kernel<<<dim3((Kp / 4 + 255) / 256, M), 256, 0, st>>>(M, K, Kp, A, lda, Asl);
     check_launch("split_a_kernel");
-    dim3 gb((N + 31) / 32, (Kp + 31) / 32);
-    split_b_kernel<<<gb, dim3(32, 8), 0, st>>>(K, N, Kp, B, ldb, Bcat);
+    split_b_kernel<<<dim3((N + 63) / 64, Kp / 64), 256, 0, st>>>(K, N, Kp, B, ldb, Bsl);
     check_launch("split_b_kernel");
   }
-  CUtensorMap ma = make_map(Acat, M, Kc);
-  CUtensorMap mb = make_map(Bcat, N, Kc);
-  static bool attr = false;
-  if (!attr) {
-    SLU_CHECK_CUDA(cudaFuncSetAttribute(tc_gemm_bf16_kernel,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-    attr = true;
-  }
-  dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM);
-  tc_gemm_bf16_kernel<<<grid, kThreadsTC, SMEM_BYTES, st>>>(ma, mb, M, N, (int)Kc, alpha, beta, C,
-                                                            ldc, err);
-  check_launch("tc_gemm_bf16_kernel");
+  // 256-column tiles halve the operand traffic per flop; 128-column tiles
+  // when the wider ones would leave most SMs idle
+  const long long tiles256 = (long long)((N + 255) / 256) * ((M + BM - 1) / BM);
+  if (tiles256 >= num_sms())
+    launch_tc<256>(st, Asl, Bsl, M, N, Kp, alpha, beta, C, ldc, err);
+  else
+    launch_tc<128>(st, Asl, Bsl, M, N, Kp, alpha, beta, C, ldc, err);
 }
 
 }  // namespace slu

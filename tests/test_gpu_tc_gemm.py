@@ -1,9 +1,11 @@
 """tcgen05 split-BF16x3 GEMM (slu_gemm_split3) vs a float64 product.
 
-The kernel accumulates the six split products in float32 within chunks of 512
-terms and in float64 across chunks, so its relative error is that of a
-float32 GEMM of depth 512 whatever K is: the bound here is 3e-6 (Frobenius,
-relative)."""
+The kernel accumulates the six split products in float32 within chunks of
+512 terms of the leading product (1024 with 256-column tiles) and adds the
+chunks in float32, so its relative error is about that of a float32 GEMM of
+depth 512-1024 whatever K is: the bound here is 3e-6 (Frobenius, relative).
+Shapes cover both tile widths (256 columns when the grid has at least one
+tile per SM) and ragged edges in M, N and K."""
 import numpy as np
 import pytest
 
@@ -29,7 +31,8 @@ def _run(M, N, K, alpha=1.0, beta=0.0, seed=0):
 
 
 @pytest.mark.parametrize("M,N,K", [(128, 128, 64), (300, 200, 500), (1024, 512, 2048),
-                                   (129, 1, 65), (4096, 261, 4096)])
+                                   (129, 1, 65), (4096, 261, 4096), (2000, 4000, 300),
+                                   (2048, 4096, 1024)])
 def test_split3_gemm_accuracy(M, N, K):
     need_gpu()
     got, ref = _run(M, N, K)
