@@ -26,10 +26,13 @@ Scheduling (continuous batching):
     copied out of it (one host pass).
 
 Grouped dispatch (``group_solve`` given): an idle worker takes the pending
-requests of every resident operator that has no batch in flight (each up to
-``max_batch_rhs`` columns, oldest operators first, up to ``max_group_rhs``
-columns in all) and solves them in one grouped call, whose launches serve all
-of those operators at once (sslablu_gb300.grouped).  The group's right-hand
+requests of resident operators that have no batch in flight (each up to
+``max_batch_rhs`` columns, oldest operators first) until it holds its share
+of the pending columns -- the dispatchable columns divided by the idle
+workers, at most ``max_group_rhs`` -- and solves them in one grouped call,
+whose launches serve all of those operators at once (sslablu_gb300.grouped).
+The share keeps every idle worker fed, so one group's host staging overlaps
+another's device solve.  The group's right-hand
 sides travel as one flat pinned block each way.
 
 Admission by footprint: ``admit`` factors an operator only when the resident
@@ -191,9 +194,13 @@ class SolveServer:
         if not keys:
             return None
         keys.sort(key=lambda k: self.pending[k][0].t_arrival)
+        # this worker's share of what the idle workers can take now
+        avail = sum(min(self.max_batch, sum(r.B.shape[1] for r in self.pending[k]))
+                    for k in keys)
+        share = min(self.max_group, -(-avail // max(1, self._idle)))
         job, total = [], 0
         for k in keys:
-            if job and total >= self.max_group:
+            if job and total >= share:
                 break
             reqs, cols = self._take(k)
             job.append((k, reqs))
@@ -410,7 +417,7 @@ def main():
     ap.add_argument("--workers", type=int, default=8)
     ap.add_argument("--shift", type=float, default=16.0)
     ap.add_argument("--max-batch", type=int, default=64)
-    ap.add_argument("--group-workers", type=int, default=2)
+    ap.add_argument("--group-workers", type=int, default=8)
     ap.add_argument("--seed", type=int, default=20261205)
     a = ap.parse_args()
     ops = _build_hbs_ops(a.operators, a.seed, shift=a.shift)
