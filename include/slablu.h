@@ -40,6 +40,7 @@ extern "C" {
 typedef struct slu_handle_s* slu_handle_t;
 typedef struct slu_hbs_s* slu_hbs_t;
 typedef struct slu_dense_rb_s* slu_rb_t;
+typedef struct slu_solve_plan_s* slu_solve_plan_t;
 
 /* ---------------------------------------------------------------- runtime */
 int slu_version(void);
@@ -128,6 +129,19 @@ int slu_ulv_solve_noalloc(slu_handle_t h, slu_hbs_t op, double* B, int ldb, int 
  * new array: this is that solve without the copy). */
 int slu_ulv_solve_into(slu_handle_t h, slu_hbs_t op, const double* X, int ldx, double* Y,
                        int ldy, int nrhs, int trans);
+
+/* Solve plan: slu_ulv_solve_into for fixed X, Y (device or pinned host
+ * pointers), nrhs and trans, captured once as a CUDA graph with its own
+ * scratch (and the launch plans tuned for nrhs at creation).  Each
+ * slu_ulv_solve_plan_launch then solves whatever X holds into Y with one
+ * graph launch on h's stream instead of one kernel launch per tree step;
+ * wait != 0 also waits for the result.  A plan refuses to launch
+ * (SLU_ERR_STATE) once its operator is refactored or destroyed; destroy
+ * plans with slu_ulv_solve_plan_destroy.  Beyond upstream. */
+int slu_ulv_solve_plan_create(slu_handle_t h, slu_hbs_t op, const double* X, int ldx, double* Y,
+                              int ldy, int nrhs, int trans, slu_solve_plan_t* out);
+int slu_ulv_solve_plan_launch(slu_handle_t h, slu_solve_plan_t plan, int wait);
+int slu_ulv_solve_plan_destroy(slu_solve_plan_t plan);
 
 /* Single-precision copy of the ULV factors and a float32 solve with the same
  * sweep; used inside iterative refinement (no upstream counterpart: the

@@ -13,6 +13,9 @@ struct slu_handle_s {
 struct slu_hbs_s {
   slu::Hbs H;
 };
+struct slu_solve_plan_s {
+  slu::SolvePlan P;
+};
 struct slu_dense_rb_s {
   slu::RbSolver S;
   bool thomas = false;

@@ -275,6 +275,29 @@ int slu_ulv_solve_into(slu_handle_t h, slu_hbs_t op, const double* X, int ldx, d
   });
 }
 
+int slu_ulv_solve_plan_create(slu_handle_t h, slu_hbs_t op, const double* X, int ldx, double* Y,
+                              int ldy, int nrhs, int trans, slu_solve_plan_t* out) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h && op && X && Y && out, "null argument");
+    SLU_REQUIRE(nrhs >= 1 && ldx >= nrhs && ldy >= nrhs, "bad right-hand side shape");
+    SLU_REQUIRE(op->H.has_ulv, "HBS operator has no ULV factorisation");
+    auto p = std::make_unique<slu_solve_plan_s>();
+    slu::solve_plan_create(h->h, op->H, X, ldx, Y, ldy, nrhs, trans != 0, p->P);
+    *out = p.release();
+  });
+}
+
+int slu_ulv_solve_plan_launch(slu_handle_t h, slu_solve_plan_t plan, int wait) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h && plan, "null argument");
+    slu::solve_plan_launch(h->h, plan->P, wait != 0);
+  });
+}
+
+int slu_ulv_solve_plan_destroy(slu_solve_plan_t plan) {
+  return guard(nullptr, [&] { delete plan; });
+}
+
 int slu_hbs_prepare_f32(slu_handle_t h, slu_hbs_t op) {
   return guard(h, [&] {
     SLU_REQUIRE(h && op, "null argument");

@@ -136,7 +136,33 @@ struct Hbs {
   // dropped whenever the step operators are recomposed
   std::map<std::pair<int, int>, std::vector<PlanKnobs>> tuned;
   void invalidate_plans() { refine_plans.clear(); }
+  // bumped whenever the step operators are recomposed: captured solve plans
+  // hold their addresses and refuse to run after a change
+  unsigned long long sweep_gen = 0;
+  // expires with the operator (captured solve plans check it before running)
+  std::shared_ptr<char> alive = std::make_shared<char>(0);
 };
+
+// One solve (mode N or T) captured as a CUDA graph for fixed right-hand-side
+// and solution buffers, with its own scratch (ulv_solve.cu): a launch is one
+// graph launch instead of one kernel launch per tree step.
+struct SolvePlan {
+  const Hbs* H = nullptr;
+  std::weak_ptr<char> alive;
+  unsigned long long gen = 0;
+  DevBuf scratch;
+  cudaGraphExec_t exec = nullptr;
+  long long kernels = 0;
+  SolvePlan() = default;
+  SolvePlan(const SolvePlan&) = delete;
+  SolvePlan& operator=(const SolvePlan&) = delete;
+  ~SolvePlan() {
+    if (exec) cudaGraphExecDestroy(exec);
+  }
+};
+void solve_plan_create(Handle& h, const Hbs& H, const double* X, int ldx, double* Y, int ldy,
+                       int c, bool trans, SolvePlan& P);
+void solve_plan_launch(Handle& h, SolvePlan& P, bool wait);
 
 // compression + interleaved ULV (HBSnew.HBSMAT.constructHBS_ULV)
 void hbs_compress(Handle& h, Hbs& H, int Nb_leaf, int rk, int s, const double* Om,

@@ -370,6 +370,15 @@ __global__ void __launch_bounds__(kMaxThreads) step_kernel(const Step<T> s) {
 }
 }  // namespace
 
+// Sets the step kernel's shared-memory limit for the plan of `s` (before a
+// stream capture, which should contain launches only).
+template <typename T>
+void prepare_step(Step<T> s, const PlanKnobs& kn = PlanKnobs()) {
+  Step<T>* one = &s;
+  const LaunchPlan p = plan_steps(&one, 1, kn);
+  ensure_smem(reinterpret_cast<const void*>(step_kernel<T>), p.smem);
+}
+
 // One step as one launch (programmatic dependent launch); with `lt` the
 // launch is bracketed by timing events.
 template <typename T>

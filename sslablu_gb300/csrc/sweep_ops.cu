@@ -69,6 +69,7 @@ void hbs_make_sweep(Handle& h, Hbs& H) {
   cudaStream_t st = h.stream;
   H.invalidate_plans();
   H.tuned.clear();
+  ++H.sweep_gen;
   const int L = H.L;
   size_t mmax = 0;
   for (int t = 0; t + 1 < L; ++t) {

@@ -152,6 +152,70 @@ void ulv_solve_fused(cudaStream_t st, const Hbs& H, T* B, int ldb, int c, T* scr
                 kn ? (*kn)[i] : PlanKnobs());
 }
 
+void solve_plan_create(Handle& h, const Hbs& H, const double* X, int ldx, double* Y, int ldy,
+                       int c, bool trans, SolvePlan& P) {
+  SLU_REQUIRE(H.has_sweep, "step operators not composed");
+  cudaStream_t st = h.stream;
+  const size_t stride = ((8 * (size_t)H.N * c + 255) & ~size_t(255)) / 8;
+  P.scratch.alloc(8 * 5 * stride, st);
+  double* scratch = P.scratch.as<double>();
+  // pinned host X / Y are read and written by the first and last steps
+  // directly (measured faster than copy nodes staging them in the graph)
+  const std::vector<StepRec<double>> steps =
+      trans ? solve_steps_T<double>(H, X, ldx, Y, ldy, c, scratch, stride)
+            : solve_steps<double>(H, X, ldx, Y, ldy, c, scratch, stride);
+  const std::vector<PlanKnobs>* kn = nullptr;
+  if (!trans) {
+    auto it = H.tuned.find({type_code<double>(), c});
+    if (it != H.tuned.end() && it->second.size() == steps.size()) kn = &it->second;
+  }
+  for (size_t i = 0; i < steps.size(); ++i)
+    sweep::prepare_step(steps[i].s, kn ? (*kn)[i] : PlanKnobs());
+  SLU_CHECK_CUDA(cudaStreamSynchronize(st));   // the scratch exists before the capture
+  // capture on a private stream (the caller's may be the legacy default
+  // stream, which cannot be captured); the graph launches on the caller's
+  cudaStream_t cs = nullptr;
+  SLU_CHECK_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  cudaGraph_t g = nullptr;
+  const long long n0 = launch_thread();
+  try {
+    SLU_CHECK_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+    try {
+      for (size_t i = 0; i < steps.size(); ++i)
+        launch_step(cs, steps[i].s, steps[i].what, nullptr, 0, 0, kn ? (*kn)[i] : PlanKnobs());
+    } catch (...) {
+      cudaStreamEndCapture(cs, &g);
+      if (g) cudaGraphDestroy(g);
+      throw;
+    }
+    SLU_CHECK_CUDA(cudaStreamEndCapture(cs, &g));
+    // captured launches run when the graph is replayed: count them there
+    P.kernels = launch_thread() - n0;
+    launch_total() -= P.kernels;
+    launch_thread() = n0;
+    const cudaError_t e = cudaGraphInstantiate(&P.exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess)
+      throw Error(SLU_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+  } catch (...) {
+    cudaStreamDestroy(cs);
+    throw;
+  }
+  SLU_CHECK_CUDA(cudaStreamDestroy(cs));
+  P.H = &H;
+  P.alive = H.alive;
+  P.gen = H.sweep_gen;
+}
+
+void solve_plan_launch(Handle& h, SolvePlan& P, bool wait) {
+  if (P.alive.expired()) throw Error(SLU_ERR_STATE, "the solve plan's operator was destroyed");
+  if (P.H->sweep_gen != P.gen)
+    throw Error(SLU_ERR_STATE, "the operator was refactored after the solve plan was made");
+  SLU_CHECK_CUDA(cudaGraphLaunch(P.exec, h.stream));
+  count_launches(P.kernels);
+  if (wait) SLU_CHECK_CUDA(cudaStreamSynchronize(h.stream));
+}
+
 namespace {
 
 // Coordinate descent on the whole solve: starting from the default caps,

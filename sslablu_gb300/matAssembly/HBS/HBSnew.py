@@ -347,6 +347,36 @@ class HBSMAT:
         X, one = dv.prepare_rhs(b)
         return dv.finish(self._dev_solve(X, mode == "T"), b, one)
 
+    def solve_plan(self, b, out=None, mode="N"):
+        """Beyond upstream: the solve of b into out captured once (a CUDA
+        graph over the library's step launches, with the launch plans tuned
+        for b's column count at this point) for repeated solves through the
+        same buffers -- a serving loop's staging blocks, a time-stepping
+        loop.  b and out are 2-D contiguous float64 tensors of one shape,
+        both on the device or both in pinned host memory (out allocated
+        like b when None).  ``plan()`` solves what b holds into out and
+        returns out: for host buffers once the result is there, for device
+        buffers as soon as the solve is queued on the current stream.  The
+        plan refuses to run once this operator is refactored."""
+        if mode not in ("N", "T"):
+            raise NotImplementedError("mode not recognized")
+        if not isinstance(b, torch.Tensor) or b.dim() != 2 or b.dtype != torch.float64 \
+                or not b.is_contiguous():
+            raise ValueError("b must be a contiguous 2-D float64 tensor")
+        host = not b.is_cuda
+        if host and not b.is_pinned():
+            raise ValueError("a host b must be pinned")
+        if out is None:
+            out = torch.empty(b.shape, dtype=torch.float64,
+                              **({"pin_memory": True} if host else {"device": b.device}))
+        if out.shape != b.shape or not out.is_contiguous() or out.dtype != torch.float64 \
+                or out.is_cuda == host or (host and not out.is_pinned()):
+            raise ValueError("out must be a contiguous float64 tensor of b's shape, "
+                             "where b is (device, or pinned host)")
+        if b.shape[0] != self.shape[0]:
+            raise ValueError("b has %d rows, the operator %d" % (b.shape[0], self.shape[0]))
+        return SolvePlan(self, b, out, mode == "T", host)
+
     def autotune(self, nrhs, precision="f64", reps=9):
         """Times the launches of a mode-N solve of `nrhs` columns under a set
         of launch-plan caps and keeps the fastest per launch for later solves
@@ -390,3 +420,29 @@ class HBSMAT:
                                    X.shape[1], B.shape[1], float(tol), int(maxit),
                                    ctypes.byref(it), ctypes.byref(rr)))
         return dv.finish(X, b, one), it.value, rr.value
+
+
+class SolvePlan:
+    """A captured solve of HBSMAT.solve_plan (slu_ulv_solve_plan_*)."""
+
+    def __init__(self, H, b, out, trans, host):
+        c = b.shape[1]
+        self.b, self.out, self._H = b, out, H     # the plan reads and writes these
+        self._host = host
+        self._launch = L.lib().slu_ulv_solve_plan_launch
+        p = ctypes.c_void_p()
+        L.check(L.lib().slu_ulv_solve_plan_create(L.handle(), H._op, L.ptr(b), c, L.ptr(out), c,
+                                                  c, int(trans), ctypes.byref(p)))
+        self._p = p
+
+    def __call__(self):
+        L.check(self._launch(L.handle(), self._p, int(self._host)))
+        return self.out
+
+    def close(self):
+        if getattr(self, "_p", None) is not None and L._lib is not None:
+            L.lib().slu_ulv_solve_plan_destroy(self._p)
+        self._p = None
+
+    def __del__(self):
+        self.close()

@@ -299,3 +299,46 @@ def test_mode_T_float32_and_pinned_host():
     assert not y.is_cuda and y.is_pinned()
     assert torch.equal(y, H.solve(hp.cuda(), mode="T").cpu())
     assert relerr(y.numpy(), x64) < TOL
+
+
+def test_solve_plan_matches_solve_and_refuses_after_refactor():
+    """HBSMAT.solve_plan (one CUDA graph per solve) equals the solve through
+    slu_ulv_solve_into bitwise for modes N and T, on device buffers and on
+    pinned host buffers, with new data in b on every call and with tuned
+    launch plans; a refactored operator's plan refuses to run."""
+    need_gpu()
+    import torch
+    from sslablu_gb300 import _lib as L
+    from sslablu_gb300.synthetic import random_hbs_factors
+    U, D, V, Nbvec = random_hbs_factors(16, 64, 4, quad=False, rng=np.random.default_rng(8),
+                                        shift=16.0)
+    N = D[0].shape[0]
+    H = _hbs_with_perm(U, D, V, Nbvec, np.random.default_rng(9).permutation(N))
+    rng = np.random.default_rng(10)
+    for mode in ("N", "T"):
+        bd = torch.empty((N, 5), dtype=torch.float64, device="cuda")
+        plan = H.solve_plan(bd, mode=mode)
+        bh = torch.empty((N, 5), dtype=torch.float64).pin_memory()
+        hplan = H.solve_plan(bh, mode=mode)
+        assert hplan.out.is_pinned() and not hplan.out.is_cuda
+        for _ in range(3):
+            x = rng.standard_normal((N, 5))
+            bd.copy_(torch.from_numpy(x))
+            bh.copy_(torch.from_numpy(x))
+            y = plan()
+            torch.cuda.synchronize()
+            ref = H.solve(bd, mode=mode)
+            assert torch.equal(y, ref)
+            assert torch.equal(hplan(), ref.cpu())
+        plan.close()
+        hplan.close()
+    H.autotune(5)
+    bd = torch.from_numpy(rng.standard_normal((N, 5))).cuda()
+    plan = H.solve_plan(bd)
+    y = plan().clone()
+    torch.cuda.synchronize()
+    assert torch.equal(y, H.solve(bd))
+    H.compute_ULV()
+    with pytest.raises(L.SluError):
+        plan()
+    plan.close()
