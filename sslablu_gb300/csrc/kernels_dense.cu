@@ -382,6 +382,109 @@ lu_kernel(int n, double* __restrict__ A, int lda, long long sA, int* __restrict_
   if (threadIdx.x == 0 && first_zero && info) atomicCAS(info + blockIdx.x, 0, first_zero);
 }
 
+// Blocked LU (LAPACK getrf's right-looking scheme): for each panel of kb
+// columns, (1) the panel is factored with partial pivoting over all rows
+// below its top (one CTA per matrix; the swaps act on the panel's columns),
+// (2) the panel's swaps are applied to the other columns and the U row block
+// right of the panel is solved with the panel's unit lower triangle, (3) the
+// trailing block takes the rank-kb update as one batched GEMM over all SMs.
+// The pivots are those of the unblocked elimination (each is chosen in the
+// fully updated column).
+constexpr int kLuPanel = 32;
+
+__global__ void __launch_bounds__(1024)
+lu_panel_kernel(int n, int k0, int kb, double* __restrict__ A, int lda, long long sA,
+                int* __restrict__ piv, long long sP, int* info) {
+  A += blockIdx.x * sA;
+  piv += blockIdx.x * sP;
+  __shared__ double sv[32];
+  __shared__ int si[32];
+  int first_zero = 0;
+  const int k1 = k0 + kb;
+  for (int j = k0; j < k1; ++j) {
+    double best = -1.0;
+    int bi = j;
+    for (int i = j + threadIdx.x; i < n; i += blockDim.x) {
+      const double v = fabs(A[(long long)i * lda + j]);
+      if (v > best) { best = v; bi = i; }
+    }
+    double pv;
+    int p;
+    argmax_abs_block(best, bi, sv, si, pv, p);
+    if (threadIdx.x == 0) piv[j] = p;
+    if (p != j) {
+      for (int c = k0 + threadIdx.x; c < k1; c += blockDim.x) {
+        const double t = A[(long long)j * lda + c];
+        A[(long long)j * lda + c] = A[(long long)p * lda + c];
+        A[(long long)p * lda + c] = t;
+      }
+    }
+    __syncthreads();
+    const double d = A[(long long)j * lda + j];
+    if (d == 0.0) {
+      if (!first_zero) first_zero = j + 1;
+      __syncthreads();
+      continue;
+    }
+    const double inv = 1.0 / d;
+    for (int i = j + 1 + threadIdx.x; i < n; i += blockDim.x) A[(long long)i * lda + j] *= inv;
+    __syncthreads();
+    const int w = k1 - j - 1;   // panel columns right of j
+    if (w > 0) {
+      const long long tot = (long long)(n - j - 1) * w;
+      for (long long e = threadIdx.x; e < tot; e += blockDim.x) {
+        const int i = j + 1 + (int)(e / w), c = j + 1 + (int)(e % w);
+        A[(long long)i * lda + c] -= A[(long long)i * lda + j] * A[(long long)j * lda + c];
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && first_zero && info) atomicCAS(info + blockIdx.x, 0, first_zero);
+}
+
+// One thread per column outside the panel: the panel's row swaps in order,
+// then (right of the panel) U12 = L11^{-1} A12 by forward substitution.
+__global__ void __launch_bounds__(256)
+lu_swap_trsm_kernel(int n, int k0, int kb, double* __restrict__ A, int lda, long long sA,
+                    const int* __restrict__ piv, long long sP) {
+  A += blockIdx.y * sA;
+  piv += blockIdx.y * sP;
+  __shared__ double L11[kLuPanel][kLuPanel + 1];
+  __shared__ int pv[kLuPanel];
+  for (int e = threadIdx.x; e < kb * kb; e += blockDim.x) {
+    const int i = e / kb, r = e - i * kb;
+    L11[i][r] = A[(long long)(k0 + i) * lda + k0 + r];
+  }
+  for (int j = threadIdx.x; j < kb; j += blockDim.x) pv[j] = piv[k0 + j];
+  __syncthreads();
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k1 = k0 + kb;
+  if (c >= n || (c >= k0 && c < k1)) return;
+  double* col = A + c;
+  for (int j = 0; j < kb; ++j) {
+    const int p = pv[j];
+    if (p != k0 + j) {
+      const double t = col[(long long)(k0 + j) * lda];
+      col[(long long)(k0 + j) * lda] = col[(long long)p * lda];
+      col[(long long)p * lda] = t;
+    }
+  }
+  if (c < k1) return;
+  double x[kLuPanel];
+#pragma unroll
+  for (int i = 0; i < kLuPanel; ++i) x[i] = i < kb ? col[(long long)(k0 + i) * lda] : 0.0;
+#pragma unroll
+  for (int i = 1; i < kLuPanel; ++i) {
+    double acc = x[i];
+#pragma unroll
+    for (int r = 0; r < i; ++r) acc -= L11[i][r] * x[r];
+    x[i] = acc;
+  }
+#pragma unroll
+  for (int i = 0; i < kLuPanel; ++i)
+    if (i < kb) col[(long long)(k0 + i) * lda] = x[i];
+}
+
 template <typename T>
 __global__ void lu_solve_kernel(bool trans, int n, const T* __restrict__ LU, int lda,
                                 long long sA, const int* __restrict__ piv, long long sP,
@@ -586,8 +689,25 @@ __global__ void lu_solve_tiled_kernel(int n, const T* __restrict__ LU, int lda, 
 void lu_factor(cudaStream_t st, int n, double* A, int lda, long long sA, int* piv, long long sP,
                int batch, int* info) {
   if (n <= 0 || batch <= 0) return;
-  lu_kernel<<<batch, 1024, 0, st>>>(n, A, lda, sA, piv, sP, info);
-  check_launch("lu_kernel");
+  if (n <= 2 * kLuPanel) {   // small blocks: one kernel, one CTA per matrix
+    lu_kernel<<<batch, 1024, 0, st>>>(n, A, lda, sA, piv, sP, info);
+    check_launch("lu_kernel");
+    return;
+  }
+  SLU_REQUIRE(batch <= 65535, "LU batch too large");
+  for (int k0 = 0; k0 < n; k0 += kLuPanel) {
+    const int kb = std::min(kLuPanel, n - k0), k1 = k0 + kb;
+    lu_panel_kernel<<<batch, 1024, 0, st>>>(n, k0, kb, A, lda, sA, piv, sP, info);
+    check_launch("lu_panel_kernel");
+    lu_swap_trsm_kernel<<<dim3((n + 255) / 256, batch), 256, 0, st>>>(n, k0, kb, A, lda, sA, piv,
+                                                                       sP);
+    check_launch("lu_swap_trsm_kernel");
+    if (k1 < n)
+      gemm_batched<double>(st, false, false, n - k1, n - k1, kb, -1.0,
+                           A + (long long)k1 * lda + k0, lda, sA, 0,
+                           A + (long long)k0 * lda + k1, lda, sA, 0, 1.0,
+                           A + (long long)k1 * lda + k1, lda, sA, 0, batch);
+  }
 }
 
 template <typename T>

@@ -92,3 +92,29 @@ def test_rb_mixed_cases(golden):
         x = rb.solve(rhs)
         assert rb.relres <= 1e-10
         assert relerr(x, g["x_np_%d_%d" % (nS, m)]) < 1e-10
+
+
+@pytest.mark.parametrize("n", [50, 97, 300, 1000])
+def test_lu_factor_matches_lapack(n):
+    """Batched LU (slu_lu_factor; blocked above 64 columns) vs LAPACK getrf
+    (scipy.linalg.lu_factor): the same pivots and the same factors to
+    rounding, three matrices per call; a zero column gives LAPACK's info."""
+    need_gpu()
+    import scipy.linalg as sl
+    import torch
+    from sslablu_gb300 import _lib as L
+    rng = np.random.default_rng(n)
+    A = rng.standard_normal((3, n, n))
+    A[2, :, n // 2 + 3] = 0.0          # singular: zero pivot at column n//2 + 3
+    Ad = torch.from_numpy(A.copy()).cuda()
+    piv = torch.zeros((3, n), dtype=torch.int32, device="cuda")
+    info = torch.zeros(3, dtype=torch.int32, device="cuda")
+    L.check(L.lib().slu_lu_factor(L.handle(), n, L.ptr(Ad), n, n * n, L.ptr(piv), n, 3,
+                                  L.ptr(info)))
+    L.sync()
+    got, gp, gi = Ad.cpu().numpy(), piv.cpu().numpy(), info.cpu().numpy()
+    for b in range(3):
+        lu, p = sl.lu_factor(A[b], check_finite=False)
+        assert np.array_equal(gp[b], p), b
+        assert np.linalg.norm(got[b] - lu) <= 1e-12 * np.linalg.norm(lu) * np.sqrt(n), b
+    assert gi[0] == 0 and gi[1] == 0 and gi[2] == n // 2 + 4
