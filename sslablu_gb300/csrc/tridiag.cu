@@ -18,6 +18,7 @@
 // GEMMs instead of triangular sweeps: the same result to rounding, and every
 // block solve parallel over the block's rows.
 #include "tridiag.cuh"
+#include "sweep_host.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -36,6 +37,127 @@ void make_inverses(cudaStream_t st, int m, const DevBuf& LU, const DevBuf& piv, 
   identity_cols(st, m, 0, m, dp(Inv), (long long)mm, nS);
   lu_solve<double>(st, false, m, dp(LU), m, (long long)mm, ip(piv), m, dp(Inv), m,
                    (long long)mm, m, nS);
+}
+// Fop_j <- [I | 0 | 0] (nR blocks of m x 3m)
+__global__ void rb_fop_init_kernel(int nR, int m, double* __restrict__ F) {
+  const long long w = 3LL * m, total = (long long)nR * m * w;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long q = e % ((long long)m * w);
+    const int r = (int)(q / w), c = (int)(q - r * w);
+    F[e] = (c == r) ? 1.0 : 0.0;
+  }
+}
+
+// The fused solve operators of every reduction level (see RbLevel).
+void build_fused_ops(cudaStream_t st, RbSolver& S) {
+  const int m = S.m;
+  const long long mm = (long long)m * m, w = 3LL * m;
+  for (size_t l = 0; l + 1 < S.levels.size(); ++l) {
+    RbLevel& P = S.levels[l];
+    const int nR = P.nS / 2;
+    P.Fop.alloc(8 * (size_t)nR * 3 * mm, st);
+    P.Bop.alloc(8 * (size_t)nR * 3 * mm, st);
+    double* F = dp(P.Fop);
+    double* Bo = dp(P.Bop);
+    const long long tot = (long long)nR * 3 * mm;
+    rb_fop_init_kernel<<<(int)std::min<long long>((tot + 255) / 256, 8LL * num_sms()), 256, 0,
+                         st>>>(nR, m, F);
+    check_launch("rb_fop_init_kernel");
+    // -SiM_{2j} Inv_{2j-1} (j >= 1), -SiP_{2j} Inv_{2j+1}
+    if (nR > 1)
+      gemm_batched<double>(st, false, false, m, m, m, -1.0, dp(P.SiM) + 2 * mm, m, 2 * mm, 0,
+                           dp(P.Inv) + mm, m, 2 * mm, 0, 0.0, F + 3 * mm + m, (int)w, 3 * mm, 0,
+                           nR - 1);
+    gemm_batched<double>(st, false, false, m, m, m, -1.0, dp(P.SiP), m, 2 * mm, 0, dp(P.Inv) + mm,
+                         m, 2 * mm, 0, 0.0, F + 2 * m, (int)w, 3 * mm, 0, nR);
+    // [Inv_o | -Inv_o SiM_o | -Inv_o SiP_o]
+    copy_batched<double>(st, m, m, dp(P.Inv) + mm, m, 2 * mm, 0, Bo, (int)w, 3 * mm, 0, nR);
+    gemm_batched<double>(st, false, false, m, m, m, -1.0, dp(P.Inv) + mm, m, 2 * mm, 0,
+                         dp(P.SiM) + mm, m, 2 * mm, 0, 0.0, Bo + m, (int)w, 3 * mm, 0, nR);
+    gemm_batched<double>(st, false, false, m, m, m, -1.0, dp(P.Inv) + mm, m, 2 * mm, 0,
+                         dp(P.SiP) + mm, m, 2 * mm, 0, 0.0, Bo + 2 * m, (int)w, 3 * mm, 0, nR);
+  }
+  S.fused = true;
+}
+
+// rb_solve with the fused operators: one step kernel per reduction level,
+// one for the coarsest block, one per back-substitution level.  Level l's
+// right-hand side V_l has a zero block before block 0 (read as v_{-1} next
+// to the zero middle block of Fop_0); the solution X holds the blocks in
+// their final order -- level l's block k is block k 2^l -- plus a zero
+// block after the last (read as x_{nblk} next to the zero right block of
+// the last Bop).
+void rb_solve_fused(Handle& h, const RbSolver& S, double* B, int ldb, int c) {
+  cudaStream_t st = h.stream;
+  const int m = S.m, nblk = S.nblk, nL = (int)S.levels.size();
+  const long long mc = (long long)m * c;
+  size_t tot = (size_t)(nblk + 1) * mc;
+  for (const RbLevel& L : S.levels) tot += (size_t)(L.nS + 1) * mc;
+  h.ws.reserve(8 * tot + 8 * 256, st);
+  double* base = h.ws.take<double>(tot);
+  SLU_CHECK_CUDA(cudaMemsetAsync(base, 0, 8 * tot, st));
+  std::vector<double*> V(nL);
+  double* p = base;
+  for (int l = 0; l < nL; ++l) {
+    V[l] = p;
+    p += (size_t)(S.levels[l].nS + 1) * mc;
+  }
+  double* X = p;
+  copy_batched<double>(st, nblk * m, c, B, ldb, 0, 0, V[0] + mc, c, 0, 0, 1);
+  auto step = [&](const double* op, long long sS, int nb, int w, int nin) {
+    sweep::Step<double> s{};
+    s.S = op;
+    s.sS = sS;
+    s.rows = m;
+    s.w = w;
+    s.nb = nb;
+    s.c = c;
+    s.nin = nin;
+    s.split = m;
+    for (int q = 0; q < 3; ++q) {
+      s.in_ld[q] = c;
+      s.in_rows[q] = m;
+    }
+    s.out_ld[0] = c;
+    return s;
+  };
+  // reduction: v'_j = Fop_j [v_{2j}; v_{2j-1}; v_{2j+1}]
+  for (int l = 0; l + 1 < nL; ++l) {
+    const RbLevel& P = S.levels[l];
+    const int nR = P.nS / 2;
+    sweep::Step<double> s = step(dp(P.Fop), 3LL * m * m, nR, 3 * m, 3);
+    s.in_p[0] = V[l] + mc;
+    s.in_p[1] = V[l];
+    s.in_p[2] = V[l] + 2 * mc;
+    for (int q = 0; q < 3; ++q) s.in_blk[q] = 2LL * m;
+    s.out_p[0] = V[l + 1] + mc;
+    s.out_blk[0] = m;
+    sweep::launch_step(st, s, "rb_reduce_step");
+  }
+  {  // coarsest block: x_0 = Inv v_0
+    sweep::Step<double> s = step(dp(S.levels[nL - 1].Inv), 0, 1, m, 1);
+    s.in_p[0] = V[nL - 1] + mc;
+    s.out_p[0] = X;
+    sweep::launch_step(st, s, "rb_coarse_step");
+  }
+  // back substitution: x_o = Bop_j [v_o; x_{o-1}; x_{o+1}], o = 2j + 1
+  for (int l = nL - 2; l >= 0; --l) {
+    const RbLevel& P = S.levels[l];
+    const int nR = P.nS / 2;
+    const long long sm = (1LL << l) * m;   // rows between level-l blocks in X
+    sweep::Step<double> s = step(dp(P.Bop), 3LL * m * m, nR, 3 * m, 3);
+    s.in_p[0] = V[l] + 2 * mc;
+    s.in_blk[0] = 2LL * m;
+    s.in_p[1] = X;
+    s.in_blk[1] = 2 * sm;
+    s.in_p[2] = X + 2 * sm * c;
+    s.in_blk[2] = 2 * sm;
+    s.out_p[0] = X + sm * c;
+    s.out_blk[0] = 2 * sm;
+    sweep::launch_step(st, s, "rb_back_step");
+  }
+  copy_batched<double>(st, nblk * m, c, X, c, 0, 0, B, ldb, 0, 0, 1);
 }
 }  // namespace
 
@@ -124,9 +246,15 @@ void rb_factor(Handle& h, RbSolver& S, int nblk, int m, const double* SiM, const
     S.levels.push_back(std::move(N));
     l = nR;
   }
+  S.fused = false;
+  if (m <= kRbFusedMax) build_fused_ops(st, S);
 }
 
 void rb_solve(Handle& h, const RbSolver& S, double* B, int ldb, int c) {
+  if (S.fused) {
+    rb_solve_fused(h, S, B, ldb, c);
+    return;
+  }
   cudaStream_t st = h.stream;
   const int m = S.m, nblk = S.nblk;
   const size_t mm = (size_t)m * m, mc = (size_t)m * c;

@@ -10,11 +10,22 @@ struct RbLevel {
   // inverses of the pivot blocks, formed once from their LU factors: every
   // solve-phase block solve is then one (batched) GEMM
   DevBuf Inv;
+  // fused solve operators (blocks of m <= kRbFusedMax), m x 3m each, built at
+  // factor time:  Fop_j = [I | -SiM_{2j} Inv_{2j-1} | -SiP_{2j} Inv_{2j+1}]
+  // (reduction of even block 2j, Fop_0's middle block zero) and
+  // Bop_j = [Inv_o | -Inv_o SiM_o | -Inv_o SiP_o] (back substitution of odd
+  // block o = 2j + 1)
+  DevBuf Fop, Bop;
 };
+
+// Largest block for the fused red-black solve (a step CTA stages row
+// slices of a 3m-wide operator and a 3m-long z tile in 96 KB).
+constexpr int kRbFusedMax = 256;
 
 struct RbSolver {
   int m = 0, nblk = 0;
   bool mixed = false;              // Schur products on the tensor cores
+  bool fused = false;              // levels carry Fop / Bop (m <= kRbFusedMax)
   std::vector<RbLevel> levels;     // levels[0] = the input system
 };
 
