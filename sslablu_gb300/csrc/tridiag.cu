@@ -208,11 +208,13 @@ void rb_factor(Handle& h, RbSolver& S, int nblk, int m, const double* SiM, const
     N.LU.alloc(8 * nR * mm, st);
     N.piv.alloc(4 * (size_t)nR * m, st);
     const long long m2 = 2 * (long long)m;
-    // X_o = T_o^{-1} [SiM_o | SiP_o] for odd o
-    copy_batched<double>(st, m, m, dp(P.SiM) + mm, m, 2 * mm, 0, X, (int)m2, 2 * mm, 0, nR);
-    copy_batched<double>(st, m, m, dp(P.SiP) + mm, m, 2 * mm, 0, X + m, (int)m2, 2 * mm, 0, nR);
-    lu_solve<double>(st, false, m, dp(P.LU) + mm, m, 2 * mm, ip(P.piv) + m, 2 * m, X, (int)m2,
-                     2 * mm, (int)m2, nR);
+    // X_o = T_o^{-1} [SiM_o | SiP_o] for odd o, as products with the
+    // inverses formed when the level was factored (GEMMs over all SMs
+    // instead of substitutions)
+    gemm_batched<double>(st, false, false, m, m, m, 1.0, dp(P.Inv) + mm, m, 2 * mm, 0,
+                         dp(P.SiM) + mm, m, 2 * mm, 0, 0.0, X, (int)m2, 2 * mm, 0, nR);
+    gemm_batched<double>(st, false, false, m, m, m, 1.0, dp(P.Inv) + mm, m, 2 * mm, 0,
+                         dp(P.SiP) + mm, m, 2 * mm, 0, 0.0, X + m, (int)m2, 2 * mm, 0, nR);
     // G1_j = SiM_{2j} X_{2j-1} (j >= 1; SiM_0 is zero), G2_j = SiP_{2j} X_{2j+1}
     if (!mixed) {
       if (nR > 1)
