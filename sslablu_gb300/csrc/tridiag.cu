@@ -49,6 +49,17 @@ __global__ void rb_fop_init_kernel(int nR, int m, double* __restrict__ F) {
   }
 }
 
+// F_b <- [I | 0] (nb blocks of m x w, w >= m)
+__global__ void ident_wide_kernel(int nb, int m, int w, double* __restrict__ F) {
+  const long long total = (long long)nb * m * w;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long q = e % ((long long)m * w);
+    const int r = (int)(q / w), c = (int)(q - (long long)r * w);
+    F[e] = (c == r) ? 1.0 : 0.0;
+  }
+}
+
 // The fused solve operators of every reduction level (see RbLevel).
 void build_fused_ops(cudaStream_t st, RbSolver& S) {
   const int m = S.m;
@@ -427,6 +438,29 @@ void thomas_factor(Handle& h, RbSolver& S, int nblk, int m, const double* SiM, c
   if (nblk > 1)
     transpose_batched(st, m, m, dp(L.SiM) + mm, m, (long long)mm, 0, dp(L.T) + mm, m,
                       (long long)mm, 0, nblk - 1);
+  S.fused = false;
+  if (m <= kRbFusedMax) {
+    // fused solve operators (m x 2m per block): Fop_i = [I | -A_i] (i >= 1),
+    // Bop_i = [B_i^{-1} | -B_i^{-1} C_i] (the last block: [B^{-1} | 0])
+    const long long w = 2LL * m;
+    L.Fop.alloc(8 * (size_t)nblk * 2 * mm, st);
+    L.Bop.alloc(8 * (size_t)nblk * 2 * mm, st);
+    const long long tot = (long long)nblk * 2 * mm;
+    ident_wide_kernel<<<(int)std::min<long long>((tot + 255) / 256, 8LL * num_sms()), 256, 0,
+                        st>>>(nblk, m, (int)w, dp(L.Fop));
+    check_launch("ident_wide_kernel");
+    if (nblk > 1)
+      add_batched<double>(st, m, m, -1.0, dp(L.T) + mm, m, (long long)mm, 0,
+                          dp(L.Fop) + 2 * mm + m, (int)w, 2 * (long long)mm, 0, nblk - 1);
+    SLU_CHECK_CUDA(cudaMemsetAsync(dp(L.Bop), 0, 8 * (size_t)nblk * 2 * mm, st));
+    copy_batched<double>(st, m, m, dp(L.Inv), m, (long long)mm, 0, dp(L.Bop), (int)w,
+                         2 * (long long)mm, 0, nblk);
+    if (nblk > 1)
+      gemm_batched<double>(st, false, false, m, m, m, -1.0, dp(L.Inv), m, (long long)mm, 0,
+                           dp(L.SiP), m, (long long)mm, 0, 0.0, dp(L.Bop) + m, (int)w,
+                           2 * (long long)mm, 0, nblk - 1);
+    S.fused = true;
+  }
 }
 
 void thomas_solve(Handle& h, const RbSolver& S, double* B, int ldb, int c) {
@@ -434,6 +468,48 @@ void thomas_solve(Handle& h, const RbSolver& S, double* B, int ldb, int c) {
   const int m = S.m, n = S.nblk;
   const size_t mm = (size_t)m * m;
   const RbLevel& L = S.levels[0];
+  if (S.fused) {
+    // one step kernel per block and sweep: y_i = [I | -A_i] [b_i; y_{i-1}]
+    // into Y (y_0 = b_0 copied), then x_i = Bop_i [y_i; x_{i+1}] into B
+    // (the last block reads y_{n-1} twice; Bop's right half is zero there)
+    const long long mc = (long long)m * c;
+    h.ws.reserve(8 * (size_t)n * mc + 256, st);
+    double* Y = h.ws.take<double>((size_t)n * mc);
+    copy_batched<double>(st, m, c, B, ldb, 0, 0, Y, c, 0, 0, 1);
+    auto step = [&](const double* op, const double* in0, int ld0, const double* in1, int ld1,
+                    double* out, int ldo) {
+      sweep::Step<double> s{};
+      s.S = op;
+      s.rows = m;
+      s.w = 2 * m;
+      s.nb = 1;
+      s.c = c;
+      s.nin = 2;
+      s.in_p[0] = in0;
+      s.in_ld[0] = ld0;
+      s.in_rows[0] = m;
+      s.in_p[1] = in1;
+      s.in_ld[1] = ld1;
+      s.in_rows[1] = m;
+      s.split = m;
+      s.out_p[0] = out;
+      s.out_ld[0] = ldo;
+      return s;
+    };
+    for (int i = 1; i < n; ++i)
+      sweep::launch_step(st, step(dp(L.Fop) + 2 * i * mm, B + (size_t)i * m * ldb, ldb,
+                                  Y + (i - 1) * mc, c, Y + i * mc, c),
+                         "thomas_fwd_step");
+    sweep::launch_step(st, step(dp(L.Bop) + 2 * (n - 1) * mm, Y + (n - 1) * mc, c,
+                                Y + (n - 1) * mc, c, B + (size_t)(n - 1) * m * ldb, ldb),
+                       "thomas_bwd_step");
+    for (int i = n - 2; i >= 0; --i)
+      sweep::launch_step(st, step(dp(L.Bop) + 2 * i * mm, Y + i * mc, c,
+                                  B + (size_t)(i + 1) * m * ldb, ldb, B + (size_t)i * m * ldb,
+                                  ldb),
+                         "thomas_bwd_step");
+    return;
+  }
   // d_i -= A_i d_{i-1}  (omsdirectsolve.py:125-126)
   for (int i = 1; i < n; ++i)
     gemm_batched<double>(st, false, false, m, c, m, -1.0, dp(L.T) + i * mm, m, 0, 0,
