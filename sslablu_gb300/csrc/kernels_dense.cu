@@ -443,6 +443,71 @@ lu_panel_kernel(int n, int k0, int kb, double* __restrict__ A, int lda, long lon
   if (threadIdx.x == 0 && first_zero && info) atomicCAS(info + blockIdx.x, 0, first_zero);
 }
 
+// The same panel factorisation with the panel (rows k0.., kb columns) held
+// in shared memory, row pitch kb + 1 (column reads hit distinct banks): one
+// load, one store, and every column step at shared-memory latency.
+constexpr size_t kPanelSmemMax = 200 * 1024;
+
+__global__ void __launch_bounds__(1024)
+lu_panel_smem_kernel(int n, int k0, int kb, double* __restrict__ A, int lda, long long sA,
+                     int* __restrict__ piv, long long sP, int* info) {
+  A += blockIdx.x * sA;
+  piv += blockIdx.x * sP;
+  extern __shared__ double Ps[];
+  __shared__ double sv[32];
+  __shared__ int si[32];
+  const int R = n - k0, pitch = kb + 1;
+  for (int e = threadIdx.x; e < R * kb; e += blockDim.x) {
+    const int i = e / kb, c = e - i * kb;
+    Ps[i * pitch + c] = A[(long long)(k0 + i) * lda + k0 + c];
+  }
+  __syncthreads();
+  int first_zero = 0;
+  for (int jj = 0; jj < kb; ++jj) {
+    double best = -1.0;
+    int bi = jj;
+    for (int i = jj + threadIdx.x; i < R; i += blockDim.x) {
+      const double v = fabs(Ps[i * pitch + jj]);
+      if (v > best) { best = v; bi = i; }
+    }
+    double pv;
+    int p;
+    argmax_abs_block(best, bi, sv, si, pv, p);
+    if (threadIdx.x == 0) piv[k0 + jj] = k0 + p;
+    if (p != jj) {
+      for (int c = threadIdx.x; c < kb; c += blockDim.x) {
+        const double t = Ps[jj * pitch + c];
+        Ps[jj * pitch + c] = Ps[p * pitch + c];
+        Ps[p * pitch + c] = t;
+      }
+    }
+    __syncthreads();
+    const double d = Ps[jj * pitch + jj];
+    if (d == 0.0) {
+      if (!first_zero) first_zero = k0 + jj + 1;
+      __syncthreads();
+      continue;
+    }
+    const double inv = 1.0 / d;
+    for (int i = jj + 1 + threadIdx.x; i < R; i += blockDim.x) Ps[i * pitch + jj] *= inv;
+    __syncthreads();
+    const int w = kb - jj - 1;
+    if (w > 0) {
+      const int tot = (R - jj - 1) * w;
+      for (int e = threadIdx.x; e < tot; e += blockDim.x) {
+        const int i = jj + 1 + e / w, c = jj + 1 + e % w;
+        Ps[i * pitch + c] -= Ps[i * pitch + jj] * Ps[jj * pitch + c];
+      }
+    }
+    __syncthreads();
+  }
+  for (int e = threadIdx.x; e < R * kb; e += blockDim.x) {
+    const int i = e / kb, c = e - i * kb;
+    A[(long long)(k0 + i) * lda + k0 + c] = Ps[i * pitch + c];
+  }
+  if (threadIdx.x == 0 && first_zero && info) atomicCAS(info + blockIdx.x, 0, first_zero);
+}
+
 // One thread per column outside the panel: the panel's row swaps in order,
 // then (right of the panel) U12 = L11^{-1} A12 by forward substitution.
 __global__ void __launch_bounds__(256)
@@ -770,8 +835,15 @@ void lu_factor(cudaStream_t st, int n, double* A, int lda, long long sA, int* pi
   SLU_REQUIRE(batch <= 65535, "LU batch too large");
   for (int k0 = 0; k0 < n; k0 += kLuPanel) {
     const int kb = std::min(kLuPanel, n - k0), k1 = k0 + kb;
-    lu_panel_kernel<<<batch, 1024, 0, st>>>(n, k0, kb, A, lda, sA, piv, sP, info);
-    check_launch("lu_panel_kernel");
+    const size_t psm = sizeof(double) * (size_t)(n - k0) * (kb + 1);
+    if (psm <= kPanelSmemMax) {
+      ensure_smem(reinterpret_cast<const void*>(lu_panel_smem_kernel), psm);
+      lu_panel_smem_kernel<<<batch, 1024, psm, st>>>(n, k0, kb, A, lda, sA, piv, sP, info);
+      check_launch("lu_panel_smem_kernel");
+    } else {
+      lu_panel_kernel<<<batch, 1024, 0, st>>>(n, k0, kb, A, lda, sA, piv, sP, info);
+      check_launch("lu_panel_kernel");
+    }
     lu_swap_trsm_kernel<<<dim3((n + 255) / 256, batch), 256, 0, st>>>(n, k0, kb, A, lda, sA, piv,
                                                                        sP);
     check_launch("lu_swap_trsm_kernel");
@@ -840,11 +912,11 @@ void lu_solve(cudaStream_t st, bool trans, int n, const T* LU, int lda, long lon
               const int* piv, long long sP, T* X, int ldx, long long sX, int nrhs, int batch) {
   if (n <= 0 || nrhs <= 0 || batch <= 0) return;
   if constexpr (std::is_same<T, double>::value) {
-    // transposed solves of large blocks with many columns: panels + GEMM
+    // transposed solves of blocks from 128 with many columns: panels + GEMM
     // updates over all SMs (the tiled one-CTA-per-chunk kernel below serves
     // the other orientation: measured faster there, 163 vs 184 ms in a
     // 1024-point red-black factorisation)
-    if (trans && n >= 512 && nrhs >= 64 && batch <= 65535) {
+    if (trans && n >= 128 && nrhs >= 64 && batch <= 65535) {
       lu_solve_blocked(st, trans, n, LU, lda, sA, piv, sP, X, ldx, sX, nrhs, batch);
       return;
     }
