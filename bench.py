@@ -88,6 +88,11 @@ class ClockSampler:
                 ["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.QUERY,
                  "--format=csv,noheader,nounits", "-lms", "50"], stdout=self.f,
                 stderr=subprocess.DEVNULL)
+            # the sampler takes a moment to start: wait (at most 5 s) for its
+            # first sample, so the timed region is covered
+            t0 = time.time()
+            while time.time() - t0 < 5.0 and os.path.getsize(self.path) == 0:
+                time.sleep(0.02)
         except Exception:
             self.proc = None
 
