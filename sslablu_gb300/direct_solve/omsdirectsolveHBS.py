@@ -32,6 +32,24 @@ from .omsdirectsolve import DirectSolver
 # ---------------------------------------------------------------------------
 # operator helpers
 # ---------------------------------------------------------------------------
+def _refine(solver, rhs, tol, maxit):
+    """Iterative refinement of solver.solve against solver.apply (the exact
+    block-tridiagonal operator, float64): x += solve(b - A x) until every
+    column's relative residual is at most tol.  Returns (x, solves, relres)."""
+    B, one = dv.prepare_rhs(rhs)
+    bn = torch.linalg.norm(B, dim=0).clamp_min(np.finfo(np.float64).tiny)
+    X = solver.solve(B)
+    it, rel = 1, float("inf")
+    while True:
+        R = B - solver.apply(X)
+        rel = float((torch.linalg.norm(R, dim=0) / bn).max())
+        if rel <= tol or it >= maxit:
+            break
+        X = X + solver.solve(R)
+        it += 1
+    return dv.finish(X, rhs, one), it, rel
+
+
 class _DevOp:
     """Device operator with the scipy LinearOperator call surface."""
 
@@ -275,6 +293,30 @@ class ThomasSolverHBS(DirectSolver):
             raise ValueError("Factorization not set")
         return dv.finish(x, rhs, one)
 
+    def apply(self, x):
+        """Beyond upstream: the identity-diagonal block-tridiagonal operator
+        the solver was factored from (factorize without T), applied with the
+        given couplings in float64."""
+        if self.solve_method != "id_diag":
+            raise NotImplementedError("apply needs the identity-diagonal factorisation")
+        X, one = dv.prepare_rhs(x)
+        m, n = self.m, len(self.A)
+        Y = X.clone()
+        for i in range(n + 1):
+            blk = slice(i * m, (i + 1) * m)
+            if i > 0:
+                Y[blk] += dv.dev_apply(self.A[i - 1], X[(i - 1) * m:i * m])
+            if i < n:
+                Y[blk] += dv.dev_apply(self.C[i], X[(i + 1) * m:(i + 2) * m])
+        return dv.finish(Y, x, one)
+
+    def solve_refined(self, rhs, tol=1e-10, maxit=5):
+        """Beyond upstream: solve() refined against apply() (float64
+        residuals with the exact couplings), which removes the error of the
+        HBS compressions.  Returns (x, solves, worst column relative
+        residual)."""
+        return _refine(self, rhs, tol, maxit)
+
 
 # ---------------------------------------------------------------------------
 # HBS red-black, omsdirectsolveHBS.py:359-558
@@ -400,3 +442,29 @@ class RedBlackSolverHBS(DirectSolver):
                 blk = vs[l - 1][(i + 1) * m:(i + 2) * m] - c
                 vs[l - 1][(i + 1) * m:(i + 2) * m] = dv.dev_solve(Th[i + 1], blk)
         return dv.finish(vs[0], rhs, one)
+
+    def apply(self, x):
+        """Beyond upstream: the block-tridiagonal operator the solver was
+        factored from (the level-0 couplings and diagonal blocks as given,
+        float64)."""
+        SiM, T, _, SiP = self.RB[0]
+        m, nS = self.m, len(SiM)
+        X, one = dv.prepare_rhs(x)
+        Y = torch.empty_like(X)
+        for i in range(nS):
+            y = dv.dev_apply(T[i], X[i * m:(i + 1) * m])
+            if i > 0:
+                y = y + dv.dev_apply(SiM[i], X[(i - 1) * m:i * m])
+            if i < nS - 1:
+                y = y + dv.dev_apply(SiP[i], X[(i + 1) * m:(i + 2) * m])
+            Y[i * m:(i + 1) * m] = y
+        return dv.finish(Y, x, one)
+
+    def solve_refined(self, rhs, tol=1e-10, maxit=5):
+        """Beyond upstream: solve() refined against apply() (float64
+        residuals with the exact couplings): the red-black levels compress
+        Schur complements sampled through the compressed blocks below them,
+        and at large sizes their errors compound (3-5e-7 at 32 slabs x 4096
+        points); refinement restores the tolerance.  Returns (x, solves,
+        worst column relative residual)."""
+        return _refine(self, rhs, tol, maxit)

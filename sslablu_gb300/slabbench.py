@@ -135,6 +135,11 @@ def hbs(a):
             X = solver.solve(Bd).cpu().numpy()
             res[name] = {"factor_ms": 1e3 * t_f, "solve_64rhs_ms": 1e3 * t_s,
                          "rhs_per_s_64rhs": 64 / t_s, "relres_64rhs": _relres(S, X, B)}
+            # refined against the exact couplings to 1e-10
+            t_r = _events(lambda: solver.solve_refined(Bd), max(1, reps // 2))
+            Xr, it, _ = solver.solve_refined(Bd)
+            res[name].update({"refined_solve_64rhs_ms": 1e3 * t_r, "refined_solves": it,
+                              "relres_refined_64rhs": _relres(S, Xr.cpu().numpy(), B)})
         return res
 
     out.update(gpu_arms(a.m, a.reps))

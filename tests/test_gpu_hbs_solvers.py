@@ -82,3 +82,31 @@ def test_rbhbs_kernel(golden, rk):
     T.factorize(_ops(S, tree))
     y = T.solve(g["b"])
     assert relerr(y, g["x_th_%d" % rk]) < 1e-10
+
+
+def test_hbs_slab_solvers_refined(golden):
+    """solve_refined on the exponential-kernel system at rank 16: the
+    red-black solve is truncation bound (plain residual ~1e-5) and refinement
+    against the exact couplings brings it to 1e-10; Thomas is resolved
+    already (one solve); apply() is the dense block-tridiagonal matrix."""
+    need_gpu()
+    from sslablu_gb300.direct_solve.omsdirectsolveHBS import RedBlackSolverHBS, ThomasSolverHBS
+    g = golden("rbhbs_kernel")
+    m, nS, leaf, nlev = int(g["m"]), int(g["nS"]), int(g["leaf"]), int(g["nlev"])
+    tree = types.SimpleNamespace(perm_leaf=np.arange(m), nleaves=m // leaf, nlevels=nlev)
+    S = kernel_system(m, nS)
+    M = tridiag_matrix(S, m)
+    b = g["b"]
+    x0 = np.random.default_rng(3).standard_normal(M.shape[0])
+    for seed, make, bound in ((11, lambda: RedBlackSolverHBS(m, 16, tree, False), True),
+                              (12, lambda: ThomasSolverHBS(m, 16), False)):
+        np.random.seed(seed)
+        sv = make()
+        sv.factorize(_ops(S, tree))
+        assert relerr(sv.apply(x0), M @ x0) < 1e-13
+        x, it, rel = sv.solve_refined(b, tol=1e-10, maxit=8)
+        if bound:
+            assert relerr(M @ sv.solve(b), b) > 1e-8      # the plain solve is truncation bound
+            assert 2 <= it <= 8
+        assert x.shape == b.shape and it >= 1
+        assert rel <= 1e-10 and relerr(M @ x, b) < 1e-10
