@@ -951,19 +951,6 @@ template void lu_solve<float>(cudaStream_t, bool, int, const float*, int, long l
 // ============================================================== permutations etc.
 namespace {
 template <typename T>
-__global__ void permute_rows_kernel(bool scatter, int n, int ncol, const int64_t* __restrict__ perm,
-                                    const T* __restrict__ src, int lds, T* __restrict__ dst,
-                                    int ldd) {
-  long long total = (long long)n * ncol;
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
-       e += (long long)gridDim.x * blockDim.x) {
-    int i = (int)(e / ncol), c = (int)(e % ncol);
-    long long p = perm[i];
-    if (scatter) dst[p * ldd + c] = src[(long long)i * lds + c];
-    else dst[(long long)i * ldd + c] = src[p * lds + c];
-  }
-}
-template <typename T>
 __global__ void axpby_kernel(long long n, T a, const T* __restrict__ x, T b, T* __restrict__ y) {
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
        e += (long long)gridDim.x * blockDim.x)
@@ -985,19 +972,6 @@ inline int grid_for(long long n) {
   return (int)(g < 1 ? 1 : (g > cap ? cap : g));
 }
 }  // namespace
-
-template <typename T>
-void permute_rows(cudaStream_t st, bool scatter, int n, int ncol, const int64_t* perm,
-                  const T* src, int lds, T* dst, int ldd) {
-  if (n <= 0 || ncol <= 0) return;
-  permute_rows_kernel<T><<<grid_for((long long)n * ncol), 256, 0, st>>>(scatter, n, ncol, perm,
-                                                                        src, lds, dst, ldd);
-  check_launch("permute_rows_kernel");
-}
-template void permute_rows<double>(cudaStream_t, bool, int, int, const int64_t*, const double*,
-                                   int, double*, int);
-template void permute_rows<float>(cudaStream_t, bool, int, int, const int64_t*, const float*, int,
-                                  float*, int);
 
 template <typename T>
 void axpby(cudaStream_t st, long long n, T a, const T* x, T b, T* y) {

@@ -158,12 +158,6 @@ template <typename T>
 void lu_solve(cudaStream_t st, bool trans, int n, const T* LU, int lda, long long sA,
               const int* piv, long long sP, T* X, int ldx, long long sX, int nrhs, int batch);
 
-// Gather / scatter rows: dst[i, :] = src[perm[i], :] (gather) or
-// dst[perm[i], :] = src[i, :] (scatter).  Row length ncol, leading dims given.
-template <typename T>
-void permute_rows(cudaStream_t st, bool scatter, int n, int ncol, const int64_t* perm,
-                  const T* src, int lds, T* dst, int ldd);
-
 // Elementwise helpers.
 template <typename T>
 void axpby(cudaStream_t st, long long n, T a, const T* x, T b, T* y);  // y = a x + b y
