@@ -280,7 +280,7 @@ class SolveServer:
         return [flat[o:o + n * c].reshape(n, c) for o, n, c in layout]
 
     def _worker(self, w):
-        stream = torch.cuda.Stream()
+        stream = None   # created with the first job (no device work before)
         stage = {}
         while True:
             job = self._jobs.get()
@@ -288,6 +288,8 @@ class SolveServer:
                 return
             t_start = self._now()
             try:
+                if stream is None:
+                    stream = torch.cuda.Stream()
                 if self.group_solve is not None:
                     Xs, err = self._solve_group(job, stream, stage), None
                 else:
