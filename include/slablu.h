@@ -141,6 +141,13 @@ int slu_ulv_solve_into(slu_handle_t h, slu_hbs_t op, const double* X, int ldx, d
 int slu_ulv_solve_plan_create(slu_handle_t h, slu_hbs_t op, const double* X, int ldx, double* Y,
                               int ldy, int nrhs, int trans, slu_solve_plan_t* out);
 int slu_ulv_solve_plan_launch(slu_handle_t h, slu_solve_plan_t plan, int wait);
+/* The grouped solve of slu_ulv_solve_grouped (B[i] <- A_i^{-1} B[i], mode N)
+ * for fixed blocks as a solve plan: the step tables of every member are
+ * built and uploaded once and the group's launches captured as one CUDA
+ * graph; launch and destroy it like any solve plan. */
+int slu_ulv_solve_grouped_plan_create(slu_handle_t h, int count, const slu_hbs_t* ops,
+                                      double* const* B, const int* ldb, const int* nrhs,
+                                      slu_solve_plan_t* out);
 int slu_ulv_solve_plan_destroy(slu_solve_plan_t plan);
 
 /* Single-precision copy of the ULV factors and a float32 solve with the same

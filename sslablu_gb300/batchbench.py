@@ -11,6 +11,8 @@ solves every system once.  Arms, each timed with CUDA events on the current
 stream after warm-up (the factors of the batch exceed L2, so no flush):
   * per_operator_f64: one ``HBSMAT.solve`` sweep per system (2L-1 launches each);
   * grouped_f64: one grouped sweep for the whole batch (2 maxL - 1 launches);
+  * grouped_f64_plan: the same sweep through a grouped solve plan (step
+    tables built and uploaded once, the launches replayed as one graph);
   * grouped_mixed: grouped float32 sweeps refined to 1e-10 with double-float
     residuals.
 Prints one JSON line: RHS/s and systems/s per arm, the worst relative
@@ -76,7 +78,7 @@ def main():
     ap.add_argument("--reps", type=int, default=20)
     ap.add_argument("--seed", type=int, default=20261205)
     a = ap.parse_args()
-    from .grouped import solve_grouped_device
+    from .grouped import GroupedSolvePlan, solve_grouped_device
 
     t0 = time.perf_counter()
     ops = build_batch(a.systems, a.seed)
@@ -96,6 +98,11 @@ def main():
 
     def grouped_f64():
         solve_grouped_device(ops, work)
+
+    plan = GroupedSolvePlan(ops, work)
+
+    def grouped_f64_plan():
+        plan()
 
     outs = [torch.empty_like(r) for r in rhs]
     iters = []
@@ -123,6 +130,7 @@ def main():
                      zip(*np.unique([H.shape[0] for H in ops], return_counts=True))}}
     for name, fn, xs in [("per_operator_f64", per_operator, work),
                          ("grouped_f64", grouped_f64, work),
+                         ("grouped_f64_plan", grouped_f64_plan, work),
                          ("grouped_mixed", grouped_mixed, outs)]:
         reset()
         fn()          # first call: one-time preparation (factor copies)

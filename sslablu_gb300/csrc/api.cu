@@ -287,6 +287,23 @@ int slu_ulv_solve_plan_create(slu_handle_t h, slu_hbs_t op, const double* X, int
   });
 }
 
+int slu_ulv_solve_grouped_plan_create(slu_handle_t h, int count, const slu_hbs_t* ops,
+                                      double* const* B, const int* ldb, const int* nrhs,
+                                      slu_solve_plan_t* out) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h && out, "null argument");
+    SLU_REQUIRE(count >= 0 && (count == 0 || ops), "null argument");
+    std::vector<slu::Hbs*> H(count);
+    for (int i = 0; i < count; ++i) {
+      SLU_REQUIRE(ops[i], "null operator");
+      H[i] = &ops[i]->H;
+    }
+    auto p = std::make_unique<slu_solve_plan_s>();
+    slu::grouped_solve_plan_create(h->h, count, H.data(), B, ldb, nrhs, p->P);
+    *out = p.release();
+  });
+}
+
 int slu_ulv_solve_plan_launch(slu_handle_t h, slu_solve_plan_t plan, int wait) {
   return guard(h, [&] {
     SLU_REQUIRE(h && plan, "null argument");

@@ -405,6 +405,90 @@ void hbs_solve_grouped(Handle& h, int count, Hbs* const* ops, double* const* B, 
   launch_solve<double>(st, steps, reinterpret_cast<const StepSeg<double>*>(dtab + at));
 }
 
+void grouped_solve_plan_create(Handle& h, int count, Hbs* const* ops, double* const* B,
+                               const int* ldb, const int* c, SolvePlan& P) {
+  SLU_REQUIRE(count >= 0 && (count == 0 || (ops && B && ldb && c)), "null argument");
+  std::vector<const Hbs*> H;
+  std::vector<double*> Bm;
+  std::vector<int> cm, ldm;
+  for (int i = 0; i < count; ++i) {
+    SLU_REQUIRE(ops[i], "null operator");
+    SLU_REQUIRE(c[i] >= 0, "bad right-hand-side count");
+    if (c[i] == 0) continue;
+    SLU_REQUIRE(B[i] && ldb[i] >= c[i], "bad right-hand side");
+    SLU_REQUIRE(ops[i]->has_ulv && ops[i]->has_sweep, "ULV factors not computed");
+    H.push_back(ops[i]);
+    Bm.push_back(B[i]);
+    cm.push_back(c[i]);
+    ldm.push_back(ldb[i]);
+  }
+  const int m = (int)H.size();
+  for (const Hbs* x : H) {
+    P.H.push_back(x);
+    P.alive.push_back(x->alive);
+    P.gen.push_back(x->sweep_gen);
+  }
+  if (m == 0) return;
+  cudaStream_t st = h.stream;
+  // plan-owned device regions: the task table, then five buffers per member
+  size_t nseg = 0;
+  for (const Hbs* x : H) nseg += 2 * (size_t)x->L;
+  Plan plan;
+  plan.add(blob_bound(nseg * sizeof(StepSeg<double>), 1));
+  std::vector<size_t> stride(m);
+  for (int i = 0; i < m; ++i) {
+    stride[i] = round64((size_t)H[i]->N * cm[i]);
+    plan.add(5 * stride[i] * sizeof(double));
+  }
+  P.scratch.alloc(plan.total(), st);
+  char* base = static_cast<char*>(P.scratch.p);
+  char* dtab = base;
+  size_t off = (plan.bytes[0] + 255) & ~size_t(255);
+  std::vector<SolveBufs<double>> buf(m);
+  for (int i = 0; i < m; ++i) {
+    double* s = reinterpret_cast<double*>(base + off);
+    buf[i].ru = s;
+    for (int j = 0; j < 4; ++j) buf[i].P[j] = s + (j + 1) * stride[i];
+    off += (5 * stride[i] * sizeof(double) + 255) & ~size_t(255);
+  }
+  StepTable<double> steps;
+  build_solve<double>(H, cm, Bm, ldm, buf, steps);
+  Blob blob;
+  const size_t at = blob.put(steps.segs);
+  SLU_REQUIRE(blob.host.size() <= plan.bytes[0], "task table overflow");
+  upload(h, blob, dtab);
+  auto kern = group_step_kernel<double>;
+  for (const sweep::LaunchPlan& p : steps.plan)
+    if (p.ctas > 0) ensure_smem(reinterpret_cast<const void*>(kern), p.smem);
+  SLU_CHECK_CUDA(cudaStreamSynchronize(st));   // table and buffers in place before the capture
+  cudaStream_t cs = nullptr;
+  SLU_CHECK_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  cudaGraph_t g = nullptr;
+  const long long n0 = launch_thread();
+  try {
+    SLU_CHECK_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+    try {
+      launch_solve<double>(cs, steps, reinterpret_cast<const StepSeg<double>*>(dtab + at));
+    } catch (...) {
+      cudaStreamEndCapture(cs, &g);
+      if (g) cudaGraphDestroy(g);
+      throw;
+    }
+    SLU_CHECK_CUDA(cudaStreamEndCapture(cs, &g));
+    P.kernels = launch_thread() - n0;
+    launch_total() -= P.kernels;
+    launch_thread() = n0;
+    const cudaError_t e = cudaGraphInstantiate(&P.exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess)
+      throw Error(SLU_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+  } catch (...) {
+    cudaStreamDestroy(cs);
+    throw;
+  }
+  SLU_CHECK_CUDA(cudaStreamDestroy(cs));
+}
+
 void hbs_apply_grouped(Handle& h, int count, Hbs* const* ops, const int* trans,
                        const double* const* X, const int* ldx, double* const* Y, const int* ldy,
                        const int* c) {

@@ -147,9 +147,10 @@ struct Hbs {
 // and solution buffers, with its own scratch (ulv_solve.cu): a launch is one
 // graph launch instead of one kernel launch per tree step.
 struct SolvePlan {
-  const Hbs* H = nullptr;
-  std::weak_ptr<char> alive;
-  unsigned long long gen = 0;
+  // the operators the graph reads (one; or every member of a grouped solve)
+  std::vector<const Hbs*> H;
+  std::vector<std::weak_ptr<char>> alive;
+  std::vector<unsigned long long> gen;
   DevBuf scratch;
   cudaGraphExec_t exec = nullptr;
   long long kernels = 0;
@@ -163,6 +164,10 @@ struct SolvePlan {
 void solve_plan_create(Handle& h, const Hbs& H, const double* X, int ldx, double* Y, int ldy,
                        int c, bool trans, SolvePlan& P);
 void solve_plan_launch(Handle& h, SolvePlan& P, bool wait);
+// The grouped mode-N solve of hbs_solve_grouped (B[i] <- A_i^{-1} B[i]) for
+// fixed blocks, captured once: step tables built and uploaded at creation.
+void grouped_solve_plan_create(Handle& h, int count, Hbs* const* ops, double* const* B,
+                               const int* ldb, const int* c, SolvePlan& P);
 
 // compression + interleaved ULV (HBSnew.HBSMAT.constructHBS_ULV)
 void hbs_compress(Handle& h, Hbs& H, int Nb_leaf, int rk, int s, const double* Om,

@@ -202,15 +202,19 @@ void solve_plan_create(Handle& h, const Hbs& H, const double* X, int ldx, double
     throw;
   }
   SLU_CHECK_CUDA(cudaStreamDestroy(cs));
-  P.H = &H;
-  P.alive = H.alive;
-  P.gen = H.sweep_gen;
+  P.H = {&H};
+  P.alive = {H.alive};
+  P.gen = {H.sweep_gen};
 }
 
 void solve_plan_launch(Handle& h, SolvePlan& P, bool wait) {
-  if (P.alive.expired()) throw Error(SLU_ERR_STATE, "the solve plan's operator was destroyed");
-  if (P.H->sweep_gen != P.gen)
-    throw Error(SLU_ERR_STATE, "the operator was refactored after the solve plan was made");
+  for (size_t i = 0; i < P.H.size(); ++i) {
+    if (P.alive[i].expired())
+      throw Error(SLU_ERR_STATE, "an operator of the solve plan was destroyed");
+    if (P.H[i]->sweep_gen != P.gen[i])
+      throw Error(SLU_ERR_STATE, "an operator was refactored after the solve plan was made");
+  }
+  if (!P.exec) return;   // a grouped plan without members
   SLU_CHECK_CUDA(cudaGraphLaunch(P.exec, h.stream));
   count_launches(P.kernels);
   if (wait) SLU_CHECK_CUDA(cudaStreamSynchronize(h.stream));

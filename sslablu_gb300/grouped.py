@@ -49,6 +49,42 @@ def solve_grouped_device(ops, Bs, precision="f64", tol=1e-10, maxit=10, Xs=None)
     return Xs, it.value, list(np.frombuffer(rr, dtype=np.float64))
 
 
+class GroupedSolvePlan:
+    """solve_grouped_device(ops, Bs) for fixed blocks, captured once
+    (slu_ulv_solve_grouped_plan_create): ``plan()`` solves whatever the Bs
+    hold, in place, with one graph launch on the current stream."""
+
+    def __init__(self, ops, Bs):
+        n = len(ops)
+        for H, B in zip(ops, Bs):
+            if B.dtype != torch.float64 or not B.is_cuda or not B.is_contiguous() or B.dim() != 2:
+                raise ValueError("right-hand sides must be contiguous 2-D float64 CUDA tensors")
+            if B.shape[0] != H.shape[0]:
+                raise ValueError("right-hand side has %d rows, operator %d"
+                                 % (B.shape[0], H.shape[0]))
+        self.ops, self.Bs = list(ops), list(Bs)   # the plan reads and writes these
+        op_arr = (ctypes.c_void_p * max(n, 1))(*[H._op for H in ops])
+        bp = (ctypes.c_void_p * max(n, 1))(*[t.data_ptr() for t in Bs])
+        ld = (ctypes.c_int * max(n, 1))(*[t.shape[1] for t in Bs])
+        p = ctypes.c_void_p()
+        L.check(L.lib().slu_ulv_solve_grouped_plan_create(L.handle(), n, op_arr, bp, ld, ld,
+                                                          ctypes.byref(p)))
+        self._p = p
+        self._launch = L.lib().slu_ulv_solve_plan_launch
+
+    def __call__(self):
+        L.check(self._launch(L.handle(), self._p, 0))
+        return self.Bs
+
+    def close(self):
+        if getattr(self, "_p", None) is not None and L._lib is not None:
+            L.lib().slu_ulv_solve_plan_destroy(self._p)
+        self._p = None
+
+    def __del__(self):
+        self.close()
+
+
 def apply_grouped(ops, Xs, trans=False, Ys=None):
     """Grouped apply on contiguous float64 CUDA tensors: Ys[i] = A_i Xs[i]
     (or A_i^T Xs[i] where ``trans`` -- one flag, or one per member -- is

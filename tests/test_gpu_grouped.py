@@ -141,3 +141,41 @@ def test_grouped_apply_equals_solo():
     for H, X, Y, t in zip(ops, Xs, Ys, trans):
         ref = H._dev_apply(X, t)
         assert torch.equal(Y, ref)
+
+
+def test_grouped_solve_plan_equals_grouped_solve():
+    """A grouped solve plan (step tables built once, launches replayed as one
+    graph) gives the grouped solve's results bitwise, with new data in the
+    blocks on every call, and refuses to run after a member is refactored."""
+    need_gpu()
+    import torch
+    from sslablu_gb300 import _lib as L
+    from sslablu_gb300.grouped import GroupedSolvePlan, solve_grouped_device
+    from sslablu_gb300.matAssembly.HBS.HBSnew import HBSMAT
+    from sslablu_gb300.synthetic import random_hbs_factors
+    ops = []
+    for j, (N, k) in enumerate([(128, 16), (512, 24), (256, 33), (1024, 16)]):
+        Lv = int(np.log2(N // 64)) + 1
+        U, D, V, Nbvec = random_hbs_factors(k, 64, Lv, quad=False,
+                                            rng=np.random.default_rng(j), shift=16.0)
+        ops.append(HBSMAT().set_mats(U, D, V, list(Nbvec), fac=2))
+        ops[-1].compute_ULV()
+    cols = [3, 8, 1, 5]
+    Bs = [torch.empty((H.shape[0], c), dtype=torch.float64, device="cuda")
+          for H, c in zip(ops, cols)]
+    plan = GroupedSolvePlan(ops, Bs)
+    rng = np.random.default_rng(7)
+    for _ in range(3):
+        data = [rng.standard_normal(tuple(B.shape)) for B in Bs]
+        for B, d in zip(Bs, data):
+            B.copy_(torch.from_numpy(d))
+        plan()
+        ref = [torch.from_numpy(d).cuda() for d in data]
+        solve_grouped_device(ops, ref)
+        torch.cuda.synchronize()
+        for B, R in zip(Bs, ref):
+            assert torch.equal(B, R)
+    ops[1].compute_ULV()
+    with pytest.raises(L.SluError):
+        plan()
+    plan.close()
