@@ -541,6 +541,12 @@ def run_other(args):
                     config={"workload": g["workload"], "sizes": g["sizes"],
                             "arm": "grouped float64 sweep through a grouped solve plan (step "
                                    "tables built once, launches replayed as one CUDA graph)"},
+                    mixed={"value": g["grouped_mixed_plan"]["rhs_per_s"], "unit": "RHS/s",
+                           "dtype": "grouped double-float sweeps + double-float residuals, "
+                                    "refined to 1e-10 (grouped refinement plan)",
+                           "ms_per_step": g["grouped_mixed_plan"]["ms_per_step"],
+                           "speedup_vs_plain": g["grouped_mixed_plan"]["rhs_per_s"] /
+                           g["grouped_f64_plan"]["rhs_per_s"]},
                     arms=g,
                     cpu_baseline={"value": nrhs / ts, "unit": "RHS/s", "cores": os.cpu_count(),
                                   "kind": "port",

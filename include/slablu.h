@@ -41,6 +41,7 @@ typedef struct slu_handle_s* slu_handle_t;
 typedef struct slu_hbs_s* slu_hbs_t;
 typedef struct slu_dense_rb_s* slu_rb_t;
 typedef struct slu_solve_plan_s* slu_solve_plan_t;
+typedef struct slu_refine_plan_s* slu_refine_plan_t;
 
 /* ---------------------------------------------------------------- runtime */
 int slu_version(void);
@@ -141,6 +142,18 @@ int slu_ulv_solve_into(slu_handle_t h, slu_hbs_t op, const double* X, int ldx, d
 int slu_ulv_solve_plan_create(slu_handle_t h, slu_hbs_t op, const double* X, int ldx, double* Y,
                               int ldy, int nrhs, int trans, slu_solve_plan_t* out);
 int slu_ulv_solve_plan_launch(slu_handle_t h, slu_solve_plan_t plan, int wait);
+/* The grouped refinement of slu_refine_grouped for fixed blocks B[i] -> X[i]
+ * (device pointers), made once: buffers and task tables built and uploaded
+ * at creation, an iteration replayed as CUDA graphs.  slu_refine_plan_run
+ * refines whatever the B[i] hold (same results, iteration count and errors
+ * as slu_refine_grouped); a plan refuses to run (SLU_ERR_STATE) once one of
+ * its operators is refactored or destroyed.  Beyond upstream. */
+int slu_refine_grouped_plan_create(slu_handle_t h, int count, const slu_hbs_t* ops,
+                                   const double* const* B, const int* ldb, double* const* X,
+                                   const int* ldx, const int* nrhs, slu_refine_plan_t* out);
+int slu_refine_plan_run(slu_handle_t h, slu_refine_plan_t plan, double tol, int maxit,
+                        int* iters_out, double* relres_out);
+int slu_refine_plan_destroy(slu_refine_plan_t plan);
 /* The grouped solve of slu_ulv_solve_grouped (B[i] <- A_i^{-1} B[i], mode N)
  * for fixed blocks as a solve plan: the step tables of every member are
  * built and uploaded once and the group's launches captured as one CUDA

@@ -47,6 +47,9 @@ SIGNATURES = {
     "slu_ulv_solve_plan_create": [P, P, P, c_int, P, c_int, c_int, c_int, ctypes.POINTER(c_void_p)],
     "slu_ulv_solve_plan_launch": [P, P, c_int],
     "slu_ulv_solve_grouped_plan_create": [P, c_int, P, P, P, P, ctypes.POINTER(c_void_p)],
+    "slu_refine_grouped_plan_create": [P, c_int, P, P, P, P, P, P, ctypes.POINTER(c_void_p)],
+    "slu_refine_plan_run": [P, P, c_double, c_int, P, P],
+    "slu_refine_plan_destroy": [P],
     "slu_ulv_solve_plan_destroy": [P],
     "slu_ulv_autotune": [P, P, c_int, c_int, c_int, P, c_int, P],
     "slu_hbs_set_refine_inner": [P, c_int],

@@ -14,7 +14,9 @@ stream after warm-up (the factors of the batch exceed L2, so no flush):
   * grouped_f64_plan: the same sweep through a grouped solve plan (step
     tables built and uploaded once, the launches replayed as one graph);
   * grouped_mixed: grouped float32 sweeps refined to 1e-10 with double-float
-    residuals.
+    residuals;
+  * grouped_mixed_plan: the same through a grouped refinement plan (buffers
+    and task tables built once, each iteration replayed as a CUDA graph).
 Prints one JSON line: RHS/s and systems/s per arm, the worst relative
 residual of each arm against the float64 operators, and launches per step.
 """
@@ -78,7 +80,7 @@ def main():
     ap.add_argument("--reps", type=int, default=20)
     ap.add_argument("--seed", type=int, default=20261205)
     a = ap.parse_args()
-    from .grouped import GroupedSolvePlan, solve_grouped_device
+    from .grouped import GroupedRefinePlan, GroupedSolvePlan, solve_grouped_device
 
     t0 = time.perf_counter()
     ops = build_batch(a.systems, a.seed)
@@ -111,6 +113,12 @@ def main():
         _, it, _ = solve_grouped_device(ops, rhs, "mixed", 1e-10, 10, Xs=outs)
         iters.append(it)
 
+    outs_p = [torch.empty_like(r) for r in rhs]
+    rplan = GroupedRefinePlan(ops, rhs, outs_p)
+
+    def grouped_mixed_plan():
+        rplan(1e-10, 10)
+
     def worst_residual(xs):
         w = 0.0
         for H, B, X in zip(ops, rhs, xs):
@@ -131,7 +139,8 @@ def main():
     for name, fn, xs in [("per_operator_f64", per_operator, work),
                          ("grouped_f64", grouped_f64, work),
                          ("grouped_f64_plan", grouped_f64_plan, work),
-                         ("grouped_mixed", grouped_mixed, outs)]:
+                         ("grouped_mixed", grouped_mixed, outs),
+                         ("grouped_mixed_plan", grouped_mixed_plan, outs_p)]:
         reset()
         fn()          # first call: one-time preparation (factor copies)
         torch.cuda.synchronize()

@@ -16,6 +16,9 @@ struct slu_hbs_s {
 struct slu_solve_plan_s {
   slu::SolvePlan P;
 };
+struct slu_refine_plan_s {
+  std::unique_ptr<slu::GroupRefinePlan> P;
+};
 struct slu_dense_rb_s {
   slu::RbSolver S;
   bool thomas = false;

@@ -381,6 +381,30 @@ std::vector<slu::Hbs*> group_ops(int count, const slu_hbs_t* ops) {
 }
 }  // namespace
 
+int slu_refine_grouped_plan_create(slu_handle_t h, int count, const slu_hbs_t* ops,
+                                   const double* const* B, const int* ldb, double* const* X,
+                                   const int* ldx, const int* nrhs, slu_refine_plan_t* out) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h && out, "null argument");
+    std::vector<slu::Hbs*> H = group_ops(count, ops);
+    auto p = std::make_unique<slu_refine_plan_s>();
+    p->P = slu::grouped_refine_plan_create(h->h, count, H.data(), B, ldb, X, ldx, nrhs);
+    *out = p.release();
+  });
+}
+
+int slu_refine_plan_run(slu_handle_t h, slu_refine_plan_t plan, double tol, int maxit,
+                        int* iters_out, double* relres_out) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h && plan && plan->P, "null argument");
+    plan->P->run(h->h, tol, maxit, iters_out, relres_out);
+  });
+}
+
+int slu_refine_plan_destroy(slu_refine_plan_t plan) {
+  return guard(nullptr, [&] { delete plan; });
+}
+
 int slu_ulv_solve_grouped(slu_handle_t h, int count, const slu_hbs_t* ops, double* const* B,
                           const int* ldb, const int* nrhs) {
   return guard(h, [&] {

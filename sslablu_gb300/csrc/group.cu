@@ -24,6 +24,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <memory>
 
 #include "hbs.cuh"
 #include "refine_kernels.cuh"
@@ -560,122 +561,164 @@ inline void accum_inner(cudaStream_t st, long long n, const float* y, double* x,
   check_launch("accum_k");
 }
 
+// Buffers, task tables and launches of one grouped refinement: the members
+// with columns, one contiguous device region (carved in the order below),
+// and the launches of an iteration (cast, inner sweep, correction,
+// double-float residual, column norms, norms to the host).
 template <typename T>
-void refine_grouped(Handle& h, int count, Hbs* const* ops, const double* const* B,
-                    const int* ldb, double* const* X, const int* ldx, const int* c, double tol,
-                    int maxit, int* iters, double* relres) {
-  constexpr bool kDf = sizeof(T) == 8;
-  std::vector<int> idx;
-  for (int i = 0; i < count; ++i) {
-    SLU_REQUIRE(ops[i], "null operator");
-    SLU_REQUIRE(c[i] >= 0, "bad right-hand-side count");
-    if (relres) relres[i] = 0.0;
-    if (c[i] == 0) continue;
-    SLU_REQUIRE(B[i] && X[i] && ldb[i] >= c[i] && ldx[i] >= c[i], "bad right-hand side");
-    SLU_REQUIRE(ops[i]->has_ulv, "ULV factors not computed");
-    idx.push_back(i);
-  }
-  if (iters) *iters = 0;
-  const int m = (int)idx.size();
-  if (m == 0) return;
-  cudaStream_t st = h.stream;
-  for (int i : idx) {
-    if (kDf && !ops[i]->has_dfs) hbs_make_dfs(h, *ops[i]);
-    if (!kDf && !ops[i]->has_f32) hbs_make_f32(h, *ops[i]);
-    if (!ops[i]->has_df) hbs_make_df(h, *ops[i]);
-  }
-  std::vector<const Hbs*> H(m);
-  std::vector<int> cm(m);
-  std::vector<size_t> off(m), stride(m);
-  size_t E = 0;
-  int C = 0;
-  size_t nseg = 0;
-  for (int j = 0; j < m; ++j) {
-    H[j] = ops[idx[j]];
-    cm[j] = c[idx[j]];
-    off[j] = E;
-    E += (size_t)H[j]->N * cm[j];
-    C += cm[j];
-    stride[j] = round64((size_t)H[j]->N * cm[j]);
-    nseg += 2 * (size_t)H[j]->L;
-  }
-  // device regions
+struct GroupRefine {
+  std::vector<int> idx, cm;
+  std::vector<const Hbs*> H;
+  int m = 0, C = 0;
+  size_t E = 0, nseg = 0;
+  std::vector<size_t> off, stride;
   Plan plan;
-  const size_t tab_bytes = blob_bound(nseg * (sizeof(StepSeg<T>) + sizeof(StepSeg<dfloat>)) +
-                                          (size_t)C * sizeof(ColSeg) + 2 * m * sizeof(CopySeg),
-                                      5);
-  plan.add(tab_bytes);
-  plan.add(8 * E);  // B
-  plan.add(8 * E);  // X
-  plan.add(8 * E);  // r
-  plan.add(sizeof(T) * E);  // inner right-hand sides / corrections
-  plan.add(16 * (size_t)C);  // [bn | rn]
-  plan.add(sizeof(dfloat) * E);  // X as double-float pairs (residual apply input)
-  plan.add(sizeof(dfloat) * E);  // A X as double-float pairs
-  for (int j = 0; j < m; ++j) plan.add(5 * stride[j] * sizeof(T));
-  for (int j = 0; j < m; ++j)
-    plan.add(sizeof(dfloat) * hbs_apply_scratch_elems(*H[j], cm[j]));
-  h.ws.reserve(plan.total(), st);
-  char* dtab = h.ws.take<char>(plan.bytes[0]);
-  double* dB = h.ws.take<double>(E);
-  double* dX = h.ws.take<double>(E);
-  double* dr = h.ws.take<double>(E);
-  T* df = h.ws.take<T>(E);
-  double* norms = h.ws.take<double>(2 * (size_t)C);
-  dfloat* xdf = h.ws.take<dfloat>(E);
-  dfloat* ydf = h.ws.take<dfloat>(E);
-  std::vector<SolveBufs<T>> sbuf(m);
-  for (int j = 0; j < m; ++j) {
-    T* s = h.ws.take<T>(5 * stride[j]);
-    sbuf[j].ru = s;
-    for (int q = 0; q < 4; ++q) sbuf[j].P[q] = s + (q + 1) * stride[j];
-  }
-  std::vector<ApplyBufs<dfloat>> abuf(m);
-  for (int j = 0; j < m; ++j)
-    abuf[j] = carve_apply(*H[j], cm[j], h.ws.take<dfloat>(hbs_apply_scratch_elems(*H[j], cm[j])));
-  // task tables
-  std::vector<T*> fB(m);
-  std::vector<const dfloat*> xX(m);
-  std::vector<dfloat*> rY(m);
-  for (int j = 0; j < m; ++j) {
-    fB[j] = df + off[j];
-    xX[j] = xdf + off[j];
-    rY[j] = ydf + off[j];
-  }
+  double *dB = nullptr, *dX = nullptr, *dr = nullptr, *norms = nullptr;
+  T* df = nullptr;
+  dfloat *xdf = nullptr, *ydf = nullptr;
   StepTable<T> ssteps;
-  build_solve<T>(H, cm, fB, cm, sbuf, ssteps);
   StepTable<dfloat> dsteps;
-  build_apply_df(H, cm, xX, rY, abuf, dsteps);
-  std::vector<ColSeg> cols;
-  cols.reserve(C);
-  std::vector<CopySeg> cin(m), cpy_out(m);
-  long long maxe = 1;
-  for (int j = 0; j < m; ++j) {
-    for (int q = 0; q < cm[j]; ++q) cols.push_back({(long long)(off[j] + q), H[j]->N, cm[j]});
-    cin[j] = {B[idx[j]], dB + off[j], ldb[idx[j]], cm[j], H[j]->N, cm[j]};
-    cpy_out[j] = {dX + off[j], X[idx[j]], cm[j], ldx[idx[j]], H[j]->N, cm[j]};
-    maxe = std::max(maxe, (long long)H[j]->N * cm[j]);
-  }
-  Blob blob;
-  const size_t a_s = blob.put(ssteps.segs), a_d = blob.put(dsteps.segs), a_c = blob.put(cols),
-               a_i = blob.put(cin), a_o = blob.put(cpy_out);
-  SLU_REQUIRE(blob.host.size() <= tab_bytes, "task table overflow");
-  upload(h, blob, dtab);
-  const auto* d_s = reinterpret_cast<const StepSeg<T>*>(dtab + a_s);
-  const auto* d_d = reinterpret_cast<const StepSeg<dfloat>*>(dtab + a_d);
-  const auto* d_c = reinterpret_cast<const ColSeg*>(dtab + a_c);
-  const auto* d_i = reinterpret_cast<const CopySeg*>(dtab + a_i);
-  const auto* d_o = reinterpret_cast<const CopySeg*>(dtab + a_o);
-  const dim3 cgrid(m, (unsigned)std::min<long long>(64, (maxe + 1023) / 1024));
-  const long long En = (long long)E;
-  double* host = reinterpret_cast<double*>(h.readback.acquire(16 * (size_t)C));
+  const StepSeg<T>* d_s = nullptr;
+  const StepSeg<dfloat>* d_d = nullptr;
+  const ColSeg* d_c = nullptr;
+  const CopySeg *d_i = nullptr, *d_o = nullptr;
+  dim3 cgrid;
+  double* host = nullptr;   // pinned [bn | rn], C each
 
-  auto iteration = [&](bool first) {
+  // Members with columns, their factor copies, the region's sizes.
+  bool init(Handle& h, int count, Hbs* const* ops, const double* const* B, const int* ldb,
+            double* const* X, const int* ldx, const int* c) {
+    constexpr bool kDf = sizeof(T) == 8;
+    for (int i = 0; i < count; ++i) {
+      SLU_REQUIRE(ops[i], "null operator");
+      SLU_REQUIRE(c[i] >= 0, "bad right-hand-side count");
+      if (c[i] == 0) continue;
+      SLU_REQUIRE(B[i] && X[i] && ldb[i] >= c[i] && ldx[i] >= c[i], "bad right-hand side");
+      SLU_REQUIRE(ops[i]->has_ulv, "ULV factors not computed");
+      idx.push_back(i);
+    }
+    m = (int)idx.size();
+    if (m == 0) return false;
+    for (int i : idx) {
+      if (kDf && !ops[i]->has_dfs) hbs_make_dfs(h, *ops[i]);
+      if (!kDf && !ops[i]->has_f32) hbs_make_f32(h, *ops[i]);
+      if (!ops[i]->has_df) hbs_make_df(h, *ops[i]);
+    }
+    H.resize(m);
+    cm.resize(m);
+    off.resize(m);
+    stride.resize(m);
+    for (int j = 0; j < m; ++j) {
+      H[j] = ops[idx[j]];
+      cm[j] = c[idx[j]];
+      off[j] = E;
+      E += (size_t)H[j]->N * cm[j];
+      C += cm[j];
+      stride[j] = round64((size_t)H[j]->N * cm[j]);
+      nseg += 2 * (size_t)H[j]->L;
+    }
+    plan.add(blob_bound(nseg * (sizeof(StepSeg<T>) + sizeof(StepSeg<dfloat>)) +
+                            (size_t)C * sizeof(ColSeg) + 2 * m * sizeof(CopySeg),
+                        5));
+    plan.add(8 * E);  // B
+    plan.add(8 * E);  // X
+    plan.add(8 * E);  // r
+    plan.add(sizeof(T) * E);  // inner right-hand sides / corrections
+    plan.add(16 * (size_t)C);  // [bn | rn]
+    plan.add(sizeof(dfloat) * E);  // X as double-float pairs (residual apply input)
+    plan.add(sizeof(dfloat) * E);  // A X as double-float pairs
+    for (int j = 0; j < m; ++j) plan.add(5 * stride[j] * sizeof(T));
+    for (int j = 0; j < m; ++j)
+      plan.add(sizeof(dfloat) * hbs_apply_scratch_elems(*H[j], cm[j]));
+    return true;
+  }
+
+  // Carves the region (plan.total() bytes at base), builds the task tables
+  // and uploads them on h's stream.
+  void carve(Handle& h, char* base, const double* const* B, const int* ldb, double* const* X,
+             const int* ldx) {
+    size_t at = 0;
+    auto take = [&](size_t bytes) {
+      char* p = base + at;
+      at += (bytes + 255) & ~size_t(255);
+      return p;
+    };
+    char* dtab = take(plan.bytes[0]);
+    dB = reinterpret_cast<double*>(take(8 * E));
+    dX = reinterpret_cast<double*>(take(8 * E));
+    dr = reinterpret_cast<double*>(take(8 * E));
+    df = reinterpret_cast<T*>(take(sizeof(T) * E));
+    norms = reinterpret_cast<double*>(take(16 * (size_t)C));
+    xdf = reinterpret_cast<dfloat*>(take(sizeof(dfloat) * E));
+    ydf = reinterpret_cast<dfloat*>(take(sizeof(dfloat) * E));
+    std::vector<SolveBufs<T>> sbuf(m);
+    for (int j = 0; j < m; ++j) {
+      T* s = reinterpret_cast<T*>(take(5 * stride[j] * sizeof(T)));
+      sbuf[j].ru = s;
+      for (int q = 0; q < 4; ++q) sbuf[j].P[q] = s + (q + 1) * stride[j];
+    }
+    std::vector<ApplyBufs<dfloat>> abuf(m);
+    for (int j = 0; j < m; ++j)
+      abuf[j] = carve_apply(*H[j], cm[j],
+                            reinterpret_cast<dfloat*>(take(sizeof(dfloat) *
+                                                           hbs_apply_scratch_elems(*H[j], cm[j]))));
+    std::vector<T*> fB(m);
+    std::vector<const dfloat*> xX(m);
+    std::vector<dfloat*> rY(m);
+    for (int j = 0; j < m; ++j) {
+      fB[j] = df + off[j];
+      xX[j] = xdf + off[j];
+      rY[j] = ydf + off[j];
+    }
+    build_solve<T>(H, cm, fB, cm, sbuf, ssteps);
+    build_apply_df(H, cm, xX, rY, abuf, dsteps);
+    std::vector<ColSeg> cols;
+    cols.reserve(C);
+    std::vector<CopySeg> cin(m), cpy_out(m);
+    long long maxe = 1;
+    for (int j = 0; j < m; ++j) {
+      for (int q = 0; q < cm[j]; ++q) cols.push_back({(long long)(off[j] + q), H[j]->N, cm[j]});
+      cin[j] = {B[idx[j]], dB + off[j], ldb[idx[j]], cm[j], H[j]->N, cm[j]};
+      cpy_out[j] = {dX + off[j], X[idx[j]], cm[j], ldx[idx[j]], H[j]->N, cm[j]};
+      maxe = std::max(maxe, (long long)H[j]->N * cm[j]);
+    }
+    Blob blob;
+    const size_t a_s = blob.put(ssteps.segs), a_d = blob.put(dsteps.segs), a_c = blob.put(cols),
+                 a_i = blob.put(cin), a_o = blob.put(cpy_out);
+    SLU_REQUIRE(blob.host.size() <= plan.bytes[0], "task table overflow");
+    upload(h, blob, dtab);
+    d_s = reinterpret_cast<const StepSeg<T>*>(dtab + a_s);
+    d_d = reinterpret_cast<const StepSeg<dfloat>*>(dtab + a_d);
+    d_c = reinterpret_cast<const ColSeg*>(dtab + a_c);
+    d_i = reinterpret_cast<const CopySeg*>(dtab + a_i);
+    d_o = reinterpret_cast<const CopySeg*>(dtab + a_o);
+    cgrid = dim3(m, (unsigned)std::min<long long>(64, (maxe + 1023) / 1024));
+  }
+
+  // Shared-memory limits of every step launch (before a stream capture).
+  void prepare_launches() const {
+    for (const sweep::LaunchPlan& p : ssteps.plan)
+      if (p.ctas > 0) ensure_smem(reinterpret_cast<const void*>(group_step_kernel<T>), p.smem);
+    for (const sweep::LaunchPlan& p : dsteps.plan)
+      if (p.ctas > 0)
+        ensure_smem(reinterpret_cast<const void*>(group_step_kernel<dfloat>), p.smem);
+  }
+
+  void copy_in(cudaStream_t st) const {
+    seg_copy_k<<<cgrid, 256, 0, st>>>(d_i);
+    check_launch("seg_copy_k");
+  }
+  void copy_out(cudaStream_t st) const {
+    seg_copy_k<<<cgrid, 256, 0, st>>>(d_o);
+    check_launch("seg_copy_k");
+  }
+
+  void iteration(cudaStream_t st, bool first) const {
+    const long long En = (long long)E;
     if (first) {
       colnorm_seg_k<<<C, 256, 0, st>>>(d_c, dB, norms);
       check_launch("colnorm_seg_k");
-      SLU_CHECK_CUDA(
-          cudaMemcpyAsync(host, norms, 8 * (size_t)C, cudaMemcpyDeviceToHost, st));
+      SLU_CHECK_CUDA(cudaMemcpyAsync(host, norms, 8 * (size_t)C, cudaMemcpyDeviceToHost, st));
     }
     to_inner(st, En, first ? dB : dr, df);
     launch_solve<T>(st, ssteps, d_s);
@@ -689,23 +732,14 @@ void refine_grouped(Handle& h, int count, Hbs* const* ops, const double* const* 
     check_launch("colnorm_seg_k");
     SLU_CHECK_CUDA(
         cudaMemcpyAsync(host + C, norms + C, 8 * (size_t)C, cudaMemcpyDeviceToHost, st));
-  };
+  }
 
-  seg_copy_k<<<cgrid, 256, 0, st>>>(d_i);
-  check_launch("seg_copy_k");
-  iteration(true);
-  int it = 1;
-  double worst = 0.0;
-  std::vector<double> member(m, 0.0);
-  for (;;) {
-    if (!kDf && it < 2 && it < maxit && tol < 1e-6) {  // float32: no check yet
-      iteration(false);
-      ++it;
-      continue;
-    }
-    SLU_CHECK_CUDA(cudaStreamSynchronize(st));
-    worst = 0.0;
+  // Worst relative residual over all columns (host norms of the last
+  // iteration); member[j] = member j's worst.
+  double check(std::vector<double>& member) const {
+    double worst = 0.0;
     int col = 0;
+    member.assign(m, 0.0);
     for (int j = 0; j < m; ++j) {
       double w = 0.0;
       for (int q = 0; q < cm[j]; ++q, ++col) {
@@ -715,18 +749,169 @@ void refine_grouped(Handle& h, int count, Hbs* const* ops, const double* const* 
       member[j] = w;
       worst = std::max(worst, w);
     }
+    return worst;
+  }
+};
+
+// The refinement loop: first() then next() until every column reaches tol
+// (float32 inner sweeps: no check before the second correction).
+template <typename T, class First, class Next>
+double refine_loop(cudaStream_t st, const GroupRefine<T>& g, double tol, int maxit, First first,
+                   Next next, int* iters, std::vector<double>& member) {
+  constexpr bool kDf = sizeof(T) == 8;
+  first();
+  int it = 1;
+  double worst = 0.0;
+  for (;;) {
+    if (!kDf && it < 2 && it < maxit && tol < 1e-6) {
+      next();
+      ++it;
+      continue;
+    }
+    SLU_CHECK_CUDA(cudaStreamSynchronize(st));
+    worst = g.check(member);
     if (worst <= tol || it >= maxit) break;
-    iteration(false);
+    next();
     ++it;
   }
-  h.readback.release(st);
-  seg_copy_k<<<cgrid, 256, 0, st>>>(d_o);
-  check_launch("seg_copy_k");
   if (iters) *iters = it;
+  return worst;
+}
+
+template <typename T>
+void refine_grouped(Handle& h, int count, Hbs* const* ops, const double* const* B,
+                    const int* ldb, double* const* X, const int* ldx, const int* c, double tol,
+                    int maxit, int* iters, double* relres) {
   if (relres)
-    for (int j = 0; j < m; ++j) relres[idx[j]] = member[j];
+    for (int i = 0; i < count; ++i) relres[i] = 0.0;
+  if (iters) *iters = 0;
+  GroupRefine<T> g;
+  if (!g.init(h, count, ops, B, ldb, X, ldx, c)) return;
+  cudaStream_t st = h.stream;
+  h.ws.reserve(g.plan.total(), st);
+  g.carve(h, h.ws.take<char>(g.plan.total()), B, ldb, X, ldx);
+  g.host = reinterpret_cast<double*>(h.readback.acquire(16 * (size_t)g.C));
+  std::vector<double> member;
+  const double worst = refine_loop(
+      st, g, tol, maxit,
+      [&] {
+        g.copy_in(st);
+        g.iteration(st, true);
+      },
+      [&] { g.iteration(st, false); }, iters, member);
+  h.readback.release(st);
+  g.copy_out(st);
+  if (relres)
+    for (int j = 0; j < g.m; ++j) relres[g.idx[j]] = member[j];
   if (worst > tol) throw Error(SLU_ERR_NOT_CONVERGED, "refinement did not reach the tolerance");
 }
+
+// A grouped refinement for fixed blocks: the region, task tables and pinned
+// norms owned by the plan; one iteration captured as CUDA graphs (the first
+// with the copy-in and the norms of B, the next ones, the copy-out).
+template <typename T>
+struct GroupRefinePlanT : GroupRefinePlan {
+  GroupRefine<T> g;
+  DevBuf region;
+  double* pinned = nullptr;
+  cudaGraphExec_t first = nullptr, next = nullptr, out = nullptr;
+  long long kf = 0, kn = 0, ko = 0;
+  ~GroupRefinePlanT() override {
+    if (first) cudaGraphExecDestroy(first);
+    if (next) cudaGraphExecDestroy(next);
+    if (out) cudaGraphExecDestroy(out);
+    if (pinned) cudaFreeHost(pinned);
+  }
+
+  template <class F>
+  cudaGraphExec_t capture(cudaStream_t cs, F enqueue, long long& kernels) {
+    cudaGraph_t gr = nullptr;
+    const long long n0 = launch_thread();
+    SLU_CHECK_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+    try {
+      enqueue();
+    } catch (...) {
+      cudaStreamEndCapture(cs, &gr);
+      if (gr) cudaGraphDestroy(gr);
+      throw;
+    }
+    SLU_CHECK_CUDA(cudaStreamEndCapture(cs, &gr));
+    kernels = launch_thread() - n0;
+    launch_total() -= kernels;
+    launch_thread() = n0;
+    cudaGraphExec_t ex = nullptr;
+    const cudaError_t e = cudaGraphInstantiate(&ex, gr, 0);
+    cudaGraphDestroy(gr);
+    if (e != cudaSuccess)
+      throw Error(SLU_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+    return ex;
+  }
+
+  void create(Handle& h, int count, Hbs* const* ops, const double* const* B, const int* ldb,
+              double* const* X, const int* ldx, const int* c) {
+    total = count;
+    if (!g.init(h, count, ops, B, ldb, X, ldx, c)) return;
+    for (const Hbs* x : g.H) {
+      alive.push_back(x->alive);
+      gen.push_back(x->sweep_gen);
+      H.push_back(x);
+    }
+    idx = g.idx;
+    cudaStream_t st = h.stream;
+    region.alloc(g.plan.total(), st);
+    g.carve(h, static_cast<char*>(region.p), B, ldb, X, ldx);
+    SLU_CHECK_CUDA(cudaMallocHost(&pinned, 16 * (size_t)g.C));
+    g.host = pinned;
+    g.prepare_launches();
+    SLU_CHECK_CUDA(cudaStreamSynchronize(st));   // region and tables in place
+    cudaStream_t cs = nullptr;
+    SLU_CHECK_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    try {
+      first = capture(cs, [&] {
+        g.copy_in(cs);
+        g.iteration(cs, true);
+      }, kf);
+      next = capture(cs, [&] { g.iteration(cs, false); }, kn);
+      out = capture(cs, [&] { g.copy_out(cs); }, ko);
+    } catch (...) {
+      cudaStreamDestroy(cs);
+      throw;
+    }
+    SLU_CHECK_CUDA(cudaStreamDestroy(cs));
+  }
+
+  void run(Handle& h, double tol, int maxit, int* iters, double* relres) override {
+    SLU_REQUIRE(maxit >= 1, "bad iteration limit");
+    for (size_t i = 0; i < H.size(); ++i) {
+      if (alive[i].expired())
+        throw Error(SLU_ERR_STATE, "an operator of the refinement plan was destroyed");
+      if (H[i]->sweep_gen != gen[i])
+        throw Error(SLU_ERR_STATE, "an operator was refactored after the plan was made");
+    }
+    if (relres)
+      for (int i = 0; i < total; ++i) relres[i] = 0.0;
+    if (iters) *iters = 0;
+    if (!first) return;
+    cudaStream_t st = h.stream;
+    std::vector<double> member;
+    const double worst = refine_loop(
+        st, g, tol, maxit,
+        [&] {
+          SLU_CHECK_CUDA(cudaGraphLaunch(first, st));
+          count_launches(kf);
+        },
+        [&] {
+          SLU_CHECK_CUDA(cudaGraphLaunch(next, st));
+          count_launches(kn);
+        },
+        iters, member);
+    SLU_CHECK_CUDA(cudaGraphLaunch(out, st));
+    count_launches(ko);
+    if (relres)
+      for (int j = 0; j < g.m; ++j) relres[idx[j]] = member[j];
+    if (worst > tol) throw Error(SLU_ERR_NOT_CONVERGED, "refinement did not reach the tolerance");
+  }
+};
 
 }  // namespace
 
@@ -741,6 +926,24 @@ void hbs_refine_grouped(Handle& h, int count, Hbs* const* ops, const double* con
   for (int i = 0; i < count; ++i) f32 = f32 && ops[i] && ops[i]->refine_inner == 0;
   if (f32) refine_grouped<float>(h, count, ops, B, ldb, X, ldx, c, tol, maxit, iters, relres);
   else refine_grouped<dfloat>(h, count, ops, B, ldb, X, ldx, c, tol, maxit, iters, relres);
+}
+
+std::unique_ptr<GroupRefinePlan> grouped_refine_plan_create(Handle& h, int count,
+                                                            Hbs* const* ops, const double* const* B,
+                                                            const int* ldb, double* const* X,
+                                                            const int* ldx, const int* c) {
+  SLU_REQUIRE(count >= 0 && (count == 0 || (ops && B && ldb && X && ldx && c)),
+              "null argument");
+  bool f32 = count > 0;
+  for (int i = 0; i < count; ++i) f32 = f32 && ops[i] && ops[i]->refine_inner == 0;
+  if (f32) {
+    auto p = std::make_unique<GroupRefinePlanT<float>>();
+    p->create(h, count, ops, B, ldb, X, ldx, c);
+    return p;
+  }
+  auto p = std::make_unique<GroupRefinePlanT<dfloat>>();
+  p->create(h, count, ops, B, ldb, X, ldx, c);
+  return p;
 }
 
 }  // namespace slu

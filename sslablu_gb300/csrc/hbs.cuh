@@ -169,6 +169,23 @@ void solve_plan_launch(Handle& h, SolvePlan& P, bool wait);
 void grouped_solve_plan_create(Handle& h, int count, Hbs* const* ops, double* const* B,
                                const int* ldb, const int* c, SolvePlan& P);
 
+// The grouped mixed-precision refinement of hbs_refine_grouped for fixed
+// blocks: buffers and task tables built once, an iteration replayed as CUDA
+// graphs (group.cu).
+struct GroupRefinePlan {
+  std::vector<const Hbs*> H;
+  std::vector<std::weak_ptr<char>> alive;
+  std::vector<unsigned long long> gen;
+  std::vector<int> idx;   // member index of each operator with columns
+  int total = 0;          // members given (relres entries)
+  virtual ~GroupRefinePlan() = default;
+  virtual void run(Handle& h, double tol, int maxit, int* iters, double* relres) = 0;
+};
+std::unique_ptr<GroupRefinePlan> grouped_refine_plan_create(Handle& h, int count,
+                                                            Hbs* const* ops, const double* const* B,
+                                                            const int* ldb, double* const* X,
+                                                            const int* ldx, const int* c);
+
 // compression + interleaved ULV (HBSnew.HBSMAT.constructHBS_ULV)
 void hbs_compress(Handle& h, Hbs& H, int Nb_leaf, int rk, int s, const double* Om,
                   const double* Psi, const double* Y, const double* Z, bool ulv);

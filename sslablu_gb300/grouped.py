@@ -85,6 +85,48 @@ class GroupedSolvePlan:
         self.close()
 
 
+class GroupedRefinePlan:
+    """solve_grouped_device(ops, Bs, "mixed", ..., Xs=Xs) for fixed blocks,
+    made once (slu_refine_grouped_plan_create): ``plan(tol, maxit)`` refines
+    whatever the Bs hold into the Xs and returns (Xs, iterations, relres)."""
+
+    def __init__(self, ops, Bs, Xs=None):
+        n = len(ops)
+        for H, B in zip(ops, Bs):
+            if B.dtype != torch.float64 or not B.is_cuda or not B.is_contiguous() or B.dim() != 2:
+                raise ValueError("right-hand sides must be contiguous 2-D float64 CUDA tensors")
+            if B.shape[0] != H.shape[0]:
+                raise ValueError("right-hand side has %d rows, operator %d"
+                                 % (B.shape[0], H.shape[0]))
+        if Xs is None:
+            Xs = [torch.empty_like(t) for t in Bs]
+        self.ops, self.Bs, self.Xs = list(ops), list(Bs), list(Xs)
+        op_arr = (ctypes.c_void_p * max(n, 1))(*[H._op for H in ops])
+        bp = (ctypes.c_void_p * max(n, 1))(*[t.data_ptr() for t in Bs])
+        xp = (ctypes.c_void_p * max(n, 1))(*[t.data_ptr() for t in Xs])
+        ld = (ctypes.c_int * max(n, 1))(*[t.shape[1] for t in Bs])
+        p = ctypes.c_void_p()
+        L.check(L.lib().slu_refine_grouped_plan_create(L.handle(), n, op_arr, bp, ld, xp, ld, ld,
+                                                       ctypes.byref(p)))
+        self._p = p
+        self._n = n
+
+    def __call__(self, tol=1e-10, maxit=10):
+        it = ctypes.c_int()
+        rr = (ctypes.c_double * max(self._n, 1))()
+        L.check(L.lib().slu_refine_plan_run(L.handle(), self._p, float(tol), int(maxit),
+                                            ctypes.byref(it), rr))
+        return self.Xs, it.value, list(np.frombuffer(rr, dtype=np.float64)[:self._n])
+
+    def close(self):
+        if getattr(self, "_p", None) is not None and L._lib is not None:
+            L.lib().slu_refine_plan_destroy(self._p)
+        self._p = None
+
+    def __del__(self):
+        self.close()
+
+
 def apply_grouped(ops, Xs, trans=False, Ys=None):
     """Grouped apply on contiguous float64 CUDA tensors: Ys[i] = A_i Xs[i]
     (or A_i^T Xs[i] where ``trans`` -- one flag, or one per member -- is

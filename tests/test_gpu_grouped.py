@@ -179,3 +179,44 @@ def test_grouped_solve_plan_equals_grouped_solve():
     with pytest.raises(L.SluError):
         plan()
     plan.close()
+
+
+def test_grouped_refine_plan_equals_grouped_refinement():
+    """A grouped refinement plan (buffers and tables built once, iterations
+    replayed as CUDA graphs) gives the per-call grouped refinement's results
+    bitwise, with the same iteration count and residuals, on new data every
+    call; it refuses to run after a member is refactored."""
+    need_gpu()
+    import torch
+    from sslablu_gb300 import _lib as L
+    from sslablu_gb300.grouped import GroupedRefinePlan, solve_grouped_device
+    from sslablu_gb300.matAssembly.HBS.HBSnew import HBSMAT
+    from sslablu_gb300.synthetic import random_hbs_factors
+    ops = []
+    for j, (N, k) in enumerate([(256, 16), (512, 24), (128, 16)]):
+        Lv = int(np.log2(N // 64)) + 1
+        U, D, V, Nbvec = random_hbs_factors(k, 64, Lv, quad=False,
+                                            rng=np.random.default_rng(j + 5), shift=16.0)
+        ops.append(HBSMAT().set_mats(U, D, V, list(Nbvec), fac=2))
+        ops[-1].compute_ULV()
+    cols = [4, 2, 7]
+    Bs = [torch.empty((H.shape[0], c), dtype=torch.float64, device="cuda")
+          for H, c in zip(ops, cols)]
+    plan = GroupedRefinePlan(ops, Bs)
+    rng = np.random.default_rng(9)
+    for _ in range(2):
+        data = [rng.standard_normal(tuple(B.shape)) for B in Bs]
+        for B, d in zip(Bs, data):
+            B.copy_(torch.from_numpy(d))
+        Xs, it, rr = plan(1e-10, 10)
+        ref = [torch.from_numpy(d).cuda() for d in data]
+        Xr, it_r, rr_r = solve_grouped_device(ops, ref, "mixed", 1e-10, 10)
+        torch.cuda.synchronize()
+        assert it == it_r and np.allclose(rr, rr_r, rtol=0, atol=0)
+        for X, R in zip(Xs, Xr):
+            assert torch.equal(X, R)
+        assert max(rr) <= 1e-10
+    ops[0].compute_ULV()
+    with pytest.raises(L.SluError):
+        plan(1e-10, 10)
+    plan.close()
