@@ -183,15 +183,22 @@ def run_reference(args, rank, world):
 # DRAM bytes (read + written) per launch of each solve step group, averaged
 # over the group's launches in the ncu launch list of
 # `python bench.py --steps 2 --warmup 3` (profiles/ulv_step_c2_launches.txt).
-NCU_TRAFFIC = {"step_kernel<double> (backward)": 1864064,
-               "step_kernel<double> (forward)": 926037,
+# DRAM bytes per launch from the ncu capture of the step kernels (per-level
+# figures in profiles/ulv_step_c2_launches.txt), averaged over the levels the
+# C2 chain launches: backward and forward levels 0-3 (the top operator stands
+# in for levels 4 .. root)
+NCU_TRAFFIC = {"step_kernel<double> (backward)": 2600000,
+               "step_kernel<double> (forward)": 1297408,
                "step_kernel<double> (root)": 134016}
 FP64_NOMINAL_TFLOPS = 1.25   # GB300 float64 (no measured figure in the peaks file)
 
 
-def launch_cost(kind, Nb, n, k, nu, c, leaf, single=False):
+def launch_cost(kind, Nb, n, k, nu, c, leaf, single=False, top=False):
     """Algorithmic (bytes, flops) of one fused solve launch: the block
     operators read once, the right-hand-side blocks read and written once."""
+    if kind == 1 and top:   # [y; v] = Top x, Top 2M x M for the M = Nb n rows of its level
+        M = Nb * n
+        return 8 * (2 * M * M + M * c + 2 * M * c), 2 * 2 * M * M * c
     if kind == 0:      # [ru; x_parent] = Q^T x
         rows, w = n, n
     elif kind == 1:    # [y; v] = [R^-1 Q^T; D R^-1 Q^T] x
@@ -230,8 +237,10 @@ def launch_roofline(H, B, flush, hbm, src, reps):
     launches = []
     for (t, kd), m in zip(meta, med):
         Nb, n, k, nu = (geo[4 * t + j] for j in range(4))
-        by, fl = launch_cost(kd, Nb, n, k, nu, c, t == 0, nl.value == 1)
-        launches.append({"kernel": "step_kernel<double> (%s)" % names[kd], "level": t,
+        top = kd == 1 and t < nl.value - 1
+        by, fl = launch_cost(kd, Nb, n, k, nu, c, t == 0, nl.value == 1, top)
+        label = "top" if top else names[kd]
+        launches.append({"kernel": "step_kernel<double> (%s)" % label, "level": t,
                          "ms": float(m), "alg_bytes": int(by), "alg_flops": int(fl)})
     # the dominant kernel: the one with the largest share of the solve; its
     # roofline uses per-launch averages over its launches (one per level)

@@ -145,12 +145,12 @@ void build_solve(const std::vector<const Hbs*>& H, const std::vector<int>& c,
                  const std::vector<SolveBufs<T>>& buf, StepTable<T>& tab) {
   const int m = (int)H.size();
   int maxL = 0;
-  for (int i = 0; i < m; ++i) maxL = std::max(maxL, H[i]->L);
+  for (int i = 0; i < m; ++i) maxL = std::max(maxL, sweep::chain_levels(*H[i]));
   std::vector<sweep::Step<T>> v;
   for (int t = 0; t + 1 < maxL; ++t) {
     v.clear();
     for (int i = 0; i < m; ++i) {
-      if (H[i]->L < t + 2) continue;
+      if (sweep::chain_levels(*H[i]) < t + 2) continue;
       v.push_back(sweep::forward_step<T>(
           *H[i], t, t == 0 ? B[i] : buf[i].P[(t - 1) & 1], t == 0 ? ldb[i] : c[i],
           t == 0 ? H[i]->perm.as<int64_t>() : nullptr, buf[i].ru + H[i]->NN[t] * c[i],
@@ -160,16 +160,20 @@ void build_solve(const std::vector<const Hbs*>& H, const std::vector<int>& c,
   }
   v.clear();
   for (int i = 0; i < m; ++i) {
-    const int L = H[i]->L;
-    v.push_back(sweep::root_step<T>(*H[i], L == 1 ? B[i] : buf[i].P[(L - 2) & 1],
-                                    L == 1 ? ldb[i] : c[i], B[i], ldb[i], buf[i].P[2],
-                                    buf[i].P[3], c[i]));
+    const int L = sweep::chain_levels(*H[i]);
+    if (H[i]->top >= 1)
+      v.push_back(sweep::top_step<T>(*H[i], buf[i].P[(L - 2) & 1], c[i], buf[i].P[2],
+                                     buf[i].P[3], c[i]));
+    else
+      v.push_back(sweep::root_step<T>(*H[i], L == 1 ? B[i] : buf[i].P[(L - 2) & 1],
+                                      L == 1 ? ldb[i] : c[i], B[i], ldb[i], buf[i].P[2],
+                                      buf[i].P[3], c[i]));
   }
   tab.add(v);
   for (int t = maxL - 2; t >= 0; --t) {
     v.clear();
     for (int i = 0; i < m; ++i) {
-      const int L = H[i]->L;
+      const int L = sweep::chain_levels(*H[i]);
       if (L < t + 2) continue;
       const int in = ((L - 2 - t) % 2 == 0) ? 2 : 0, out = in == 2 ? 0 : 2;
       v.push_back(sweep::backward_step<T>(*H[i], t, buf[i].ru + H[i]->NN[t] * c[i],

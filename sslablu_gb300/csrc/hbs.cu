@@ -491,6 +491,7 @@ void hbs_make_f32(Handle& h, Hbs& H) {
     cp(l.Sw, l.Swf);
     cp(l.SwT, l.SwTf);
   }
+  if (H.top >= 1) cp(H.Top, H.Topf);
   H.has_f32 = true;
 }
 

@@ -112,6 +112,13 @@ struct Hbs {
   std::vector<Level> lv;           // lv[0] = leaves, lv[L-1] = root
   DevBuf perm;                     // int64[N]
   DevBuf iperm;                    // int64[N], iperm[perm[i]] = i
+  // Top of the mode-N solve as one operator: the map from the vector entering
+  // forward step `top` to the y and v vectors of backward step `top` (levels
+  // top .. root), 2 N_top x N_top, composed at factor time from the steps it
+  // replaces; -1 when the tree has no level of at most kTopRows rows below
+  // the root's children.
+  int top = -1;
+  DevBuf Top, Topf, Topdf;
   bool identity_perm = true;
   std::vector<long long> NN;       // NNvec, L+1 entries
   bool has_mats = false, has_ulv = false, has_f32 = false, has_df = false, has_dfs = false;
@@ -298,6 +305,7 @@ struct FacPtr<double> {
   static const double* Qt(const Level& l) { return l.Qt.as<double>(); }
   static const double* Sw(const Level& l) { return l.Sw.as<double>(); }
   static const double* SwT(const Level& l) { return l.SwT.as<double>(); }
+  static const double* Top(const Hbs& H) { return H.Top.as<double>(); }
 };
 template <>
 struct FacPtr<float> {
@@ -310,12 +318,14 @@ struct FacPtr<float> {
   static const float* Qt(const Level& l) { return l.Qtf.as<float>(); }
   static const float* Sw(const Level& l) { return l.Swf.as<float>(); }
   static const float* SwT(const Level& l) { return l.SwTf.as<float>(); }
+  static const float* Top(const Hbs& H) { return H.Topf.as<float>(); }
 };
 
 template <>
 struct FacPtr<dfloat> {
   static const dfloat* Qt(const Level& l) { return l.Qtdf.as<dfloat>(); }
   static const dfloat* Sw(const Level& l) { return l.Swdf.as<dfloat>(); }
+  static const dfloat* Top(const Hbs& H) { return H.Topdf.as<dfloat>(); }
 };
 
 // Grouped solves over many operators (group.cu): one launch per tree step for

@@ -72,6 +72,34 @@ Step<T> root_step(const Hbs& H, const T* src, int lds, T* B, int ldb, T* Y, T* V
   return s;
 }
 
+// Largest level (rows) the top operator may start at.
+constexpr int kTopRows = 256;
+
+// Levels of the solve chain: the top step stands in for levels top .. root.
+inline int chain_levels(const Hbs& H) { return H.top >= 1 ? H.top + 1 : H.L; }
+
+// The top step: [y; v] = Top x for the vector x entering level `top`.
+template <typename T>
+Step<T> top_step(const Hbs& H, const T* src, int lds, T* Y, T* V, int c) {
+  const long long M = (long long)H.lv[H.top].Nb * H.lv[H.top].n;
+  Step<T> s{};
+  s.S = FacPtr<T>::Top(H);
+  s.rows = (int)(2 * M);
+  s.w = (int)M;
+  s.nb = 1;
+  s.c = c;
+  s.nin = 1;
+  s.in_p[0] = src;
+  s.in_ld[0] = lds;
+  s.in_rows[0] = (int)M;
+  s.split = (int)M;
+  s.out_p[0] = Y;
+  s.out_ld[0] = c;
+  s.out_p[1] = V;
+  s.out_ld[1] = c;
+  return s;
+}
+
 // Backward step t: [y_new; v_new] = [G; H] [ru; v; y_next]; the leaf step
 // writes y_new to the caller's rows through the permutation.
 template <typename T>

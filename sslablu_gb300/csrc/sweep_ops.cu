@@ -8,6 +8,7 @@
 // as ULVsparse.solve does per right-hand side, here once per factor column);
 // the products are batched float64 GEMMs.
 #include "hbs.cuh"
+#include "sweep_host.cuh"
 
 #include <algorithm>
 
@@ -136,6 +137,56 @@ void hbs_make_sweep(Handle& h, Hbs& H) {
     transpose_children_kernel<<<grid_for(ne), 256, 0, st>>>(nb, rows, w, l.n, kc,
                                                             l.Sw.as<double>(), l.SwT.as<double>());
     check_launch("transpose_children_kernel");
+  }
+  // The top of the mode-N chain as one operator: the steps from the first
+  // level of at most kTopRows rows (below the root's children) up to the
+  // root and back, applied to the identity, give [y; v] of that level as a
+  // 2M x M matrix.  For the C2 tree (M = 256) it holds no more entries than
+  // the five steps it replaces.
+  H.top = -1;
+  H.Top.alloc(0, st);
+  int top = -1;
+  for (int t = 1; t + 1 < L; ++t)
+    if ((long long)H.lv[t].Nb * H.lv[t].n <= sweep::kTopRows) {
+      top = t;
+      break;
+    }
+  if (top >= 1) {
+    const int M = H.lv[top].Nb * H.lv[top].n;
+    const size_t stride = ((size_t)M * M + 31) & ~size_t(31);   // 256-byte aligned
+    DevBuf work;
+    work.alloc(8 * 6 * stride, st);
+    double* I = work.as<double>();
+    double* ru = I + stride;
+    double* P[4] = {I + 2 * stride, I + 3 * stride, I + 4 * stride, I + 5 * stride};
+    identity_cols(st, M, 0, M, I, 0, 1);
+    H.Top.alloc(8 * 2 * (size_t)M * M, st);
+    double* Tp = H.Top.as<double>();
+    const std::vector<long long>& NN = H.NN;
+    const double* src = I;
+    for (int t = top; t + 1 < L; ++t) {
+      sweep::launch_step(st,
+                         sweep::forward_step<double>(H, t, src, M, nullptr,
+                                                     ru + (NN[t] - NN[top]) * M,
+                                                     P[(t - top) & 1], M),
+                         "top_compose_step");
+      src = P[(t - top) & 1];
+    }
+    sweep::launch_step(st, sweep::root_step<double>(H, src, M, nullptr, 0, P[2], P[3], M),
+                       "top_compose_step");
+    int in = 2;
+    for (int t = L - 2; t >= top; --t) {
+      const int out = in == 2 ? 0 : 2;
+      const bool last = t == top;
+      sweep::launch_step(st,
+                         sweep::backward_step<double>(H, t, ru + (NN[t] - NN[top]) * M, P[in + 1],
+                                                      P[in], last ? Tp : P[out],
+                                                      last ? Tp + (size_t)M * M : P[out + 1],
+                                                      nullptr, 0, M),
+                         "top_compose_step");
+      in = out;
+    }
+    H.top = top;
   }
   H.has_sweep = true;
   H.has_f32 = false;

@@ -55,22 +55,26 @@ std::vector<StepRec<T>> solve_steps(const Hbs& H, const T* X, int ldx, T* B, int
   std::vector<StepRec<T>> v;
   const T* src = X;
   int lds = ldx;
-  for (int t = 0; t + 1 < L; ++t) {
+  const int Lc = sweep::chain_levels(H);
+  for (int t = 0; t + 1 < Lc; ++t) {
     v.push_back({sweep::forward_step<T>(H, t, src, lds, t == 0 ? perm : nullptr, ru + NN[t] * c,
                                         P[t & 1], c),
                  "ulv_fwd_step", t, 0});
     src = P[t & 1];
     lds = c;
   }
-  v.push_back({sweep::root_step<T>(H, src, lds, B, ldb, P[2], P[3], c), "ulv_root_step", L - 1,
-               1});
+  if (H.top >= 1)
+    v.push_back({sweep::top_step<T>(H, src, lds, P[2], P[3], c), "ulv_top_step", H.top, 1});
+  else
+    v.push_back({sweep::root_step<T>(H, src, lds, B, ldb, P[2], P[3], c), "ulv_root_step", L - 1,
+                 1});
   if (L == 1 && X != B) {   // one-level tree: the root reads X, writes B
     sweep::Step<T>& r = v.back().s;
     r.in_p[0] = X;
     r.in_ld[0] = ldx;
   }
   int in = 2;
-  for (int t = L - 2; t >= 0; --t) {
+  for (int t = Lc - 2; t >= 0; --t) {
     const int out = (in == 2) ? 0 : 2;
     v.push_back({sweep::backward_step<T>(H, t, ru + NN[t] * c, P[in + 1], P[in], P[out],
                                          P[out + 1], B, ldb, c),
@@ -383,6 +387,7 @@ void hbs_make_dfs(Handle& h, Hbs& H) {
     split_dfs(st, l.Qt, l.Qtdf);
     split_dfs(st, l.Sw, l.Swdf);
   }
+  if (H.top >= 1) split_dfs(st, H.Top, H.Topdf);
   H.has_dfs = true;
 }
 

@@ -163,7 +163,10 @@ def test_autotuned_plans_keep_results():
     b = np.random.default_rng(5).standard_normal((H.shape[0], 16))
     x0, xd0 = H.solve(b), H.solve_dfloat(b)
     kn = H.autotune(16, reps=3)
-    assert len(kn) == 2 * len(Nbvec) - 1 and all(len(k) == 3 and min(k) >= 1 for k in kn)
+    # one cap set per launch: 2 L - 1 steps, or fewer where the top levels
+    # run as one composed operator
+    assert len(kn) % 2 == 1 and 3 <= len(kn) <= 2 * len(Nbvec) - 1
+    assert all(len(k) == 3 and min(k) >= 1 for k in kn)
     H.autotune(16, "dfloat", reps=3)
     assert np.array_equal(H.solve(b), x0)
     assert np.array_equal(H.solve_dfloat(b), xd0)
