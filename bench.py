@@ -410,7 +410,7 @@ def run_gpu(args, rank, world):
             "dtype": "f64", "data": "synthetic",
             "config": workload_config({"factor_s": t_factor,
                                        "arm": "plain float64 ULV solve through a solve plan "
-                                              "(HBSMAT.solve_plan: the 13 step launches "
+                                              "(HBSMAT.solve_plan: the 9 step launches "
                                               "replayed as one CUDA graph)",
                                        "launch_plans": "autotuned per launch (target CTAs/SM, "
                                                        "row floor, column cap)",
@@ -418,7 +418,7 @@ def run_gpu(args, rank, world):
             "p50_ms": 1e3 * p50, "p99_ms": 1e3 * float(np.percentile(ts_plain, 99)),
             "relres": res_plain,
             "per_call": {"value": world * NRHS * args.steps / sum(ts_call), "unit": UNIT,
-                         "arm": "HBSMAT solve per call (13 stream launches)",
+                         "arm": "HBSMAT solve per call (9 stream launches)",
                          "p50_ms": 1e3 * statistics.median(ts_call),
                          "e2e_value": world * NRHS * args.steps / sum(e2e_call),
                          "e2e_p50_ms": 1e3 * statistics.median(e2e_call)},
