@@ -6,7 +6,8 @@ that composition in numpy -- mode N: Qt = Q^T, [G; H] from W, R, Uu, U, D;
 mode T: the same steps transposed, in reverse order, with the columns of
 [G; H]^T reordered to the children's [v; y] ranges (the index map of
 transpose_children_kernel) -- and check both against the oracle's
-ULVsparse.solve on random exact HBS operators, binary and quad trees."""
+ULVsparse.solve on random exact HBS operators, binary and quad trees; and
+the top of the chain composed into one operator (hbs_make_sweep's top step)."""
 import numpy as np
 import pytest
 
@@ -91,6 +92,67 @@ def _solve_T(U, D, Qs, Nbvec, Sw, root, b):
         zz = np.concatenate([ru[t], x.reshape(Nb, k, -1)], axis=1)
         x = np.einsum("bij,bjc->bic", Qs[t].reshape(Nb, n, n), zz).reshape(-1, b.shape[1])
     return x
+
+
+def _chain(U, D, Qs, Nbvec, Sw, root, x, t0):
+    """Forward steps t0 .. L-2, root, backward steps L-2 .. t0 on the level-t0
+    vector x: returns [y_t0; v_t0] (t0 >= 1), or the solution (t0 = 0)."""
+    L = len(D)
+    ru = {}
+    for t in range(t0, L - 1):
+        Nb, n, k = Nbvec[t], D[t].shape[1], U[t].shape[1]
+        z = np.einsum("bij,bjc->bic", Qs[t].reshape(Nb, n, n).transpose(0, 2, 1),
+                      x.reshape(Nb, n, -1))
+        ru[t] = z[:, :n - k]
+        x = z[:, n - k:].reshape(-1, z.shape[2])
+    yv = root @ x
+    n = D[L - 1].shape[1]
+    y, v = yv[:n], yv[n:]
+    for t in range(L - 2, t0 - 1, -1):
+        Nb, k = Nbvec[t], U[t].shape[1]
+        z = np.concatenate([ru[t], v.reshape(Nb, k, -1), y.reshape(Nb, k, -1)], axis=1)
+        out = np.einsum("bij,bjc->bic", Sw[t], z)
+        n = D[t].shape[1]
+        y = out[:, :n].reshape(-1, z.shape[2])
+        v = out[:, n:].reshape(-1, z.shape[2]) if t > 0 else None
+    return y if t0 == 0 else np.vstack([y, v])
+
+
+@pytest.mark.parametrize("k,nl,L,quad", [(8, 16, 5, False), (8, 16, 4, True), (16, 32, 4, False)])
+def test_top_operator_matches_ulv_solve(k, nl, L, quad):
+    """The top of the chain as one operator (levels t0 .. root, composed by
+    running those steps on the identity) reproduces ULVsparse.solve when the
+    solve runs forward steps below t0, the top product, backward steps below
+    t0."""
+    rng = np.random.default_rng(k + nl + L)
+    np.random.seed(k * 3 + L)
+    S, Nbvec = oh.gen_random_hbs(k, nl, L, quad=quad)
+    U, D, V = S.Umats, S.Dmats, S.Vmats
+    Qs, Ws, Uus, Rs, NN = oh.compute_ULV(U, D, V, Nbvec)
+    Nbvec = list(Nbvec)
+    Sw, root = _compose(U, D, Qs, Ws, Uus, Rs, Nbvec)
+    b = rng.standard_normal((D[0].shape[0], 2))
+    ref = oh.ulv_solve(U, D, Qs, Ws, Uus, Rs, NN, Nbvec, b.copy())
+    for t0 in range(1, L - 1):
+        M = Nbvec[t0] * D[t0].shape[1]
+        Top = _chain(U, D, Qs, Nbvec, Sw, root, np.eye(M), t0)      # 2M x M
+        x, ru = b, []
+        for t in range(t0):
+            Nb, n, kk = Nbvec[t], D[t].shape[1], U[t].shape[1]
+            z = np.einsum("bij,bjc->bic", Qs[t].reshape(Nb, n, n).transpose(0, 2, 1),
+                          x.reshape(Nb, n, -1))
+            ru.append(z[:, :n - kk])
+            x = z[:, n - kk:].reshape(-1, b.shape[1])
+        yv = Top @ x
+        y, v = yv[:M], yv[M:]
+        for t in range(t0 - 1, -1, -1):
+            Nb, kk = Nbvec[t], U[t].shape[1]
+            z = np.concatenate([ru[t], v.reshape(Nb, kk, -1), y.reshape(Nb, kk, -1)], axis=1)
+            out = np.einsum("bij,bjc->bic", Sw[t], z)
+            n = D[t].shape[1]
+            y = out[:, :n].reshape(-1, b.shape[1])
+            v = out[:, n:].reshape(-1, b.shape[1]) if t > 0 else None
+        assert np.linalg.norm(y - ref) <= 1e-11 * np.linalg.norm(ref), t0
 
 
 @pytest.mark.parametrize("k,nl,L,quad", [(8, 16, 4, False), (8, 16, 3, True), (5, 16, 3, False),
