@@ -9,7 +9,8 @@ leaf shift of 16 (the I + S form of the interface systems), ULV-factored on
 the device; ``--nrhs`` right-hand sides ~ N(0, 1) per system.  One step
 solves every system once.  Arms, each timed with CUDA events on the current
 stream after warm-up (the factors of the batch exceed L2, so no flush):
-  * per_operator_f64: one ``HBSMAT.solve`` sweep per system (2L-1 launches each);
+  * per_operator_f64: one ``HBSMAT.solve`` sweep per system (2L-1 launches each, fewer
+    where the top levels run as one composed operator);
   * grouped_f64: one grouped sweep for the whole batch (2 maxL - 1 launches);
   * grouped_f64_plan: the same sweep through a grouped solve plan (step
     tables built and uploaded once, the launches replayed as one graph);

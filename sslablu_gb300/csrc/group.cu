@@ -4,7 +4,7 @@
 // matAssembly/HBS/HBSnew.py:393-416, through ULVsparse.solve,
 // matAssembly/HBS/ULVsparse.py:296-327); the slab solvers call it for every
 // block of every level.  Solving a group of operators with the per-operator
-// kernels costs 2L-1 launches per operator, each too small to fill 152 SMs.
+// kernels costs up to 2L-1 launches per operator, each too small to fill 152 SMs.
 // Here each tree step of every member becomes a *segment* of one launch: a
 // task table lists, per segment, the member's factors, buffers and column
 // chunking, and the CTA range it owns; a CTA finds its segment by binary

@@ -41,7 +41,8 @@ template <> constexpr int type_code<double>() { return 0; }
 template <> constexpr int type_code<float>() { return 1; }
 template <> constexpr int type_code<dfloat>() { return 2; }
 
-// The 2L-1 launches of a mode-N solve, in order: the right-hand sides are
+// The launches of a mode-N solve, in order (2L-1, or 2 top + 1 with the top
+// levels as one composed operator): the right-hand sides are
 // read from X (ld ldx) and the solution written to B (ld ldb); X == B solves
 // in place.
 template <typename T>
