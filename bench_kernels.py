@@ -1,11 +1,12 @@
-"""Kernel micro-benchmarks (CUDA-event timing on the launching stream).
+"""Kernel micro-benchmarks (CUDA-event timing on the launching stream), beside
+bench.py: the commands the kernel summaries under profiles/ were made with.
 
-    python -m sslablu_gb300.microbench tc_gemm [--m 4096 --n 261 --k 4096 --reps 20]
-    python -m sslablu_gb300.microbench f64_gemm [...]
+    python bench_kernels.py tc_gemm [--m 4096 --n 261 --k 4096 --reps 20]
+    python bench_kernels.py f64_gemm [...]
 
-    python -m sslablu_gb300.microbench compress [--m 4096 --reps 5]
-    python -m sslablu_gb300.microbench solve [--m 4096 --n 16 --reps 20]
-    python -m sslablu_gb300.microbench refine [--m 4096 --reps 10]
+    python bench_kernels.py compress [--m 4096 --reps 5]
+    python bench_kernels.py solve [--m 4096 --n 16 --reps 20]
+    python bench_kernels.py refine [--m 4096 --reps 10]
 
 tc_gemm : slu_gemm_split3 (tcgen05 split-BF16x3, float32 accumulation)
 f64_gemm: slu_gemm_batched (float64 CUDA-core GEMM) on the same shape
@@ -29,13 +30,17 @@ sketches sampled through the resident operator; prints the median time and
 the relative error of the compressed operator's apply.
 """
 import argparse
+import os
+import sys
 import json
 import statistics
 
 import numpy as np
 import torch
 
-from . import _lib
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+
+from sslablu_gb300 import _lib
 
 
 def main():
@@ -94,8 +99,8 @@ def main():
 
 
 def solve(a):
-    from .matAssembly.HBS.HBSnew import HBSMAT
-    from .synthetic import decaying_sigma, random_hbs_factors
+    from sslablu_gb300.matAssembly.HBS.HBSnew import HBSMAT
+    from sslablu_gb300.synthetic import decaying_sigma, random_hbs_factors
     N, c = a.m, a.n
     Lv = int(np.log2(N // 64)) + 1
     np.random.seed(1)
@@ -146,8 +151,8 @@ def solve(a):
 
 
 def refine(a):
-    from .matAssembly.HBS.HBSnew import HBSMAT
-    from .synthetic import decaying_sigma, random_hbs_factors
+    from sslablu_gb300.matAssembly.HBS.HBSnew import HBSMAT
+    from sslablu_gb300.synthetic import decaying_sigma, random_hbs_factors
     N = a.m
     Lv = int(np.log2(N // 64)) + 1
     np.random.seed(1)
@@ -193,8 +198,8 @@ def refine(a):
 
 def compress(a):
     import time
-    from .matAssembly.HBS.HBSnew import HBSMAT
-    from .synthetic import decaying_sigma, random_hbs_factors
+    from sslablu_gb300.matAssembly.HBS.HBSnew import HBSMAT
+    from sslablu_gb300.synthetic import decaying_sigma, random_hbs_factors
     N = a.m
     Lv = int(np.log2(N // 64)) + 1
     np.random.seed(1)

@@ -118,8 +118,9 @@ int slu_ulv_solve(slu_handle_t h, slu_hbs_t op, double* B, int ldb, int nrhs, in
  * looks up the array's device address with cudaGetSymbolAddress; make that
  * first call before any stream capture.  All calls on a device share the
  * array: calls that overlap on the GPU race and must be serialised by the
- * caller.  The operator must already be factored (slu_hbs_compress with
- * compute_ulv or slu_ulv_factor). */
+ * caller.  The handle's stream must belong to the current device
+ * (SLU_ERR_ARG otherwise).  The operator must already be factored
+ * (slu_hbs_compress with compute_ulv or slu_ulv_factor). */
 int slu_ulv_solve_noalloc(slu_handle_t h, slu_hbs_t op, double* B, int ldb, int nrhs, int trans);
 
 /* Out-of-place solve: Y (N x nrhs, ld ldy) <- A^{-1} X (trans = 0) or
@@ -271,6 +272,14 @@ int slu_hbs_export(slu_handle_t h, slu_hbs_t op, int what, int level, double* ds
 /* Bytes of stored factors: which = 0 HBS (U, V, D; HBSMAT.nbytes,
  * HBSnew.py:296-302), 1 solve factors. */
 int slu_hbs_nbytes(slu_hbs_t op, int which, size_t* out);
+
+/* Measured float64 FMA throughput of the current device: a register-only
+ * kernel of independent FMA chains, 8 CTAs of 256 threads per SM, `iters`
+ * FMAs per chain, timed with CUDA events (best of 3 after a warm-up launch).
+ * *tflops_out = 2 * FMAs / time; *ms_out (may be NULL) the launch time.  The
+ * ceiling of the roofline of the float64 step kernels.  No upstream
+ * counterpart. */
+int slu_fp64_peak(slu_handle_t h, int iters, double* tflops_out, double* ms_out);
 
 /* ---------------------------------------------------------------- dense kernels
  * Batched LU with partial pivoting of nb matrices A_b (n x n, row-major, lda,

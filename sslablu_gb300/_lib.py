@@ -72,6 +72,7 @@ SIGNATURES = {
     "slu_rb_destroy": [P],
     "slu_thomas_factor": [P, c_int, c_int, P, P, P, ctypes.POINTER(c_void_p)],
     "slu_thomas_solve": [P, P, P, c_int, c_int],
+    "slu_fp64_peak": [P, c_int, P, P],
 }
 
 ERRORS = {1: "bad argument", 2: "allocation failed", 3: "CUDA error", 4: "numerical failure",

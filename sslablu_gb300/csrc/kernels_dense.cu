@@ -7,6 +7,7 @@
 // (ULVsparse.py:213-226) and the pivot-block LU of the red-black elimination
 // (direct_solve/omsdirectsolve.py:211,333 lu_factor / lu_solve).
 #include "slablu_internal.cuh"
+#include "smem_limit.h"
 
 #include <mutex>
 #include <type_traits>
@@ -23,15 +24,17 @@ long long& launch_thread() {
 }
 
 void ensure_smem(const void* kernel, size_t bytes) {
-  static std::mutex mu;
-  static std::map<const void*, size_t> done;
-  if (bytes <= 48 * 1024) return;
-  std::lock_guard<std::mutex> lock(mu);
-  size_t& cur = done[kernel];
-  if (cur >= bytes) return;
-  SLU_CHECK_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)bytes));
-  cur = bytes;
+  static SmemLimit cache;
+  int dev = 0;
+  SLU_CHECK_CUDA(cudaGetDevice(&dev));
+  cudaError_t err = cudaSuccess;
+  cache.raise(dev, kernel, bytes, [&](size_t b) {
+    err = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b);
+    return err == cudaSuccess ? 0 : 1;
+  });
+  if (err != cudaSuccess)
+    throw Error(SLU_ERR_CUDA, std::string("cudaFuncSetAttribute(MaxDynamicSharedMemorySize): ") +
+                                  cudaGetErrorString(err));
 }
 
 int num_sms() {

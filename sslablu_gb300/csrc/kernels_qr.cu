@@ -331,9 +331,7 @@ void panel_qr(cudaStream_t st, int m, int nfac, int ncol, double* W, int ldw, lo
   size_t sm = (size_t)m * ncol * sizeof(double);
   int use_smem = sm <= 200 * 1024;
   if (!use_smem) sm = 0;
-  if (sm > 48 * 1024)
-    SLU_CHECK_CUDA(cudaFuncSetAttribute(panel_qr_kernel,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  ensure_smem(reinterpret_cast<const void*>(panel_qr_kernel), sm);
   panel_qr_kernel<<<batch, 512, sm, st>>>(m, nfac, ncol, W, ldw, sW, tau, sTau, use_smem, W,
                                           tau, batch);
   check_launch("panel_qr_kernel");
@@ -345,9 +343,7 @@ void panel_qr2(cudaStream_t st, int m, int nfac, int ncol, double* W, double* W2
   size_t sm = (size_t)m * ncol * sizeof(double);
   int use_smem = sm <= 200 * 1024;
   if (!use_smem) sm = 0;
-  if (sm > 48 * 1024)
-    SLU_CHECK_CUDA(cudaFuncSetAttribute(panel_qr_kernel,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  ensure_smem(reinterpret_cast<const void*>(panel_qr_kernel), sm);
   panel_qr_kernel<<<2 * batch, 512, sm, st>>>(m, nfac, ncol, W, ldw, sW, tau, sTau, use_smem,
                                               W2, tau2, batch);
   check_launch("panel_qr_kernel");
@@ -370,9 +366,7 @@ void jacobi_left_sv(cudaStream_t st, int m, int n, const double* A, int lda, lon
   int np = n + (n & 1);
   size_t sm = (size_t)(m | 1) * np * sizeof(double) + np * sizeof(double) + np * sizeof(int);
   SLU_REQUIRE(sm <= 220 * 1024, "jacobi: block too large for shared memory");
-  if (sm > 48 * 1024)
-    SLU_CHECK_CUDA(cudaFuncSetAttribute(jacobi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)sm));
+  ensure_smem(reinterpret_cast<const void*>(jacobi_kernel), sm);
   int threads = 32 * std::min(32, std::max(2, (np / 2 * JAC_LANES + 31) / 32));
   jacobi_kernel<<<batch, threads, sm, st>>>(m, n, A, lda, sA, r, U, ldu, sU, sv, sS, info,
                                             lower ? 1 : 0, A, U, batch);
@@ -387,9 +381,7 @@ void jacobi_left_sv2(cudaStream_t st, int m, int n, const double* A, const doubl
   int np = n + (n & 1);
   size_t sm = (size_t)(m | 1) * np * sizeof(double) + np * sizeof(double) + np * sizeof(int);
   SLU_REQUIRE(sm <= 220 * 1024, "jacobi: block too large for shared memory");
-  if (sm > 48 * 1024)
-    SLU_CHECK_CUDA(cudaFuncSetAttribute(jacobi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)sm));
+  ensure_smem(reinterpret_cast<const void*>(jacobi_kernel), sm);
   int threads = 32 * std::min(32, std::max(2, (np / 2 * JAC_LANES + 31) / 32));
   jacobi_kernel<<<2 * batch, threads, sm, st>>>(m, n, A, lda, sA, r, U, ldu, sU, nullptr, 0, info,
                                                 lower ? 1 : 0, A2, U2, batch);

@@ -38,9 +38,18 @@ std::mutex g_scratch_mu;
 void* g_scratch_addr[kMaxDevices] = {};
 
 // Device address of g_noalloc_scratch on the current device (looked up once).
-void* noalloc_scratch_current_device() {
+// The kernels run on the handle's stream, so that stream must belong to the
+// current device: the address of another device's copy of the array would be
+// a peer address (a fault, or silent traffic over the interconnect).
+void* noalloc_scratch_current_device(cudaStream_t st) {
   int dev = 0;
   SLU_CHECK_CUDA(cudaGetDevice(&dev));
+  int sdev = dev;
+  SLU_CHECK_CUDA(cudaStreamGetDevice(st, &sdev));
+  SLU_REQUIRE(sdev == dev,
+              "slu_ulv_solve_noalloc: the handle's stream belongs to device " +
+                  std::to_string(sdev) + " but device " + std::to_string(dev) +
+                  " is current; make the stream's device current first");
   SLU_REQUIRE(dev >= 0 && dev < kMaxDevices, "device ordinal out of range for the static scratch");
   std::lock_guard<std::mutex> lock(g_scratch_mu);
   if (!g_scratch_addr[dev]) {
@@ -69,7 +78,7 @@ int slu_ulv_solve_noalloc(slu_handle_t h, slu_hbs_t op, double* B, int ldb, int 
                            " scratch bytes, above the fixed limit of " +
                            std::to_string(kNoallocScratchBytes) +
                            " (use slu_ulv_solve, or fewer right-hand sides per call)");
-    double* scratch = static_cast<double*>(noalloc_scratch_current_device());
+    double* scratch = static_cast<double*>(noalloc_scratch_current_device(h->h.stream));
     slu::hbs_solve_scratch<double>(h->h.stream, H, trans != 0, B, ldb, nrhs, scratch);
   });
 }

@@ -200,8 +200,11 @@ void tc_gemm_split3(cudaStream_t st, int M, int N, int K, double alpha, const do
 
 int num_sms();
 
-// cudaFuncSetAttribute(MaxDynamicSharedMemorySize) only when a kernel needs
-// more than it was last given (cached; safe to call while a stream captures).
+// cudaFuncSetAttribute(MaxDynamicSharedMemorySize) on the current device only
+// when a kernel needs more than that device last gave it; the limit only
+// grows, under one lock, so concurrent host threads launching the same kernel
+// at different sizes cannot lower it under one another (SmemLimit,
+// smem_limit.h).  Safe to call while a stream captures.
 void ensure_smem(const void* kernel, size_t bytes);
 
 }  // namespace slu

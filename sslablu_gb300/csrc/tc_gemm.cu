@@ -515,11 +515,7 @@ void launch_tc(cudaStream_t st, const __nv_bfloat16* Asl, const __nv_bfloat16* B
   using G = TcCfg<BN>;
   CUtensorMap ma = make_map(Asl, M, 3LL * Kp, BM);
   CUtensorMap mb = make_map(Bsl, N, 3LL * Kp, BN);
-  static std::once_flag once;
-  std::call_once(once, [] {
-    SLU_CHECK_CUDA(cudaFuncSetAttribute(tc_gemm_bf16_kernel<BN>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, G::kSmem));
-  });
+  ensure_smem(reinterpret_cast<const void*>(tc_gemm_bf16_kernel<BN>), G::kSmem);
   dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM);
   tc_gemm_bf16_kernel<BN><<<grid, kThreadsTC, G::kSmem, st>>>(ma, mb, M, N, Kp, alpha, beta, C,
                                                                 ldc, err);

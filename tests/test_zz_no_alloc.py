@@ -55,6 +55,53 @@ def test_noalloc_matches_allocating_solve_twice():
         assert relerr(x_new, x_ref) < TOL, "call %d" % call
 
 
+def _pool_used_bytes():
+    """Bytes in use from the current device's default stream-ordered memory
+    pool, the pool the library's handles take their workspaces from
+    (cudaMallocAsync); read through the driver API."""
+    import torch
+    cu = ctypes.CDLL("libcuda.so.1")
+    dev = ctypes.c_int()
+    assert cu.cuDeviceGet(ctypes.byref(dev), torch.cuda.current_device()) == 0
+    pool = ctypes.c_void_p()
+    assert cu.cuDeviceGetDefaultMemPool(ctypes.byref(pool), dev) == 0
+    used = ctypes.c_uint64()
+    CU_MEMPOOL_ATTR_USED_MEM_CURRENT = 7
+    assert cu.cuMemPoolGetAttribute(pool, CU_MEMPOOL_ATTR_USED_MEM_CURRENT,
+                                    ctypes.byref(used)) == 0
+    return used.value
+
+
+def test_noalloc_allocates_nothing():
+    """On a fresh stream (so a fresh handle with no workspace yet) the
+    allocation-free solve leaves the pool's in-use bytes unchanged, while the
+    ordinary solve on the same handle grows them (so the measurement can see
+    an allocation)."""
+    need_gpu()
+    import torch
+    from sslablu_gb300 import _lib
+    H = _factored_hbs(seed=37)
+    N = H.shape[0]
+    b = np.random.default_rng(5).standard_normal((N, 24))
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        h = _lib.handle()                       # created here: allocates its status words
+        torch.cuda.synchronize()
+        B = torch.from_numpy(b).cuda()
+        B2 = B.clone()
+        torch.cuda.synchronize()
+        before = _pool_used_bytes()
+        for _ in range(2):
+            assert _lib.lib().slu_ulv_solve_noalloc(h, H._op, _lib.ptr(B), 24, 24, 0) == 0
+        torch.cuda.synchronize()
+        after_noalloc = _pool_used_bytes()
+        assert _lib.lib().slu_ulv_solve(h, H._op, _lib.ptr(B2), 24, 24, 0) == 0
+        torch.cuda.synchronize()
+        after_solve = _pool_used_bytes()
+    assert after_noalloc == before, (before, after_noalloc)
+    assert after_solve > after_noalloc, (after_noalloc, after_solve)
+
+
 def test_noalloc_rejects_oversize():
     need_gpu()
     from sslablu_gb300 import _lib
