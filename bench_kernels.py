@@ -45,12 +45,14 @@ from sslablu_gb300 import _lib
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("kernel", choices=["tc_gemm", "f64_gemm", "compress", "solve", "refine"])
+    ap.add_argument("kernel", choices=["tc_gemm", "f64_gemm", "compress", "solve", "refine",
+                                       "tensor"])
     ap.add_argument("--m", type=int, default=4096)
     ap.add_argument("--n", type=int, default=261)
     ap.add_argument("--k", type=int, default=4096)
     ap.add_argument("--reps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--widths", default="", help="refine: right-hand-side counts, comma separated")
     ap.add_argument("--precision", default="f64", choices=["f64", "dfloat"],
                     help="solve: float64 (per-level and grouped) or the double-float sweep")
     a = ap.parse_args()
@@ -60,6 +62,8 @@ def main():
         return solve(a)
     if a.kernel == "refine":
         return refine(a)
+    if a.kernel == "tensor":
+        return tensor_sweep(a)
     m, n, k = a.m, a.n, a.k
     rng = np.random.default_rng(0)
     A = torch.from_numpy(rng.standard_normal((m, k))).cuda()
@@ -150,6 +154,37 @@ def solve(a):
     print(json.dumps(out))
 
 
+def tensor_sweep(a):
+    """The tensor-core sweep (slu_ulv_solve_ozaki) and apply on the N = m,
+    leaf 64, rank 32 operator for --n right-hand sides: median times."""
+    from sslablu_gb300.matAssembly.HBS.HBSnew import HBSMAT
+    from sslablu_gb300.synthetic import decaying_sigma, random_hbs_factors
+    N, c = a.m, a.n
+    Lv = int(np.log2(N // 64)) + 1
+    np.random.seed(1)
+    U, D, V, Nbvec = random_hbs_factors(32, 64, Lv, quad=False, sigma=decaying_sigma(32),
+                                        shift=16.0)
+    H = HBSMAT().set_mats(U, D, V, list(Nbvec), fac=2)
+    H.compute_ULV()
+    B = torch.from_numpy(np.random.default_rng(c).standard_normal((N, c))).cuda()
+    st = torch.cuda.current_stream()
+    out = {"kernel": "tensor", "N": N, "nrhs": c}
+    for name, fn in (("solve", lambda: H.solve_ozaki(B)), ("apply", lambda: H.apply_ozaki(B))):
+        for _ in range(a.warmup):
+            fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(a.reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            fn()
+            e1.record(st)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        out[name + "_ms"] = statistics.median(ts) if ts else None
+    print(json.dumps(out))
+
+
 def refine(a):
     from sslablu_gb300.matAssembly.HBS.HBSnew import HBSMAT
     from sslablu_gb300.synthetic import decaying_sigma, random_hbs_factors
@@ -177,7 +212,8 @@ def refine(a):
             ts.append(e0.elapsed_time(e1) * 1e-3)
         return statistics.median(ts)
 
-    for c in (16, 64, 256, 1024):
+    widths = [int(x) for x in a.widths.split(",")] if a.widths else (16, 64, 256, 1024)
+    for c in widths:
         B = torch.from_numpy(np.random.default_rng(c).standard_normal((N, c))).cuda()
         t64 = timed(lambda: H._dev_solve(B, False))
         x64 = H._dev_solve(B, False)
@@ -185,7 +221,19 @@ def refine(a):
         xdf = H.solve_dfloat(B)
         row = {"f64_ms": 1e3 * t64, "dfloat_ms": 1e3 * tdf, "dfloat_speedup": t64 / tdf,
                "dfloat_vs_f64": float(torch.linalg.norm(xdf - x64) / torch.linalg.norm(x64))}
-        for inner in ("dfloat", "float32"):
+        # tensor-core sweep (digit-split bfloat16 products) and apply
+        toz = timed(lambda: H.solve_ozaki(B))
+        xoz = H.solve_ozaki(B)
+        row.update({"tensor_ms": 1e3 * toz, "tensor_speedup": t64 / toz,
+                    "tensor_vs_f64": float(torch.linalg.norm(xoz - x64) /
+                                           torch.linalg.norm(x64))})
+        ta64 = timed(lambda: H._dev_apply(x64, False))
+        taoz = timed(lambda: H.apply_ozaki(x64))
+        row.update({"apply_f64_ms": 1e3 * ta64, "apply_tensor_ms": 1e3 * taoz,
+                    "apply_tensor_vs_f64": float(torch.linalg.norm(H.apply_ozaki(x64) -
+                                                                   H._dev_apply(x64, False)) /
+                                                 torch.linalg.norm(B))})
+        for inner in ("dfloat", "float32", "tensor"):
             res = {}
             tmx = timed(lambda: res.update(r=H.solve_refined(B, tol=1e-10, inner=inner)))
             row["mixed_%s_ms" % inner] = 1e3 * tmx

@@ -194,8 +194,32 @@ int slu_ulv_solve_dfloat(slu_handle_t h, slu_hbs_t op, double* B, int ldb, int n
 int slu_refine(slu_handle_t h, slu_hbs_t op, const double* B, int ldb, double* X, int ldx,
                int nrhs, double tol, int maxit, int* iters_out, double* relres_out);
 /* Inner solve of slu_refine for `op`: mode 1 double-float sweep (default),
- * mode 0 float32 sweep. */
+ * mode 0 float32 sweep, mode 2 the tensor-core sweep of slu_ulv_solve_ozaki
+ * with the residual from slu_hbs_apply_ozaki's tensor-core apply. */
 int slu_hbs_set_refine_inner(slu_hbs_t op, int mode);
+
+/* Tensor-core (tcgen05) mode-N solve and apply at float64-level accuracy.
+ * Every step product of the ULV sweep (ULVsparse.solve,
+ * matAssembly/HBS/ULVsparse.py:296-327) and of the HBS apply
+ * (HBSnew.HBSMAT.matmat, matAssembly/HBS/HBSnew.py:308-350) runs as bfloat16
+ * tensor-core products of error-free base-256 digit splits of both operands
+ * (the Ozaki scheme: 7 digits each, the 28 digit pairs of weight >= 2^-64
+ * accumulated exactly in float32 per digit diagonal, the diagonals summed in
+ * double-float); vectors between steps are float32 pairs, each right-hand-
+ * side column normalised on entry by the power of two of its largest entry
+ * (any float64 magnitude).  Relative error ~2^-50 of |S||z| per product.
+ * Steps must read at most 96 rows per block
+ * (SLU_ERR_ARG otherwise).  slu_hbs_prepare_ozaki builds the operator digits
+ * (7 bf16 digits + a row scale per operator entry) once after a
+ * factorisation; the solve / apply do it on first use.
+ * slu_ulv_solve_ozaki: Y <- A^{-1} X; slu_hbs_apply_ozaki: Y <- A X (X, Y
+ * N x nrhs float64, device, distinct).  No upstream counterpart: the
+ * tensor-core form of the mixed-precision path. */
+int slu_hbs_prepare_ozaki(slu_handle_t h, slu_hbs_t op);
+int slu_ulv_solve_ozaki(slu_handle_t h, slu_hbs_t op, const double* X, int ldx, double* Y,
+                        int ldy, int nrhs);
+int slu_hbs_apply_ozaki(slu_handle_t h, slu_hbs_t op, const double* X, int ldx, double* Y,
+                        int ldy, int nrhs);
 
 /* Null-space rule of the next slu_hbs_compress of `op`: mode 0 projects each
  * block's sketch on the last n columns of the complete Q of Om_blk^T

@@ -73,6 +73,9 @@ SIGNATURES = {
     "slu_thomas_factor": [P, c_int, c_int, P, P, P, ctypes.POINTER(c_void_p)],
     "slu_thomas_solve": [P, P, P, c_int, c_int],
     "slu_fp64_peak": [P, c_int, P, P],
+    "slu_hbs_prepare_ozaki": [P, P],
+    "slu_ulv_solve_ozaki": [P, P, P, c_int, P, c_int, c_int],
+    "slu_hbs_apply_ozaki": [P, P, P, c_int, P, c_int, c_int],
 }
 
 ERRORS = {1: "bad argument", 2: "allocation failed", 3: "CUDA error", 4: "numerical failure",

@@ -351,10 +351,50 @@ int slu_ulv_solve_dfloat(slu_handle_t h, slu_hbs_t op, double* B, int ldb, int n
   });
 }
 
+int slu_hbs_prepare_ozaki(slu_handle_t h, slu_hbs_t op) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h && op, "null argument");
+    SLU_REQUIRE(op->H.has_ulv, "HBS operator has no ULV factorisation");
+    slu::hbs_make_oz(h->h, op->H);
+  });
+}
+
+int slu_ulv_solve_ozaki(slu_handle_t h, slu_hbs_t op, const double* X, int ldx, double* Y,
+                        int ldy, int nrhs) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h && op && X && Y, "null argument");
+    SLU_REQUIRE(nrhs >= 1 && ldx >= nrhs && ldy >= nrhs, "bad right-hand side shape");
+    slu::Hbs& H = op->H;
+    SLU_REQUIRE(H.has_ulv, "HBS operator has no ULV factorisation");
+    if (!H.has_oz) slu::hbs_make_oz(h->h, H);
+    const size_t bytes = slu::hbs_oz_scratch_bytes(H, nrhs);
+    h->h.ws.reserve(bytes + 256, h->h.stream);
+    void* scratch = h->h.ws.take<char>(bytes);
+    slu::ulv_solve_oz(h->h.stream, H, X, ldx, Y, ldy, nrhs, scratch,
+                      reinterpret_cast<unsigned int*>(h->h.info.as<int>()) + 1);
+  });
+}
+
+int slu_hbs_apply_ozaki(slu_handle_t h, slu_hbs_t op, const double* X, int ldx, double* Y,
+                        int ldy, int nrhs) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h && op && X && Y, "null argument");
+    SLU_REQUIRE(nrhs >= 1 && ldx >= nrhs && ldy >= nrhs, "bad right-hand side shape");
+    slu::Hbs& H = op->H;
+    SLU_REQUIRE(H.has_ulv, "HBS operator has no ULV factorisation");
+    if (!H.has_oz) slu::hbs_make_oz(h->h, H);
+    const size_t bytes = slu::hbs_oz_scratch_bytes(H, nrhs);
+    h->h.ws.reserve(bytes + 256, h->h.stream);
+    void* scratch = h->h.ws.take<char>(bytes);
+    slu::hbs_apply_oz(h->h.stream, H, X, ldx, Y, ldy, nrhs, scratch,
+                      reinterpret_cast<unsigned int*>(h->h.info.as<int>()) + 1);
+  });
+}
+
 int slu_hbs_set_refine_inner(slu_hbs_t op, int mode) {
   return guard(nullptr, [&] {
     SLU_REQUIRE(op, "null argument");
-    SLU_REQUIRE(mode == 0 || mode == 1, "refine inner mode must be 0 or 1");
+    SLU_REQUIRE(mode >= 0 && mode <= 2, "refine inner mode must be 0, 1 or 2");
     if (op->H.refine_inner != mode) op->H.invalidate_plans();
     op->H.refine_inner = mode;
   });

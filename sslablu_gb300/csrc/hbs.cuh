@@ -68,6 +68,20 @@ struct Handle {
   std::string last_error;
 };
 
+// A step operator in the digit form of the tensor-core sweep (ozaki.cu):
+// each row of every block scaled by its own power of two 2^E (max |row| <
+// 2^E) and written as seven balanced base-256 digits, digit s a bfloat16
+// value d * 2^(-8 s) (|d| <= 256, exact in bfloat16).  Per (block, row tile
+// of NT rows, digit) one NT x wP image in the tcgen05 shared-memory core-
+// matrix order (8 x 8 tiles of 128 bytes, K-major, no swizzle), so one bulk
+// copy lands a digit slice ready for the MMA; rsc holds 2^E per row (0 for
+// padding rows and zero rows).
+struct OzOp {
+  DevBuf dig, rsc;
+  int Nb = 0, rows = 0, w = 0;
+  int NT = 0, wP = 0, ntile = 0;
+};
+
 struct Level {
   int Nb = 0;   // blocks on this level
   int n = 0;    // rows (and columns of D) per block
@@ -93,6 +107,9 @@ struct Level {
   // ranges, child after child; the transposed forward steps use Q itself
   DevBuf SwT, SwTf;
   DevBuf Qtdf, Swdf;   // double-float copies (interleaved hi/lo pairs)
+  // digit forms for the tensor-core (tcgen05) sweep and residual: Qt, Sw
+  // (the root: Sw), Aup, Adn (the root: Adn)
+  OzOp ozQt, ozSw, ozUp, ozDn;
 };
 
 struct RefinePlan;  // refine.cu: buffers + CUDA graphs of one refinement iteration
@@ -123,12 +140,14 @@ struct Hbs {
   std::vector<long long> NN;       // NNvec, L+1 entries
   bool has_mats = false, has_ulv = false, has_f32 = false, has_df = false, has_dfs = false;
   bool has_sweep = false;   // step operators composed (hbs_make_sweep)
+  bool has_oz = false;      // digit forms for the tensor-core sweep (hbs_make_oz)
   // apply operators, mode N / T (hbs_make_apply); composed on first use, so
   // set only after the composing stream has finished (other threads may read
   // them from their own streams right after)
   std::atomic<bool> has_apply[2] = {false, false};
   std::mutex lazy_mu;   // serialises first-use composition across threads
-  // inner sweep of the mixed-precision refinement: 0 float32, 1 double-float
+  // inner sweep of the mixed-precision refinement: 0 float32, 1 double-float,
+  // 2 tensor-core digit sweep with a tensor-core digit residual (ozaki.cu)
   int refine_inner = 1;
   int rk = 0, nsamples = 0;
   // null space of a sketch block's Om^T used by compression: false takes the
@@ -289,6 +308,21 @@ size_t hbs_apply_df_scratch_bytes(const Hbs& H, int c);
 void hbs_apply_df(cudaStream_t st, const Hbs& H, const double* X, int ldx, double* Y, int ldy,
                   int c, void* scratch);
 size_t hbs_nbytes(const Hbs& H, int which);
+
+// ---------------------------------------------------------------- tensor-core sweep
+// (ozaki.cu) Digit forms of the mode-N solve and apply step operators, and the
+// solve / apply run as tcgen05 block products of bfloat16 digits with exact
+// float32 accumulation.  Vectors between steps are double-float pairs.
+void hbs_make_oz(Handle& h, Hbs& H);
+// Scratch (bytes) of ulv_solve_oz / hbs_apply_oz for c right-hand sides.
+size_t hbs_oz_scratch_bytes(const Hbs& H, int c);
+// Y <- A^{-1} X (mode N) and Y <- A X on the tensor cores; X, Y N x c
+// float64 (distinct buffers), scratch of hbs_oz_scratch_bytes bytes; err a
+// device word set on a device wait timeout.
+void ulv_solve_oz(cudaStream_t st, const Hbs& H, const double* X, int ldx, double* Y, int ldy,
+                  int c, void* scratch, unsigned* err);
+void hbs_apply_oz(cudaStream_t st, const Hbs& H, const double* X, int ldx, double* Y, int ldy,
+                  int c, void* scratch, unsigned* err);
 
 // Factor pointers of one level by arithmetic type (float64 factors or their
 // float32 copies).

@@ -1,0 +1,832 @@
+// Tensor-core ULV sweep and HBS apply: every step product on tcgen05 with
+// error-free bfloat16 digit splitting.
+//
+// The mode-N solve (ULVsparse.solve, matAssembly/HBS/ULVsparse.py:296-327)
+// and the HBS apply (HBSnew.HBSMAT.matmat, matAssembly/HBS/HBSnew.py:308-350)
+// run here as the same block-sparse steps as the float64 step kernels
+// (sweep.cuh, sweep_host.cuh): out_b = S_b z_b per block, z_b gathered from up
+// to three row ranges.  Each product is evaluated to float64-level accuracy
+// from bfloat16 tensor-core products, by the error-free splitting scheme of
+// Ozaki, Ogita, Oishi and Rump ("Error-free transformations of matrix
+// multiplication by using fast routines of matrix multiplication", Numer.
+// Algorithms 59, 2012), in the form used on tensor cores by Mukunoki, Ozaki,
+// Ogita and Imamura (ISC 2020):
+//
+//   * every row i of S_b is scaled by a power of two 2^E_i (max |row| < 2^E_i)
+//     and written as seven balanced base-256 digits, S_ik = 2^E_i sum_s
+//     a_s,ik 2^(-8 s), |a_1| <= 256, |a_s| <= 128 (factor time, float64);
+//   * every column j of z_b is scaled by 2^F_j and split the same way in the
+//     kernel, from the double-float (or float64) input, with float32
+//     error-free extraction (x + sigma - sigma, sigma = 1.5 2^p) and two exact
+//     TwoSum merges of the low word: seven digits z_t, |z_4| <= 256, the others
+//     <= 128 (|z_1| <= 256);
+//   * for every digit pair with s + t <= 8 (28 products) the tensor cores form
+//     A_s Z_t in float32; all pairs of one diagonal d = s + t go into one TMEM
+//     accumulator.  Every term of accumulator d is an integer multiple of
+//     2^(-8 d) and, for steps of at most 96 columns (K), every partial sum
+//     stays below 2^24 such units, so float32 accumulation is exact;
+//   * the epilogue adds the seven diagonals exactly, as an int64 fixed-point
+//     number (the diagonals lie on nested 2^-8d grids), rounds once to a
+//     float32 pair (or a float64 for the caller's output) and scales by
+//     2^(E_i + F_j).  The exact sum matters: a residual b - A x cancels
+//     ~10^3-fold, and a float32-pair summation of the diagonals would keep
+//     only 2^-48 of the largest one.
+// The dropped digit pairs and the truncated digits leave a relative error of
+// about 2^-55 of |S| |z| per product: float64-level.  Vectors between steps
+// are double-float pairs (8 bytes, ~48 bits), so no step uses the float64
+// pipe; only a float64 input is split and a float64 output assembled.
+//
+// Kernel (one CTA per block, row tile of NT <= 64 operator rows and 128
+// right-hand-side columns; 8 digitiser warps + 1 MMA warp, one CTA per SM):
+//   1. one bulk copy (cp.async.bulk, mbarrier complete_tx) brings the seven
+//      operator digit images, stored in global memory already in the
+//      core-matrix order the MMA reads (8 x 8 bf16 tiles of 128 bytes,
+//      K-major, no swizzle), before the wait for the previous launch;
+//   2. griddepcontrol.wait (programmatic dependent launch); the digitiser
+//      warps find each column's largest magnitude (two threads per column,
+//      16 loads in flight each), then digitise z chunk by chunk (32 k) into
+//      two chunk buffers of seven 128 x 32 digit images;
+//   3. the MMA warp issues tcgen05.mma.kind::f16 (M = 128 columns, N = NT
+//      rows, K = 16) for the 28 digit pairs of each chunk into seven TMEM
+//      accumulators of NT columns as soon as the chunk is written, and hands
+//      the buffer back with tcgen05.commit: chunk c + 1 is digitised while
+//      the tensor cores work on chunk c;
+//   4. the digitiser warps read the accumulators (tcgen05.ld), combine,
+//      scale and store (one thread per column: coalesced rows).
+// Every mbarrier wait is bounded (2^22 polls); on a timeout the kernel sets
+// the handle's device error word, waits (bounded) for its own copies, frees
+// its TMEM and returns.
+#include <cuda_bf16.h>
+
+#include "hbs.cuh"
+#include "sweep_host.cuh"
+
+namespace slu {
+namespace oz {
+
+constexpr int kDig = 7;           // digits per operand
+constexpr int kM = 128;           // right-hand-side columns per CTA (MMA M)
+constexpr int kMaxW = 96;         // widest step whose diagonal sums stay exact in float32
+constexpr int kMaxNT = 64;        // operator rows per CTA (MMA N)
+constexpr int kKC = 32;           // k per digitised chunk of z (two chunk buffers)
+constexpr int kDigWarps = 8;      // digitise z, then the epilogue
+constexpr int kThreads = 32 * (kDigWarps + 1);   // + one MMA warp
+constexpr long long kWaitLimit = 1LL << 22;
+
+struct OzStep {
+  sweep::Step<dfloat> s;   // geometry and vectors (s.S unused)
+  const uint16_t* dig;     // digit images: [Nb][ntile][kDig][NT * wP] bf16
+  const float* rsc;        // row scales: [Nb][ntile * NT]
+  int NT, wP, ntile;
+  int in_f64;              // input range 0 holds float64 values (the caller's)
+  int out_f64;             // output 0 receives float64 values (the caller's)
+  // per-column normalisation of the caller's vectors: colbits[j] holds the
+  // high word of the float64 bits of max_i |X_ij| over the whole column;
+  // float64 inputs enter scaled by 2^-s_j (m_j < 2^s_j) and float64 outputs
+  // leave scaled by 2^s_j, so every vector between steps stays near unit
+  // magnitude, inside the float32 exponent range, whatever the float64 scale
+  const unsigned* colbits;
+  unsigned* err;           // device error word (timeouts)
+};
+
+// s_j of a column from its max-magnitude bits (0 for a zero column):
+// max < 2^s_j.
+__device__ __forceinline__ int col_shift(unsigned bits) {
+  return bits == 0 ? 0 : min(1023, (int)((bits >> 20) & 0x7FF) - 1022);
+}
+
+// Dynamic shared memory: two z chunk buffers (seven 128 x 32 digit images
+// each) and the seven NT x wP operator digit images, 1 KB alignment slack.
+__host__ __device__ inline size_t smem_bytes(int NT, int wP) {
+  return 2 * (size_t)kDig * kM * kKC * 2 + (size_t)kDig * NT * wP * 2 + 1024;
+}
+
+// ---------------------------------------------------------------- PTX helpers
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+// Bounded wait for the phase with the given parity; false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  const uint32_t addr = smem_u32(bar);
+  for (long long i = 0; i < kWaitLimit; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+// Contiguous global -> shared bulk copy completing on an mbarrier.
+__device__ __forceinline__ void bulk_copy(void* dst, const void* src, uint32_t bytes,
+                                          uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+// Shared-memory matrix descriptor, K-major, no swizzle: core matrices of
+// 8 rows x 16 bytes; lbo = bytes between core matrices adjacent in K,
+// sbo = bytes between 8-row groups.
+__device__ __forceinline__ uint64_t desc_noswz(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr >> 4) & 0x3FFFu);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;   // descriptor version
+  return d;                 // base offset 0, swizzle none
+}
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
+                                         uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+
+// ---------------------------------------------------------------- arithmetic
+// x rounded to a multiple of ulp(sig) (|x| < sig / 3): Ozaki's extraction.
+__device__ __forceinline__ float extract(float x, float sig) {
+  return __fsub_rn(__fadd_rn(x, sig), sig);
+}
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+__device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  e = __fsub_rn(b, __fsub_rn(s, a));
+}
+// x 2^-sh as float32 pair (h, l), with integer operations only (no float64
+// pipe): h is the scaled x with its mantissa cut to 24 bits, l the remaining
+// 29 bits rounded to float32 (48 significant bits in all).  The shift is
+// applied to the exponent, so it is exact; results below 2^-126 become 0
+// (after normalisation these are below 2^-126 of the column's largest entry).
+__device__ __forceinline__ void f64_split(double x, int sh, float& h, float& l) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned sgn = (unsigned)(b >> 63) << 31;
+  const int e = (int)((b >> 52) & 0x7FF) - sh;   // biased exponent of x 2^-sh
+  const int fe = e - 1023 + 127;
+  if (((b >> 52) & 0x7FF) == 0 || fe <= 0) {
+    h = 0.f;
+    l = 0.f;
+    return;
+  }
+  if (fe >= 255) {   // beyond float32: propagate as infinity
+    h = __uint_as_float(sgn | 0x7F800000u);
+    l = 0.f;
+    return;
+  }
+  const unsigned long long mant = b & 0xFFFFFFFFFFFFFull;
+  h = __uint_as_float(sgn | ((unsigned)fe << 23) | (unsigned)(mant >> 29));
+  const unsigned low = (unsigned)(mant & 0x1FFFFFFFull);
+  // low * 2^(e - 1075) in two exact power-of-two steps (2^-64, then
+  // 2^(e - 1011)), so neither factor leaves the float32 range early
+  const int pe = e - 1011 + 127;
+  const float lo = pe >= 1 ? __fmul_rn(__fmul_rn(__uint2float_rn(low), 0x1p-64f),
+                                       __uint_as_float((unsigned)min(pe, 254) << 23))
+                           : 0.f;
+  l = sgn ? -lo : lo;
+}
+// bfloat16 bits of a float32 with at most 8 significant bits (exact).
+__device__ __forceinline__ uint32_t bf_bits(float q) { return __float_as_uint(q) >> 16; }
+
+// a * 2^u for a float32 a that is an integer multiple of 2^-u (the digit
+// diagonals are), from its bits: exact, integer operations only.
+__device__ __forceinline__ long long grid_int(float a, int u) {
+  const unsigned b = __float_as_uint(a);
+  const int e = (int)((b >> 23) & 255);
+  if (e == 0) return 0;
+  const long long m = (long long)((b & 0x7FFFFFu) | 0x800000u);
+  const int sh = e - 150 + u;
+  const long long v = sh >= 0 ? (m << sh) : (m >> -sh);
+  return (b >> 31) ? -v : v;
+}
+
+// The exact sum of the seven digit diagonals, v = I 2^-48 + r: diagonals
+// 2..6 (grids 2^-16 .. 2^-48) as one int64 in units of 2^-48 (|I| < 2^57),
+// the two smallest (2^-56, 2^-64; at most 2^-32 of the largest) in float32.
+// The digit products cancel heavily when |S z| is much smaller than
+// |S| |z| (a residual b - A x), so the sum must be exact before it is
+// rounded: a float32 pair built by TwoSums would keep only 2^-48 of the
+// largest diagonal.
+struct DiagSum {
+  long long I;
+  float r;
+};
+__device__ __forceinline__ DiagSum diag_sum(const float (&a)[kDig]) {
+  long long I = grid_int(a[0], 16);
+  I = (I << 8) + grid_int(a[1], 24);
+  I = (I << 8) + grid_int(a[2], 32);
+  I = (I << 8) + grid_int(a[3], 40);
+  I = (I << 8) + grid_int(a[4], 48);
+  return {I, __fadd_rn(a[5], a[6])};
+}
+// v as a float32 pair (H + Lo, |Lo| <= ulp(H) / 2): H is I rounded to 24
+// bits, Lo the rest plus r.
+__device__ __forceinline__ void diag_pair(const DiagSum& d, float& H, float& Lo) {
+  float hf = 0.f, lf = 0.f;
+  if (d.I != 0) {
+    const unsigned long long aI = (unsigned long long)(d.I < 0 ? -d.I : d.I);
+    const int p = 63 - __clzll((long long)aI);   // leading bit of |I|
+    if (p < 24) {
+      hf = __fmul_rn(__int2float_rn((int)d.I), 0x1p-48f);
+    } else {
+      const int sh = p - 23;
+      const long long q = (d.I + (1LL << (sh - 1))) >> sh;   // |q| <= 2^24
+      const long long rem = d.I - (q << sh);                  // |rem| <= 2^(sh-1)
+      hf = __fmul_rn(__int2float_rn((int)q), __uint_as_float((unsigned)(127 + sh - 48) << 23));
+      lf = __fmul_rn(__ll2float_rn(rem), 0x1p-48f);
+    }
+  }
+  float s, e;
+  fast_two_sum(hf, __fadd_rn(lf, d.r), s, e);
+  H = s;
+  Lo = e;
+}
+// v in float64 (outputs to the caller).
+__device__ __forceinline__ double diag_double(const DiagSum& d) {
+  return fma((double)d.I, 0x1p-48, (double)d.r);
+}
+
+// ---------------------------------------------------------------- the kernel
+__global__ void __launch_bounds__(kThreads, 1) oz_step_kernel(const OzStep o) {
+  extern __shared__ unsigned char smraw[];
+  __shared__ __align__(8) uint64_t op_bar, done_bar;
+  __shared__ __align__(8) uint64_t zfull[2], zempty[2];
+  __shared__ uint32_t tmem_slot;
+  __shared__ volatile int s_fail;
+  __shared__ const char* rowp[kMaxW];
+  __shared__ int rowf64[kMaxW];
+  __shared__ char* outp[kMaxNT];
+  __shared__ int outf64[kMaxNT];
+  __shared__ float rs[kMaxNT];
+  __shared__ float colmax[2][kM];
+
+  const sweep::Step<dfloat>& s = o.s;
+  const int NT = o.NT, wP = o.wP, w = s.w;
+  const int nct = (s.c + kM - 1) / kM;
+  const int per_b = o.ntile * nct;
+  const int b = blockIdx.x / per_b;
+  const int rem = blockIdx.x - b * per_b;
+  const int rt = rem / nct, ct = rem - rt * nct;
+  const int c0 = ct * kM, r0 = rt * NT;
+  const int nr = min(NT, s.rows - r0);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t zsl = (uint32_t)kM * kKC * 2;   // one digit of one z chunk
+  const uint32_t zdb = (uint32_t)kDig * zsl;     // one z chunk buffer (all digits)
+  const uint32_t obytes = (uint32_t)NT * wP * 2; // one operator digit image
+  const int nch = (wP + kKC - 1) / kKC;
+  unsigned char* sm = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
+  unsigned char* zbuf = sm;             // two z chunk buffers
+  unsigned char* opb = sm + 2 * zdb;    // the seven operator digit images
+  const uint16_t* opdig = o.dig + (size_t)(b * o.ntile + rt) * kDig * NT * wP;
+  uint32_t ncols = 32;
+  while (ncols < (uint32_t)(kDig * NT)) ncols <<= 1;
+
+  if (tid == 0) {
+    mbar_init(&op_bar, 1);
+    mbar_init(&done_bar, 1);
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&zfull[i], kDigWarps);
+      mbar_init(&zempty[i], 1);
+    }
+    s_fail = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  // the operator digits are constant: their copy starts before the wait for
+  // the previous launch of the stream (one bulk copy of the seven images)
+  if (tid == 0) {
+    mbar_expect_tx(&op_bar, kDig * obytes);
+    bulk_copy(opb, opdig, kDig * obytes, &op_bar);
+  }
+  // input row of every k (the first range optionally through the
+  // permutation), output row of every tile row, row scales
+  for (int k = tid; k < w; k += kThreads) {
+    int q = 0, kk = k;
+    while (q + 1 < s.nin && kk >= s.in_rows[q]) kk -= s.in_rows[q++];
+    long long row = (long long)b * s.in_blk[q] + kk;
+    if (q == 0 && s.in_perm) row = __ldg(s.in_perm + row);
+    rowp[k] = reinterpret_cast<const char*>(s.in_p[q] + row * s.in_ld[q] + c0);
+    rowf64[k] = (q == 0 && o.in_f64) ? 1 : 0;
+  }
+  for (int i = tid; i < NT; i += kThreads) {
+    char* p = nullptr;
+    int f = 0;
+    float sc = 0.f;
+    if (i < nr) {
+      const int row = r0 + i;
+      if (row < s.split) {
+        const long long q = (long long)b * s.out_blk[0] + row;
+        const long long dst = s.out_perm ? __ldg(s.out_perm + q) : q;
+        p = reinterpret_cast<char*>(s.out_p[0] + dst * s.out_ld[0] + c0);
+        f = o.out_f64;
+      } else {
+        const long long q = (long long)b * s.out_blk[1] + (row - s.split);
+        p = reinterpret_cast<char*>(s.out_p[1] + q * s.out_ld[1] + c0);
+      }
+      sc = __ldg(o.rsc + (size_t)(b * o.ntile + rt) * NT + i);
+    }
+    outp[i] = p;
+    outf64[i] = f;
+    rs[i] = sc;
+  }
+  sweep::grid_dependency_wait();
+  if (warp == kDigWarps) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_slot)),
+                 "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_slot;
+
+  if (warp == kDigWarps) {
+    // ---------------- MMA warp: digit pair (s, t), s + t <= 8 -> accumulator
+    // s + t, chunk by chunk of z as the digitisers finish them
+    if (lane == 0) {
+      const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(NT >> 3) << 17) |
+                             ((uint32_t)(kM >> 4) << 24);
+      const uint32_t osbo = (uint32_t)wP * 16;   // operator: bytes per 8-row group
+      bool fail = !mbar_wait(&op_bar, 0);
+      for (int c = 0; c < nch && !fail; ++c) {
+        const int b2 = c & 1;
+        if (!mbar_wait(&zfull[b2], (uint32_t)(c >> 1) & 1u)) {
+          fail = true;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const int ksteps = min(kKC, wP - c * kKC) / 16;
+        // descriptors of digit 0 of the chunk (z) and of the operator at this
+        // chunk's k; a start-address offset is added in 16-byte units
+        const uint64_t a0 = desc_noswz(smem_u32(zbuf + b2 * zdb), 128, kKC * 16);
+        const uint64_t b0 =
+            desc_noswz(smem_u32(opb) + (uint32_t)c * (kKC / 8) * 128, 128, osbo);
+        const uint64_t ostep = obytes >> 4;
+        // every diagonal is first written by the pair (0, d) of chunk 0's
+        // first k step: that MMA overwrites, every other one accumulates
+#pragma unroll
+        for (int si = 0; si < kDig; ++si) {
+#pragma unroll
+          for (int ti = 0; si + ti < kDig; ++ti) {
+            const uint32_t dt = tmem + (uint32_t)((si + ti) * NT);
+            const uint64_t ad = a0 + (uint64_t)((ti * zsl) >> 4);
+            const uint64_t bd = b0 + (uint64_t)si * ostep;
+            mma_bf16(dt, ad, bd, idesc, (c | si) != 0 ? 1u : 0u);
+            if (ksteps > 1) mma_bf16(dt, ad + 16, bd + 16, idesc, 1u);
+          }
+        }
+        mma_commit(&zempty[b2]);   // this chunk buffer is free once these MMAs finish
+      }
+      if (fail) {
+        s_fail = 1;
+        if (o.err) atomicOr(o.err, 1u);
+        __threadfence_block();
+        mbar_wait(&op_bar, 0);   // the operator copy must land before the CTA exits
+      }
+      mma_commit(&done_bar);
+    }
+    __syncwarp();
+  } else {
+    // ---------------- digitiser warps (256 threads): thread (j, half) owns
+    // column j and the k of each chunk's half `half` (16 k)
+    const int j = tid & (kM - 1), half = tid >> 7;
+    const bool col_ok = c0 + j < s.c;
+    const int csh = (o.colbits && col_ok) ? col_shift(__ldg(o.colbits + c0 + j)) : 0;
+    auto load = [&](int k, float& h, float& l) {
+      h = 0.f;
+      l = 0.f;
+      if (col_ok && k < w) {
+        const char* p = rowp[k] + 8 * j;
+        if (rowf64[k]) {
+          f64_split(*reinterpret_cast<const double*>(p), csh, h, l);
+        } else {
+          const float2 v = *reinterpret_cast<const float2*>(p);
+          h = v.x;
+          l = v.y;
+        }
+      }
+    };
+    // column scale: largest |h| over the column's k (16 loads in flight)
+    float mx = 0.f;
+    for (int c = 0; c < nch; ++c) {
+      const int k0 = c * kKC + half * 16;
+      if (k0 >= wP) continue;
+      float hv[16], lv[16];
+#pragma unroll
+      for (int u = 0; u < 16; ++u) load(k0 + u, hv[u], lv[u]);
+#pragma unroll
+      for (int u = 0; u < 16; ++u) mx = fmaxf(mx, fabsf(hv[u]));
+    }
+    colmax[half][j] = mx;
+    asm volatile("bar.sync 1, %0;" ::"r"(kDigWarps * 32) : "memory");
+    float inv = 1.f, cs = 0.f;   // 2^-F and 2^F of the column (0: zero column)
+    {
+      const float m = fmaxf(colmax[0][j], colmax[1][j]);
+      if (m > 0.f) {
+        int F = (int)((__float_as_uint(m) >> 23) & 255) - 126;   // m < 2^F
+        F = max(-100, min(100, F));
+        inv = __uint_as_float((unsigned)(127 - F) << 23);
+        cs = __uint_as_float((unsigned)(127 + F) << 23);
+      }
+    }
+    bool fail = false;
+    for (int c = 0; c < nch; ++c) {
+      const int b2 = c & 1;
+      if (c >= 2 && !mbar_wait(&zempty[b2], (uint32_t)((c >> 1) - 1) & 1u)) fail = true;
+      const int k0 = c * kKC + half * 16;
+      if (k0 < wP) {
+        float hv[16], lv[16];
+#pragma unroll
+        for (int u = 0; u < 16; ++u) load(k0 + u, hv[u], lv[u]);
+#pragma unroll
+        for (int g = 0; g < 2; ++g) {
+          uint32_t wd[kDig][4];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            float hs = __fmul_rn(hv[8 * g + u], inv), ls = __fmul_rn(lv[8 * g + u], inv);
+            float q[kDig];
+            q[0] = extract(hs, 0x1.8p15f);
+            hs = __fsub_rn(hs, q[0]);
+            q[1] = extract(hs, 0x1.8p7f);
+            hs = __fsub_rn(hs, q[1]);
+            q[2] = extract(hs, 0x1.8p-1f);
+            hs = __fsub_rn(hs, q[2]);
+            float a, e;
+            two_sum(hs, ls, a, e);
+            q[3] = extract(a, 0x1.8p-9f);
+            a = __fsub_rn(a, q[3]);
+            q[4] = extract(a, 0x1.8p-17f);
+            a = __fsub_rn(a, q[4]);
+            float a2, e2;
+            two_sum(a, e, a2, e2);
+            q[5] = extract(a2, 0x1.8p-25f);
+            a2 = __fsub_rn(a2, q[5]);
+            q[6] = extract(__fadd_rn(a2, e2), 0x1.8p-33f);
+#pragma unroll
+            for (int t = 0; t < kDig; ++t) {
+              const uint32_t bits = bf_bits(q[t]);
+              if (u & 1) wd[t][u >> 1] |= bits << 16;
+              else wd[t][u >> 1] = bits;
+            }
+          }
+          // 16-byte row (8 k) of column j in core matrix (j / 8, half * 2 + g)
+          const uint32_t off = (uint32_t)(j >> 3) * (kKC * 16) +
+                               (uint32_t)(half * 2 + g) * 128 + (uint32_t)(j & 7) * 16;
+          unsigned char* zb = zbuf + b2 * zdb + off;
+#pragma unroll
+          for (int t = 0; t < kDig; ++t)
+            *reinterpret_cast<uint4*>(zb + (size_t)t * zsl) =
+                make_uint4(wd[t][0], wd[t][1], wd[t][2], wd[t][3]);
+        }
+      }
+      // generic-proxy writes -> visible to the tensor cores; one arrival per warp
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&zfull[b2]);
+    }
+    sweep::launch_dependents();
+    if (fail) {
+      s_fail = 1;
+      if (o.err) atomicOr(o.err, 1u);
+    }
+
+    // ---------------- epilogue: warp (qd, half) reads TMEM lanes 32 qd ..
+    // (its columns) and rows half * 16 + 32 i of the tile
+    const bool ok = mbar_wait(&done_bar, 0);
+    __syncwarp();
+    const bool all_ok = __all_sync(0xffffffffu, ok) && !s_fail;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (all_ok) {
+      const int qd = warp & 3, rhalf = warp >> 2;
+      const int col = qd * 32 + lane;
+      const bool cok = c0 + col < s.c;
+      // float64 outputs leave scaled back by 2^s_col (exactly, in float64)
+      const int osh = (o.colbits && cok) ? col_shift(__ldg(o.colbits + c0 + col)) : 0;
+      const double oscale = __longlong_as_double((long long)(1023 + osh) << 52);
+      const uint32_t lanes = (uint32_t)(qd * 32) << 16;
+      // col == tid % 128: this thread digitised column col, so cs is its scale
+      const float csc = cs;
+      for (int r16 = rhalf * 16; r16 < NT; r16 += 32) {
+        uint32_t v[kDig][16];
+#pragma unroll
+        for (int di = 0; di < kDig; ++di)
+          tmem_ld16(tmem + lanes + (uint32_t)(di * NT + r16), v[di]);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          const int row = r16 + i;
+          if (row >= nr || !cok) continue;
+          float a[kDig];
+#pragma unroll
+          for (int di = 0; di < kDig; ++di) a[di] = __uint_as_float(v[di][i]);
+          const DiagSum ds = diag_sum(a);
+          const float g = __fmul_rn(rs[row], csc);
+          char* p = outp[row] + 8 * col;
+          if (outf64[row]) {
+            *reinterpret_cast<double*>(p) = diag_double(ds) * ((double)g * oscale);
+          } else {
+            float H, Lo;
+            diag_pair(ds, H, Lo);
+            *reinterpret_cast<float2*>(p) = make_float2(__fmul_rn(H, g), __fmul_rn(Lo, g));
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == kDigWarps)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols)
+                 : "memory");
+}
+
+// ---------------------------------------------------------------- operator digits
+// One warp per (block, row): the row's power-of-two scale and its seven
+// balanced base-256 digits, written into the core-matrix images.
+__global__ void oz_digits_kernel(const double* __restrict__ S, long long sS, int ld, int Nb,
+                                 int rows, int w, int NT, int wP, int ntile,
+                                 uint16_t* __restrict__ dig, float* __restrict__ rsc) {
+  const int gw = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (gw >= Nb * rows) return;
+  const int b = gw / rows, r = gw - b * rows;
+  const double* row = S + (long long)b * sS + (long long)r * ld;
+  double mx = 0.0;
+  for (int k = lane; k < w; k += 32) mx = fmax(mx, fabs(row[k]));
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  int E = 0;
+  if (mx > 0.0) frexp(mx, &E);   // mx < 2^E
+  E = max(-120, min(126, E));
+  const int rt = r / NT, rr = r - rt * NT;
+  if (lane == 0) rsc[(size_t)(b * ntile + rt) * NT + rr] = mx > 0.0 ? ldexpf(1.f, E) : 0.f;
+  if (mx == 0.0) return;
+  uint16_t* img = dig + (size_t)(b * ntile + rt) * kDig * NT * wP;
+  const size_t base = (size_t)(rr >> 3) * (wP * 8) + (size_t)(rr & 7) * 8;
+  for (int k = lane; k < w; k += 32) {
+    long long F = llrint(ldexp(row[k], 56 - E));   // |F| < 2^56
+    int d[kDig];
+    for (int t = kDig - 1; t >= 1; --t) {
+      const long long dd = ((F + 128) & 255) - 128;
+      d[t] = (int)dd;
+      F = (F - dd) >> 8;
+    }
+    d[0] = (int)F;
+    const size_t off = base + (size_t)(k >> 3) * 64 + (k & 7);
+    for (int t = 0; t < kDig; ++t) {
+      const float q = ldexpf((float)d[t], -8 * (t + 1));
+      img[(size_t)t * NT * wP + off] = (uint16_t)(__float_as_uint(q) >> 16);
+    }
+  }
+}
+
+// colbits[j] = high word of the float64 bits of max_i |x_ij| (positive
+// float64 bit patterns order like their values, so an integer atomicMax on
+// the high words finds the largest exponent).  colbits must be zeroed first.
+__global__ void oz_colmax_kernel(int rows, int c, const double* __restrict__ X, int ldx,
+                                 unsigned* __restrict__ colbits) {
+  const int j = blockIdx.x * 32 + (threadIdx.x & 31);
+  if (j >= c) return;
+  unsigned m = 0;
+  for (long long i = (long long)blockIdx.y * (blockDim.x >> 5) + (threadIdx.x >> 5); i < rows;
+       i += (long long)gridDim.y * (blockDim.x >> 5)) {
+    const unsigned hi = (unsigned)((unsigned long long)__double_as_longlong(X[i * ldx + j]) >> 32);
+    m = max(m, hi & 0x7FFFFFFFu);
+  }
+  if (m) atomicMax(colbits + j, m);
+}
+
+void col_max(cudaStream_t st, int rows, int c, const double* X, int ldx, unsigned* colbits) {
+  SLU_CHECK_CUDA(cudaMemsetAsync(colbits, 0, 4 * (size_t)c, st));
+  dim3 grid((c + 31) / 32, (unsigned)std::min<long long>(64, std::max(1, rows / 64)));
+  oz_colmax_kernel<<<grid, 256, 0, st>>>(rows, c, X, ldx, colbits);
+  check_launch("oz_colmax_kernel");
+}
+
+void make_op(cudaStream_t st, OzOp& o, const double* S, int Nb, int rows, int w) {
+  SLU_REQUIRE(S, "tensor-core sweep: step operator not composed");
+  SLU_REQUIRE(w >= 1 && w <= kMaxW,
+              "tensor-core sweep: a step reads " + std::to_string(w) +
+                  " rows per block; at most 96 keep its digit sums exact");
+  o.Nb = Nb;
+  o.rows = rows;
+  o.w = w;
+  o.NT = rows > 32 ? 64 : (rows > 16 ? 32 : 16);
+  o.ntile = (rows + o.NT - 1) / o.NT;
+  o.wP = (w + 15) / 16 * 16;
+  const size_t nd = (size_t)Nb * o.ntile * kDig * o.NT * o.wP;
+  o.dig.alloc(2 * nd, st);
+  SLU_CHECK_CUDA(cudaMemsetAsync(o.dig.p, 0, 2 * nd, st));
+  const size_t nr = (size_t)Nb * o.ntile * o.NT;
+  o.rsc.alloc(4 * nr, st);
+  SLU_CHECK_CUDA(cudaMemsetAsync(o.rsc.p, 0, 4 * nr, st));
+  const long long warps = (long long)Nb * rows;
+  oz_digits_kernel<<<(unsigned)((warps + 7) / 8), 256, 0, st>>>(
+      S, (long long)rows * w, w, Nb, rows, w, o.NT, o.wP, o.ntile, o.dig.as<uint16_t>(),
+      o.rsc.as<float>());
+  check_launch("oz_digits_kernel");
+}
+
+void launch(cudaStream_t st, const sweep::Step<dfloat>& s, const OzOp& op, bool in_f64,
+            bool out_f64, const unsigned* colbits, unsigned* err, const char* what) {
+  SLU_REQUIRE(op.dig.p && s.rows == op.rows && s.w == op.w && s.nb == op.Nb,
+              "tensor-core sweep: digit operator does not match its step");
+  OzStep o{};
+  o.s = s;
+  o.dig = op.dig.as<uint16_t>();
+  o.rsc = op.rsc.as<float>();
+  o.NT = op.NT;
+  o.wP = op.wP;
+  o.ntile = op.ntile;
+  o.in_f64 = in_f64 ? 1 : 0;
+  o.out_f64 = out_f64 ? 1 : 0;
+  o.colbits = (in_f64 || out_f64) ? colbits : nullptr;
+  o.err = err;
+  sweep::LaunchPlan p;
+  p.ctas = (long long)s.nb * op.ntile * ((s.c + kM - 1) / kM);
+  p.threads = kThreads;
+  p.smem = smem_bytes(op.NT, op.wP);
+  SLU_REQUIRE(p.ctas < (1LL << 31), "tensor-core sweep: step too large");
+  ensure_smem(reinterpret_cast<const void*>(oz_step_kernel), p.smem);
+  sweep::launch_pdl(oz_step_kernel, p, st, what, o);
+}
+
+}  // namespace oz
+
+void hbs_make_oz(Handle& h, Hbs& H) {
+  SLU_REQUIRE(H.has_sweep, "step operators not composed (factor the operator first)");
+  std::lock_guard<std::mutex> lock(H.lazy_mu);
+  if (H.has_oz) return;
+  if (!H.has_apply[0]) hbs_make_apply(h, H, false);
+  cudaStream_t st = h.stream;
+  const int L = H.L;
+  for (int t = 0; t + 1 < L; ++t) {
+    Level& l = H.lv[t];
+    oz::make_op(st, l.ozQt, l.Qt.as<double>(), l.Nb, l.n, l.n);
+    oz::make_op(st, l.ozSw, l.Sw.as<double>(), l.Nb, t == 0 ? l.n : 2 * l.n, l.nu + 2 * l.k);
+    oz::make_op(st, l.ozUp, l.Aup.as<double>(), l.Nb, l.k, l.n);
+    oz::make_op(st, l.ozDn, l.Adn.as<double>(), l.Nb, l.n, l.n + l.k);
+  }
+  Level& r = H.lv[L - 1];
+  oz::make_op(st, r.ozSw, r.Sw.as<double>(), 1, L == 1 ? r.n : 2 * r.n, r.n);
+  oz::make_op(st, r.ozDn, r.Adn.as<double>(), 1, r.n, r.n);
+  SLU_CHECK_CUDA(cudaStreamSynchronize(st));
+  H.has_oz = true;
+}
+
+size_t hbs_oz_scratch_bytes(const Hbs& H, int c) {
+  const size_t nc = ((size_t)H.N * c + 63) & ~size_t(63);
+  const size_t solve = 5 * nc;
+  const size_t apply = hbs_apply_scratch_elems(H, c);
+  return sizeof(dfloat) * std::max(solve, apply) + (((size_t)4 * c + 255) & ~size_t(255)) + 256;
+}
+
+namespace {
+// Scratch split: the column maxima first, the step vectors after them.
+unsigned* oz_colbits(void* scratch) { return static_cast<unsigned*>(scratch); }
+dfloat* oz_vectors(void* scratch, int c) {
+  return reinterpret_cast<dfloat*>(static_cast<char*>(scratch) +
+                                   (((size_t)4 * c + 255) & ~size_t(255)));
+}
+}  // namespace
+
+void ulv_solve_oz(cudaStream_t st, const Hbs& H, const double* X, int ldx, double* Y, int ldy,
+                  int c, void* scratch, unsigned* err) {
+  SLU_REQUIRE(H.has_oz, "tensor-core sweep not prepared");
+  SLU_REQUIRE(static_cast<const void*>(X) != static_cast<const void*>(Y),
+              "tensor-core sweep: input and output must be different buffers");
+  const int L = H.L;
+  const int64_t* perm = H.perm.as<int64_t>();
+  const size_t nc = ((size_t)H.N * c + 63) & ~size_t(63);
+  unsigned* cb = oz_colbits(scratch);
+  dfloat* ws = oz_vectors(scratch, c);
+  dfloat* ru = ws;
+  dfloat* P[4] = {ws + nc, ws + 2 * nc, ws + 3 * nc, ws + 4 * nc};
+  // the caller's float64 vectors are read by the first step and written by
+  // the last; the step vectors in between are double-float pairs
+  const dfloat* x = reinterpret_cast<const dfloat*>(X);
+  dfloat* y = reinterpret_cast<dfloat*>(Y);
+  const std::vector<long long>& NN = H.NN;
+  oz::col_max(st, H.N, c, X, ldx, cb);
+  if (L == 1) {
+    sweep::Step<dfloat> s = sweep::root_step<dfloat>(H, x, ldx, y, ldy, nullptr, nullptr, c);
+    s.in_p[0] = x;
+    s.in_ld[0] = ldx;
+    oz::launch(st, s, H.lv[0].ozSw, true, true, cb, err, "oz_root_step");
+    return;
+  }
+  const dfloat* src = x;
+  int lds = ldx;
+  for (int t = 0; t + 1 < L; ++t) {
+    oz::launch(st,
+               sweep::forward_step<dfloat>(H, t, src, lds, t == 0 ? perm : nullptr,
+                                           ru + NN[t] * c, P[t & 1], c),
+               H.lv[t].ozQt, t == 0, false, cb, err, "oz_fwd_step");
+    src = P[t & 1];
+    lds = c;
+  }
+  oz::launch(st, sweep::root_step<dfloat>(H, src, lds, y, ldy, P[2], P[3], c), H.lv[L - 1].ozSw,
+             false, false, cb, err, "oz_root_step");
+  int in = 2;
+  for (int t = L - 2; t >= 0; --t) {
+    const int out = (in == 2) ? 0 : 2;
+    oz::launch(st,
+               sweep::backward_step<dfloat>(H, t, ru + NN[t] * c, P[in + 1], P[in], P[out],
+                                            P[out + 1], y, ldy, c),
+               H.lv[t].ozSw, false, t == 0, cb, err, "oz_bwd_step");
+    in = out;
+  }
+}
+
+void hbs_apply_oz(cudaStream_t st, const Hbs& H, const double* X, int ldx, double* Y, int ldy,
+                  int c, void* scratch, unsigned* err) {
+  SLU_REQUIRE(H.has_oz, "tensor-core sweep not prepared");
+  SLU_REQUIRE(static_cast<const void*>(X) != static_cast<const void*>(Y),
+              "tensor-core apply: input and output must be different buffers");
+  const int L = H.L;
+  const int64_t* perm = H.perm.as<int64_t>();
+  unsigned* cb = oz_colbits(scratch);
+  dfloat* ws = oz_vectors(scratch, c);
+  const dfloat* x = reinterpret_cast<const dfloat*>(X);
+  dfloat* y = reinterpret_cast<dfloat*>(Y);
+  std::vector<dfloat*> VV(L, nullptr);
+  size_t off = 0;
+  for (int t = 0; t + 1 < L; ++t) {
+    VV[t + 1] = ws + off;
+    off += ((size_t)H.lv[t].Nb * H.lv[t].k * c + 63) & ~size_t(63);
+  }
+  dfloat* u[2] = {ws + off, ws + off + (((size_t)H.N * c + 63) & ~size_t(63))};
+  oz::col_max(st, H.N, c, X, ldx, cb);
+  if (L == 1) {
+    const Level& r = H.lv[0];
+    oz::launch(st,
+               sweep::down_step<dfloat>(r, nullptr, true, x, ldx, perm, nullptr, y, ldy, perm, c),
+               r.ozDn, true, true, cb, err, "oz_apply_root");
+    return;
+  }
+  for (int t = 0; t + 1 < L; ++t) {
+    const Level& l = H.lv[t];
+    oz::launch(st,
+               sweep::up_step<dfloat>(l, nullptr, t == 0 ? x : VV[t], t == 0 ? ldx : c,
+                                      t == 0 ? perm : nullptr, VV[t + 1], c),
+               l.ozUp, t == 0, false, cb, err, "oz_apply_up");
+  }
+  const Level& r = H.lv[L - 1];
+  oz::launch(st,
+             sweep::down_step<dfloat>(r, nullptr, true, VV[L - 1], c, nullptr, nullptr, u[0], c,
+                                      nullptr, c),
+             r.ozDn, false, false, cb, err, "oz_apply_root");
+  int cur = 0;
+  for (int t = L - 2; t >= 0; --t) {
+    const Level& l = H.lv[t];
+    const bool leaf = t == 0;
+    oz::launch(st,
+               sweep::down_step<dfloat>(l, nullptr, false, leaf ? x : VV[t], leaf ? ldx : c,
+                                        leaf ? perm : nullptr, u[cur], leaf ? y : u[cur ^ 1],
+                                        leaf ? ldy : c, leaf ? perm : nullptr, c),
+               l.ozDn, leaf, leaf, cb, err, "oz_apply_down");
+    cur ^= 1;
+  }
+}
+
+}  // namespace slu

@@ -14,6 +14,7 @@
 // from the second correction on (a float32 solve alone never reaches a
 // float64 tolerance).
 #include <cmath>
+#include <cstring>
 
 #include "abi_types.cuh"
 #include "refine_kernels.cuh"
@@ -22,9 +23,9 @@ namespace slu {
 
 struct RefinePlan {
   int c = 0;
-  int inner = 0;   // 0 float32 sweep (f), 1 double-float sweep (d)
-  DevBuf B, X, r, f, d, bn, rn, solve_ws, df_ws;
-  double* host_norms = nullptr;   // pinned: [bn (c) | rn (c)]
+  int inner = 0;   // 0 float32 sweep (f), 1 double-float sweep (d), 2 tensor-core sweep
+  DevBuf B, X, r, f, d, bn, rn, solve_ws, df_ws, ozerr;
+  double* host_norms = nullptr;   // pinned: [bn (c) | rn (c) | error word]
   cudaGraphExec_t first = nullptr, next = nullptr;
   long long first_kernels = 0, next_kernels = 0;   // kernel nodes per graph
   ~RefinePlan() {
@@ -48,6 +49,28 @@ void enqueue_iteration(cudaStream_t st, const Hbs& H, RefinePlan& P, bool first)
     SLU_CHECK_CUDA(cudaMemcpyAsync(P.host_norms, P.bn.p, 8 * c, cudaMemcpyDeviceToHost, st));
   }
   const double* rhs = first ? B : r;
+  if (P.inner == 2) {
+    // tensor-core sweep and residual (ozaki.cu): the first solve writes X in
+    // float64 directly; corrections come back as double-float pairs
+    unsigned* err = P.ozerr.as<unsigned>();
+    double* d = P.d.as<double>();
+    if (first) {
+      ulv_solve_oz(st, H, rhs, c, X, c, c, P.solve_ws.p, err);
+    } else {
+      ulv_solve_oz(st, H, rhs, c, d, c, c, P.solve_ws.p, err);
+      add_k<<<gsz(n), 256, 0, st>>>(n, d, X);
+      check_launch("add_k");
+    }
+    hbs_apply_oz(st, H, X, c, r, c, c, P.solve_ws.p, err);
+    resid_k<<<gsz(n), 256, 0, st>>>(n, B, r);
+    check_launch("resid_k");
+    colnorm2_k<<<c, 256, 0, st>>>(N, c, r, c, P.rn.as<double>());
+    check_launch("colnorm2_k");
+    SLU_CHECK_CUDA(cudaMemcpyAsync(P.host_norms + c, P.rn.p, 8 * c, cudaMemcpyDeviceToHost, st));
+    SLU_CHECK_CUDA(cudaMemcpyAsync(P.host_norms + 2 * c, P.ozerr.p, 8, cudaMemcpyDeviceToHost,
+                                   st));
+    return;
+  }
   if (P.inner == 1) {
     dfloat* d = P.d.as<dfloat>();
     to_dfs_k<<<gsz(n), 256, 0, st>>>(n, rhs, d);
@@ -109,13 +132,20 @@ RefinePlan& plan_for(Handle& h, Hbs& H, int c) {
   P->B.alloc(8 * n, st);
   P->X.alloc(8 * n, st);
   P->r.alloc(8 * n, st);
-  if (P->inner == 1) P->d.alloc(8 * n, st);
+  if (P->inner >= 1) P->d.alloc(8 * n, st);
   else P->f.alloc(4 * n, st);
   P->bn.alloc(8 * (size_t)c, st);
   P->rn.alloc(8 * (size_t)c, st);
-  P->solve_ws.alloc(hbs_solve_scratch_bytes(H, c, P->inner == 1 ? 8 : 4), st);
-  P->df_ws.alloc(hbs_apply_df_scratch_bytes(H, c), st);
-  SLU_CHECK_CUDA(cudaMallocHost(&P->host_norms, 16 * (size_t)c));
+  if (P->inner == 2) {
+    P->solve_ws.alloc(hbs_oz_scratch_bytes(H, c), st);
+    P->ozerr.alloc(8, st);
+    SLU_CHECK_CUDA(cudaMemsetAsync(P->ozerr.p, 0, 8, st));
+  } else {
+    P->solve_ws.alloc(hbs_solve_scratch_bytes(H, c, P->inner == 1 ? 8 : 4), st);
+    P->df_ws.alloc(hbs_apply_df_scratch_bytes(H, c), st);
+  }
+  SLU_CHECK_CUDA(cudaMallocHost(&P->host_norms, 16 * (size_t)c + 16));
+  P->host_norms[2 * c] = 0.0;
   SLU_CHECK_CUDA(cudaStreamSynchronize(st));
   // an uncaptured run first: sets kernel attributes and validates the sequence
   SLU_CHECK_CUDA(cudaMemsetAsync(P->B.p, 0, 8 * n, st));
@@ -143,9 +173,13 @@ RefinePlan& plan_for(Handle& h, Hbs& H, int c) {
 void hbs_refine(Handle& h, Hbs& H, const double* B, int ldb, double* X, int ldx, int c,
                 double tol, int maxit, int* iters, double* relres) {
   cudaStream_t st = h.stream;
-  if (H.refine_inner == 1 && !H.has_dfs) hbs_make_dfs(h, H);
-  if (H.refine_inner == 0 && !H.has_f32) hbs_make_f32(h, H);
-  if (!H.has_df) hbs_make_df(h, H);
+  if (H.refine_inner == 2) {
+    if (!H.has_oz) hbs_make_oz(h, H);
+  } else {
+    if (H.refine_inner == 1 && !H.has_dfs) hbs_make_dfs(h, H);
+    if (H.refine_inner == 0 && !H.has_f32) hbs_make_f32(h, H);
+    if (!H.has_df) hbs_make_df(h, H);
+  }
   RefinePlan& P = plan_for(h, H, c);
   SLU_CHECK_CUDA(cudaMemcpy2DAsync(P.B.p, 8 * (size_t)c, B, 8 * (size_t)ldb, 8 * (size_t)c,
                                    H.N, cudaMemcpyDeviceToDevice, st));
@@ -161,6 +195,15 @@ void hbs_refine(Handle& h, Hbs& H, const double* B, int ldb, double* X, int ldx,
       continue;
     }
     SLU_CHECK_CUDA(cudaStreamSynchronize(st));
+    if (P.inner == 2) {
+      unsigned long long ew = 0;
+      std::memcpy(&ew, P.host_norms + 2 * c, 8);
+      if (ew != 0) {
+        SLU_CHECK_CUDA(cudaMemsetAsync(P.ozerr.p, 0, 8, st));
+        P.host_norms[2 * c] = 0.0;
+        throw Error(SLU_ERR_TIMEOUT, "tensor-core sweep: a device wait timed out");
+      }
+    }
     worst = 0.0;
     for (int j = 0; j < c; ++j) {
       const double bj = P.host_norms[j], rj = P.host_norms[c + j];

@@ -67,6 +67,13 @@ __global__ void resid_dfs_k(long long n, const double* __restrict__ b, const dfl
   }
 }
 
+// x += d
+__global__ void add_k(long long n, const double* __restrict__ d, double* __restrict__ x) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+       e += (long long)gridDim.x * blockDim.x)
+    x[e] += d[e];
+}
+
 // r = b - r
 __global__ void resid_k(long long n, const double* __restrict__ b, double* __restrict__ r) {
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;

@@ -402,15 +402,39 @@ class HBSMAT:
                                              B.shape[1]))
         return dv.finish(B, b, one)
 
+    def solve_ozaki(self, b):
+        """Mode-N solve on the tensor cores (slu_ulv_solve_ozaki): every step
+        product as bfloat16 tcgen05 products of error-free base-256 digit
+        splits of operator and vector (Ozaki scheme), float64-level accuracy;
+        double-float vectors between steps."""
+        X, one = dv.prepare_rhs(b)
+        X = dv.as_2d(X).contiguous()
+        Y = torch.empty_like(X)
+        L.check(L.lib().slu_ulv_solve_ozaki(L.handle(), self._op, L.ptr(X), X.shape[1],
+                                            L.ptr(Y), Y.shape[1], X.shape[1]))
+        return dv.finish(Y, b, one)
+
+    def apply_ozaki(self, x):
+        """A x on the tensor cores (slu_hbs_apply_ozaki): the apply steps as
+        digit-split bfloat16 products, float64-level accuracy."""
+        X, one = dv.prepare_rhs(x)
+        X = dv.as_2d(X).contiguous()
+        Y = torch.empty_like(X)
+        L.check(L.lib().slu_hbs_apply_ozaki(L.handle(), self._op, L.ptr(X), X.shape[1],
+                                            L.ptr(Y), Y.shape[1], X.shape[1]))
+        return dv.finish(Y, x, one)
+
     def solve_refined(self, b, tol=1e-10, maxit=10, inner="dfloat"):
         """Mixed-precision solve: ULV sweeps on the float32 units
         (``inner='dfloat'``: double-float, usually one iteration;
-        ``'float32'``: plain float32, two or three) corrected by float64-
-        accurate residuals of this operator until ||b - A x|| / ||b|| <= tol
-        per column.  Returns (x, iterations, worst relative residual)."""
-        modes = {"float32": 0, "dfloat": 1}
+        ``'float32'``: plain float32, two or three) or on the tensor cores
+        (``'tensor'``: digit-split bfloat16 products, with the residual from
+        the tensor-core apply) corrected by float64-accurate residuals of
+        this operator until ||b - A x|| / ||b|| <= tol per column.  Returns
+        (x, iterations, worst relative residual)."""
+        modes = {"float32": 0, "dfloat": 1, "tensor": 2}
         if inner not in modes:
-            raise ValueError("inner must be 'dfloat' or 'float32'")
+            raise ValueError("inner must be 'dfloat', 'float32' or 'tensor'")
         L.check(L.lib().slu_hbs_set_refine_inner(self._op, modes[inner]))
         B, one = dv.prepare_rhs(b)
         X = torch.empty_like(B)

@@ -110,3 +110,28 @@ def test_hbs_slab_solvers_refined(golden):
             assert 2 <= it <= 8
         assert x.shape == b.shape and it >= 1
         assert rel <= 1e-10 and relerr(M @ x, b) < 1e-10
+
+
+def test_rbhbs_concurrent_compressions_repeat(golden):
+    """One red-black level's compressions run on worker threads, each at its
+    own tree level and so its own shared-memory size for the panel QR and
+    Jacobi kernels (omsdirectsolveHBS.py:436-483 _build_level: three
+    compressions per kept node).  Repeated factorisations with the same
+    seed must all succeed and give the same solution to rounding."""
+    need_gpu()
+    from sslablu_gb300.direct_solve.omsdirectsolveHBS import RedBlackSolverHBS
+    g = golden("rbhbs_kernel")
+    m, nS, leaf, nlev = int(g["m"]), int(g["nS"]), int(g["leaf"]), int(g["nlev"])
+    tree = types.SimpleNamespace(perm_leaf=np.arange(m), nleaves=m // leaf, nlevels=nlev)
+    S = kernel_system(m, nS)
+    M = tridiag_matrix(S, m)
+    res_ref = relerr(M @ g["x_rb_24"], g["b"])
+    xs = []
+    for _ in range(4):
+        np.random.seed(11)
+        R = RedBlackSolverHBS(m, 24, tree, False)
+        R.factorize(_ops(S, tree))
+        xs.append(R.solve(g["b"]))
+        assert relerr(M @ xs[-1], g["b"]) < 2 * res_ref
+    for x in xs[1:]:
+        assert relerr(x, xs[0]) < 1e-8
