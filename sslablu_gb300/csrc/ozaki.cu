@@ -25,12 +25,13 @@
 //     accumulator.  Every term of accumulator d is an integer multiple of
 //     2^(-8 d) and, for steps of at most 96 columns (K), every partial sum
 //     stays below 2^24 such units, so float32 accumulation is exact;
-//   * the epilogue adds the seven diagonals exactly, as an int64 fixed-point
-//     number (the diagonals lie on nested 2^-8d grids), rounds once to a
+//   * the epilogue adds the seven diagonals exactly, in float32 (TwoSums and
+//     additions whose results provably fit their grid: the diagonals lie on
+//     nested 2^-8d grids with known bounds, see diag_sum), rounds once to a
 //     float32 pair (or a float64 for the caller's output) and scales by
 //     2^(E_i + F_j).  The exact sum matters: a residual b - A x cancels
-//     ~10^3-fold, and a float32-pair summation of the diagonals would keep
-//     only 2^-48 of the largest one.
+//     ~10^3-fold, and a rounded summation of the diagonals would keep only
+//     2^-48 of the largest one.
 // The dropped digit pairs and the truncated digits leave a relative error of
 // about 2^-55 of |S| |z| per product: float64-level.  Vectors between steps
 // are double-float pairs (8 bytes, ~48 bits), so no step uses the float64
@@ -188,10 +189,6 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   const float bb = __fsub_rn(s, a);
   e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
-__device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e) {
-  s = __fadd_rn(a, b);
-  e = __fsub_rn(b, __fsub_rn(s, a));
-}
 // x 2^-sh as float32 pair (h, l), with integer operations only (no float64
 // pipe): h is the scaled x with its mantissa cut to 24 bits, l the remaining
 // 29 bits rounded to float32 (48 significant bits in all).  The shift is
@@ -226,62 +223,48 @@ __device__ __forceinline__ void f64_split(double x, int sh, float& h, float& l) 
 // bfloat16 bits of a float32 with at most 8 significant bits (exact).
 __device__ __forceinline__ uint32_t bf_bits(float q) { return __float_as_uint(q) >> 16; }
 
-// a * 2^u for a float32 a that is an integer multiple of 2^-u (the digit
-// diagonals are), from its bits: exact, integer operations only.
-__device__ __forceinline__ long long grid_int(float a, int u) {
-  const unsigned b = __float_as_uint(a);
-  const int e = (int)((b >> 23) & 255);
-  if (e == 0) return 0;
-  const long long m = (long long)((b & 0x7FFFFFu) | 0x800000u);
-  const int sh = e - 150 + u;
-  const long long v = sh >= 0 ? (m << sh) : (m >> -sh);
-  return (b >> 31) ? -v : v;
-}
-
-// The exact sum of the seven digit diagonals, v = I 2^-48 + r: diagonals
-// 2..6 (grids 2^-16 .. 2^-48) as one int64 in units of 2^-48 (|I| < 2^57),
-// the two smallest (2^-56, 2^-64; at most 2^-32 of the largest) in float32.
+// The seven digit diagonals a_0..a_6 summed with no rounding error, as four
+// float32 terms v = h + l + e + f.  After the row and column scaling every
+// operator and vector entry is below 1 in magnitude, so with K <= 96 and the
+// digit bounds above, a_d is an integer multiple of 2^-(8d+16) with
+// |a_0| < 2^7, |a_1| < 2^-1.4, |a_2| < 2^-9.1, |a_3| < 2^-16.4,
+// |a_4| < 2^-24.6, |a_5| < 2^-32.2, |a_6| < 2^-40.1.  Alternating TwoSums
+// (exact by construction) with plain additions whose results provably fit
+// in 24 bits of their grid:
+//   (h, l) = TwoSum(a_0, a_1):  l a multiple of 2^-24, |l| <= ulp(h)/2 <= 2^-18
+//   l + a_2:  grid 2^-32, magnitude < 2^-9, so 23 bits: exact
+//   (l, e) = TwoSum(l, a_3):    e a multiple of 2^-40, |e| <= 2^-33
+//   e + a_4:  grid 2^-48, magnitude < 2^-24.5: exact
+//   (e, f) = TwoSum(e, a_5):    f a multiple of 2^-56, |f| <= 2^-49
+//   f + a_6:  grid 2^-64, magnitude < 2^-39.9: exact.
 // The digit products cancel heavily when |S z| is much smaller than
-// |S| |z| (a residual b - A x), so the sum must be exact before it is
-// rounded: a float32 pair built by TwoSums would keep only 2^-48 of the
-// largest diagonal.
+// |S| |z| (the apply inside a residual b - A x), so no rounding may happen
+// before the sum is complete; the only rounding is the final one to a
+// float32 pair or a float64 (~2^-48 of |v| for the pair).
 struct DiagSum {
-  long long I;
-  float r;
+  float h, l, e, f;
 };
 __device__ __forceinline__ DiagSum diag_sum(const float (&a)[kDig]) {
-  long long I = grid_int(a[0], 16);
-  I = (I << 8) + grid_int(a[1], 24);
-  I = (I << 8) + grid_int(a[2], 32);
-  I = (I << 8) + grid_int(a[3], 40);
-  I = (I << 8) + grid_int(a[4], 48);
-  return {I, __fadd_rn(a[5], a[6])};
+  DiagSum d;
+  float l, e, f;
+  two_sum(a[0], a[1], d.h, l);
+  two_sum(__fadd_rn(l, a[2]), a[3], d.l, e);
+  two_sum(__fadd_rn(e, a[4]), a[5], d.e, f);
+  d.f = __fadd_rn(f, a[6]);
+  return d;
 }
-// v as a float32 pair (H + Lo, |Lo| <= ulp(H) / 2): H is I rounded to 24
-// bits, Lo the rest plus r.
+// v as a float32 pair (H + Lo, |Lo| <= ulp(H) / 2).  h + l may cancel, so H
+// takes e in with a second TwoSum before the small terms are added.
 __device__ __forceinline__ void diag_pair(const DiagSum& d, float& H, float& Lo) {
-  float hf = 0.f, lf = 0.f;
-  if (d.I != 0) {
-    const unsigned long long aI = (unsigned long long)(d.I < 0 ? -d.I : d.I);
-    const int p = 63 - __clzll((long long)aI);   // leading bit of |I|
-    if (p < 24) {
-      hf = __fmul_rn(__int2float_rn((int)d.I), 0x1p-48f);
-    } else {
-      const int sh = p - 23;
-      const long long q = (d.I + (1LL << (sh - 1))) >> sh;   // |q| <= 2^24
-      const long long rem = d.I - (q << sh);                  // |rem| <= 2^(sh-1)
-      hf = __fmul_rn(__int2float_rn((int)q), __uint_as_float((unsigned)(127 + sh - 48) << 23));
-      lf = __fmul_rn(__ll2float_rn(rem), 0x1p-48f);
-    }
-  }
-  float s, e;
-  fast_two_sum(hf, __fadd_rn(lf, d.r), s, e);
-  H = s;
-  Lo = e;
+  float s, t, t2;
+  two_sum(d.h, d.l, s, t);
+  two_sum(s, d.e, s, t2);
+  two_sum(s, __fadd_rn(__fadd_rn(t, t2), d.f), H, Lo);
 }
-// v in float64 (outputs to the caller).
+// v in float64 (outputs to the caller): h + l and e + f are exact in float64
+// (spans of at most 47 and 40 bits), one rounding in the last addition.
 __device__ __forceinline__ double diag_double(const DiagSum& d) {
-  return fma((double)d.I, 0x1p-48, (double)d.r);
+  return ((double)d.h + (double)d.l) + ((double)d.e + (double)d.f);
 }
 
 // ---------------------------------------------------------------- the kernel

@@ -4,8 +4,11 @@ every member's result equals the result of its own solve.
 
 Float64: each column runs the same sequence of operations as the
 per-operator solve, whatever the column chunking, so the bound is 1e-15
-(relative).  Mixed: every member reaches the 1e-10 relative residual against
-its float64 operator and agrees with its own refined solve to 1e-8."""
+(relative); every member also matches the CPU oracle's float64 solve of the
+same operator (oracle/hbs.py: ULVsparse.solve restated, with the same random
+sketches when the operator is compressed) to 1e-12.  Mixed: every member
+reaches the 1e-10 relative residual measured with the oracle's float64 apply
+and matches the oracle's solution to 1e-10."""
 import numpy as np
 import pytest
 
@@ -19,25 +22,43 @@ SHAPES = [(8, 16, 5, False), (16, 32, 4, False), (8, 32, 3, False), (16, 16, 6, 
           (32, 64, 5, False), (8, 16, 3, True), (12, 24, 2, False)]
 
 
-def _operators(shift=4.0, compress=False):
+def _operators(shift=4.0, compress=False, oracle=False):
+    """The GPU operators, and with ``oracle`` also their CPU oracle twins
+    (the same factors, or the same compression from the same sketches)."""
+    from oracle.hbs import OracleHBS
     from sslablu_gb300.matAssembly.HBS.HBSnew import HBSMAT
     from sslablu_gb300.synthetic import random_hbs_factors
-    ops = []
+    ops, orcs = [], []
     for j, (k, nl, L, quad) in enumerate(SHAPES):
         np.random.seed(300 + j)
         U, D, V, Nbvec = random_hbs_factors(k, nl, L, quad=quad, shift=shift)
         fac = 4 if quad else 2
         A = HBSMAT().set_mats(U, D, V, list(Nbvec), fac=fac)
+        O = OracleHBS().set_mats(U, D, V, list(Nbvec), fac=fac)
         nsamp = (6 * k + 4 * nl + 5) if quad else (4 * k + 2 * nl + 5)
         if compress and nsamp < A.shape[0]:
             H = HBSMAT(A, tree=None, quad=quad)
             H.set_Nbvec(list(Nbvec))
+            state = np.random.get_state()
             H.construct(k, True)
+            if oracle:
+                np.random.set_state(state)
+                O = OracleHBS(O, None, Nbvec[0], len(Nbvec), fac).construct(k)
+                O.compute_ULV()
         else:
             A.compute_ULV()
             H = A
+            if oracle:
+                O.compute_ULV()
         ops.append(H)
-    return ops
+        orcs.append(O)
+    return (ops, orcs) if oracle else ops
+
+
+def _oracle_residual(O, x, b):
+    """Worst column of ||b - A x|| / ||b|| with the oracle's float64 apply."""
+    r = np.asarray(b) - O.matmat(np.asarray(x))
+    return float(np.max(np.linalg.norm(r, axis=0) / np.linalg.norm(b, axis=0)))
 
 
 def _rhs(ops, counts, seed):
@@ -49,13 +70,14 @@ def _rhs(ops, counts, seed):
 def test_grouped_f64_equals_solo(compress):
     need_gpu()
     from sslablu_gb300.grouped import solve_grouped
-    ops = _operators(compress=compress)
+    ops, orcs = _operators(compress=compress, oracle=True)
     counts = [1, 3, 8, 16, 5, 2, 7]
     bs = _rhs(ops, counts, 1)
     xs = solve_grouped(list(zip(ops, bs)))
-    for H, b, x in zip(ops, bs, xs):
+    for H, O, b, x in zip(ops, orcs, bs, xs):
         assert x.shape == b.shape
         assert relerr(x, H.solve(b)) <= 1e-15
+        assert relerr(x, O.solve(b)) <= 1e-12
 
 
 def test_grouped_f64_repeated_members_and_edges():
@@ -63,7 +85,7 @@ def test_grouped_f64_repeated_members_and_edges():
     right-hand side, a member with no columns and an empty group."""
     need_gpu()
     from sslablu_gb300.grouped import solve_grouped
-    ops = _operators()
+    ops, orcs = _operators(oracle=True)
     group = []
     rng = np.random.default_rng(2)
     for rep in range(9):
@@ -74,24 +96,27 @@ def test_grouped_f64_repeated_members_and_edges():
     group.append((ops[1], np.zeros((ops[1].shape[0], 0))))           # no columns
     xs = solve_grouped(group)
     assert len(xs) == len(group)
+    twin = {id(H): O for H, O in zip(ops, orcs)}
     for (H, b), x in zip(group, xs):
         assert x.shape == b.shape
         if b.size:
             assert relerr(x, H.solve(b)) <= 1e-15
+            assert relerr(x, twin[id(H)].solve(b)) <= 1e-12
     assert solve_grouped([]) == []
 
 
 def test_grouped_mixed_refinement():
     need_gpu()
     from sslablu_gb300.grouped import solve_grouped
-    ops = _operators(compress=True)
+    ops, orcs = _operators(compress=True, oracle=True)
     counts = [4, 1, 16, 8, 3, 5, 2]
     bs = _rhs(ops, counts, 3)
     xs, iters, rr = solve_grouped(list(zip(ops, bs)), precision="mixed", tol=1e-10)
     assert 1 <= iters <= 10 and len(rr) == len(ops)
-    for H, b, x, r in zip(ops, bs, xs, rr):
+    for H, O, b, x, r in zip(ops, orcs, bs, xs, rr):
         assert r <= 1e-10
-        assert relerr(H.matmat(x), b) <= 1e-10
+        assert _oracle_residual(O, x, b) <= 1e-10
+        assert relerr(x, O.solve(b)) <= 1e-10
         solo, _, rs = H.solve_refined(b, tol=1e-10)
         assert rs <= 1e-10
         assert relerr(x, solo) < 1e-8
@@ -103,6 +128,7 @@ def test_per_level_solve_equals_grouped_for_uneven_ranks(k):
     per-level kernels (which switch to one-batch prefetching of the block
     matrices on small levels) agree with the grouped sweep to rounding."""
     need_gpu()
+    from oracle.hbs import OracleHBS
     from sslablu_gb300.grouped import solve_grouped
     from sslablu_gb300.matAssembly.HBS.HBSnew import HBSMAT
     from sslablu_gb300.synthetic import random_hbs_factors
@@ -112,10 +138,13 @@ def test_per_level_solve_equals_grouped_for_uneven_ranks(k):
                                             rng=np.random.default_rng(N + k), shift=16.0)
         H = HBSMAT().set_mats(U, D, V, list(Nbvec), fac=2)
         H.compute_ULV()
+        O = OracleHBS().set_mats(U, D, V, list(Nbvec), fac=2)
+        O.compute_ULV()
         b = np.random.default_rng(k).standard_normal((N, 8))
         x_solo = H.solve(b)
         x_grp = solve_grouped([(H, b)])[0]
-        assert relerr(H.matmat(x_grp), b) < 1e-12, (N, k)
+        assert _oracle_residual(O, x_grp, b) < 1e-12, (N, k)
+        assert relerr(x_grp, O.solve(b)) < 1e-12, (N, k)
         assert relerr(x_solo, x_grp) < 1e-13, (N, k)
 
 
