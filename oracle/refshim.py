@@ -71,7 +71,7 @@ def _install_pipeline_stubs():
 
 def import_pipeline():
     """Return the upstream slab pipeline modules (oms, stencil solver, pdo,
-    square geometry, assemblers) as a namespace."""
+    square and cube geometries, assemblers) as a namespace."""
     install()
     import contextlib
     import io
@@ -81,9 +81,10 @@ def import_pipeline():
         import solver.solver as solver
         import pdo.pdo as pdo
         import geometry.geom_2D.square as square
+        import geometry.geom_3D.cube as cube
         import matAssembly.matAssembler as matAssembler
         import matAssembly.HBS.slabTree as slabTree
-    return types.SimpleNamespace(oms=oms, solver=solver, pdo=pdo, square=square,
+    return types.SimpleNamespace(oms=oms, solver=solver, pdo=pdo, square=square, cube=cube,
                                  matAssembler=matAssembler, slabTree=slabTree)
 
 

@@ -19,6 +19,11 @@ the large outputs are stored.  Fixtures written (all small):
   c1_poisson64.npz   multislab.oms + stencil 2D Poisson, 8 slabs, 64-point
                      interfaces (the C1 layout at reduced size): S blocks, rhs
                      and the Thomas / red-black / functional-Thomas solutions
+  c1_poisson256.npz  the same at C1's 256-point interfaces: rhs, solutions and
+                     a fingerprint of the S blocks (regenerated by the oracle)
+  c3_helmholtz_small.npz  multislab.oms + 3-D stencil variable-coefficient
+                     Helmholtz (k = 20), 4 interfaces of 8 x 8 points: S blocks,
+                     rhs, Thomas / red-black solutions
   rbhbs_kernel.npz   RedBlackSolverHBS / ThomasSolverHBS on an exponential-
                      kernel block-tridiagonal system (truncation dominated)
   rbhbs_gauss.npz    the same on a Gaussian-kernel system that rank 16
@@ -167,6 +172,87 @@ def c1_poisson(ref, P):
     np.savez_compressed(os.path.join(HERE, "c1_poisson64.npz"),
                         Sl=Sl, Sr=Sr, rhs=rhs, x_th=x_th, x_rb=x_rb, x_f=x_f,
                         Stot_x=Stot @ x_th, nc=nc)
+
+
+def c1_poisson256(ref, P):
+    """The C1 layout at its full interface size: 8 slabs, 7 interfaces of
+    256 points (Ny = 258; Nx = 65 per double slab, hx = hy ~ 1/256).  The S
+    blocks are not stored (the oracle's closed form regenerates them; a
+    fingerprint pins it): rhs, the Thomas and padded red-black solutions."""
+    sq = P.square
+    nslabs, nx, ny = 8, 65, 258
+    slabs, conn, H = sq.dSlabs(nslabs)
+    gb = lambda p: sq.gb(p, jax_avail=False)
+    pdo = P.pdo.PDO2d(c11=P.pdo.const(1.0), c22=P.pdo.const(1.0))
+    opts = P.solver.solverOptions("stencil", [nx, ny])
+    O = P.oms.oms(slabs, pdo, gb, opts, conn)
+    bc = lambda p: np.sin(np.pi * p[:, 0]) * np.sinh(np.pi * p[:, 1])
+    import warnings
+    with contextlib.redirect_stdout(QUIET), warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        S, rhs_list, Ntot, nc = O.construct_Stot_helper(bc, P.matAssembler.denseMatAssembler())
+        Stot, rhs = O.construct_Stot_and_rhstot_linearOperator(S, rhs_list, Ntot, nc)
+    n = len(S)
+    T = [np.eye(nc) for _ in range(n)]
+    th = ref.omsdirectsolve.BlockTridiagonalSolver(nc)
+    th.factorize(S, T)
+    x_th = th.solve(rhs)
+    Sp = [[S[i][0] if i > 0 else np.zeros((nc, nc)), S[i][-1] if i < n - 1 else np.zeros((nc, nc))]
+          for i in range(n)] + [[np.zeros((nc, nc)), np.zeros((nc, nc))]]
+    with contextlib.redirect_stdout(QUIET):
+        rb = ref.omsdirectsolve.RedBlackSolver(nc)
+        rb.factorize(Sp, [np.eye(nc)] * (n + 1))
+        x_rb = rb.solve(np.concatenate([rhs, np.zeros(nc)]))
+    fp = np.stack([S[1][0][:8, :8], S[1][-1][:8, :8], S[1][0][-8:, -8:]])
+    norms = np.array([[np.linalg.norm(S[i][0]) if i > 0 else 0.0,
+                       np.linalg.norm(S[i][-1]) if i < n - 1 else 0.0] for i in range(n)])
+    np.savez_compressed(os.path.join(HERE, "c1_poisson256.npz"), rhs=rhs, x_th=x_th, x_rb=x_rb,
+                        Stot_x=Stot @ x_th, nc=nc, nx=nx, nslabs=nslabs, fingerprint=fp,
+                        norms=norms)
+
+
+def c3_helmholtz_small(ref, P):
+    """The C3 operator family at a size upstream solves in seconds: 3-D
+    variable-coefficient Helmholtz (Delta u + k^2 c(x) u, k = 20,
+    c = 1 + 0.5 sin(2 pi x) sin(2 pi y) sin(2 pi z)) on [0,1]^3 cut into 5
+    slabs (4 interfaces of 8 x 8 points: Ny = Nz = 10, Nx = 5 per double
+    slab), stencil discretisation, dense S blocks.  Stores the couplings,
+    rhs (Dirichlet data of a smooth field) and the Thomas / red-black
+    solutions."""
+    cube = P.cube
+    nslabs, nx, ny, nz, kappa = 5, 5, 10, 10, 20.0
+    slabs, conn, H = cube.dSlabs(nslabs)
+    gb = lambda p: cube.gb(p, jax_avail=False)
+    one = lambda p: np.ones_like(p[:, 0])
+    cfun = lambda p: kappa ** 2 * (1.0 + 0.5 * np.sin(2 * np.pi * p[:, 0]) *
+                                   np.sin(2 * np.pi * p[:, 1]) * np.sin(2 * np.pi * p[:, 2]))
+    pdo = P.pdo.PDO3d(c11=one, c22=one, c33=one, c=cfun)
+    opts = P.solver.solverOptions("stencil", [nx, ny, nz])
+    O = P.oms.oms(slabs, pdo, gb, opts, conn)
+    bc = lambda p: np.sin(np.pi * p[:, 0] + 0.3) * np.cos(2 * p[:, 1]) * np.cosh(p[:, 2])
+    import warnings
+    with contextlib.redirect_stdout(QUIET), warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        S, rhs_list, Ntot, nc = O.construct_Stot_helper(bc, P.matAssembler.denseMatAssembler())
+        Stot, rhs = O.construct_Stot_and_rhstot_linearOperator(S, rhs_list, Ntot, nc)
+    n = len(S)
+    Sl = np.zeros((n, nc, nc))
+    Sr = np.zeros((n, nc, nc))
+    for i, row in enumerate(S):
+        if i > 0:
+            Sl[i] = row[0]
+        if i < n - 1:
+            Sr[i] = row[-1]
+    th = ref.omsdirectsolve.BlockTridiagonalSolver(nc)
+    th.factorize(S, [np.eye(nc) for _ in range(n)])
+    x_th = th.solve(rhs)
+    with contextlib.redirect_stdout(QUIET):
+        rb = ref.omsdirectsolve.RedBlackSolver(nc)
+        rb.factorize([[Sl[i], Sr[i]] for i in range(n)], [np.eye(nc)] * n)
+        x_rb = rb.solve(rhs)
+    np.savez_compressed(os.path.join(HERE, "c3_helmholtz_small.npz"), Sl=Sl, Sr=Sr, rhs=rhs,
+                        x_th=x_th, x_rb=x_rb, Stot_x=Stot @ x_th, nc=nc, nx=nx, ny=ny, nz=nz,
+                        nslabs=nslabs, kappa=kappa)
 
 
 def kernel_system(m=64, nS=4):
@@ -401,6 +487,8 @@ def main():
     sig = 10.0 ** (-12.0 * np.arange(32) / 31.0)
     hbs_case(ref, "hbs_c2_n512", 32, 64, 4, False, 103, sigma=sig, nrhs=4, store_factors=False)
     c1_poisson(ref, P)
+    c1_poisson256(ref, P)
+    c3_helmholtz_small(ref, P)
     rbhbs(ref)
     rbhbs_gauss(ref)
     slab_trees(ref)

@@ -56,6 +56,45 @@ def test_c1_poisson(golden):
     assert relerr(xr, g["x_rb"]) < 1e-12
 
 
+def test_c1_poisson_full_interfaces(golden):
+    """C1 at its full size (7 interfaces of 256 points): couplings from the
+    oracle's closed form of upstream's stencil slab maps (pinned against
+    upstream by tests/test_oracle_golden.py), Thomas and padded red-black
+    solutions against upstream's own solvers' outputs."""
+    need_gpu()
+    from oracle.slabmaps import poisson2d_couplings
+    from sslablu_gb300.direct_solve.omsdirectsolve import BlockTridiagonalSolver, RedBlackSolver
+    g = golden("c1_poisson256")
+    nc, n = int(g["nc"]), int(g["nslabs"]) - 1
+    C = poisson2d_couplings(nc, n + 1, int(g["nx"]))
+    S = [[C[0][1]]] + [[C[i][0], C[i][1]] for i in range(1, n - 1)] + [[C[n - 1][0]]]
+    th = BlockTridiagonalSolver(nc)
+    th.factorize(S, [np.eye(nc)] * n)
+    assert relerr(th.solve(g["rhs"]), g["x_th"]) < 1e-12
+    Sp = [[C[i][0], C[i][1]] for i in range(n)] + [[np.zeros((nc, nc))] * 2]
+    rb = RedBlackSolver(nc)
+    rb.factorize(Sp, [np.eye(nc)] * (n + 1))
+    xr = rb.solve(np.concatenate([g["rhs"], np.zeros(nc)]))
+    assert relerr(xr, g["x_rb"]) < 1e-12
+
+
+def test_c3_helmholtz_small(golden):
+    """3-D variable-coefficient Helmholtz couplings (k = 20) from upstream's
+    stencil pipeline: the GPU Thomas and red-black solvers against upstream's
+    solutions of the same system."""
+    need_gpu()
+    from sslablu_gb300.direct_solve.omsdirectsolve import BlockTridiagonalSolver, RedBlackSolver
+    g = golden("c3_helmholtz_small")
+    n, nc = g["Sl"].shape[0], int(g["nc"])
+    S = [[g["Sr"][0]]] + [[g["Sl"][i], g["Sr"][i]] for i in range(1, n - 1)] + [[g["Sl"][n - 1]]]
+    th = BlockTridiagonalSolver(nc)
+    th.factorize(S, [np.eye(nc)] * n)
+    assert relerr(th.solve(g["rhs"]), g["x_th"]) < 1e-12
+    rb = RedBlackSolver(nc)
+    rb.factorize([[g["Sl"][i], g["Sr"][i]] for i in range(n)], [np.eye(nc)] * n)
+    assert relerr(rb.solve(g["rhs"]), g["x_rb"]) < 1e-12
+
+
 def test_rb_non_power_of_two_raises():
     need_gpu()
     from sslablu_gb300.direct_solve.omsdirectsolve import RedBlackSolver

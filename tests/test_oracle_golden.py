@@ -220,3 +220,56 @@ def test_oracle_hbstorch_rule_matches_upstream(golden):
     O2 = oh.OracleHBS(A, perm, 16, 5, 2)
     O2.compress_from_sketches(k, Om[perm], Psi[perm], (A @ Om)[perm], (A.T @ Psi)[perm])
     assert relerr(O2.matmat(x), g["Ax"]) > 1e-8
+
+
+def test_poisson2d_slab_maps_match_upstream(golden):
+    """The DST closed form of the 2-D stencil slab maps (oracle/slabmaps.py)
+    against upstream's own maps: the 64-point C1-layout blocks entry by
+    entry, and at C1's full 256-point interfaces a stored fingerprint, the
+    block norms and the interface operator's action on upstream's solution."""
+    from oracle.slabmaps import poisson2d_couplings
+    g = golden("c1_poisson64")
+    S = poisson2d_couplings(64, 8, 17)
+    for i in range(7):
+        assert np.abs(S[i][0] - g["Sl"][i]).max() < 1e-15
+        assert np.abs(S[i][1] - g["Sr"][i]).max() < 1e-15
+    g = golden("c1_poisson256")
+    m = int(g["nc"])
+    S = poisson2d_couplings(m, int(g["nslabs"]), int(g["nx"]))
+    fp = g["fingerprint"]
+    assert np.abs(S[1][0][:8, :8] - fp[0]).max() < 1e-15
+    assert np.abs(S[1][1][:8, :8] - fp[1]).max() < 1e-15
+    assert np.abs(S[1][0][-8:, -8:] - fp[2]).max() < 1e-15
+    norms = np.array([[np.linalg.norm(a), np.linalg.norm(b)] for a, b in S])
+    assert np.abs(norms - g["norms"]).max() < 1e-13
+    x = g["x_th"]
+    n = len(S)
+    Sx = x.copy()
+    for i in range(n):
+        if i > 0:
+            Sx[i * m:(i + 1) * m] += S[i][0] @ x[(i - 1) * m:i * m]
+        if i < n - 1:
+            Sx[i * m:(i + 1) * m] += S[i][1] @ x[(i + 1) * m:(i + 2) * m]
+    assert relerr(Sx, g["Stot_x"]) < 1e-13
+
+
+def test_helmholtz3d_slab_maps_match_upstream(golden):
+    """The 3-D variable-coefficient Helmholtz slab maps (7-point stencil,
+    sparse LU of the slab interior) against upstream's oms + stencil solver
+    on 4 interfaces of 8 x 8 points; the sampled form (one sparse solve per
+    sketch, both orientations) against the dense maps."""
+    from oracle.slabmaps import helmholtz3d_sample, helmholtz3d_slab_maps
+    g = golden("c3_helmholtz_small")
+    ns = int(g["nslabs"])
+    H = 1.0 / ns
+    geo = (int(g["nx"]), int(g["ny"]), int(g["nz"]), 2 * H, float(g["kappa"]))
+    for i in range(ns - 1):
+        L, R = helmholtz3d_slab_maps(*geo, x0=(i + 1) * H - H)
+        if i > 0:
+            assert np.abs(L - g["Sl"][i]).max() < 1e-11 * np.abs(g["Sl"][i]).max()
+        if i < ns - 2:
+            assert np.abs(R - g["Sr"][i]).max() < 1e-11 * np.abs(g["Sr"][i]).max()
+    Om = np.random.default_rng(0).standard_normal((L.shape[0], 5))
+    x0 = (ns - 1) * H - H
+    assert relerr(helmholtz3d_sample(*geo, x0, Om, 0), L @ Om) < 1e-13
+    assert relerr(helmholtz3d_sample(*geo, x0, Om, 1, trans=True), R.T @ Om) < 1e-13
