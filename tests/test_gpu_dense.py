@@ -80,19 +80,33 @@ def test_c1_poisson_full_interfaces(golden):
 
 def test_c3_helmholtz_small(golden):
     """3-D variable-coefficient Helmholtz couplings (k = 20) from upstream's
-    stencil pipeline: the GPU Thomas and red-black solvers against upstream's
-    solutions of the same system."""
+    stencil pipeline: the GPU Thomas and red-black solvers on the same
+    system.  At this coarse grid k = 20 is near a resonance of the interface
+    system (condition number ~1.3e6): upstream's own Thomas and red-black
+    solutions differ by 5.4e-10 and leave residuals of 1.3e-10 and 8.9e-10,
+    so the bar is conditioning-aware -- each GPU solution within 2e-9 of
+    the dense LAPACK solution and of upstream's, with a residual below 2e-9
+    (within 2x of what upstream reaches)."""
     need_gpu()
     from sslablu_gb300.direct_solve.omsdirectsolve import BlockTridiagonalSolver, RedBlackSolver
     g = golden("c3_helmholtz_small")
     n, nc = g["Sl"].shape[0], int(g["nc"])
+    M = np.eye(n * nc)
+    for i in range(n):
+        if i > 0:
+            M[i * nc:(i + 1) * nc, (i - 1) * nc:i * nc] = g["Sl"][i]
+        if i < n - 1:
+            M[i * nc:(i + 1) * nc, (i + 1) * nc:(i + 2) * nc] = g["Sr"][i]
+    xd = np.linalg.solve(M, g["rhs"])
     S = [[g["Sr"][0]]] + [[g["Sl"][i], g["Sr"][i]] for i in range(1, n - 1)] + [[g["Sl"][n - 1]]]
     th = BlockTridiagonalSolver(nc)
     th.factorize(S, [np.eye(nc)] * n)
-    assert relerr(th.solve(g["rhs"]), g["x_th"]) < 1e-12
     rb = RedBlackSolver(nc)
     rb.factorize([[g["Sl"][i], g["Sr"][i]] for i in range(n)], [np.eye(nc)] * n)
-    assert relerr(rb.solve(g["rhs"]), g["x_rb"]) < 1e-12
+    for x, ref in ((th.solve(g["rhs"]), g["x_th"]), (rb.solve(g["rhs"]), g["x_rb"])):
+        assert relerr(M @ x, g["rhs"]) < 2e-9
+        assert relerr(x, xd) < 2e-9
+        assert relerr(x, ref) < 2e-9
 
 
 def test_rb_non_power_of_two_raises():
