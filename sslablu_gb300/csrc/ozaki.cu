@@ -38,14 +38,14 @@
 // pipe; only a float64 input is split and a float64 output assembled.
 //
 // Kernel (one CTA per block, row tile of NT <= 64 operator rows and 128
-// right-hand-side columns; 8 digitiser warps + 1 MMA warp, one CTA per SM):
+// right-hand-side columns; 16 digitiser warps + 1 MMA warp, one CTA per SM):
 //   1. one bulk copy (cp.async.bulk, mbarrier complete_tx) brings the seven
 //      operator digit images, stored in global memory already in the
 //      core-matrix order the MMA reads (8 x 8 bf16 tiles of 128 bytes,
 //      K-major, no swizzle), before the wait for the previous launch;
 //   2. griddepcontrol.wait (programmatic dependent launch); the digitiser
-//      warps find each column's largest magnitude (two threads per column,
-//      16 loads in flight each), then digitise z chunk by chunk (32 k) into
+//      warps find each column's largest magnitude (four threads per column,
+//      8 loads in flight each), then digitise z chunk by chunk (32 k) into
 //      two chunk buffers of seven 128 x 32 digit images;
 //   3. the MMA warp issues tcgen05.mma.kind::f16 (M = 128 columns, N = NT
 //      rows, K = 16) for the 28 digit pairs of each chunk into seven TMEM
@@ -53,7 +53,8 @@
 //      the buffer back with tcgen05.commit: chunk c + 1 is digitised while
 //      the tensor cores work on chunk c;
 //   4. the digitiser warps read the accumulators (tcgen05.ld), combine,
-//      scale and store (one thread per column: coalesced rows).
+//      scale and store (one thread per column: coalesced rows); float64
+//      outputs are assembled from the float32 pair with integer operations.
 // Every mbarrier wait is bounded (2^22 polls); on a timeout the kernel sets
 // the handle's device error word, waits (bounded) for its own copies, frees
 // its TMEM and returns.
@@ -70,7 +71,7 @@ constexpr int kM = 128;           // right-hand-side columns per CTA (MMA M)
 constexpr int kMaxW = 96;         // widest step whose diagonal sums stay exact in float32
 constexpr int kMaxNT = 64;        // operator rows per CTA (MMA N)
 constexpr int kKC = 32;           // k per digitised chunk of z (two chunk buffers)
-constexpr int kDigWarps = 8;      // digitise z, then the epilogue
+constexpr int kDigWarps = 16;     // digitise z, then the epilogue
 constexpr int kThreads = 32 * (kDigWarps + 1);   // + one MMA warp
 constexpr long long kWaitLimit = 1LL << 22;
 
@@ -169,13 +170,11 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
           smem_u32(bar))
       : "memory");
 }
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
-        "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        "=r"(r[7])
       : "r"(taddr));
 }
 
@@ -220,8 +219,6 @@ __device__ __forceinline__ void f64_split(double x, int sh, float& h, float& l) 
                            : 0.f;
   l = sgn ? -lo : lo;
 }
-// bfloat16 bits of a float32 with at most 8 significant bits (exact).
-__device__ __forceinline__ uint32_t bf_bits(float q) { return __float_as_uint(q) >> 16; }
 
 // The seven digit diagonals a_0..a_6 summed with no rounding error, as four
 // float32 terms v = h + l + e + f.  After the row and column scaling every
@@ -261,10 +258,38 @@ __device__ __forceinline__ void diag_pair(const DiagSum& d, float& H, float& Lo)
   two_sum(s, d.e, s, t2);
   two_sum(s, __fadd_rn(__fadd_rn(t, t2), d.f), H, Lo);
 }
-// v in float64 (outputs to the caller): h + l and e + f are exact in float64
-// (spans of at most 47 and 40 bits), one rounding in the last addition.
-__device__ __forceinline__ double diag_double(const DiagSum& d) {
-  return ((double)d.h + (double)d.l) + ((double)d.e + (double)d.f);
+// (H + Lo) 2^sh as a float64, from the bits with integer operations only
+// (GB300's float64 pipe runs at 1/64 of the float32 rate).  With
+// |Lo| <= ulp(H) / 2 the sum has H's exponent (or one less) and its
+// significand is H's 24 bits followed by Lo's bits, rounded at 2^-52 of H
+// (to nearest, ties up): error <= 2^-53 relative, as a float64 addition.
+// Results below float64's normal range flush to zero (the caller's values
+// are normalised per column, so these are ~2^-1000 of the column's largest).
+__device__ __forceinline__ double pair_to_f64(float H, float Lo, int sh) {
+  const unsigned hb = __float_as_uint(H);
+  const int eh = (int)((hb >> 23) & 255);
+  if (eh == 0) return 0.0;   // zero, or a float32 subnormal (< 2^-126 of the column scale)
+  long long M = (long long)((hb & 0x7FFFFFu) | 0x800000u) << 29;   // 2^52 <= M < 2^53
+  const unsigned lb = __float_as_uint(Lo);
+  const int el = (int)((lb >> 23) & 255);
+  if (el != 0) {
+    const long long ml = (long long)((lb & 0x7FFFFFu) | 0x800000u);
+    const int d = eh - el;   // >= 24
+    long long add = 0;
+    if (d <= 29) add = ml << (29 - d);
+    else if (d < 54) add = (ml + (1LL << (d - 30))) >> (d - 29);
+    M += ((hb ^ lb) >> 31) ? -add : add;
+  }
+  int e = eh - 127 + 1023 + sh;   // biased float64 exponent
+  if (M < (1LL << 52)) {
+    M <<= 1;
+    e -= 1;
+  }
+  const unsigned long long sgn = (unsigned long long)(hb >> 31) << 63;
+  if (e <= 0) return __longlong_as_double((long long)sgn);
+  if (e >= 2047) return __longlong_as_double((long long)(sgn | 0x7FF0000000000000ull));
+  return __longlong_as_double(
+      (long long)(sgn | ((unsigned long long)e << 52) | ((unsigned long long)M & 0xFFFFFFFFFFFFFull)));
 }
 
 // ---------------------------------------------------------------- the kernel
@@ -279,7 +304,7 @@ __global__ void __launch_bounds__(kThreads, 1) oz_step_kernel(const OzStep o) {
   __shared__ char* outp[kMaxNT];
   __shared__ int outf64[kMaxNT];
   __shared__ float rs[kMaxNT];
-  __shared__ float colmax[2][kM];
+  __shared__ float colmax[kDigWarps / 4][kM];
 
   const sweep::Step<dfloat>& s = o.s;
   const int NT = o.NT, wP = o.wP, w = s.w;
@@ -411,9 +436,9 @@ __global__ void __launch_bounds__(kThreads, 1) oz_step_kernel(const OzStep o) {
     }
     __syncwarp();
   } else {
-    // ---------------- digitiser warps (256 threads): thread (j, half) owns
-    // column j and the k of each chunk's half `half` (16 k)
-    const int j = tid & (kM - 1), half = tid >> 7;
+    // ---------------- digitiser warps (512 threads): thread (j, qk) owns
+    // column j and the k of each chunk's quarter qk (8 k: one core-matrix row)
+    const int j = tid & (kM - 1), qk = tid >> 7;
     const bool col_ok = c0 + j < s.c;
     const int csh = (o.colbits && col_ok) ? col_shift(__ldg(o.colbits + c0 + j)) : 0;
     auto load = [&](int k, float& h, float& l) {
@@ -430,22 +455,22 @@ __global__ void __launch_bounds__(kThreads, 1) oz_step_kernel(const OzStep o) {
         }
       }
     };
-    // column scale: largest |h| over the column's k (16 loads in flight)
+    // column scale: largest |h| over the column's k (8 loads in flight)
     float mx = 0.f;
     for (int c = 0; c < nch; ++c) {
-      const int k0 = c * kKC + half * 16;
+      const int k0 = c * kKC + qk * 8;
       if (k0 >= wP) continue;
-      float hv[16], lv[16];
+      float hv[8], lv[8];
 #pragma unroll
-      for (int u = 0; u < 16; ++u) load(k0 + u, hv[u], lv[u]);
+      for (int u = 0; u < 8; ++u) load(k0 + u, hv[u], lv[u]);
 #pragma unroll
-      for (int u = 0; u < 16; ++u) mx = fmaxf(mx, fabsf(hv[u]));
+      for (int u = 0; u < 8; ++u) mx = fmaxf(mx, fabsf(hv[u]));
     }
-    colmax[half][j] = mx;
+    colmax[qk][j] = mx;
     asm volatile("bar.sync 1, %0;" ::"r"(kDigWarps * 32) : "memory");
     float inv = 1.f, cs = 0.f;   // 2^-F and 2^F of the column (0: zero column)
     {
-      const float m = fmaxf(colmax[0][j], colmax[1][j]);
+      const float m = fmaxf(fmaxf(colmax[0][j], colmax[1][j]), fmaxf(colmax[2][j], colmax[3][j]));
       if (m > 0.f) {
         int F = (int)((__float_as_uint(m) >> 23) & 255) - 126;   // m < 2^F
         F = max(-100, min(100, F));
@@ -457,17 +482,16 @@ __global__ void __launch_bounds__(kThreads, 1) oz_step_kernel(const OzStep o) {
     for (int c = 0; c < nch; ++c) {
       const int b2 = c & 1;
       if (c >= 2 && !mbar_wait(&zempty[b2], (uint32_t)((c >> 1) - 1) & 1u)) fail = true;
-      const int k0 = c * kKC + half * 16;
+      const int k0 = c * kKC + qk * 8;
       if (k0 < wP) {
-        float hv[16], lv[16];
+        float hv[8], lv[8];
 #pragma unroll
-        for (int u = 0; u < 16; ++u) load(k0 + u, hv[u], lv[u]);
-#pragma unroll
-        for (int g = 0; g < 2; ++g) {
+        for (int u = 0; u < 8; ++u) load(k0 + u, hv[u], lv[u]);
+        {
           uint32_t wd[kDig][4];
 #pragma unroll
           for (int u = 0; u < 8; ++u) {
-            float hs = __fmul_rn(hv[8 * g + u], inv), ls = __fmul_rn(lv[8 * g + u], inv);
+            float hs = __fmul_rn(hv[u], inv), ls = __fmul_rn(lv[u], inv);
             float q[kDig];
             q[0] = extract(hs, 0x1.8p15f);
             hs = __fsub_rn(hs, q[0]);
@@ -486,16 +510,20 @@ __global__ void __launch_bounds__(kThreads, 1) oz_step_kernel(const OzStep o) {
             q[5] = extract(a2, 0x1.8p-25f);
             a2 = __fsub_rn(a2, q[5]);
             q[6] = extract(__fadd_rn(a2, e2), 0x1.8p-33f);
+            // two bfloat16 halves per word: the high halves of the float32
+            // digits of k = u - 1 and u (one byte permute per pair)
+            if (u & 1) {
 #pragma unroll
-            for (int t = 0; t < kDig; ++t) {
-              const uint32_t bits = bf_bits(q[t]);
-              if (u & 1) wd[t][u >> 1] |= bits << 16;
-              else wd[t][u >> 1] = bits;
+              for (int t = 0; t < kDig; ++t)
+                wd[t][u >> 1] = __byte_perm(wd[t][u >> 1], __float_as_uint(q[t]), 0x7632);
+            } else {
+#pragma unroll
+              for (int t = 0; t < kDig; ++t) wd[t][u >> 1] = __float_as_uint(q[t]);
             }
           }
-          // 16-byte row (8 k) of column j in core matrix (j / 8, half * 2 + g)
-          const uint32_t off = (uint32_t)(j >> 3) * (kKC * 16) +
-                               (uint32_t)(half * 2 + g) * 128 + (uint32_t)(j & 7) * 16;
+          // 16-byte row (8 k) of column j in core matrix (j / 8, qk)
+          const uint32_t off = (uint32_t)(j >> 3) * (kKC * 16) + (uint32_t)qk * 128 +
+                               (uint32_t)(j & 7) * 16;
           unsigned char* zb = zbuf + b2 * zdb + off;
 #pragma unroll
           for (int t = 0; t < kDig; ++t)
@@ -514,43 +542,42 @@ __global__ void __launch_bounds__(kThreads, 1) oz_step_kernel(const OzStep o) {
       if (o.err) atomicOr(o.err, 1u);
     }
 
-    // ---------------- epilogue: warp (qd, half) reads TMEM lanes 32 qd ..
-    // (its columns) and rows half * 16 + 32 i of the tile
+    // ---------------- epilogue: warp (qd, rq) reads TMEM lanes 32 qd ..
+    // (its columns) and rows rq * 8 + 32 i of the tile
     const bool ok = mbar_wait(&done_bar, 0);
     __syncwarp();
     const bool all_ok = __all_sync(0xffffffffu, ok) && !s_fail;
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (all_ok) {
-      const int qd = warp & 3, rhalf = warp >> 2;
+      const int qd = warp & 3, rq = warp >> 2;
       const int col = qd * 32 + lane;
       const bool cok = c0 + col < s.c;
-      // float64 outputs leave scaled back by 2^s_col (exactly, in float64)
+      // float64 outputs leave scaled back by 2^s_col
       const int osh = (o.colbits && cok) ? col_shift(__ldg(o.colbits + c0 + col)) : 0;
-      const double oscale = __longlong_as_double((long long)(1023 + osh) << 52);
       const uint32_t lanes = (uint32_t)(qd * 32) << 16;
       // col == tid % 128: this thread digitised column col, so cs is its scale
       const float csc = cs;
-      for (int r16 = rhalf * 16; r16 < NT; r16 += 32) {
-        uint32_t v[kDig][16];
+      for (int r8 = rq * 8; r8 < NT; r8 += 32) {
+        uint32_t v[kDig][8];
 #pragma unroll
         for (int di = 0; di < kDig; ++di)
-          tmem_ld16(tmem + lanes + (uint32_t)(di * NT + r16), v[di]);
+          tmem_ld8(tmem + lanes + (uint32_t)(di * NT + r8), v[di]);
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-        for (int i = 0; i < 16; ++i) {
-          const int row = r16 + i;
+        for (int i = 0; i < 8; ++i) {
+          const int row = r8 + i;
           if (row >= nr || !cok) continue;
           float a[kDig];
 #pragma unroll
           for (int di = 0; di < kDig; ++di) a[di] = __uint_as_float(v[di][i]);
-          const DiagSum ds = diag_sum(a);
-          const float g = __fmul_rn(rs[row], csc);
+          float H, Lo;
+          diag_pair(diag_sum(a), H, Lo);
+          const float g = __fmul_rn(rs[row], csc);   // a power of two, or 0
           char* p = outp[row] + 8 * col;
           if (outf64[row]) {
-            *reinterpret_cast<double*>(p) = diag_double(ds) * ((double)g * oscale);
+            const int ge = (int)((__float_as_uint(g) >> 23) & 255);
+            *reinterpret_cast<double*>(p) = ge ? pair_to_f64(H, Lo, ge - 127 + osh) : 0.0;
           } else {
-            float H, Lo;
-            diag_pair(ds, H, Lo);
             *reinterpret_cast<float2*>(p) = make_float2(__fmul_rn(H, g), __fmul_rn(Lo, g));
           }
         }
