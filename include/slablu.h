@@ -342,6 +342,13 @@ int slu_rb_factor(slu_handle_t h, int nblk, int m, const double* SiM, const doub
                   const double* T, slu_rb_t* out);
 /* B (nblk*m x nrhs, ldb) <- solution, in place. */
 int slu_rb_solve(slu_handle_t h, slu_rb_t rb, double* B, int ldb, int nrhs);
+/* Periodic red-black (RedBlackSolver with cyclic=True,
+ * direct_solve/omsdirectsolve.py:207-209, 249-250, 269-272, 315-327): as
+ * slu_rb_factor, with SiM[0] coupling block 0 to block nblk-1 and
+ * SiP[nblk-1] coupling the last block to block 0; nblk a power of two >= 2.
+ * Solve with slu_rb_solve (and slu_rb_refine). */
+int slu_rb_factor_cyclic(slu_handle_t h, int nblk, int m, const double* SiM, const double* SiP,
+                         const double* T, slu_rb_t* out);
 /* Mixed-precision variant of slu_rb_factor: the Schur-complement products of
  * every level (SiM_i T^{-1} [SiM|SiP], omsdirectsolve.py:316-324) run on the
  * tcgen05 tensor cores (slu_gemm_split3); pivot-block LU factors and solves
@@ -356,6 +363,27 @@ int slu_rb_factor_mixed(slu_handle_t h, int nblk, int m, const double* SiM, cons
 int slu_rb_refine(slu_handle_t h, slu_rb_t rb, const double* B, int ldb, double* X, int ldx,
                   int nrhs, double tol, int maxit, int* iters_out, double* relres_out);
 int slu_rb_destroy(slu_rb_t rb);
+
+/* Slab source-target maps of the stencil discretisation, applied through
+ * solves of the slab interiors (multislab/oms.py:96-125, oms.compute_stmaps:
+ * S_J g = (A_ii^{-1} A_ib[:, J] g)[Ic]; the operators rkHBS assembly samples,
+ * matAssembly/matAssembler.py:112-117).  nslabs double slabs
+ * [x0[s], x0[s] + width] x [0,1] (nz = 0) or x [0,1]^2, each with nx grid
+ * points across (odd) and ny (nz) along y (z), stencil of
+ * solver/stencil/stencilSolver.py (c11 = c22 = c33 = 1, zeroth-order term
+ * kappa^2 c(x); coef 0: c = 1, coef 1: c = 1 + 0.5 sin 2pi x sin 2pi y
+ * sin 2pi z).  Interface vectors have m = (ny-2)(nz-2) rows per slab (z
+ * fastest; m = ny-2 in 2-D), slab s at rows s*m .. s*m+m-1, ncols columns
+ * (leading dimensions ldx / ldy), device float64.
+ *   trans = 0: YL_s = S_l(s) XL_s + S_r(s) XR_s (XL or XR may be NULL);
+ *   trans = 1: YL_s = S_l(s)^T XL_s, YR_s = S_r(s)^T XL_s (either output NULL).
+ * The interior solves are Chebyshev iterations on -A_ii with the step count
+ * fixed by its spectral bounds for relative accuracy tol (*steps_out);
+ * SLU_ERR_ARG when -A_ii is not definite (slab too wide for kappa). */
+int slu_slab_maps_apply(slu_handle_t h, int nx, int ny, int nz, double width, double kappa,
+                        int coef, int nslabs, const double* x0, const double* XL,
+                        const double* XR, int ldx, double* YL, double* YR, int ldy, int ncols,
+                        int trans, double tol, int* steps_out);
 
 /* Dense block Thomas (direct_solve/omsdirectsolve.py:48-141,
  * BlockTridiagonalSolver.factorize_helper / solve_helper) with the same block
