@@ -636,6 +636,17 @@ int slu_rb_factor(slu_handle_t h, int nblk, int m, const double* SiM, const doub
   });
 }
 
+int slu_rb_factor_cyclic(slu_handle_t h, int nblk, int m, const double* SiM, const double* SiP,
+                         const double* T, slu_rb_t* out) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h && SiM && SiP && T && out, "null argument");
+    SLU_REQUIRE(nblk >= 2, "a periodic red-black system needs at least two blocks");
+    auto p = std::make_unique<slu_dense_rb_s>();
+    slu::rb_factor(h->h, p->S, nblk, m, SiM, SiP, T, false, true);
+    *out = p.release();
+  });
+}
+
 int slu_rb_factor_mixed(slu_handle_t h, int nblk, int m, const double* SiM, const double* SiP,
                         const double* T, slu_rb_t* out) {
   return guard(h, [&] {

@@ -12,6 +12,12 @@
 //   G1 = SiM_i [T_{i-1}^{-1} SiM_{i-1} | T_{i-1}^{-1} SiP_{i-1}]
 //   G2 = SiP_i [T_{i+1}^{-1} SiM_{i+1} | T_{i+1}^{-1} SiP_{i+1}]
 //   A_i = -G1[:, :m],  B_i = T_i - G1[:, m:] - G2[:, :m],  C_i = -G2[:, m:].
+// Periodic systems (cyclic = true, omsdirectsolve.py:207-209, 249-250,
+// 269-272, 315-327) keep SiM_0 and SiP_{n-1} as the couplings to the last and
+// first block: block 0's left neighbour is the last odd block at every level,
+// the last kept block's right neighbour wraps to block 0 in the back
+// substitution, and when a level reduces to one block its couplings to
+// itself are folded into the diagonal (B_0 += A_0 + C_0).
 // Upstream rebuilds each T from its LU factors (omsdirectsolve.py:31-46,314);
 // this keeps T itself, the same matrix up to rounding.  The solve phase
 // applies the pivot-block inverses (formed once from the LU factors) as
@@ -173,13 +179,15 @@ void rb_solve_fused(Handle& h, const RbSolver& S, double* B, int ldb, int c) {
 }  // namespace
 
 void rb_factor(Handle& h, RbSolver& S, int nblk, int m, const double* SiM, const double* SiP,
-               const double* T, bool mixed) {
+               const double* T, bool mixed, bool cyclic) {
   cudaStream_t st = h.stream;
   SLU_REQUIRE(nblk >= 1 && (nblk & (nblk - 1)) == 0, "red-black needs a power-of-two block count");
   SLU_REQUIRE(m >= 1, "bad block size");
   S.m = m;
   S.nblk = nblk;
   S.mixed = mixed;
+  S.cyclic = cyclic;
+  SLU_REQUIRE(!(cyclic && mixed), "the periodic red-black factorisation is float64 only");
   DevBuf tcws;
   if (mixed) tcws.alloc(tc_gemm_workspace_bytes(m, 2 * m, m), st);
   S.levels.clear();
@@ -196,8 +204,10 @@ void rb_factor(Handle& h, RbSolver& S, int nblk, int m, const double* SiM, const
     L0.piv.alloc(4 * (size_t)nblk * m, st);
     SLU_CHECK_CUDA(cudaMemcpyAsync(dp(L0.SiM), SiM, 8 * nblk * mm, cudaMemcpyDeviceToDevice, st));
     SLU_CHECK_CUDA(cudaMemcpyAsync(dp(L0.SiP), SiP, 8 * nblk * mm, cudaMemcpyDeviceToDevice, st));
-    SLU_CHECK_CUDA(cudaMemsetAsync(dp(L0.SiM), 0, 8 * mm, st));
-    SLU_CHECK_CUDA(cudaMemsetAsync(dp(L0.SiP) + (nblk - 1) * mm, 0, 8 * mm, st));
+    if (!cyclic) {
+      SLU_CHECK_CUDA(cudaMemsetAsync(dp(L0.SiM), 0, 8 * mm, st));
+      SLU_CHECK_CUDA(cudaMemsetAsync(dp(L0.SiP) + (nblk - 1) * mm, 0, 8 * mm, st));
+    }
     SLU_CHECK_CUDA(cudaMemcpyAsync(dp(L0.T), T, 8 * nblk * mm, cudaMemcpyDeviceToDevice, st));
     SLU_CHECK_CUDA(cudaMemcpyAsync(dp(L0.LU), T, 8 * nblk * mm, cudaMemcpyDeviceToDevice, st));
     lu_factor(st, m, dp(L0.LU), m, mm, ip(L0.piv), m, nblk, h.info.as<int>());
@@ -244,7 +254,14 @@ void rb_factor(Handle& h, RbSolver& S, int nblk, int m, const double* SiM, const
         tc_gemm_split3(st, m, (int)m2, m, 1.0, dp(P.SiP) + 2 * j * mm, m, X + 2 * j * mm,
                        (int)m2, 0.0, G2 + 2 * j * mm, (int)m2, tcws.p, err);
     }
-    SLU_CHECK_CUDA(cudaMemsetAsync(G1, 0, 8 * 2 * mm, st));
+    if (cyclic) {
+      // block 0's left neighbour is the last odd block (index 2 nR - 1)
+      gemm_batched<double>(st, false, false, m, (int)m2, m, 1.0, dp(P.SiM), m, 0, 0,
+                           X + 2 * (size_t)(nR - 1) * mm, (int)m2, 0, 0, 0.0, G1, (int)m2, 0, 0,
+                           1);
+    } else {
+      SLU_CHECK_CUDA(cudaMemsetAsync(G1, 0, 8 * 2 * mm, st));
+    }
     // A = -G1[:, :m]; C = -G2[:, m:]; B = T_even - G1[:, m:] - G2[:, :m]
     copy_batched<double>(st, m, m, dp(P.T), m, 2 * mm, 0, dp(N.T), m, mm, 0, nR);
     add_batched<double>(st, m, m, -1.0, G1 + m, (int)m2, 2 * mm, 0, dp(N.T), m, mm, 0, nR);
@@ -253,6 +270,11 @@ void rb_factor(Handle& h, RbSolver& S, int nblk, int m, const double* SiM, const
     SLU_CHECK_CUDA(cudaMemsetAsync(dp(N.SiP), 0, 8 * nR * mm, st));
     add_batched<double>(st, m, m, -1.0, G1, (int)m2, 2 * mm, 0, dp(N.SiM), m, mm, 0, nR);
     add_batched<double>(st, m, m, -1.0, G2 + m, (int)m2, 2 * mm, 0, dp(N.SiP), m, mm, 0, nR);
+    if (cyclic && nR == 1) {
+      // one periodic block: its couplings act on itself (omsdirectsolve.py:326-327)
+      add_batched<double>(st, m, m, 1.0, dp(N.SiM), m, 0, 0, dp(N.T), m, 0, 0, 1);
+      add_batched<double>(st, m, m, 1.0, dp(N.SiP), m, 0, 0, dp(N.T), m, 0, 0, 1);
+    }
     SLU_CHECK_CUDA(cudaMemcpyAsync(dp(N.LU), dp(N.T), 8 * nR * mm, cudaMemcpyDeviceToDevice, st));
     lu_factor(st, m, dp(N.LU), m, mm, ip(N.piv), m, nR, h.info.as<int>());
     make_inverses(st, m, N.LU, N.piv, nR, N.Inv);
@@ -260,7 +282,7 @@ void rb_factor(Handle& h, RbSolver& S, int nblk, int m, const double* SiM, const
     l = nR;
   }
   S.fused = false;
-  if (m <= kRbFusedMax) build_fused_ops(st, S);
+  if (m <= kRbFusedMax && !cyclic) build_fused_ops(st, S);
 }
 
 void rb_solve(Handle& h, const RbSolver& S, double* B, int ldb, int c) {
@@ -294,6 +316,9 @@ void rb_solve(Handle& h, const RbSolver& S, double* B, int ldb, int c) {
                            mc, 0, 1.0, v[l + 1] + mc, c, mc, 0, nR - 1);
     gemm_batched<double>(st, false, false, m, c, m, -1.0, dp(P.SiP), m, 2 * mm, 0, z, c, mc, 0,
                          1.0, v[l + 1], c, mc, 0, nR);
+    if (S.cyclic)   // v'_0 -= SiM_0 z_{last odd}
+      gemm_batched<double>(st, false, false, m, c, m, -1.0, dp(P.SiM), m, 0, 0,
+                           z + (size_t)(nR - 1) * mc, c, 0, 0, 1.0, v[l + 1], c, 0, 0, 1);
   }
   // coarsest block (omsdirectsolve.py:261)
   gemm_batched<double>(st, false, false, m, c, m, 1.0, dp(S.levels[nL - 1].Inv), m, 0, 0,
@@ -310,6 +335,10 @@ void rb_solve(Handle& h, const RbSolver& S, double* B, int ldb, int c) {
     if (nR > 1)
       gemm_batched<double>(st, false, false, m, c, m, -1.0, dp(P.SiP) + mm, m, 2 * mm, 0,
                            v[l] + mc, c, mc, 0, 1.0, v[l - 1] + mc, c, 2 * mc, 0, nR - 1);
+    if (S.cyclic)   // the last odd block's right neighbour is block 0
+      gemm_batched<double>(st, false, false, m, c, m, -1.0,
+                           dp(P.SiP) + (2 * (size_t)nR - 1) * mm, m, 0, 0, v[l], c, 0, 0, 1.0,
+                           v[l - 1] + (2 * (size_t)nR - 1) * mc, c, 0, 0, 1);
     gemm_batched<double>(st, false, false, m, c, m, 1.0, dp(P.Inv) + mm, m, 2 * mm, 0,
                          v[l - 1] + mc, c, 2 * mc, 0, 0.0, z, c, mc, 0, nR);
     copy_batched<double>(st, m, c, z, c, mc, 0, v[l - 1] + mc, c, 2 * mc, 0, nR);
@@ -333,6 +362,12 @@ void rb_apply(Handle& h, const RbSolver& S, const double* X, int ldx, double* Y,
                          1.0, Y + by, ldy, by, 0, n - 1);
     gemm_batched<double>(st, false, false, m, c, m, 1.0, dp(L0.SiP), m, mm, 0, X + bx, ldx, bx, 0,
                          1.0, Y, ldy, by, 0, n - 1);
+  }
+  if (S.cyclic) {   // wrap-around couplings of a periodic system
+    gemm_batched<double>(st, false, false, m, c, m, 1.0, dp(L0.SiM), m, 0, 0,
+                         X + (long long)(n - 1) * bx, ldx, 0, 0, 1.0, Y, ldy, 0, 0, 1);
+    gemm_batched<double>(st, false, false, m, c, m, 1.0, dp(L0.SiP) + (size_t)(n - 1) * mm, m, 0,
+                         0, X, ldx, 0, 0, 1.0, Y + (long long)(n - 1) * by, ldy, 0, 0, 1);
   }
 }
 

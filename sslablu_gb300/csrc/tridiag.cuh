@@ -26,11 +26,12 @@ struct RbSolver {
   int m = 0, nblk = 0;
   bool mixed = false;              // Schur products on the tensor cores
   bool fused = false;              // levels carry Fop / Bop (m <= kRbFusedMax)
+  bool cyclic = false;             // periodic: SiM[0] couples to the last block, SiP[-1] to the first
   std::vector<RbLevel> levels;     // levels[0] = the input system
 };
 
 void rb_factor(Handle& h, RbSolver& S, int nblk, int m, const double* SiM, const double* SiP,
-               const double* T, bool mixed = false);
+               const double* T, bool mixed = false, bool cyclic = false);
 // Y = A X for the stored input system (level 0), X and Y nblk*m x nrhs.
 void rb_apply(Handle& h, const RbSolver& S, const double* X, int ldx, double* Y, int ldy,
               int nrhs);

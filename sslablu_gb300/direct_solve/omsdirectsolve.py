@@ -56,16 +56,17 @@ def _dense_block(B, m):
     return dv.to_dev(np.asarray(B @ np.identity(m)))
 
 
-def stack_blocks(S_rk_list, T, m):
-    """(SiM, SiP, T) as (n, m, m) device tensors; SiM[0] = SiP[-1] = 0."""
+def stack_blocks(S_rk_list, T, m, cyclic=False):
+    """(SiM, SiP, T) as (n, m, m) device tensors; SiM[0] = SiP[-1] = 0 unless
+    ``cyclic`` (then they are the periodic couplings of rows of length 2)."""
     n = len(S_rk_list)
     SiM = torch.zeros((n, m, m), dtype=torch.float64, device="cuda")
     SiP = torch.zeros((n, m, m), dtype=torch.float64, device="cuda")
     for i, row in enumerate(S_rk_list):
         if len(row) >= 2:
-            if i > 0:
+            if i > 0 or cyclic:
                 SiM[i] = _dense_block(row[0], m)
-            if i < n - 1:
+            if i < n - 1 or cyclic:
                 SiP[i] = _dense_block(row[-1], m)
         elif len(row) == 1:
             if i == 0:
@@ -88,10 +89,10 @@ class _DeviceTridiag:
     _factor_fn = None
     _solve_fn = None
 
-    def _factor(self, S_rk_list, T):
+    def _factor(self, S_rk_list, T, periodic=False):
         m = _block_size(S_rk_list)
         self.m = m
-        SiM, SiP, Td = stack_blocks(S_rk_list, T, m)
+        SiM, SiP, Td = stack_blocks(S_rk_list, T, m, periodic)
         self.nblk = SiM.shape[0]
         out = ctypes.c_void_p()
         L.check(getattr(L.lib(), self._factor_fn)(L.handle(), self.nblk, m, L.ptr(SiM),
@@ -152,7 +153,9 @@ class BlockTridiagonalSolver(_DeviceTridiag, DirectSolver):
 
 
 class RedBlackSolver(_DeviceTridiag, DirectSolver):
-    """Red-black cyclic reduction, omsdirectsolve.py:177-333 (non-cyclic).
+    """Red-black cyclic reduction, omsdirectsolve.py:177-333; cyclic=True is
+    the periodic system (slu_rb_factor_cyclic: SiM[0] couples block 0 to the
+    last block and SiP[-1] the last block to block 0), float64 only.
 
     precision='mixed' (beyond upstream): the Schur-complement products of the
     elimination run on the tensor cores (split-BF16x3, slu_rb_factor_mixed),
@@ -177,9 +180,10 @@ class RedBlackSolver(_DeviceTridiag, DirectSolver):
         if not (n & (n - 1) == 0 and n != 0):
             raise ValueError("ERROR! Number of slabs is not a power of 2.")
         if self.cyclic:
-            raise NotImplementedError("cyclic red-black is not on the GPU path; "
-                                      "use BlockTridiagonalSolver(cyclic=True)")
-        self._factor(S_rk_list, T)
+            if self.precision == "mixed":
+                raise NotImplementedError("the periodic red-black solver is float64 only")
+            self._factor_fn = "slu_rb_factor_cyclic"
+        self._factor(S_rk_list, T, periodic=self.cyclic)
         self.nSlabs = n
 
     def solve(self, rhs):

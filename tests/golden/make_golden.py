@@ -13,6 +13,7 @@ the large outputs are stored.  Fixtures written (all small):
   rb_dense.npz       upstream direct_solve/test_RB.py cases: RedBlackSolver and
                      BlockTridiagonalSolver solutions
   thomas_cyclic.npz  BlockTridiagonalSolver(cyclic=True) on a periodic system
+  rb_cyclic.npz      RedBlackSolver(cyclic=True) on periodic systems of 2, 4, 8 blocks
   hbs_*.npz          HBSnew.HBSMAT(...).construct(k, True) of exact random HBS
                      matrices (test/rkprop/HBSnewTest.py generator): factors,
                      matmat/rmatmat and solve (N and T) outputs
@@ -92,6 +93,28 @@ def thomas_cyclic(ref):
     th.factorize(S, T)
     np.savez_compressed(os.path.join(HERE, "thomas_cyclic.npz"),
                         S=np.array(S), T=np.array(T), rhs=rhs, x=th.solve(rhs))
+
+
+def rb_cyclic(ref):
+    """RedBlackSolver(cyclic=True) on periodic block-tridiagonal systems of
+    2, 4 and 8 blocks (upstream's solve is 1-D: one column each)."""
+    out = {}
+    for nS, m, seed in ((2, 5, 11), (4, 6, 12), (8, 16, 13)):
+        rng = np.random.default_rng(seed)
+        S = [[0.2 * rng.standard_normal((m, m)), 0.2 * rng.standard_normal((m, m))]
+             for _ in range(nS)]
+        T = [rng.standard_normal((m, m)) + 6 * np.eye(m) for _ in range(nS)]
+        rhs = rng.standard_normal(nS * m)
+        with contextlib.redirect_stdout(QUIET):
+            rb = ref.omsdirectsolve.RedBlackSolver(m, cyclic=True)
+            rb.factorize(S, T)
+            x = rb.solve(rhs)
+        key = "%d_%d" % (nS, m)
+        out["S_" + key] = np.array(S)
+        out["T_" + key] = np.array(T)
+        out["rhs_" + key] = rhs
+        out["x_" + key] = x
+    np.savez_compressed(os.path.join(HERE, "rb_cyclic.npz"), **out)
 
 
 def hbs_case(ref, name, k, nl, L, quad, seed, sigma=None, nrhs=3, store_factors=True):
@@ -482,6 +505,7 @@ def main():
     P = refshim.import_pipeline()
     rb_dense(ref)
     thomas_cyclic(ref)
+    rb_cyclic(ref)
     hbs_case(ref, "hbs_binary_k8", 8, 16, 4, False, 101)
     hbs_case(ref, "hbs_quad_k8", 8, 8, 3, True, 102)
     sig = 10.0 ** (-12.0 * np.arange(32) / 31.0)

@@ -273,3 +273,26 @@ def test_helmholtz3d_slab_maps_match_upstream(golden):
     x0 = (ns - 1) * H - H
     assert relerr(helmholtz3d_sample(*geo, x0, Om, 0), L @ Om) < 1e-13
     assert relerr(helmholtz3d_sample(*geo, x0, Om, 1, trans=True), R.T @ Om) < 1e-13
+
+
+def _periodic_matrix(S, T):
+    nS, m = S.shape[0], S.shape[2]
+    M = np.zeros((nS * m, nS * m))
+    for i in range(nS):
+        M[i * m:(i + 1) * m, i * m:(i + 1) * m] = T[i]
+        j = (i - 1) % nS
+        M[i * m:(i + 1) * m, j * m:(j + 1) * m] += S[i][0]
+        j = (i + 1) % nS
+        M[i * m:(i + 1) * m, j * m:(j + 1) * m] += S[i][1]
+    return M
+
+
+def test_rb_cyclic_fixture_is_the_periodic_system(golden):
+    """Upstream's RedBlackSolver(cyclic=True) solves the periodic system in
+    which SiM[0] couples block 0 to the last block and SiP[-1] the last
+    block to block 0 (with two blocks both couplings land on the other
+    block): the fixture agrees with a dense solve of that system."""
+    g = golden("rb_cyclic")
+    for key in ("2_5", "4_6", "8_16"):
+        M = _periodic_matrix(g["S_" + key], g["T_" + key])
+        assert relerr(np.linalg.solve(M, g["rhs_" + key]), g["x_" + key]) < 1e-14
