@@ -17,7 +17,10 @@ residual <= 1e-10 against the stored float64 HBS operator:
   dfloat : the double-float ULV sweep alone (slu_ulv_solve_dfloat), its
            residual checked after the timed region as for plain
 `value` is the plain float64 path's RHS solves/s; the other arms are reported
-beside it.  Inputs (factors ~ 20 MB) fit in L2, so L2 is flushed (a 256 MB
+beside it.  `served` repeats the plain / mixed comparison at the batch widths
+continuous batching serves one resident operator with (--served-rhs, default
+1024 and 4096 right-hand sides), the mixed path there on the tensor cores
+(digit-split bfloat16 tcgen05 products, refined to 1e-10).  Inputs (factors ~ 20 MB) fit in L2, so L2 is flushed (a 256 MB
 write) before every timed step, outside the timed events.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
@@ -303,6 +306,43 @@ def replica_throughput(world, units_per_rank, slowest_seconds):
 
 
 # ---------------------------------------------------------------- GPU leg
+def served_widths(H, args, flush, stream, timed, world):
+    """The same operator at served batch widths (continuous batching gathers
+    many requests for one resident operator into one solve): plain float64
+    solves against the mixed path with the tensor-core sweep and residual
+    (HBSMAT.solve_refined(inner='tensor'): every step product as bfloat16
+    tcgen05 products of error-free digit splits, refined to 1e-10 against a
+    float64-accurate residual of the stored operator).  Per width: RHS/s,
+    p50/p99 of the step, iterations, worst residual (float64 apply, after the
+    timed region) and the speedup."""
+    import torch
+    out = []
+    for c in args.served_rhs:
+        Bc = torch.from_numpy(np.random.default_rng(SEED + c).standard_normal((N, c))).cuda()
+        steps = max(3, min(args.steps, 10))
+        ts_p, l_p, Xp = timed(lambda: H._dev_solve(Bc, False), steps, args.warmup)
+        ts_m, l_m, mo = timed(lambda: H.solve_refined(Bc, tol=TOL, maxit=10, inner="tensor"),
+                              steps, args.warmup)
+        Xm, iters, _ = mo
+        R = Bc - H._dev_apply(Xm, False)
+        res = float((R.norm(dim=0) / Bc.norm(dim=0)).max())
+        err = float((Xm - Xp).norm() / Xp.norm())
+        tp, tm = sum(ts_p), sum(ts_m)
+        out.append({"nrhs": c,
+                    "plain": {"value": world * c * steps / tp, "unit": UNIT,
+                              "p50_ms": 1e3 * statistics.median(ts_p), "gpu_launches": l_p,
+                              "arm": "float64 ULV solve (HBSMAT.solve)"},
+                    "mixed": {"value": world * c * steps / tm, "unit": UNIT,
+                              "p50_ms": 1e3 * statistics.median(ts_m),
+                              "p99_ms": 1e3 * float(np.percentile(ts_m, 99)),
+                              "iters": iters, "relres": res, "relerr_vs_plain": err,
+                              "speedup_vs_plain": tp / tm, "gpu_launches": l_m,
+                              "dtype": "bf16 tcgen05 products of error-free digit splits "
+                                       "(f32 accumulation) + f64-accurate residual refinement"}})
+        del Bc
+    return out
+
+
 def run_gpu(args, rank, world):
     import torch
     import torch.distributed as dist
@@ -415,6 +455,7 @@ def run_gpu(args, rank, world):
         return ts
     e2e = e2e_times(plan_host)
     e2e_call = e2e_times(lambda: H.solve(hp, out=out_h))
+    served = served_widths(H, args, flush, stream, timed, world)
     clk = clocks.stop()
 
     res_plain = residual(Xp)
@@ -460,6 +501,7 @@ def run_gpu(args, rank, world):
                       "iters": iters, "relres": res_mixed,
                       "speedup_vs_plain": tot_plain / tot_mixed,
                       "gpu_launches": launches_mixed},
+            "served": served,
             "dfloat": {"value": world * NRHS * args.steps / tot_df, "unit": UNIT,
                        "dtype": "double-float (f32 pairs) ULV sweep, no refinement",
                        "p50_ms": 1e3 * statistics.median(ts_df),
@@ -606,6 +648,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--workload", default="c2", choices=["c2", "c1_dense", "c3_hbs", "c4_batch"])
+    ap.add_argument("--served-rhs", type=lambda v: [int(x) for x in v.split(",") if x],
+                    default=[1024, 4096],
+                    help="batch widths of the served mixed vs plain comparison (comma separated)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.workload != "c2":

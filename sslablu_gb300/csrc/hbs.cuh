@@ -321,8 +321,12 @@ size_t hbs_oz_scratch_bytes(const Hbs& H, int c);
 // device word set on a device wait timeout.
 void ulv_solve_oz(cudaStream_t st, const Hbs& H, const double* X, int ldx, double* Y, int ldy,
                   int c, void* scratch, unsigned* err);
+// With resb (N x c, leading dimension ldy) the apply returns the residual
+// Y = resb - A X instead, and rnorm2 (c entries, zeroed by the caller)
+// accumulates its squared column norms.
 void hbs_apply_oz(cudaStream_t st, const Hbs& H, const double* X, int ldx, double* Y, int ldy,
-                  int c, void* scratch, unsigned* err);
+                  int c, void* scratch, unsigned* err, const double* resb = nullptr,
+                  double* rnorm2 = nullptr);
 
 // Factor pointers of one level by arithmetic type (float64 factors or their
 // float32 copies).

@@ -89,6 +89,13 @@ struct OzStep {
   // magnitude, inside the float32 exponent range, whatever the float64 scale
   const unsigned* colbits;
   unsigned* err;           // device error word (timeouts)
+  // residual form of the float64 output (the refinement's last apply step):
+  // with resb set, the caller's rows receive resb - (S z) instead of S z
+  // (resb in the output's layout and leading dimension), and rnorm2[j]
+  // accumulates the squared 2-norm of column j of that residual (atomics;
+  // zeroed by the caller)
+  const double* resb;
+  double* rnorm2;
 };
 
 // s_j of a column from its max-magnitude bits (0 for a zero column):
@@ -302,6 +309,7 @@ __global__ void __launch_bounds__(kThreads, 1) oz_step_kernel(const OzStep o) {
   __shared__ const char* rowp[kMaxW];
   __shared__ int rowf64[kMaxW];
   __shared__ char* outp[kMaxNT];
+  __shared__ const char* resp[kMaxNT];
   __shared__ int outf64[kMaxNT];
   __shared__ float rs[kMaxNT];
   __shared__ float colmax[kDigWarps / 4][kM];
@@ -357,6 +365,7 @@ __global__ void __launch_bounds__(kThreads, 1) oz_step_kernel(const OzStep o) {
   }
   for (int i = tid; i < NT; i += kThreads) {
     char* p = nullptr;
+    const char* pb = nullptr;
     int f = 0;
     float sc = 0.f;
     if (i < nr) {
@@ -366,6 +375,7 @@ __global__ void __launch_bounds__(kThreads, 1) oz_step_kernel(const OzStep o) {
         const long long dst = s.out_perm ? __ldg(s.out_perm + q) : q;
         p = reinterpret_cast<char*>(s.out_p[0] + dst * s.out_ld[0] + c0);
         f = o.out_f64;
+        if (o.resb) pb = reinterpret_cast<const char*>(o.resb + dst * s.out_ld[0] + c0);
       } else {
         const long long q = (long long)b * s.out_blk[1] + (row - s.split);
         p = reinterpret_cast<char*>(s.out_p[1] + q * s.out_ld[1] + c0);
@@ -373,6 +383,7 @@ __global__ void __launch_bounds__(kThreads, 1) oz_step_kernel(const OzStep o) {
       sc = __ldg(o.rsc + (size_t)(b * o.ntile + rt) * NT + i);
     }
     outp[i] = p;
+    resp[i] = pb;
     outf64[i] = f;
     rs[i] = sc;
   }
@@ -455,12 +466,16 @@ __global__ void __launch_bounds__(kThreads, 1) oz_step_kernel(const OzStep o) {
         }
       }
     };
-    // column scale: largest |h| over the column's k (8 loads in flight)
+    // column scale: largest |h| over the column's k (8 loads in flight),
+    // chunks in reverse order so that chunk 0's values stay in registers for
+    // the first digitisation
     float mx = 0.f;
-    for (int c = 0; c < nch; ++c) {
+    float hv[8], lv[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) hv[u] = lv[u] = 0.f;
+    for (int c = nch - 1; c >= 0; --c) {
       const int k0 = c * kKC + qk * 8;
       if (k0 >= wP) continue;
-      float hv[8], lv[8];
 #pragma unroll
       for (int u = 0; u < 8; ++u) load(k0 + u, hv[u], lv[u]);
 #pragma unroll
@@ -481,12 +496,21 @@ __global__ void __launch_bounds__(kThreads, 1) oz_step_kernel(const OzStep o) {
     bool fail = false;
     for (int c = 0; c < nch; ++c) {
       const int b2 = c & 1;
-      if (c >= 2 && !mbar_wait(&zempty[b2], (uint32_t)((c >> 1) - 1) & 1u)) fail = true;
       const int k0 = c * kKC + qk * 8;
-      if (k0 < wP) {
-        float hv[8], lv[8];
+      // the next chunk's loads go out before this chunk is digitised
+      float nh[8], nl[8];
+      const bool more = c + 1 < nch && k0 + kKC < wP;
 #pragma unroll
-        for (int u = 0; u < 8; ++u) load(k0 + u, hv[u], lv[u]);
+      for (int u = 0; u < 8; ++u) {
+        nh[u] = 0.f;
+        nl[u] = 0.f;
+      }
+      if (more) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) load(k0 + kKC + u, nh[u], nl[u]);
+      }
+      if (c >= 2 && !mbar_wait(&zempty[b2], (uint32_t)((c >> 1) - 1) & 1u)) fail = true;
+      if (k0 < wP) {
         {
           uint32_t wd[kDig][4];
 #pragma unroll
@@ -535,6 +559,11 @@ __global__ void __launch_bounds__(kThreads, 1) oz_step_kernel(const OzStep o) {
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       __syncwarp();
       if (lane == 0) mbar_arrive(&zfull[b2]);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        hv[u] = nh[u];
+        lv[u] = nl[u];
+      }
     }
     sweep::launch_dependents();
     if (fail) {
@@ -557,6 +586,7 @@ __global__ void __launch_bounds__(kThreads, 1) oz_step_kernel(const OzStep o) {
       const uint32_t lanes = (uint32_t)(qd * 32) << 16;
       // col == tid % 128: this thread digitised column col, so cs is its scale
       const float csc = cs;
+      float rsq = 0.f;   // squared residual norm of this column (residual form)
       for (int r8 = rq * 8; r8 < NT; r8 += 32) {
         uint32_t v[kDig][8];
 #pragma unroll
@@ -576,12 +606,36 @@ __global__ void __launch_bounds__(kThreads, 1) oz_step_kernel(const OzStep o) {
           char* p = outp[row] + 8 * col;
           if (outf64[row]) {
             const int ge = (int)((__float_as_uint(g) >> 23) & 255);
-            *reinterpret_cast<double*>(p) = ge ? pair_to_f64(H, Lo, ge - 127 + osh) : 0.0;
+            if (resp[row]) {
+              // r = b - S z in the row's scale 2^sh: b split into a float
+              // pair there (integer operations), one double-float
+              // subtraction, then back to float64 like the plain output
+              const int sh = ge ? ge - 127 + osh : osh;
+              const double bv = *reinterpret_cast<const double*>(resp[row] + 8 * col);
+              float bh, bl;
+              f64_split(bv, sh, bh, bl);
+              if (!ge) {
+                H = 0.f;
+                Lo = 0.f;
+              }
+              float rh, rl;
+              two_sum(bh, -H, rh, rl);
+              rl = __fadd_rn(rl, __fsub_rn(bl, Lo));
+              two_sum(rh, rl, rh, rl);
+              *reinterpret_cast<double*>(p) = pair_to_f64(rh, rl, sh);
+              const float rr = ge ? __fmul_rn(rh, g) : __fmul_rn(rh, __uint_as_float(127u << 23));
+              rsq = __fmaf_rn(rr, rr, rsq);
+            } else {
+              *reinterpret_cast<double*>(p) = ge ? pair_to_f64(H, Lo, ge - 127 + osh) : 0.0;
+            }
           } else {
             *reinterpret_cast<float2*>(p) = make_float2(__fmul_rn(H, g), __fmul_rn(Lo, g));
           }
         }
       }
+      // rsq holds the column's squares scaled by 2^(-2 osh)
+      if (o.rnorm2 && cok && rsq > 0.f)
+        atomicAdd(o.rnorm2 + c0 + col, ldexp((double)rsq, 2 * osh));
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -678,7 +732,8 @@ void make_op(cudaStream_t st, OzOp& o, const double* S, int Nb, int rows, int w)
 }
 
 void launch(cudaStream_t st, const sweep::Step<dfloat>& s, const OzOp& op, bool in_f64,
-            bool out_f64, const unsigned* colbits, unsigned* err, const char* what) {
+            bool out_f64, const unsigned* colbits, unsigned* err, const char* what,
+            const double* resb = nullptr, double* rnorm2 = nullptr) {
   SLU_REQUIRE(op.dig.p && s.rows == op.rows && s.w == op.w && s.nb == op.Nb,
               "tensor-core sweep: digit operator does not match its step");
   OzStep o{};
@@ -692,6 +747,9 @@ void launch(cudaStream_t st, const sweep::Step<dfloat>& s, const OzOp& op, bool 
   o.out_f64 = out_f64 ? 1 : 0;
   o.colbits = (in_f64 || out_f64) ? colbits : nullptr;
   o.err = err;
+  SLU_REQUIRE(!resb || (out_f64 && s.out_ld[0] >= s.c), "residual form needs a float64 output");
+  o.resb = resb;
+  o.rnorm2 = rnorm2;
   sweep::LaunchPlan p;
   p.ctas = (long long)s.nb * op.ntile * ((s.c + kM - 1) / kM);
   p.threads = kThreads;
@@ -789,7 +847,7 @@ void ulv_solve_oz(cudaStream_t st, const Hbs& H, const double* X, int ldx, doubl
 }
 
 void hbs_apply_oz(cudaStream_t st, const Hbs& H, const double* X, int ldx, double* Y, int ldy,
-                  int c, void* scratch, unsigned* err) {
+                  int c, void* scratch, unsigned* err, const double* resb, double* rnorm2) {
   SLU_REQUIRE(H.has_oz, "tensor-core sweep not prepared");
   SLU_REQUIRE(static_cast<const void*>(X) != static_cast<const void*>(Y),
               "tensor-core apply: input and output must be different buffers");
@@ -811,7 +869,7 @@ void hbs_apply_oz(cudaStream_t st, const Hbs& H, const double* X, int ldx, doubl
     const Level& r = H.lv[0];
     oz::launch(st,
                sweep::down_step<dfloat>(r, nullptr, true, x, ldx, perm, nullptr, y, ldy, perm, c),
-               r.ozDn, true, true, cb, err, "oz_apply_root");
+               r.ozDn, true, true, cb, err, "oz_apply_root", resb, rnorm2);
     return;
   }
   for (int t = 0; t + 1 < L; ++t) {
@@ -834,7 +892,8 @@ void hbs_apply_oz(cudaStream_t st, const Hbs& H, const double* X, int ldx, doubl
                sweep::down_step<dfloat>(l, nullptr, false, leaf ? x : VV[t], leaf ? ldx : c,
                                         leaf ? perm : nullptr, u[cur], leaf ? y : u[cur ^ 1],
                                         leaf ? ldy : c, leaf ? perm : nullptr, c),
-               l.ozDn, leaf, leaf, cb, err, "oz_apply_down");
+               l.ozDn, leaf, leaf, cb, err, "oz_apply_down", leaf ? resb : nullptr,
+               leaf ? rnorm2 : nullptr);
     cur ^= 1;
   }
 }

@@ -13,6 +13,7 @@
 // and replayed.  With the float32 inner sweep the host looks at the norms only
 // from the second correction on (a float32 solve alone never reaches a
 // float64 tolerance).
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 
@@ -44,8 +45,15 @@ void enqueue_iteration(cudaStream_t st, const Hbs& H, RefinePlan& P, bool first)
   double* X = P.X.as<double>();
   double* r = P.r.as<double>();
   if (first) {
-    colnorm2_k<<<c, 256, 0, st>>>(N, c, B, c, P.bn.as<double>());
-    check_launch("colnorm2_k");
+    if (P.inner == 2) {
+      SLU_CHECK_CUDA(cudaMemsetAsync(P.bn.p, 0, 8 * (size_t)c, st));
+      colsumsq_k<<<dim3((c + 127) / 128, std::min(64, std::max(1, N / 64))), 128, 0, st>>>(
+          N, c, B, c, P.bn.as<double>());
+      check_launch("colsumsq_k");
+    } else {
+      colnorm2_k<<<c, 256, 0, st>>>(N, c, B, c, P.bn.as<double>());
+      check_launch("colnorm2_k");
+    }
     SLU_CHECK_CUDA(cudaMemcpyAsync(P.host_norms, P.bn.p, 8 * c, cudaMemcpyDeviceToHost, st));
   }
   const double* rhs = first ? B : r;
@@ -61,11 +69,9 @@ void enqueue_iteration(cudaStream_t st, const Hbs& H, RefinePlan& P, bool first)
       add_k<<<gsz(n), 256, 0, st>>>(n, d, X);
       check_launch("add_k");
     }
-    hbs_apply_oz(st, H, X, c, r, c, c, P.solve_ws.p, err);
-    resid_k<<<gsz(n), 256, 0, st>>>(n, B, r);
-    check_launch("resid_k");
-    colnorm2_k<<<c, 256, 0, st>>>(N, c, r, c, P.rn.as<double>());
-    check_launch("colnorm2_k");
+    // r = B - A X straight from the apply's last step, with its column norms
+    SLU_CHECK_CUDA(cudaMemsetAsync(P.rn.p, 0, 8 * (size_t)c, st));
+    hbs_apply_oz(st, H, X, c, r, c, c, P.solve_ws.p, err, B, P.rn.as<double>());
     SLU_CHECK_CUDA(cudaMemcpyAsync(P.host_norms + c, P.rn.p, 8 * c, cudaMemcpyDeviceToHost, st));
     SLU_CHECK_CUDA(cudaMemcpyAsync(P.host_norms + 2 * c, P.ozerr.p, 8, cudaMemcpyDeviceToHost,
                                    st));

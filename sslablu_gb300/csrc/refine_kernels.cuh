@@ -74,6 +74,23 @@ __global__ void add_k(long long n, const double* __restrict__ d, double* __restr
     x[e] += d[e];
 }
 
+// out[j] += sum_i A_ij^2 for a rows x cols row-major block: one thread per
+// column (consecutive threads read consecutive columns: coalesced), rows
+// split over blockIdx.y; out zeroed by the caller.
+__global__ void colsumsq_k(int rows, int cols, const double* __restrict__ A, int lda,
+                           double* __restrict__ out) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= cols) return;
+  const int per = (rows + gridDim.y - 1) / gridDim.y;
+  const int i0 = blockIdx.y * per, i1 = min(rows, i0 + per);
+  double s = 0.0;
+  for (int i = i0; i < i1; ++i) {
+    const double v = A[(long long)i * lda + j];
+    s = fma(v, v, s);
+  }
+  if (i1 > i0) atomicAdd(out + j, s);
+}
+
 // r = b - r
 __global__ void resid_k(long long n, const double* __restrict__ b, double* __restrict__ r) {
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;

@@ -2,6 +2,7 @@
 
     python -m sslablu_gb300.slabbench dense [--m 256 --slabs 8]
     python -m sslablu_gb300.slabbench hbs   [--m 1024 --slabs 8 --leaf 64 --rank 24]
+    python -m sslablu_gb300.slabbench helmholtz [--slabs 33 --n 64 --leaf 128 --rank 64]
 
 Workloads (seeded synthetic couplings of the interface system I + S,
 sslablu_gb300.synthetic.slab_couplings; the slab PDE pipeline that produces
@@ -146,18 +147,111 @@ def hbs(a):
     return out
 
 
+def helmholtz(a):
+    """The C3 pipeline on real slab operators: 3-D variable-coefficient
+    Helmholtz (k = kappa, c = 1 + 0.5 sin 2pi x sin 2pi y sin 2pi z) on
+    [0,1]^3 cut into a.slabs slabs, a.n x a.n interface planes, stencil
+    discretisation with 5 points across a double slab.
+      1. the slab maps S_l, S_r sampled on the GPU through batched slab solves
+         (multislab.slabmaps; oms.compute_stmaps) and compressed by the rkHBS
+         assembler (leaf a.leaf, rank a.rank; matAssembler.py:104-133);
+      2. RedBlackSolverHBS factorisation of the compressed interface system;
+      3. 64 right-hand sides (smooth seeded interface data) solved by GMRES on
+         the exact interface operator (slab solves, float64) with the
+         red-black HBS solve as preconditioner, to a 1e-10 relative residual
+         (test/3D/cubeTest.py:158-186).
+    Reports the stage times, GMRES steps, residual against the exact
+    operator, and the residual of the preconditioner alone."""
+    from .direct_solve.omsdirectsolveHBS import RedBlackSolverHBS
+    from .matAssembly.matAssembler import rkHMatAssembler
+    from .multislab.gmres import gmres
+    from .multislab.slabmaps import SlabGeometry, StotOperator, slab_stmaps
+    g = SlabGeometry(a.slabs, 5, a.n + 2, a.n + 2, kappa=a.kappa, coef=1)
+    m, nif = g.m, g.nif
+    np.random.seed(20261207)
+    asm = rkHMatAssembler(a.leaf, a.rank)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    S_rk = []
+    t_sample = 0.0
+    for st_l, st_r in slab_stmaps(g):
+        row = []
+        for st in (st_l, st_r):
+            if st is not None:
+                row.append(asm.assemble(st))
+                t_sample += asm.stats.timeSample
+        S_rk.append(row)
+    torch.cuda.synchronize()
+    t_compress = time.perf_counter() - t0
+    tree = S_rk[0][0].tree
+    rb = RedBlackSolverHBS(m, a.rank, tree, False)
+    t0 = time.perf_counter()
+    rb.factorize(S_rk)
+    torch.cuda.synchronize()
+    t_factor = time.perf_counter() - t0
+    St = StotOperator(g)
+    # smooth seeded interface data: low-order trig series per plane
+    pts = g.points(0)
+    rng = np.random.default_rng(7)
+    B = np.zeros((nif * m, a.nrhs))
+    for j in range(a.nrhs):
+        for i in range(nif):
+            coef = rng.standard_normal((4, 4))
+            v = np.zeros(m)
+            for p in range(4):
+                for q in range(4):
+                    v += coef[p, q] * np.sin((p + 1) * np.pi * pts[:, 1]) * \
+                        np.sin((q + 1) * np.pi * pts[:, 2])
+            B[i * m:(i + 1) * m, j] = v
+    Bd = torch.from_numpy(B).cuda()
+    # the preconditioner alone (one red-black HBS solve)
+    Xp = rb.solve(Bd)
+    R = Bd - St.dev_matmat(Xp)
+    res_pre = float((R.norm(dim=0) / Bd.norm(dim=0)).max())
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(a.reps):
+        t0 = time.perf_counter()
+        X, steps, rel = gmres(St.dev_matmat, Bd, rb.solve, tol=1e-10, restart=30, maxiter=200)
+        torch.cuda.synchronize()
+        ts.append(time.perf_counter() - t0)
+    R = Bd - St.dev_matmat(X)
+    res = float((R.norm(dim=0) / Bd.norm(dim=0)).max())
+    t_solve = statistics.median(ts)
+    # one exact interface apply and one preconditioner solve, timed alone
+    t_apply = _wall(lambda: St.dev_matmat(Bd), 3)[0]
+    t_pre = _wall(lambda: rb.solve(Bd), 3)[0]
+    return {"workload": "3-D Helmholtz k=%g, c = 1 + 0.5 sin sin sin, %d slabs, %d x %d "
+                        "interfaces (m=%d), 5-point slabs, rkHBS leaf %d rank %d"
+                        % (a.kappa, a.slabs, a.n, a.n, m, a.leaf, a.rank),
+            "interfaces": nif, "m": m, "nrhs": a.nrhs,
+            "maps_sample_compress_s": t_compress, "maps_sample_s": t_sample,
+            "chebyshev_steps": St.maps.steps or None,
+            "rb_hbs_factor_s": t_factor,
+            "preconditioner_relres": res_pre,
+            "gmres_steps": steps, "relres": res, "gmres_relres": rel,
+            "solve_s": t_solve, "rhs_per_s": a.nrhs / t_solve,
+            "stot_apply_ms": 1e3 * t_apply, "rb_hbs_solve_ms": 1e3 * t_pre}
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
-    ap.add_argument("kind", choices=["dense", "hbs"])
+    ap.add_argument("kind", choices=["dense", "hbs", "helmholtz"])
     ap.add_argument("--m", type=int, default=None)
     ap.add_argument("--slabs", type=int, default=8)
     ap.add_argument("--leaf", type=int, default=64)
     ap.add_argument("--rank", type=int, default=24)
     ap.add_argument("--reps", type=int, default=10)
+    ap.add_argument("--n", type=int, default=64, help="helmholtz: interface plane n x n")
+    ap.add_argument("--kappa", type=float, default=20.0)
+    ap.add_argument("--nrhs", type=int, default=64)
     a = ap.parse_args()
     if a.m is None:
         a.m = 256 if a.kind == "dense" else 1024
-    out = dense(a) if a.kind == "dense" else hbs(a)
+    if a.kind == "helmholtz":
+        out = helmholtz(a)
+    else:
+        out = dense(a) if a.kind == "dense" else hbs(a)
     print(json.dumps(out))
 
 
