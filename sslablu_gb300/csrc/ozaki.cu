@@ -71,8 +71,10 @@ constexpr int kM = 128;           // right-hand-side columns per CTA (MMA M)
 constexpr int kMaxW = 96;         // widest step whose diagonal sums stay exact in float32
 constexpr int kMaxNT = 64;        // operator rows per CTA (MMA N)
 constexpr int kKC = 32;           // k per digitised chunk of z (two chunk buffers)
-constexpr int kDigWarps = 16;     // digitise z, then the epilogue
-constexpr int kThreads = 32 * (kDigWarps + 1);   // + one MMA warp
+constexpr int kDigWarps = 16;     // digitise z
+constexpr int kEpiWarps = 8;      // read the accumulators, combine, store (2 per lane quadrant)
+constexpr int kMmaWarp = kDigWarps + kEpiWarps;   // issues the tensor-core MMAs
+constexpr int kThreads = 32 * (kMmaWarp + 1);
 constexpr long long kWaitLimit = 1LL << 22;
 
 struct OzStep {
@@ -300,12 +302,39 @@ __device__ __forceinline__ double pair_to_f64(float H, float Lo, int sh) {
 }
 
 // ---------------------------------------------------------------- the kernel
+// Tile t of a step: block b, row tile rt, column tile ct (ct fastest, so the
+// consecutive tiles of a CTA share their operator digits).
+struct Tile {
+  int b, rt, ct;
+};
+__device__ __forceinline__ Tile tile_of(int t, int ntile, int nct) {
+  Tile T;
+  const int per_b = ntile * nct;
+  T.b = t / per_b;
+  const int rem = t - T.b * per_b;
+  T.rt = rem / nct;
+  T.ct = rem - T.rt * nct;
+  return T;
+}
+
+// Persistent, warp-specialised: each CTA (one per SM) runs a contiguous range
+// of tiles.  Digitiser warps (16) prepare tile i + 1 -- input rows, column
+// scales, digit chunks -- while the MMA warp and the epilogue warps (8, two
+// per TMEM lane quadrant) finish tile i; the accumulators of one tile fill
+// the tensor memory, so the MMAs of tile i + 1 start when the epilogue has
+// read tile i's.  mbarriers: op_full (operator digits landed), tmem_full
+// (a tile's MMAs done), tmem_empty (its accumulators read), zfull / zempty
+// (digit chunk buffers), cs_full / cs_free (column scales, by tile parity).
 __global__ void __launch_bounds__(kThreads, 1) oz_step_kernel(const OzStep o) {
   extern __shared__ unsigned char smraw[];
-  __shared__ __align__(8) uint64_t op_bar, done_bar;
-  __shared__ __align__(8) uint64_t zfull[2], zempty[2];
+  __shared__ __align__(8) uint64_t op_full, tmem_full, tmem_empty;
+  __shared__ __align__(8) uint64_t zfull[2], zempty[2], cs_full[2], cs_free[2];
   __shared__ uint32_t tmem_slot;
   __shared__ volatile int s_fail;
+  // per-role failure flags, written before and read after a role barrier so
+  // every warp of the role takes the same branch (named barriers have no
+  // timeout: a role must never leave its loop partly)
+  __shared__ volatile int d_fail, e_fail;
   __shared__ const char* rowp[kMaxW];
   __shared__ int rowf64[kMaxW];
   __shared__ char* outp[kMaxNT];
@@ -313,16 +342,14 @@ __global__ void __launch_bounds__(kThreads, 1) oz_step_kernel(const OzStep o) {
   __shared__ int outf64[kMaxNT];
   __shared__ float rs[kMaxNT];
   __shared__ float colmax[kDigWarps / 4][kM];
+  __shared__ float cscale[2][kM];
 
   const sweep::Step<dfloat>& s = o.s;
   const int NT = o.NT, wP = o.wP, w = s.w;
   const int nct = (s.c + kM - 1) / kM;
-  const int per_b = o.ntile * nct;
-  const int b = blockIdx.x / per_b;
-  const int rem = blockIdx.x - b * per_b;
-  const int rt = rem / nct, ct = rem - rt * nct;
-  const int c0 = ct * kM, r0 = rt * NT;
-  const int nr = min(NT, s.rows - r0);
+  const int ntiles = s.nb * o.ntile * nct;
+  const int t0 = (int)((long long)blockIdx.x * ntiles / gridDim.x);
+  const int nt = (int)((long long)(blockIdx.x + 1) * ntiles / gridDim.x) - t0;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t zsl = (uint32_t)kM * kKC * 2;   // one digit of one z chunk
   const uint32_t zdb = (uint32_t)kDig * zsl;     // one z chunk buffer (all digits)
@@ -332,186 +359,332 @@ __global__ void __launch_bounds__(kThreads, 1) oz_step_kernel(const OzStep o) {
       (reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
   unsigned char* zbuf = sm;             // two z chunk buffers
   unsigned char* opb = sm + 2 * zdb;    // the seven operator digit images
-  const uint16_t* opdig = o.dig + (size_t)(b * o.ntile + rt) * kDig * NT * wP;
   uint32_t ncols = 32;
   while (ncols < (uint32_t)(kDig * NT)) ncols <<= 1;
 
   if (tid == 0) {
-    mbar_init(&op_bar, 1);
-    mbar_init(&done_bar, 1);
+    mbar_init(&op_full, 1);
+    mbar_init(&tmem_full, 1);
+    mbar_init(&tmem_empty, kEpiWarps);
     for (int i = 0; i < 2; ++i) {
       mbar_init(&zfull[i], kDigWarps);
       mbar_init(&zempty[i], 1);
+      mbar_init(&cs_full[i], kDigWarps);
+      mbar_init(&cs_free[i], kEpiWarps);
     }
     s_fail = 0;
+    d_fail = 0;
+    e_fail = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
-  // the operator digits are constant: their copy starts before the wait for
-  // the previous launch of the stream (one bulk copy of the seven images)
-  if (tid == 0) {
-    mbar_expect_tx(&op_bar, kDig * obytes);
-    bulk_copy(opb, opdig, kDig * obytes, &op_bar);
-  }
-  // input row of every k (the first range optionally through the
-  // permutation), output row of every tile row, row scales
-  for (int k = tid; k < w; k += kThreads) {
-    int q = 0, kk = k;
-    while (q + 1 < s.nin && kk >= s.in_rows[q]) kk -= s.in_rows[q++];
-    long long row = (long long)b * s.in_blk[q] + kk;
-    if (q == 0 && s.in_perm) row = __ldg(s.in_perm + row);
-    rowp[k] = reinterpret_cast<const char*>(s.in_p[q] + row * s.in_ld[q] + c0);
-    rowf64[k] = (q == 0 && o.in_f64) ? 1 : 0;
-  }
-  for (int i = tid; i < NT; i += kThreads) {
-    char* p = nullptr;
-    const char* pb = nullptr;
-    int f = 0;
-    float sc = 0.f;
-    if (i < nr) {
-      const int row = r0 + i;
-      if (row < s.split) {
-        const long long q = (long long)b * s.out_blk[0] + row;
-        const long long dst = s.out_perm ? __ldg(s.out_perm + q) : q;
-        p = reinterpret_cast<char*>(s.out_p[0] + dst * s.out_ld[0] + c0);
-        f = o.out_f64;
-        if (o.resb) pb = reinterpret_cast<const char*>(o.resb + dst * s.out_ld[0] + c0);
-      } else {
-        const long long q = (long long)b * s.out_blk[1] + (row - s.split);
-        p = reinterpret_cast<char*>(s.out_p[1] + q * s.out_ld[1] + c0);
-      }
-      sc = __ldg(o.rsc + (size_t)(b * o.ntile + rt) * NT + i);
+  // the first tile's operator digits are constant: their copy starts before
+  // the wait for the previous launch; the accumulators are allocated there
+  // too (only a CTA still running on this SM can hold tensor memory, and it
+  // frees it without waiting on this one)
+  if (warp == kMmaWarp) {
+    if (lane == 0 && nt > 0) {
+      const Tile T = tile_of(t0, o.ntile, nct);
+      mbar_expect_tx(&op_full, kDig * obytes);
+      bulk_copy(opb, o.dig + (size_t)(T.b * o.ntile + T.rt) * kDig * NT * wP, kDig * obytes,
+                &op_full);
     }
-    outp[i] = p;
-    resp[i] = pb;
-    outf64[i] = f;
-    rs[i] = sc;
-  }
-  sweep::grid_dependency_wait();
-  if (warp == kDigWarps) {
+    __syncwarp();
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(&tmem_slot)),
                  "r"(ncols)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
+  sweep::grid_dependency_wait();
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_slot;
 
-  if (warp == kDigWarps) {
+  if (warp == kMmaWarp) {
     // ---------------- MMA warp: digit pair (s, t), s + t <= 8 -> accumulator
     // s + t, chunk by chunk of z as the digitisers finish them
     if (lane == 0) {
       const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(NT >> 3) << 17) |
                              ((uint32_t)(kM >> 4) << 24);
       const uint32_t osbo = (uint32_t)wP * 16;   // operator: bytes per 8-row group
-      bool fail = !mbar_wait(&op_bar, 0);
-      for (int c = 0; c < nch && !fail; ++c) {
-        const int b2 = c & 1;
-        if (!mbar_wait(&zfull[b2], (uint32_t)(c >> 1) & 1u)) {
+      const uint64_t ostep = obytes >> 4;
+      bool fail = false;
+      int g = 0, nload = 1;
+      int opkey = -1;
+      if (nt > 0) {
+        const Tile T = tile_of(t0, o.ntile, nct);
+        opkey = T.b * o.ntile + T.rt;
+      }
+      for (int i = 0; i < nt && !fail; ++i) {
+        const Tile T = tile_of(t0 + i, o.ntile, nct);
+        const int key = T.b * o.ntile + T.rt;
+        if (key != opkey) {
+          // new operator digits once the previous tile's MMAs have read the old
+          if (!mbar_wait(&tmem_full, (uint32_t)((i - 1) & 1))) {
+            fail = true;
+            break;
+          }
+          mbar_expect_tx(&op_full, kDig * obytes);
+          bulk_copy(opb, o.dig + (size_t)key * kDig * NT * wP, kDig * obytes, &op_full);
+          opkey = key;
+          ++nload;
+        }
+        if (!mbar_wait(&op_full, (uint32_t)((nload - 1) & 1))) {
+          fail = true;
+          break;
+        }
+        // the epilogue has read the previous tile's accumulators
+        if (i > 0 && !mbar_wait(&tmem_empty, (uint32_t)((i - 1) & 1))) {
           fail = true;
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const int ksteps = min(kKC, wP - c * kKC) / 16;
-        // descriptors of digit 0 of the chunk (z) and of the operator at this
-        // chunk's k; a start-address offset is added in 16-byte units
-        const uint64_t a0 = desc_noswz(smem_u32(zbuf + b2 * zdb), 128, kKC * 16);
-        const uint64_t b0 =
-            desc_noswz(smem_u32(opb) + (uint32_t)c * (kKC / 8) * 128, 128, osbo);
-        const uint64_t ostep = obytes >> 4;
-        // every diagonal is first written by the pair (0, d) of chunk 0's
-        // first k step: that MMA overwrites, every other one accumulates
-#pragma unroll
-        for (int si = 0; si < kDig; ++si) {
-#pragma unroll
-          for (int ti = 0; si + ti < kDig; ++ti) {
-            const uint32_t dt = tmem + (uint32_t)((si + ti) * NT);
-            const uint64_t ad = a0 + (uint64_t)((ti * zsl) >> 4);
-            const uint64_t bd = b0 + (uint64_t)si * ostep;
-            mma_bf16(dt, ad, bd, idesc, (c | si) != 0 ? 1u : 0u);
-            if (ksteps > 1) mma_bf16(dt, ad + 16, bd + 16, idesc, 1u);
+        for (int c = 0; c < nch; ++c, ++g) {
+          const int b2 = g & 1;
+          if (!mbar_wait(&zfull[b2], (uint32_t)(g >> 1) & 1u)) {
+            fail = true;
+            break;
           }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const int ksteps = min(kKC, wP - c * kKC) / 16;
+          // descriptors of digit 0 of the chunk (z) and of the operator at
+          // this chunk's k; a start-address offset is added in 16-byte units
+          const uint64_t a0 = desc_noswz(smem_u32(zbuf + b2 * zdb), 128, kKC * 16);
+          const uint64_t b0 =
+              desc_noswz(smem_u32(opb) + (uint32_t)c * (kKC / 8) * 128, 128, osbo);
+          // every diagonal is first written by the pair (0, d) of the tile's
+          // first k step: that MMA overwrites, every other one accumulates
+#pragma unroll
+          for (int si = 0; si < kDig; ++si) {
+#pragma unroll
+            for (int ti = 0; si + ti < kDig; ++ti) {
+              const uint32_t dt = tmem + (uint32_t)((si + ti) * NT);
+              const uint64_t ad = a0 + (uint64_t)((ti * zsl) >> 4);
+              const uint64_t bd = b0 + (uint64_t)si * ostep;
+              mma_bf16(dt, ad, bd, idesc, (c | si) != 0 ? 1u : 0u);
+              if (ksteps > 1) mma_bf16(dt, ad + 16, bd + 16, idesc, 1u);
+            }
+          }
+          mma_commit(&zempty[b2]);   // this chunk buffer is free once these MMAs finish
         }
-        mma_commit(&zempty[b2]);   // this chunk buffer is free once these MMAs finish
+        if (fail) break;
+        mma_commit(&tmem_full);
       }
       if (fail) {
         s_fail = 1;
         if (o.err) atomicOr(o.err, 1u);
         __threadfence_block();
-        mbar_wait(&op_bar, 0);   // the operator copy must land before the CTA exits
+        // the last operator copy must land before the CTA exits
+        mbar_wait(&op_full, (uint32_t)((nload - 1) & 1));
       }
-      mma_commit(&done_bar);
     }
     __syncwarp();
+  } else if (warp >= kDigWarps) {
+    // ---------------- epilogue warps: warp (qd, rh) reads TMEM lanes 32 qd ..
+    // (its columns) and the 8-row groups rh * 8 + 16 i of the tile
+    const int qd = warp & 3, rh = (warp - kDigWarps) >> 2, etid = tid - kDigWarps * 32;
+    const int col = qd * 32 + lane;
+    const uint32_t lanes = (uint32_t)(qd * 32) << 16;
+    for (int i = 0; i < nt; ++i) {
+      const Tile T = tile_of(t0 + i, o.ntile, nct);
+      const int c0 = T.ct * kM, r0 = T.rt * NT;
+      const int nr = min(NT, s.rows - r0);
+      // output row of every tile row, row scales (the previous tile's
+      // readers are done: all four warps passed the barrier below)
+      if (etid == 0 && s_fail) e_fail = 1;
+      asm volatile("bar.sync 2, %0;" ::"r"(kEpiWarps * 32) : "memory");
+      if (e_fail) continue;   // the same for every epilogue warp
+      for (int r = etid; r < NT; r += kEpiWarps * 32) {
+        char* p = nullptr;
+        const char* pb = nullptr;
+        int f = 0;
+        float sc = 0.f;
+        if (r < nr) {
+          const int row = r0 + r;
+          if (row < s.split) {
+            const long long q = (long long)T.b * s.out_blk[0] + row;
+            const long long dst = s.out_perm ? __ldg(s.out_perm + q) : q;
+            p = reinterpret_cast<char*>(s.out_p[0] + dst * s.out_ld[0] + c0);
+            f = o.out_f64;
+            if (o.resb) pb = reinterpret_cast<const char*>(o.resb + dst * s.out_ld[0] + c0);
+          } else {
+            const long long q = (long long)T.b * s.out_blk[1] + (row - s.split);
+            p = reinterpret_cast<char*>(s.out_p[1] + q * s.out_ld[1] + c0);
+          }
+          sc = __ldg(o.rsc + (size_t)(T.b * o.ntile + T.rt) * NT + r);
+        }
+        outp[r] = p;
+        resp[r] = pb;
+        outf64[r] = f;
+        rs[r] = sc;
+      }
+      asm volatile("bar.sync 2, %0;" ::"r"(kEpiWarps * 32) : "memory");
+      const bool ok = mbar_wait(&cs_full[i & 1], (uint32_t)((i >> 1) & 1)) &&
+                      mbar_wait(&tmem_full, (uint32_t)(i & 1));
+      __syncwarp();
+      if (!__all_sync(0xffffffffu, ok)) {
+        if (lane == 0) {
+          e_fail = 1;
+          s_fail = 1;
+          if (o.err) atomicOr(o.err, 1u);
+        }
+        continue;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const bool cok = c0 + col < s.c;
+      // float64 outputs leave scaled back by 2^s_col
+      const int osh = (o.colbits && cok) ? col_shift(__ldg(o.colbits + c0 + col)) : 0;
+      const float csc = cscale[i & 1][col];
+      float rsq = 0.f;   // squared residual norm of this column (residual form)
+      for (int r8 = rh * 8; r8 < NT; r8 += 16) {
+        uint32_t v[kDig][8];
+#pragma unroll
+        for (int di = 0; di < kDig; ++di)
+          tmem_ld8(tmem + lanes + (uint32_t)(di * NT + r8), v[di]);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int i8 = 0; i8 < 8; ++i8) {
+          const int row = r8 + i8;
+          if (row >= nr || !cok) continue;
+          float a[kDig];
+#pragma unroll
+          for (int di = 0; di < kDig; ++di) a[di] = __uint_as_float(v[di][i8]);
+          float H, Lo;
+          diag_pair(diag_sum(a), H, Lo);
+          const float gs = __fmul_rn(rs[row], csc);   // a power of two, or 0
+          char* p = outp[row] + 8 * col;
+          if (outf64[row]) {
+            const int ge = (int)((__float_as_uint(gs) >> 23) & 255);
+            if (resp[row]) {
+              // r = b - S z in the row's scale 2^sh: b split into a float
+              // pair there (integer operations), one double-float
+              // subtraction, then back to float64 like the plain output
+              const int sh = ge ? ge - 127 + osh : osh;
+              const double bv = *reinterpret_cast<const double*>(resp[row] + 8 * col);
+              float bh, bl;
+              f64_split(bv, sh, bh, bl);
+              if (!ge) {
+                H = 0.f;
+                Lo = 0.f;
+              }
+              float rh, rl;
+              two_sum(bh, -H, rh, rl);
+              rl = __fadd_rn(rl, __fsub_rn(bl, Lo));
+              two_sum(rh, rl, rh, rl);
+              *reinterpret_cast<double*>(p) = pair_to_f64(rh, rl, sh);
+              const float rr = ge ? __fmul_rn(rh, gs) : rh;
+              rsq = __fmaf_rn(rr, rr, rsq);
+            } else {
+              *reinterpret_cast<double*>(p) = ge ? pair_to_f64(H, Lo, ge - 127 + osh) : 0.0;
+            }
+          } else {
+            *reinterpret_cast<float2*>(p) = make_float2(__fmul_rn(H, gs), __fmul_rn(Lo, gs));
+          }
+        }
+      }
+      // the accumulators and this tile's column scales may be reused
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) {
+        mbar_arrive(&tmem_empty);
+        mbar_arrive(&cs_free[i & 1]);
+      }
+      // rsq holds the column's squares scaled by 2^(-2 osh)
+      if (o.rnorm2 && cok && rsq > 0.f)
+        atomicAdd(o.rnorm2 + c0 + col, ldexp((double)rsq, 2 * osh));
+    }
   } else {
     // ---------------- digitiser warps (512 threads): thread (j, qk) owns
     // column j and the k of each chunk's quarter qk (8 k: one core-matrix row)
     const int j = tid & (kM - 1), qk = tid >> 7;
-    const bool col_ok = c0 + j < s.c;
-    const int csh = (o.colbits && col_ok) ? col_shift(__ldg(o.colbits + c0 + j)) : 0;
-    auto load = [&](int k, float& h, float& l) {
-      h = 0.f;
-      l = 0.f;
-      if (col_ok && k < w) {
-        const char* p = rowp[k] + 8 * j;
-        if (rowf64[k]) {
-          f64_split(*reinterpret_cast<const double*>(p), csh, h, l);
-        } else {
-          const float2 v = *reinterpret_cast<const float2*>(p);
-          h = v.x;
-          l = v.y;
+    int g = 0;
+    bool fail = false;
+    for (int i = 0; i < nt; ++i) {
+      const Tile T = tile_of(t0 + i, o.ntile, nct);
+      const int c0 = T.ct * kM;
+      // input row of every k (the first range optionally through the
+      // permutation); the previous tile's readers are done at this barrier
+      if (fail) d_fail = 1;
+      if (tid == 0 && s_fail) d_fail = 1;
+      asm volatile("bar.sync 1, %0;" ::"r"(kDigWarps * 32) : "memory");
+      if (d_fail) continue;   // the same for every digitiser warp
+      for (int k = tid; k < w; k += kDigWarps * 32) {
+        int q = 0, kk = k;
+        while (q + 1 < s.nin && kk >= s.in_rows[q]) kk -= s.in_rows[q++];
+        long long row = (long long)T.b * s.in_blk[q] + kk;
+        if (q == 0 && s.in_perm) row = __ldg(s.in_perm + row);
+        rowp[k] = reinterpret_cast<const char*>(s.in_p[q] + row * s.in_ld[q] + c0);
+        rowf64[k] = (q == 0 && o.in_f64) ? 1 : 0;
+      }
+      asm volatile("bar.sync 1, %0;" ::"r"(kDigWarps * 32) : "memory");
+      const bool col_ok = c0 + j < s.c;
+      const int csh = (o.colbits && col_ok) ? col_shift(__ldg(o.colbits + c0 + j)) : 0;
+      auto load = [&](int k, float& h, float& l) {
+        h = 0.f;
+        l = 0.f;
+        if (col_ok && k < w) {
+          const char* p = rowp[k] + 8 * j;
+          if (rowf64[k]) {
+            f64_split(*reinterpret_cast<const double*>(p), csh, h, l);
+          } else {
+            const float2 v = *reinterpret_cast<const float2*>(p);
+            h = v.x;
+            l = v.y;
+          }
+        }
+      };
+      // column scale: largest |h| over the column's k (8 loads in flight),
+      // chunks in reverse order so that chunk 0's values stay in registers
+      // for the first digitisation
+      float mx = 0.f;
+      float hv[8], lv[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) hv[u] = lv[u] = 0.f;
+      for (int c = nch - 1; c >= 0; --c) {
+        const int k0 = c * kKC + qk * 8;
+        if (k0 >= wP) continue;
+#pragma unroll
+        for (int u = 0; u < 8; ++u) load(k0 + u, hv[u], lv[u]);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) mx = fmaxf(mx, fabsf(hv[u]));
+      }
+      colmax[qk][j] = mx;
+      asm volatile("bar.sync 1, %0;" ::"r"(kDigWarps * 32) : "memory");
+      float inv = 1.f, cs = 0.f;   // 2^-F and 2^F of the column (0: zero column)
+      {
+        const float m =
+            fmaxf(fmaxf(colmax[0][j], colmax[1][j]), fmaxf(colmax[2][j], colmax[3][j]));
+        if (m > 0.f) {
+          int F = (int)((__float_as_uint(m) >> 23) & 255) - 126;   // m < 2^F
+          F = max(-100, min(100, F));
+          inv = __uint_as_float((unsigned)(127 - F) << 23);
+          cs = __uint_as_float((unsigned)(127 + F) << 23);
         }
       }
-    };
-    // column scale: largest |h| over the column's k (8 loads in flight),
-    // chunks in reverse order so that chunk 0's values stay in registers for
-    // the first digitisation
-    float mx = 0.f;
-    float hv[8], lv[8];
+      // publish the column scales for the epilogue (its tile i - 2 is done)
+      if (i >= 2 && !mbar_wait(&cs_free[i & 1], (uint32_t)(((i >> 1) - 1) & 1))) fail = true;
+      if (qk == 0) cscale[i & 1][j] = cs;
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&cs_full[i & 1]);
+      for (int c = 0; c < nch; ++c, ++g) {
+        const int b2 = g & 1;
+        const int k0 = c * kKC + qk * 8;
+        // the next chunk's loads go out before this chunk is digitised
+        float nh[8], nl[8];
+        const bool more = c + 1 < nch && k0 + kKC < wP;
 #pragma unroll
-    for (int u = 0; u < 8; ++u) hv[u] = lv[u] = 0.f;
-    for (int c = nch - 1; c >= 0; --c) {
-      const int k0 = c * kKC + qk * 8;
-      if (k0 >= wP) continue;
+        for (int u = 0; u < 8; ++u) {
+          nh[u] = 0.f;
+          nl[u] = 0.f;
+        }
+        if (more) {
 #pragma unroll
-      for (int u = 0; u < 8; ++u) load(k0 + u, hv[u], lv[u]);
-#pragma unroll
-      for (int u = 0; u < 8; ++u) mx = fmaxf(mx, fabsf(hv[u]));
-    }
-    colmax[qk][j] = mx;
-    asm volatile("bar.sync 1, %0;" ::"r"(kDigWarps * 32) : "memory");
-    float inv = 1.f, cs = 0.f;   // 2^-F and 2^F of the column (0: zero column)
-    {
-      const float m = fmaxf(fmaxf(colmax[0][j], colmax[1][j]), fmaxf(colmax[2][j], colmax[3][j]));
-      if (m > 0.f) {
-        int F = (int)((__float_as_uint(m) >> 23) & 255) - 126;   // m < 2^F
-        F = max(-100, min(100, F));
-        inv = __uint_as_float((unsigned)(127 - F) << 23);
-        cs = __uint_as_float((unsigned)(127 + F) << 23);
-      }
-    }
-    bool fail = false;
-    for (int c = 0; c < nch; ++c) {
-      const int b2 = c & 1;
-      const int k0 = c * kKC + qk * 8;
-      // the next chunk's loads go out before this chunk is digitised
-      float nh[8], nl[8];
-      const bool more = c + 1 < nch && k0 + kKC < wP;
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        nh[u] = 0.f;
-        nl[u] = 0.f;
-      }
-      if (more) {
-#pragma unroll
-        for (int u = 0; u < 8; ++u) load(k0 + kKC + u, nh[u], nl[u]);
-      }
-      if (c >= 2 && !mbar_wait(&zempty[b2], (uint32_t)((c >> 1) - 1) & 1u)) fail = true;
-      if (k0 < wP) {
-        {
+          for (int u = 0; u < 8; ++u) load(k0 + kKC + u, nh[u], nl[u]);
+        }
+        if (g >= 2 && !mbar_wait(&zempty[b2], (uint32_t)((g >> 1) - 1) & 1u)) fail = true;
+        if (k0 < wP) {
           uint32_t wd[kDig][4];
 #pragma unroll
           for (int u = 0; u < 8; ++u) {
@@ -554,15 +727,15 @@ __global__ void __launch_bounds__(kThreads, 1) oz_step_kernel(const OzStep o) {
             *reinterpret_cast<uint4*>(zb + (size_t)t * zsl) =
                 make_uint4(wd[t][0], wd[t][1], wd[t][2], wd[t][3]);
         }
-      }
-      // generic-proxy writes -> visible to the tensor cores; one arrival per warp
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&zfull[b2]);
+        // generic-proxy writes -> visible to the tensor cores; one arrival per warp
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&zfull[b2]);
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        hv[u] = nh[u];
-        lv[u] = nl[u];
+        for (int u = 0; u < 8; ++u) {
+          hv[u] = nh[u];
+          lv[u] = nl[u];
+        }
       }
     }
     sweep::launch_dependents();
@@ -570,77 +743,10 @@ __global__ void __launch_bounds__(kThreads, 1) oz_step_kernel(const OzStep o) {
       s_fail = 1;
       if (o.err) atomicOr(o.err, 1u);
     }
-
-    // ---------------- epilogue: warp (qd, rq) reads TMEM lanes 32 qd ..
-    // (its columns) and rows rq * 8 + 32 i of the tile
-    const bool ok = mbar_wait(&done_bar, 0);
-    __syncwarp();
-    const bool all_ok = __all_sync(0xffffffffu, ok) && !s_fail;
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (all_ok) {
-      const int qd = warp & 3, rq = warp >> 2;
-      const int col = qd * 32 + lane;
-      const bool cok = c0 + col < s.c;
-      // float64 outputs leave scaled back by 2^s_col
-      const int osh = (o.colbits && cok) ? col_shift(__ldg(o.colbits + c0 + col)) : 0;
-      const uint32_t lanes = (uint32_t)(qd * 32) << 16;
-      // col == tid % 128: this thread digitised column col, so cs is its scale
-      const float csc = cs;
-      float rsq = 0.f;   // squared residual norm of this column (residual form)
-      for (int r8 = rq * 8; r8 < NT; r8 += 32) {
-        uint32_t v[kDig][8];
-#pragma unroll
-        for (int di = 0; di < kDig; ++di)
-          tmem_ld8(tmem + lanes + (uint32_t)(di * NT + r8), v[di]);
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          const int row = r8 + i;
-          if (row >= nr || !cok) continue;
-          float a[kDig];
-#pragma unroll
-          for (int di = 0; di < kDig; ++di) a[di] = __uint_as_float(v[di][i]);
-          float H, Lo;
-          diag_pair(diag_sum(a), H, Lo);
-          const float g = __fmul_rn(rs[row], csc);   // a power of two, or 0
-          char* p = outp[row] + 8 * col;
-          if (outf64[row]) {
-            const int ge = (int)((__float_as_uint(g) >> 23) & 255);
-            if (resp[row]) {
-              // r = b - S z in the row's scale 2^sh: b split into a float
-              // pair there (integer operations), one double-float
-              // subtraction, then back to float64 like the plain output
-              const int sh = ge ? ge - 127 + osh : osh;
-              const double bv = *reinterpret_cast<const double*>(resp[row] + 8 * col);
-              float bh, bl;
-              f64_split(bv, sh, bh, bl);
-              if (!ge) {
-                H = 0.f;
-                Lo = 0.f;
-              }
-              float rh, rl;
-              two_sum(bh, -H, rh, rl);
-              rl = __fadd_rn(rl, __fsub_rn(bl, Lo));
-              two_sum(rh, rl, rh, rl);
-              *reinterpret_cast<double*>(p) = pair_to_f64(rh, rl, sh);
-              const float rr = ge ? __fmul_rn(rh, g) : __fmul_rn(rh, __uint_as_float(127u << 23));
-              rsq = __fmaf_rn(rr, rr, rsq);
-            } else {
-              *reinterpret_cast<double*>(p) = ge ? pair_to_f64(H, Lo, ge - 127 + osh) : 0.0;
-            }
-          } else {
-            *reinterpret_cast<float2*>(p) = make_float2(__fmul_rn(H, g), __fmul_rn(Lo, g));
-          }
-        }
-      }
-      // rsq holds the column's squares scaled by 2^(-2 osh)
-      if (o.rnorm2 && cok && rsq > 0.f)
-        atomicAdd(o.rnorm2 + c0 + col, ldexp((double)rsq, 2 * osh));
-    }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if (warp == kDigWarps)
+  if (warp == kMmaWarp)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols)
                  : "memory");
 }
@@ -751,10 +857,11 @@ void launch(cudaStream_t st, const sweep::Step<dfloat>& s, const OzOp& op, bool 
   o.resb = resb;
   o.rnorm2 = rnorm2;
   sweep::LaunchPlan p;
-  p.ctas = (long long)s.nb * op.ntile * ((s.c + kM - 1) / kM);
+  const long long ntiles = (long long)s.nb * op.ntile * ((s.c + kM - 1) / kM);
+  p.ctas = std::min<long long>(ntiles, num_sms());   // persistent: one CTA per SM
   p.threads = kThreads;
   p.smem = smem_bytes(op.NT, op.wP);
-  SLU_REQUIRE(p.ctas < (1LL << 31), "tensor-core sweep: step too large");
+  SLU_REQUIRE(ntiles < (1LL << 31), "tensor-core sweep: step too large");
   ensure_smem(reinterpret_cast<const void*>(oz_step_kernel), p.smem);
   sweep::launch_pdl(oz_step_kernel, p, st, what, o);
 }

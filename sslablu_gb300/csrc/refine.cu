@@ -38,11 +38,14 @@ struct RefinePlan {
 
 namespace {
 
-void enqueue_iteration(cudaStream_t st, const Hbs& H, RefinePlan& P, bool first) {
+// One refinement iteration.  Bc / Xc (leading dimension c) replace the plan's
+// B and X buffers when given (the tensor-core inner mode's direct path).
+void enqueue_iteration(cudaStream_t st, const Hbs& H, RefinePlan& P, bool first,
+                       const double* Bc = nullptr, double* Xc = nullptr) {
   const int N = H.N, c = P.c;
   const long long n = (long long)N * c;
-  double* B = P.B.as<double>();
-  double* X = P.X.as<double>();
+  const double* B = Bc ? Bc : P.B.as<double>();
+  double* X = Xc ? Xc : P.X.as<double>();
   double* r = P.r.as<double>();
   if (first) {
     if (P.inner == 2) {
@@ -187,10 +190,18 @@ void hbs_refine(Handle& h, Hbs& H, const double* B, int ldb, double* X, int ldx,
     if (!H.has_df) hbs_make_df(h, H);
   }
   RefinePlan& P = plan_for(h, H, c);
-  SLU_CHECK_CUDA(cudaMemcpy2DAsync(P.B.p, 8 * (size_t)c, B, 8 * (size_t)ldb, 8 * (size_t)c,
-                                   H.N, cudaMemcpyDeviceToDevice, st));
-  SLU_CHECK_CUDA(cudaGraphLaunch(P.first, st));
-  count_launches(P.first_kernels);
+  // the tensor-core mode on dense caller blocks runs its iterations straight
+  // on the caller's B and X: its launches are long enough that the graph's
+  // launch savings do not pay for staging copies of B and X
+  const bool direct = P.inner == 2 && ldb == c && ldx == c;
+  if (direct) {
+    enqueue_iteration(st, H, P, true, B, X);
+  } else {
+    SLU_CHECK_CUDA(cudaMemcpy2DAsync(P.B.p, 8 * (size_t)c, B, 8 * (size_t)ldb, 8 * (size_t)c,
+                                     H.N, cudaMemcpyDeviceToDevice, st));
+    SLU_CHECK_CUDA(cudaGraphLaunch(P.first, st));
+    count_launches(P.first_kernels);
+  }
   int it = 1;
   double worst = 0.0;
   for (;;) {
@@ -216,12 +227,17 @@ void hbs_refine(Handle& h, Hbs& H, const double* B, int ldb, double* X, int ldx,
       worst = std::max(worst, std::sqrt(rj) / (bj > 0 ? std::sqrt(bj) : 1.0));
     }
     if (worst <= tol || it >= maxit) break;
-    SLU_CHECK_CUDA(cudaGraphLaunch(P.next, st));
-    count_launches(P.next_kernels);
+    if (direct) {
+      enqueue_iteration(st, H, P, false, B, X);
+    } else {
+      SLU_CHECK_CUDA(cudaGraphLaunch(P.next, st));
+      count_launches(P.next_kernels);
+    }
     ++it;
   }
-  SLU_CHECK_CUDA(cudaMemcpy2DAsync(X, 8 * (size_t)ldx, P.X.p, 8 * (size_t)c, 8 * (size_t)c, H.N,
-                                   cudaMemcpyDeviceToDevice, st));
+  if (!direct)
+    SLU_CHECK_CUDA(cudaMemcpy2DAsync(X, 8 * (size_t)ldx, P.X.p, 8 * (size_t)c, 8 * (size_t)c,
+                                     H.N, cudaMemcpyDeviceToDevice, st));
   if (iters) *iters = it;
   if (relres) *relres = worst;
   if (worst > tol) throw Error(SLU_ERR_NOT_CONVERGED, "refinement did not reach the tolerance");

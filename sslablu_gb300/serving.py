@@ -409,6 +409,113 @@ def _build_hbs_ops(count, seed, sizes=(2048, 4096, 8192), shift=16.0):
     return ops
 
 
+def _build_dense_rb_ops(count, sizes=(128, 256)):
+    """C1-family operators: red-black factorisations of 2-D Laplace interface
+    systems (8 slabs, 7 interfaces of m points padded to 8 blocks, as
+    upstream's RedBlackSolver needs), their couplings made on the GPU by the
+    slab solves of multislab.slabmaps (every double slab of a uniform
+    Laplace geometry has the same maps).  Returns (key, solver, rows,
+    footprint)."""
+    from .direct_solve.omsdirectsolve import RedBlackSolver
+    from .multislab.slabmaps import SlabGeometry, SlabMaps
+    maps = {}
+    for m in sizes:
+        nx = int(round(0.25 * (m + 1))) | 1
+        g = SlabGeometry(8, nx, m + 2)
+        I = torch.eye(m, dtype=torch.float64, device="cuda")
+        sm = SlabMaps(g, [1], tol=1e-13)
+        Sl = sm.apply(I, None).cpu().numpy()
+        Sr = sm.apply(None, I).cpu().numpy()
+        maps[m] = (Sl, Sr)
+    ops = []
+    for j in range(count):
+        m = sizes[j % len(sizes)]
+        Sl, Sr = maps[m]
+        Z = np.zeros((m, m))
+        S = [[Z if i == 0 else Sl, Sr if i < 6 else Z] for i in range(7)] + [[Z, Z]]
+        rb = RedBlackSolver(m)
+        rb.factorize(S, [np.eye(m)] * 8)
+        rb.dense_system = _tridiag_dense(Sl, Sr, 7)   # for the residual check
+        ops.append(("rb%d_m%d" % (j, m), rb, 7 * m, 8 * 8 * m * m * 8))
+    return ops
+
+
+def _tridiag_dense(Sl, Sr, n):
+    m = Sl.shape[0]
+    M = np.eye(n * m)
+    for i in range(n):
+        if i > 0:
+            M[i * m:(i + 1) * m, (i - 1) * m:i * m] = Sl
+        if i < n - 1:
+            M[i * m:(i + 1) * m, (i + 1) * m:(i + 2) * m] = Sr
+    return M
+
+
+def rb_padded_solver(rb, m):
+    """Device solve of a red-black factorisation of 7 interfaces padded to 8."""
+    def solve(X):
+        Xp = torch.cat([X, torch.zeros((m, X.shape[1]), dtype=X.dtype, device=X.device)], 0)
+        return rb.solve(Xp.contiguous())[:7 * m]
+    return solve
+
+
+def mix_main(a):
+    """C5: resident operators from the C1 and C2/C3 families under one budget
+    (HBS interface operators of 2048-8192 points, red-black factorisations of
+    Laplace slab systems), served at several Poisson arrival rates; per rate
+    RHS/s, p50 / p99 latency and the worst residual of every result."""
+    import json
+    n_hbs = a.operators // 2
+    hbs = _build_hbs_ops(n_hbs, a.seed, shift=a.shift)
+    rbs = _build_dense_rb_ops(a.operators - n_hbs)
+    solvers = {}
+    sizes = {}
+    for key, H, n in hbs:
+        solvers[key] = (H, n, H.nbytes, "hbs")
+        sizes[key] = n
+    for key, rb, n, fp in rbs:
+        solvers[key] = (rb, n, fp, "rb")
+        sizes[key] = n
+    out = {"workload": "%d resident operators: %d exact-HBS interface operators (N in "
+                       "2048/4096/8192, leaf 64, rank 32) and %d red-black factorisations of "
+                       "2-D Laplace slab systems (7 x 128 / 7 x 256 points, couplings from the "
+                       "GPU slab solves); Poisson arrivals, 1-64 RHS per request"
+                       % (a.operators, n_hbs, a.operators - n_hbs),
+           "rates": []}
+    for rate in a.rates:
+        srv = SolveServer(budget_bytes=64 << 30, workers=a.workers, max_batch_rhs=a.max_batch)
+        try:
+            for key, (op, n, fp, kind) in solvers.items():
+                if kind == "hbs":
+                    srv.admit(key, lambda op=op: op, fp, lambda o: hbs_solver(o, "f64"))
+                else:
+                    m = n // 7
+                    srv.admit(key, lambda op=op: op, fp, lambda o, m=m: rb_padded_solver(o, m))
+            count = int(min(a.requests, max(200, rate * a.seconds)))
+            srv.run(poisson_trace(list(sizes), rate, min(200, count), seed=a.seed + 1,
+                                  sizes=sizes))
+            done = srv.run(poisson_trace(list(sizes), rate, count, seed=a.seed, sizes=sizes))
+            st = srv.stats()
+            worst = 0.0
+            for r in done:
+                if r.error is not None:
+                    continue
+                op, n, fp, kind = solvers[r.key]
+                if kind == "hbs":
+                    R = r.B - op.matmat(r.X)
+                else:
+                    R = r.B - op.dense_system @ r.X
+                worst = max(worst, float(np.max(np.linalg.norm(R, axis=0) /
+                                                np.linalg.norm(r.B, axis=0))))
+            st.update(rate=rate, worst_relres=worst,
+                      errors=sum(r.error is not None for r in done),
+                      offered_rhs_per_s=rate * 32.5)
+            out["rates"].append(st)
+        finally:
+            srv.close()
+    print(json.dumps(out))
+
+
 def main():
     import argparse
     import json
@@ -421,7 +528,15 @@ def main():
     ap.add_argument("--max-batch", type=int, default=64)
     ap.add_argument("--group-workers", type=int, default=8)
     ap.add_argument("--seed", type=int, default=20261205)
+    ap.add_argument("--mix", action="store_true",
+                    help="C5: operators of the C1 and C2/C3 families, swept over --rates")
+    ap.add_argument("--rates", type=lambda v: [float(x) for x in v.split(",")],
+                    default=[2000.0, 10000.0, 50000.0])
+    ap.add_argument("--seconds", type=float, default=1.0,
+                    help="--mix: trace length per rate (requests = rate * seconds)")
     a = ap.parse_args()
+    if a.mix:
+        return mix_main(a)
     ops = _build_hbs_ops(a.operators, a.seed, shift=a.shift)
     sizes = {k: n for k, _, n in ops}
     out = {"workload": "%d resident exact-HBS operators (N in 2048/4096/8192, leaf 64, rank 32, "

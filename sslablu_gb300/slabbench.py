@@ -155,11 +155,21 @@ def helmholtz(a):
       1. the slab maps S_l, S_r sampled on the GPU through batched slab solves
          (multislab.slabmaps; oms.compute_stmaps) and compressed by the rkHBS
          assembler (leaf a.leaf, rank a.rank; matAssembler.py:104-133);
-      2. RedBlackSolverHBS factorisation of the compressed interface system;
+      2. RedBlackSolverHBS factorisation of the compressed interface system
+         of wavenumber a.prec_kappa (the preconditioner's operator);
       3. 64 right-hand sides (smooth seeded interface data) solved by GMRES on
-         the exact interface operator (slab solves, float64) with the
-         red-black HBS solve as preconditioner, to a 1e-10 relative residual
-         (test/3D/cubeTest.py:158-186).
+         the exact interface operator of wavenumber a.kappa (slab solves,
+         float64) with the red-black HBS solve as preconditioner, to a 1e-10
+         relative residual (test/3D/cubeTest.py:158-186).
+    With prec_kappa = kappa this is upstream's iterative solve.  At k = 20
+    the weak-admissibility red-black HBS factorisation of the Helmholtz
+    couplings is unstable at moderate ranks -- the Schur complements it
+    compresses are near-singular, and compression errors are amplified by
+    their inverses; upstream's algorithm does the same, and its Thomas
+    variant is worse -- so the default preconditioner is the red-black HBS
+    factorisation of the Laplace interface system (prec_kappa = 0: a
+    shifted-Laplacian preconditioner for Helmholtz, after Erlangga, Vuik and
+    Oosterlee, Appl. Numer. Math. 50, 2004), which HBS compresses well.
     Reports the stage times, GMRES steps, residual against the exact
     operator, and the residual of the preconditioner alone."""
     from .direct_solve.omsdirectsolveHBS import RedBlackSolverHBS
@@ -167,6 +177,7 @@ def helmholtz(a):
     from .multislab.gmres import gmres
     from .multislab.slabmaps import SlabGeometry, StotOperator, slab_stmaps
     g = SlabGeometry(a.slabs, 5, a.n + 2, a.n + 2, kappa=a.kappa, coef=1)
+    gp = SlabGeometry(a.slabs, 5, a.n + 2, a.n + 2, kappa=a.prec_kappa, coef=1)
     m, nif = g.m, g.nif
     np.random.seed(20261207)
     asm = rkHMatAssembler(a.leaf, a.rank)
@@ -174,7 +185,7 @@ def helmholtz(a):
     t0 = time.perf_counter()
     S_rk = []
     t_sample = 0.0
-    for st_l, st_r in slab_stmaps(g):
+    for st_l, st_r in slab_stmaps(gp):
         row = []
         for st in (st_l, st_r):
             if st is not None:
@@ -222,8 +233,9 @@ def helmholtz(a):
     t_apply = _wall(lambda: St.dev_matmat(Bd), 3)[0]
     t_pre = _wall(lambda: rb.solve(Bd), 3)[0]
     return {"workload": "3-D Helmholtz k=%g, c = 1 + 0.5 sin sin sin, %d slabs, %d x %d "
-                        "interfaces (m=%d), 5-point slabs, rkHBS leaf %d rank %d"
-                        % (a.kappa, a.slabs, a.n, a.n, m, a.leaf, a.rank),
+                        "interfaces (m=%d), 5-point slabs, rkHBS leaf %d rank %d; "
+                        "preconditioner: red-black HBS of the k=%g interface system"
+                        % (a.kappa, a.slabs, a.n, a.n, m, a.leaf, a.rank, a.prec_kappa),
             "interfaces": nif, "m": m, "nrhs": a.nrhs,
             "maps_sample_compress_s": t_compress, "maps_sample_s": t_sample,
             "chebyshev_steps": St.maps.steps or None,
@@ -244,6 +256,8 @@ def main():
     ap.add_argument("--reps", type=int, default=10)
     ap.add_argument("--n", type=int, default=64, help="helmholtz: interface plane n x n")
     ap.add_argument("--kappa", type=float, default=20.0)
+    ap.add_argument("--prec-kappa", type=float, default=0.0,
+                    help="helmholtz: wavenumber of the preconditioner's interface system")
     ap.add_argument("--nrhs", type=int, default=64)
     a = ap.parse_args()
     if a.m is None:
