@@ -157,6 +157,21 @@ class RB_linop(_DevOp):
         return r
 
 
+class _SumOp(_DevOp):
+    """The sum of linear operators (both orientations)."""
+
+    def __init__(self, ops):
+        self.ops = ops
+        self.shape = tuple(ops[0].shape)
+
+    def _dev_apply(self, X, trans=False):
+        X = dv.as_2d(X)
+        r = dv.dev_apply(self.ops[0], X, trans).clone()
+        for op in self.ops[1:]:
+            r += dv.dev_apply(op, X, trans)
+        return r
+
+
 class Sprime_Linop(_DevOp):
     """I - Sl Sp^{-1} Sr, or I - Sl Sr when id=True (omsdirectsolveHBS.py:108-141)."""
 
@@ -374,12 +389,11 @@ class RedBlackSolverHBS(DirectSolver):
         nS = len(S_rk_list)
         if not (nS & (nS - 1) == 0 and nS != 0):
             raise ValueError("Number of slabs must be a power of 2.")
-        if self.cyclic:
-            raise NotImplementedError("cyclic red-black HBS is not provided")
         SiM = [s[0] for s in S_rk_list]
         SiP = [s[-1] for s in S_rk_list]
-        SiM[0] = _linop_from_mat(np.zeros((m, m)))
-        SiP[-1] = _linop_from_mat(np.zeros((m, m)))
+        if not self.cyclic:   # periodic: SiM[0] and SiP[-1] are the wrap couplings
+            SiM[0] = _linop_from_mat(np.zeros((m, m)))
+            SiP[-1] = _linop_from_mat(np.zeros((m, m)))
         if T is None:
             T = [id_op(m) for _ in range(nS)]
         RB = [(SiM, T, T, SiP)]
@@ -394,14 +408,21 @@ class RedBlackSolverHBS(DirectSolver):
         """omsdirectsolveHBS.py:436-483 (same compression order)."""
         SiM, T, Th, SiP = lev
         B_lin = []
+        cyc = self.cyclic
         for i in range(0, nS, 2):
-            spm = SiP[(i - 1) % nS] if i > 0 else None
-            smp = SiM[(i + 1) % nS] if i < nS - 1 else None
+            spm = SiP[(i - 1) % nS] if (i > 0 or cyc) else None
+            smp = SiM[(i + 1) % nS] if (i < nS - 1 or cyc) else None
             tm = Th[(i - 1) % nS] if spm is not None else None
             tp = Th[(i + 1) % nS] if smp is not None else None
             B_lin.append(RB_linop(T[i], tm, tp, SiP[i], SiM[i], smp, spm))
         A_lin = [STS_linop(SiM[i], Th[(i - 1) % nS], SiM[(i - 1) % nS]) for i in range(0, nS, 2)]
         C_lin = [STS_linop(SiP[i], Th[(i + 1) % nS], SiP[(i + 1) % nS]) for i in range(0, nS, 2)]
+        if cyc and nS == 2:
+            # one periodic block left: its couplings A, C act on the block
+            # itself, so the diagonal to compress is B + A + C (the dense
+            # solver's B_0 += A_0 + C_0, omsdirectsolve.py:326-327; upstream's
+            # HBS solver leaves A and C out of its last block)
+            B_lin = [_SumOp([B_lin[0], A_lin[0], C_lin[0]])]
         # upstream compresses T_new, then A, then C (one sketch pair each, in
         # that order); the compressions are independent of one another
         hs = self._hbs_many(B_lin + A_lin + C_lin, rk)
@@ -423,10 +444,12 @@ class RedBlackSolverHBS(DirectSolver):
             for j in range(nR):
                 i = 2 * j
                 c = vp[i * m:(i + 1) * m].clone()
-                if i > 0:
-                    c -= dv.dev_apply(SiM[i], dv.dev_solve(Th[i - 1], vp[(i - 1) * m:i * m]))
-                if i < nS - 1:
-                    c -= dv.dev_apply(SiP[i], dv.dev_solve(Th[i + 1], vp[(i + 1) * m:(i + 2) * m]))
+                if i > 0 or self.cyclic:
+                    q = (i - 1) % nS
+                    c -= dv.dev_apply(SiM[i], dv.dev_solve(Th[q], vp[q * m:(q + 1) * m]))
+                if i < nS - 1 or self.cyclic:
+                    q = (i + 1) % nS
+                    c -= dv.dev_apply(SiP[i], dv.dev_solve(Th[q], vp[q * m:(q + 1) * m]))
                 vn[j * m:(j + 1) * m] = c
             vs.append(vn)
         vs[-1] = dv.dev_solve(RB[-1][2][0], vs[-1])                     # coarsest
@@ -437,8 +460,9 @@ class RedBlackSolverHBS(DirectSolver):
                 i = 2 * j
                 vs[l - 1][i * m:(i + 1) * m] = vs[l][j * m:(j + 1) * m]
                 c = dv.dev_apply(SiM[i + 1], vs[l][j * m:(j + 1) * m])
-                if j + 1 < nR:
-                    c = c + dv.dev_apply(SiP[i + 1], vs[l][(j + 1) * m:(j + 2) * m])
+                if j + 1 < nR or self.cyclic:
+                    q = (j + 1) % nR
+                    c = c + dv.dev_apply(SiP[i + 1], vs[l][q * m:(q + 1) * m])
                 blk = vs[l - 1][(i + 1) * m:(i + 2) * m] - c
                 vs[l - 1][(i + 1) * m:(i + 2) * m] = dv.dev_solve(Th[i + 1], blk)
         return dv.finish(vs[0], rhs, one)
@@ -453,10 +477,12 @@ class RedBlackSolverHBS(DirectSolver):
         Y = torch.empty_like(X)
         for i in range(nS):
             y = dv.dev_apply(T[i], X[i * m:(i + 1) * m])
-            if i > 0:
-                y = y + dv.dev_apply(SiM[i], X[(i - 1) * m:i * m])
-            if i < nS - 1:
-                y = y + dv.dev_apply(SiP[i], X[(i + 1) * m:(i + 2) * m])
+            if i > 0 or self.cyclic:
+                q = (i - 1) % nS
+                y = y + dv.dev_apply(SiM[i], X[q * m:(q + 1) * m])
+            if i < nS - 1 or self.cyclic:
+                q = (i + 1) % nS
+                y = y + dv.dev_apply(SiP[i], X[q * m:(q + 1) * m])
             Y[i * m:(i + 1) * m] = y
         return dv.finish(Y, x, one)
 
