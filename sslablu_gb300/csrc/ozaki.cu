@@ -638,17 +638,32 @@ __global__ void __launch_bounds__(kThreads, 1) oz_step_kernel(const OzStep o) {
       // column scale: largest |h| over the column's k (8 loads in flight),
       // chunks in reverse order so that chunk 0's values stay in registers
       // for the first digitisation
+      // (the next chunk's loads are in flight while this chunk is scanned)
       float mx = 0.f;
       float hv[8], lv[8];
 #pragma unroll
       for (int u = 0; u < 8; ++u) hv[u] = lv[u] = 0.f;
-      for (int c = nch - 1; c >= 0; --c) {
-        const int k0 = c * kKC + qk * 8;
-        if (k0 >= wP) continue;
+      if ((nch - 1) * kKC + qk * 8 < wP) {
 #pragma unroll
-        for (int u = 0; u < 8; ++u) load(k0 + u, hv[u], lv[u]);
+        for (int u = 0; u < 8; ++u) load((nch - 1) * kKC + qk * 8 + u, hv[u], lv[u]);
+      }
+      for (int c = nch - 1; c >= 0; --c) {
+        float ph[8], pl[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) ph[u] = pl[u] = 0.f;
+        if (c > 0 && (c - 1) * kKC + qk * 8 < wP) {
+#pragma unroll
+          for (int u = 0; u < 8; ++u) load((c - 1) * kKC + qk * 8 + u, ph[u], pl[u]);
+        }
 #pragma unroll
         for (int u = 0; u < 8; ++u) mx = fmaxf(mx, fabsf(hv[u]));
+        if (c > 0) {
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            hv[u] = ph[u];
+            lv[u] = pl[u];
+          }
+        }
       }
       colmax[qk][j] = mx;
       asm volatile("bar.sync 1, %0;" ::"r"(kDigWarps * 32) : "memory");

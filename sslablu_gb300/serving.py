@@ -80,18 +80,21 @@ class Resident:
 
 
 def hbs_solver(H, precision="f64", tol=1e-10, maxit=10):
-    """Device solve callable for a factored HBSMAT (ULV).  The mixed path pads
+    """Device solve callable for a factored HBSMAT (ULV).  The mixed paths pad
     a batch to a power-of-two column count (zero columns converge at once) so
-    each operator keeps only a few refinement plans (CUDA graphs)."""
+    each operator keeps only a few refinement plans.  precision 'tensor'
+    refines the tensor-core sweep (it pays from a few hundred columns per
+    batch); 'mixed' the double-float sweep."""
     if precision == "f64":
         return lambda X: H._dev_solve(X, False)
+    inner = "tensor" if precision == "tensor" else "dfloat"
 
     def mixed(X):
         c = X.shape[1]
         w = 1 << (c - 1).bit_length()
         if w != c:
             X = torch.cat([X, torch.zeros((X.shape[0], w - c), dtype=X.dtype, device=X.device)], 1)
-        x, _, _ = H.solve_refined(X.contiguous(), tol=tol, maxit=maxit)
+        x, _, _ = H.solve_refined(X.contiguous(), tol=tol, maxit=maxit, inner=inner)
         return x[:, :c]
     return mixed
 
@@ -481,13 +484,14 @@ def mix_main(a):
                        "2-D Laplace slab systems (7 x 128 / 7 x 256 points, couplings from the "
                        "GPU slab solves); Poisson arrivals, 1-64 RHS per request"
                        % (a.operators, n_hbs, a.operators - n_hbs),
-           "rates": []}
+           "hbs_precision": a.hbs_precision, "max_batch_rhs": a.max_batch, "rates": []}
     for rate in a.rates:
         srv = SolveServer(budget_bytes=64 << 30, workers=a.workers, max_batch_rhs=a.max_batch)
         try:
             for key, (op, n, fp, kind) in solvers.items():
                 if kind == "hbs":
-                    srv.admit(key, lambda op=op: op, fp, lambda o: hbs_solver(o, "f64"))
+                    srv.admit(key, lambda op=op: op, fp,
+                              lambda o: hbs_solver(o, a.hbs_precision))
                 else:
                     m = n // 7
                     srv.admit(key, lambda op=op: op, fp, lambda o, m=m: rb_padded_solver(o, m))
@@ -534,6 +538,8 @@ def main():
                     default=[2000.0, 10000.0, 50000.0])
     ap.add_argument("--seconds", type=float, default=1.0,
                     help="--mix: trace length per rate (requests = rate * seconds)")
+    ap.add_argument("--hbs-precision", default="f64", choices=["f64", "mixed", "tensor"],
+                    help="--mix: solve path of the HBS operators")
     a = ap.parse_args()
     if a.mix:
         return mix_main(a)
