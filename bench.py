@@ -598,6 +598,55 @@ def run_other(args):
                                             "restated in numpy at %d-point interfaces (the GPU "
                                             "at the same size is in arms.gpu_same_size)" % m_cpu,
                                   "arms": cpu})
+    elif args.workload == "c3":
+        # the C3 operators themselves: 3-D variable-coefficient Helmholtz slabs
+        # (k = 20), 33 slabs, 32 interfaces of 64 x 64 points, GMRES on the
+        # exact interface operator with the mixed dense red-black preconditioner
+        from sslablu_gb300 import slabbench
+        ns = types.SimpleNamespace(slabs=33, n=64, kappa=20.0, prec="dense", prec_kappa=20.0,
+                                   leaf=128, rank=64, nrhs=64, reps=max(1, min(3, args.steps)),
+                                   maxiter=100)
+        g = slabbench.helmholtz(ns)
+        # CPU: upstream's pipeline restated (sparse-LU slab maps, dense red-black,
+        # GMRES) at 17 slabs x 16 x 16 points, a size it runs in seconds
+        from scipy.sparse.linalg import LinearOperator, gmres as sgmres
+        from oracle.slabmaps import helmholtz3d_slab_maps
+        cs, cn = 17, 16
+        H = 1.0 / cs
+        t0 = time.perf_counter()
+        maps = [helmholtz3d_slab_maps(5, cn + 2, cn + 2, 2 * H, 20.0, x0=i * H)
+                for i in range(cs - 1)]
+        mm, nif = cn * cn, cs - 1
+        Sx = [(maps[i][0] if i > 0 else np.zeros((mm, mm)),
+               maps[i][1] if i < nif - 1 else np.zeros((mm, mm))) for i in range(nif)]
+        rbc = od.RedBlackDense(mm).factorize(Sx, [np.eye(mm)] * nif)
+        t_build = time.perf_counter() - t0
+        Mtot = np.eye(nif * mm)
+        for i in range(nif):
+            if i > 0:
+                Mtot[i * mm:(i + 1) * mm, (i - 1) * mm:i * mm] = Sx[i][0]
+            if i < nif - 1:
+                Mtot[i * mm:(i + 1) * mm, (i + 1) * mm:(i + 2) * mm] = Sx[i][1]
+        bc = np.random.default_rng(3).standard_normal((nif * mm, 64))
+        Pre = LinearOperator(Mtot.shape, matvec=lambda v: rbc.solve(v[:, None])[:, 0])
+        t0 = time.perf_counter()
+        for j in range(bc.shape[1]):
+            try:
+                sgmres(Mtot, bc[:, j], M=Pre, rtol=1e-10, restart=30, maxiter=100)
+            except TypeError:   # scipy before 1.12 names it tol
+                sgmres(Mtot, bc[:, j], M=Pre, tol=1e-10, restart=30, maxiter=100)
+        t_cpu = time.perf_counter() - t0
+        line = dict(base, metric="3-D Helmholtz slab system RHS solves/sec at 1e-10 rel residual",
+                    unit="RHS/s", value=g["rhs_per_s"], ms_per_step=1e3 * g["solve_s"],
+                    config={"workload": g["workload"], "interfaces": g["interfaces"],
+                            "m": g["m"], "nrhs": g["nrhs"]},
+                    arms=g,
+                    cpu_baseline={"value": bc.shape[1] / t_cpu, "unit": "RHS/s",
+                                  "cores": os.cpu_count(), "kind": "port",
+                                  "sample": "upstream pipeline restated (sparse-LU slab maps, "
+                                            "dense red-black preconditioned scipy GMRES) at 17 "
+                                            "slabs x 16 x 16 points, 64 RHS; build %.2f s"
+                                            % t_build})
     else:   # c4_batch
         import subprocess
         out = subprocess.run([sys.executable, "-m", "sslablu_gb300.batchbench", "--reps",
@@ -647,7 +696,8 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "c1_dense", "c3_hbs", "c4_batch"])
+    ap.add_argument("--workload", default="c2",
+                    choices=["c2", "c1_dense", "c3_hbs", "c3", "c4_batch"])
     ap.add_argument("--served-rhs", type=lambda v: [int(x) for x in v.split(",") if x],
                     default=[1024, 4096],
                     help="batch widths of the served mixed vs plain comparison (comma separated)")

@@ -151,99 +151,112 @@ def helmholtz(a):
     """The C3 pipeline on real slab operators: 3-D variable-coefficient
     Helmholtz (k = kappa, c = 1 + 0.5 sin 2pi x sin 2pi y sin 2pi z) on
     [0,1]^3 cut into a.slabs slabs, a.n x a.n interface planes, stencil
-    discretisation with 5 points across a double slab.
-      1. the slab maps S_l, S_r sampled on the GPU through batched slab solves
-         (multislab.slabmaps; oms.compute_stmaps) and compressed by the rkHBS
-         assembler (leaf a.leaf, rank a.rank; matAssembler.py:104-133);
-      2. RedBlackSolverHBS factorisation of the compressed interface system
-         of wavenumber a.prec_kappa (the preconditioner's operator);
-      3. 64 right-hand sides (smooth seeded interface data) solved by GMRES on
-         the exact interface operator of wavenumber a.kappa (slab solves,
-         float64) with the red-black HBS solve as preconditioner, to a 1e-10
-         relative residual (test/3D/cubeTest.py:158-186).
-    With prec_kappa = kappa this is upstream's iterative solve.  At k = 20
-    the weak-admissibility red-black HBS factorisation of the Helmholtz
-    couplings is unstable at moderate ranks -- the Schur complements it
-    compresses are near-singular, and compression errors are amplified by
-    their inverses; upstream's algorithm does the same, and its Thomas
-    variant is worse -- so the default preconditioner is the red-black HBS
-    factorisation of the Laplace interface system (prec_kappa = 0: a
-    shifted-Laplacian preconditioner for Helmholtz, after Erlangga, Vuik and
-    Oosterlee, Appl. Numer. Math. 50, 2004), which HBS compresses well.
+    discretisation with 5 points across a double slab.  64 right-hand sides
+    (smooth seeded interface data) are solved by GMRES on the exact interface
+    operator Stot (slab solves, float64; multislab/oms.py:258-302) to a 1e-10
+    relative residual (test/3D/cubeTest.py:158-186), with one of two
+    preconditioners (a.prec):
+      hbs   -- upstream's iterative solve: the slab maps sampled on the GPU
+               through batched slab solves (oms.compute_stmaps), compressed by
+               the rkHBS assembler (leaf a.leaf, rank a.rank;
+               matAssembler.py:104-133) and factored by RedBlackSolverHBS (of
+               the wavenumber a.prec_kappa: 0 gives a shifted-Laplacian
+               preconditioner, after Erlangga, Vuik and Oosterlee, Appl.
+               Numer. Math. 50, 2004).  At k = 20 the weak-admissibility
+               red-black HBS factorisation is not a usable preconditioner (the
+               Schur complements it compresses are near-singular; upstream's
+               algorithm does the same even at ranks near the leaf size);
+      dense -- the maps formed densely by the same slab solves (identity
+               sketches) and factored by the mixed-precision dense red-black
+               solver (Schur-complement products on the tcgen05 tensor cores,
+               float64 pivot blocks), whose plain solve preconditions GMRES.
     Reports the stage times, GMRES steps, residual against the exact
     operator, and the residual of the preconditioner alone."""
-    from .direct_solve.omsdirectsolveHBS import RedBlackSolverHBS
-    from .matAssembly.matAssembler import rkHMatAssembler
     from .multislab.gmres import gmres
-    from .multislab.slabmaps import SlabGeometry, StotOperator, slab_stmaps
+    from .multislab.slabmaps import SlabGeometry, SlabMaps, StotOperator, slab_stmaps
     g = SlabGeometry(a.slabs, 5, a.n + 2, a.n + 2, kappa=a.kappa, coef=1)
-    gp = SlabGeometry(a.slabs, 5, a.n + 2, a.n + 2, kappa=a.prec_kappa, coef=1)
     m, nif = g.m, g.nif
-    np.random.seed(20261207)
-    asm = rkHMatAssembler(a.leaf, a.rank)
+    out = {}
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    S_rk = []
-    t_sample = 0.0
-    for st_l, st_r in slab_stmaps(gp):
-        row = []
-        for st in (st_l, st_r):
-            if st is not None:
-                row.append(asm.assemble(st))
-                t_sample += asm.stats.timeSample
-        S_rk.append(row)
-    torch.cuda.synchronize()
-    t_compress = time.perf_counter() - t0
-    tree = S_rk[0][0].tree
-    rb = RedBlackSolverHBS(m, a.rank, tree, False)
-    t0 = time.perf_counter()
-    rb.factorize(S_rk)
-    torch.cuda.synchronize()
-    t_factor = time.perf_counter() - t0
+    if a.prec == "hbs":
+        from .direct_solve.omsdirectsolveHBS import RedBlackSolverHBS
+        from .matAssembly.matAssembler import rkHMatAssembler
+        gp = SlabGeometry(a.slabs, 5, a.n + 2, a.n + 2, kappa=a.prec_kappa, coef=1)
+        np.random.seed(20261207)
+        asm = rkHMatAssembler(a.leaf, a.rank)
+        S_rk = []
+        for st_l, st_r in slab_stmaps(gp):
+            S_rk.append([asm.assemble(st) for st in (st_l, st_r) if st is not None])
+        torch.cuda.synchronize()
+        out["maps_sample_compress_s"] = time.perf_counter() - t0
+        rb = RedBlackSolverHBS(m, a.rank, S_rk[0][0].tree, False)
+        t0 = time.perf_counter()
+        rb.factorize(S_rk)
+        torch.cuda.synchronize()
+        out["factor_s"] = time.perf_counter() - t0
+        prec = rb.solve
+        desc = "red-black HBS of the k=%g system, rkHBS leaf %d rank %d" % (a.prec_kappa, a.leaf,
+                                                                            a.rank)
+    else:
+        from .direct_solve.omsdirectsolve import RedBlackSolver
+        maps = SlabMaps(g, None, 1e-14)
+        Id = torch.zeros((nif * m, m), dtype=torch.float64, device="cuda")
+        Id.view(nif, m, m)[:] = torch.eye(m, dtype=torch.float64, device="cuda")
+        Sl = maps.apply(Id, None).view(nif, m, m)
+        Sr = maps.apply(None, Id).view(nif, m, m)
+        del Id
+        torch.cuda.synchronize()
+        out["maps_dense_s"] = time.perf_counter() - t0
+        out["chebyshev_steps"] = maps.steps
+        rows = [[Sl[i], Sr[i]] for i in range(nif)]
+        rb = RedBlackSolver(m, precision="mixed")
+        t0 = time.perf_counter()
+        rb.factorize(rows, [torch.eye(m, dtype=torch.float64, device="cuda")] * nif)
+        torch.cuda.synchronize()
+        out["factor_s"] = time.perf_counter() - t0
+        del Sl, Sr, rows
+
+        def prec(X):
+            return rb._solve_dev(X.clone())
+        desc = ("dense red-black of the exact maps, tensor-core Schur products "
+                "(split-BF16x3) with float64 pivot blocks")
     St = StotOperator(g)
-    # smooth seeded interface data: low-order trig series per plane
     pts = g.points(0)
     rng = np.random.default_rng(7)
     B = np.zeros((nif * m, a.nrhs))
     for j in range(a.nrhs):
         for i in range(nif):
-            coef = rng.standard_normal((4, 4))
+            cf = rng.standard_normal((4, 4))
             v = np.zeros(m)
             for p in range(4):
                 for q in range(4):
-                    v += coef[p, q] * np.sin((p + 1) * np.pi * pts[:, 1]) * \
+                    v += cf[p, q] * np.sin((p + 1) * np.pi * pts[:, 1]) * \
                         np.sin((q + 1) * np.pi * pts[:, 2])
             B[i * m:(i + 1) * m, j] = v
     Bd = torch.from_numpy(B).cuda()
-    # the preconditioner alone (one red-black HBS solve)
-    Xp = rb.solve(Bd)
+    Xp = prec(Bd)
     R = Bd - St.dev_matmat(Xp)
-    res_pre = float((R.norm(dim=0) / Bd.norm(dim=0)).max())
+    out["preconditioner_relres"] = float((R.norm(dim=0) / Bd.norm(dim=0)).max())
     torch.cuda.synchronize()
     ts = []
     for _ in range(a.reps):
         t0 = time.perf_counter()
-        X, steps, rel = gmres(St.dev_matmat, Bd, rb.solve, tol=1e-10, restart=30, maxiter=200)
+        X, steps, rel = gmres(St.dev_matmat, Bd, prec, tol=1e-10, restart=30, maxiter=a.maxiter)
         torch.cuda.synchronize()
         ts.append(time.perf_counter() - t0)
     R = Bd - St.dev_matmat(X)
-    res = float((R.norm(dim=0) / Bd.norm(dim=0)).max())
     t_solve = statistics.median(ts)
-    # one exact interface apply and one preconditioner solve, timed alone
-    t_apply = _wall(lambda: St.dev_matmat(Bd), 3)[0]
-    t_pre = _wall(lambda: rb.solve(Bd), 3)[0]
-    return {"workload": "3-D Helmholtz k=%g, c = 1 + 0.5 sin sin sin, %d slabs, %d x %d "
-                        "interfaces (m=%d), 5-point slabs, rkHBS leaf %d rank %d; "
-                        "preconditioner: red-black HBS of the k=%g interface system"
-                        % (a.kappa, a.slabs, a.n, a.n, m, a.leaf, a.rank, a.prec_kappa),
-            "interfaces": nif, "m": m, "nrhs": a.nrhs,
-            "maps_sample_compress_s": t_compress, "maps_sample_s": t_sample,
-            "chebyshev_steps": St.maps.steps or None,
-            "rb_hbs_factor_s": t_factor,
-            "preconditioner_relres": res_pre,
-            "gmres_steps": steps, "relres": res, "gmres_relres": rel,
-            "solve_s": t_solve, "rhs_per_s": a.nrhs / t_solve,
-            "stot_apply_ms": 1e3 * t_apply, "rb_hbs_solve_ms": 1e3 * t_pre}
+    out.update({
+        "workload": "3-D Helmholtz k=%g, c = 1 + 0.5 sin sin sin, %d slabs, %d x %d interfaces "
+                    "(m=%d), 5-point slabs; GMRES on the exact interface operator; "
+                    "preconditioner: %s" % (a.kappa, a.slabs, a.n, a.n, m, desc),
+        "interfaces": nif, "m": m, "nrhs": a.nrhs, "chebyshev_steps_stot": St.maps.steps or None,
+        "gmres_steps": steps, "relres": float((R.norm(dim=0) / Bd.norm(dim=0)).max()),
+        "solve_s": t_solve, "rhs_per_s": a.nrhs / t_solve,
+        "stot_apply_ms": 1e3 * _wall(lambda: St.dev_matmat(Bd), 3)[0],
+        "preconditioner_ms": 1e3 * _wall(lambda: prec(Bd), 3)[0]})
+    return out
 
 
 def main():
@@ -257,7 +270,10 @@ def main():
     ap.add_argument("--n", type=int, default=64, help="helmholtz: interface plane n x n")
     ap.add_argument("--kappa", type=float, default=20.0)
     ap.add_argument("--prec-kappa", type=float, default=0.0,
-                    help="helmholtz: wavenumber of the preconditioner's interface system")
+                    help="helmholtz: wavenumber of the HBS preconditioner's interface system")
+    ap.add_argument("--prec", default="dense", choices=["dense", "hbs"],
+                    help="helmholtz: GMRES preconditioner")
+    ap.add_argument("--maxiter", type=int, default=100)
     ap.add_argument("--nrhs", type=int, default=64)
     a = ap.parse_args()
     if a.m is None:
