@@ -342,6 +342,11 @@ int slu_rb_factor(slu_handle_t h, int nblk, int m, const double* SiM, const doub
                   const double* T, slu_rb_t* out);
 /* B (nblk*m x nrhs, ldb) <- solution, in place. */
 int slu_rb_solve(slu_handle_t h, slu_rb_t rb, double* B, int ldb, int nrhs);
+/* The red-black solve with its block products on the tcgen05 tensor cores
+ * (split-BF16x3 GEMMs, float32-level accuracy; B in place): a fast
+ * approximate solve for preconditioning an iterative solve of the exact
+ * operator (no upstream counterpart).  Any factorisation of slu_rb_factor*. */
+int slu_rb_solve_tc(slu_handle_t h, slu_rb_t rb, double* B, int ldb, int nrhs);
 /* Periodic red-black (RedBlackSolver with cyclic=True,
  * direct_solve/omsdirectsolve.py:207-209, 249-250, 269-272, 315-327): as
  * slu_rb_factor, with SiM[0] coupling block 0 to block nblk-1 and

@@ -74,6 +74,7 @@ SIGNATURES = {
     "slu_thomas_solve": [P, P, P, c_int, c_int],
     "slu_fp64_peak": [P, c_int, P, P],
     "slu_rb_factor_cyclic": [P, c_int, c_int, P, P, P, ctypes.POINTER(c_void_p)],
+    "slu_rb_solve_tc": [P, P, P, c_int, c_int],
     "slu_slab_maps_apply": [P, c_int, c_int, c_int, c_double, c_double, c_int, c_int, P, P, P,
                             c_int, P, P, c_int, c_int, c_int, c_double, P],
     "slu_hbs_prepare_ozaki": [P, P],

@@ -647,6 +647,15 @@ int slu_rb_factor_cyclic(slu_handle_t h, int nblk, int m, const double* SiM, con
   });
 }
 
+int slu_rb_solve_tc(slu_handle_t h, slu_rb_t rb, double* B, int ldb, int nrhs) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h && rb && B, "null argument");
+    SLU_REQUIRE(!rb->thomas, "handle was made by slu_thomas_factor");
+    SLU_REQUIRE(nrhs >= 1 && ldb >= nrhs, "bad right-hand side shape");
+    slu::rb_solve(h->h, rb->S, B, ldb, nrhs, true);
+  });
+}
+
 int slu_rb_factor_mixed(slu_handle_t h, int nblk, int m, const double* SiM, const double* SiP,
                         const double* T, slu_rb_t* out) {
   return guard(h, [&] {

@@ -285,8 +285,8 @@ void rb_factor(Handle& h, RbSolver& S, int nblk, int m, const double* SiM, const
   if (m <= kRbFusedMax && !cyclic) build_fused_ops(st, S);
 }
 
-void rb_solve(Handle& h, const RbSolver& S, double* B, int ldb, int c) {
-  if (S.fused) {
+void rb_solve(Handle& h, const RbSolver& S, double* B, int ldb, int c, bool tc) {
+  if (S.fused && !tc) {
     rb_solve_fused(h, S, B, ldb, c);
     return;
   }
@@ -297,32 +297,42 @@ void rb_solve(Handle& h, const RbSolver& S, double* B, int ldb, int c) {
   // v[l]: nS_l * m x c
   size_t tot = 0;
   for (const RbLevel& L : S.levels) tot += (size_t)L.nS * mc;
-  h.ws.reserve(8 * (tot + (size_t)nblk / 2 * mc + mc) + 8 * 256, st);
+  const size_t tcb = tc ? tc_gemm_workspace_bytes(m, c, m) : 0;
+  h.ws.reserve(8 * (tot + (size_t)nblk / 2 * mc + mc) + tcb + 8 * 256, st);
   std::vector<double*> v(nL);
   for (int l = 0; l < nL; ++l) v[l] = h.ws.take<double>((size_t)S.levels[l].nS * mc);
   double* z = h.ws.take<double>(std::max<size_t>(1, (size_t)nblk / 2) * mc);
+  void* tcws = tc ? h.ws.take<char>(tcb) : nullptr;
+  unsigned int* err = reinterpret_cast<unsigned int*>(h.info.as<int>()) + 1;
+  // C_b = alpha A_b V_b + beta C_b for b < batch (A_b m x m, V_b and C_b m x c):
+  // float64 batched GEMM, or with `tc` split-BF16x3 tensor-core products
+  auto G = [&](double alpha, const double* A, long long sA, const double* V, long long sV,
+               double beta, double* C, long long sC, int batch) {
+    if (!tc) {
+      gemm_batched<double>(st, false, false, m, c, m, alpha, A, m, sA, 0, V, c, sV, 0, beta, C, c,
+                           sC, 0, batch);
+      return;
+    }
+    for (int b = 0; b < batch; ++b)
+      tc_gemm_split3(st, m, c, m, alpha, A + b * sA, m, V + b * sV, c, beta, C + b * sC, c, tcws,
+                     err);
+  };
   copy_batched<double>(st, nblk * m, c, B, ldb, 0, 0, v[0], c, 0, 0, 1);
   // forward reduction (omsdirectsolve.py:238-258)
   for (int l = 0; l + 1 < nL; ++l) {
     const RbLevel& P = S.levels[l];
     const int nR = P.nS / 2;
     // z_o = T_o^{-1} v_o (odd o)
-    gemm_batched<double>(st, false, false, m, c, m, 1.0, dp(P.Inv) + mm, m, 2 * mm, 0, v[l] + mc,
-                         c, 2 * mc, 0, 0.0, z, c, mc, 0, nR);
+    G(1.0, dp(P.Inv) + mm, 2 * mm, v[l] + mc, 2 * mc, 0.0, z, mc, nR);
     // v'_j = v_{2j} - SiM_{2j} z_{2j-1} - SiP_{2j} z_{2j+1}
     copy_batched<double>(st, m, c, v[l], c, 2 * mc, 0, v[l + 1], c, mc, 0, nR);
-    if (nR > 1)
-      gemm_batched<double>(st, false, false, m, c, m, -1.0, dp(P.SiM) + 2 * mm, m, 2 * mm, 0, z, c,
-                           mc, 0, 1.0, v[l + 1] + mc, c, mc, 0, nR - 1);
-    gemm_batched<double>(st, false, false, m, c, m, -1.0, dp(P.SiP), m, 2 * mm, 0, z, c, mc, 0,
-                         1.0, v[l + 1], c, mc, 0, nR);
+    if (nR > 1) G(-1.0, dp(P.SiM) + 2 * mm, 2 * mm, z, mc, 1.0, v[l + 1] + mc, mc, nR - 1);
+    G(-1.0, dp(P.SiP), 2 * mm, z, mc, 1.0, v[l + 1], mc, nR);
     if (S.cyclic)   // v'_0 -= SiM_0 z_{last odd}
-      gemm_batched<double>(st, false, false, m, c, m, -1.0, dp(P.SiM), m, 0, 0,
-                           z + (size_t)(nR - 1) * mc, c, 0, 0, 1.0, v[l + 1], c, 0, 0, 1);
+      G(-1.0, dp(P.SiM), 0, z + (size_t)(nR - 1) * mc, 0, 1.0, v[l + 1], 0, 1);
   }
   // coarsest block (omsdirectsolve.py:261)
-  gemm_batched<double>(st, false, false, m, c, m, 1.0, dp(S.levels[nL - 1].Inv), m, 0, 0,
-                       v[nL - 1], c, 0, 0, 0.0, z, c, 0, 0, 1);
+  G(1.0, dp(S.levels[nL - 1].Inv), 0, v[nL - 1], 0, 0.0, z, 0, 1);
   copy_batched<double>(st, m, c, z, c, 0, 0, v[nL - 1], c, 0, 0, 1);
   // back substitution (omsdirectsolve.py:263-277)
   for (int l = nL - 1; l > 0; --l) {
@@ -330,17 +340,12 @@ void rb_solve(Handle& h, const RbSolver& S, double* B, int ldb, int c) {
     const int nR = P.nS / 2;
     // odd blocks first use the coarse (even) solution still stored in v[l]
     // g_o = v_o - SiM_o x_{o-1} - SiP_o x_{o+1}
-    gemm_batched<double>(st, false, false, m, c, m, -1.0, dp(P.SiM) + mm, m, 2 * mm, 0, v[l], c, mc,
-                         0, 1.0, v[l - 1] + mc, c, 2 * mc, 0, nR);
-    if (nR > 1)
-      gemm_batched<double>(st, false, false, m, c, m, -1.0, dp(P.SiP) + mm, m, 2 * mm, 0,
-                           v[l] + mc, c, mc, 0, 1.0, v[l - 1] + mc, c, 2 * mc, 0, nR - 1);
+    G(-1.0, dp(P.SiM) + mm, 2 * mm, v[l], mc, 1.0, v[l - 1] + mc, 2 * mc, nR);
+    if (nR > 1) G(-1.0, dp(P.SiP) + mm, 2 * mm, v[l] + mc, mc, 1.0, v[l - 1] + mc, 2 * mc, nR - 1);
     if (S.cyclic)   // the last odd block's right neighbour is block 0
-      gemm_batched<double>(st, false, false, m, c, m, -1.0,
-                           dp(P.SiP) + (2 * (size_t)nR - 1) * mm, m, 0, 0, v[l], c, 0, 0, 1.0,
-                           v[l - 1] + (2 * (size_t)nR - 1) * mc, c, 0, 0, 1);
-    gemm_batched<double>(st, false, false, m, c, m, 1.0, dp(P.Inv) + mm, m, 2 * mm, 0,
-                         v[l - 1] + mc, c, 2 * mc, 0, 0.0, z, c, mc, 0, nR);
+      G(-1.0, dp(P.SiP) + (2 * (size_t)nR - 1) * mm, 0, v[l], 0, 1.0,
+        v[l - 1] + (2 * (size_t)nR - 1) * mc, 0, 1);
+    G(1.0, dp(P.Inv) + mm, 2 * mm, v[l - 1] + mc, 2 * mc, 0.0, z, mc, nR);
     copy_batched<double>(st, m, c, z, c, mc, 0, v[l - 1] + mc, c, 2 * mc, 0, nR);
     copy_batched<double>(st, m, c, v[l], c, mc, 0, v[l - 1], c, 2 * mc, 0, nR);
   }

@@ -38,7 +38,9 @@ void rb_apply(Handle& h, const RbSolver& S, const double* X, int ldx, double* Y,
 // Refinement of A x = b with the (mixed) factors and a float64 residual.
 void rb_refine(Handle& h, const RbSolver& S, const double* B, int ldb, double* X, int ldx,
                int nrhs, double tol, int maxit, int* iters, double* relres);
-void rb_solve(Handle& h, const RbSolver& S, double* B, int ldb, int nrhs);
+// tc: the block products as split-BF16x3 tensor-core GEMMs (float32
+// accuracy: a preconditioner-grade solve) instead of float64 GEMMs.
+void rb_solve(Handle& h, const RbSolver& S, double* B, int ldb, int nrhs, bool tc = false);
 void thomas_factor(Handle& h, RbSolver& S, int nblk, int m, const double* SiM, const double* SiP,
                    const double* T);
 void thomas_solve(Handle& h, const RbSolver& S, double* B, int ldb, int nrhs);

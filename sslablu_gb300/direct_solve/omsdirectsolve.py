@@ -198,3 +198,13 @@ class RedBlackSolver(_DeviceTridiag, DirectSolver):
             self.iters, self.relres = it.value, rr.value
             return dv.finish(X, rhs, one)
         return dv.finish(self._solve_dev(B.clone()), rhs, one)
+
+    def solve_tc(self, rhs):
+        """Beyond upstream: the solve with its block products on the tensor
+        cores (split-BF16x3 GEMMs, float32-level accuracy; slu_rb_solve_tc):
+        a fast approximate solve for preconditioning an iterative solve of the
+        exact operator."""
+        B, one = dv.prepare_rhs(rhs)
+        B = B.clone().contiguous()
+        L.check(L.lib().slu_rb_solve_tc(L.handle(), self._h, L.ptr(B), B.shape[1], B.shape[1]))
+        return dv.finish(B, rhs, one)

@@ -78,6 +78,39 @@ def test_c1_poisson_full_interfaces(golden):
     assert relerr(xr, g["x_rb"]) < 1e-12
 
 
+def test_rb_solve_tc_approximates_the_solve(golden):
+    """The red-black solve with its block products on the tensor cores
+    (split-BF16x3, float32-level; slu_rb_solve_tc) on the C1 system at
+    256-point interfaces (blocks above the fused-solve size use the same
+    path): within 1e-5 of upstream's float64 solution, and a GMRES
+    preconditioner that takes the exact system to 1e-10 in a few steps."""
+    need_gpu()
+    import torch
+    from oracle.slabmaps import poisson2d_couplings
+    from sslablu_gb300.direct_solve.omsdirectsolve import RedBlackSolver
+    from sslablu_gb300.multislab.gmres import gmres
+    g = golden("c1_poisson256")
+    nc, n = int(g["nc"]), int(g["nslabs"]) - 1
+    C = poisson2d_couplings(nc, n + 1, int(g["nx"]))
+    Sp = [[C[i][0], C[i][1]] for i in range(n)] + [[np.zeros((nc, nc))] * 2]
+    for prec in ("f64", "mixed"):
+        rb = RedBlackSolver(nc, precision=prec)
+        rb.factorize(Sp, [np.eye(nc)] * (n + 1))
+        b = np.concatenate([g["rhs"], np.zeros(nc)])
+        xt = rb.solve_tc(b)
+        assert relerr(xt, g["x_rb"]) < 1e-5, prec
+    M = np.eye((n + 1) * nc)
+    for i in range(n):
+        if i > 0:
+            M[i * nc:(i + 1) * nc, (i - 1) * nc:i * nc] = C[i][0]
+        if i < n - 1:
+            M[i * nc:(i + 1) * nc, (i + 1) * nc:(i + 2) * nc] = C[i][1]
+    Md = torch.from_numpy(M).cuda()
+    B = torch.from_numpy(np.random.default_rng(2).standard_normal(((n + 1) * nc, 4))).cuda()
+    X, steps, rel = gmres(lambda V: Md @ V, B, rb.solve_tc, tol=1e-10)
+    assert rel <= 1e-10 and steps <= 6
+
+
 def test_c3_helmholtz_small(golden):
     """3-D variable-coefficient Helmholtz couplings (k = 20) from upstream's
     stencil pipeline: the GPU Thomas and red-black solvers on the same
