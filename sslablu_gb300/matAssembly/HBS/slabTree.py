@@ -20,8 +20,15 @@ NE).  A box stops splitting at ``min_leaf_size`` points or at ``max_level``
 keep their boundary DOFs (``bDOFs``) and internal boxes their interface DOFs
 (``iDOFs``), as upstream leaves them after construction.
 
-Not built here: the adjacency lists (slabTree.py:343-547) and the nested
-interface solve (665-714), which serve the strong-admissibility variants.
+Adjacency (slabTree.py:343-547), the near-field structure of the
+strong-admissibility HBS: per level, the pairs of boxes that touch --
+binary trees by the split-direction rule ('partial', the default) or by a
+geometric contact test of the children of touching parents ('full'); quad
+trees by the sibling and parent-pair rule -- gathered into
+``level_adj_list[l][r]``, the set of level-local ranks adjacent to the box
+of rank r at depth l (ranks follow the sorted box indices).
+
+Not built here: the nested interface solve (665-714).
 """
 import numpy as np
 
@@ -97,6 +104,7 @@ class slabTree:
             self._split_quad(root)
         else:
             self._split_rect(root)
+        self._build_level_adjacency()
         self._build_perm()
         for node in self._boxes.values():
             if not node.is_leaf:
@@ -204,6 +212,95 @@ class slabTree:
                      "right": np.concatenate([se.bDOFs["right"], ne.bDOFs["right"]]),
                      "down": np.concatenate([sw.bDOFs["down"], se.bDOFs["down"]]),
                      "up": np.concatenate([nw.bDOFs["up"], ne.bDOFs["up"]])}
+
+    # ------------------------------------------------------------ adjacency
+    def _pairs_partial(self):
+        """slabTree.py:349-374: siblings touch across the split of their
+        parent; of two touching parents, the children facing each other
+        touch (one pair when the parents met across this level's split
+        direction, two side-by-side pairs otherwise)."""
+        out = [[]]
+        for lvl in range(1, self.nlevels):
+            along = "vertical" if lvl % 2 == 1 else "horizontal"
+            across = "horizontal" if along == "vertical" else "vertical"
+            cur = [(nd.children[0].index, nd.children[1].index, along)
+                   for nd in self.get_nodes_level(lvl - 1)]
+            for a, b, d in out[-1]:
+                ca, cb = self._boxes[a].children, self._boxes[b].children
+                if d == along:
+                    cur.append((ca[1].index, cb[0].index, along))
+                else:
+                    cur.append((ca[0].index, cb[0].index, across))
+                    cur.append((ca[1].index, cb[1].index, across))
+            out.append(cur)
+        return out
+
+    def _touch(self, P, Q, alpha=1e-3):
+        """slabTree.py:380-402: boxes touch when the gap along every axis is
+        at most alpha times the smaller width there."""
+        bp, bq = P.bounds, Q.bounds
+        for ax in range(len(bp) // 2):
+            lo_p, hi_p, lo_q, hi_q = bp[2 * ax], bp[2 * ax + 1], bq[2 * ax], bq[2 * ax + 1]
+            gap = max(lo_p - hi_q, lo_q - hi_p)
+            if gap > alpha * min(hi_p - lo_p, hi_q - lo_q):
+                return False
+        return True
+
+    def _pairs_full(self):
+        """slabTree.py:404-441: candidates are siblings and the children of
+        touching parents; a candidate is kept when the boxes touch."""
+        out = [[]]
+        for lvl in range(1, self.nlevels):
+            cand = [(nd.children[0], nd.children[1]) for nd in self.get_nodes_level(lvl - 1)
+                    if not nd.is_leaf]
+            for a, b, _ in out[-1]:
+                A, B = self._boxes[a], self._boxes[b]
+                if not (A.is_leaf or B.is_leaf):
+                    cand += [(p, q) for p in A.children for q in B.children]
+            out.append([(p.index, q.index, None) for p, q in cand if self._touch(p, q)])
+        return out
+
+    def _pairs_quad(self):
+        """slabTree.py:443-489: the four sibling pairs of every split box,
+        and the facing children of touching parents."""
+        out = [[]]
+        for lvl in range(1, self.nlevels):
+            cur = []
+            for nd in self.get_nodes_level(lvl - 1):
+                if nd.is_leaf:
+                    continue
+                sw, se, nw, ne = (c.index for c in nd.children)
+                cur += [(sw, se, "horizontal"), (nw, ne, "horizontal"),
+                        (sw, nw, "vertical"), (se, ne, "vertical")]
+            for a, b, d in out[-1]:
+                A, B = self._boxes[a], self._boxes[b]
+                if A.is_leaf or B.is_leaf:
+                    continue
+                a_sw, a_se, a_nw, a_ne = (c.index for c in A.children)
+                b_sw, b_se, b_nw, b_ne = (c.index for c in B.children)
+                if d == "horizontal":     # A left of B
+                    cur += [(a_se, b_sw, d), (a_ne, b_nw, d)]
+                else:                     # A below B
+                    cur += [(a_nw, b_sw, d), (a_ne, b_se, d)]
+            out.append(cur)
+        return out
+
+    def _build_level_adjacency(self):
+        """slabTree.py:495-545: level_adj_list from the touching pairs."""
+        if self._quad:
+            pairs = self._pairs_quad()
+        elif self._adjacency == "full":
+            pairs = self._pairs_full()
+        else:
+            pairs = self._pairs_partial()
+        self.level_adj_list = []
+        for lvl, plist in enumerate(pairs):
+            rank = {g: r for r, g in enumerate(self.get_boxes_level(lvl))}
+            adj = [set() for _ in rank]
+            for a, b, _ in plist:
+                adj[rank[a]].add(rank[b])
+                adj[rank[b]].add(rank[a])
+            self.level_adj_list.append(adj)
 
     def _build_perm(self):
         """slabTree.py:206-213: leaf point lists, leaves in box-index order."""

@@ -32,6 +32,11 @@ the large outputs are stored.  Fixtures written (all small):
   slab_trees.npz     slabTree on lines, rectangles (binary and quad) and a plane
                      in 3-D: perm_leaf, nleaves, nlevels, leaf boundary DOFs and
                      interface DOFs
+  slab_adjacency.npz slabTree.level_adj_list of the same trees ('partial' and
+                     'full' adjacency for the binary ones)
+  hbs_strong.npz     HBStorch_strong.HBSMAT (strong admissibility) on planes
+                     of points with partial, full and quad adjacency:
+                     matmat / rmatmat, leaf near-field tile norms, nbytes
   hbstorch.npz       HBStorch.HBSMAT(tree=slabTree).construct(k, Om, Psi, Y, Z)
                      of an exact HBS matrix in a rectangle tree's ordering, with
                      the rkHBS assembler's sample count (s < 2n at the leaves):
@@ -419,6 +424,97 @@ def slab_trees(ref):
     np.savez_compressed(os.path.join(HERE, "slab_trees.npz"), **out)
 
 
+def adjacency_record(t):
+    """level_adj_list flattened: per level, per rank, the sorted neighbours
+    (counts and concatenated ranks)."""
+    cnt, nbr = [], []
+    for adj in t.level_adj_list:
+        for a in adj:
+            cnt.append(len(a))
+            nbr.extend(sorted(a))
+    return np.array([len(a) for a in t.level_adj_list]), np.array(cnt), np.array(nbr, dtype=np.int64)
+
+
+def slab_adjacency(ref):
+    """slabTree.level_adj_list of the slab tree cases, binary trees with
+    'partial' and 'full' adjacency, quad trees with their own rule."""
+    import matAssembly.HBS.slabTree as ST
+    out = {}
+    for name, kind, n, quad, leaf in SLAB_TREE_CASES:
+        for adj in (("partial",) if quad else ("partial", "full")):
+            with contextlib.redirect_stdout(QUIET):
+                t = ST.slabTree(slab_cloud(kind, n), quad, leaf, adjacency=adj)
+            lv, cnt, nbr = adjacency_record(t)
+            key = "%s_%s_" % (name, adj)
+            out[key + "levels"], out[key + "count"], out[key + "nbr"] = lv, cnt, nbr
+    np.savez_compressed(os.path.join(HERE, "slab_adjacency.npz"), **out)
+
+
+def strong_kernel(XX, shift=0.05, eps=0.02):
+    """exp(-r) / (r + eps) between a plane of points and its copy shifted by
+    `shift` along x: a smooth operator whose near field decays slowly, the
+    shape of a slab coupling between neighbouring interfaces."""
+    D = np.linalg.norm(XX[:, None, :] - XX[None, :, :] - np.array([shift, 0.0, 0.0]), axis=2)
+    return np.exp(-D) / (D + eps)
+
+
+STRONG_CASES = [
+    # name, cloud, quad, leaf, adjacency, rank, seed
+    ("plane_partial", "plane32", False, 64, "partial", 16, 31),
+    ("plane_full", "plane32", False, 64, "full", 16, 32),
+    ("plane_quad", "plane32", True, 64, "partial", 16, 33),
+    ("rect_full", "rect16z", False, 16, "full", 6, 34),
+]
+
+
+def strong_cloud(kind):
+    if kind == "rect16z":
+        g = slab_cloud("rect16")
+        return np.concatenate([np.zeros((g.shape[0], 1)), g], 1)
+    return slab_cloud(kind)
+
+
+def strong_samples(name, kind, quad, leaf, adj, rk, seed):
+    """Inputs of a strong-admissibility case (regenerated by the tests):
+    the tree, the operator, sketches with upstream's thinSlab3D sample count
+    s = kmax max(2 rk, leaf) + rk + 20 (kmax 9 full, 5 partial), and x."""
+    XX = strong_cloud(kind)
+    A = strong_kernel(XX)
+    kmax = 9 if adj == "full" else 5
+    s = kmax * max(2 * rk, leaf) + rk + 20
+    rng = np.random.default_rng(seed)
+    N = A.shape[0]
+    Om, Psi = rng.standard_normal((N, s)), rng.standard_normal((N, s))
+    x = rng.standard_normal((N, 3))
+    return XX, A, Om, Psi, x
+
+
+def hbs_strong(ref):
+    """HBStorch_strong.HBSMAT(tree=slabTree(adjacency=...)).construct(rk, Om,
+    Psi, Y, Z): matmat / rmatmat of the compressed operator, the Frobenius
+    norm of every leaf-level near-field tile (sorted by (row, col)), nbytes."""
+    import matAssembly.HBS.slabTree as ST
+    import matAssembly.HBS.HBStorch_strong as HS
+    out = {}
+    for name, kind, quad, leaf, adj, rk, seed in STRONG_CASES:
+        XX, A, Om, Psi, x = strong_samples(name, kind, quad, leaf, adj, rk, seed)
+        with contextlib.redirect_stdout(QUIET):
+            tree = ST.slabTree(XX, quad, leaf, adjacency=adj)
+            H = HS.HBSMAT(device="cpu", tree=tree, quad=quad)
+            H.construct(rk, Om, Psi, A @ Om, A.T @ Psi, profile=False)
+        E0 = H.Emats[0]
+        order = np.lexsort((E0.col.numpy(), E0.row.numpy()))
+        p = name + "_"
+        out[p + "Ax"] = np.asarray(H.matmat(x))
+        out[p + "ATx"] = np.asarray(H.rmatmat(x))
+        out[p + "tile_norms"] = np.linalg.norm(E0.val.numpy()[order], axis=(1, 2))
+        out[p + "tile_rc"] = np.stack([E0.row.numpy()[order], E0.col.numpy()[order]], 1)
+        out[p + "nlev"] = np.array([len(H.Umats), len(H.Emats)])
+        out[p + "nbytes"] = np.array(H.nbytes)
+        out[p + "relerr"] = np.array(np.linalg.norm(out[p + "Ax"] - A @ x) / np.linalg.norm(A @ x))
+    np.savez_compressed(os.path.join(HERE, "hbs_strong.npz"), **out)
+
+
 def exact_in_tree_order(k, nl, L, seed, perm):
     """Dense A with A[perm][:, perm] equal to an exact random HBS matrix."""
     np.random.seed(seed)
@@ -516,6 +612,8 @@ def main():
     rbhbs(ref)
     rbhbs_gauss(ref)
     slab_trees(ref)
+    slab_adjacency(ref)
+    hbs_strong(ref)
     hbstorch(ref)
     assembler(ref)
     for f in sorted(os.listdir(HERE)):

@@ -296,3 +296,44 @@ def test_rb_cyclic_fixture_is_the_periodic_system(golden):
     for key in ("2_5", "4_6", "8_16"):
         M = _periodic_matrix(g["S_" + key], g["T_" + key])
         assert relerr(np.linalg.solve(M, g["rhs_" + key]), g["x_" + key]) < 1e-14
+
+
+def test_slab_adjacency_mirror_matches_upstream(golden):
+    """slabTree.level_adj_list (the strong-admissibility near field) against
+    upstream's: binary trees with 'partial' and 'full' adjacency, quad trees,
+    on lines, rectangles and a plane in 3-D."""
+    from sslablu_gb300.matAssembly.HBS.slabTree import slabTree
+    from tests.golden.make_golden import SLAB_TREE_CASES, adjacency_record, slab_cloud
+    g = golden("slab_adjacency")
+    for name, kind, n, quad, leaf in SLAB_TREE_CASES:
+        for adj in (("partial",) if quad else ("partial", "full")):
+            t = slabTree(slab_cloud(kind, n), quad, leaf, adjacency=adj)
+            lv, cnt, nbr = adjacency_record(t)
+            k = "%s_%s_" % (name, adj)
+            assert np.array_equal(lv, g[k + "levels"]), k
+            assert np.array_equal(cnt, g[k + "count"]), k
+            assert np.array_equal(nbr, g[k + "nbr"]), k
+
+
+def test_strong_oracle_matches_upstream(golden):
+    """oracle.strong (HBStorch_strong restated in numpy) against upstream's
+    own construct + sweep on the same sketches: apply in both orientations
+    to 1e-12, the leaf near-field tiles (norms) to 1e-9, the level count."""
+    from oracle.strong import StrongHBS
+    from sslablu_gb300.matAssembly.HBS.slabTree import slabTree
+    from tests.golden.make_golden import STRONG_CASES, strong_samples
+    g = golden("hbs_strong")
+    for case in STRONG_CASES:
+        name, kind, quad, leaf, adj, rk, seed = case
+        XX, A, Om, Psi, x = strong_samples(*case)
+        t = slabTree(XX, quad, leaf, adjacency=adj)
+        O = StrongHBS(t.perm_leaf, t.nleaves, t.level_adj_list, 4 if quad else 2)
+        O.construct(rk, Om, Psi, A @ Om, A.T @ Psi)
+        p = name + "_"
+        for got, ref in ((O.apply(x), g[p + "Ax"]), (O.apply(x, True), g[p + "ATx"])):
+            assert np.linalg.norm(got - ref) <= 1e-12 * np.linalg.norm(ref), name
+        rc = g[p + "tile_rc"]
+        norms = np.array([np.linalg.norm(O.E[0].tiles[(int(i), int(j))]) for i, j in rc])
+        assert len(O.E[0].tiles) == len(rc), name
+        assert np.allclose(norms, g[p + "tile_norms"], rtol=1e-9, atol=0), name
+        assert [len(O.U), len(O.E) + 1] == list(g[p + "nlev"]), name
