@@ -42,6 +42,7 @@ typedef struct slu_hbs_s* slu_hbs_t;
 typedef struct slu_dense_rb_s* slu_rb_t;
 typedef struct slu_solve_plan_s* slu_solve_plan_t;
 typedef struct slu_refine_plan_s* slu_refine_plan_t;
+typedef struct slu_strong_s* slu_strong_t;
 
 /* ---------------------------------------------------------------- runtime */
 int slu_version(void);
@@ -396,6 +397,44 @@ int slu_slab_maps_apply(slu_handle_t h, int nx, int ny, int nz, double width, do
 int slu_thomas_factor(slu_handle_t h, int nblk, int m, const double* SiM, const double* SiP,
                       const double* T, slu_rb_t* out);
 int slu_thomas_solve(slu_handle_t h, slu_rb_t th, double* B, int ldb, int nrhs);
+
+/* ------------------------------------------------ strong admissibility */
+/* Strong-admissibility HBS operator (matAssembly/HBS/HBStorch_strong.py,
+ * HBSMAT 908-1310): per level A = U B V^T + E with E block sparse on each
+ * block's near field (its level adjacency plus itself).  N points in
+ * nleaves uniform leaves of a tree with fac children per box (2 or 4);
+ * perm_host[i] = caller row of tree position i (the tree's perm_leaf; NULL =
+ * identity).  Replaces HBSMAT.__init__ (925-975). */
+int slu_strong_create(slu_handle_t h, long long N, int nleaves, int fac,
+                      const int64_t* perm_host, slu_strong_t* out);
+int slu_strong_destroy(slu_strong_t op);
+/* Compression from sketches (HBSMAT.construct / constructHBS, 1000-1107):
+ * Om, Psi, Y = A Om', Z = A^T Psi' (device, N x s row-major, rows already
+ * in tree order), rank rk.  nlev levels carry a far field (leaf first); for
+ * level t, nb[t] blocks and the near fields as CSR (host arrays: nf_ptr has
+ * nb[t] + 1 entries per level, offsets relative to that level's nf_idx
+ * slice; each list holds the block itself and is symmetric).  Above the
+ * last one the remaining operator is the dense base B = Y pinv(Om).
+ * SLU_ERR_ARG when a near-field stack is rank deficient (min |R_ii| <= 1e-12
+ * max |R_ii|) or wider than s, where upstream falls back to a truncated
+ * SVD. */
+int slu_strong_compress(slu_handle_t h, slu_strong_t op, int rk, int s, const double* Om,
+                        const double* Psi, const double* Y, const double* Z, int nlev,
+                        const int* nb, const int* nf_ptr, const int* nf_idx);
+/* Y <- A X (trans = 0) or A^T X (HBSMAT._sweep / matmat / rmatmat,
+ * 1232-1299); X, Y N x nrhs device float64 in the caller's ordering,
+ * distinct. */
+int slu_strong_apply(slu_handle_t h, slu_strong_t op, int trans, const double* X, int ldx,
+                     double* Y, int ldy, int nrhs);
+/* Queries: what 0 compressed levels (-1 before compression), 1 blocks,
+ * 2 block size, 3 rank, 4 near-field tiles of `level`, 5 rows of the dense
+ * base, 6 near-field stacks factored, 7 bytes of U, V, E (tiles and their
+ * int64 coordinates) and the base (HBSMAT.nbytes, 993-998). */
+int slu_strong_info(slu_strong_t op, int what, int level, long long* out);
+/* Copies out a level's factors (host or device dst): what 0 U, 1 V
+ * (Nb x b x r), 2 the tiles (nnz x b x b, sorted by (row, col)), 3 the tile
+ * coordinates (int32 row, col pairs; host dst), 4 the dense base. */
+int slu_strong_export(slu_handle_t h, slu_strong_t op, int what, int level, void* dst);
 
 #ifdef __cplusplus
 }

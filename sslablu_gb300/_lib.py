@@ -77,6 +77,12 @@ SIGNATURES = {
     "slu_rb_solve_tc": [P, P, P, c_int, c_int],
     "slu_slab_maps_apply": [P, c_int, c_int, c_int, c_double, c_double, c_int, c_int, P, P, P,
                             c_int, P, P, c_int, c_int, c_int, c_double, P],
+    "slu_strong_create": [P, c_longlong, c_int, c_int, P, ctypes.POINTER(c_void_p)],
+    "slu_strong_destroy": [P],
+    "slu_strong_compress": [P, P, c_int, c_int, P, P, P, P, c_int, P, P, P],
+    "slu_strong_apply": [P, P, c_int, P, c_int, P, c_int, c_int],
+    "slu_strong_info": [P, c_int, c_int, ctypes.POINTER(c_longlong)],
+    "slu_strong_export": [P, P, c_int, c_int, P],
     "slu_hbs_prepare_ozaki": [P, P],
     "slu_ulv_solve_ozaki": [P, P, P, c_int, P, c_int, c_int],
     "slu_hbs_apply_ozaki": [P, P, P, c_int, P, c_int, c_int],

@@ -11,6 +11,8 @@
 //     (ULVsparse.py:51-61).
 // Reflectors follow the LAPACK geqrf convention (beta = -sign(alpha)*norm,
 // v[0] = 1), so the trailing columns of Q match LAPACK's to rounding.
+#include <algorithm>
+
 #include "slablu_internal.cuh"
 
 namespace slu {
@@ -267,12 +269,14 @@ jacobi_kernel(int m, int n, const double* __restrict__ A, int lda, long long sA,
     if (lane == 0) nrm[c] = sqrt(s);
   }
   __syncthreads();
-  // rank of each column by decreasing norm (ties by index)
+  // rank of each column by decreasing norm (ties by index).  A NaN norm
+  // (non-finite input) ranks below every number, so the ranks stay a
+  // permutation and every order[] slot is written
   for (int c = threadIdx.x; c < np; c += blockDim.x) {
     int rk = 0;
-    double v = nrm[c];
+    const double v = nrm[c] == nrm[c] ? nrm[c] : -1.0;
     for (int o = 0; o < np; ++o) {
-      double w = nrm[o];
+      const double w = nrm[o] == nrm[o] ? nrm[o] : -1.0;
       rk += (w > v) || (w == v && o < c);
     }
     order[rk] = c;
@@ -285,7 +289,7 @@ jacobi_kernel(int m, int n, const double* __restrict__ A, int lda, long long sA,
   // normalised leading columns; columns that carry no direction are
   // completed below by Gram-Schmidt on the unit vectors
   for (int j = warp; j < r; j += nwarps) {
-    int c = order[j < np ? j : np - 1];
+    const int c = min(max(order[j < np ? j : np - 1], 0), np - 1);
     double s = nrm[c];
     if (svb && lane == 0) svb[j] = (j < n) ? s : 0.0;
     bool ok = (j < n) && s > tiny;
@@ -296,7 +300,7 @@ jacobi_kernel(int m, int n, const double* __restrict__ A, int lda, long long sA,
   // completion (rare: zero or rank-deficient input); serial over columns
   if (warp == 0) {
     for (int j = 0; j < r; ++j) {
-      int c = order[j < np ? j : np - 1];
+      const int c = min(max(order[j < np ? j : np - 1], 0), np - 1);
       bool ok = (j < n) && nrm[c] > tiny;
       if (ok) continue;
       for (int e = 0; e < m; ++e) {
@@ -323,7 +327,101 @@ jacobi_kernel(int m, int n, const double* __restrict__ A, int lda, long long sA,
     }
   }
 }
+// Compact WY form of a factored panel of jb reflectors (LAPACK larft,
+// forward, columnwise): Vc (jb x mp, row-major) holds the reflectors with
+// their unit diagonal and zeros above it written out, and T (jb x jb, upper)
+// satisfies H_0 H_1 ... H_{jb-1} = I - V T V^T (V = Vc^T).  One CTA per
+// matrix; the panel is read from the column-major work array (column a at
+// P + a * ldw, rows 0..mp-1 relative to the panel's diagonal).
+constexpr int kWY = 32;   // panel width of the blocked QR
+__global__ void __launch_bounds__(256)
+wy_kernel(int mp, int jb, const double* __restrict__ P, int ldw, long long sW,
+          const double* __restrict__ tau, long long sTau, double* __restrict__ Vc, long long sV,
+          double* __restrict__ T, long long sT) {
+  __shared__ double G[kWY][kWY + 1];
+  __shared__ double Ts[kWY][kWY + 1];
+  const long long b = blockIdx.x;
+  P += b * sW;
+  tau += b * sTau;
+  Vc += b * sV;
+  T += b * sT;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  for (long long e = threadIdx.x; e < (long long)jb * mp; e += blockDim.x) {
+    const int a = (int)(e / mp), r = (int)(e - (long long)a * mp);
+    Vc[e] = r < a ? 0.0 : (r == a ? 1.0 : P[(long long)a * ldw + r]);
+  }
+  // G(a, c) = v_a . v_c for a < c: v_c starts at row c (unit), v_a there
+  // holds P(a, c) (a < c), both below
+  for (int q = warp; q < jb * jb; q += nwarps) {
+    const int a = q / jb, c = q - a * jb;
+    if (a >= c) continue;
+    double d = 0.0;
+    for (int r = c + 1 + lane; r < mp; r += 32)
+      d += P[(long long)a * ldw + r] * P[(long long)c * ldw + r];
+    for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+    if (lane == 0) G[a][c] = d + P[(long long)a * ldw + c];
+  }
+  __syncthreads();
+  // T(i, i) = tau_i; T(0:i, i) = -tau_i T(0:i, 0:i) G(0:i, i), one column
+  // at a time by the first warp (lane r owns row r)
+  if (warp == 0) {
+    for (int i = 0; i < jb; ++i) {
+      const double ti = tau[i];
+      double v = 0.0;
+      if (lane < i) {
+        for (int c = lane; c < i; ++c) v += Ts[lane][c] * G[c][i];
+        v *= -ti;
+      }
+      __syncwarp();
+      if (lane < i) Ts[lane][i] = v;
+      if (lane == i) Ts[i][i] = ti;
+      if (lane > i && lane < jb) Ts[lane][i] = 0.0;
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < jb * jb; e += blockDim.x) T[e] = Ts[e / jb][e % jb];
+}
+
 }  // namespace
+
+size_t qr_blocked_ws_elems(int m, int ncol, int batch) {
+  return (size_t)batch * ((size_t)kWY * m + (size_t)kWY * kWY + 2 * (size_t)ncol * kWY) + 64;
+}
+
+void qr_blocked(cudaStream_t st, int m, int nfac, int ncol, double* W, int ldw, long long sW,
+                double* tau, long long sTau, int batch, double* ws) {
+  if (batch <= 0 || m <= 0 || nfac <= 0) return;
+  if (nfac <= 2 * kWY) {
+    panel_qr(st, m, nfac, ncol, W, ldw, sW, tau, sTau, batch);
+    return;
+  }
+  SLU_REQUIRE(ws, "qr_blocked: workspace missing");
+  const long long sV = (long long)kWY * m, sT = (long long)kWY * kWY, sX = (long long)ncol * kWY;
+  double* Vc = ws;
+  double* T = Vc + batch * sV;
+  double* X1 = T + batch * sT;
+  double* X2 = X1 + batch * sX;
+  const int nf = std::min(nfac, m);
+  for (int j0 = 0; j0 < nf; j0 += kWY) {
+    const int jb = std::min(kWY, nf - j0), mp = m - j0;
+    double* Pj = W + (long long)j0 * ldw + j0;
+    panel_qr(st, mp, jb, jb, Pj, ldw, sW, tau + j0, sTau, batch);
+    const int nc = ncol - j0 - jb;
+    if (nc <= 0) continue;
+    wy_kernel<<<batch, 256, 0, st>>>(mp, jb, Pj, ldw, sW, tau + j0, sTau, Vc, sV, T, sT);
+    check_launch("wy_kernel");
+    // trailing columns C (mp x nc, column-major: C^T row-major with ld ldw)
+    // <- Q^T C, i.e. C^T <- C^T - (C^T V) T V^T
+    double* Ct = Pj + (long long)jb * ldw;
+    gemm_batched<double>(st, false, true, nc, jb, mp, 1.0, Ct, ldw, sW, 0, Vc, mp, sV, 0, 0.0, X1,
+                         jb, sX, 0, batch);
+    gemm_batched<double>(st, false, false, nc, jb, jb, 1.0, X1, jb, sX, 0, T, jb, sT, 0, 0.0, X2,
+                         jb, sX, 0, batch);
+    gemm_batched<double>(st, false, false, nc, mp, jb, -1.0, X2, jb, sX, 0, Vc, mp, sV, 0, 1.0, Ct,
+                         ldw, sW, 0, batch);
+  }
+}
 
 void panel_qr(cudaStream_t st, int m, int nfac, int ncol, double* W, int ldw, long long sW,
               double* tau, long long sTau, int batch) {

@@ -114,6 +114,15 @@ void gemm_batched(cudaStream_t st, bool ta, bool tb, int M, int N, int K, T alph
 void panel_qr(cudaStream_t st, int m, int nfac, int ncol, double* W, int ldw,
               long long sW, double* tau, long long sTau, int batch);
 
+// The same factorisation for wide panels (nfac > 64): 32-column panels by
+// panel_qr, the trailing columns updated in the compact WY form
+// (C <- (I - V T^T V^T) C) by three batched GEMMs per panel over all SMs.
+// ws holds qr_blocked_ws_elems(m, ncol, batch) doubles; nfac <= 64 runs
+// panel_qr itself (ws unused).
+size_t qr_blocked_ws_elems(int m, int ncol, int batch);
+void qr_blocked(cudaStream_t st, int m, int nfac, int ncol, double* W, int ldw, long long sW,
+                double* tau, long long sTau, int batch, double* ws);
+
 // Two panel factorisations of the same shapes in one launch (W, tau and
 // W2, tau2, batch blocks each).
 void panel_qr2(cudaStream_t st, int m, int nfac, int ncol, double* W, double* W2, int ldw,
