@@ -647,6 +647,43 @@ def run_other(args):
                                             "dense red-black preconditioned scipy GMRES) at 17 "
                                             "slabs x 16 x 16 points, 64 RHS; build %.2f s"
                                             % t_build})
+    elif args.workload == "c3_strong":
+        # strong-admissibility HBS (HBStorch_strong) of a coupling between two
+        # 64 x 64 interface planes (C3's interface size), full adjacency
+        from sslablu_gb300 import slabbench
+        from sslablu_gb300.matAssembly.HBS.slabTree import slabTree
+        from sslablu_gb300.synthetic import plane_coupling, plane_points
+        from oracle.strong import StrongHBS
+        ns = types.SimpleNamespace(n=64, leaf=128, rank=32, adjacency="full", nrhs=64,
+                                   reps=max(3, min(10, args.steps)))
+        g = slabbench.strong(ns)
+        XX = plane_points(ns.n)
+        A = plane_coupling(XX)
+        N, s = A.shape[0], g["samples"]
+        rng = np.random.default_rng(0)
+        Om, Psi = rng.standard_normal((N, s)), rng.standard_normal((N, s))
+        tree = slabTree(XX, False, ns.leaf, adjacency="full")
+        O = StrongHBS(tree.perm_leaf, tree.nleaves, tree.level_adj_list)
+        t0 = time.perf_counter()
+        O.construct(ns.rank, Om, Psi, A @ Om, A.T @ Psi)
+        t_con = time.perf_counter() - t0
+        X = rng.standard_normal((N, ns.nrhs))
+        ts = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            O.apply(X)
+            ts.append(time.perf_counter() - t0)
+        line = dict(base, metric="strong-admissibility HBS applies (RHS/s), 64 RHS", unit="RHS/s",
+                    value=g["apply_rhs_per_s"], ms_per_step=g["apply_ms"],
+                    config={"workload": g["workload"], "N": N, "samples": s,
+                            "construct_s": g["construct_s"]},
+                    arms=g,
+                    cpu_baseline={"value": ns.nrhs / statistics.median(ts), "unit": "RHS/s",
+                                  "cores": os.cpu_count(), "kind": "port",
+                                  "sample": "upstream HBStorch_strong restated in numpy "
+                                            "(oracle), same operator and sketches, 64 RHS; "
+                                            "construct %.2f s" % t_con,
+                                  "construct_s": t_con})
     else:   # c4_batch
         import subprocess
         out = subprocess.run([sys.executable, "-m", "sslablu_gb300.batchbench", "--reps",
@@ -697,7 +734,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--workload", default="c2",
-                    choices=["c2", "c1_dense", "c3_hbs", "c3", "c4_batch"])
+                    choices=["c2", "c1_dense", "c3_hbs", "c3", "c3_strong", "c4_batch"])
     ap.add_argument("--served-rhs", type=lambda v: [int(x) for x in v.split(",") if x],
                     default=[1024, 4096],
                     help="batch widths of the served mixed vs plain comparison (comma separated)")

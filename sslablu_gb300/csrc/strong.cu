@@ -49,8 +49,7 @@ struct SLevel {
   int Nb = 0, b = 0, r = 0;
   int nnz = 0;
   DevBuf U, V, tiles;          // Nb*b x r, Nb*b x r, nnz x b x b
-  DevBuf rptr, rent;           // CSR by row i: entries (tile, j)
-  DevBuf cptr, cent;           // CSR by column j: entries (tile, i)
+  DevBuf rc;                   // int2 (row, col) of every tile
   std::vector<int> trow, tcol; // tile t = (trow[t], tcol[t]), sorted by (row, col)
 };
 
@@ -135,56 +134,55 @@ __global__ void diag_check_kernel(const double* __restrict__ W, int ldw, long lo
   if (lane == 0 && !(mn > 1e-12 * mx)) atomicAdd(bad, 1);
 }
 
-// out_i (b x c, ld ldo) += alpha * sum_e op(T_e) X_src(e) over the entries
-// e of CSR row i (op = identity, or the transpose for trans): a 64 x 64
-// output tile per CTA (16 x 16 threads, 4 x 4 outputs each), K staged
-// through shared memory 16 at a time.
+// out_dst(t) (b x c, ld ldo) += alpha * op(T_t) X_src(t) for every tile t
+// (op = identity, dst = row(t), src = col(t); for trans the transpose,
+// dst = col(t), src = row(t)): one CTA per (64 x 64 output tile, tile t),
+// so a level's products spread over all SMs; the contributions of the
+// tiles of one block row meet in float64 atomic adds (their order, and so
+// the last bit of the sum, may vary between runs).  16 x 16 threads, 4 x 4
+// outputs each, K staged through shared memory 16 at a time.
 constexpr int kBT = 64, kBK = 16;
 __global__ void __launch_bounds__(256)
 bsr_mm_kernel(int trans, int b, int c, double alpha, const double* __restrict__ tiles,
-              const int* __restrict__ ptr, const int2* __restrict__ ent,
-              const double* __restrict__ X, int ldx, double* __restrict__ out, int ldo) {
+              const int2* __restrict__ rc, const double* __restrict__ X, int ldx,
+              double* __restrict__ out, int ldo) {
   __shared__ double As[kBK][kBT + 1];
   __shared__ double Bs[kBK][kBT];
-  const int i = blockIdx.z;
+  const int t = blockIdx.z;
   const int r0 = blockIdx.y * kBT, c0 = blockIdx.x * kBT;
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int2 ij = rc[t];
+  const int dst = trans ? ij.y : ij.x, src = trans ? ij.x : ij.y;
+  const double* T = tiles + (long long)t * b * b;
+  const double* Xs = X + (long long)src * b * ldx;
   double acc[4][4] = {};
-  const int e0 = __ldg(ptr + i), e1 = __ldg(ptr + i + 1);
-  const long long bb = (long long)b * b;
-  for (int e = e0; e < e1; ++e) {
-    const int2 en = ent[e];
-    const double* T = tiles + (long long)en.x * bb;
-    const double* Xs = X + (long long)en.y * b * ldx;
-    for (int k0 = 0; k0 < b; k0 += kBK) {
-      for (int q = threadIdx.x; q < kBK * kBT; q += 256) {
-        const int kk = q / kBT, rr = q - kk * kBT;   // A(r0 + rr, k0 + kk)
-        const int row = r0 + rr, col = k0 + kk;
-        double v = 0.0;
-        if (row < b && col < b) v = trans ? T[(long long)col * b + row] : T[(long long)row * b + col];
-        As[kk][rr] = v;
-        const int cc = c0 + rr;                      // X(k0 + kk, c0 + rr)
-        Bs[kk][rr] = (col < b && cc < c) ? Xs[(long long)col * ldx + cc] : 0.0;
-      }
-      __syncthreads();
-#pragma unroll
-      for (int kk = 0; kk < kBK; ++kk) {
-        double a[4], bv[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          a[u] = As[kk][ty + 16 * u];
-          bv[u] = Bs[kk][tx + 16 * u];
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-#pragma unroll
-          for (int v = 0; v < 4; ++v) acc[u][v] = fma(a[u], bv[v], acc[u][v]);
-      }
-      __syncthreads();
+  for (int k0 = 0; k0 < b; k0 += kBK) {
+    for (int q = threadIdx.x; q < kBK * kBT; q += 256) {
+      const int kk = q / kBT, rr = q - kk * kBT;   // A(r0 + rr, k0 + kk)
+      const int row = r0 + rr, col = k0 + kk;
+      double v = 0.0;
+      if (row < b && col < b) v = trans ? T[(long long)col * b + row] : T[(long long)row * b + col];
+      As[kk][rr] = v;
+      const int cc = c0 + rr;                      // X(k0 + kk, c0 + rr)
+      Bs[kk][rr] = (col < b && cc < c) ? Xs[(long long)col * ldx + cc] : 0.0;
     }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < kBK; ++kk) {
+      double a[4], bv[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        a[u] = As[kk][ty + 16 * u];
+        bv[u] = Bs[kk][tx + 16 * u];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] = fma(a[u], bv[v], acc[u][v]);
+    }
+    __syncthreads();
   }
-  if (e1 == e0) return;
-  double* o = out + (long long)i * b * ldo;
+  double* o = out + (long long)dst * b * ldo;
 #pragma unroll
   for (int u = 0; u < 4; ++u) {
     const int row = r0 + ty + 16 * u;
@@ -192,7 +190,7 @@ bsr_mm_kernel(int trans, int b, int c, double alpha, const double* __restrict__ 
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
       const int col = c0 + tx + 16 * v;
-      if (col < c) o[(long long)row * ldo + col] += alpha * acc[u][v];
+      if (col < c) atomicAdd(o + (long long)row * ldo + col, alpha * acc[u][v]);
     }
   }
 }
@@ -245,11 +243,10 @@ void tile_put(cudaStream_t st, int mode, const double* src, const int* tid, int 
 void bsr_mm(cudaStream_t st, bool trans, const SLevel& l, int c, double alpha, const double* X,
             int ldx, double* out, int ldo) {
   if (l.nnz == 0 || c <= 0) return;
-  SLU_REQUIRE(l.Nb <= 65535, "strong HBS: too many blocks on a level");
-  dim3 grid((unsigned)((c + kBT - 1) / kBT), (unsigned)((l.b + kBT - 1) / kBT), (unsigned)l.Nb);
-  bsr_mm_kernel<<<grid, 256, 0, st>>>(
-      trans ? 1 : 0, l.b, c, alpha, l.tiles.as<double>(), (trans ? l.cptr : l.rptr).as<int>(),
-      (trans ? l.cent : l.rent).as<int2>(), X, ldx, out, ldo);
+  SLU_REQUIRE(l.nnz <= 65535, "strong HBS: more than 65535 near-field tiles on a level");
+  dim3 grid((unsigned)((c + kBT - 1) / kBT), (unsigned)((l.b + kBT - 1) / kBT), (unsigned)l.nnz);
+  bsr_mm_kernel<<<grid, 256, 0, st>>>(trans ? 1 : 0, l.b, c, alpha, l.tiles.as<double>(),
+                                      l.rc.as<int2>(), X, ldx, out, ldo);
   check_launch("bsr_mm_kernel");
 }
 
@@ -457,18 +454,9 @@ void strong_compress(Handle& h, Op& S, int rk, int s, const double* Om, const do
     l.V.alloc(8 * (size_t)Nb * b * r, st);
     l.tiles.alloc(8 * (size_t)l.nnz * b * b, st);
     {
-      std::vector<int> rp(Nb + 1), cp(Nb + 1, 0);
-      std::vector<int2> re(l.nnz), ce(l.nnz);
-      for (int i = 0; i <= Nb; ++i) rp[i] = P.tile_of_row_start[i];
-      for (int t2 = 0; t2 < l.nnz; ++t2) re[t2] = make_int2(t2, P.tcol[t2]);
-      for (int t2 = 0; t2 < l.nnz; ++t2) cp[P.tcol[t2] + 1]++;
-      for (int j = 0; j < Nb; ++j) cp[j + 1] += cp[j];
-      std::vector<int> fill(cp.begin(), cp.end() - 1);
-      for (int t2 = 0; t2 < l.nnz; ++t2) ce[fill[P.tcol[t2]]++] = make_int2(t2, P.trow[t2]);
-      upload(st, l.rptr, rp);
-      upload(st, l.rent, re);
-      upload(st, l.cptr, cp);
-      upload(st, l.cent, ce);
+      std::vector<int2> rc(l.nnz);
+      for (int t2 = 0; t2 < l.nnz; ++t2) rc[t2] = make_int2(P.trow[t2], P.tcol[t2]);
+      upload(st, l.rc, rc);
     }
     // pass 0: Omega stacks, Y -> U and term 1; pass 1: Psi stacks, Z -> V
     // and term 2 (needs every U of the level, so all groups of pass 0 first)

@@ -3,6 +3,7 @@
     python -m sslablu_gb300.slabbench dense [--m 256 --slabs 8]
     python -m sslablu_gb300.slabbench hbs   [--m 1024 --slabs 8 --leaf 64 --rank 24]
     python -m sslablu_gb300.slabbench helmholtz [--slabs 33 --n 64 --leaf 128 --rank 64]
+    python -m sslablu_gb300.slabbench strong [--n 64 --leaf 128 --rank 32 --adjacency full]
 
 Workloads (seeded synthetic couplings of the interface system I + S,
 sslablu_gb300.synthetic.slab_couplings; the slab PDE pipeline that produces
@@ -15,6 +16,9 @@ real S blocks is outside this package):
   hbs   -- the C3 solve structure at reduced size: red-black and Thomas with
            every block an HBS compression (leaf, rank as given) of an implicit
            operator; factor time, 64-RHS solve time, residual.
+  strong -- strong-admissibility HBS of a coupling between two interface
+           planes: construct time, apply throughput, accuracy, and the
+           weak-admissibility HBS at the same rank beside it.
 GPU times are CUDA-event medians on device-resident data; factor times are
 wall-clock around the factorisation (host-driven).  Prints one JSON line.
 (`python bench.py --workload c1_dense|c3_hbs` runs the same measurements with
@@ -261,9 +265,60 @@ def helmholtz(a):
     return out
 
 
+def strong(a):
+    """Strong-admissibility HBS (HBStorch_strong) of the coupling between two
+    nearby n x n interface planes: construct from sketches (warm median of
+    reps, the first call separate), apply throughput for nrhs columns,
+    accuracy against the dense operator, and the weak-admissibility HBS at
+    the same rank for comparison."""
+    from .matAssembly.HBS.HBStorch_strong import HBSMAT
+    from .matAssembly.HBS import HBStorch
+    from .matAssembly.HBS.slabTree import slabTree
+    from .synthetic import plane_coupling, plane_points
+    XX = plane_points(a.n)
+    A = plane_coupling(XX)
+    N = A.shape[0]
+    kmax = 9 if a.adjacency == "full" else 5
+    s = kmax * max(2 * a.rank, a.leaf) + a.rank + 20
+    rng = np.random.default_rng(0)
+    Ad = torch.from_numpy(A).cuda()
+    Om = torch.from_numpy(rng.standard_normal((N, s))).cuda()
+    Psi = torch.from_numpy(rng.standard_normal((N, s))).cuda()
+    Y, Z = Ad @ Om, Ad.T @ Psi
+    tree = slabTree(XX, False, a.leaf, adjacency=a.adjacency)
+    H = HBSMAT(device="cuda", tree=tree)
+    t_cold, _ = _wall(lambda: H.construct(a.rank, Om, Psi, Y, Z), reps=1)
+    t_warm, _ = _wall(lambda: H.construct(a.rank, Om, Psi, Y, Z), reps=max(1, a.reps))
+    X = torch.from_numpy(rng.standard_normal((N, a.nrhs))).cuda()
+    t_apply = _events(lambda: H._dev_apply(X), a.reps)
+    err = float(torch.linalg.norm(H._dev_apply(X) - Ad @ X) / torch.linalg.norm(Ad @ X))
+    errT = float(torch.linalg.norm(H._dev_apply(X, True) - Ad.T @ X) / torch.linalg.norm(Ad.T @ X))
+    t_dense = _events(lambda: Ad @ X, a.reps)
+    # weak admissibility at the same rank (the rkHBS assembler's sample count)
+    wtree = slabTree(XX, False, a.leaf)
+    sw = max(2 * a.rank, a.leaf) + a.rank + 10
+    W = HBStorch.HBSMAT(device="cuda", tree=wtree)
+    Omw, Psiw = Om[:, :sw].contiguous(), Psi[:, :sw].contiguous()
+    W.construct(a.rank, Omw.cpu().numpy(), Psiw.cpu().numpy(), (Ad @ Omw).cpu().numpy(),
+                (Ad.T @ Psiw).cpu().numpy())
+    werr = float(np.linalg.norm(W.matmat(X.cpu().numpy()) - (Ad @ X).cpu().numpy())
+                 / float(torch.linalg.norm(Ad @ X)))
+    return {"workload": "strong-admissibility HBS of an exp(-r)/(r+0.02) coupling between "
+                        "%d x %d interface planes 0.05 apart, %s adjacency, leaf %d, rank %d"
+                        % (a.n, a.n, a.adjacency, a.leaf, a.rank),
+            "N": N, "samples": s, "levels": len(H.Umats), "stacks": H.factor_stats["qr"],
+            "construct_s": t_warm, "construct_cold_s": t_cold,
+            "apply_ms": 1e3 * t_apply, "nrhs": a.nrhs, "apply_rhs_per_s": a.nrhs / t_apply,
+            "dense_apply_ms": 1e3 * t_dense, "relerr": err, "relerr_T": errT,
+            "nbytes": H.nbytes, "dense_bytes": 8 * N * N,
+            "weak_same_rank_relerr": werr}
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
-    ap.add_argument("kind", choices=["dense", "hbs", "helmholtz"])
+    ap.add_argument("kind", choices=["dense", "hbs", "helmholtz", "strong"])
+    ap.add_argument("--adjacency", default="full", choices=["full", "partial"],
+                    help="strong: near-field rule of the slab tree")
     ap.add_argument("--m", type=int, default=None)
     ap.add_argument("--slabs", type=int, default=8)
     ap.add_argument("--leaf", type=int, default=64)
@@ -280,7 +335,9 @@ def main():
     a = ap.parse_args()
     if a.m is None:
         a.m = 256 if a.kind == "dense" else 1024
-    if a.kind == "helmholtz":
+    if a.kind == "strong":
+        out = strong(a)
+    elif a.kind == "helmholtz":
         out = helmholtz(a)
     else:
         out = dense(a) if a.kind == "dense" else hbs(a)

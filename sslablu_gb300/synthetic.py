@@ -86,3 +86,20 @@ def tridiag_apply(S, X):
         if i < nS - 1:
             Y[i * m:(i + 1) * m] += S[i][1] @ X[(i + 1) * m:(i + 2) * m]
     return Y
+
+
+def plane_points(n, x=0.5):
+    """n x n grid on the plane x = const of the unit cube (the interface
+    plane of a 3-D slab), as an (n*n, 3) point cloud."""
+    g = np.stack(np.meshgrid(np.linspace(0, 1, n), np.linspace(0, 1, n), indexing="ij"),
+                 -1).reshape(-1, 2)
+    return np.concatenate([np.full((g.shape[0], 1), x), g], 1)
+
+
+def plane_coupling(XX, shift=0.05, eps=0.02):
+    """exp(-r) / (r + eps) between the points and their copy moved by `shift`
+    along x: a smooth coupling between two nearby interfaces whose near
+    field decays slowly (the case strong admissibility is built for).
+    Returns a float64 numpy array."""
+    D = np.linalg.norm(XX[:, None, :] - XX[None, :, :] - np.array([shift, 0.0, 0.0]), axis=2)
+    return np.exp(-D) / (D + eps)
