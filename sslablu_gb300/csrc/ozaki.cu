@@ -247,25 +247,26 @@ __device__ __forceinline__ void f64_split(double x, int sh, float& h, float& l) 
 // |S| |z| (the apply inside a residual b - A x), so no rounding may happen
 // before the sum is complete; the only rounding is the final one to a
 // float32 pair or a float64 (~2^-48 of |v| for the pair).
-struct DiagSum {
-  float h, l, e, f;
-};
-__device__ __forceinline__ DiagSum diag_sum(const float (&a)[kDig]) {
-  DiagSum d;
-  float l, e, f;
-  two_sum(a[0], a[1], d.h, l);
-  two_sum(__fadd_rn(l, a[2]), a[3], d.l, e);
-  two_sum(__fadd_rn(e, a[4]), a[5], d.e, f);
-  d.f = __fadd_rn(f, a[6]);
-  return d;
+// Then v as a float32 pair (H + Lo, |Lo| <= ulp(H) / 2): h + l may cancel,
+// so H takes e in with a second TwoSum before the small terms are added.
+// Two outputs at once: packed float32x2 additions (IEEE round-to-nearest,
+// each lane exactly the scalar operation).
+__device__ __forceinline__ float2 f2neg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ void two_sum2(float2 a, float2 b, float2& s, float2& e) {
+  s = __fadd2_rn(a, b);
+  const float2 bb = __fadd2_rn(s, f2neg(a));
+  e = __fadd2_rn(__fadd2_rn(a, f2neg(__fadd2_rn(s, f2neg(bb)))), __fadd2_rn(b, f2neg(bb)));
 }
-// v as a float32 pair (H + Lo, |Lo| <= ulp(H) / 2).  h + l may cancel, so H
-// takes e in with a second TwoSum before the small terms are added.
-__device__ __forceinline__ void diag_pair(const DiagSum& d, float& H, float& Lo) {
-  float s, t, t2;
-  two_sum(d.h, d.l, s, t);
-  two_sum(s, d.e, s, t2);
-  two_sum(s, __fadd_rn(__fadd_rn(t, t2), d.f), H, Lo);
+__device__ __forceinline__ void diag_pair2(const float2 (&a)[kDig], float2& H, float2& Lo) {
+  float2 h, l, e, f, l2, e2;
+  two_sum2(a[0], a[1], h, l);
+  two_sum2(__fadd2_rn(l, a[2]), a[3], l2, e);
+  two_sum2(__fadd2_rn(e, a[4]), a[5], e2, f);
+  f = __fadd2_rn(f, a[6]);
+  float2 s, t, t2;
+  two_sum2(h, l2, s, t);
+  two_sum2(s, e2, s, t2);
+  two_sum2(s, __fadd2_rn(__fadd2_rn(t, t2), f), H, Lo);
 }
 // (H + Lo) 2^sh as a float64, from the bits with integer operations only
 // (GB300's float64 pipe runs at 1/64 of the float32 rate).  With
@@ -540,6 +541,7 @@ __global__ void __launch_bounds__(kThreads, 1) oz_step_kernel(const OzStep o) {
       float rsq = 0.f;   // squared residual norm of this column (residual form)
       for (int r8 = rh * 8; r8 < NT; r8 += 16) {
         uint32_t v[kDig][8];
+        float hp[2], lp[2];
 #pragma unroll
         for (int di = 0; di < kDig; ++di)
           tmem_ld8(tmem + lanes + (uint32_t)(di * NT + r8), v[di]);
@@ -547,12 +549,21 @@ __global__ void __launch_bounds__(kThreads, 1) oz_step_kernel(const OzStep o) {
 #pragma unroll
         for (int i8 = 0; i8 < 8; ++i8) {
           const int row = r8 + i8;
-          if (row >= nr || !cok) continue;
-          float a[kDig];
+          // rows i8, i8 + 1 combined together (packed float32x2)
+          float2 H2, L2;
+          if ((i8 & 1) == 0) {
+            float2 a[kDig];
 #pragma unroll
-          for (int di = 0; di < kDig; ++di) a[di] = __uint_as_float(v[di][i8]);
-          float H, Lo;
-          diag_pair(diag_sum(a), H, Lo);
+            for (int di = 0; di < kDig; ++di)
+              a[di] = make_float2(__uint_as_float(v[di][i8]), __uint_as_float(v[di][i8 + 1]));
+            diag_pair2(a, H2, L2);
+            hp[0] = H2.x;
+            hp[1] = H2.y;
+            lp[0] = L2.x;
+            lp[1] = L2.y;
+          }
+          if (row >= nr || !cok) continue;
+          float H = hp[i8 & 1], Lo = lp[i8 & 1];
           const float gs = __fmul_rn(rs[row], csc);   // a power of two, or 0
           char* p = outp[row] + 8 * col;
           if (outf64[row]) {
