@@ -287,6 +287,13 @@ def strong(a):
     Y, Z = Ad @ Om, Ad.T @ Psi
     tree = slabTree(XX, False, a.leaf, adjacency=a.adjacency)
     H = HBSMAT(device="cuda", tree=tree)
+    if getattr(a, "once", False):
+        # one construct and one apply, nothing else (for launch lists)
+        H.construct(a.rank, Om, Psi, Y, Z)
+        X = torch.from_numpy(rng.standard_normal((N, a.nrhs))).cuda()
+        H._dev_apply(X)
+        torch.cuda.synchronize()
+        return {"workload": "strong construct + one apply", "N": N, "samples": s}
     t_cold, _ = _wall(lambda: H.construct(a.rank, Om, Psi, Y, Z), reps=1)
     t_warm, _ = _wall(lambda: H.construct(a.rank, Om, Psi, Y, Z), reps=max(1, a.reps))
     X = torch.from_numpy(rng.standard_normal((N, a.nrhs))).cuda()
@@ -319,6 +326,8 @@ def main():
     ap.add_argument("kind", choices=["dense", "hbs", "helmholtz", "strong"])
     ap.add_argument("--adjacency", default="full", choices=["full", "partial"],
                     help="strong: near-field rule of the slab tree")
+    ap.add_argument("--once", action="store_true",
+                    help="strong: one construct and one apply only (for profiling)")
     ap.add_argument("--m", type=int, default=None)
     ap.add_argument("--slabs", type=int, default=8)
     ap.add_argument("--leaf", type=int, default=64)
