@@ -120,3 +120,59 @@ def test_hbstorch_construct_with_ulv_sampling():
     x = np.random.default_rng(3).standard_normal((A.shape[0], 2))
     assert relerr(H.matmat(x), A.matmat(x)) < 1e-10
     assert relerr(A.matmat(H.solve(x, "cuda")), x) < 1e-10
+
+
+def test_mat_assembler_mixed_sampling(golden):
+    """precision='mixed' takes the samples of an explicit matrix on the
+    tensor cores (split-BF16x3, ~1e-7 relative); the compressed operator of
+    the upstream assembler case then agrees with upstream's float64 result to
+    the sampling accuracy (1e-5), and the float64 default stays at 1e-12."""
+    need_gpu()
+    import types
+    from sslablu_gb300.matAssembly import matAssembler as MA
+    from sslablu_gb300.matAssembly.HBS.slabTree import slabTree
+    g = golden("assembler")
+    XX = _grid16()
+    perm = slabTree(XX, False, 8).perm_leaf
+    A = _exact_in_tree_order(3, 8, 6, 9, perm)
+    stmap = types.SimpleNamespace(A=A, XXI=XX)
+    for prec, tol in (("f64", TOL), ("mixed", 1e-5)):
+        np.random.seed(11)
+        asm = MA.matAssembler(MA.matAssemblerOptions("rkHBS", 0, 8, 3, precision=prec))
+        H = asm.assemble(stmap)
+        assert relerr(H.matmat(g["x"]), g["Ax"]) < tol, prec
+        assert relerr(H.rmatmat(g["x"]), g["ATx"]) < tol, prec
+
+
+def test_mat_assembler_rkhbs_strong():
+    """rkHMatAssembler_strong (upstream's rkHBS_strong names a class its
+    module lacks): the assembled strong-admissibility operator equals the
+    oracle's compression from the same draws (1e-12) and resolves the
+    coupling far better than the weak rkHBS at the same rank."""
+    need_gpu()
+    import types
+    from oracle.strong import StrongHBS
+    from sslablu_gb300.matAssembly import matAssembler as MA
+    from sslablu_gb300.matAssembly.HBS.slabTree import slabTree
+    from sslablu_gb300.synthetic import plane_coupling, plane_points
+    XX = plane_points(32)
+    A = plane_coupling(XX)
+    N, rk, leaf = A.shape[0], 16, 64
+    stmap = types.SimpleNamespace(A=A, XXI=XX)
+    np.random.seed(5)
+    asm = MA.rkHMatAssembler_strong(leaf, rk)
+    H = asm.assemble(stmap)
+    s = 5 * max(2 * rk, leaf) + rk + 20
+    np.random.seed(5)
+    Om = np.random.standard_normal((N, s))
+    Psi = np.random.standard_normal((N, s))
+    t = slabTree(XX, False, leaf)
+    O = StrongHBS(t.perm_leaf, t.nleaves, t.level_adj_list).construct(rk, Om, Psi, A @ Om,
+                                                                      A.T @ Psi)
+    x = np.random.default_rng(6).standard_normal((N, 3))
+    assert relerr(H.matmat(x), O.apply(x)) < TOL
+    assert relerr(H.rmatmat(x), O.apply(x, True)) < TOL
+    assert asm.stats.nbytes == H.nbytes > 0
+    np.random.seed(5)
+    W = MA.rkHMatAssembler(leaf, rk).assemble(stmap)
+    assert relerr(H.matmat(x), A @ x) < 0.2 * relerr(W.matmat(x), A @ x)
