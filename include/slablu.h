@@ -164,6 +164,21 @@ int slu_ulv_solve_grouped_plan_create(slu_handle_t h, int count, const slu_hbs_t
                                       double* const* B, const int* ldb, const int* nrhs,
                                       slu_solve_plan_t* out);
 int slu_ulv_solve_plan_destroy(slu_solve_plan_t plan);
+/* A fixed program of grouped phases as a solve plan: the phases run in
+ * order, each over its own members (count[p] of them; the member arrays are
+ * concatenated over the phases).  kind 0: X[i] <- A_i^{-1} X[i] (mode N, in
+ * place, the grouped solve); kind 1: Y[i] <- A_i X[i] (the grouped apply);
+ * X, Y device float64 blocks of nrhs[i] columns, leading dimension ld[i].
+ * Elementwise blocks of n[i] contiguous doubles (ops ignored): kind 2
+ * Y = X, 3 Y = 0, 4 Y += X, 5 Y -= X, 6 Y = X - Y.  Every table is built and
+ * uploaded once and the program captured as one CUDA graph; launch with
+ * slu_ulv_solve_plan_launch.  Used to run the red-black HBS solves of many
+ * slab systems together (omsdirectsolveHBS.py:489-558, RedBlackSolverHBS.solve,
+ * for a batch).  Beyond upstream. */
+int slu_grouped_program_create(slu_handle_t h, int nphase, const int* kind, const int* count,
+                               const slu_hbs_t* ops, double* const* X, double* const* Y,
+                               const int* ld, const int* nrhs, const long long* n,
+                               slu_solve_plan_t* out);
 
 /* Single-precision copy of the ULV factors and a float32 solve with the same
  * sweep; used inside iterative refinement (no upstream counterpart: the

@@ -77,6 +77,7 @@ SIGNATURES = {
     "slu_rb_solve_tc": [P, P, P, c_int, c_int],
     "slu_slab_maps_apply": [P, c_int, c_int, c_int, c_double, c_double, c_int, c_int, P, P, P,
                             c_int, P, P, c_int, c_int, c_int, c_double, P],
+    "slu_grouped_program_create": [P, c_int, P, P, P, P, P, P, P, P, ctypes.POINTER(c_void_p)],
     "slu_strong_create": [P, c_longlong, c_int, c_int, P, ctypes.POINTER(c_void_p)],
     "slu_strong_destroy": [P],
     "slu_strong_compress": [P, P, c_int, c_int, P, P, P, P, c_int, P, P, P],

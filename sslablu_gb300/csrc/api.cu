@@ -304,6 +304,25 @@ int slu_ulv_solve_grouped_plan_create(slu_handle_t h, int count, const slu_hbs_t
   });
 }
 
+int slu_grouped_program_create(slu_handle_t h, int nphase, const int* kind, const int* count,
+                               const slu_hbs_t* ops, double* const* X, double* const* Y,
+                               const int* ld, const int* nrhs, const long long* n,
+                               slu_solve_plan_t* out) {
+  return guard(h, [&] {
+    SLU_REQUIRE(h && out, "null argument");
+    SLU_REQUIRE(nphase >= 0 && (nphase == 0 || (kind && count)), "null argument");
+    long long total = 0;
+    for (int p = 0; p < nphase; ++p) total += count[p];
+    std::vector<slu::Hbs*> H(total, nullptr);
+    if (ops)
+      for (long long i = 0; i < total; ++i) H[i] = ops[i] ? &ops[i]->H : nullptr;
+    auto p = std::make_unique<slu_solve_plan_s>();
+    slu::grouped_program_create(h->h, nphase, kind, count, ops ? H.data() : nullptr, X, Y, ld,
+                                nrhs, n, p->P);
+    *out = p.release();
+  });
+}
+
 int slu_ulv_solve_plan_launch(slu_handle_t h, slu_solve_plan_t plan, int wait) {
   return guard(h, [&] {
     SLU_REQUIRE(h && plan, "null argument");

@@ -103,6 +103,28 @@ __global__ void seg_copy_k(const CopySeg* __restrict__ segs) {
   }
 }
 
+// One contiguous block of an elementwise phase of a grouped program.
+struct EwSeg {
+  const double* x;
+  double* y;
+  long long n;
+  int kind;   // 2 copy y = x, 3 zero y = 0, 4 add y += x, 5 sub y -= x, 6 rsub y = x - y
+};
+
+__global__ void ew_seg_k(const EwSeg* __restrict__ segs) {
+  const EwSeg s = segs[blockIdx.x];
+  for (long long e = (long long)blockIdx.y * blockDim.x + threadIdx.x; e < s.n;
+       e += (long long)gridDim.y * blockDim.x) {
+    switch (s.kind) {
+      case 2: s.y[e] = s.x[e]; break;
+      case 3: s.y[e] = 0.0; break;
+      case 4: s.y[e] = s.y[e] + s.x[e]; break;
+      case 5: s.y[e] = s.y[e] - s.x[e]; break;
+      default: s.y[e] = s.x[e] - s.y[e]; break;
+    }
+  }
+}
+
 // ------------------------------------------------------------------ host side
 // Per-member device buffers of a grouped ULV sweep (five of `stride`).
 template <typename T>
@@ -474,6 +496,157 @@ void grouped_solve_plan_create(Handle& h, int count, Hbs* const* ops, double* co
     SLU_CHECK_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
     try {
       launch_solve<double>(cs, steps, reinterpret_cast<const StepSeg<double>*>(dtab + at));
+    } catch (...) {
+      cudaStreamEndCapture(cs, &g);
+      if (g) cudaGraphDestroy(g);
+      throw;
+    }
+    SLU_CHECK_CUDA(cudaStreamEndCapture(cs, &g));
+    P.kernels = launch_thread() - n0;
+    launch_total() -= P.kernels;
+    launch_thread() = n0;
+    const cudaError_t e = cudaGraphInstantiate(&P.exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess)
+      throw Error(SLU_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+  } catch (...) {
+    cudaStreamDestroy(cs);
+    throw;
+  }
+  SLU_CHECK_CUDA(cudaStreamDestroy(cs));
+}
+
+void grouped_program_create(Handle& h, int nphase, const int* kind, const int* count,
+                            Hbs* const* ops, double* const* X, double* const* Y,
+                            const int* ld, const int* c, const long long* n, SolvePlan& P) {
+  SLU_REQUIRE(nphase >= 0 && (nphase == 0 || (kind && count)), "null argument");
+  cudaStream_t st = h.stream;
+  // pass 1: members of every phase, tables and the scratch each phase needs
+  struct Phase {
+    int kind;
+    std::vector<const Hbs*> H;
+    std::vector<int> cm, ldm, tr;
+    std::vector<double*> Xm, Ym;
+    std::vector<const double*> Xc;
+    std::vector<EwSeg> ew;
+    size_t scratch = 0;
+  };
+  std::vector<Phase> ph(nphase);
+  long long at = 0;
+  size_t nseg_total = 0, scratch_max = 0;
+  for (int p = 0; p < nphase; ++p) {
+    Phase& f = ph[p];
+    f.kind = kind[p];
+    SLU_REQUIRE(f.kind >= 0 && f.kind <= 6, "unknown grouped program phase");
+    SLU_REQUIRE(count[p] >= 0, "bad phase size");
+    for (int q = 0; q < count[p]; ++q, ++at) {
+      if (f.kind <= 1) {
+        SLU_REQUIRE(ops && ops[at] && X && X[at] && ld && c, "null argument");
+        SLU_REQUIRE(c[at] >= 1 && ld[at] >= c[at], "bad right-hand side");
+        Hbs& Hq = *ops[at];
+        if (f.kind == 0) {
+          SLU_REQUIRE(Hq.has_ulv && Hq.has_sweep, "ULV factors not computed");
+        } else {
+          SLU_REQUIRE(Y && Y[at], "null argument");
+          SLU_REQUIRE(Hq.has_mats, "HBS factors not loaded");
+          if (!Hq.has_apply[0]) {
+            std::lock_guard<std::mutex> lock(Hq.lazy_mu);
+            if (!Hq.has_apply[0]) hbs_make_apply(h, Hq, false);
+          }
+          f.Ym.push_back(Y[at]);
+          f.Xc.push_back(X[at]);
+          f.tr.push_back(0);
+        }
+        f.H.push_back(&Hq);
+        f.Xm.push_back(X[at]);
+        f.cm.push_back(c[at]);
+        f.ldm.push_back(ld[at]);
+      } else {
+        SLU_REQUIRE(n && n[at] >= 0 && Y && Y[at] && (f.kind == 3 || (X && X[at])),
+                    "bad elementwise block");
+        f.ew.push_back(EwSeg{f.kind == 3 ? nullptr : X[at], Y[at], n[at], f.kind});
+      }
+    }
+    for (size_t i = 0; i < f.H.size(); ++i) {
+      if (f.kind == 0) f.scratch += (5 * round64((size_t)f.H[i]->N * f.cm[i]) * 8 + 255) & ~size_t(255);
+      else f.scratch += (8 * hbs_apply_scratch_elems(*f.H[i], f.cm[i]) + 255) & ~size_t(255);
+      nseg_total += 2 * (size_t)f.H[i]->L;
+    }
+    nseg_total += f.ew.size();
+    scratch_max = std::max(scratch_max, f.scratch);
+    for (const Hbs* x : f.H) {
+      P.H.push_back(x);
+      P.alive.push_back(x->alive);
+      P.gen.push_back(x->sweep_gen);
+    }
+  }
+  // device memory: all tables (uploaded once), then one scratch region the
+  // phases share (they run one after another)
+  const size_t tab_bytes = blob_bound(nseg_total * std::max(sizeof(StepSeg<double>),
+                                                            sizeof(EwSeg)), 2 * nphase + 1);
+  P.scratch.alloc(tab_bytes + scratch_max + 512, st);
+  char* dtab = static_cast<char*>(P.scratch.p);
+  char* dscr = dtab + ((tab_bytes + 255) & ~size_t(255));
+  Blob blob;
+  std::vector<StepTable<double>> tabs(nphase);
+  std::vector<size_t> tab_at(nphase, 0);
+  for (int p = 0; p < nphase; ++p) {
+    Phase& f = ph[p];
+    if (f.kind >= 2) {
+      if (!f.ew.empty()) tab_at[p] = blob.put(f.ew);
+      continue;
+    }
+    if (f.H.empty()) continue;
+    size_t off = 0;
+    if (f.kind == 0) {
+      std::vector<SolveBufs<double>> buf(f.H.size());
+      for (size_t i = 0; i < f.H.size(); ++i) {
+        const size_t stride = round64((size_t)f.H[i]->N * f.cm[i]);
+        double* sb = reinterpret_cast<double*>(dscr + off);
+        buf[i].ru = sb;
+        for (int j = 0; j < 4; ++j) buf[i].P[j] = sb + (j + 1) * stride;
+        off += (5 * stride * 8 + 255) & ~size_t(255);
+      }
+      build_solve<double>(f.H, f.cm, f.Xm, f.ldm, buf, tabs[p]);
+    } else {
+      std::vector<ApplyBufs<double>> buf(f.H.size());
+      for (size_t i = 0; i < f.H.size(); ++i) {
+        buf[i] = carve_apply(*f.H[i], f.cm[i], reinterpret_cast<double*>(dscr + off));
+        off += (8 * hbs_apply_scratch_elems(*f.H[i], f.cm[i]) + 255) & ~size_t(255);
+      }
+      build_apply64(f.H, f.tr, f.cm, f.Xc, f.ldm, f.Ym, f.ldm, buf, tabs[p]);
+    }
+    tab_at[p] = blob.put(tabs[p].segs);
+  }
+  SLU_REQUIRE(blob.host.size() <= tab_bytes, "task table overflow");
+  upload(h, blob, dtab);
+  auto kern = group_step_kernel<double>;
+  for (int p = 0; p < nphase; ++p)
+    for (const sweep::LaunchPlan& lp : tabs[p].plan)
+      if (lp.ctas > 0) ensure_smem(reinterpret_cast<const void*>(kern), lp.smem);
+  SLU_CHECK_CUDA(cudaStreamSynchronize(st));   // tables in place before the capture
+  cudaStream_t cs = nullptr;
+  SLU_CHECK_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  cudaGraph_t g = nullptr;
+  const long long n0 = launch_thread();
+  try {
+    SLU_CHECK_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+    try {
+      for (int p = 0; p < nphase; ++p) {
+        const Phase& f = ph[p];
+        if (f.kind >= 2) {
+          if (f.ew.empty()) continue;
+          long long nmax = 1;
+          for (const EwSeg& e : f.ew) nmax = std::max(nmax, e.n);
+          dim3 grid((unsigned)f.ew.size(),
+                    (unsigned)std::min<long long>((nmax + 255) / 256, 64));
+          ew_seg_k<<<grid, 256, 0, cs>>>(reinterpret_cast<const EwSeg*>(dtab + tab_at[p]));
+          check_launch("ew_seg_k");
+        } else if (!f.H.empty()) {
+          launch_solve<double>(cs, tabs[p],
+                               reinterpret_cast<const StepSeg<double>*>(dtab + tab_at[p]));
+        }
+      }
     } catch (...) {
       cudaStreamEndCapture(cs, &g);
       if (g) cudaGraphDestroy(g);

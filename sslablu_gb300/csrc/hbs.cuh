@@ -195,6 +195,14 @@ void solve_plan_launch(Handle& h, SolvePlan& P, bool wait);
 void grouped_solve_plan_create(Handle& h, int count, Hbs* const* ops, double* const* B,
                                const int* ldb, const int* c, SolvePlan& P);
 
+// A fixed sequence of grouped phases -- solves (kind 0, in place), applies
+// (kind 1) and elementwise block operations (kinds 2-6: copy, zero, add,
+// subtract, reverse subtract) -- with every table uploaded once and the
+// whole sequence captured as one CUDA graph (group.cu).
+void grouped_program_create(Handle& h, int nphase, const int* kind, const int* count,
+                            Hbs* const* ops, double* const* X, double* const* Y,
+                            const int* ld, const int* c, const long long* n, SolvePlan& P);
+
 // The grouped mixed-precision refinement of hbs_refine_grouped for fixed
 // blocks: buffers and task tables built once, an iteration replayed as CUDA
 // graphs (group.cu).

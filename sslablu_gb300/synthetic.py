@@ -103,3 +103,26 @@ def plane_coupling(XX, shift=0.05, eps=0.02):
     Returns a float64 numpy array."""
     D = np.linalg.norm(XX[:, None, :] - XX[None, :, :] - np.array([shift, 0.0, 0.0]), axis=2)
     return np.exp(-D) / (D + eps)
+
+
+def poisson_slab_map(m, nx, width, height=1.0):
+    """The slab map S = (A_ii^{-1} A_ib[:, J])[Ic, :] of a double slab of the
+    5-point Poisson stencil (c11 = c22 = 1): m interior points along the
+    interface (spacing height / (m + 1)), nx grid points across the slab of
+    the given width (odd, so the centre line is a grid line).  With Dirichlet
+    ends the operator separates: in the sine basis Q of the interface
+    direction, mode q decouples into a three-term recurrence across the slab
+    whose solution from one edge to the centre is -1 / (2 cosh(M theta_q)),
+    M = (nx - 1) / 2, cosh theta_q = 1 + 2 (hx / hy)^2 sin^2(pi q / (2 (m + 1))).
+    The left and the right map are equal.  Returns S (m x m float64)."""
+    if nx % 2 == 0 or nx < 3:
+        raise ValueError("nx must be odd and >= 3")
+    hx = width / (nx - 1)
+    hy = height / (m + 1)
+    q = np.arange(1, m + 1)
+    t = 2.0 * (hx / hy) ** 2 * np.sin(np.pi * q / (2 * (m + 1))) ** 2
+    theta = np.log1p(t + np.sqrt(t * (t + 2.0)))           # arccosh(1 + t)
+    x = 0.5 * (nx - 1) * theta
+    sig = -np.exp(-x) / (1.0 + np.exp(-2.0 * x))            # -1 / (2 cosh x)
+    Q = np.sqrt(2.0 / (m + 1)) * np.sin(np.pi * np.outer(q, q) / (m + 1))
+    return (Q * sig) @ Q.T

@@ -1,0 +1,74 @@
+"""Grouped red-black HBS solves (direct_solve/grouped_rb.py) of uneven 2-D
+Poisson interface systems against each system's own RedBlackSolverHBS.solve
+(itself pinned to upstream in test_gpu_hbs_solvers.py) and against the
+exact float64 systems built from the stencil slab maps."""
+import numpy as np
+import pytest
+
+from tests._gpu import need_gpu
+
+pytestmark = pytest.mark.gpu
+
+
+def test_grouped_rb_hbs_matches_per_system_solves():
+    """Eight systems of 4..11 interfaces (padded to 4, 8, 16 blocks) and
+    128 / 256-point interfaces, 3 RHS each: the grouped solve equals every
+    system's own solve to 1e-12 and solves the exact system to the
+    compression accuracy."""
+    need_gpu()
+    import torch
+    from sslablu_gb300.direct_solve.grouped_rb import solve_rb_hbs_grouped
+    from sslablu_gb300.rbbatch import build_system, exact_apply
+    specs = [(4, 128, 16), (5, 256, 24), (8, 128, 20), (11, 256, 32), (6, 128, 48),
+             (9, 256, 16), (4, 256, 40), (7, 128, 28)]
+    built = [build_system(nI, m, rk, 100 + j) for j, (nI, m, rk) in enumerate(specs)]
+    rng = np.random.default_rng(3)
+    Bs = []
+    for (nI, m, rk), (rb, S, P) in zip(specs, built):
+        b = np.zeros((P * m, 3))
+        b[:nI * m] = rng.standard_normal((nI * m, 3))
+        Bs.append(torch.from_numpy(b).cuda())
+    from sslablu_gb300.direct_solve.grouped_rb import GroupedRBSolvePlan
+    xg = solve_rb_hbs_grouped([b[0] for b in built], Bs)
+    plan = GroupedRBSolvePlan([b[0] for b in built], Bs)
+    xq = [x.clone() for x in plan()]
+    for B in Bs:                                  # the plan reads whatever Bs hold
+        B.mul_(2.0)
+    xq2 = plan()
+    for (nI, m, rk), (rb, S, P), B, x, y, y2 in zip(specs, built, Bs, xg, xq, xq2):
+        xp = rb.solve(B) / 2.0
+        for z in (x, y, y2 / 2.0):
+            assert float(torch.linalg.norm(z - xp) / torch.linalg.norm(xp)) <= 1e-12
+        R = B / 2.0 - exact_apply(S, nI, P, x)
+        rel = torch.linalg.norm(R, dim=0) / torch.linalg.norm(B / 2.0, dim=0)
+        assert float(rel.max()) <= 1e-6, (nI, m, rk)
+    plan.close()
+
+
+def test_grouped_rb_hbs_one_dimensional_and_cyclic():
+    """1-D right-hand sides come back 1-D, and a periodic system (cyclic
+    red-black, wrap-around couplings) solved in a group equals its own
+    solve."""
+    need_gpu()
+    import torch
+    from sslablu_gb300.direct_solve.grouped_rb import solve_rb_hbs_grouped
+    from sslablu_gb300.direct_solve.omsdirectsolveHBS import RedBlackSolverHBS
+    from sslablu_gb300.rbbatch import build_system
+    rb0, S0, P0 = build_system(4, 128, 16, 7)
+    H = rb0.RB[0][0][1]                        # the compressed coupling of that system
+    per = RedBlackSolverHBS(128, 16, H.tree, False, cyclic=True)
+    per.factorize([[H, H] for _ in range(4)])
+    rng = np.random.default_rng(5)
+    b0 = rng.standard_normal(P0 * 128)
+    b1 = rng.standard_normal((4 * 128, 2))
+    x0, x1 = solve_rb_hbs_grouped([rb0, per], [b0, b1])
+    from sslablu_gb300.direct_solve.grouped_rb import GroupedRBSolvePlan
+    Bq = [torch.from_numpy(b0[:, None].copy()).cuda(), torch.from_numpy(b1.copy()).cuda()]
+    q0, q1 = GroupedRBSolvePlan([rb0, per], Bq)()
+    assert isinstance(x0, np.ndarray) and x0.shape == b0.shape
+    r0 = rb0.solve(b0)
+    r1 = per.solve(b1)
+    assert np.linalg.norm(x0 - r0) <= 1e-12 * np.linalg.norm(r0)
+    assert np.linalg.norm(x1 - r1) <= 1e-12 * np.linalg.norm(r1)
+    assert np.linalg.norm(q0.cpu().numpy()[:, 0] - r0) <= 1e-12 * np.linalg.norm(r0)
+    assert np.linalg.norm(q1.cpu().numpy() - r1) <= 1e-12 * np.linalg.norm(r1)

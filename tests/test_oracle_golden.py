@@ -337,3 +337,14 @@ def test_strong_oracle_matches_upstream(golden):
         assert len(O.E[0].tiles) == len(rc), name
         assert np.allclose(norms, g[p + "tile_norms"], rtol=1e-9, atol=0), name
         assert [len(O.U), len(O.E) + 1] == list(g[p + "nlev"]), name
+
+
+def test_poisson_slab_map_closed_form():
+    """The closed-form Poisson slab map of the workload generator equals the
+    oracle's (pinned to upstream's stencil pipeline) on both edges."""
+    from oracle.slabmaps import poisson2d_slab_maps
+    from sslablu_gb300.synthetic import poisson_slab_map
+    for m, nx, w in [(64, 5, 0.25), (128, 41, 2 / 9), (200, 17, 0.1)]:
+        S = poisson_slab_map(m, nx, w)
+        for ref in poisson2d_slab_maps(m, nx, w):
+            assert np.abs(S - ref).max() <= 1e-13 * np.abs(ref).max()
