@@ -684,6 +684,53 @@ def run_other(args):
                                             "(oracle), same operator and sketches, 64 RHS; "
                                             "construct %.2f s" % t_con,
                                   "construct_s": t_con})
+    elif args.workload == "c4_rbhbs":
+        # C4 as slab systems: uneven 2-D Poisson interface systems, each red-black
+        # HBS factored, solved together through one grouped program per step
+        from sslablu_gb300 import rbbatch
+        from sslablu_gb300.synthetic import poisson_slab_map
+        g, specs, built, Bs, res = rbbatch.run(systems=args.systems, nrhs=8,
+                                               reps=max(3, min(10, args.steps)))
+        # CPU: the oracle's red-black HBS (upstream's restated in numpy) on
+        # the first systems of the batch with 128-point interfaces
+        t_f = t_s = 0.0
+        nrhs_cpu, used = 0, 0
+        for (nI, m, rk), (rb, S, P), B in zip(specs, built, Bs):
+            if m != 128 or used >= 3:
+                continue
+            H = rb.RB[0][0][1]
+            td = (np.asarray(H.tree.perm_leaf), H.tree.nleaves, H.tree.nlevels)
+            Sd = S.cpu().numpy()
+            Z = np.zeros((m, m))
+            Sop = [(od.dense_op(Sd if 0 < i < nI else Z), od.dense_op(Sd if i < nI - 1 else Z))
+                   for i in range(P)]
+            np.random.seed(11)
+            t0 = time.perf_counter()
+            sv = od.RedBlackHBS(m, rk, td, False).factorize(Sop)
+            t_f += time.perf_counter() - t0
+            b = B.cpu().numpy()
+            t0 = time.perf_counter()
+            for j in range(b.shape[1]):
+                sv.solve(b[:, j])
+            t_s += time.perf_counter() - t0
+            nrhs_cpu += b.shape[1]
+            used += 1
+        line = dict(base, metric="batched red-black HBS RHS solves/sec (uneven 2-D Poisson "
+                                 "slab systems x 8 RHS)", unit="RHS/s",
+                    value=g["grouped_plan"]["rhs_per_s"],
+                    ms_per_step=g["grouped_plan"]["ms_per_step"],
+                    config={"workload": g["workload"], "systems": g["systems"],
+                            "sizes": g["sizes"], "factor_s": g["factor_s"],
+                            "arm": "every system's red-black solve as one grouped program "
+                                   "(GroupedRBSolvePlan: one CUDA graph per step)"},
+                    gpu_launches=g["grouped_plan"]["gpu_launches"],
+                    arms=g,
+                    cpu_baseline={"value": nrhs_cpu / t_s if t_s else None, "unit": "RHS/s",
+                                  "cores": os.cpu_count(), "kind": "port",
+                                  "sample": "upstream RedBlackSolverHBS restated in numpy, "
+                                            "the first %d systems with 128-point interfaces "
+                                            "(dense couplings), 8 RHS each; factor %.2f s"
+                                            % (used, t_f)})
     else:   # c4_batch
         import subprocess
         out = subprocess.run([sys.executable, "-m", "sslablu_gb300.batchbench", "--reps",
@@ -734,7 +781,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--workload", default="c2",
-                    choices=["c2", "c1_dense", "c3_hbs", "c3", "c3_strong", "c4_batch"])
+                    choices=["c2", "c1_dense", "c3_hbs", "c3", "c3_strong", "c4_batch",
+                             "c4_rbhbs"])
+    ap.add_argument("--systems", type=int, default=512,
+                    help="c4_rbhbs: number of slab systems in the batch")
     ap.add_argument("--served-rhs", type=lambda v: [int(x) for x in v.split(",") if x],
                     default=[1024, 4096],
                     help="batch widths of the served mixed vs plain comparison (comma separated)")

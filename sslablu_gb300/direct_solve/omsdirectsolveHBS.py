@@ -214,6 +214,29 @@ def _shape0(op):
 
 # concurrent compressions per red-black level (worker threads, one stream each)
 _LEVEL_WORKERS = 12
+_POOL = None
+_POOL_LOCK = threading.Lock()
+_TLS = threading.local()
+
+
+def _level_pool():
+    """The worker threads of the level compressions, made once per process:
+    each keeps one stream per device (and so one library handle and scratch
+    arena) for every factorisation, however many systems are factored."""
+    global _POOL
+    with _POOL_LOCK:
+        if _POOL is None:
+            _POOL = cf.ThreadPoolExecutor(max_workers=_LEVEL_WORKERS)
+        return _POOL
+
+
+def _worker_stream(dev):
+    streams = getattr(_TLS, "streams", None)
+    if streams is None:
+        streams = _TLS.streams = {}
+    if dev not in streams:
+        streams[dev] = torch.cuda.Stream(dev)
+    return streams[dev]
 
 
 # ---------------------------------------------------------------------------
@@ -368,20 +391,17 @@ class RedBlackSolverHBS(DirectSolver):
             return [h]
         dev = torch.cuda.current_device()
         torch.cuda.current_stream(dev).synchronize()   # inputs ready for every stream
-        local = threading.local()
 
         def run(job):
             h, Om, Psi = job
-            if getattr(local, "stream", None) is None:
-                local.stream = torch.cuda.Stream(dev)
             torch.cuda.set_device(dev)
-            with torch.cuda.stream(local.stream):
+            st = _worker_stream(dev)
+            with torch.cuda.stream(st):
                 h.construct_drawn(rk, Om, Psi)
-            local.stream.synchronize()
+            st.synchronize()
             return h
 
-        with cf.ThreadPoolExecutor(max_workers=min(len(jobs), _LEVEL_WORKERS)) as ex:
-            return list(ex.map(run, jobs))
+        return list(_level_pool().map(run, jobs))
 
     def factorize(self, S_rk_list, T=None):
         """omsdirectsolveHBS.py:397-430."""
