@@ -13,7 +13,9 @@
 // mixed path needs; the float64 path never uses this kernel.
 //
 // Kernel: one CTA per 128 x BN output tile (BN = 256 when the grid still
-// fills the GPU, else 128), 320 threads, one CTA per SM.
+// fills the GPU, else 128), 320 threads, one CTA per SM; tiles in bands of
+// 16 tile rows, column by column within a band (operand panels reused from
+// L2 by the CTAs resident together).
 //   warp 8 lane 0 : TMA producer, ring of (A 128 x 64, B BN x 64) bf16 slabs
 //                   (128B-swizzled, one mbarrier per stage, complete_tx); the
 //                   slice of each product is picked by the TMA coordinate
@@ -51,6 +53,7 @@ constexpr int CHUNK = 8;                         // k-tiles (of BK) per x0 y0 ch
 constexpr int kEpiWarps = 8;
 constexpr int kThreadsTC = 32 * (kEpiWarps + 2); // warps 0-7 epilogue, 8 TMA, 9 MMA
 constexpr long long kWaitLimit = 1LL << 22;      // try_wait rounds before giving up
+constexpr int kBand = 16;                        // tile rows per band of the tile order
 
 template <int BN>
 struct TcCfg {
@@ -194,7 +197,22 @@ tc_gemm_bf16_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_consta
   unsigned char* smem = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  // grouped tile order: the tiles run in bands of kBand tile rows, column
+  // by column inside a band, so the CTAs resident at one time share a few A
+  // row panels and a few B column panels (row-major order re-read every B
+  // panel once per few rows of tiles)
+  int tm, tn;
+  {
+    const int tiles_n = (N + BN - 1) / BN, tiles_m = (M + BM - 1) / BM;
+    const int id = blockIdx.x;
+    const int band = id / (kBand * tiles_n);
+    const int first = band * kBand;
+    const int rows = min(tiles_m - first, kBand);
+    const int in = id - band * kBand * tiles_n;
+    tm = first + in % rows;
+    tn = in / rows;
+  }
+  const int m0 = tm * BM, n0 = tn * BN;
   const int KT1 = Kp / BK;          // k-tiles of one product
   const int KT = 6 * KT1;
   const int NC = chunk_count(KT1, G::kChunk);
@@ -516,9 +534,10 @@ void launch_tc(cudaStream_t st, const __nv_bfloat16* Asl, const __nv_bfloat16* B
   CUtensorMap ma = make_map(Asl, M, 3LL * Kp, BM);
   CUtensorMap mb = make_map(Bsl, N, 3LL * Kp, BN);
   ensure_smem(reinterpret_cast<const void*>(tc_gemm_bf16_kernel<BN>), G::kSmem);
-  dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM);
-  tc_gemm_bf16_kernel<BN><<<grid, kThreadsTC, G::kSmem, st>>>(ma, mb, M, N, Kp, alpha, beta, C,
-                                                                ldc, err);
+  const long long tiles = (long long)((N + BN - 1) / BN) * ((M + BM - 1) / BM);
+  SLU_REQUIRE(tiles < (1LL << 31), "GEMM has too many tiles");
+  tc_gemm_bf16_kernel<BN><<<(unsigned)tiles, kThreadsTC, G::kSmem, st>>>(ma, mb, M, N, Kp, alpha,
+                                                                          beta, C, ldc, err);
   check_launch("tc_gemm_bf16_kernel");
 }
 
