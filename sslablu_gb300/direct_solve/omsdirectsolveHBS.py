@@ -364,11 +364,19 @@ class RedBlackSolverHBS(DirectSolver):
     level is an HBS compression (+ ULV for the diagonal) of an implicit
     operator, all on the GPU."""
 
-    def __init__(self, m, rk, tree, quad, cyclic=False):
+    def __init__(self, m, rk, tree, quad, cyclic=False, sketch_seed=None):
         super().__init__(m, cyclic)
         self.rk = rk
         self.tree = tree
         self.quad = quad
+        # beyond upstream: with sketch_seed the compressions draw their
+        # sketches on the device from one seeded torch generator (no host
+        # draws, no uploads); by default numpy's global RNG in upstream's
+        # order, so seeded runs reproduce upstream's sketches
+        self._gen = None
+        if sketch_seed is not None:
+            self._gen = torch.Generator(device="cuda")
+            self._gen.manual_seed(int(sketch_seed))
 
     def _hbs(self, linop, rk=None):
         """omsdirectsolveHBS.py:383-391."""
@@ -384,7 +392,7 @@ class RedBlackSolverHBS(DirectSolver):
         jobs = []
         for op in linops:
             h = HBSnew.HBSMAT(op, self.tree, self.quad)
-            jobs.append((h,) + h._sketches(rk))
+            jobs.append((h,) + h._sketches(rk, self._gen))
         if len(jobs) == 1:
             h, Om, Psi = jobs[0]
             h.construct_drawn(rk, Om, Psi)

@@ -138,8 +138,16 @@ class HBSMAT:
             self.constructHBS(rk)
 
     def _sketches(self, rk, rng=None):
+        """Om, Psi (N x s) from numpy's global RNG (upstream's draws), a numpy
+        Generator, or a torch.Generator on the device (drawn there: no host
+        draws and no upload; not upstream's stream)."""
         s = samples_for(rk, self.nl, self.fac)
         self.nSamples = s
+        if isinstance(rng, torch.Generator):
+            dev = rng.device if rng.device.type == "cuda" else torch.device("cuda")
+            Om = torch.randn((self.shape[1], s), generator=rng, dtype=torch.float64, device=dev)
+            Psi = torch.randn((self.shape[0], s), generator=rng, dtype=torch.float64, device=dev)
+            return Om, Psi
         if rng is None:
             Om = np.random.standard_normal(size=(self.shape[1], s))
             Psi = np.random.standard_normal(size=(self.shape[0], s))

@@ -9,7 +9,8 @@ interface size m ~ U{128, 256, 512, 1024, 2048}.  The slab maps S are the
 cells).  Each system's coupling is compressed once by the rkHBS assembler
 (leaf 64, rank ~ U{16..48}) and shared by all its interfaces.  Systems are
 padded to a power-of-two block count with decoupled identity blocks, as
-red-black requires, and factored by RedBlackSolverHBS.  ``--nrhs``
+red-black requires, and factored by RedBlackSolverHBS (sketches drawn on the
+device from a seeded generator).  ``--nrhs``
 right-hand sides ~ N(0, 1) per system (zero on the padding).
 
 Arms, each timed with CUDA events on the current stream after warm-up:
@@ -67,7 +68,7 @@ def build_system(nI, m, rk, seed):
         left = H if 0 < i < nI else Z
         right = H if i < nI - 1 else Z
         S_rk.append([left, right])
-    rb = RedBlackSolverHBS(m, rk, H.tree, False)
+    rb = RedBlackSolverHBS(m, rk, H.tree, False, sketch_seed=seed)
     rb.factorize(S_rk)
     return rb, torch.from_numpy(S).cuda(), P
 

@@ -72,3 +72,27 @@ def test_grouped_rb_hbs_one_dimensional_and_cyclic():
     assert np.linalg.norm(x1 - r1) <= 1e-12 * np.linalg.norm(r1)
     assert np.linalg.norm(q0.cpu().numpy()[:, 0] - r0) <= 1e-12 * np.linalg.norm(r0)
     assert np.linalg.norm(q1.cpu().numpy() - r1) <= 1e-12 * np.linalg.norm(r1)
+
+
+def test_device_sketches_factor_to_the_same_accuracy():
+    """RedBlackSolverHBS(sketch_seed=...) draws its compressions' sketches on
+    the device (beyond upstream); the factorisation is as accurate as with
+    upstream's host draws, and reproducible for a seed."""
+    need_gpu()
+    import torch
+    from sslablu_gb300.direct_solve.omsdirectsolveHBS import RedBlackSolverHBS
+    from sslablu_gb300.rbbatch import build_system, exact_apply
+    rb, S, P = build_system(6, 256, 24, 11)
+    H = rb.RB[0][0][1]
+    S_rk = [[rb.RB[0][0][i], rb.RB[0][3][i]] for i in range(P)]
+    b = torch.from_numpy(np.random.default_rng(2).standard_normal((P * 256, 2))).cuda()
+    b[6 * 256:] = 0.0
+    xs = []
+    for _ in range(2):
+        d = RedBlackSolverHBS(256, 24, H.tree, False, sketch_seed=5)
+        d.factorize(S_rk)
+        xs.append(d.solve(b))
+    assert torch.equal(xs[0], xs[1])
+    for x in (xs[0], rb.solve(b)):
+        r = torch.linalg.norm(b - exact_apply(S, 6, P, x), dim=0) / torch.linalg.norm(b, dim=0)
+        assert float(r.max()) <= 1e-6
