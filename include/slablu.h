@@ -224,18 +224,19 @@ int slu_hbs_set_refine_inner(slu_hbs_t op, int mode);
  * double-float); vectors between steps are float32 pairs, each right-hand-
  * side column normalised on entry by the power of two of its largest entry
  * (any float64 magnitude).  Relative error ~2^-50 of |S||z| per product.
- * Steps must read at most 96 rows per block
+ * Steps must read at most 128 rows per block
  * (SLU_ERR_ARG otherwise).  slu_hbs_prepare_ozaki builds the operator digits
  * (7 bf16 digits + a row scale per operator entry) once after a
  * factorisation; the solve / apply do it on first use.
- * slu_ulv_solve_ozaki: Y <- A^{-1} X; slu_hbs_apply_ozaki: Y <- A X (X, Y
- * N x nrhs float64, device, distinct).  No upstream counterpart: the
+ * slu_ulv_solve_ozaki: Y <- A^{-1} X, or A^{-T} X with trans (the
+ * transposed steps of slu_ulv_solve's mode T); slu_hbs_apply_ozaki: Y <- A X,
+ * or A^T X (X, Y N x nrhs float64, device, distinct).  No upstream counterpart: the
  * tensor-core form of the mixed-precision path. */
 int slu_hbs_prepare_ozaki(slu_handle_t h, slu_hbs_t op);
 int slu_ulv_solve_ozaki(slu_handle_t h, slu_hbs_t op, const double* X, int ldx, double* Y,
-                        int ldy, int nrhs);
+                        int ldy, int nrhs, int trans);
 int slu_hbs_apply_ozaki(slu_handle_t h, slu_hbs_t op, const double* X, int ldx, double* Y,
-                        int ldy, int nrhs);
+                        int ldy, int nrhs, int trans);
 
 /* Null-space rule of the next slu_hbs_compress of `op`: mode 0 projects each
  * block's sketch on the last n columns of the complete Q of Om_blk^T

@@ -85,8 +85,8 @@ SIGNATURES = {
     "slu_strong_info": [P, c_int, c_int, ctypes.POINTER(c_longlong)],
     "slu_strong_export": [P, P, c_int, c_int, P],
     "slu_hbs_prepare_ozaki": [P, P],
-    "slu_ulv_solve_ozaki": [P, P, P, c_int, P, c_int, c_int],
-    "slu_hbs_apply_ozaki": [P, P, P, c_int, P, c_int, c_int],
+    "slu_ulv_solve_ozaki": [P, P, P, c_int, P, c_int, c_int, c_int],
+    "slu_hbs_apply_ozaki": [P, P, P, c_int, P, c_int, c_int, c_int],
 }
 
 ERRORS = {1: "bad argument", 2: "allocation failed", 3: "CUDA error", 4: "numerical failure",

@@ -189,6 +189,7 @@ int slu_hbs_set_level(slu_handle_t h, slu_hbs_t op, int level, int Nb, int n, in
       H.has_mats = true;
       H.has_ulv = false;
       H.has_sweep = false;
+      H.has_oz = H.has_ozT = false;
       H.has_f32 = false;
       H.has_dfs = false;
       H.has_df = false;
@@ -201,17 +202,22 @@ int slu_hbs_set_level(slu_handle_t h, slu_hbs_t op, int level, int Nb, int n, in
 int slu_hbs_set_ulv_level(slu_handle_t h, slu_hbs_t op, int level, const double* Q,
                           const double* W, const double* R, const double* Uu) {
   return guard(h, [&] {
-    SLU_REQUIRE(h && op && Q && R, "null argument");
+    SLU_REQUIRE(h && op, "null argument");
     slu::Hbs& H = op->H;
     SLU_REQUIRE(H.has_mats, "set every level with slu_hbs_set_level first");
     SLU_REQUIRE(level >= 0 && level < H.L, "level out of range");
     const bool root = (level == H.L - 1);
-    SLU_REQUIRE(root || (W && Uu), "non-root levels need W and Uu");
     cudaStream_t st = h->h.stream;
     slu::Level& l = H.lv[level];
     const size_t rows = (size_t)l.Nb * l.n;
     l.kU = root ? 0 : l.k;
     l.uu_rows = root ? 0 : l.n - l.k;
+    // a factor with no entries (n = k: no eliminated rows, empty R and Uu)
+    // may come as a null pointer
+    SLU_REQUIRE(Q || rows * l.n == 0, "null Q");
+    SLU_REQUIRE(R || (size_t)l.Nb * l.nu * l.n == 0, "null R");
+    SLU_REQUIRE(root || W || rows * l.n == 0, "non-root levels need W");
+    SLU_REQUIRE(root || Uu || (size_t)l.Nb * l.uu_rows * l.kU == 0, "non-root levels need Uu");
     auto put = [&](slu::DevBuf& b, const double* src, size_t count) {
       b.alloc(8 * count, st);
       if (count) SLU_CHECK_CUDA(cudaMemcpyAsync(b.p, src, 8 * count, cudaMemcpyDeviceToDevice, st));
@@ -224,11 +230,13 @@ int slu_hbs_set_ulv_level(slu_handle_t h, slu_hbs_t op, int level, const double*
     }
     l.Uf.release(); l.Df.release(); l.Qf.release(); l.Wf.release(); l.Rf.release(); l.Uuf.release();
     bool all = true;
-    for (int t = 0; t < H.L; ++t) all = all && H.lv[t].Q.p && H.lv[t].R.p;
+    for (int t = 0; t < H.L; ++t)
+      all = all && H.lv[t].Q.p && (H.lv[t].R.p || (size_t)H.lv[t].Nb * H.lv[t].nu == 0);
     H.has_ulv = all;
     H.has_f32 = false;
     H.has_dfs = false;
     H.has_sweep = false;
+    H.has_oz = H.has_ozT = false;
     H.invalidate_plans();
     if (all) slu::hbs_make_sweep(h->h, H);
   });
@@ -379,34 +387,38 @@ int slu_hbs_prepare_ozaki(slu_handle_t h, slu_hbs_t op) {
 }
 
 int slu_ulv_solve_ozaki(slu_handle_t h, slu_hbs_t op, const double* X, int ldx, double* Y,
-                        int ldy, int nrhs) {
+                        int ldy, int nrhs, int trans) {
   return guard(h, [&] {
     SLU_REQUIRE(h && op && X && Y, "null argument");
     SLU_REQUIRE(nrhs >= 1 && ldx >= nrhs && ldy >= nrhs, "bad right-hand side shape");
     slu::Hbs& H = op->H;
     SLU_REQUIRE(H.has_ulv, "HBS operator has no ULV factorisation");
-    if (!H.has_oz) slu::hbs_make_oz(h->h, H);
+    if (trans ? !H.has_ozT : !H.has_oz) (trans ? slu::hbs_make_ozT : slu::hbs_make_oz)(h->h, H);
     const size_t bytes = slu::hbs_oz_scratch_bytes(H, nrhs);
     h->h.ws.reserve(bytes + 256, h->h.stream);
     void* scratch = h->h.ws.take<char>(bytes);
-    slu::ulv_solve_oz(h->h.stream, H, X, ldx, Y, ldy, nrhs, scratch,
-                      reinterpret_cast<unsigned int*>(h->h.info.as<int>()) + 1);
+    unsigned* err = reinterpret_cast<unsigned int*>(h->h.info.as<int>()) + 1;
+    if (trans)
+      slu::ulv_solve_oz_T(h->h.stream, H, X, ldx, Y, ldy, nrhs, scratch, err);
+    else
+      slu::ulv_solve_oz(h->h.stream, H, X, ldx, Y, ldy, nrhs, scratch, err);
   });
 }
 
 int slu_hbs_apply_ozaki(slu_handle_t h, slu_hbs_t op, const double* X, int ldx, double* Y,
-                        int ldy, int nrhs) {
+                        int ldy, int nrhs, int trans) {
   return guard(h, [&] {
     SLU_REQUIRE(h && op && X && Y, "null argument");
     SLU_REQUIRE(nrhs >= 1 && ldx >= nrhs && ldy >= nrhs, "bad right-hand side shape");
     slu::Hbs& H = op->H;
     SLU_REQUIRE(H.has_ulv, "HBS operator has no ULV factorisation");
-    if (!H.has_oz) slu::hbs_make_oz(h->h, H);
+    if (trans ? !H.has_ozT : !H.has_oz) (trans ? slu::hbs_make_ozT : slu::hbs_make_oz)(h->h, H);
     const size_t bytes = slu::hbs_oz_scratch_bytes(H, nrhs);
     h->h.ws.reserve(bytes + 256, h->h.stream);
     void* scratch = h->h.ws.take<char>(bytes);
     slu::hbs_apply_oz(h->h.stream, H, X, ldx, Y, ldy, nrhs, scratch,
-                      reinterpret_cast<unsigned int*>(h->h.info.as<int>()) + 1);
+                      reinterpret_cast<unsigned int*>(h->h.info.as<int>()) + 1, nullptr, nullptr,
+                      trans != 0);
   });
 }
 

@@ -368,6 +368,7 @@ void hbs_compress(Handle& h, Hbs& H, int Nb0, int rk, int s, const double* Om, c
   H.has_dfs = false;
   H.has_df = false;
   H.has_sweep = false;
+  H.has_oz = H.has_ozT = false;
   H.has_apply[0] = H.has_apply[1] = false;
   H.invalidate_plans();
   if (ulv) hbs_make_sweep(h, H);
@@ -418,6 +419,7 @@ void hbs_factor(Handle& h, Hbs& H) {
   H.has_ulv = true;
   H.has_f32 = false;
   H.has_dfs = false;
+  H.has_oz = H.has_ozT = false;   // digit forms of the step operators are stale
   H.invalidate_plans();
   hbs_make_sweep(h, H);
 }

@@ -110,6 +110,9 @@ struct Level {
   // digit forms for the tensor-core (tcgen05) sweep and residual: Qt, Sw
   // (the root: Sw), Aup, Adn (the root: Adn)
   OzOp ozQt, ozSw, ozUp, ozDn;
+  // and of the transposed solve and apply: Q, SwT (the root: SwT), AupT,
+  // AdnT (the root: AdnT)
+  OzOp ozQ, ozSwT, ozUpT, ozDnT;
 };
 
 struct RefinePlan;  // refine.cu: buffers + CUDA graphs of one refinement iteration
@@ -141,6 +144,7 @@ struct Hbs {
   bool has_mats = false, has_ulv = false, has_f32 = false, has_df = false, has_dfs = false;
   bool has_sweep = false;   // step operators composed (hbs_make_sweep)
   bool has_oz = false;      // digit forms for the tensor-core sweep (hbs_make_oz)
+  bool has_ozT = false;     // ... of the transposed solve and apply (hbs_make_ozT)
   // apply operators, mode N / T (hbs_make_apply); composed on first use, so
   // set only after the composing stream has finished (other threads may read
   // them from their own streams right after)
@@ -322,6 +326,8 @@ size_t hbs_nbytes(const Hbs& H, int which);
 // solve / apply run as tcgen05 block products of bfloat16 digits with exact
 // float32 accumulation.  Vectors between steps are double-float pairs.
 void hbs_make_oz(Handle& h, Hbs& H);
+// The digit forms of the transposed (mode T) solve and apply operators.
+void hbs_make_ozT(Handle& h, Hbs& H);
 // Scratch (bytes) of ulv_solve_oz / hbs_apply_oz for c right-hand sides.
 size_t hbs_oz_scratch_bytes(const Hbs& H, int c);
 // Y <- A^{-1} X (mode N) and Y <- A X on the tensor cores; X, Y N x c
@@ -329,12 +335,16 @@ size_t hbs_oz_scratch_bytes(const Hbs& H, int c);
 // device word set on a device wait timeout.
 void ulv_solve_oz(cudaStream_t st, const Hbs& H, const double* X, int ldx, double* Y, int ldy,
                   int c, void* scratch, unsigned* err);
+// Y <- A^{-T} X on the tensor cores (the transposed steps of the float64
+// mode-T solve, caller ordering through the inverse permutation).
+void ulv_solve_oz_T(cudaStream_t st, const Hbs& H, const double* X, int ldx, double* Y,
+                    int ldy, int c, void* scratch, unsigned* err);
 // With resb (N x c, leading dimension ldy) the apply returns the residual
 // Y = resb - A X instead, and rnorm2 (c entries, zeroed by the caller)
 // accumulates its squared column norms.
 void hbs_apply_oz(cudaStream_t st, const Hbs& H, const double* X, int ldx, double* Y, int ldy,
                   int c, void* scratch, unsigned* err, const double* resb = nullptr,
-                  double* rnorm2 = nullptr);
+                  double* rnorm2 = nullptr, bool trans = false);
 
 // Factor pointers of one level by arithmetic type (float64 factors or their
 // float32 copies).
@@ -372,6 +382,10 @@ struct FacPtr<dfloat> {
   static const dfloat* Qt(const Level& l) { return l.Qtdf.as<dfloat>(); }
   static const dfloat* Sw(const Level& l) { return l.Swdf.as<dfloat>(); }
   static const dfloat* Top(const Hbs& H) { return H.Topdf.as<dfloat>(); }
+  // the transposed steps run on the tensor cores only (their digit forms,
+  // ozSwT / ozQ): no double-float copies of Q or SwT exist
+  static const dfloat* Q(const Level&) { return nullptr; }
+  static const dfloat* SwT(const Level&) { return nullptr; }
 };
 
 // Grouped solves over many operators (group.cu): one launch per tree step for

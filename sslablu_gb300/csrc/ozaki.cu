@@ -12,18 +12,19 @@
 // Algorithms 59, 2012), in the form used on tensor cores by Mukunoki, Ozaki,
 // Ogita and Imamura (ISC 2020):
 //
-//   * every row i of S_b is scaled by a power of two 2^E_i (max |row| < 2^E_i)
-//     and written as seven balanced base-256 digits, S_ik = 2^E_i sum_s
-//     a_s,ik 2^(-8 s), |a_1| <= 256, |a_s| <= 128 (factor time, float64);
-//   * every column j of z_b is scaled by 2^F_j and split the same way in the
-//     kernel, from the double-float (or float64) input, with float32
-//     error-free extraction (x + sigma - sigma, sigma = 1.5 2^p) and two exact
-//     TwoSum merges of the low word: seven digits z_t, |z_4| <= 256, the others
-//     <= 128 (|z_1| <= 256);
+//   * every row i of S_b is scaled by a power of two 2^E_i (max |row| <
+//     2^(E_i - 1): scaled rows lie below 1/2) and written as seven balanced
+//     base-256 digits, S_ik = 2^E_i sum_s a_s,ik 2^(-8 (s + 1)), |a_s| <= 128
+//     (factor time, float64; 55 significant bits);
+//   * every column j of z_b is scaled by 2^F_j (below 1/2 again) and split
+//     the same way in the kernel, from the double-float (or float64) input,
+//     with float32 error-free extraction (x + sigma - sigma, sigma = 1.5 2^p)
+//     and two exact TwoSum merges of the low word: seven digits z_t,
+//     |z_3| <= 256 (counting from 0), the others <= 128;
 //   * for every digit pair with s + t <= 8 (28 products) the tensor cores form
 //     A_s Z_t in float32; all pairs of one diagonal d = s + t go into one TMEM
 //     accumulator.  Every term of accumulator d is an integer multiple of
-//     2^(-8 d) and, for steps of at most 96 columns (K), every partial sum
+//     2^(-8 d) and, for steps of at most 128 columns (K), every partial sum
 //     stays below 2^24 such units, so float32 accumulation is exact;
 //   * the epilogue adds the seven diagonals exactly, in float32 (TwoSums and
 //     additions whose results provably fit their grid: the diagonals lie on
@@ -68,7 +69,7 @@ namespace oz {
 
 constexpr int kDig = 7;           // digits per operand
 constexpr int kM = 128;           // right-hand-side columns per CTA (MMA M)
-constexpr int kMaxW = 96;         // widest step whose diagonal sums stay exact in float32
+constexpr int kMaxW = 128;        // widest step whose diagonal sums stay exact in float32
 constexpr int kMaxNT = 64;        // operator rows per CTA (MMA N)
 constexpr int kKC = 32;           // k per digitised chunk of z (two chunk buffers)
 constexpr int kDigWarps = 16;     // digitise z
@@ -231,18 +232,20 @@ __device__ __forceinline__ void f64_split(double x, int sh, float& h, float& l) 
 
 // The seven digit diagonals a_0..a_6 summed with no rounding error, as four
 // float32 terms v = h + l + e + f.  After the row and column scaling every
-// operator and vector entry is below 1 in magnitude, so with K <= 96 and the
-// digit bounds above, a_d is an integer multiple of 2^-(8d+16) with
-// |a_0| < 2^7, |a_1| < 2^-1.4, |a_2| < 2^-9.1, |a_3| < 2^-16.4,
-// |a_4| < 2^-24.6, |a_5| < 2^-32.2, |a_6| < 2^-40.1.  Alternating TwoSums
-// (exact by construction) with plain additions whose results provably fit
-// in 24 bits of their grid:
-//   (h, l) = TwoSum(a_0, a_1):  l a multiple of 2^-24, |l| <= ulp(h)/2 <= 2^-18
-//   l + a_2:  grid 2^-32, magnitude < 2^-9, so 23 bits: exact
+// operator and vector entry is below 1/2 in magnitude (|v| < K / 4 <= 2^5),
+// so with K <= 128 and the digit bounds above, a_d is an integer multiple of
+// 2^-(8d+16) with |a_0| < 2^5, |a_1| < 2^-2, |a_2| < 2^-9.4, |a_3| < 2^-16.7,
+// |a_4| < 2^-24.4, |a_5| < 2^-32.2, |a_6| <= 2^-40 (at most 2^24 units of its
+// grid each: exact float32 accumulation).  Alternating TwoSums (exact by
+// construction) with plain additions whose results provably fit in 24 bits
+// of their grid:
+//   (h, l) = TwoSum(a_0, a_1):  l a multiple of 2^-24, |l| <= ulp(h)/2 <= 2^-19
+//   l + a_2:  grid 2^-32, magnitude < 2^-9.3: exact
 //   (l, e) = TwoSum(l, a_3):    e a multiple of 2^-40, |e| <= 2^-33
-//   e + a_4:  grid 2^-48, magnitude < 2^-24.5: exact
-//   (e, f) = TwoSum(e, a_5):    f a multiple of 2^-56, |f| <= 2^-49
-//   f + a_6:  grid 2^-64, magnitude < 2^-39.9: exact.
+//   e + a_4:  grid 2^-48, magnitude < 2^-24.3: exact
+//   (e, f) = TwoSum(e, a_5):    f a multiple of 2^-56, |f| <= 2^-48
+//   f + a_6:  grid 2^-64, magnitude <= 2^-40 (1 + 2^-8): exact but for one
+//             unit of 2^-64 at the extreme bound (~2^-69 of |v|'s bound).
 // The digit products cancel heavily when |S z| is much smaller than
 // |S| |z| (the apply inside a residual b - A x), so no rounding may happen
 // before the sum is complete; the only rounding is the final one to a
@@ -683,7 +686,9 @@ __global__ void __launch_bounds__(kThreads, 1) oz_step_kernel(const OzStep o) {
         const float m =
             fmaxf(fmaxf(colmax[0][j], colmax[1][j]), fmaxf(colmax[2][j], colmax[3][j]));
         if (m > 0.f) {
-          int F = (int)((__float_as_uint(m) >> 23) & 255) - 126;   // m < 2^F
+          // m < 2^(F - 1): the scaled column lies below 1/2, so every
+          // digit is at most 128 units (256 for the fourth)
+          int F = (int)((__float_as_uint(m) >> 23) & 255) - 125;
           F = max(-100, min(100, F));
           inv = __uint_as_float((unsigned)(127 - F) << 23);
           cs = __uint_as_float((unsigned)(127 + F) << 23);
@@ -793,14 +798,14 @@ __global__ void oz_digits_kernel(const double* __restrict__ S, long long sS, int
   for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
   int E = 0;
   if (mx > 0.0) frexp(mx, &E);   // mx < 2^E
-  E = max(-120, min(126, E));
+  E = max(-119, min(126, E)) + 1;   // rows scaled below 1/2: every digit <= 128
   const int rt = r / NT, rr = r - rt * NT;
   if (lane == 0) rsc[(size_t)(b * ntile + rt) * NT + rr] = mx > 0.0 ? ldexpf(1.f, E) : 0.f;
   if (mx == 0.0) return;
   uint16_t* img = dig + (size_t)(b * ntile + rt) * kDig * NT * wP;
   const size_t base = (size_t)(rr >> 3) * (wP * 8) + (size_t)(rr & 7) * 8;
   for (int k = lane; k < w; k += 32) {
-    long long F = llrint(ldexp(row[k], 56 - E));   // |F| < 2^56
+    long long F = llrint(ldexp(row[k], 56 - E));   // |F| < 2^55
     int d[kDig];
     for (int t = kDig - 1; t >= 1; --t) {
       const long long dd = ((F + 128) & 255) - 128;
@@ -843,11 +848,14 @@ void make_op(cudaStream_t st, OzOp& o, const double* S, int Nb, int rows, int w)
   SLU_REQUIRE(S, "tensor-core sweep: step operator not composed");
   SLU_REQUIRE(w >= 1 && w <= kMaxW,
               "tensor-core sweep: a step reads " + std::to_string(w) +
-                  " rows per block; at most 96 keep its digit sums exact");
+                  " rows per block; at most 128 keep its digit sums exact");
   o.Nb = Nb;
   o.rows = rows;
   o.w = w;
   o.NT = rows > 32 ? 64 : (rows > 16 ? 32 : 16);
+  // steps wider than 96: 32-row tiles keep the seven operator digit images
+  // of a tile (NT x wP each) and the two z chunk buffers within 227 KB
+  if (w > 96) o.NT = std::min(o.NT, 32);
   o.ntile = (rows + o.NT - 1) / o.NT;
   o.wP = (w + 15) / 16 * 16;
   const size_t nd = (size_t)Nb * o.ntile * kDig * o.NT * o.wP;
@@ -915,6 +923,27 @@ void hbs_make_oz(Handle& h, Hbs& H) {
   H.has_oz = true;
 }
 
+void hbs_make_ozT(Handle& h, Hbs& H) {
+  SLU_REQUIRE(H.has_sweep, "step operators not composed (factor the operator first)");
+  std::lock_guard<std::mutex> lock(H.lazy_mu);
+  if (H.has_ozT) return;
+  if (!H.has_apply[1]) hbs_make_apply(h, H, true);
+  cudaStream_t st = h.stream;
+  const int L = H.L;
+  for (int t = 0; t + 1 < L; ++t) {
+    Level& l = H.lv[t];
+    oz::make_op(st, l.ozQ, l.Q.as<double>(), l.Nb, l.n, l.n);
+    oz::make_op(st, l.ozSwT, l.SwT.as<double>(), l.Nb, l.nu + 2 * l.k, t == 0 ? l.n : 2 * l.n);
+    oz::make_op(st, l.ozUpT, l.AupT.as<double>(), l.Nb, l.k, l.n);
+    oz::make_op(st, l.ozDnT, l.AdnT.as<double>(), l.Nb, l.n, l.n + l.k);
+  }
+  Level& r = H.lv[L - 1];
+  oz::make_op(st, r.ozSwT, r.SwT.as<double>(), 1, r.n, L == 1 ? r.n : 2 * r.n);
+  oz::make_op(st, r.ozDnT, r.AdnT.as<double>(), 1, r.n, r.n);
+  SLU_CHECK_CUDA(cudaStreamSynchronize(st));
+  H.has_ozT = true;
+}
+
 size_t hbs_oz_scratch_bytes(const Hbs& H, int c) {
   const size_t nc = ((size_t)H.N * c + 63) & ~size_t(63);
   const size_t solve = 5 * nc;
@@ -979,9 +1008,53 @@ void ulv_solve_oz(cudaStream_t st, const Hbs& H, const double* X, int ldx, doubl
   }
 }
 
+// The transposed steps of ulv_solve_T (ulv_solve.cu, solve_steps_T) on the
+// tensor cores: backward^T steps up the tree (the caller's rows gathered
+// through the inverse permutation), the root^T step, forward^T steps down
+// (Q itself), the result scattered through the inverse permutation.
+void ulv_solve_oz_T(cudaStream_t st, const Hbs& H, const double* X, int ldx, double* Y,
+                    int ldy, int c, void* scratch, unsigned* err) {
+  SLU_REQUIRE(H.has_ozT, "tensor-core transposed sweep not prepared");
+  SLU_REQUIRE(static_cast<const void*>(X) != static_cast<const void*>(Y),
+              "tensor-core sweep: input and output must be different buffers");
+  const int L = H.L;
+  const int64_t* ip = H.iperm.as<int64_t>();
+  const size_t nc = ((size_t)H.N * c + 63) & ~size_t(63);
+  unsigned* cb = oz_colbits(scratch);
+  dfloat* ws = oz_vectors(scratch, c);
+  dfloat* ru = ws;
+  dfloat* P[2] = {ws + nc, ws + 3 * nc};   // two strides each (a backward^T writes 2k rows)
+  const dfloat* x = reinterpret_cast<const dfloat*>(X);
+  dfloat* y = reinterpret_cast<dfloat*>(Y);
+  const std::vector<long long>& NN = H.NN;
+  oz::col_max(st, H.N, c, X, ldx, cb);
+  if (L == 1) {
+    oz::launch(st, sweep::rootT_step<dfloat>(H, x, ldx, ip, y, ldy, ip, c), H.lv[0].ozSwT, true,
+               true, cb, err, "oz_rootT_step");
+    return;
+  }
+  for (int t = 0; t + 1 < L; ++t)
+    oz::launch(st,
+               sweep::backwardT_step<dfloat>(H, t, t == 0 ? x : P[(t - 1) & 1], t == 0 ? ldx : c,
+                                             t == 0 ? ip : nullptr, ru + NN[t] * c, P[t & 1], c),
+               H.lv[t].ozSwT, t == 0, false, cb, err, "oz_bwdT_step");
+  int cur = (L - 1) & 1;
+  oz::launch(st, sweep::rootT_step<dfloat>(H, P[(L - 2) & 1], c, nullptr, P[cur], c, nullptr, c),
+             H.lv[L - 1].ozSwT, false, false, cb, err, "oz_rootT_step");
+  for (int t = L - 2; t >= 0; --t) {
+    const bool leaf = t == 0;
+    oz::launch(st,
+               sweep::forwardT_step<dfloat>(H, t, ru + NN[t] * c, P[cur], leaf ? y : P[cur ^ 1],
+                                            leaf ? ldy : c, leaf ? ip : nullptr, c),
+               H.lv[t].ozQ, false, leaf, cb, err, "oz_fwdT_step");
+    cur ^= 1;
+  }
+}
+
 void hbs_apply_oz(cudaStream_t st, const Hbs& H, const double* X, int ldx, double* Y, int ldy,
-                  int c, void* scratch, unsigned* err, const double* resb, double* rnorm2) {
-  SLU_REQUIRE(H.has_oz, "tensor-core sweep not prepared");
+                  int c, void* scratch, unsigned* err, const double* resb, double* rnorm2,
+                  bool trans) {
+  SLU_REQUIRE(trans ? H.has_ozT : H.has_oz, "tensor-core apply not prepared");
   SLU_REQUIRE(static_cast<const void*>(X) != static_cast<const void*>(Y),
               "tensor-core apply: input and output must be different buffers");
   const int L = H.L;
@@ -1002,7 +1075,7 @@ void hbs_apply_oz(cudaStream_t st, const Hbs& H, const double* X, int ldx, doubl
     const Level& r = H.lv[0];
     oz::launch(st,
                sweep::down_step<dfloat>(r, nullptr, true, x, ldx, perm, nullptr, y, ldy, perm, c),
-               r.ozDn, true, true, cb, err, "oz_apply_root", resb, rnorm2);
+               (trans ? r.ozDnT : r.ozDn), true, true, cb, err, "oz_apply_root", resb, rnorm2);
     return;
   }
   for (int t = 0; t + 1 < L; ++t) {
@@ -1010,13 +1083,13 @@ void hbs_apply_oz(cudaStream_t st, const Hbs& H, const double* X, int ldx, doubl
     oz::launch(st,
                sweep::up_step<dfloat>(l, nullptr, t == 0 ? x : VV[t], t == 0 ? ldx : c,
                                       t == 0 ? perm : nullptr, VV[t + 1], c),
-               l.ozUp, t == 0, false, cb, err, "oz_apply_up");
+               (trans ? l.ozUpT : l.ozUp), t == 0, false, cb, err, "oz_apply_up");
   }
   const Level& r = H.lv[L - 1];
   oz::launch(st,
              sweep::down_step<dfloat>(r, nullptr, true, VV[L - 1], c, nullptr, nullptr, u[0], c,
                                       nullptr, c),
-             r.ozDn, false, false, cb, err, "oz_apply_root");
+             (trans ? r.ozDnT : r.ozDn), false, false, cb, err, "oz_apply_root");
   int cur = 0;
   for (int t = L - 2; t >= 0; --t) {
     const Level& l = H.lv[t];
@@ -1025,7 +1098,7 @@ void hbs_apply_oz(cudaStream_t st, const Hbs& H, const double* X, int ldx, doubl
                sweep::down_step<dfloat>(l, nullptr, false, leaf ? x : VV[t], leaf ? ldx : c,
                                         leaf ? perm : nullptr, u[cur], leaf ? y : u[cur ^ 1],
                                         leaf ? ldy : c, leaf ? perm : nullptr, c),
-               l.ozDn, leaf, leaf, cb, err, "oz_apply_down", leaf ? resb : nullptr,
+               (trans ? l.ozDnT : l.ozDn), leaf, leaf, cb, err, "oz_apply_down", leaf ? resb : nullptr,
                leaf ? rnorm2 : nullptr);
     cur ^= 1;
   }

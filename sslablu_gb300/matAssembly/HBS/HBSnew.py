@@ -410,26 +410,30 @@ class HBSMAT:
                                              B.shape[1]))
         return dv.finish(B, b, one)
 
-    def solve_ozaki(self, b):
-        """Mode-N solve on the tensor cores (slu_ulv_solve_ozaki): every step
+    def solve_ozaki(self, b, mode="N"):
+        """Solve on the tensor cores (slu_ulv_solve_ozaki): every step
         product as bfloat16 tcgen05 products of error-free base-256 digit
         splits of operator and vector (Ozaki scheme), float64-level accuracy;
-        double-float vectors between steps."""
+        double-float vectors between steps.  mode 'T' solves with A^T (the
+        transposed steps of the float64 mode-T solve)."""
+        if mode not in ("N", "T"):
+            raise ValueError("mode not recognized")
         X, one = dv.prepare_rhs(b)
         X = dv.as_2d(X).contiguous()
         Y = torch.empty_like(X)
         L.check(L.lib().slu_ulv_solve_ozaki(L.handle(), self._op, L.ptr(X), X.shape[1],
-                                            L.ptr(Y), Y.shape[1], X.shape[1]))
+                                            L.ptr(Y), Y.shape[1], X.shape[1], int(mode == "T")))
         return dv.finish(Y, b, one)
 
-    def apply_ozaki(self, x):
-        """A x on the tensor cores (slu_hbs_apply_ozaki): the apply steps as
-        digit-split bfloat16 products, float64-level accuracy."""
+    def apply_ozaki(self, x, trans=False):
+        """A x (A^T x with trans) on the tensor cores (slu_hbs_apply_ozaki):
+        the apply steps as digit-split bfloat16 products, float64-level
+        accuracy."""
         X, one = dv.prepare_rhs(x)
         X = dv.as_2d(X).contiguous()
         Y = torch.empty_like(X)
         L.check(L.lib().slu_hbs_apply_ozaki(L.handle(), self._op, L.ptr(X), X.shape[1],
-                                            L.ptr(Y), Y.shape[1], X.shape[1]))
+                                            L.ptr(Y), Y.shape[1], X.shape[1], int(bool(trans))))
         return dv.finish(Y, x, one)
 
     def solve_refined(self, b, tol=1e-10, maxit=10, inner="dfloat"):

@@ -31,9 +31,16 @@ def _levels(Dmats, Umats, Nbvec):
     return out
 
 
+def _fac(Nbvec):
+    """Children per box: the ratio of consecutive block counts, as upstream
+    derives it (ULVsparse.py:120, 143: NbB // NbA); 2 for a one-level tree."""
+    return int(Nbvec[0]) // int(Nbvec[1]) if len(Nbvec) > 1 else 2
+
+
 def compute_ULV(Umats, Dmats, Vmats, Nbvec):
-    """ULV factors of given HBS factors (ULVsparse.py:231-293)."""
-    H = HBSMAT().set_mats(Umats, Dmats, Vmats, list(Nbvec), fac=2)
+    """ULV factors of given HBS factors (ULVsparse.py:231-293); binary or
+    quad trees."""
+    H = HBSMAT().set_mats(Umats, Dmats, Vmats, list(Nbvec), fac=_fac(Nbvec))
     H.compute_ULV()
     Lv = len(Dmats)
     Uulist = [H._export(6, t) for t in range(Lv - 1)]
@@ -48,7 +55,7 @@ def solve(Umats, Dmats, Qlist, Wlist, Uulist, Rlist, NNvec, Nbvec, rhs, mode="N"
     N = int(Dmats[0].shape[0])
     geo = _levels(Dmats, Umats, Nbvec)
     H = HBSMAT()
-    H.fac = 2
+    H.fac = _fac(Nbvec)
     H.shape = (N, N)
     H.perm = np.arange(N, dtype=np.int64)
     H._new_op(N, Lv, None)

@@ -16,8 +16,6 @@ def test_ulvsparse_functions(golden, name):
     from sslablu_gb300.matAssembly.HBS import ULVsparse
     g = golden(name)
     S, Nbvec = hbs_from_fixture(g)
-    if g["quad"]:
-        pytest.skip("ULVsparse.compute_ULV mirror builds binary-tree operators only")
     Ql, Wl, Uul, Rl, NNv = ULVsparse.compute_ULV(S.Umats, S.Dmats, S.Vmats, Nbvec)
     assert np.array_equal(NNv, g["ulv_NNvec"])
     x = g["x"]

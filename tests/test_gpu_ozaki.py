@@ -83,3 +83,48 @@ def test_ozaki_c2_operator_refined():
     res = np.linalg.norm(r, axis=0) / np.linalg.norm(b, axis=0)
     assert res.max() <= 1e-10
     assert relerr(xr, O.solve(b)) < 1e-10
+
+
+@pytest.mark.parametrize("k,nl,L,quad,nrhs", [(8, 16, 4, False, 5), (16, 32, 5, False, 64),
+                                              (8, 16, 3, True, 7), (32, 64, 4, False, 300)])
+def test_ozaki_transposed_apply_and_solve(k, nl, L, quad, nrhs):
+    """A^T x and A^{-T} b on the tensor cores: the apply against the oracle's
+    rmatmat and the solve against the float64 mode-T solve (the same
+    transposed steps, pinned to upstream in test_gpu_hbs.py), 1e-12; at
+    rank 32 / leaf 64 the transposed backward steps read 128 rows per block
+    (the widest step the digit sums keep exact)."""
+    need_gpu()
+    G, O = _pair(k, nl, L, quad, seed=3 * k + nl + L + nrhs)
+    x = np.random.default_rng(nrhs + 1).standard_normal((G.shape[0], nrhs))
+    assert relerr(G.apply_ozaki(x, trans=True), O.rmatmat(x)) < TOL
+    assert relerr(G.solve_ozaki(x, mode="T"), G.solve(x, mode="T")) < TOL
+    assert relerr(G.solve_ozaki(x[:, 0], mode="T"), G.solve(x[:, 0], mode="T")) < TOL
+
+
+def test_ozaki_refactor_rebuilds_digits():
+    """A refactored operator's tensor-core solve uses the new factors (the
+    digit forms are rebuilt, not reused)."""
+    need_gpu()
+    G, O = _pair(16, 32, 4, False, seed=9)
+    x = np.random.default_rng(2).standard_normal((G.shape[0], 40))
+    import torch
+    from sslablu_gb300 import _lib as L
+    G.solve_ozaki(x)                     # builds the digit forms
+    G2, O2 = _pair(16, 32, 4, False, seed=10)
+    keep = []
+    Lv = len(O2.Dmats)
+    for t in range(Lv):                  # new factors into the same operator
+        Nb = int(O2.Nbvec[t])
+        D = torch.from_numpy(np.ascontiguousarray(O2.Dmats[t])).cuda()
+        n = D.shape[0] // Nb
+        U = V = None
+        k = 0
+        if t < Lv - 1:
+            U = torch.from_numpy(np.ascontiguousarray(O2.Umats[t])).cuda()
+            V = torch.from_numpy(np.ascontiguousarray(O2.Vmats[t])).cuda()
+            k = U.shape[1]
+        keep += [U, V, D]
+        L.check(L.lib().slu_hbs_set_level(L.handle(), G._op, t, Nb, n, k, L.ptr(U), L.ptr(V),
+                                          L.ptr(D)))
+    G.compute_ULV()
+    assert relerr(G.solve_ozaki(x), O2.solve(x)) < TOL
