@@ -721,6 +721,7 @@ def run_other(args):
                     ms_per_step=g["grouped_plan"]["ms_per_step"],
                     config={"workload": g["workload"], "systems": g["systems"],
                             "sizes": g["sizes"], "factor_s": g["factor_s"],
+                            "factor_workers": g["factor_workers"],
                             "arm": "every system's red-black solve as one grouped program "
                                    "(GroupedRBSolvePlan: one CUDA graph per step)"},
                     gpu_launches=g["grouped_plan"]["gpu_launches"],

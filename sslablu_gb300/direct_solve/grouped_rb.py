@@ -17,12 +17,57 @@ red-black requires), rank and right-hand-side count.  Blocks that are the
 identity (``id_op``, the level-0 diagonal of an I + S system) are copies;
 operators marked ``_zero`` (decoupled padding) contribute nothing; other
 dense operators run one by one.
+
+``factorize_many`` builds the systems of a batch concurrently: the
+factorisations are independent, and one system's red-black levels alone
+leave the GPU idle between its small launches and host steps.
 """
+import concurrent.futures as cf
+import threading
+
 import torch
 
 from .. import _dev as dv
 from ..grouped import apply_grouped, solve_grouped_device
-from .omsdirectsolveHBS import id_op
+from .omsdirectsolveHBS import _worker_stream, id_op
+
+
+_BUILD_POOLS = {}
+_BUILD_LOCK = threading.Lock()
+
+
+def _build_pool(workers):
+    """Worker threads for factorize_many, made once per size and kept: each
+    thread keeps one stream per device (and so one library handle), however
+    many batches are factored."""
+    with _BUILD_LOCK:
+        if workers not in _BUILD_POOLS:
+            _BUILD_POOLS[workers] = cf.ThreadPoolExecutor(max_workers=workers)
+        return _BUILD_POOLS[workers]
+
+
+def factorize_many(jobs, workers=6):
+    """Run independent factorisation jobs (callables, each building and
+    factoring one system) ``workers`` at a time.  Each job runs on a worker
+    thread with its own CUDA stream, and so its own library handle and
+    scratch arena; its stream is synchronised before the job counts as done,
+    so every result is ready for use on any stream.  Returns the results in
+    job order.  Jobs that draw from a shared host RNG must serialise those
+    draws themselves."""
+    dev = torch.cuda.current_device()
+    torch.cuda.current_stream(dev).synchronize()   # inputs made on the caller's stream
+    if workers <= 1 or len(jobs) <= 1:
+        return [j() for j in jobs]
+
+    def run(job):
+        torch.cuda.set_device(dev)
+        st = _worker_stream(dev)
+        with torch.cuda.stream(st):
+            out = job()
+        st.synchronize()
+        return out
+
+    return list(_build_pool(workers).map(run, jobs))
 
 
 def _is_hbs(op):

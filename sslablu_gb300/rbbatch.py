@@ -10,7 +10,8 @@ cells).  Each system's coupling is compressed once by the rkHBS assembler
 (leaf 64, rank ~ U{16..48}) and shared by all its interfaces.  Systems are
 padded to a power-of-two block count with decoupled identity blocks, as
 red-black requires, and factored by RedBlackSolverHBS (sketches drawn on the
-device from a seeded generator).  ``--nrhs``
+device from a seeded generator); ``--workers`` systems are built at a
+time, each on its own stream.  ``--nrhs``
 right-hand sides ~ N(0, 1) per system (zero on the padding).
 
 Arms, each timed with CUDA events on the current stream after warm-up:
@@ -25,8 +26,11 @@ float64 systems (dense maps), and the largest difference between the two
 arms.  Prints one JSON line.
 """
 import argparse
+import contextlib
+import functools
 import json
 import statistics
+import threading
 import time
 import types
 
@@ -48,9 +52,11 @@ def system_specs(systems, seed, sizes=(128, 256, 512, 1024, 2048), ranks=(16, 48
     return out
 
 
-def build_system(nI, m, rk, seed):
+def build_system(nI, m, rk, seed, rng_lock=None):
     """(solver, dense S on the device, padded block count): the factored
-    RedBlackSolverHBS of one system and its exact coupling."""
+    RedBlackSolverHBS of one system and its exact coupling.  ``rng_lock``
+    (held while numpy's global RNG is seeded and drawn from) lets systems
+    be built on several threads with the draws of a one-by-one build."""
     from .direct_solve.omsdirectsolveHBS import RedBlackSolverHBS, _linop_from_mat
     from .matAssembly.matAssembler import rkHMatAssembler
     from .synthetic import poisson_slab_map
@@ -58,8 +64,9 @@ def build_system(nI, m, rk, seed):
     nx = int(round(width * (m + 1))) // 2 * 2 + 1          # square cells, odd
     S = poisson_slab_map(m, max(nx, 3), width)
     XX = np.linspace(0.0, 1.0, m + 2)[1:-1]
-    np.random.seed(seed)
-    H = rkHMatAssembler(64, rk).assemble(types.SimpleNamespace(A=S, XXI=XX))
+    with rng_lock if rng_lock is not None else contextlib.nullcontext():
+        np.random.seed(seed)
+        H = rkHMatAssembler(64, rk).assemble(types.SimpleNamespace(A=S, XXI=XX))
     Z = _linop_from_mat(np.zeros((m, m)))
     Z._zero = True
     P = 1 << int(np.ceil(np.log2(nI)))
@@ -71,6 +78,16 @@ def build_system(nI, m, rk, seed):
     rb = RedBlackSolverHBS(m, rk, H.tree, False, sketch_seed=seed)
     rb.factorize(S_rk)
     return rb, torch.from_numpy(S).cuda(), P
+
+
+def build_systems(specs, seed, workers=6):
+    """build_system of every spec (system j seeded seed + 17 j), ``workers``
+    systems at a time (grouped_rb.factorize_many: one stream per worker)."""
+    from .direct_solve.grouped_rb import factorize_many
+    lock = threading.Lock()
+    jobs = [functools.partial(build_system, nI, m, rk, seed + 17 * j, lock)
+            for j, (nI, m, rk) in enumerate(specs)]
+    return factorize_many(jobs, workers)
 
 
 def exact_apply(S, nI, P, X):
@@ -101,12 +118,12 @@ def _time(fn, reps, warmup=2):
     return statistics.median(ts)
 
 
-def run(systems=512, nrhs=8, reps=10, seed=20261205):
+def run(systems=512, nrhs=8, reps=10, seed=20261205, workers=6):
     from .direct_solve.grouped_rb import solve_rb_hbs_grouped
     torch.cuda.set_device(0)
     specs = system_specs(systems, seed)
     t0 = time.perf_counter()
-    built = [build_system(nI, m, rk, seed + 17 * j) for j, (nI, m, rk) in enumerate(specs)]
+    built = build_systems(specs, seed, workers)
     torch.cuda.synchronize()
     t_factor = time.perf_counter() - t0
     rng = np.random.default_rng(seed + 1)
@@ -122,7 +139,7 @@ def run(systems=512, nrhs=8, reps=10, seed=20261205):
                        "compressed by rkHBS leaf 64 rank U{16..48}, red-black HBS, %d RHS "
                        "each" % (systems, nrhs),
            "systems": systems, "nrhs": nrhs, "factor_s": t_factor,
-           "factor_per_system_ms": 1e3 * t_factor / systems,
+           "factor_per_system_ms": 1e3 * t_factor / systems, "factor_workers": workers,
            "sizes": {str(s): sum(1 for sp in specs if sp[1] == s)
                      for s in (128, 256, 512, 1024, 2048)}}
     from .direct_solve.grouped_rb import GroupedRBSolvePlan
@@ -166,8 +183,10 @@ def main():
     ap.add_argument("--nrhs", type=int, default=8)
     ap.add_argument("--reps", type=int, default=10)
     ap.add_argument("--seed", type=int, default=20261205)
+    ap.add_argument("--workers", type=int, default=6,
+                    help="systems built and factored at a time (one stream each)")
     a = ap.parse_args()
-    out = run(a.systems, a.nrhs, a.reps, a.seed)[0]
+    out = run(a.systems, a.nrhs, a.reps, a.seed, a.workers)[0]
     print(json.dumps(out))
 
 
