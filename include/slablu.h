@@ -49,6 +49,12 @@ int slu_version(void);
 /* Kernels launched by this library so far in this process (host-side count,
  * all streams); a diagnostic for benchmarks. */
 long long slu_launch_count(void);
+/* Host waits made by the calling thread (slu_sync and the library's own
+ * waits): 0 spins (the default: lowest latency), 1 sleeps on a blocking-sync
+ * event.  For worker threads that run many factorisations at once, whose
+ * spinning waits would take the host cores from the threads launching work.
+ * Beyond upstream (a host runtime setting of this library). */
+void slu_set_blocking_waits(int on);
 /* Copies the last error message of this thread into buf (NUL terminated). */
 int slu_last_error(char* buf, size_t len);
 /* stream: a cudaStream_t (NULL = legacy default stream). */

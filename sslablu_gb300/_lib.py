@@ -115,6 +115,8 @@ def load_cdll(path=LIB_PATH):
         f.restype = c_int
     dll.slu_launch_count.argtypes = []
     dll.slu_launch_count.restype = c_longlong
+    dll.slu_set_blocking_waits.argtypes = [c_int]
+    dll.slu_set_blocking_waits.restype = None
     return dll
 
 

@@ -30,6 +30,8 @@ int slu_version(void) { return 1; }
 
 long long slu_launch_count(void) { return slu::launch_total().load(); }
 
+void slu_set_blocking_waits(int on) { slu::set_blocking_waits(on != 0); }
+
 int slu_last_error(char* buf, size_t len) {
   if (!buf || len == 0) return SLU_ERR_ARG;
   std::strncpy(buf, g_err.c_str(), len - 1);
@@ -59,7 +61,7 @@ int slu_destroy(slu_handle_t h) {
 int slu_set_stream(slu_handle_t h, void* stream) {
   return guard(h, [&] {
     SLU_REQUIRE(h, "null handle");
-    SLU_CHECK_CUDA(cudaStreamSynchronize(h->h.stream));
+    slu::stream_wait(h->h.stream);
     h->h.stream = reinterpret_cast<cudaStream_t>(stream);
   });
 }
@@ -67,7 +69,7 @@ int slu_set_stream(slu_handle_t h, void* stream) {
 int slu_sync(slu_handle_t h) {
   int st = guard(h, [&] {
     SLU_REQUIRE(h, "null handle");
-    SLU_CHECK_CUDA(cudaStreamSynchronize(h->h.stream));
+    slu::stream_wait(h->h.stream);
   });
   if (st != SLU_OK) return st;
   int info[64];
@@ -125,7 +127,7 @@ int slu_hbs_create(slu_handle_t h, int N, int L, int fac, const int64_t* perm_ho
     p->H.iperm.alloc(sizeof(int64_t) * N, h->h.stream);
     SLU_CHECK_CUDA(cudaMemcpyAsync(p->H.iperm.p, iperm.data(), sizeof(int64_t) * N,
                                    cudaMemcpyHostToDevice, h->h.stream));
-    SLU_CHECK_CUDA(cudaStreamSynchronize(h->h.stream));
+    slu::stream_wait(h->h.stream);
     p->H.lv.resize(L);
     *out = p.release();
   });
@@ -522,7 +524,7 @@ int slu_ulv_solve_timed(slu_handle_t h, slu_hbs_t op, double* B, int ldb, int nr
     lt.reserve(2 * (size_t)H.L);
     slu::enqueue_device_lead(st, 500);
     slu::ulv_solve_fused<double>(st, H, B, ldb, nrhs, scratch, stride, &lt);
-    SLU_CHECK_CUDA(cudaStreamSynchronize(st));
+    slu::stream_wait(st);
     const int n = (int)lt.level.size();
     *nlaunch = n;
     for (int k = 0; k < n && k < cap; ++k) {

@@ -487,7 +487,7 @@ void grouped_solve_plan_create(Handle& h, int count, Hbs* const* ops, double* co
   auto kern = group_step_kernel<double>;
   for (const sweep::LaunchPlan& p : steps.plan)
     if (p.ctas > 0) ensure_smem(reinterpret_cast<const void*>(kern), p.smem);
-  SLU_CHECK_CUDA(cudaStreamSynchronize(st));   // table and buffers in place before the capture
+  stream_wait(st);   // table and buffers in place before the capture
   cudaStream_t cs = nullptr;
   SLU_CHECK_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
   cudaGraph_t g = nullptr;
@@ -624,7 +624,7 @@ void grouped_program_create(Handle& h, int nphase, const int* kind, const int* c
   for (int p = 0; p < nphase; ++p)
     for (const sweep::LaunchPlan& lp : tabs[p].plan)
       if (lp.ctas > 0) ensure_smem(reinterpret_cast<const void*>(kern), lp.smem);
-  SLU_CHECK_CUDA(cudaStreamSynchronize(st));   // tables in place before the capture
+  stream_wait(st);   // tables in place before the capture
   cudaStream_t cs = nullptr;
   SLU_CHECK_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
   cudaGraph_t g = nullptr;
@@ -945,7 +945,7 @@ double refine_loop(cudaStream_t st, const GroupRefine<T>& g, double tol, int max
       ++it;
       continue;
     }
-    SLU_CHECK_CUDA(cudaStreamSynchronize(st));
+    stream_wait(st);
     worst = g.check(member);
     if (worst <= tol || it >= maxit) break;
     next();
@@ -1040,7 +1040,7 @@ struct GroupRefinePlanT : GroupRefinePlan {
     SLU_CHECK_CUDA(cudaMallocHost(&pinned, 16 * (size_t)g.C));
     g.host = pinned;
     g.prepare_launches();
-    SLU_CHECK_CUDA(cudaStreamSynchronize(st));   // region and tables in place
+    stream_wait(st);   // region and tables in place
     cudaStream_t cs = nullptr;
     SLU_CHECK_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
     try {

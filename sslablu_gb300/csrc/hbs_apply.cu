@@ -126,7 +126,7 @@ void hbs_make_apply(Handle& h, Hbs& H, bool trans) {
   compose_down_kernel<<<grid_for((long long)r.n * r.n), 256, 0, st>>>(
       1, r.n, 0, trans, r.D.as<double>(), nullptr, dn.as<double>());
   check_launch("compose_down_kernel");
-  SLU_CHECK_CUDA(cudaStreamSynchronize(st));
+  stream_wait(st);
   H.has_apply[trans ? 1 : 0] = true;
 }
 

@@ -37,6 +37,42 @@ void ensure_smem(const void* kernel, size_t bytes) {
                                   cudaGetErrorString(err));
 }
 
+namespace {
+struct WaitState {
+  bool blocking = false;
+  int dev = -1;
+  cudaEvent_t ev = nullptr;
+  ~WaitState() {
+    if (ev) cudaEventDestroy(ev);
+  }
+};
+WaitState& wait_state() {
+  static thread_local WaitState w;
+  return w;
+}
+}  // namespace
+
+void set_blocking_waits(bool on) { wait_state().blocking = on; }
+
+void stream_wait(cudaStream_t st) {
+  WaitState& w = wait_state();
+  if (!w.blocking) {
+    SLU_CHECK_CUDA(cudaStreamSynchronize(st));
+    return;
+  }
+  int dev = 0;
+  SLU_CHECK_CUDA(cudaGetDevice(&dev));
+  if (!w.ev || w.dev != dev) {
+    if (w.ev) cudaEventDestroy(w.ev);
+    w.ev = nullptr;
+    SLU_CHECK_CUDA(
+        cudaEventCreateWithFlags(&w.ev, cudaEventBlockingSync | cudaEventDisableTiming));
+    w.dev = dev;
+  }
+  SLU_CHECK_CUDA(cudaEventRecord(w.ev, st));
+  SLU_CHECK_CUDA(cudaEventSynchronize(w.ev));
+}
+
 int num_sms() {
   static int n = 0;
   if (!n) {

@@ -919,7 +919,7 @@ void hbs_make_oz(Handle& h, Hbs& H) {
   Level& r = H.lv[L - 1];
   oz::make_op(st, r.ozSw, r.Sw.as<double>(), 1, L == 1 ? r.n : 2 * r.n, r.n);
   oz::make_op(st, r.ozDn, r.Adn.as<double>(), 1, r.n, r.n);
-  SLU_CHECK_CUDA(cudaStreamSynchronize(st));
+  stream_wait(st);
   H.has_oz = true;
 }
 
@@ -940,7 +940,7 @@ void hbs_make_ozT(Handle& h, Hbs& H) {
   Level& r = H.lv[L - 1];
   oz::make_op(st, r.ozSwT, r.SwT.as<double>(), 1, r.n, L == 1 ? r.n : 2 * r.n);
   oz::make_op(st, r.ozDnT, r.AdnT.as<double>(), 1, r.n, r.n);
-  SLU_CHECK_CUDA(cudaStreamSynchronize(st));
+  stream_wait(st);
   H.has_ozT = true;
 }
 

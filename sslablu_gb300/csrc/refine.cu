@@ -155,11 +155,11 @@ RefinePlan& plan_for(Handle& h, Hbs& H, int c) {
   }
   SLU_CHECK_CUDA(cudaMallocHost(&P->host_norms, 16 * (size_t)c + 16));
   P->host_norms[2 * c] = 0.0;
-  SLU_CHECK_CUDA(cudaStreamSynchronize(st));
+  stream_wait(st);
   // an uncaptured run first: sets kernel attributes and validates the sequence
   SLU_CHECK_CUDA(cudaMemsetAsync(P->B.p, 0, 8 * n, st));
   enqueue_iteration(st, H, *P, true);
-  SLU_CHECK_CUDA(cudaStreamSynchronize(st));
+  stream_wait(st);
   // capture on a private stream (the caller's may be the legacy default
   // stream, which cannot be captured); the graphs launch on the caller's
   cudaStream_t cs = nullptr;
@@ -211,7 +211,7 @@ void hbs_refine(Handle& h, Hbs& H, const double* B, int ldb, double* X, int ldx,
       ++it;
       continue;
     }
-    SLU_CHECK_CUDA(cudaStreamSynchronize(st));
+    stream_wait(st);
     if (P.inner == 2) {
       unsigned long long ew = 0;
       std::memcpy(&ew, P.host_norms + 2 * c, 8);

@@ -216,4 +216,12 @@ int num_sms();
 // smem_limit.h).  Safe to call while a stream captures.
 void ensure_smem(const void* kernel, size_t bytes);
 
+// Host wait for a stream.  By default a spin (cudaStreamSynchronize: the
+// lowest latency for a single caller); on a thread that asked for blocking
+// waits (set_blocking_waits) the thread sleeps on a blocking-sync event
+// instead, so many worker threads waiting at once leave the host cores to
+// the threads that are launching work.
+void stream_wait(cudaStream_t st);
+void set_blocking_waits(bool on);
+
 }  // namespace slu

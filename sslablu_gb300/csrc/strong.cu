@@ -525,7 +525,7 @@ void strong_compress(Handle& h, Op& S, int rk, int s, const double* Om, const do
     {
       int hb = 0;
       SLU_CHECK_CUDA(cudaMemcpyAsync(&hb, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
-      SLU_CHECK_CUDA(cudaStreamSynchronize(st));
+      stream_wait(st);
       SLU_REQUIRE(hb == 0, "strong HBS: " + std::to_string(hb) +
                                " near-field stack(s) of level " + std::to_string(t) +
                                " numerically rank deficient (min |R_ii| <= 1e-12 max |R_ii|); "
@@ -564,7 +564,7 @@ void strong_compress(Handle& h, Op& S, int rk, int s, const double* Om, const do
   }
   int hinfo[16];
   SLU_CHECK_CUDA(cudaMemcpyAsync(hinfo, info, sizeof(hinfo), cudaMemcpyDeviceToHost, st));
-  SLU_CHECK_CUDA(cudaStreamSynchronize(st));
+  stream_wait(st);
   SLU_REQUIRE(hinfo[0] == 0, "strong HBS: a Jacobi SVD of a projected sketch did not converge");
   SLU_REQUIRE(hinfo[8] == 0, "strong HBS: " + std::to_string(hinfo[8]) +
                                  " near-field stack(s) numerically rank deficient "
@@ -647,7 +647,7 @@ extern "C" int slu_strong_create(slu_handle_t h, long long N, int nleaves, int f
       perm[i] = v;
     }
     strong::upload(h->h.stream, p->S.perm, perm);
-    SLU_CHECK_CUDA(cudaStreamSynchronize(h->h.stream));
+    slu::stream_wait(h->h.stream);
     *out = p.release();
   });
 }
@@ -740,6 +740,6 @@ extern "C" int slu_strong_export(slu_handle_t h, slu_strong_t op, int what, int 
         default: SLU_REQUIRE(false, "unknown strong HBS export");
       }
     }
-    SLU_CHECK_CUDA(cudaStreamSynchronize(st));
+    stream_wait(st);
   });
 }

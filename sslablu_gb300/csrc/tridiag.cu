@@ -424,7 +424,7 @@ void rb_refine(Handle& h, const RbSolver& S, const double* B, int ldb, double* X
     colnorm2_rb<<<c, 256, 0, st>>>(N, c, r, c, rn);
     check_launch("colnorm2_rb");
     SLU_CHECK_CUDA(cudaMemcpyAsync(hr.data(), rn, 8 * c, cudaMemcpyDeviceToHost, st));
-    SLU_CHECK_CUDA(cudaStreamSynchronize(st));
+    stream_wait(st);
     worst = 0.0;
     for (int j = 0; j < c; ++j)
       worst = std::max(worst, std::sqrt(hr[j]) / (hb[j] > 0 ? std::sqrt(hb[j]) : 1.0));

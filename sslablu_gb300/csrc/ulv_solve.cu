@@ -176,7 +176,7 @@ void solve_plan_create(Handle& h, const Hbs& H, const double* X, int ldx, double
   }
   for (size_t i = 0; i < steps.size(); ++i)
     sweep::prepare_step(steps[i].s, kn ? (*kn)[i] : PlanKnobs());
-  SLU_CHECK_CUDA(cudaStreamSynchronize(st));   // the scratch exists before the capture
+  stream_wait(st);   // the scratch exists before the capture
   // capture on a private stream (the caller's may be the legacy default
   // stream, which cannot be captured); the graph launches on the caller's
   cudaStream_t cs = nullptr;
@@ -222,7 +222,7 @@ void solve_plan_launch(Handle& h, SolvePlan& P, bool wait) {
   if (!P.exec) return;   // a grouped plan without members
   SLU_CHECK_CUDA(cudaGraphLaunch(P.exec, h.stream));
   count_launches(P.kernels);
-  if (wait) SLU_CHECK_CUDA(cudaStreamSynchronize(h.stream));
+  if (wait) stream_wait(h.stream);
 }
 
 namespace {
@@ -301,7 +301,7 @@ void autotune(Handle& h, Hbs& H, int c, int reps) {
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  SLU_CHECK_CUDA(cudaStreamSynchronize(st));
+  stream_wait(st);
   H.tuned[{type_code<T>(), c}] = cur;
 }
 

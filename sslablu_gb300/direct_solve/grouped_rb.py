@@ -29,7 +29,7 @@ import torch
 
 from .. import _dev as dv
 from ..grouped import apply_grouped, solve_grouped_device
-from .omsdirectsolveHBS import _worker_stream, id_op
+from .omsdirectsolveHBS import _blocking_worker, _wait, _worker_stream, id_op
 
 
 _BUILD_POOLS = {}
@@ -42,7 +42,8 @@ def _build_pool(workers):
     many batches are factored."""
     with _BUILD_LOCK:
         if workers not in _BUILD_POOLS:
-            _BUILD_POOLS[workers] = cf.ThreadPoolExecutor(max_workers=workers)
+            _BUILD_POOLS[workers] = cf.ThreadPoolExecutor(max_workers=workers,
+                                                          initializer=_blocking_worker)
         return _BUILD_POOLS[workers]
 
 
@@ -64,7 +65,7 @@ def factorize_many(jobs, workers=6):
         st = _worker_stream(dev)
         with torch.cuda.stream(st):
             out = job()
-        st.synchronize()
+        _wait(st)
         return out
 
     return list(_build_pool(workers).map(run, jobs))

@@ -19,12 +19,14 @@ red-black level, which are independent, run concurrently on worker streams
 (sketches still drawn in upstream's order on the calling thread).
 """
 import concurrent.futures as cf
+import os
 import threading
 
 import numpy as np
 import torch
 
 from .. import _dev as dv
+from .. import _lib as L
 from ..matAssembly.HBS import HBSnew
 from .omsdirectsolve import DirectSolver
 
@@ -212,11 +214,27 @@ def _shape0(op):
     return int(op.shape[0])
 
 
-# concurrent compressions per red-black level (worker threads, one stream each)
-_LEVEL_WORKERS = 12
+# concurrent compressions (worker threads, one stream each), shared by every
+# factorisation of the process; SSLABLU_LEVEL_WORKERS sets the count
+_LEVEL_WORKERS = max(1, int(os.environ.get("SSLABLU_LEVEL_WORKERS", "12")))
 _POOL = None
 _POOL_LOCK = threading.Lock()
 _TLS = threading.local()
+
+
+def _blocking_worker():
+    """Initializer of factorisation worker threads: their host waits (the
+    library's and _wait's) sleep instead of spinning, so a dozen or more
+    waiting workers leave the host cores to the ones launching work."""
+    L.lib().slu_set_blocking_waits(1)
+
+
+def _wait(stream):
+    """Wait for the work queued on ``stream`` so far, asleep (blocking-sync
+    event) rather than spinning."""
+    ev = torch.cuda.Event(blocking=True)
+    ev.record(stream)
+    ev.synchronize()
 
 
 def _level_pool():
@@ -226,7 +244,8 @@ def _level_pool():
     global _POOL
     with _POOL_LOCK:
         if _POOL is None:
-            _POOL = cf.ThreadPoolExecutor(max_workers=_LEVEL_WORKERS)
+            _POOL = cf.ThreadPoolExecutor(max_workers=_LEVEL_WORKERS,
+                                          initializer=_blocking_worker)
         return _POOL
 
 
@@ -398,7 +417,7 @@ class RedBlackSolverHBS(DirectSolver):
             h.construct_drawn(rk, Om, Psi)
             return [h]
         dev = torch.cuda.current_device()
-        torch.cuda.current_stream(dev).synchronize()   # inputs ready for every stream
+        _wait(torch.cuda.current_stream(dev))   # inputs ready for every stream
 
         def run(job):
             h, Om, Psi = job
@@ -406,7 +425,7 @@ class RedBlackSolverHBS(DirectSolver):
             st = _worker_stream(dev)
             with torch.cuda.stream(st):
                 h.construct_drawn(rk, Om, Psi)
-            st.synchronize()
+            _wait(st)
             return h
 
         return list(_level_pool().map(run, jobs))

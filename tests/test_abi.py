@@ -41,7 +41,7 @@ def test_library_exports_every_declared_symbol(cdll):
 
 def test_python_binding_covers_header(cdll):
     from sslablu_gb300 import _lib
-    bound = set(_lib.SIGNATURES) | {"slu_launch_count"}
+    bound = set(_lib.SIGNATURES) | {"slu_launch_count", "slu_set_blocking_waits"}
     assert set(declared_symbols()) <= bound
 
 
