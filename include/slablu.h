@@ -71,6 +71,9 @@ int slu_sync(slu_handle_t h);
  * perm_host = tree.perm_leaf (N host int64 entries, NULL = identity). */
 int slu_hbs_create(slu_handle_t h, int N, int L, int fac, const int64_t* perm_host,
                    slu_hbs_t* out);
+/* Frees the object's device memory stream-ordered (cudaFreeAsync on the
+ * stream each buffer was allocated on): work that reads the object on any
+ * other stream must have completed first (synchronise those streams). */
 int slu_hbs_destroy(slu_hbs_t op);
 
 /* Replaces HBSMAT.constructHBS_ULV (matAssembly/HBS/HBSnew.py:211-295) after
@@ -390,6 +393,9 @@ int slu_rb_factor_mixed(slu_handle_t h, int nblk, int m, const double* SiM, cons
  * solves (then SLU_ERR_NOT_CONVERGED). */
 int slu_rb_refine(slu_handle_t h, slu_rb_t rb, const double* B, int ldb, double* X, int ldx,
                   int nrhs, double tol, int maxit, int* iters_out, double* relres_out);
+/* Frees the object's device memory stream-ordered (cudaFreeAsync on the
+ * stream each buffer was allocated on): work that reads the object on any
+ * other stream must have completed first (synchronise those streams). */
 int slu_rb_destroy(slu_rb_t rb);
 
 /* Slab source-target maps of the stencil discretisation, applied through
@@ -429,6 +435,9 @@ int slu_thomas_solve(slu_handle_t h, slu_rb_t th, double* B, int ldb, int nrhs);
  * identity).  Replaces HBSMAT.__init__ (925-975). */
 int slu_strong_create(slu_handle_t h, long long N, int nleaves, int fac,
                       const int64_t* perm_host, slu_strong_t* out);
+/* Frees the object's device memory stream-ordered (cudaFreeAsync on the
+ * stream each buffer was allocated on): work that reads the object on any
+ * other stream must have completed first (synchronise those streams). */
 int slu_strong_destroy(slu_strong_t op);
 /* Compression from sketches (HBSMAT.construct / constructHBS, 1000-1107):
  * Om, Psi, Y = A Om', Z = A^T Psi' (device, N x s row-major, rows already
