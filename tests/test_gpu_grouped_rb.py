@@ -1,10 +1,12 @@
 """Grouped red-black HBS solves (direct_solve/grouped_rb.py) of uneven 2-D
 Poisson interface systems against each system's own RedBlackSolverHBS.solve
 (itself pinned to upstream in test_gpu_hbs_solvers.py) and against the
-exact float64 systems built from the stencil slab maps."""
+exact float64 systems built from the stencil slab maps, and one such system
+against the oracle's red-black HBS on the same draws."""
 import numpy as np
 import pytest
 
+from tests._cases import relerr
 from tests._gpu import need_gpu
 
 pytestmark = pytest.mark.gpu
@@ -119,3 +121,48 @@ def test_concurrent_builds_equal_one_by_one_builds():
         B = torch.from_numpy(b).cuda()
         xp, xs = rb_p.solve(B), rb_s.solve(B)
         assert float(torch.linalg.norm(xp - xs) / torch.linalg.norm(xs)) <= 1e-13, (nI, m, rk)
+
+
+def test_c4_system_matches_the_oracle():
+    """One system of the C4 batch's kind (5 interfaces of 128 points padded
+    to 8 blocks, stencil slab map compressed by the rkHBS assembler at rank
+    16), red-black HBS factored with upstream's sketch draws (numpy's global
+    RNG), against the oracle's red-black HBS (upstream's restated) on the
+    same coupling operator and the same draws: the solutions agree to 1e-9
+    and both solve the exact system to 1e-9."""
+    need_gpu()
+    import types
+    import torch
+    from oracle import direct as od
+    from sslablu_gb300.direct_solve.omsdirectsolveHBS import RedBlackSolverHBS, _linop_from_mat
+    from sslablu_gb300.matAssembly.matAssembler import rkHMatAssembler
+    from sslablu_gb300.rbbatch import exact_apply
+    from sslablu_gb300.synthetic import poisson_slab_map
+    nI, m, rk, P = 5, 128, 16, 8
+    width = 2.0 / (nI + 1)
+    nx = int(round(width * (m + 1))) // 2 * 2 + 1
+    S = poisson_slab_map(m, max(nx, 3), width)
+    np.random.seed(31)
+    H = rkHMatAssembler(64, rk).assemble(
+        types.SimpleNamespace(A=S, XXI=np.linspace(0.0, 1.0, m + 2)[1:-1]))
+    Hd = np.asarray(H.matmat(np.eye(m)))
+    Z = _linop_from_mat(np.zeros((m, m)))
+    Z._zero = True
+    rb = RedBlackSolverHBS(m, rk, H.tree, False)
+    np.random.seed(32)
+    rb.factorize([[H if 0 < i < nI else Z, H if i < nI - 1 else Z] for i in range(P)])
+    Zd = np.zeros((m, m))
+    tree = H.tree
+    ov = od.RedBlackHBS(m, rk, (np.asarray(tree.perm_leaf), tree.nleaves, tree.nlevels), False)
+    np.random.seed(32)
+    ov.factorize([(od.dense_op(Hd if 0 < i < nI else Zd), od.dense_op(Hd if i < nI - 1 else Zd))
+                  for i in range(P)])
+    b = np.zeros((P * m, 3))
+    b[:nI * m] = np.random.default_rng(4).standard_normal((nI * m, 3))
+    x = np.asarray(rb.solve(b))
+    xo = np.stack([np.asarray(ov.solve(b[:, j])) for j in range(3)], axis=1)
+    assert relerr(x, xo) <= 1e-9
+    Sd = torch.from_numpy(S).cuda()
+    for sol in (x, xo):
+        R = b - exact_apply(Sd, nI, P, torch.from_numpy(sol).cuda()).cpu().numpy()
+        assert float((np.linalg.norm(R, axis=0) / np.linalg.norm(b, axis=0)).max()) <= 1e-9
