@@ -155,11 +155,13 @@ def run(systems=512, nrhs=8, reps=10, seed=20261205, workers=6):
     for name, fn in arms.items():
         fn()                                   # first use composes apply operators
         torch.cuda.synchronize()
-        c0 = L.lib().slu_launch_count()
-        xs = fn()
-        torch.cuda.synchronize()
-        launches = L.lib().slu_launch_count() - c0
-        t = _time(fn, reps)
+        # an NVTX range per arm (a profiler can keep one arm's launches)
+        with torch.cuda.nvtx.range(name):
+            c0 = L.lib().slu_launch_count()
+            xs = fn()
+            torch.cuda.synchronize()
+            launches = L.lib().slu_launch_count() - c0
+            t = _time(fn, reps)
         out[name] = {"rhs_per_s": total / t, "ms_per_step": 1e3 * t, "gpu_launches": launches}
         res[name] = xs
     worst, diff = 0.0, 0.0
